@@ -1,0 +1,405 @@
+// C ABI of aerojax_gb300 (declared in include/aerojax_gb300.h).
+//
+// aj_step and aj_poisson_mg record their kernels into a CUDA graph: when the
+// caller's stream is already capturing, straight into the caller's graph;
+// otherwise into a graph owned by the library, instantiated once per distinct
+// (parameters, workspace, buffers) and launched on the caller's stream.  The
+// converging multigrid's refinement loop is a while node inside that graph,
+// so a step never waits on the host.
+#include "aj_internal.cuh"
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <string.h>
+
+namespace aj {
+
+int parity_levels(int nx, int ny, int levels, int* max_levels) {
+  // multigrid_solver.py:96-106, plus the shapes its recursion needs
+  int ml = 1, tx = nx, ty = ny;
+  while (tx % 2 == 0 && ty % 2 == 0 && ml < levels) {
+    tx /= 2;
+    ty /= 2;
+    ml++;
+  }
+  if (ml < 2) return AJ_ERR_SHAPE;
+  int n = nx, m = ny;
+  for (int k = 0; k < ml; ++k) {
+    if (n % 2 || m % 2 || n / 2 < 2 || m / 2 < 2) return AJ_ERR_SHAPE;
+    n /= 2;
+    m /= 2;
+  }
+  if (ml > AJ_MAX_LEVELS) return AJ_ERR_SHAPE;
+  *max_levels = ml;
+  return AJ_OK;
+}
+
+int converge_depth(int nx, int ny) {
+  // halve while even, at least 4 x 4 cells remain... and the coarse grid is
+  // still above AJ_MAX_COARSE / 2 cells; always coarsen at least once
+  int k = 0, n = nx, m = ny;
+  while (n % 2 == 0 && m % 2 == 0 && n / 2 >= 2 && m / 2 >= 2 &&
+         ((long)n * m > AJ_MAX_COARSE / 2 || k == 0) && k < AJ_MAX_LEVELS) {
+    n /= 2;
+    m /= 2;
+    ++k;
+  }
+  return k;
+}
+
+int check_params(const AjStepParams& p) {
+  if (p.nx < 4 || p.ny < 4) return AJ_ERR_SHAPE;
+  if (p.dx <= 0 || p.dy <= 0) return AJ_ERR_PARAM;
+  if (p.grid_type != AJ_GRID_COLLOCATED && p.grid_type != AJ_GRID_MAC) return AJ_ERR_PARAM;
+  if (p.flow_type < AJ_FLOW_VON_KARMAN || p.flow_type > AJ_FLOW_TAYLOR_GREEN) return AJ_ERR_PARAM;
+  if (p.les_model < AJ_LES_NONE || p.les_model > AJ_LES_DYNAMIC) return AJ_ERR_PARAM;
+  if (p.mg_mode != AJ_MG_PARITY && p.mg_mode != AJ_MG_CONVERGE) return AJ_ERR_PARAM;
+  if (p.mg_mode == AJ_MG_PARITY) {
+    int ml;
+    int rc = parity_levels(p.nx, p.ny, p.levels > 0 ? p.levels : 4, &ml);
+    if (rc != AJ_OK) return rc;
+    if (p.v_cycles < 1) return AJ_ERR_PARAM;
+  } else {
+    int D = converge_depth(p.nx, p.ny);
+    if (D < 1) return AJ_ERR_SHAPE;
+    long nc = (long)(p.nx >> D) * (p.ny >> D);
+    if (nc > AJ_MAX_COARSE * 2) return AJ_ERR_SHAPE;
+    if (p.mg_rtol <= 0 || p.max_cycles < 1) return AJ_ERR_PARAM;
+  }
+  if (p.cfl_dt && (p.cfl_target <= 0 || p.dt_max <= 0)) return AJ_ERR_PARAM;
+  if (!p.cfl_dt && p.dt <= 0) return AJ_ERR_PARAM;
+  return AJ_OK;
+}
+
+bool make_layout(const AjStepParams& p, Layout& L) {
+  if (check_params(p) != AJ_OK) return false;
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    size_t o = off;
+    off += (bytes + 255) & ~(size_t)255;
+    return o;
+  };
+  const long nx = p.nx, ny = p.ny, N = nx * ny;
+  const bool mac = p.grid_type == AJ_GRID_MAC;
+  const long nU = mac ? (nx + 1) * ny : N, nV = mac ? nx * (ny + 1) : N;
+  L = Layout();
+  L.scalars = take(sizeof(DevScalars) < 256 ? 256 : sizeof(DevScalars));
+  if (!mac) L.chi = take(N * 4);
+  L.sA_u = take(nU * 4);
+  L.sA_v = take(nV * 4);
+  L.sB_u = take(nU * 4);
+  L.sB_v = take(nV * 4);
+  L.sS_u = take(nU * 4);
+  L.sS_v = take(nV * 4);
+  L.k1_u = take(nU * 4);
+  L.k1_v = take(nV * 4);
+  L.nu_sgs = take(N * 4);
+  L.dyn = take(16 * N * 4);
+  L.b0 = take(N * 4);
+  L.T0 = take(N * 4);
+  if (p.mg_mode == AJ_MG_PARITY) {
+    int ml;
+    parity_levels(p.nx, p.ny, p.levels > 0 ? p.levels : 4, &ml);
+    L.nlev = ml;
+    for (int l = 0; l <= ml; ++l) {
+      L.ln[l] = p.nx >> l;
+      L.lm[l] = p.ny >> l;
+      if (l == 0) continue;
+      long n = (long)L.ln[l] * L.lm[l];
+      L.X[l] = take(n * 4);
+      L.T[l] = take(n * 4);
+      L.B[l] = take(n * 4);
+      if (mac) L.M[l] = take(n * 4);
+    }
+  } else {
+    int D = converge_depth(p.nx, p.ny);
+    L.nlev = D;
+    for (int l = 0; l <= D; ++l) {
+      L.ln[l] = p.nx >> l;
+      L.lm[l] = p.ny >> l;
+      long n = (long)L.ln[l] * L.lm[l];
+      L.X[l] = take(n * 4);
+      L.T[l] = take(n * 4);
+      L.B[l] = take(n * 4);
+    }
+    L.ncoarse = L.ln[D] * L.lm[D];
+    L.p64 = take(N * 8);
+    L.cinv = take((size_t)L.ncoarse * L.ncoarse * 8);
+  }
+  L.part = take(kPartials * 8);
+  L.total = off;
+  return true;
+}
+
+// effective parameters: step_pure hard-wires slip walls and no hyperviscosity
+// (step.py:177-180) and cannot run on the MAC grid (step.py:348 broadcasts
+// (nx+1, ny) against (nx, ny))
+static AjStepParams normalise(const AjStepParams& in) {
+  AjStepParams p = in;
+  if (p.levels <= 0) p.levels = 4;
+  if (p.variant == AJ_VARIANT_PURE) {
+    p.nu_hyper_ratio = 0.0;
+    p.slip_walls = 1;
+  }
+  if (p.mg_tolerance <= 0) p.mg_tolerance = AJ_PARITY_TOL_DEFAULT;
+  return p;
+}
+
+// ------------------------------------------------------------- graph cache
+namespace {
+std::mutex g_mu;
+std::unordered_map<std::string, cudaGraphExec_t> g_cache;
+cudaStream_t g_capture = nullptr;
+
+std::string make_key(int kind, const AjStepParams& p, std::initializer_list<const void*> ptrs) {
+  std::string k;
+  k.append(reinterpret_cast<const char*>(&kind), sizeof(kind));
+  k.append(reinterpret_cast<const char*>(&p), sizeof(p));
+  for (const void* q : ptrs) k.append(reinterpret_cast<const char*>(&q), sizeof(q));
+  return k;
+}
+
+template <typename F>
+int run_captured(const std::string& key, cudaStream_t user, F&& enqueue) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(user, &cs) != cudaSuccess) return AJ_ERR_CUDA;
+  if (cs == cudaStreamCaptureStatusActive) return enqueue(user);   // caller's own graph
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = g_cache.find(key);
+  if (it == g_cache.end()) {
+    if (!g_capture && cudaStreamCreateWithFlags(&g_capture, cudaStreamNonBlocking) != cudaSuccess)
+      return AJ_ERR_CUDA;
+    if (cudaStreamBeginCapture(g_capture, cudaStreamCaptureModeRelaxed) != cudaSuccess)
+      return AJ_ERR_CUDA;
+    int rc = enqueue(g_capture);
+    cudaGraph_t g = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(g_capture, &g);
+    if (rc != AJ_OK || ce != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();
+      return rc != AJ_OK ? rc : AJ_ERR_CUDA;
+    }
+    cudaGraphExec_t ex;
+    if (cudaGraphInstantiate(&ex, g, 0) != cudaSuccess) {
+      cudaGraphDestroy(g);
+      return AJ_ERR_CUDA;
+    }
+    cudaGraphDestroy(g);
+    it = g_cache.emplace(key, ex).first;
+  }
+  return cudaGraphLaunch(it->second, user) == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+}
+}  // namespace
+
+static int ws_ok(const Layout& L, void* ws, size_t bytes) {
+  if (!ws || bytes < L.total) return AJ_ERR_WORKSPACE;
+  if (reinterpret_cast<uintptr_t>(ws) % 256) return AJ_ERR_WORKSPACE;
+  return AJ_OK;
+}
+
+static int enqueue_step(const AjStepParams& p, const Layout& L, void* ws, const float* u,
+                        const float* v, const float* mask, const float* p_guess, float* uo,
+                        float* vo, float* po, AjStats* stats, cudaStream_t st) {
+  int rc = p.cfl_dt ? launch_cfl(p, ws, u, v, nullptr, st) : launch_set_dt(p, ws, st);
+  if (rc != AJ_OK) return rc;
+  const bool mac = p.grid_type == AJ_GRID_MAC;
+  const float* nsg = nullptr;
+  int dc = 0;
+  // step_pure computes the LES field on the collocated path but never passes it
+  // on (step.py:177-180): nothing to do.  The GUI step and MAC use it.
+  if (p.les_model != AJ_LES_NONE && (p.variant == AJ_VARIANT_GUI || mac)) {
+    float* f = at<float>(ws, L.nu_sgs);
+    rc = launch_les(p, L, ws, p.les_model, u, v, mac, f, nullptr, st);
+    if (rc != AJ_OK) return rc;
+    nsg = f;
+    dc = (p.variant == AJ_VARIANT_GUI && !mac) ? 1 : 0;
+  }
+  float* us = at<float>(ws, L.sS_u);
+  float* vs = at<float>(ws, L.sS_v);
+  rc = launch_predictor(p, L, ws, u, v, mask, nsg, dc, us, vs, st);
+  if (rc != AJ_OK) return rc;
+  rc = launch_rhs(p, L, ws, us, vs, mask, at<float>(ws, L.b0), st);
+  if (rc != AJ_OK) return rc;
+  rc = launch_pressure(p, L, ws, mask, p_guess, po, stats, st);
+  if (rc != AJ_OK) return rc;
+  return launch_correct(p, L, ws, us, vs, po, mask, uo, vo, st);
+}
+
+}  // namespace aj
+
+using namespace aj;
+
+extern "C" {
+
+int32_t aj_version(void) { return 100; }
+
+int32_t aj_check_params(const AjStepParams* prm) {
+  if (!prm) return AJ_ERR_PARAM;
+  AjStepParams p = normalise(*prm);
+  int rc = check_params(p);
+  if (rc != AJ_OK) return rc;
+  if (p.variant == AJ_VARIANT_PURE && p.grid_type == AJ_GRID_MAC) return AJ_ERR_PARAM;
+  if (p.flow_type != AJ_FLOW_VON_KARMAN) return AJ_ERR_PARAM;   // step + solver: von Karman
+  if (p.mg_mode == AJ_MG_CONVERGE && p.grid_type == AJ_GRID_MAC && p.flow_type != AJ_FLOW_VON_KARMAN)
+    return AJ_ERR_PARAM;
+  return AJ_OK;
+}
+
+size_t aj_workspace_size(const AjStepParams* prm) {
+  if (!prm) return 0;
+  Layout L;
+  if (!make_layout(normalise(*prm), L)) return 0;
+  return L.total;
+}
+
+int32_t aj_prepare(const AjStepParams* prm, const float* mask, const float* sdf, void* ws,
+                   size_t bytes, void* stream) {
+  if (!prm || !mask) return AJ_ERR_PARAM;
+  AjStepParams p = normalise(*prm);
+  int rc = check_params(p);
+  if (rc != AJ_OK) return rc;
+  Layout L;
+  make_layout(p, L);
+  if ((rc = ws_ok(L, ws, bytes)) != AJ_OK) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (cudaMemsetAsync(ws, 0, L.total, st) != cudaSuccess) return AJ_ERR_CUDA;
+  if (p.has_sdf && !sdf) return AJ_ERR_PARAM;
+  if ((rc = launch_chi(p, L, ws, mask, sdf, st)) != AJ_OK) return rc;
+  if ((rc = prepare_pressure(p, L, ws, mask, st)) != AJ_OK) return rc;
+  return cudaStreamSynchronize(st) == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+}
+
+int32_t aj_step(const AjStepParams* prm, const float* u, const float* v, const float* mask,
+                const float* p_guess, float* u_out, float* v_out, float* p_out, void* ws,
+                size_t bytes, AjStats* stats, void* stream) {
+  if (!prm || !u || !v || !mask || !u_out || !v_out || !p_out) return AJ_ERR_PARAM;
+  int rc = aj_check_params(prm);
+  if (rc != AJ_OK) return rc;
+  AjStepParams p = normalise(*prm);
+  if (p.warm_start && !p_guess) return AJ_ERR_PARAM;
+  Layout L;
+  make_layout(p, L);
+  if ((rc = ws_ok(L, ws, bytes)) != AJ_OK) return rc;
+  const float* pg = p.warm_start ? p_guess : nullptr;
+  std::string key = make_key(1, p, {ws, u, v, mask, pg, u_out, v_out, p_out, stats});
+  return run_captured(key, (cudaStream_t)stream, [&](cudaStream_t s) {
+    return enqueue_step(p, L, ws, u, v, mask, pg, u_out, v_out, p_out, stats, s);
+  });
+}
+
+int32_t aj_poisson_mg(const AjStepParams* prm, const float* rhs, const float* mask,
+                      const float* p0, float* p_out, void* ws, size_t bytes, AjStats* stats,
+                      void* stream) {
+  if (!prm || !rhs || !mask || !p_out) return AJ_ERR_PARAM;
+  AjStepParams p = normalise(*prm);
+  int rc = check_params(p);
+  if (rc != AJ_OK) return rc;
+  if (p.flow_type != AJ_FLOW_VON_KARMAN) return AJ_ERR_PARAM;
+  Layout L;
+  make_layout(p, L);
+  if ((rc = ws_ok(L, ws, bytes)) != AJ_OK) return rc;
+  if (p.mg_mode == AJ_MG_CONVERGE) p.warm_start = p0 ? 1 : 0;
+  std::string key = make_key(2, p, {ws, rhs, mask, p0, p_out, stats});
+  return run_captured(key, (cudaStream_t)stream, [&](cudaStream_t s) {
+    int r = launch_mg_rhs(p, L, ws, rhs, mask, s);
+    if (r != AJ_OK) return r;
+    return launch_pressure(p, L, ws, mask, p0, p_out, stats, s);
+  });
+}
+
+int32_t aj_les(const AjStepParams* prm, int32_t model, const float* u, const float* v,
+               float* nu_sgs, float* cd_out, void* ws, size_t bytes, void* stream) {
+  if (!prm || !u || !v || !nu_sgs) return AJ_ERR_PARAM;
+  AjStepParams p = normalise(*prm);
+  if (p.nx < 3 || p.ny < 3) return AJ_ERR_SHAPE;
+  Layout L;
+  AjStepParams q = p;
+  q.grid_type = AJ_GRID_COLLOCATED;
+  q.mg_mode = AJ_MG_CONVERGE;   // layout only needs the field buffers
+  q.mg_rtol = 1e-6;
+  q.max_cycles = 1;
+  q.cfl_dt = 0;
+  q.dt = 1.0;
+  if (model == AJ_LES_DYNAMIC) {
+    if (!make_layout(q, L)) return AJ_ERR_SHAPE;
+    int rc = ws_ok(L, ws, bytes);
+    if (rc != AJ_OK) return rc;
+  }
+  return launch_les(p, L, ws, model, u, v, 0, nu_sgs, cd_out, (cudaStream_t)stream);
+}
+
+int32_t aj_predictor(const AjStepParams* prm, const float* u, const float* v, const float* mask,
+                     const float* nu_sgs, int32_t double_count, float* u_star, float* v_star,
+                     void* ws, size_t bytes, void* stream) {
+  if (!prm || !u || !v || !mask || !u_star || !v_star) return AJ_ERR_PARAM;
+  AjStepParams p = normalise(*prm);
+  int rc = check_params(p);
+  if (rc != AJ_OK) return rc;
+  Layout L;
+  make_layout(p, L);
+  if ((rc = ws_ok(L, ws, bytes)) != AJ_OK) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  rc = p.cfl_dt ? launch_cfl(p, ws, u, v, nullptr, st) : launch_set_dt(p, ws, st);
+  if (rc != AJ_OK) return rc;
+  return launch_predictor(p, L, ws, u, v, mask, nu_sgs, double_count, u_star, v_star, st);
+}
+
+int32_t aj_cfl_dt(const AjStepParams* prm, const float* u, const float* v, float* dt_out,
+                  void* ws, size_t bytes, void* stream) {
+  if (!prm || !u || !v || !dt_out || !ws || bytes < 256) return AJ_ERR_PARAM;
+  AjStepParams p = normalise(*prm);
+  if (p.cfl_target <= 0 || p.dt_max <= 0) return AJ_ERR_PARAM;
+  return launch_cfl(p, ws, u, v, dt_out, (cudaStream_t)stream);
+}
+
+int32_t aj_profile_kernel(const AjStepParams* prm, int32_t which, const float* u,
+                          const float* v, const float* mask, void* ws, size_t bytes,
+                          void* stream) {
+  if (!prm) return AJ_ERR_PARAM;
+  AjStepParams p = normalise(*prm);
+  int rc = check_params(p);
+  if (rc != AJ_OK) return rc;
+  Layout L;
+  make_layout(p, L);
+  if ((rc = ws_ok(L, ws, bytes)) != AJ_OK) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (which >= 0 && which <= 2) return profile_pressure_kernel(p, L, ws, which, st);
+  if (which == 3) {   // the predictor (all stages) from (u, v) into the workspace
+    if (!u || !v || !mask) return AJ_ERR_PARAM;
+    return launch_predictor(p, L, ws, u, v, mask, nullptr, 0, at<float>(ws, L.sS_u),
+                            at<float>(ws, L.sS_v), st);
+  }
+  return AJ_ERR_PARAM;
+}
+
+int32_t aj_kernel_count(const AjStepParams* prm, int32_t cycles) {
+  if (!prm) return -1;
+  AjStepParams p = normalise(*prm);
+  Layout L;
+  if (!make_layout(p, L)) return -1;
+  const bool mac = p.grid_type == AJ_GRID_MAC;
+  int n = 1;                                                    // cfl or set-dt
+  if (p.les_model != AJ_LES_NONE && (p.variant == AJ_VARIANT_GUI || mac))
+    n += (mac ? 1 : 0) + (p.les_model == AJ_LES_DYNAMIC ? 4 : 1);
+  n += p.fast_mode ? 2 : 3;                                     // predictor stages
+  n += 1;                                                       // rhs
+  if (p.mg_mode == AJ_MG_PARITY) {
+    int per_cycle = 5 * L.nlev + 10 + 2;                        // 5 per level, coarsest, norm
+    n += 1 + p.v_cycles * per_cycle;                            // begin + cycles
+  } else {
+    int body = 2 * L.nlev + 3;                                  // down, coarse, up, resid, check
+    n += 4 + (cycles > 1 ? cycles : 1) * body + 1;              // begin/init/resid/check, loop, out
+  }
+  n += 1;                                                       // stats
+  n += 1;                                                       // correction
+  return n;
+}
+
+int32_t aj_release_graphs(void) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  for (auto& kv : g_cache) cudaGraphExecDestroy(kv.second);
+  g_cache.clear();
+  return AJ_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,109 @@
+// Internal declarations shared by the aerojax_gb300 CUDA translation units.
+// Fields are row-major [i][j] with j (y) contiguous; threads map along j.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+#include "../../include/aerojax_gb300.h"
+
+#define AJ_MAX_LEVELS 12
+#define AJ_MAX_COARSE 512          // cells of the converging-mode coarsest grid
+#define AJ_PARITY_TOL_DEFAULT 1e-6
+
+namespace aj {
+
+// Device scalars living at the head of the workspace.
+struct DevScalars {
+  float dt;            // step dt (set on the device each step)
+  float dt_corr;       // dt used by the pressure correction
+  unsigned int cfl_max_bits;   // max |velocity| as float bits (atomicMax)
+  unsigned int cfl_count;      // blocks finished (last-block pattern)
+  int mg_skip;         // parity mode: V-cycles after convergence are skipped
+  int mg_cycles;       // V-cycles executed in this solve
+  int mg_done;         // converging mode: target met (later cycles skip)
+  int err;             // device-side AjStatus
+  double acc[4];       // reduction accumulators (residual, rhs, spare)
+  double rel;          // last relative residual
+  double bnorm;        // ||b||
+  double abs_sq;       // sum r^2 dx dy
+  unsigned int red_count;
+  unsigned int pad_[3];
+};
+
+struct Layout {
+  size_t scalars = 0;
+  size_t chi = 0, mask_u = 0, mask_v = 0;               // geometry-derived
+  size_t sA_u = 0, sA_v = 0, sB_u = 0, sB_v = 0;        // predictor stage buffers
+  size_t sS_u = 0, sS_v = 0;                            // predictor output (u*, v*)
+  size_t k1_u = 0, k1_v = 0;                            // RK2 first slope
+  size_t nu_sgs = 0;
+  size_t dyn = 0;                                       // dynamic LES temporaries
+  size_t b0 = 0, T0 = 0;                                // multigrid level-0 rhs, scratch
+  size_t X[AJ_MAX_LEVELS + 1] = {0}, T[AJ_MAX_LEVELS + 1] = {0};
+  size_t B[AJ_MAX_LEVELS + 1] = {0}, M[AJ_MAX_LEVELS + 1] = {0};
+  size_t p64 = 0;                                       // converging mode FP64 pressure
+  size_t cinv = 0;                                      // coarsest-grid inverse (FP64)
+  size_t part = 0;                                      // per-block partial sums (FP64)
+  size_t total = 0;
+  // multigrid hierarchy
+  int nlev = 0;                 // parity: max_levels (coarsest index); converge: depth
+  int ln[AJ_MAX_LEVELS + 1] = {0}, lm[AJ_MAX_LEVELS + 1] = {0};
+  int ncoarse = 0;              // converging: coarsest cell count
+};
+
+// Number of dynamic-LES temporaries (nx*ny floats each).
+constexpr int kDynFields = 12;
+constexpr int kPartials = 4096;
+
+bool make_layout(const AjStepParams& p, Layout& L);
+int check_params(const AjStepParams& p);
+int parity_levels(int nx, int ny, int levels, int* max_levels);
+int converge_depth(int nx, int ny);
+
+template <typename T>
+inline T* at(void* ws, size_t off) { return reinterpret_cast<T*>(static_cast<char*>(ws) + off); }
+
+// ------------------------------------------------------------------ helpers
+__device__ __forceinline__ int clampi(int i, int n) { return i < 0 ? 0 : (i >= n ? n - 1 : i); }
+__device__ __forceinline__ int wrapi(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+template <bool PER>
+__device__ __forceinline__ int pidx(int i, int n) { return PER ? wrapi(i, n) : clampi(i, n); }
+
+__device__ __forceinline__ float ldg(const float* p) { return __ldg(p); }
+
+// float atomic max for non-negative values (bit pattern order == value order)
+__device__ __forceinline__ void atomic_max_nonneg(unsigned int* addr, float v) {
+  atomicMax(addr, __float_as_uint(v));
+}
+
+// ------------------------------------------------------------------ launchers
+// predictor (aj_predictor.cu)
+int launch_predictor(const AjStepParams& p, const Layout& L, void* ws, const float* u,
+                     const float* v, const float* mask, const float* nsg, int double_count,
+                     float* us, float* vs, cudaStream_t st);
+int launch_les(const AjStepParams& p, const Layout& L, void* ws, int model, const float* u,
+               const float* v, int mac_input, float* nu_sgs, float* cd, cudaStream_t st);
+int launch_cfl(const AjStepParams& p, void* ws, const float* u, const float* v,
+               float* dt_out, cudaStream_t st);
+int launch_set_dt(const AjStepParams& p, void* ws, cudaStream_t st);
+int launch_chi(const AjStepParams& p, const Layout& L, void* ws, const float* mask,
+               const float* sdf, cudaStream_t st);
+// projection (aj_project.cu)
+int launch_rhs(const AjStepParams& p, const Layout& L, void* ws, const float* us,
+               const float* vs, const float* mask, float* b, cudaStream_t st);
+int launch_correct(const AjStepParams& p, const Layout& L, void* ws, const float* us,
+                   const float* vs, const float* pr, const float* mask, float* uo, float* vo,
+                   cudaStream_t st);
+// pressure (aj_pressure.cu)
+int prepare_pressure(const AjStepParams& p, const Layout& L, void* ws, const float* mask,
+                     cudaStream_t st);
+int launch_mg_rhs(const AjStepParams& p, const Layout& L, void* ws, const float* rhs,
+                  const float* mask, cudaStream_t st);
+int launch_pressure(const AjStepParams& p, const Layout& L, void* ws, const float* mask,
+                    const float* p0, float* pout, AjStats* stats, cudaStream_t st);
+int profile_pressure_kernel(const AjStepParams& p, const Layout& L, void* ws, int which,
+                            cudaStream_t st);
+
+inline unsigned cdiv(long a, long b) { return (unsigned)((a + b - 1) / b); }
+
+}  // namespace aj

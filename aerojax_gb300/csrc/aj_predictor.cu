@@ -1,0 +1,820 @@
+// Momentum predictor: RK3 / Heun RK2 stages with implicit Brinkman
+// penalisation, upwind or WENO5 advection, Laplacian (+ biharmonic) diffusion,
+// Smagorinsky eddy viscosity and the CFL time step.
+//
+// Collocated stages follow advection_schemes/rk3_simple_new.py:175-358; the
+// MAC stages follow advection_schemes/rk3_mac.py:220-504.  Each stage is one
+// kernel that reads the stage input with its halo straight from global memory
+// (L1/L2 serve the neighbour re-reads) and writes the stage output.  The last
+// stage also applies the hard mask and the boundary conditions, by evaluating
+// the stage formula at the cell the boundary condition copies from.
+#include "aj_internal.cuh"
+#include <math.h>
+
+namespace aj {
+
+// ============================================================ set-up: chi
+// chi = sigmoid(-sdf / (0.1 dx)) when an SDF is given, else 1 - mask
+// (rk3_simple_new.py:194-200).  MAC uses chi = 1 - mask interpolated to
+// faces on the fly (rk3_mac.py:462-463), so only the collocated array exists.
+__global__ void k_chi(const float* __restrict__ mask, const float* __restrict__ sdf,
+                      float* __restrict__ chi, long n, float inv_w) {
+  long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  if (sdf) {
+    float x = -sdf[k] * inv_w;
+    // logistic function, evaluated on the branch that cannot overflow
+    float c = x >= 0.f ? 1.f / (1.f + expf(-x)) : expf(x) / (1.f + expf(x));
+    chi[k] = c;
+  } else {
+    chi[k] = 1.f - mask[k];
+  }
+}
+
+int launch_chi(const AjStepParams& p, const Layout& L, void* ws, const float* mask,
+               const float* sdf, cudaStream_t st) {
+  if (p.grid_type != AJ_GRID_COLLOCATED) return AJ_OK;
+  long n = (long)p.nx * p.ny;
+  k_chi<<<cdiv(n, 256), 256, 0, st>>>(mask, p.has_sdf ? sdf : nullptr, at<float>(ws, L.chi), n,
+                                      (float)(1.0 / (0.1 * p.dx)));
+  return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+}
+
+// ============================================================ dt
+__global__ void k_set_dt(DevScalars* sc, float dt, float dtc) {
+  sc->dt = dt;
+  sc->dt_corr = dtc > 0.f ? dtc : dt;
+}
+
+int launch_set_dt(const AjStepParams& p, void* ws, cudaStream_t st) {
+  k_set_dt<<<1, 1, 0, st>>>(at<DevScalars>(ws, 0), (float)p.dt, (float)p.dt_correction);
+  return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+}
+
+// compute_cfl_timestep (timestepping/cfl_adaptive_dt.py:6-71): block maxima,
+// atomicMax, and the last block to finish turns the maximum into dt.
+__global__ void k_cfl(const float* __restrict__ u, const float* __restrict__ v, long nu_,
+                      long nv_, int mac, DevScalars* sc, float* dt_out, double h, double nu,
+                      double cfl, double dt_min, double dt_max, float dtc_host) {
+  float m = 0.f;
+  long stride = (long)gridDim.x * blockDim.x;
+  long n = nu_ > nv_ ? nu_ : nv_;
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += stride) {
+    if (mac) {
+      if (k < nu_) m = fmaxf(m, fabsf(u[k]));
+      if (k < nv_) m = fmaxf(m, fabsf(v[k]));
+    } else {
+      float a = u[k], b = v[k];
+      m = fmaxf(m, sqrtf(a * a + b * b));
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  __shared__ float wm[32];
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) wm[w] = m;
+  __syncthreads();
+  if (w == 0) {
+    m = lane < (int)(blockDim.x >> 5) ? wm[lane] : 0.f;
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane == 0) {
+      atomic_max_nonneg(&sc->cfl_max_bits, m);
+      __threadfence();
+      unsigned int done = atomicAdd(&sc->cfl_count, 1u);
+      if (done == gridDim.x - 1) {
+        __threadfence();
+        float mx = __uint_as_float(atomicAdd(&sc->cfl_max_bits, 0u));
+        const double EPS = 1e-12;
+        double dtc = h / ((double)mx + EPS);
+        double dtv = 0.25 * h * h / (nu + EPS);
+        double dt = (dtc < dtv ? dtc : dtv) * cfl;
+        dt = dt < dt_max ? dt : dt_max;
+        dt = dt > dt_min ? dt : dt_min;
+        sc->dt = (float)dt;
+        sc->dt_corr = dtc_host > 0.f ? dtc_host : (float)dt;
+        if (dt_out) *dt_out = (float)dt;
+        sc->cfl_max_bits = 0u;
+        sc->cfl_count = 0u;
+      }
+    }
+  }
+}
+
+int launch_cfl(const AjStepParams& p, void* ws, const float* u, const float* v, float* dt_out,
+               cudaStream_t st) {
+  int mac = p.grid_type == AJ_GRID_MAC;
+  long nu_ = mac ? (long)(p.nx + 1) * p.ny : (long)p.nx * p.ny;
+  long nv_ = mac ? (long)p.nx * (p.ny + 1) : (long)p.nx * p.ny;
+  long n = nu_ > nv_ ? nu_ : nv_;
+  unsigned blocks = cdiv(n, 256 * 8);
+  if (blocks > 1216) blocks = 1216;
+  if (blocks < 1) blocks = 1;
+  k_cfl<<<blocks, 256, 0, st>>>(u, v, nu_, nv_, mac, at<DevScalars>(ws, 0), dt_out,
+                                p.dx < p.dy ? p.dx : p.dy, p.nu, p.cfl_target, p.dt_min,
+                                p.dt_max, (float)p.dt_correction);
+  return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+}
+
+// ============================================================ LES
+// |S| = sqrt(2(Sxx^2 + Syy^2 + 2 Sxy^2) + 1e-10) with periodic central
+// gradients (solver/les_models.py:22-54 via solver/operators.py:11-38).
+struct Strain {
+  float smag, sxx, syy, sxy;
+};
+
+__device__ __forceinline__ Strain strain_at(const float* __restrict__ u,
+                                            const float* __restrict__ v, int i, int j, int nx,
+                                            int ny, float h2x, float h2y) {
+  int ip = wrapi(i + 1, nx), im = wrapi(i - 1, nx), jp = wrapi(j + 1, ny), jm = wrapi(j - 1, ny);
+  float du_dx = (ldg(u + (long)ip * ny + j) - ldg(u + (long)im * ny + j)) * h2x;
+  float du_dy = (ldg(u + (long)i * ny + jp) - ldg(u + (long)i * ny + jm)) * h2y;
+  float dv_dx = (ldg(v + (long)ip * ny + j) - ldg(v + (long)im * ny + j)) * h2x;
+  float dv_dy = (ldg(v + (long)i * ny + jp) - ldg(v + (long)i * ny + jm)) * h2y;
+  Strain s;
+  s.sxx = du_dx;
+  s.syy = dv_dy;
+  s.sxy = 0.5f * (du_dy + dv_dx);
+  s.smag = sqrtf(2.0f * (s.sxx * s.sxx + s.syy * s.syy + 2.0f * s.sxy * s.sxy) + 1e-10f);
+  return s;
+}
+
+// constant_smagorinsky (les_models.py:179-200): nu_sgs = (C_s Delta)^2 |S|
+__global__ void k_les_const(const float* __restrict__ u, const float* __restrict__ v,
+                            float* __restrict__ nsg, int nx, int ny, float h2x, float h2y,
+                            float coef) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= nx || j >= ny) return;
+  Strain s = strain_at(u, v, i, j, nx, ny, h2x, h2y);
+  nsg[(long)i * ny + j] = coef * s.smag;
+}
+
+// MAC faces to cell centres (solver/operators_mac.py:118-127)
+__global__ void k_mac_to_center(const float* __restrict__ u, const float* __restrict__ v,
+                                float* __restrict__ uc, float* __restrict__ vc, int nx, int ny) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= nx || j >= ny) return;
+  uc[(long)i * ny + j] = 0.5f * (u[(long)(i + 1) * ny + j] + u[(long)i * ny + j]);
+  vc[(long)i * ny + j] = 0.5f * (v[(long)i * (ny + 1) + j + 1] + v[(long)i * (ny + 1) + j]);
+}
+
+// dynamic_smagorinsky (les_models.py:79-176) in four passes.
+// pass 1: |S| and |S| S_ij at every cell
+__global__ void k_dyn_strain(const float* __restrict__ u, const float* __restrict__ v, int nx,
+                             int ny, float h2x, float h2y, float* __restrict__ smag,
+                             float* __restrict__ ssxx, float* __restrict__ ssxy,
+                             float* __restrict__ ssyy) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= nx || j >= ny) return;
+  Strain s = strain_at(u, v, i, j, nx, ny, h2x, h2y);
+  long k = (long)i * ny + j;
+  smag[k] = s.smag;
+  ssxx[k] = s.smag * s.sxx;
+  ssxy[k] = s.smag * s.sxy;
+  ssyy[k] = s.smag * s.syy;
+}
+
+// pass 2: 5x5 periodic box filter (les_models.py:57-76) of u, v, uu, uv, vv
+// and of the three |S| S_ij products
+__global__ void k_dyn_filter(const float* __restrict__ u, const float* __restrict__ v,
+                             const float* __restrict__ ssxx, const float* __restrict__ ssxy,
+                             const float* __restrict__ ssyy, int nx, int ny,
+                             float* __restrict__ ut, float* __restrict__ vt,
+                             float* __restrict__ uut, float* __restrict__ uvt,
+                             float* __restrict__ vvt, float* __restrict__ fxx,
+                             float* __restrict__ fxy, float* __restrict__ fyy) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= nx || j >= ny) return;
+  float a_u = 0, a_v = 0, a_uu = 0, a_uv = 0, a_vv = 0, a_xx = 0, a_xy = 0, a_yy = 0;
+  for (int di = -2; di <= 2; ++di) {
+    int ii = wrapi(i - di, nx);
+    for (int dj = -2; dj <= 2; ++dj) {
+      long k = (long)ii * ny + wrapi(j - dj, ny);
+      float uu = ldg(u + k), vv = ldg(v + k);
+      a_u += uu;
+      a_v += vv;
+      a_uu += uu * uu;
+      a_uv += uu * vv;
+      a_vv += vv * vv;
+      a_xx += ldg(ssxx + k);
+      a_xy += ldg(ssxy + k);
+      a_yy += ldg(ssyy + k);
+    }
+  }
+  const float inv = 1.0f / 25.0f;
+  long k = (long)i * ny + j;
+  ut[k] = a_u * inv;
+  vt[k] = a_v * inv;
+  uut[k] = a_uu * inv;
+  uvt[k] = a_uv * inv;
+  vvt[k] = a_vv * inv;
+  fxx[k] = a_xx * inv;
+  fxy[k] = a_xy * inv;
+  fyy[k] = a_yy * inv;
+}
+
+// pass 3: Leonard stress L_ij, model tensor M_ij, contractions LM and MM
+__global__ void k_dyn_lm(const float* __restrict__ ut, const float* __restrict__ vt,
+                         const float* __restrict__ uut, const float* __restrict__ uvt,
+                         const float* __restrict__ vvt, const float* __restrict__ fxx,
+                         const float* __restrict__ fxy, const float* __restrict__ fyy, int nx,
+                         int ny, float h2x, float h2y, float a2, float* __restrict__ lm,
+                         float* __restrict__ mm) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= nx || j >= ny) return;
+  long k = (long)i * ny + j;
+  Strain st = strain_at(ut, vt, i, j, nx, ny, h2x, h2y);
+  float u_ = ut[k], v_ = vt[k];
+  float L11 = u_ * u_ - uut[k], L12 = u_ * v_ - uvt[k], L22 = v_ * v_ - vvt[k];
+  float M11 = a2 * st.smag * st.sxx - fxx[k];
+  float M12 = a2 * st.smag * st.sxy - fxy[k];
+  float M22 = a2 * st.smag * st.syy - fyy[k];
+  lm[k] = L11 * M11 + L12 * M12 + L22 * M22;
+  mm[k] = M11 * M11 + M12 * M12 + M22 * M22;
+}
+
+// pass 4: 3x3 interior average, C_d = <LM>/(<MM>+1e-8) clipped to [0, 0.2],
+// nu_sgs = C_d Delta^2 |S|
+__global__ void k_dyn_final(const float* __restrict__ lm, const float* __restrict__ mm,
+                            const float* __restrict__ smag, int nx, int ny, float delta2,
+                            float* __restrict__ nsg, float* __restrict__ cd) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= nx || j >= ny) return;
+  long k = (long)i * ny + j;
+  float alm = 0.f, amm = 0.f;
+  if (i > 0 && i < nx - 1 && j > 0 && j < ny - 1) {
+    for (int di = -1; di <= 1; ++di)
+      for (int dj = -1; dj <= 1; ++dj) {
+        long q = (long)(i + di) * ny + (j + dj);
+        alm += lm[q];
+        amm += mm[q];
+      }
+    alm *= (1.0f / 9.0f);
+    amm *= (1.0f / 9.0f);
+  }
+  float c = alm / (amm + 1e-8f);
+  c = fminf(fmaxf(c, 0.0f), 0.2f);
+  nsg[k] = c * delta2 * smag[k];
+  if (cd) cd[k] = c;
+}
+
+int launch_les(const AjStepParams& p, const Layout& L, void* ws, int model, const float* u,
+               const float* v, int mac_input, float* nsg, float* cd, cudaStream_t st) {
+  int nx = p.nx, ny = p.ny;
+  dim3 blk(32, 8), grd(cdiv(ny, 32), cdiv(nx, 8));
+  float h2x = (float)(1.0 / (2.0 * p.dx)), h2y = (float)(1.0 / (2.0 * p.dy));
+  double delta = p.les_delta > 0 ? p.les_delta : sqrt(p.dx * p.dy);
+  long n = (long)nx * ny;
+  float* D = at<float>(ws, L.dyn);
+  const float *uu = u, *vv = v;
+  if (mac_input) {
+    float* uc = D + 14 * n;
+    float* vc = D + 15 * n;
+    k_mac_to_center<<<grd, blk, 0, st>>>(u, v, uc, vc, nx, ny);
+    uu = uc;
+    vv = vc;
+  }
+  if (model == AJ_LES_SMAGORINSKY) {
+    double c = p.smagorinsky_constant * delta;
+    k_les_const<<<grd, blk, 0, st>>>(uu, vv, nsg, nx, ny, h2x, h2y, (float)(c * c));
+  } else if (model == AJ_LES_DYNAMIC) {
+    float *smag = D, *sxx = D + n, *sxy = D + 2 * n, *syy = D + 3 * n;
+    float *ut = D + 4 * n, *vt = D + 5 * n, *uut = D + 6 * n, *uvt = D + 7 * n, *vvt = D + 8 * n;
+    float *fxx = D + 9 * n, *fxy = D + 10 * n, *fyy = D + 11 * n;
+    float *lm = D + 12 * n, *mm = D + 13 * n;
+    k_dyn_strain<<<grd, blk, 0, st>>>(uu, vv, nx, ny, h2x, h2y, smag, sxx, sxy, syy);
+    k_dyn_filter<<<grd, blk, 0, st>>>(uu, vv, sxx, sxy, syy, nx, ny, ut, vt, uut, uvt, vvt, fxx,
+                                      fxy, fyy);
+    k_dyn_lm<<<grd, blk, 0, st>>>(ut, vt, uut, uvt, vvt, fxx, fxy, fyy, nx, ny, h2x, h2y, 4.0f,
+                                  lm, mm);
+    k_dyn_final<<<grd, blk, 0, st>>>(lm, mm, smag, nx, ny, (float)(delta * delta), nsg, cd);
+  } else {
+    return AJ_ERR_PARAM;
+  }
+  return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+}
+
+// ============================================================ collocated RK
+struct RkArgs {
+  const float *uin, *vin, *u0, *v0, *chi, *mask, *nsg, *k1u, *k1v;
+  float *uout, *vout, *k1u_out, *k1v_out;
+  const DevScalars* sc;
+  int nx, ny;
+  float idx, idy, idx2, idy2, nu, inv_eta, U, nuh_fac;
+  int dc, stage, rk2, flow, slip;
+};
+
+template <bool PER>
+__device__ __forceinline__ float lap_at(const float* __restrict__ f, int i, int j, int nx, int ny,
+                                        float idx2, float idy2) {
+  float c = ldg(f + (long)i * ny + j);
+  float xp = ldg(f + (long)pidx<PER>(i + 1, nx) * ny + j);
+  float xm = ldg(f + (long)pidx<PER>(i - 1, nx) * ny + j);
+  float yp = ldg(f + (long)i * ny + pidx<PER>(j + 1, ny));
+  float ym = ldg(f + (long)i * ny + pidx<PER>(j - 1, ny));
+  return (xp + xm - 2.f * c) * idx2 + (yp + ym - 2.f * c) * idy2;
+}
+
+// WENO5 reconstruction of a derivative from five one-sided differences
+// (Jiang & Shu 1996 smoothness indicators and linear weights 1/10, 6/10, 3/10;
+// Hamilton-Jacobi form of Jiang & Peng 2000).
+__device__ __forceinline__ float weno5(float v1, float v2, float v3, float v4, float v5) {
+  const float eps = 1e-6f;
+  float b1 = (13.f / 12.f) * (v1 - 2.f * v2 + v3) * (v1 - 2.f * v2 + v3) +
+             0.25f * (v1 - 4.f * v2 + 3.f * v3) * (v1 - 4.f * v2 + 3.f * v3);
+  float b2 = (13.f / 12.f) * (v2 - 2.f * v3 + v4) * (v2 - 2.f * v3 + v4) +
+             0.25f * (v2 - v4) * (v2 - v4);
+  float b3 = (13.f / 12.f) * (v3 - 2.f * v4 + v5) * (v3 - 2.f * v4 + v5) +
+             0.25f * (3.f * v3 - 4.f * v4 + v5) * (3.f * v3 - 4.f * v4 + v5);
+  float a1 = 0.1f / ((eps + b1) * (eps + b1));
+  float a2 = 0.6f / ((eps + b2) * (eps + b2));
+  float a3 = 0.3f / ((eps + b3) * (eps + b3));
+  float q1 = v1 * (1.f / 3.f) - (7.f / 6.f) * v2 + (11.f / 6.f) * v3;
+  float q2 = -v2 * (1.f / 6.f) + (5.f / 6.f) * v3 + v4 * (1.f / 3.f);
+  float q3 = v3 * (1.f / 3.f) + (5.f / 6.f) * v4 - v5 * (1.f / 6.f);
+  return (a1 * q1 + a2 * q2 + a3 * q3) / (a1 + a2 + a3);
+}
+
+// upwind-biased WENO5 derivative of f along one axis at (i, j)
+template <bool PER, int AXIS>
+__device__ __forceinline__ float weno_d(const float* __restrict__ f, int i, int j, int nx,
+                                        int ny, float ih, float vel) {
+  float g[7];
+#pragma unroll
+  for (int o = -3; o <= 3; ++o) {
+    long k = AXIS == 0 ? (long)pidx<PER>(i + o, nx) * ny + j : (long)i * ny + pidx<PER>(j + o, ny);
+    g[o + 3] = ldg(f + k);
+  }
+  // D_m = (f[m+1]-f[m])/h for m = i-3 .. i+2  ->  d[0..5]
+  float d0 = (g[1] - g[0]) * ih, d1 = (g[2] - g[1]) * ih, d2 = (g[3] - g[2]) * ih;
+  float d3 = (g[4] - g[3]) * ih, d4 = (g[5] - g[4]) * ih, d5 = (g[6] - g[5]) * ih;
+  return vel > 0.f ? weno5(d0, d1, d2, d3, d4) : weno5(d5, d4, d3, d2, d1);
+}
+
+// explicit right-hand side for one velocity component f at (i, j)
+// (rk3_simple_new.py:284-313)
+template <bool PER, bool HYPER, int ADV>
+__device__ __forceinline__ float rhs_comp(const RkArgs& a, const float* __restrict__ f, int i,
+                                          int j) {
+  const int nx = a.nx, ny = a.ny;
+  long k = (long)i * ny + j;
+  float uc = ldg(a.uin + k), vc = ldg(a.vin + k), fc = ldg(f + k);
+  float adv;
+  if (ADV == AJ_ADV_WENO5) {
+    adv = uc * weno_d<PER, 0>(f, i, j, nx, ny, a.idx, uc) +
+          vc * weno_d<PER, 1>(f, i, j, nx, ny, a.idy, vc);
+  } else {
+    float fxm = ldg(f + (long)pidx<PER>(i - 1, nx) * ny + j);
+    float fxp = ldg(f + (long)pidx<PER>(i + 1, nx) * ny + j);
+    float fym = ldg(f + (long)i * ny + pidx<PER>(j - 1, ny));
+    float fyp = ldg(f + (long)i * ny + pidx<PER>(j + 1, ny));
+    float fx = uc > 0.f ? uc * (fc - fxm) * a.idx : uc * (fxp - fc) * a.idx;
+    float fy = vc > 0.f ? vc * (fc - fym) * a.idy : vc * (fyp - fc) * a.idy;
+    adv = fx + fy;
+  }
+  float lap = lap_at<PER>(f, i, j, nx, ny, a.idx2, a.idy2);
+  float s = a.nsg ? ldg(a.nsg + k) : 0.f;
+  float nu_arg = a.dc ? a.nu + s : a.nu;              // the GUI passes nu + nu_sgs as nu
+  float nut = a.nsg ? nu_arg + s : nu_arg;            // rk: nu + nu_sgs
+  float r = -adv + nut * lap;
+  if (HYPER) {
+    // biharmonic = Laplacian of the edge-padded Laplacian
+    int ip = pidx<PER>(i + 1, nx), im = pidx<PER>(i - 1, nx);
+    int jp = pidx<PER>(j + 1, ny), jm = pidx<PER>(j - 1, ny);
+    float lxp = lap_at<PER>(f, ip, j, nx, ny, a.idx2, a.idy2);
+    float lxm = lap_at<PER>(f, im, j, nx, ny, a.idx2, a.idy2);
+    float lyp = lap_at<PER>(f, i, jp, nx, ny, a.idx2, a.idy2);
+    float lym = lap_at<PER>(f, i, jm, nx, ny, a.idx2, a.idy2);
+    float bih = (lxp + lxm - 2.f * lap) * a.idx2 + (lyp + lym - 2.f * lap) * a.idy2;
+    r -= nu_arg * a.nuh_fac * bih;
+  }
+  return r;
+}
+
+// stage update of one component at (i, j); returns the stage output
+template <bool PER, bool HYPER, int ADV>
+__device__ __forceinline__ float stage_val(const RkArgs& a, const float* f, const float* f0,
+                                           const float* k1, float* k1_out, int i, int j,
+                                           float dt) {
+  long k = (long)i * a.ny + j;
+  float r = rhs_comp<PER, HYPER, ADV>(a, f, i, j);
+  float x0 = ldg(f0 + k);
+  float den = 1.f + dt * ldg(a.chi + k) * a.inv_eta;
+  if (a.rk2) {
+    if (a.stage == 1) {
+      if (k1_out) k1_out[k] = r;
+      return (x0 + dt * r) / den;
+    }
+    return (x0 + 0.5f * dt * (ldg(k1 + k) + r)) / den;
+  }
+  if (a.stage == 1) return (x0 + dt * r) / den;
+  float xs = x0 + dt * r;
+  if (a.stage == 2) return (0.75f * x0 + 0.25f * xs) / den;
+  return ((1.f / 3.f) * x0 + (2.f / 3.f) * xs) / den;
+}
+
+template <bool PER, bool HYPER, int ADV>
+__global__ void __launch_bounds__(256) k_rk_col(RkArgs a) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  const int nx = a.nx, ny = a.ny;
+  if (i >= nx || j >= ny) return;
+  const float dt = a.sc->dt;
+  long k = (long)i * ny + j;
+  bool last = a.rk2 ? a.stage == 2 : a.stage == 3;
+  if (!last) {
+    a.uout[k] = stage_val<PER, HYPER, ADV>(a, a.uin, a.u0, a.k1u, a.k1u_out, i, j, dt);
+    a.vout[k] = stage_val<PER, HYPER, ADV>(a, a.vin, a.v0, a.k1v, a.k1v_out, i, j, dt);
+    return;
+  }
+  // final stage: hard mask (rk3_simple_new.py:334-335) then boundary
+  // conditions (:250-280), evaluated at the cell each boundary copies from.
+  float uo, vo;
+  if (a.flow == AJ_FLOW_VON_KARMAN) {
+    int ai = (i == nx - 1) ? nx - 2 : i;
+    int bj = a.slip ? (j == 0 ? 1 : (j == ny - 1 ? ny - 2 : j)) : j;
+    if (!a.slip && (j == 0 || j == ny - 1)) uo = 0.f;
+    else if (i == 0) uo = a.U;
+    else {
+      long q = (long)ai * ny + bj;
+      uo = ldg(a.mask + q) > 0.5f ? stage_val<PER, HYPER, ADV>(a, a.uin, a.u0, a.k1u, nullptr, ai, bj, dt) : 0.f;
+    }
+    if (i == 0 || j == 0 || j == ny - 1) vo = 0.f;
+    else {
+      long q = (long)ai * ny + j;
+      vo = ldg(a.mask + q) > 0.5f ? stage_val<PER, HYPER, ADV>(a, a.vin, a.v0, a.k1v, nullptr, ai, j, dt) : 0.f;
+    }
+  } else if (a.flow == AJ_FLOW_LID_DRIVEN_CAVITY) {
+    bool edge_x = (i == 0 || i == nx - 1);
+    if (edge_x || j == 0) uo = 0.f;
+    else if (j == ny - 1) uo = a.U;
+    else uo = ldg(a.mask + k) > 0.5f ? stage_val<PER, HYPER, ADV>(a, a.uin, a.u0, a.k1u, nullptr, i, j, dt) : 0.f;
+    if (edge_x || j == 0 || j == ny - 1) vo = 0.f;
+    else vo = ldg(a.mask + k) > 0.5f ? stage_val<PER, HYPER, ADV>(a, a.vin, a.v0, a.k1v, nullptr, i, j, dt) : 0.f;
+  } else {
+    bool m = ldg(a.mask + k) > 0.5f;
+    uo = m ? stage_val<PER, HYPER, ADV>(a, a.uin, a.u0, a.k1u, nullptr, i, j, dt) : 0.f;
+    vo = m ? stage_val<PER, HYPER, ADV>(a, a.vin, a.v0, a.k1v, nullptr, i, j, dt) : 0.f;
+  }
+  a.uout[k] = uo;
+  a.vout[k] = vo;
+}
+
+template <bool PER>
+static void dispatch_rk_col(const RkArgs& a, bool hyper, int adv, dim3 g, dim3 b, cudaStream_t st) {
+  if (hyper) {
+    if (adv == AJ_ADV_WENO5) k_rk_col<PER, true, AJ_ADV_WENO5><<<g, b, 0, st>>>(a);
+    else k_rk_col<PER, true, AJ_ADV_UPWIND><<<g, b, 0, st>>>(a);
+  } else {
+    if (adv == AJ_ADV_WENO5) k_rk_col<PER, false, AJ_ADV_WENO5><<<g, b, 0, st>>>(a);
+    else k_rk_col<PER, false, AJ_ADV_UPWIND><<<g, b, 0, st>>>(a);
+  }
+}
+
+// ============================================================ MAC RK
+// u: (nx+1) x ny faces, v: nx x (ny+1) faces, mask / nu_sgs: nx x ny cells.
+struct RkMac {
+  const float *uin, *vin, *u0, *v0, *mask, *nsg, *k1u, *k1v;
+  float *uout, *vout, *k1u_out, *k1v_out;
+  const DevScalars* sc;
+  int nx, ny;
+  float idx, idy, idx2, idy2, nu, inv_eta, U, nuh;
+  int stage, rk2, flow, slip;
+};
+
+// velocities after the boundary conditions of rk3_mac.py:292-330, the
+// working copy the advection term uses (:381)
+__device__ __forceinline__ float uw_at(const RkMac& a, const float* __restrict__ u, int i, int j) {
+  const int nx = a.nx, ny = a.ny;
+  if (a.flow == AJ_FLOW_VON_KARMAN) {
+    if (!a.slip && (j == 0 || j == ny - 1)) return 0.f;
+    if (i == 0) return a.U;
+    int ii = i == nx ? nx - 1 : i;
+    int jj = a.slip ? (j == 0 ? 1 : (j == ny - 1 ? ny - 2 : j)) : j;
+    return ldg(u + (long)ii * ny + jj);
+  } else if (a.flow == AJ_FLOW_LID_DRIVEN_CAVITY) {
+    if (i == 0 || i == nx) return 0.f;
+    if (j == 0) return 0.f;
+    if (j == ny - 1) return a.U;
+    return ldg(u + (long)i * ny + j);
+  }
+  return ldg(u + (long)i * ny + j);
+}
+
+__device__ __forceinline__ float vw_at(const RkMac& a, const float* __restrict__ v, int i, int j) {
+  const int nx = a.nx, ny = a.ny;
+  const int nyv = ny + 1;
+  if (a.flow == AJ_FLOW_VON_KARMAN) {
+    if (i == 0 || j == 0 || j == ny) return 0.f;
+    int ii = i == nx - 1 ? nx - 2 : i;
+    return ldg(v + (long)ii * nyv + j);
+  } else if (a.flow == AJ_FLOW_LID_DRIVEN_CAVITY) {
+    if (i == 0 || i == nx - 1 || j == 0 || j == ny) return 0.f;
+    return ldg(v + (long)i * nyv + j);
+  }
+  return ldg(v + (long)i * nyv + j);
+}
+
+// Laplacian on faces with symmetric (== edge for one cell) ghosts for slip
+// walls, or antisymmetric wall ghosts for no-slip (rk3_mac.py:268-290)
+template <int COMP>
+__device__ __forceinline__ float lap_face(const RkMac& a, const float* __restrict__ f, int i,
+                                          int j) {
+  const int n = COMP == 0 ? a.nx + 1 : a.nx;
+  const int m = COMP == 0 ? a.ny : a.ny + 1;
+  float c = ldg(f + (long)i * m + j);
+  float xp, xm, yp, ym;
+  if (a.slip) {
+    xp = ldg(f + (long)clampi(i + 1, n) * m + j);
+    xm = ldg(f + (long)clampi(i - 1, n) * m + j);
+    yp = ldg(f + (long)i * m + clampi(j + 1, m));
+    ym = ldg(f + (long)i * m + clampi(j - 1, m));
+  } else if (COMP == 0) {
+    // y ghosts are -f at the wall, then x padded by edge
+    xp = ldg(f + (long)clampi(i + 1, n) * m + j);
+    xm = ldg(f + (long)clampi(i - 1, n) * m + j);
+    yp = j + 1 < m ? ldg(f + (long)i * m + j + 1) : -c;
+    ym = j - 1 >= 0 ? ldg(f + (long)i * m + j - 1) : -c;
+  } else {
+    xp = i + 1 < n ? ldg(f + (long)(i + 1) * m + j) : -c;
+    xm = i - 1 >= 0 ? ldg(f + (long)(i - 1) * m + j) : -c;
+    yp = ldg(f + (long)i * m + clampi(j + 1, m));
+    ym = ldg(f + (long)i * m + clampi(j - 1, m));
+  }
+  return (xp + xm - 2.f * c) * a.idx2 + (yp + ym - 2.f * c) * a.idy2;
+}
+
+template <int COMP>
+__device__ __forceinline__ float bih_face(const RkMac& a, const float* __restrict__ f, int i,
+                                          int j, float lc) {
+  // Laplacian of the face Laplacian with the same ghost rule
+  const int n = COMP == 0 ? a.nx + 1 : a.nx;
+  const int m = COMP == 0 ? a.ny : a.ny + 1;
+  float xp, xm, yp, ym;
+  if (a.slip) {
+    xp = lap_face<COMP>(a, f, clampi(i + 1, n), j);
+    xm = lap_face<COMP>(a, f, clampi(i - 1, n), j);
+    yp = lap_face<COMP>(a, f, i, clampi(j + 1, m));
+    ym = lap_face<COMP>(a, f, i, clampi(j - 1, m));
+  } else if (COMP == 0) {
+    xp = lap_face<COMP>(a, f, clampi(i + 1, n), j);
+    xm = lap_face<COMP>(a, f, clampi(i - 1, n), j);
+    yp = j + 1 < m ? lap_face<COMP>(a, f, i, j + 1) : -lc;
+    ym = j - 1 >= 0 ? lap_face<COMP>(a, f, i, j - 1) : -lc;
+  } else {
+    xp = i + 1 < n ? lap_face<COMP>(a, f, i + 1, j) : -lc;
+    xm = i - 1 >= 0 ? lap_face<COMP>(a, f, i - 1, j) : -lc;
+    yp = lap_face<COMP>(a, f, i, clampi(j + 1, m));
+    ym = lap_face<COMP>(a, f, i, clampi(j - 1, m));
+  }
+  return (xp + xm - 2.f * lc) * a.idx2 + (yp + ym - 2.f * lc) * a.idy2;
+}
+
+// x-face interpolation of a cell field (operators_mac.py:130-137)
+__device__ __forceinline__ float xface(const float* __restrict__ c, int i, int j, int nx, int ny) {
+  return 0.5f * (ldg(c + (long)clampi(i, nx) * ny + j) + ldg(c + (long)clampi(i - 1, nx) * ny + j));
+}
+__device__ __forceinline__ float yface(const float* __restrict__ c, int i, int j, int nx, int ny) {
+  return 0.5f * (ldg(c + (long)i * ny + clampi(j, ny)) + ldg(c + (long)i * ny + clampi(j - 1, ny)));
+}
+
+// u-momentum right-hand side at u-face (i, j) (rk3_mac.py:373-400, 425-458)
+template <bool HYPER>
+__device__ float rhs_mac_u(const RkMac& a, int i, int j) {
+  const int nx = a.nx, ny = a.ny;
+  float uw = uw_at(a, a.uin, i, j);
+  // v at the u-face: centre average of v_work, edge-padded in x, face average
+  auto vcen = [&](int ci) {
+    ci = clampi(ci, nx);
+    return 0.5f * (vw_at(a, a.vin, ci, j + 1) + vw_at(a, a.vin, ci, j));
+  };
+  float v_at_u = 0.5f * (vcen(i) + vcen(i - 1));
+  float uxm = uw_at(a, a.uin, i > 0 ? i - 1 : 0, j);
+  float uxp = uw_at(a, a.uin, i < nx ? i + 1 : nx, j);
+  float back = (uw - uxm) * a.idx, fwd = (uxp - uw) * a.idx;
+  float al = 0.5f * (1.f + tanhf(uw / 0.05f));
+  float adv_x = uw * (al * back + (1.f - al) * fwd);
+  float du_dy;
+  if (j == 0) du_dy = (uw_at(a, a.uin, i, 1) - uw) * a.idy;
+  else if (j == ny - 1) du_dy = (uw - uw_at(a, a.uin, i, ny - 2)) * a.idy;
+  else du_dy = (uw_at(a, a.uin, i, j + 1) - uw_at(a, a.uin, i, j - 1)) * (0.5f * a.idy);
+  float adv = (adv_x + v_at_u * du_dy) * xface(a.mask, i, j, nx, ny);
+  float lap = lap_face<0>(a, a.uin, i, j);
+  float nut = a.nsg ? a.nu + xface(a.nsg, i, j, nx, ny) : a.nu;
+  float r = -adv + nut * lap;
+  if (HYPER) r -= a.nuh * bih_face<0>(a, a.uin, i, j, lap);
+  return r;
+}
+
+template <bool HYPER>
+__device__ float rhs_mac_v(const RkMac& a, int i, int j) {
+  const int nx = a.nx, ny = a.ny;
+  float vw = vw_at(a, a.vin, i, j);
+  auto ucen = [&](int cj) {
+    cj = clampi(cj, ny);
+    return 0.5f * (uw_at(a, a.uin, i + 1, cj) + uw_at(a, a.uin, i, cj));
+  };
+  float u_at_v = 0.5f * (ucen(j) + ucen(j - 1));
+  float vym = vw_at(a, a.vin, i, j > 0 ? j - 1 : 0);
+  float vyp = vw_at(a, a.vin, i, j < ny ? j + 1 : ny);
+  float back = (vw - vym) * a.idy, fwd = (vyp - vw) * a.idy;
+  float al = 0.5f * (1.f + tanhf(vw / 0.05f));
+  float adv_y = vw * (al * back + (1.f - al) * fwd);
+  float dv_dx;
+  if (i == 0) dv_dx = (vw_at(a, a.vin, 1, j) - vw) * a.idx;
+  else if (i == nx - 1) dv_dx = (vw - vw_at(a, a.vin, nx - 2, j)) * a.idx;
+  else dv_dx = (vw_at(a, a.vin, i + 1, j) - vw_at(a, a.vin, i - 1, j)) * (0.5f * a.idx);
+  float adv = (u_at_v * dv_dx + adv_y) * yface(a.mask, i, j, nx, ny);
+  float lap = lap_face<1>(a, a.vin, i, j);
+  float nut = a.nsg ? a.nu + yface(a.nsg, i, j, nx, ny) : a.nu;
+  float r = -adv + nut * lap;
+  if (HYPER) r -= a.nuh * bih_face<1>(a, a.vin, i, j, lap);
+  return r;
+}
+
+template <int COMP, bool HYPER>
+__device__ __forceinline__ float stage_mac(const RkMac& a, int i, int j, float dt, float* k1o) {
+  const int m = COMP == 0 ? a.ny : a.ny + 1;
+  long k = (long)i * m + j;
+  float r = COMP == 0 ? rhs_mac_u<HYPER>(a, i, j) : rhs_mac_v<HYPER>(a, i, j);
+  float x0 = ldg((COMP == 0 ? a.u0 : a.v0) + k);
+  // chi on faces = face average of (1 - mask)
+  float chi;
+  if (COMP == 0) {
+    chi = 0.5f * ((1.f - ldg(a.mask + (long)clampi(i, a.nx) * a.ny + j)) +
+                  (1.f - ldg(a.mask + (long)clampi(i - 1, a.nx) * a.ny + j)));
+  } else {
+    chi = 0.5f * ((1.f - ldg(a.mask + (long)i * a.ny + clampi(j, a.ny))) +
+                  (1.f - ldg(a.mask + (long)i * a.ny + clampi(j - 1, a.ny))));
+  }
+  float den = 1.f + dt * chi * a.inv_eta;
+  if (a.rk2) {
+    if (a.stage == 1) {
+      if (k1o) k1o[k] = r;
+      return (x0 + dt * r) / den;
+    }
+    return (x0 + 0.5f * dt * (ldg((COMP == 0 ? a.k1u : a.k1v) + k) + r)) / den;
+  }
+  if (a.stage == 1) return (x0 + dt * r) / den;
+  float xs = x0 + dt * r;
+  if (a.stage == 2) return (0.75f * x0 + 0.25f * xs) / den;
+  float out = ((1.f / 3.f) * x0 + (2.f / 3.f) * xs) / den;
+  return chi < 0.5f ? out : 0.f;                     // hard mask (rk3_mac.py:483-484)
+}
+
+template <bool HYPER>
+__global__ void __launch_bounds__(256) k_rk_mac(RkMac a) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  const int nx = a.nx, ny = a.ny;
+  const float dt = a.sc->dt;
+  bool last = a.rk2 ? a.stage == 2 : a.stage == 3;
+  // u faces
+  if (i <= nx && j < ny) {
+    long k = (long)i * ny + j;
+    float o;
+    if (!last) {
+      o = stage_mac<0, HYPER>(a, i, j, dt, a.k1u_out);
+    } else if (a.flow == AJ_FLOW_VON_KARMAN) {
+      if (!a.slip && (j == 0 || j == ny - 1)) o = 0.f;
+      else if (i == 0) o = a.U;
+      else {
+        int ii = i == nx ? nx - 1 : i;
+        int jj = a.slip ? (j == 0 ? 1 : (j == ny - 1 ? ny - 2 : j)) : j;
+        o = stage_mac<0, HYPER>(a, ii, jj, dt, nullptr);
+      }
+    } else if (a.flow == AJ_FLOW_LID_DRIVEN_CAVITY) {
+      if (i == 0 || i == nx || j == 0) o = 0.f;
+      else if (j == ny - 1) o = a.U;
+      else o = stage_mac<0, HYPER>(a, i, j, dt, nullptr);
+    } else {
+      o = stage_mac<0, HYPER>(a, i, j, dt, nullptr);
+    }
+    a.uout[k] = o;
+  }
+  // v faces
+  if (i < nx && j <= ny) {
+    long k = (long)i * (ny + 1) + j;
+    float o;
+    if (!last) {
+      o = stage_mac<1, HYPER>(a, i, j, dt, a.k1v_out);
+    } else if (a.flow == AJ_FLOW_VON_KARMAN) {
+      if (i == 0 || j == 0 || j == ny) o = 0.f;
+      else o = stage_mac<1, HYPER>(a, i == nx - 1 ? nx - 2 : i, j, dt, nullptr);
+    } else if (a.flow == AJ_FLOW_LID_DRIVEN_CAVITY) {
+      if (i == 0 || i == nx - 1 || j == 0 || j == ny) o = 0.f;
+      else o = stage_mac<1, HYPER>(a, i, j, dt, nullptr);
+    } else {
+      o = stage_mac<1, HYPER>(a, i, j, dt, nullptr);
+    }
+    a.vout[k] = o;
+  }
+}
+
+// ============================================================ driver
+int launch_predictor(const AjStepParams& p, const Layout& L, void* ws, const float* u,
+                     const float* v, const float* mask, const float* nsg, int double_count,
+                     float* us, float* vs, cudaStream_t st) {
+  const DevScalars* sc = at<DevScalars>(ws, 0);
+  const int nx = p.nx, ny = p.ny;
+  const bool rk2 = p.fast_mode != 0;
+  const int nstage = rk2 ? 2 : 3;
+  const bool hyper = p.nu_hyper_ratio > 0.0;
+  float* A[2] = {at<float>(ws, L.sA_u), at<float>(ws, L.sA_v)};
+  float* B[2] = {at<float>(ws, L.sB_u), at<float>(ws, L.sB_v)};
+  float* K[2] = {at<float>(ws, L.k1_u), at<float>(ws, L.k1_v)};
+  const double eta = p.grid_type == AJ_GRID_MAC ? (p.brinkman_eta > 1e-10 ? p.brinkman_eta : 1e-10)
+                                                : p.brinkman_eta;
+  if (p.grid_type == AJ_GRID_COLLOCATED) {
+    if (p.advection != AJ_ADV_UPWIND && p.advection != AJ_ADV_WENO5) return AJ_ERR_PARAM;
+    RkArgs a{};
+    a.u0 = u;
+    a.v0 = v;
+    a.chi = at<float>(ws, L.chi);
+    a.mask = mask;
+    a.nsg = nsg;
+    a.k1u = K[0];
+    a.k1v = K[1];
+    a.sc = sc;
+    a.nx = nx;
+    a.ny = ny;
+    a.idx = (float)(1.0 / p.dx);
+    a.idy = (float)(1.0 / p.dy);
+    a.idx2 = (float)(1.0 / (p.dx * p.dx));
+    a.idy2 = (float)(1.0 / (p.dy * p.dy));
+    a.nu = (float)p.nu;
+    a.inv_eta = (float)(1.0 / eta);
+    a.U = (float)p.U_inf;
+    a.nuh_fac = (float)(p.nu_hyper_ratio * p.dx * p.dy);
+    a.dc = double_count;
+    a.rk2 = rk2;
+    a.flow = p.flow_type;
+    a.slip = p.slip_walls;
+    dim3 blk(32, 8), grd(cdiv(ny, 32), cdiv(nx, 8));
+    const float* in_u = u;
+    const float* in_v = v;
+    for (int s = 1; s <= nstage; ++s) {
+      a.stage = s;
+      a.uin = in_u;
+      a.vin = in_v;
+      bool last = s == nstage;
+      float** dst = (s % 2 == 1) ? A : B;
+      a.uout = last ? us : dst[0];
+      a.vout = last ? vs : dst[1];
+      a.k1u_out = (rk2 && s == 1) ? K[0] : nullptr;
+      a.k1v_out = (rk2 && s == 1) ? K[1] : nullptr;
+      if (p.flow_type == AJ_FLOW_TAYLOR_GREEN) dispatch_rk_col<true>(a, hyper, p.advection, grd, blk, st);
+      else dispatch_rk_col<false>(a, hyper, p.advection, grd, blk, st);
+      in_u = a.uout;
+      in_v = a.vout;
+    }
+  } else {
+    if (p.advection != AJ_ADV_UPWIND) return AJ_ERR_PARAM;   // MAC: tanh-blended upwind only
+    RkMac a{};
+    a.u0 = u;
+    a.v0 = v;
+    a.mask = mask;
+    a.nsg = nsg;
+    a.k1u = K[0];
+    a.k1v = K[1];
+    a.sc = sc;
+    a.nx = nx;
+    a.ny = ny;
+    a.idx = (float)(1.0 / p.dx);
+    a.idy = (float)(1.0 / p.dy);
+    a.idx2 = (float)(1.0 / (p.dx * p.dx));
+    a.idy2 = (float)(1.0 / (p.dy * p.dy));
+    a.nu = (float)p.nu;
+    a.inv_eta = (float)(1.0 / eta);
+    a.U = (float)p.U_inf;
+    a.nuh = (float)(p.nu * p.nu_hyper_ratio * p.dx * p.dy);
+    a.rk2 = rk2;
+    a.flow = p.flow_type;
+    a.slip = p.slip_walls;
+    dim3 blk(32, 8), grd(cdiv(ny + 1, 32), cdiv(nx + 1, 8));
+    const float* in_u = u;
+    const float* in_v = v;
+    for (int s = 1; s <= nstage; ++s) {
+      a.stage = s;
+      a.uin = in_u;
+      a.vin = in_v;
+      bool last = s == nstage;
+      float** dst = (s % 2 == 1) ? A : B;
+      a.uout = last ? us : dst[0];
+      a.vout = last ? vs : dst[1];
+      a.k1u_out = (rk2 && s == 1) ? K[0] : nullptr;
+      a.k1v_out = (rk2 && s == 1) ? K[1] : nullptr;
+      if (hyper) k_rk_mac<true><<<grd, blk, 0, st>>>(a);
+      else k_rk_mac<false><<<grd, blk, 0, st>>>(a);
+      in_u = a.uout;
+      in_v = a.vout;
+    }
+  }
+  return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+}
+
+}  // namespace aj

@@ -1,0 +1,294 @@
+// Projection: divergence of the predicted velocity -> pressure right-hand side,
+// and the pressure-gradient correction with the interface projection, the
+// boundary conditions and the hard mask.  Also the obstacle geometry set-up.
+//
+// Collocated PURE  : solver/pure_functions/step.py:182-199 and :259-397
+// Collocated GUI   : solver/simulation/step_handlers.py:92-98 and :128-185
+// MAC GUI          : solver/simulation/step_handlers.py:218-224 and :238-293
+// Boundary conditions are fused by evaluating the corrected velocity at the
+// cell each boundary copies from, so the kernel writes every cell exactly once.
+#include "aj_internal.cuh"
+#include <math.h>
+
+namespace aj {
+
+// ------------------------------------------------------------------ rhs
+// writes the multigrid right-hand side b directly:
+//   collocated: div = central difference on the interior, 0 on the ring
+//               (solver/operators.py:81-96); PURE rhs = div*mask/dt, GUI div/dt
+//   MAC:        div = face differences (solver/operators_mac.py:73-80),
+//               rhs = div/dt, b = rhs*mask (multigrid_solver_mac.py:78)
+//   von Karman: b[-1, :] = 0 (multigrid_solver.py:75-77)
+__global__ void __launch_bounds__(256) k_rhs(const float* __restrict__ us,
+                                             const float* __restrict__ vs,
+                                             const float* __restrict__ mask,
+                                             float* __restrict__ b, int nx, int ny, float h2x,
+                                             float h2y, float idx, float idy, int mac, int pure,
+                                             int outlet, const DevScalars* sc) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= nx || j >= ny) return;
+  const float dt = sc->dt;
+  long k = (long)i * ny + j;
+  float out;
+  if (mac) {
+    float du = (ldg(us + (long)(i + 1) * ny + j) - ldg(us + (long)i * ny + j)) * idx;
+    float dv = (ldg(vs + (long)i * (ny + 1) + j + 1) - ldg(vs + (long)i * (ny + 1) + j)) * idy;
+    out = ((du + dv) / dt) * ldg(mask + k);
+  } else {
+    float div = 0.f;
+    if (i > 0 && i < nx - 1 && j > 0 && j < ny - 1)
+      div = (ldg(us + (long)(i + 1) * ny + j) - ldg(us + (long)(i - 1) * ny + j)) * h2x +
+            (ldg(vs + (long)i * ny + j + 1) - ldg(vs + (long)i * ny + j - 1)) * h2y;
+    out = pure ? (div * ldg(mask + k)) / dt : div / dt;
+  }
+  if (outlet && i == nx - 1) out = 0.f;
+  b[k] = out;
+}
+
+int launch_rhs(const AjStepParams& p, const Layout& L, void* ws, const float* us,
+               const float* vs, const float* mask, float* b, cudaStream_t st) {
+  dim3 blk(32, 8), grd(cdiv(p.ny, 32), cdiv(p.nx, 8));
+  k_rhs<<<grd, blk, 0, st>>>(us, vs, mask, b, p.nx, p.ny, (float)(1.0 / (2.0 * p.dx)),
+                             (float)(1.0 / (2.0 * p.dy)), (float)(1.0 / p.dx),
+                             (float)(1.0 / p.dy), p.grid_type == AJ_GRID_MAC,
+                             p.variant == AJ_VARIANT_PURE, p.flow_type == AJ_FLOW_VON_KARMAN,
+                             at<DevScalars>(ws, 0));
+  return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+}
+
+// ------------------------------------------------------------------ correction
+struct Corr {
+  const float *us, *vs, *p, *mask;
+  float *uo, *vo;
+  const DevScalars* sc;
+  int nx, ny, variant, flow;
+  float idx, idy, h2x, h2y, thresh, U;
+};
+
+// non-periodic gradient: central interior, one-sided edges (operators.py:17-56)
+__device__ __forceinline__ float gnx(const float* __restrict__ f, int a, int b, int nx, int ny,
+                                     float idx, float h2x) {
+  if (a == 0) return (ldg(f + (long)ny + b) - ldg(f + b)) * idx;
+  if (a == nx - 1) return (ldg(f + (long)(nx - 1) * ny + b) - ldg(f + (long)(nx - 2) * ny + b)) * idx;
+  return (ldg(f + (long)(a + 1) * ny + b) - ldg(f + (long)(a - 1) * ny + b)) * h2x;
+}
+__device__ __forceinline__ float gny(const float* __restrict__ f, int a, int b, int nx, int ny,
+                                     float idy, float h2y) {
+  const float* r = f + (long)a * ny;
+  if (b == 0) return (ldg(r + 1) - ldg(r)) * idy;
+  if (b == ny - 1) return (ldg(r + ny - 1) - ldg(r + ny - 2)) * idy;
+  return (ldg(r + b + 1) - ldg(r + b - 1)) * h2y;
+}
+
+// corrected velocity at (a, b) before the boundary conditions (COMP 0 = u)
+template <int COMP>
+__device__ __forceinline__ float w_pure(const Corr& c, int a, int b, float dt) {
+  long k = (long)a * c.ny + b;
+  if (!(ldg(c.mask + k) > 0.5f)) return 0.f;                      // step.py:348-349
+  float dpx = gnx(c.p, a, b, c.nx, c.ny, c.idx, c.h2x);
+  float dpy = gny(c.p, a, b, c.nx, c.ny, c.idy, c.h2y);
+  float dmx = gnx(c.mask, a, b, c.nx, c.ny, c.idx, c.h2x);
+  float dmy = gny(c.mask, a, b, c.nx, c.ny, c.idy, c.h2y);
+  float gm = sqrtf(dmx * dmx + dmy * dmy);
+  if (gm > c.thresh) {                                             // step.py:313-335
+    float nxv = dmx / (gm + 1e-8f), nyv = dmy / (gm + 1e-8f);
+    float dn = dpx * nxv + dpy * nyv;
+    dpx = dpx - dn * nxv;
+    dpy = dpy - dn * nyv;
+  }
+  if (a == 0) dpx = 0.f;                                           // step.py:341
+  return COMP == 0 ? ldg(c.us + k) - dt * dpx : ldg(c.vs + k) - dt * dpy;
+}
+
+template <int COMP>
+__device__ __forceinline__ float w_gui(const Corr& c, int a, int b, float dt) {
+  long k = (long)a * c.ny + b;
+  if (COMP == 0) {
+    float dpx = a == 0 ? 0.f : gnx(c.p, a, b, c.nx, c.ny, c.idx, c.h2x);   // :134-135
+    return ldg(c.us + k) - dt * dpx;
+  }
+  return ldg(c.vs + k) - dt * gny(c.p, a, b, c.nx, c.ny, c.idy, c.h2y);
+}
+
+__global__ void __launch_bounds__(256) k_correct_col(Corr c) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  const int nx = c.nx, ny = c.ny;
+  if (i >= nx || j >= ny) return;
+  long k = (long)i * ny + j;
+  const float dt = c.sc->dt_corr;
+  float uo, vo;
+  int ai = (i == nx - 1) ? nx - 2 : i;
+  if (c.variant == AJ_VARIANT_PURE) {
+    // BC of step.py:365-377, then the hard mask at (i, j) (:396-397)
+    int bj = j == 0 ? 1 : (j == ny - 1 ? ny - 2 : j);
+    uo = (i == 0) ? c.U : w_pure<0>(c, ai, bj, dt);
+    vo = (i == 0 || j == 0 || j == ny - 1) ? 0.f : w_pure<1>(c, ai, j, dt);
+  } else {
+    // BC of step_handlers.py:143-161 (inlet excludes the corners, no-slip walls)
+    if (j == 0 || j == ny - 1) uo = 0.f;
+    else uo = (i == 0) ? c.U : w_gui<0>(c, ai, j, dt);
+    vo = (i == 0 || j == 0 || j == ny - 1) ? 0.f : w_gui<1>(c, ai, j, dt);
+  }
+  bool m = ldg(c.mask + k) > 0.5f;                                 // step_handlers.py:182-183
+  c.uo[k] = m ? uo : 0.f;
+  c.vo[k] = m ? vo : 0.f;
+}
+
+// MAC GUI correction: staggered gradients (operators_mac.py:40-55; the face
+// gradient on the boundary faces is 0), BC of step_handlers.py:256-274
+__global__ void __launch_bounds__(256) k_correct_mac(Corr c) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  const int nx = c.nx, ny = c.ny;
+  const float dt = c.sc->dt_corr;
+  if (i <= nx && j < ny) {
+    float o;
+    if (j == 0 || j == ny - 1) o = 0.f;
+    else if (i == 0) o = c.U;
+    else {
+      int a = i == nx ? nx - 1 : i;
+      float dpx = (ldg(c.p + (long)clampi(a, nx) * ny + j) - ldg(c.p + (long)clampi(a - 1, nx) * ny + j)) * c.idx;
+      o = ldg(c.us + (long)a * ny + j) - dt * dpx;
+    }
+    c.uo[(long)i * ny + j] = o;
+  }
+  if (i < nx && j <= ny) {
+    float o;
+    if (i == 0 || j == 0 || j == ny) o = 0.f;
+    else {
+      int a = i == nx - 1 ? nx - 2 : i;
+      float dpy = (ldg(c.p + (long)a * ny + clampi(j, ny)) - ldg(c.p + (long)a * ny + clampi(j - 1, ny))) * c.idy;
+      o = ldg(c.vs + (long)a * (ny + 1) + j) - dt * dpy;
+    }
+    c.vo[(long)i * (ny + 1) + j] = o;
+  }
+}
+
+int launch_correct(const AjStepParams& p, const Layout& L, void* ws, const float* us,
+                   const float* vs, const float* pr, const float* mask, float* uo, float* vo,
+                   cudaStream_t st) {
+  Corr c{};
+  c.us = us;
+  c.vs = vs;
+  c.p = pr;
+  c.mask = mask;
+  c.uo = uo;
+  c.vo = vo;
+  c.sc = at<DevScalars>(ws, 0);
+  c.nx = p.nx;
+  c.ny = p.ny;
+  c.variant = p.variant;
+  c.flow = p.flow_type;
+  c.idx = (float)(1.0 / p.dx);
+  c.idy = (float)(1.0 / p.dy);
+  c.h2x = (float)(1.0 / (2.0 * p.dx));
+  c.h2y = (float)(1.0 / (2.0 * p.dy));
+  c.thresh = (float)(0.1 / p.dx);
+  c.U = (float)p.U_inf;
+  dim3 blk(32, 8);
+  if (p.grid_type == AJ_GRID_MAC) {
+    dim3 grd(cdiv(p.ny + 1, 32), cdiv(p.nx + 1, 8));
+    k_correct_mac<<<grd, blk, 0, st>>>(c);
+  } else {
+    dim3 grd(cdiv(p.ny, 32), cdiv(p.nx, 8));
+    k_correct_col<<<grd, blk, 0, st>>>(c);
+  }
+  return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+}
+
+// ------------------------------------------------------------------ geometry
+struct Geo {
+  int kind;
+  double g[8];
+};
+
+__device__ double sdf_at(const Geo& G, double X, double Y) {
+  switch (G.kind) {
+    case AJ_GEOM_CYLINDER:                                   // mask_generator.py:151-153
+      return sqrt((X - G.g[0]) * (X - G.g[0]) + (Y - G.g[1]) * (Y - G.g[1])) - G.g[2];
+    case AJ_GEOM_CYL3_ROW: {                                 // cylinder_array.py:8-42
+      double r = G.g[2] / 2.0, best = 1e300;
+      for (int q = 0; q < 3; ++q) {
+        double cx = G.g[0] + q * G.g[3];
+        double d = sqrt((X - cx) * (X - cx) + (Y - G.g[1]) * (Y - G.g[1])) - r;
+        best = q == 0 ? d : fmin(best, d);
+      }
+      return best;
+    }
+    case AJ_GEOM_CYL3_TRI: {                                 // equilateral triangle, apex upstream
+      double r = G.g[2] / 2.0, s = G.g[3], R = s / sqrt(3.0);
+      double px[3] = {G.g[0] - R, G.g[0] + 0.5 * R, G.g[0] + 0.5 * R};
+      double py[3] = {G.g[1], G.g[1] + 0.5 * s, G.g[1] - 0.5 * s};
+      double best = 1e300;
+      for (int q = 0; q < 3; ++q) {
+        double d = sqrt((X - px[q]) * (X - px[q]) + (Y - py[q]) * (Y - py[q])) - r;
+        best = q == 0 ? d : fmin(best, d);
+      }
+      return best;
+    }
+    case AJ_GEOM_NACA4: {                                    // naca_airfoils.py:109-178
+      double chord = G.g[0], aoa = G.g[1] * (M_PI / 180.0), x0 = G.g[2], y0 = G.g[3];
+      double m = G.g[4], pp = G.g[5], t = G.g[6];
+      double Xl = X - x0, Yl = Y - y0;
+      double Xr = Xl * cos(aoa) - Yl * sin(aoa);
+      double Yr = Xl * sin(aoa) + Yl * cos(aoa);
+      double xn = Xr / chord, yn = Yr / chord;
+      bool inc = xn >= 0.0 && xn <= 1.0;
+      double xs = fmin(fmax(xn, 0.0), 1.0);
+      double yt = 5.0 * t * (0.2969 * sqrt(fabs(xs)) - 0.1260 * xs - 0.3516 * xs * xs +
+                             0.2843 * xs * xs * xs - 0.1015 * xs * xs * xs * xs);
+      double yc, dyc;
+      if (xn <= pp) {
+        yc = m / (pp * pp) * (2.0 * pp * xn - xn * xn);
+        dyc = 2.0 * m / (pp * pp) * (pp - xn);
+      } else {
+        yc = m / ((1.0 - pp) * (1.0 - pp)) * ((1.0 - 2.0 * pp) + 2.0 * pp * xn - xn * xn);
+        dyc = 2.0 * m / ((1.0 - pp) * (1.0 - pp)) * (pp - xn);
+      }
+      double th = atan(dyc);
+      double yu = yc + yt * cos(th), yl = yc - yt * cos(th);
+      double ds = fmin(fabs(yn - yu) * chord, fabs(yn - yl) * chord);
+      double dle = sqrt(Xr * Xr + Yr * Yr);
+      double dte = sqrt((Xr - chord) * (Xr - chord) + Yr * Yr);
+      double dist = inc ? ds : fmin(dle, dte);
+      bool inside = inc && (yn >= yl - 0.01) && (yn <= yu + 0.01);
+      return inside ? -dist : dist;
+    }
+    default:
+      return 1e30;
+  }
+}
+
+__global__ void k_geometry(Geo G, int nx, int ny, double sx, double sy, double inv_eps,
+                           float* __restrict__ mask, float* __restrict__ sdf) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= nx || j >= ny) return;
+  double X = i * sx, Y = j * sy;                             // linspace(0, l, n)
+  double s = sdf_at(G, X, Y);
+  double x = -s * inv_eps;                                   // mask = 1 - sigmoid(-sdf/eps)
+  double chi = x >= 0.0 ? 1.0 / (1.0 + exp(-x)) : exp(x) / (1.0 + exp(x));
+  long k = (long)i * ny + j;
+  if (mask) mask[k] = (float)(1.0 - chi);
+  if (sdf) sdf[k] = (float)s;
+}
+
+}  // namespace aj
+
+extern "C" int32_t aj_geometry(int32_t nx, int32_t ny, double lx, double ly, int32_t kind,
+                               const double* geo_host, double eps, float* mask, float* sdf,
+                               void* stream) {
+  using namespace aj;
+  if (nx < 2 || ny < 2 || eps <= 0.0) return AJ_ERR_PARAM;
+  Geo G{};
+  G.kind = kind;
+  int ng = kind == AJ_GEOM_NACA4 ? 7 : (kind == AJ_GEOM_CYLINDER ? 3 : 4);
+  if (kind < AJ_GEOM_CYLINDER || kind > AJ_GEOM_CYL3_TRI || !geo_host) return AJ_ERR_PARAM;
+  for (int q = 0; q < ng; ++q) G.g[q] = geo_host[q];
+  dim3 blk(32, 8), grd(cdiv(ny, 32), cdiv(nx, 8));
+  k_geometry<<<grd, blk, 0, (cudaStream_t)stream>>>(G, nx, ny, lx / (nx - 1), ly / (ny - 1),
+                                                     1.0 / eps, mask, sdf);
+  return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+}

@@ -1,0 +1,386 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 projection step on the NACA 0012 MAC workload.
+
+Workload (the metric's configuration): MAC grid 2048x512, NACA 0012 at 10 deg
+(chord 256 cells, leading edge at cell (400, 256)), Re = 1000, Smagorinsky LES
+C_s = 0.17, dt from CFL 0.5 on the device, pressure solved to a 1e-6 relative
+residual (FP64 norm) by the converging multigrid.  One "step" is one full
+projection step (LES, RK3 predictor, divergence, pressure solve, correction,
+boundary conditions).
+
+Arms on the GPU (all through aj_step, whole step captured in one CUDA graph):
+  method   pressure warm-started from the previous step's pressure
+  plain    the plain GPU multigrid step: zero initial guess, same tolerance
+value = cell-steps/s of `method`; the plain arm is reported next to it.
+
+`python bench.py --impl reference` times the reference algorithm's CPU path
+(the NumPy port of the reference GUI step, float32, 5 reference V-cycles) on
+the host cores.  The reference itself is JAX and cannot be installed here.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mcell-steps/s at 2048×512 FP32, NN-warm-start+MG vs plain MG at equal div tol"
+UNIT = "Mcell-steps/s"
+FLUSH_BYTES = 256 << 20          # larger than the 126 MB L2
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nx", type=int, default=2048)
+    ap.add_argument("--ny", type=int, default=512)
+    ap.add_argument("--cpu-sample-steps", type=int, default=20)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi sampled every 200 ms during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.idx)], stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+# ------------------------------------------------------------------ CPU arm
+def cpu_step_fn(nx, ny):
+    """The reference algorithm on the host: NumPy float32 port of the GUI MAC
+    step with the reference multigrid (5 V-cycles, the GUI default)."""
+    import numpy as np
+    from oracle import ref_np as R
+    lx, ly = 32.0 * nx / 2048, 8.0 * ny / 512
+    dx, dy = lx / nx, ly / ny
+    X, Y = R.grid_coords(nx, ny, lx, ly)
+    chord = 256 * dx * nx / 2048
+    xle, yle = (400 * nx // 2048) * lx / (nx - 1), (ny // 2) * ly / (ny - 1)
+    sdf = R.sdf_naca4(X, Y, chord, 10.0, xle, yle, 0.0, 0.0, 0.12)
+    f = np.float32
+    mask = R.mask_from_sdf(sdf, 0.05 * dx).astype(f)
+    rng = np.random.default_rng(0)
+    u = (1.0 + 1e-3 * rng.standard_normal((nx + 1, ny))).astype(f)
+    v = np.zeros((nx, ny + 1), f)
+    nu = chord / 1000.0
+
+    def step(u, v):
+        dt = f(R.compute_cfl_timestep(u, v, dx, dy, nu, 0.5, 1e-6, 1.0))
+        return R.step_gui(u, v, mask, dt, sdf=None, dx=f(dx), dy=f(dy), nu=f(nu), U_inf=f(1.0),
+                          grid_type="mac", use_les=True, les_model="smagorinsky",
+                          smagorinsky_constant=f(0.17), brinkman_eta=f(1e-4), v_cycles=5)
+    return step, u, v
+
+
+def run_cpu(nx, ny, steps, warmup):
+    step, u, v = cpu_step_fn(nx, ny)
+    for _ in range(warmup):
+        u, v, _ = step(u, v)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        u, v, _ = step(u, v)
+    el = time.perf_counter() - t0
+    return nx * ny * steps / el / 1e6, el
+
+
+def reference_arm(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    steps, warm = max(1, args.steps), max(0, args.warmup)
+    val, el = run_cpu(args.nx, args.ny, steps, warm)
+    sample = (f"{steps} full {args.nx}x{args.ny} MAC steps after {warm} warm-up steps, "
+              "NumPy float32 port of the reference GUI step (5 reference V-cycles)")
+    print(json.dumps({
+        "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
+        "warmup": warm, "ms_per_step": el / steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "impl": "reference",
+        "data": "synthetic (seeded NACA 0012 flow)",
+        "config": {"workload": f"naca0012_{args.nx}x{args.ny}_mac_re1000_les",
+                   "solver": "reference multigrid, 5 V-cycles (the GUI default)"},
+        "cpu_baseline": {"value": val, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
+        "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+# ------------------------------------------------------------------ GPU arm
+def gpu_arm(args):
+    import torch
+    import aerojax_gb300 as aj
+    from aerojax_gb300 import _lib, configs
+    from aerojax_gb300.build import build
+
+    world, rank, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", rank=rank, world_size=world)
+    torch.cuda.set_device(local)
+    build()
+    dev = torch.device("cuda", local)
+    L = _lib.lib()
+
+    case = configs.naca_mac_2048x512(device=dev, nx=args.nx, ny=args.ny, mg_mode="converge",
+                                     seed=rank)
+    cells = args.nx * args.ny
+    mask = case["mask"]
+    flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=dev)
+
+    def make_arm(warm):
+        from dataclasses import replace
+        cfg = replace(case["cfg"], warm_start=warm)
+        plan = aj.get_plan(cfg, dev)
+        plan.prepare(mask)
+        bufs = [(case["u"].clone(), case["v"].clone(), torch.zeros((args.nx, args.ny), device=dev))
+                for _ in range(2)]
+        return plan, bufs
+
+    def run(plan, bufs, k, timed, warm):
+        """k steps, ping-ponging two state buffers; per-step CUDA events."""
+        st = torch.cuda.current_stream()
+        times, cycles = [], []
+        cur = 0
+        for _ in range(k):
+            src, dst = bufs[cur], bufs[1 - cur]
+            flush.zero_()                               # evict the working set from L2
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            aj.run_step(plan, src[0], src[1], mask, p_guess=src[2] if warm else None, out=dst)
+            e1.record(st)
+            times.append((e0, e1))
+            cur = 1 - cur
+            if timed:
+                cycles.append(plan.stats_buf.clone())
+        torch.cuda.synchronize()
+        ms = sum(a.elapsed_time(b) for a, b in times)
+        cyc = []
+        for s in cycles:
+            raw = _lib.AjStats.from_buffer_copy(bytes(s.cpu().numpy().tobytes()))
+            cyc.append((raw.cycles, raw.rel_residual, raw.err))
+        return ms, cyc
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(x):
+        if world > 1:
+            import torch.distributed as dist
+            t = torch.tensor([x], device=dev, dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            return float(t.item())
+        return x
+
+    results = {}
+    clocks = ClockSampler(local)
+    for name, warm in (("plain", False), ("method", True)):
+        plan, bufs = make_arm(warm)
+        run(plan, bufs, max(3, args.warmup), False, warm)
+        barrier()
+        if name == "method":
+            clocks.start()
+        ms, cyc = run(plan, bufs, args.steps, True, warm)
+        if name == "method":
+            clk = clocks.stop()
+        barrier()
+        ms = max_over_ranks(ms)
+        results[name] = dict(ms=ms, cycles=cyc, plan=plan, bufs=bufs)
+
+    meth = results["method"]
+    ms_step = meth["ms"] / args.steps
+    value = world * cells / (ms_step * 1e-3) / 1e6
+    plain_ms = results["plain"]["ms"] / args.steps
+    plain_value = world * cells / (plain_ms * 1e-3) / 1e6
+    cyc_m = [c[0] for c in meth["cycles"]]
+    cyc_p = [c[0] for c in results["plain"]["cycles"]]
+    rel_m = max(c[1] for c in meth["cycles"])
+    rel_p = max(c[1] for c in results["plain"]["cycles"])
+    errs = sorted({c[2] for c in meth["cycles"] + results["plain"]["cycles"]})
+    plan = meth["plan"]
+    launches = sum(int(L.aj_kernel_count(ctypes.byref(plan.params), c)) for c in cyc_m)
+
+    # ---- e2e: host buffers, H2D of the step's inputs, D2H of its result
+    nxu, nyv = (args.nx + 1) * args.ny, args.nx * (args.ny + 1)
+    pin = lambda t: t.detach().cpu().pin_memory()
+    h_in = [pin(meth["bufs"][0][0]), pin(meth["bufs"][0][1]), pin(meth["bufs"][0][2])]
+    h_out = [torch.empty_like(h_in[0]).pin_memory(), torch.empty_like(h_in[1]).pin_memory(),
+             torch.empty_like(h_in[2]).pin_memory()]
+    d_in = [t.clone() for t in meth["bufs"][0]]
+    d_out = [t.clone() for t in meth["bufs"][1]]
+    st = torch.cuda.current_stream()
+
+    def e2e_steps(k):
+        ev = []
+        for _ in range(k):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            for d, h in zip(d_in, h_in):
+                d.copy_(h, non_blocking=True)
+            aj.run_step(plan, d_in[0], d_in[1], mask, p_guess=d_in[2], out=tuple(d_out))
+            for h, d in zip(h_out, d_out):
+                h.copy_(d, non_blocking=True)
+            e1.record(st)
+            ev.append((e0, e1))
+            torch.cuda.synchronize()                 # the host owns the result now
+            for a, b in zip(h_in, h_out):
+                a.copy_(b)
+        return sum(a.elapsed_time(b) for a, b in ev)
+    e2e_steps(3)
+    barrier()
+    e2e_ms = max_over_ranks(e2e_steps(args.steps)) / args.steps
+    e2e_val = world * cells / (e2e_ms * 1e-3) / 1e6
+    h2d = 4 * (nxu + nyv + cells)
+    d2h = 4 * (nxu + nyv + cells)
+
+    # ---- roofline: the dominant kernel timed alone (events on the launch stream)
+    roof = roofline(args, plan, meth["bufs"][0], mask, flush, L)
+
+    if rank != 0:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
+    cpu = None
+    if not args.no_cpu_baseline:
+        n = args.cpu_sample_steps
+        cval, cel = run_cpu(args.nx, args.ny, n, 1)
+        cpu = {"value": cval, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"{n} full {args.nx}x{args.ny} MAC steps ({cel:.1f} s), NumPy float32 "
+                         "port of the reference GUI step with 5 reference V-cycles"}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded NACA 0012 flow; the solver generates every step)",
+        "config": {
+            "workload": case["name"], "nx": args.nx, "ny": args.ny, "grid": "mac",
+            "method": "converging MG (FP32 red-black V-cycles, FP64 refinement, coarsest and "
+                      "norms) warm-started from the previous pressure; NN warm start not built yet",
+            "rel_residual_target": 1e-6, "rel_residual_max": rel_m,
+            "mg_cycles_mean": statistics.mean(cyc_m) if cyc_m else None,
+            "plain_mg_value": plain_value, "plain_mg_ms_per_step": plain_ms,
+            "plain_mg_cycles_mean": statistics.mean(cyc_p) if cyc_p else None,
+            "plain_rel_residual_max": rel_p, "device_errors": errs,
+            "speedup_vs_plain": value / plain_value,
+            "l2": "flushed before every step (256 MiB write outside the timed events)",
+            "parallelism": "replicas only" if world > 1 else "single GPU",
+        },
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "clocks": clk,
+    }
+    print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def roofline(args, plan, state, mask, flush, L):
+    """Times the converging level-0 prolongation/smoothing/update kernel alone:
+    per launch it reads r (4 B), e (4 B), the coarse correction (1 B) and
+    reads and writes the FP64 pressure (16 B): 25 algorithmic bytes per cell."""
+    import torch
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peak, src = 6800.0, "fallback"
+    if os.path.exists(peaks_path):
+        with open(peaks_path) as f:
+            peak, src = float(json.load(f)["hbm_gbs"]), "measured"
+    st = torch.cuda.current_stream()
+    which, bpc = 1, 25
+    times = []
+    for k in range(13):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        rc = L.aj_profile_kernel(ctypes.byref(plan.params), which, state[0].data_ptr(),
+                                 state[1].data_ptr(), mask.data_ptr(), plan.ws.data_ptr(),
+                                 plan.nbytes, st.cuda_stream)
+        e1.record(st)
+        if rc:
+            return None
+        if k >= 3:
+            times.append((e0, e1))
+    torch.cuda.synchronize()
+    dur = statistics.mean(a.elapsed_time(b) for a, b in times) * 1e-3
+    algo = bpc * args.nx * args.ny
+    achieved = algo / dur / 1e9
+    return {"kernel": "k_cv_up (level 0: prolongation + 2 red-black sweeps + FP64 update)",
+            "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": src, "traffic": None,
+            "algorithmic_bytes_per_launch": algo, "launch_us": dur * 1e6}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

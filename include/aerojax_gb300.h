@@ -1,0 +1,195 @@
+/*
+ * aerojax_gb300 — C ABI of the GB300 (sm_103a) projection-step library.
+ *
+ * The library replaces the hot path of AeroJAX's incompressible projection
+ * step.  Each entry point below names the reference function it stands in for
+ * (paths are relative to the AeroJAX project root).
+ *
+ * Conventions shared by every entry point
+ *  - 2-D fields are float32, C order, indexed [i][j] with x on the first axis
+ *    and y contiguous (solver/params.py:56, meshgrid indexing='ij').
+ *    Collocated: u, v, p are nx*ny.  MAC: u is (nx+1)*ny, v is nx*(ny+1),
+ *    p is nx*ny (solver/params.py:16-18).
+ *  - All pointers are device pointers unless stated otherwise.  The caller
+ *    owns every buffer; the library never allocates.  Scratch memory comes
+ *    from a caller-allocated workspace sized by aj_workspace_size().
+ *  - Work is enqueued on the given stream; nothing synchronises the host.
+ *    aj_step / aj_poisson_mg issue no host reads and no allocation, so they
+ *    can be captured in a CUDA graph after aj_prepare has run.
+ *  - Return value: AJ_OK or an AjStatus error code (argument checks happen
+ *    on the host before anything is enqueued).  Errors detected on the device
+ *    (non-finite values, non-convergence in converging mode) are written to
+ *    AjStats::err, read back asynchronously by the caller.
+ */
+#ifndef AEROJAX_GB300_H
+#define AEROJAX_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  AJ_OK = 0,
+  AJ_ERR_SHAPE = 1,         /* grid not divisible for multigrid: the reference's ValueError
+                               (pressure_solvers/multigrid_solver.py:104-106)            */
+  AJ_ERR_PARAM = 2,         /* unsupported option / bad scalar                           */
+  AJ_ERR_NONFINITE = 3,     /* NaN/Inf seen in the pressure residual (device-side)       */
+  AJ_ERR_NOT_CONVERGED = 4, /* converging mode hit max_cycles above rtol (device-side)   */
+  AJ_ERR_TIMEOUT = 5,       /* a bounded device-side wait gave up                        */
+  AJ_ERR_CUDA = 6,          /* a CUDA launch failed                                      */
+  AJ_ERR_WORKSPACE = 7      /* workspace too small or null                               */
+} AjStatus;
+
+enum { AJ_GRID_COLLOCATED = 0, AJ_GRID_MAC = 1 };
+enum { AJ_FLOW_VON_KARMAN = 0, AJ_FLOW_LID_DRIVEN_CAVITY = 1, AJ_FLOW_TAYLOR_GREEN = 2 };
+/* PURE = step_pure (solver/pure_functions/step.py:49-467);
+   GUI  = BaselineSolver._step (solver/simulation/step_handlers.py:62-301). */
+enum { AJ_VARIANT_PURE = 0, AJ_VARIANT_GUI = 1 };
+enum { AJ_LES_NONE = 0, AJ_LES_SMAGORINSKY = 1, AJ_LES_DYNAMIC = 2 };
+enum { AJ_ADV_UPWIND = 0, AJ_ADV_WENO5 = 1 };
+/* PARITY   = the reference V-cycle, fixed v_cycles, absolute early exit;
+   CONVERGE = red-black Gauss-Seidel V-cycles inside FP64 iterative
+              refinement, FP64 coarsest solve and norms, relative stop. */
+enum { AJ_MG_PARITY = 0, AJ_MG_CONVERGE = 1 };
+
+/* Every scalar and static option of one step.  Mirrors the keyword arguments
+   of step_pure (solver/pure_functions/step.py:50-66) plus the attributes the
+   GUI step reads from BaselineSolver (step_handlers.py:64-90). */
+typedef struct {
+  int32_t nx, ny;                /* cell counts (p shape)                             */
+  int32_t grid_type;             /* AJ_GRID_*                                         */
+  int32_t flow_type;             /* AJ_FLOW_*  (von_karman is the configs' flow)      */
+  int32_t variant;               /* AJ_VARIANT_*                                      */
+  int32_t les_model;             /* AJ_LES_*                                          */
+  int32_t advection;             /* AJ_ADV_*                                          */
+  int32_t mg_mode;               /* AJ_MG_*                                           */
+  int32_t fast_mode;             /* 1 = Heun RK2, 0 = RK3 (rk3_simple_new.py:356)     */
+  int32_t slip_walls;            /* 1 = slip walls inside the predictor               */
+  int32_t v_cycles;              /* parity mode: V-cycles per solve                   */
+  int32_t levels;                /* parity mode: multigrid levels (reference: 4)      */
+  int32_t max_cycles;            /* converging mode: cap on refinement cycles         */
+  int32_t has_sdf;               /* collocated: chi from sdf (rk3_simple_new.py:194)  */
+  int32_t cfl_dt;                /* 1 = dt from the CFL rule on the device each step  */
+  int32_t warm_start;            /* converging mode: start from p_guess               */
+  double dx, dy;
+  double dt;                     /* used when cfl_dt == 0                             */
+  double dt_correction;          /* GUI: trace-time self.dt (step_handlers.py:139);
+                                    <= 0 means "same as dt"                           */
+  double nu, U_inf, brinkman_eta;
+  double smagorinsky_constant;
+  double nu_hyper_ratio;         /* GUI only; step_pure hard-wires 0 (step.py:178)    */
+  double mg_tolerance;           /* parity: absolute early-exit tol (default 1e-6)    */
+  double mg_rtol;                /* converging: relative residual target (1e-6)       */
+  double cfl_target, dt_min, dt_max;  /* timestepping/cfl_adaptive_dt.py:6-71       */
+  double les_delta;              /* LES filter width; <= 0 means sqrt(dx*dy)
+                                    (step_handlers.py:71)                              */
+} AjStepParams;
+
+/* Device-resident per-call statistics (written by the last kernels of a call). */
+typedef struct {
+  int32_t cycles;        /* V-cycles executed                                      */
+  int32_t converged;     /* parity: absolute test met; converging: rtol met        */
+  int32_t err;           /* AJ_OK or a device-side AjStatus                        */
+  int32_t pad;
+  double rel_residual;   /* ||b - A p||_2 / ||b||_2 (FP64) after the solve         */
+  double rhs_norm;       /* ||b||_2 (FP64)                                         */
+  double dt;             /* dt the step used                                       */
+  double abs_residual_sq;/* sum r^2 * dx * dy (the reference's early-exit quantity)*/
+} AjStats;
+
+/* Library version, e.g. 100 for 0.1.0. */
+int32_t aj_version(void);
+
+/* Bytes of device workspace needed for the given parameters (0 on bad params). */
+size_t aj_workspace_size(const AjStepParams* prm);
+
+/* Validates parameters the way the reference would at trace time.
+   Returns AJ_OK, AJ_ERR_SHAPE (multigrid_solver.py:96-106) or AJ_ERR_PARAM. */
+int32_t aj_check_params(const AjStepParams* prm);
+
+/* Per-geometry set-up: Brinkman chi (rk3_simple_new.py:194-200), face masks,
+   multigrid mask pyramid (multigrid_solver_mac.py:213-214), converging-mode
+   coarse-grid inverse.  Must run again when the mask, sdf, grid or solver
+   options change.  mask: nx*ny; sdf: nx*ny or NULL.  Synchronous. */
+int32_t aj_prepare(const AjStepParams* prm, const float* mask, const float* sdf,
+                   void* workspace, size_t workspace_bytes, void* stream);
+
+/* One projection step.  Replaces step_pure (solver/pure_functions/step.py:49-467)
+   for variant PURE and BaselineSolver._step (step_handlers.py:296-301) for
+   variant GUI.  u_out/v_out/p_out must not alias the inputs; p_guess (nx*ny,
+   nullable) seeds converging mode when warm_start is set. stats: device ptr or
+   NULL. */
+int32_t aj_step(const AjStepParams* prm, const float* u, const float* v, const float* mask,
+                const float* p_guess, float* u_out, float* v_out, float* p_out,
+                void* workspace, size_t workspace_bytes, AjStats* stats, void* stream);
+
+/* The pressure solve alone.  Replaces poisson_multigrid
+   (pressure_solvers/multigrid_solver.py:55-241) for grid_type COLLOCATED and
+   poisson_multigrid_mac (pressure_solvers/multigrid_solver_mac.py:59-246) for
+   grid_type MAC.  rhs, mask, p: nx*ny.  p0 nullable (zero guess). */
+int32_t aj_poisson_mg(const AjStepParams* prm, const float* rhs, const float* mask,
+                      const float* p0, float* p, void* workspace, size_t workspace_bytes,
+                      AjStats* stats, void* stream);
+
+/* Smagorinsky eddy viscosity.  Replaces constant_smagorinsky
+   (solver/les_models.py:179-200) and dynamic_smagorinsky (:79-176) on
+   collocated inputs (nx*ny).  model: AJ_LES_SMAGORINSKY or AJ_LES_DYNAMIC.
+   cd_out nullable.  Dynamic needs a workspace of aj_workspace_size() with
+   les_model = AJ_LES_DYNAMIC. */
+int32_t aj_les(const AjStepParams* prm, int32_t model, const float* u, const float* v,
+               float* nu_sgs, float* cd_out, void* workspace, size_t workspace_bytes,
+               void* stream);
+
+/* RK3/RK2 predictor with Brinkman penalisation.  Replaces rk_step_unified
+   (advection_schemes/rk3_simple_new.py:175-358) for COLLOCATED and
+   rk_step_unified_mac (advection_schemes/rk3_mac.py:220-504) for MAC.
+   nu_sgs nullable; `double_count` = 1 reproduces the GUI collocated call that
+   passes nu + nu_sgs as nu (step_handlers.py:76,84-85). Needs aj_prepare. */
+int32_t aj_predictor(const AjStepParams* prm, const float* u, const float* v,
+                     const float* mask, const float* nu_sgs, int32_t double_count,
+                     float* u_star, float* v_star, void* workspace, size_t workspace_bytes,
+                     void* stream);
+
+/* CFL time step on the device.  Replaces compute_cfl_timestep
+   (timestepping/cfl_adaptive_dt.py:6-71).  dt_out: one float (device). */
+int32_t aj_cfl_dt(const AjStepParams* prm, const float* u, const float* v, float* dt_out,
+                  void* workspace, size_t workspace_bytes, void* stream);
+
+/* Obstacle geometry: SDF and mask = 1 - sigmoid(-sdf/eps)
+   (solver/simulation/mask_generator.py:10-160, obstacles/naca_airfoils.py:109-178,
+   obstacles/cylinder_array.py:8-42).  Coordinates are linspace(0, lx, nx) x
+   linspace(0, ly, ny) (solver/params.py:51-56).  kind: AJ_GEOM_*.  geo[]:
+     CYLINDER : cx, cy, r
+     NACA4    : chord, aoa_deg, x_le, y_le, m, p, t
+     CYL3_ROW : cx, cy, diameter, spacing          (three in a row along x)
+     CYL3_TRI : cx, cy, diameter, spacing          (equilateral triangle)       */
+enum { AJ_GEOM_NONE = 0, AJ_GEOM_CYLINDER = 1, AJ_GEOM_NACA4 = 2, AJ_GEOM_CYL3_ROW = 3,
+       AJ_GEOM_CYL3_TRI = 4 };
+int32_t aj_geometry(int32_t nx, int32_t ny, double lx, double ly, int32_t kind,
+                    const double* geo_host, double eps, float* mask, float* sdf, void* stream);
+
+/* Instrumentation: one launch of a hot kernel on the workspace's current
+   contents after an aj_step, so that it can be timed alone.  which:
+   0/1/2 = converging multigrid level-0 down / up / FP64-residual kernel;
+   3 = the predictor stages from (u, v).  No reference counterpart. */
+int32_t aj_profile_kernel(const AjStepParams* prm, int32_t which, const float* u,
+                          const float* v, const float* mask, void* workspace,
+                          size_t workspace_bytes, void* stream);
+
+/* Number of kernels one aj_step launches for these parameters when the
+   converging solver ran `cycles` V-cycles (parity mode ignores `cycles`).
+   Instrumentation only; no reference counterpart. */
+int32_t aj_kernel_count(const AjStepParams* prm, int32_t cycles);
+
+/* Drops the CUDA graphs aj_step / aj_poisson_mg instantiated for uncaptured
+   streams (they are keyed by parameters, workspace and buffer pointers).
+   Call only while none of them is executing.  No reference counterpart. */
+int32_t aj_release_graphs(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AEROJAX_GB300_H */

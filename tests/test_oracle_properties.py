@@ -1,0 +1,111 @@
+"""Known-answer checks of the oracle's new parts (converging multigrid, WENO5)
+and of the reference behaviours it must reproduce (shape errors).  CPU only."""
+import numpy as np
+import pytest
+
+from oracle import ref_np as R
+
+
+def _direct_solve(b, dx, dy):
+    """Sparse direct solve of the reference operator with the pinned outlet row."""
+    sp = pytest.importorskip("scipy.sparse")
+    spl = pytest.importorskip("scipy.sparse.linalg")
+    nx, ny = b.shape
+    N = nx * ny
+    rows, cols, vals = [], [], []
+    for k in range(N):
+        e = np.zeros(N)
+        e[k] = 1.0
+        col = R.lap_ref(e.reshape(nx, ny), dx, dy).ravel()
+        nz = np.nonzero(col)[0]
+        rows += list(nz)
+        cols += [k] * len(nz)
+        vals += list(col[nz])
+    A = sp.csr_matrix((vals, (rows, cols)), shape=(N, N)).tolil()
+    for j in range(ny):
+        r = (nx - 1) * ny + j
+        A[r, :] = 0
+        A[r, r] = 1.0
+    bb = b.copy()
+    bb[-1] = 0
+    return spl.spsolve(A.tocsr(), bb.ravel()).reshape(nx, ny)
+
+
+def test_converging_mg_matches_direct_solve():
+    nx, ny, dx, dy = 64, 32, 1 / 64, 1 / 64
+    b = np.random.default_rng(1).standard_normal((nx, ny))
+    x = _direct_solve(b, dx, dy)
+    p, info = R.mg_converge(b, dx, dy, rtol=1e-12, max_cycles=60)
+    assert info["rel_residual"] <= 1e-12
+    assert np.max(np.abs(p - x)) / np.max(np.abs(x)) < 1e-10
+
+
+@pytest.mark.parametrize("shape", [(128, 32), (256, 64), (96, 48)])
+def test_converging_mg_rate(shape):
+    nx, ny = shape
+    b = np.random.default_rng(2).standard_normal((nx, ny))
+    p, info = R.mg_converge(b, 1 / 64, 1 / 64, rtol=1e-8, max_cycles=30)
+    h = info["history"]
+    rates = [h[i + 1] / h[i] for i in range(len(h) - 1)]
+    assert info["rel_residual"] <= 1e-8
+    assert max(rates) < 0.25          # a working multigrid, not a smoother
+
+
+def test_warm_start_saves_cycles():
+    nx, ny, dx = 128, 32, 1 / 64
+    b = np.random.default_rng(3).standard_normal((nx, ny))
+    p, info = R.mg_converge(b, dx, dx, rtol=1e-6)
+    p2, info2 = R.mg_converge(b * 1.001, dx, dx, rtol=1e-6, p0=p)
+    assert info2["cycles"] < info["cycles"]
+
+
+def test_weno5_order():
+    """Fifth-order convergence of the WENO5 derivative on a smooth field."""
+    errs = []
+    for n in (32, 64, 128):
+        x = np.arange(n) / n * 2 * np.pi
+        f = np.sin(x)[:, None] * np.ones((1, 4))
+        d = R.weno5_derivative(f, np.ones_like(f), 2 * np.pi / n, 0, "wrap")
+        errs.append(np.max(np.abs(d[:, 0] - np.cos(x))))
+    orders = [np.log2(errs[i] / errs[i + 1]) for i in range(2)]
+    assert min(orders) > 4.5
+
+
+def test_weno5_upwind_direction():
+    n = 64
+    x = np.arange(n) / n * 2 * np.pi
+    f = np.sin(x)[:, None] * np.ones((1, 3))
+    h = 2 * np.pi / n
+    dpos = R.weno5_derivative(f, np.ones_like(f), h, 0, "wrap")
+    dneg = R.weno5_derivative(f, -np.ones_like(f), h, 0, "wrap")
+    assert np.max(np.abs(dpos - dneg)) < 1e-5       # both O(h^5)-consistent on smooth data
+    assert not np.array_equal(dpos, dneg)           # but different stencils
+
+
+@pytest.mark.parametrize("shape,ok", [((512, 96), True), ((64, 32), True), ((100, 64), False),
+                                      ((64, 40), False), ((32, 16), False), ((2048, 512), True)])
+def test_parity_level_rule(shape, ok):
+    """multigrid_solver.py:96-106: non-divisible grids raise ValueError."""
+    if ok:
+        assert R.mg_levels_ok(*shape) == 4
+    else:
+        with pytest.raises(ValueError):
+            R.mg_levels_ok(*shape)
+
+
+def test_float32_oracle_close_to_float64():
+    """The float32 evaluation (the timed CPU baseline) tracks float64."""
+    rng = np.random.default_rng(4)
+    nx, ny = 128, 32
+    u = 1 + 0.01 * rng.standard_normal((nx, ny))
+    v = 0.01 * rng.standard_normal((nx, ny))
+    mask = np.ones((nx, ny))
+    args = dict(dx=1 / 32, dy=1 / 32, nu=0.01, U_inf=1.0, brinkman_eta=1e-3, v_cycles=3)
+    a = R.step_pure(u, v, 2e-3, mask, None, args["dx"], args["dy"], args["nu"], 1.0, v_cycles=3,
+                    brinkman_eta=1e-3)
+    b = R.step_pure(u.astype(np.float32), v.astype(np.float32), np.float32(2e-3),
+                    mask.astype(np.float32), None, np.float32(args["dx"]), np.float32(args["dy"]),
+                    np.float32(0.01), np.float32(1.0), v_cycles=3, brinkman_eta=np.float32(1e-3))
+    for x, y in zip(a, b):
+        assert y.dtype == np.float32
+        assert np.max(np.abs(x - y)) / np.max(np.abs(x)) < 1e-4
