@@ -61,7 +61,10 @@ def naca_mac_2048x512(device="cuda", seed=0, nx=2048, ny=512, mg_mode="converge"
     chord = 256 * dx * nx / 2048
     nu = U * chord / Re
     eps = compute_eps_multiplier(Re) * dx
-    xle, yle = (400 * nx // 2048) * lx / (nx - 1), (ny // 2) * ly / (ny - 1)
+    # leading edge at (400 dx, 256 dy): placed on a grid node exactly, the
+    # reference's NACA distance (obstacles/naca_airfoils.py:137-145) divides
+    # 0/0 there for a symmetric section and the mask becomes NaN
+    xle, yle = (400 * nx // 2048) * dx, (ny // 2) * dy
     mask, _ = make_geometry("naca4", nx, ny, lx, ly, (chord, 10.0, xle, yle, 0.0, 0.0, 0.12), eps,
                             device)
     re = get_re_parameters(Re, nx)

@@ -11,6 +11,7 @@
 #include <string>
 #include <unordered_map>
 #include <string.h>
+#include <stdlib.h>
 
 namespace aj {
 
@@ -45,6 +46,21 @@ int converge_depth(int nx, int ny) {
     ++k;
   }
   return k;
+}
+
+bool eager_mode() {
+  static int v = -1;
+  if (v < 0) {
+    const char* e = getenv("AEROJAX_EAGER");
+    v = (e && e[0] && e[0] != '0') ? 1 : 0;
+  }
+  return v == 1;
+}
+
+int eager_unroll(int max_cycles) {
+  const char* e = getenv("AEROJAX_UNROLL");
+  int n = e ? atoi(e) : max_cycles;
+  return n < 1 ? 1 : (n > max_cycles ? max_cycles : n);
 }
 
 int check_params(const AjStepParams& p) {
@@ -164,6 +180,7 @@ int run_captured(const std::string& key, cudaStream_t user, F&& enqueue) {
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   if (cudaStreamIsCapturing(user, &cs) != cudaSuccess) return AJ_ERR_CUDA;
   if (cs == cudaStreamCaptureStatusActive) return enqueue(user);   // caller's own graph
+  if (eager_mode()) return enqueue(user);                          // profiling mode
   std::lock_guard<std::mutex> lk(g_mu);
   auto it = g_cache.find(key);
   if (it == g_cache.end()) {

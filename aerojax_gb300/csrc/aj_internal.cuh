@@ -27,6 +27,7 @@ struct DevScalars {
   double bnorm;        // ||b||
   double abs_sq;       // sum r^2 dx dy
   unsigned int red_count;
+  int loops;           // converging mode: executions of the while body
   unsigned int pad_[3];
 };
 
@@ -105,5 +106,12 @@ int profile_pressure_kernel(const AjStepParams& p, const Layout& L, void* ws, in
                             cudaStream_t st);
 
 inline unsigned cdiv(long a, long b) { return (unsigned)((a + b - 1) / b); }
+
+// Profiling mode: AEROJAX_EAGER=1 makes aj_step / aj_poisson_mg launch their
+// kernels straight onto the stream instead of through a CUDA graph (profilers
+// cannot attribute kernels inside graphs with conditional nodes); the
+// converging loop then runs AEROJAX_UNROLL bodies (default max_cycles).
+bool eager_mode();
+int eager_unroll(int max_cycles);
 
 }  // namespace aj

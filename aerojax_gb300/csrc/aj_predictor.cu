@@ -657,7 +657,8 @@ __device__ __forceinline__ float stage_mac(const RkMac& a, int i, int j, float d
       if (k1o) k1o[k] = r;
       return (x0 + dt * r) / den;
     }
-    return (x0 + 0.5f * dt * (ldg((COMP == 0 ? a.k1u : a.k1v) + k) + r)) / den;
+    float out = (x0 + 0.5f * dt * (ldg((COMP == 0 ? a.k1u : a.k1v) + k) + r)) / den;
+    return chi < 0.5f ? out : 0.f;                   // hard mask (rk3_mac.py:498-499)
   }
   if (a.stage == 1) return (x0 + dt * r) / den;
   float xs = x0 + dt * r;

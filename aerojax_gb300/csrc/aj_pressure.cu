@@ -347,27 +347,31 @@ __device__ __forceinline__ float cv_diag(const CvLvl& L, int gi, int gj) {
 }
 
 // red-black half-sweeps over a shared-memory tile; cells outside the domain
-// hold zero and never change (the diagonal carries the ghost rule)
+// hold zero and never change (the diagonal carries the ghost rule).  Every
+// half-sweep covers the whole tile: after half-sweep h the cells at distance
+// >= h+1 from the tile border hold exact red-black values, and the cells
+// nearer the border (stale neighbours) lie outside every value that is stored.
 template <int SI, int SJ>
 __device__ __forceinline__ void cv_sweeps(float* E, const float* R, const CvLvl& L, int gi0,
                                           int gj0, int nhalf) {
+  constexpr int ROWS = SI - 2, HW = (SJ - 1) / 2;   // cells of one colour per row (upper bound)
   const int tid = threadIdx.y * blockDim.x + threadIdx.x;
   const int nth = blockDim.x * blockDim.y;
+  const float inv_int = 1.f / (-2.f * (L.ax + L.ay));
   for (int h = 0; h < nhalf; ++h) {
     const int color = h & 1;
-    const int lo = h + 1, hiI = SI - 1 - h, hiJ = SJ - 1 - h;
-    const int rows = hiI - lo, width = hiJ - lo, hw = (width + 1) >> 1;
-    for (int t = tid; t < rows * hw; t += nth) {
-      int r = t / hw, kk = t - r * hw;
-      int ti = lo + r;
-      int tj = lo + ((color - ti - lo) & 1) + 2 * kk;
-      if (tj >= hiJ) continue;
-      int gi = gi0 + ti, gj = gj0 + tj;
-      if (gi < 0 || gi >= L.n || gj < 0 || gj >= L.m) continue;
+    for (int t = tid; t < ROWS * HW; t += nth) {
+      const int r = t / HW, kk = t - r * HW;
+      const int ti = 1 + r;
+      const int tj = 1 + ((color - ti - 1) & 1) + 2 * kk;
+      if (tj >= SJ - 1) continue;
+      const int gi = gi0 + ti, gj = gj0 + tj;
+      if ((unsigned)gi >= (unsigned)L.n || (unsigned)gj >= (unsigned)L.m) continue;
       if (L.level == 0 && gi == L.n - 1) continue;          // pinned outlet row
       const int c = ti * SJ + tj;
-      float nb = L.ax * (E[c + SJ] + E[c - SJ]) + L.ay * (E[c + 1] + E[c - 1]);
-      E[c] = (R[c] - nb) / cv_diag(L, gi, gj);
+      const float nb = L.ax * (E[c + SJ] + E[c - SJ]) + L.ay * (E[c + 1] + E[c - 1]);
+      const bool inner = gi > 0 && gi < L.n - 1 && gj > 0 && gj < L.m - 1;
+      E[c] = (R[c] - nb) * (inner ? inv_int : 1.f / cv_diag(L, gi, gj));
     }
     __syncthreads();
   }
@@ -531,6 +535,7 @@ __global__ void __launch_bounds__(256) k_cv_resid(const double* __restrict__ p64
 
 __global__ void k_cv_begin(DevScalars* sc) {
   sc->mg_done = 0;
+  sc->loops = 0;
   sc->mg_cycles = 0;
   sc->acc[0] = 0.0;
   sc->acc[1] = 0.0;
@@ -562,7 +567,15 @@ __global__ void k_cv_check(DevScalars* sc, double rtol, int max_cycles, int firs
   }
   sc->acc[0] = 0.0;
   sc->acc[1] = 0.0;
-  if (use_handle) cudaGraphSetConditional(h, sc->mg_done ? 0u : 1u);
+  if (use_handle) {
+    // independent bound on the while node: never more bodies than max_cycles + 1
+    sc->loops += 1;
+    if (sc->loops > max_cycles + 1 && !sc->mg_done) {
+      sc->err = AJ_ERR_NOT_CONVERGED;
+      sc->mg_done = 1;
+    }
+    cudaGraphSetConditional(h, sc->mg_done ? 0u : 1u);
+  }
 }
 
 __global__ void k_cv_out(const double* __restrict__ p64, float* __restrict__ p, long N) {
@@ -650,9 +663,16 @@ static int converge_solve(const AjStepParams& p, const Layout& L, void* ws, cons
   const cudaGraphNode_t* deps;
   const cudaGraphEdgeData* ed;
   size_t nd;
-  if (cudaStreamGetCaptureInfo(st, &cs, &id, &g, &deps, &ed, &nd) != cudaSuccess ||
-      cs != cudaStreamCaptureStatusActive)
-    return AJ_ERR_CUDA;   // callers always capture (aj_api.cu)
+  if (cudaStreamGetCaptureInfo(st, &cs, &id, &g, &deps, &ed, &nd) != cudaSuccess)
+    return AJ_ERR_CUDA;
+  if (cs != cudaStreamCaptureStatusActive) {
+    // eager launches (profiling mode, see aj_api.cu): a fixed number of loop
+    // bodies, each skipping its work once the target is met
+    int unroll = eager_unroll(p.max_cycles);
+    for (int k = 0; k < unroll; ++k) cv_body(p, L, ws, 0, 0, st);
+    k_cv_out<<<cdiv(N, 256), 256, 0, st>>>(p64, pout, N);
+    return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+  }
   cudaGraphConditionalHandle h;
   if (cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault) != cudaSuccess)
     return AJ_ERR_CUDA;

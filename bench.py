@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--ny", type=int, default=512)
     ap.add_argument("--cpu-sample-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--quick", action="store_true",
+                    help="timed GPU arms only (no clock soak, e2e or CPU leg): for profiling")
     return ap.parse_args()
 
 
@@ -114,7 +116,7 @@ def cpu_step_fn(nx, ny):
     dx, dy = lx / nx, ly / ny
     X, Y = R.grid_coords(nx, ny, lx, ly)
     chord = 256 * dx * nx / 2048
-    xle, yle = (400 * nx // 2048) * lx / (nx - 1), (ny // 2) * ly / (ny - 1)
+    xle, yle = (400 * nx // 2048) * dx, (ny // 2) * dy
     sdf = R.sdf_naca4(X, Y, chord, 10.0, xle, yle, 0.0, 0.0, 0.12)
     f = np.float32
     mask = R.mask_from_sdf(sdf, 0.05 * dx).astype(f)
@@ -231,17 +233,27 @@ def gpu_arm(args):
             return float(t.item())
         return x
 
+    def soak(plan, bufs, warm, seconds):
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < seconds:
+            run(plan, bufs, 20, False, warm)
+
     results = {}
     clocks = ClockSampler(local)
     for name, warm in (("plain", False), ("method", True)):
         plan, bufs = make_arm(warm)
         run(plan, bufs, max(3, args.warmup), False, warm)
         barrier()
-        if name == "method":
-            clocks.start()
+        sample_clocks = name == "method" and not args.quick
+        if sample_clocks:
+            clocks.start()                      # sample clocks over >= 1.5 s of load
+            soak(plan, bufs, warm, 1.0)
         ms, cyc = run(plan, bufs, args.steps, True, warm)
-        if name == "method":
+        if sample_clocks:
+            soak(plan, bufs, warm, 0.5)
             clk = clocks.stop()
+        elif name == "method":
+            clk = None
         barrier()
         ms = max_over_ranks(ms)
         results[name] = dict(ms=ms, cycles=cyc, plan=plan, bufs=bufs)
@@ -286,12 +298,15 @@ def gpu_arm(args):
             for a, b in zip(h_in, h_out):
                 a.copy_(b)
         return sum(a.elapsed_time(b) for a, b in ev)
-    e2e_steps(3)
-    barrier()
-    e2e_ms = max_over_ranks(e2e_steps(args.steps)) / args.steps
-    e2e_val = world * cells / (e2e_ms * 1e-3) / 1e6
     h2d = 4 * (nxu + nyv + cells)
     d2h = 4 * (nxu + nyv + cells)
+    e2e = None
+    if not args.quick:
+        e2e_steps(3)
+        barrier()
+        e2e_ms = max_over_ranks(e2e_steps(args.steps)) / args.steps
+        e2e = {"value": world * cells / (e2e_ms * 1e-3) / 1e6, "unit": UNIT,
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
 
     # ---- roofline: the dominant kernel timed alone (events on the launch stream)
     roof = roofline(args, plan, meth["bufs"][0], mask, flush, L)
@@ -302,7 +317,7 @@ def gpu_arm(args):
             dist.destroy_process_group()
         return
     cpu = None
-    if not args.no_cpu_baseline:
+    if not args.no_cpu_baseline and not args.quick:
         n = args.cpu_sample_steps
         cval, cel = run_cpu(args.nx, args.ny, n, 1)
         cpu = {"value": cval, "unit": UNIT, "cores": 1, "kind": "port",
@@ -328,8 +343,7 @@ def gpu_arm(args):
         },
         "roofline": roof,
         "cpu_baseline": cpu,
-        "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h},
+        "e2e": e2e,
         "gpu_launches": launches,
         "clocks": clk,
     }
