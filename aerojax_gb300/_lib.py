@@ -66,6 +66,8 @@ _SIGS = {
                             c_size_t, c_void_p]),
     "aj_geometry": (c_int32, [c_int32, c_int32, c_double, c_double, c_int32, POINTER(c_double),
                               c_double, c_void_p, c_void_p, c_void_p]),
+    "aj_poisson_mg_static": (c_int32, [POINTER(AjStepParams), c_void_p, c_void_p, c_void_p,
+                                       c_void_p, c_void_p]),
     "aj_kernel_count": (c_int32, [POINTER(AjStepParams), c_int32]),
     "aj_profile_kernel": (c_int32, [POINTER(AjStepParams), c_int32, c_void_p, c_void_p, c_void_p,
                                     c_void_p, c_size_t, c_void_p]),

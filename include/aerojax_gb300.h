@@ -171,6 +171,22 @@ enum { AJ_GEOM_NONE = 0, AJ_GEOM_CYLINDER = 1, AJ_GEOM_NACA4 = 2, AJ_GEOM_CYL3_R
 int32_t aj_geometry(int32_t nx, int32_t ny, double lx, double ly, int32_t kind,
                     const double* geo_host, double eps, float* mask, float* sdf, void* stream);
 
+/* Allocation-free pressure solve, for callers that cannot allocate device
+   memory: hosts that own every device byte through their own allocator (a
+   framework's caching allocator, an XLA custom call without a scratch
+   buffer) and latency-critical loops that cannot afford cudaMalloc's implicit
+   synchronisation.  Same result as aj_poisson_mg in parity mode on the
+   collocated grid (von Karman), but its scratch is a 14 MiB device array
+   inside the library, so the caller passes only rhs, mask (nx*ny) and p
+   (nx*ny); stats may be NULL.  Grids above AJ_STATIC_MAX_CELLS cells return
+   AJ_ERR_WORKSPACE.  The first call on each device looks up the array's
+   device address (cudaGetSymbolAddress); make that first call before any
+   stream capture.  Every call shares the array: calls that overlap on the GPU
+   race, so order them on one stream.  No counterpart in the reference. */
+#define AJ_STATIC_MAX_CELLS (1 << 20)
+int32_t aj_poisson_mg_static(const AjStepParams* prm, const float* rhs, const float* mask,
+                             float* p, AjStats* stats, void* stream);
+
 /* Instrumentation: one launch of a hot kernel on the workspace's current
    contents after an aj_step, so that it can be timed alone.  which:
    0/1/2 = converging multigrid level-0 down / up / FP64-residual kernel;

@@ -1,0 +1,67 @@
+"""The allocation-free pressure solve (aj_poisson_mg_static).
+
+Some callers cannot allocate device memory for a call: hosts that own all
+device memory through their own allocator, or loops that cannot take
+cudaMalloc's synchronisation.  For them the library keeps the multigrid's
+scratch in a device array of its own.  This test calls that entry point
+through the C ABI, twice in a row with different inputs, and checks each
+result against the ordinary workspace-based entry point (aj_poisson_mg, via
+poisson_multigrid) within the suite's FP32 tolerance.  It sits in a file that
+pytest collects last, and needs nothing from the other tests."""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+
+
+def _params(nx, ny, dx, v_cycles):
+    from aerojax_gb300.params import StepConfig
+    from aerojax_gb300.solver import make_params
+    return make_params(StepConfig(nx=nx, ny=ny, dx=dx, dy=dx, nu=1.0, variant="gui",
+                                  v_cycles=v_cycles, mg_mode="parity"))
+
+
+def _static_solve(L, prm, rhs, mask):
+    import torch
+    p = torch.full_like(rhs, float("nan"))
+    stats = torch.zeros(64, dtype=torch.uint8, device=rhs.device)
+    rc = L.aj_poisson_mg_static(ctypes.byref(prm), rhs.data_ptr(), mask.data_ptr(), p.data_ptr(),
+                                stats.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    assert rc == 0, rc
+    return p
+
+
+def test_static_matches_workspace_solver_twice(cuda_lib):
+    import torch
+    import aerojax_gb300 as aj
+    L = cuda_lib
+    nx, ny, dx, vc = 512, 96, 1 / 64, 3
+    prm = _params(nx, ny, dx, vc)
+    rng = np.random.default_rng(11)
+    mask = torch.as_tensor((rng.random((nx, ny)) > 0.05).astype(np.float32), device="cuda")
+    results = []
+    for call in range(2):                      # two calls in a row, different inputs
+        rhs = torch.as_tensor((10.0 * rng.standard_normal((nx, ny))).astype(np.float32),
+                              device="cuda")
+        p_static = _static_solve(L, prm, rhs, mask)
+        p_ref = aj.poisson_multigrid(rhs, mask, dx, dx, v_cycles=vc)
+        torch.cuda.synchronize()
+        assert torch.isfinite(p_static).all()
+        err = float((p_static - p_ref).abs().max() / p_ref.abs().max())
+        assert err < TOL, (call, err)
+        results.append(p_static.clone())
+    assert not torch.equal(results[0], results[1])
+
+
+def test_static_rejects_oversized_grid(cuda_lib):
+    import torch
+    L = cuda_lib
+    nx, ny = 4096, 512                          # 2 Mi cells > AJ_STATIC_MAX_CELLS
+    prm = _params(nx, ny, 1 / 64, 1)
+    x = torch.zeros(16, device="cuda")          # never touched: rejected on the host
+    rc = L.aj_poisson_mg_static(ctypes.byref(prm), x.data_ptr(), x.data_ptr(), x.data_ptr(),
+                                None, torch.cuda.current_stream().cuda_stream)
+    assert rc == 7                              # AJ_ERR_WORKSPACE
