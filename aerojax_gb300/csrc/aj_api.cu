@@ -36,11 +36,11 @@ int parity_levels(int nx, int ny, int levels, int* max_levels) {
 }
 
 int converge_depth(int nx, int ny) {
-  // halve while even, at least 4 x 4 cells remain... and the coarse grid is
-  // still above AJ_MAX_COARSE / 2 cells; always coarsen at least once
+  // halve while both sizes are even and the halves keep >= 2 cells, until the
+  // coarse grid has <= AJ_MAX_COARSE cells; always coarsen at least once
   int k = 0, n = nx, m = ny;
   while (n % 2 == 0 && m % 2 == 0 && n / 2 >= 2 && m / 2 >= 2 &&
-         ((long)n * m > AJ_MAX_COARSE / 2 || k == 0) && k < AJ_MAX_LEVELS) {
+         ((long)n * m > AJ_MAX_COARSE || k == 0) && k < AJ_MAX_LEVELS) {
     n /= 2;
     m /= 2;
     ++k;
@@ -79,7 +79,7 @@ int check_params(const AjStepParams& p) {
     int D = converge_depth(p.nx, p.ny);
     if (D < 1) return AJ_ERR_SHAPE;
     long nc = (long)(p.nx >> D) * (p.ny >> D);
-    if (nc > AJ_MAX_COARSE * 2) return AJ_ERR_SHAPE;
+    if (nc > AJ_MAX_COARSE_HARD) return AJ_ERR_SHAPE;
     if (p.mg_rtol <= 0 || p.max_cycles < 1) return AJ_ERR_PARAM;
   }
   if (p.cfl_dt && (p.cfl_target <= 0 || p.dt_max <= 0)) return AJ_ERR_PARAM;
@@ -140,7 +140,10 @@ bool make_layout(const AjStepParams& p, Layout& L) {
     }
     L.ncoarse = L.ln[D] * L.lm[D];
     L.p64 = take(N * 8);
+    L.p64b = take(N * 8);
     L.cinv = take((size_t)L.ncoarse * L.ncoarse * 8);
+    // levels lc..D run in one thread block with everything in shared memory
+    L.lc = converge_first_block_level(L);
   }
   L.part = take(kPartials * 8);
   L.total = off;
@@ -404,7 +407,7 @@ int32_t aj_kernel_count(const AjStepParams* prm, int32_t cycles) {
     int per_cycle = 5 * L.nlev + 10 + 2;                        // 5 per level, coarsest, norm
     n += 1 + p.v_cycles * per_cycle;                            // begin + cycles
   } else {
-    int body = 2 * L.nlev + 3;                                  // down, coarse, up, resid, check
+    int body = 2 * L.lc + 1;                                    // downs, one-block coarse, ups
     n += 4 + (cycles > 1 ? cycles : 1) * body + 1;              // begin/init/resid/check, loop, out
   }
   n += 1;                                                       // stats

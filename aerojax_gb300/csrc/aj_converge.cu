@@ -1,0 +1,872 @@
+// Converging multigrid: solves the reference's discrete pressure operator
+// (5-point Laplacian with edge ghosts, outlet row pinned at 0; the operator of
+// pressure_solvers/multigrid_solver.py:173-183) to ||b - A p||_2 <= rtol ||b||_2.
+//
+// Structure of one refinement iteration (one body of the graph's while node):
+//   levels 0 .. lc-1   k_cv_down: 2 red-black sweeps from e = 0 in a shared-
+//                      memory tile, residual, 2x2 restriction
+//   levels lc .. D     k_cv_block: one 1024-thread block holding the smallest
+//                      levels (<= 1024 cells) in shared memory: sweeps,
+//                      restriction, the FP64 dense solve of the coarsest grid,
+//                      prolongation, sweeps
+//   levels lc-1 .. 1   k_cv_up: e += P(e_coarse), 2 red-black sweeps
+//   level 0            k_cv_up0: the same, then p += e, the residual
+//                      r = b - A p for the next iteration, its FP64 norm, and
+//                      (last block) the convergence test that sets the while
+//                      node's condition with cudaGraphSetConditional
+//
+// Precision.  The V-cycle runs in FP32.  The refinement state p and the
+// refinement residual are kept in double-FP32 ("double-single") arithmetic:
+// p = hi + lo with |lo| <= ulp(hi)/2, updated and applied with the error-free
+// transformations TwoSum (Knuth) and TwoProd (Dekker, via fma), which carry a
+// ~48-bit significand on the FP32 pipes.  GB300 executes FP64 at 1/64 of the
+// FP32 rate, and a plain-FP64 residual cost ~25 us per cycle at 2048x512.
+// FP64 proper is kept where it is cheap: the coarsest-grid dense solve and the
+// global norms that decide termination.
+// The pressure state ping-pongs between two buffers (a tile's halo must see the
+// old values while neighbouring tiles write the new ones).
+// Coarse operators are rediscretised at spacing 2^l h; the outlet Dirichlet
+// point stays where the fine grid has it (ghost g * e_last with
+// g = (theta - 1) / theta, theta = (1 - 2^-l) / 2).  The oracle is
+// oracle/ref_np.py mg_converge (FP64 throughout).
+#include "aj_internal.cuh"
+#include <math.h>
+#include <string.h>
+#include <vector>
+
+namespace aj {
+
+constexpr int CV_NS = 2;                         // red-black sweeps per smoothing phase
+constexpr int CV_H = 2 * CV_NS + 1;              // tile halo: sweeps + one cell for the residual
+constexpr int CV_THREADS = 256;
+constexpr int CV_BLOCK_THREADS = 1024;
+constexpr int CV_BLOCK_MAX_CELLS = 1024;         // levels handled by the one-block kernel
+
+template <int TI, int TJ>
+struct Tile {
+  static constexpr int SI = TI + 2 * CV_H, SJ = TJ + 2 * CV_H, NT = SI * SJ;
+};
+using TileL0 = Tile<32, 64>;                     // level 0: 512 tiles at 2048x512
+using TileLc = Tile<16, 32>;                     // coarser levels: 4x more tiles
+
+struct CvLvl {
+  int n, m, level;
+  float ax, ay, g;   // g: outlet ghost factor of this level (level >= 1)
+};
+
+static double ghost_factor(int level) {
+  double th = 0.5 * (1.0 - pow(2.0, -level));
+  return (th - 1.0) / th;
+}
+
+static CvLvl cv_level(const AjStepParams& p, const Layout& L, int l) {
+  CvLvl c;
+  c.n = L.ln[l];
+  c.m = L.lm[l];
+  c.level = l;
+  double hx = p.dx * (double)(1 << l), hy = p.dy * (double)(1 << l);
+  c.ax = (float)(1.0 / (hx * hx));
+  c.ay = (float)(1.0 / (hy * hy));
+  c.g = l > 0 ? (float)ghost_factor(l) : 0.f;
+  return c;
+}
+
+// ---------------------------------------------------------------- double-FP32
+struct df {
+  float hi, lo;
+};
+// Knuth's TwoSum: s + e == a + b exactly
+__device__ __forceinline__ df two_sum(float a, float b) {
+  float s = a + b;
+  float bb = s - a;
+  float e = (a - (s - bb)) + (b - bb);
+  return {s, e};
+}
+// Dekker's FastTwoSum, valid for |a| >= |b|
+__device__ __forceinline__ df quick_two_sum(float a, float b) {
+  float s = a + b;
+  return {s, b - (s - a)};
+}
+// Dekker's TwoProd with a fused multiply-add: p + e == a * b exactly
+__device__ __forceinline__ df two_prod(float a, float b) {
+  float p = a * b;
+  return {p, fmaf(a, b, -p)};
+}
+__device__ __forceinline__ df df_add(df a, df b) {
+  df s = two_sum(a.hi, b.hi);
+  df t = two_sum(a.lo, b.lo);
+  s.lo += t.hi;
+  s = quick_two_sum(s.hi, s.lo);
+  s.lo += t.lo;
+  return quick_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ df df_neg(df a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ df df_mul(df a, df b) {
+  df p = two_prod(a.hi, b.hi);
+  p.lo += a.hi * b.lo + a.lo * b.hi;
+  return quick_two_sum(p.hi, p.lo);
+}
+__device__ __forceinline__ df df_add_f(df a, float b) {
+  df s = two_sum(a.hi, b);
+  s.lo += a.lo;
+  return quick_two_sum(s.hi, s.lo);
+}
+// r = b - (ax ((xp - c) + (xm - c)) + ay ((yp - c) + (ym - c))), all double-FP32
+__device__ __forceinline__ df df_residual(float b, df c, df xp, df xm, df yp, df ym, df ax, df ay) {
+  const df nc = df_neg(c);
+  const df sx = df_add(df_add(xp, nc), df_add(xm, nc));
+  const df sy = df_add(df_add(yp, nc), df_add(ym, nc));
+  const df ap = df_add(df_mul(ax, sx), df_mul(ay, sy));
+  return df_add_f(df_neg(ap), b);
+}
+
+struct DfCoef {
+  float axh, axl, ayh, ayl;   // 1/dx^2 and 1/dy^2 split into hi + lo
+};
+static DfCoef df_coef(double ax, double ay) {
+  DfCoef c;
+  c.axh = (float)ax;
+  c.axl = (float)(ax - (double)c.axh);
+  c.ayh = (float)ay;
+  c.ayl = (float)(ay - (double)c.ayh);
+  return c;
+}
+
+// ---------------------------------------------------------------- tiles
+__device__ __forceinline__ float cv_diag(const CvLvl& L, int gi, int gj) {
+  float d = -2.f * (L.ax + L.ay);
+  if (gi == 0) d += L.ax;
+  if (gj == 0) d += L.ay;
+  if (gj == L.m - 1) d += L.ay;
+  if (gi == L.n - 1) d += (L.level == 0) ? L.ax : L.ax * L.g;
+  return d;
+}
+
+// red-black half-sweeps over the whole shared-memory tile; cells outside the
+// domain hold 0 and never change (the diagonal carries the ghost rule).  After
+// half-sweep h the cells at distance >= h+1 from the tile border hold exact
+// red-black values; the cells nearer the border are never stored.
+template <class TL>
+__device__ __forceinline__ void cv_sweeps(float* E, const float* R, const CvLvl& L, int gi0,
+                                          int gj0) {
+  constexpr int SJ = TL::SJ, ROWS = TL::SI - 2, HW = (SJ - 1) / 2;
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  const float inv_int = 1.f / (-2.f * (L.ax + L.ay));
+  for (int h = 0; h < 2 * CV_NS; ++h) {
+    const int color = h & 1;
+    for (int t = tid; t < ROWS * HW; t += CV_THREADS) {
+      const int r = t / HW, kk = t - r * HW;
+      const int ti = 1 + r;
+      const int tj = 1 + ((color - ti - 1) & 1) + 2 * kk;
+      if (tj >= SJ - 1) continue;
+      const int gi = gi0 + ti, gj = gj0 + tj;
+      if ((unsigned)gi >= (unsigned)L.n || (unsigned)gj >= (unsigned)L.m) continue;
+      if (L.level == 0 && gi == L.n - 1) continue;          // pinned outlet row
+      const int c = ti * SJ + tj;
+      const float nb = L.ax * (E[c + SJ] + E[c - SJ]) + L.ay * (E[c + 1] + E[c - 1]);
+      const bool inner = gi > 0 && gi < L.n - 1 && gj > 0 && gj < L.m - 1;
+      E[c] = (R[c] - nb) * (inner ? inv_int : 1.f / cv_diag(L, gi, gj));
+    }
+    __syncthreads();
+  }
+}
+
+// cell-centred bilinear prolongation of the coarse correction (ghosts:
+// Neumann copies at inlet and walls, outlet ghost g * value)
+__device__ __forceinline__ float cv_prolong(const float* __restrict__ ec, int nc, int mc, float g,
+                                            int gi, int gj) {
+  const int I = gi >> 1, J = gj >> 1;
+  const int Ii = (gi & 1) ? I + 1 : I - 1;
+  int Jj = (gj & 1) ? J + 1 : J - 1;
+  Jj = Jj < 0 ? 0 : (Jj >= mc ? mc - 1 : Jj);
+  const float c0 = ldg(ec + (long)I * mc + J);
+  const float cy = ldg(ec + (long)I * mc + Jj);
+  float cx, cxy;
+  if (Ii < 0) {
+    cx = c0;
+    cxy = cy;
+  } else if (Ii >= nc) {
+    cx = g * c0;
+    cxy = g * cy;
+  } else {
+    cx = ldg(ec + (long)Ii * mc + J);
+    cxy = ldg(ec + (long)Ii * mc + Jj);
+  }
+  return (9.f * c0 + 3.f * cx + 3.f * cy + cxy) * (1.f / 16.f);
+}
+
+// tile + halo load: E = e_in + P(ec) (or 0), R = r; unrolled so the loads are
+// in flight together
+template <class TL, bool ZERO_E>
+__device__ __forceinline__ void cv_load(float* E, float* R, const CvLvl& L, int gi0, int gj0,
+                                        const float* __restrict__ r, const float* __restrict__ e_in,
+                                        const float* __restrict__ ec, int nc, int mc, float gc) {
+  constexpr int NT = TL::NT, SJ = TL::SJ, IT = (NT + CV_THREADS - 1) / CV_THREADS;
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+#pragma unroll
+  for (int it = 0; it < IT; ++it) {
+    const int t = tid + it * CV_THREADS;
+    if (t < NT) {
+      const int ti = t / SJ, tj = t - ti * SJ;
+      const int gi = gi0 + ti, gj = gj0 + tj;
+      const bool in = (unsigned)gi < (unsigned)L.n && (unsigned)gj < (unsigned)L.m;
+      float rr = 0.f, e = 0.f;
+      if (in) {
+        const long k = (long)gi * L.m + gj;
+        rr = ldg(r + k);
+        if (!ZERO_E && !(L.level == 0 && gi == L.n - 1))
+          e = ldg(e_in + k) + cv_prolong(ec, nc, mc, gc, gi, gj);
+      }
+      E[t] = e;
+      R[t] = rr;
+    }
+  }
+  __syncthreads();
+}
+
+// pre-smoothing from e = 0, residual, 2x2 average onto the coarse rhs
+template <int TI, int TJ>
+__global__ void __launch_bounds__(CV_THREADS) k_cv_down(CvLvl L, const float* __restrict__ r,
+                                                        float* __restrict__ e_out,
+                                                        float* __restrict__ rc, const int* done) {
+  using TL = Tile<TI, TJ>;
+  constexpr int SJ = TL::SJ;
+  if (*done) return;
+  __shared__ float E[TL::NT];
+  __shared__ float R[TL::NT];
+  const int i0 = blockIdx.y * TI, j0 = blockIdx.x * TJ;
+  const int gi0 = i0 - CV_H, gj0 = j0 - CV_H;
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  cv_load<TL, true>(E, R, L, gi0, gj0, r, nullptr, nullptr, 0, 0, 0.f);
+  cv_sweeps<TL>(E, R, L, gi0, gj0);
+  // store e and compute the residual on the tile interior (in place in R)
+  for (int t = tid; t < TI * TJ; t += CV_THREADS) {
+    const int ti = CV_H + t / TJ, tj = CV_H + t % TJ;
+    const int gi = gi0 + ti, gj = gj0 + tj;
+    if (gi >= L.n || gj >= L.m) continue;
+    const int c = ti * SJ + tj;
+    e_out[(long)gi * L.m + gj] = E[c];
+    float res = 0.f;
+    if (!(L.level == 0 && gi == L.n - 1)) {
+      const float nb = L.ax * (E[c + SJ] + E[c - SJ]) + L.ay * (E[c + 1] + E[c - 1]);
+      res = R[c] - (nb + cv_diag(L, gi, gj) * E[c]);
+    }
+    R[c] = res;
+  }
+  __syncthreads();
+  const int mc = L.m >> 1, nc = L.n >> 1;
+  for (int t = tid; t < (TI / 2) * (TJ / 2); t += CV_THREADS) {
+    const int ci = t / (TJ / 2), cj = t % (TJ / 2);
+    const int I = (i0 >> 1) + ci, J = (j0 >> 1) + cj;
+    if (I >= nc || J >= mc) continue;
+    const int c = (CV_H + 2 * ci) * SJ + CV_H + 2 * cj;
+    rc[(long)I * mc + J] = 0.25f * (R[c] + R[c + SJ] + R[c + 1] + R[c + SJ + 1]);
+  }
+}
+
+// e + P(e_coarse), post-smoothing, store (levels >= 1)
+template <int TI, int TJ>
+__global__ void __launch_bounds__(CV_THREADS) k_cv_up(CvLvl L, const float* __restrict__ r,
+                                                      const float* __restrict__ e_in,
+                                                      const float* __restrict__ ec, int nc, int mc,
+                                                      float gc, float* __restrict__ e_out,
+                                                      const int* done) {
+  using TL = Tile<TI, TJ>;
+  if (*done) return;
+  __shared__ float E[TL::NT];
+  __shared__ float R[TL::NT];
+  const int i0 = blockIdx.y * TI, j0 = blockIdx.x * TJ;
+  const int gi0 = i0 - CV_H, gj0 = j0 - CV_H;
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  cv_load<TL, false>(E, R, L, gi0, gj0, r, e_in, ec, nc, mc, gc);
+  cv_sweeps<TL>(E, R, L, gi0, gj0);
+  for (int t = tid; t < TI * TJ; t += CV_THREADS) {
+    const int ti = CV_H + t / TJ, tj = CV_H + t % TJ;
+    const int gi = gi0 + ti, gj = gj0 + tj;
+    if (gi >= L.n || gj >= L.m) continue;
+    e_out[(long)gi * L.m + gj] = E[ti * TL::SJ + tj];
+  }
+}
+
+struct CvCheck {
+  double rtol;
+  int max_cycles;
+  int use_handle;
+  cudaGraphConditionalHandle h;
+};
+
+// convergence bookkeeping after a V-cycle (device scalars; one thread)
+__device__ void cv_check_body(DevScalars* sc, const CvCheck& ck) {
+  if (!sc->mg_done) {
+    sc->mg_cycles += 1;
+    double nb = sc->bnorm > 0.0 ? sc->bnorm : 1.0;
+    double rel = sqrt(sc->acc[0]) / nb;
+    sc->rel = rel;
+    sc->abs_sq = sc->acc[0];
+    if (!isfinite(rel)) {
+      sc->err = AJ_ERR_NONFINITE;
+      sc->mg_done = 1;
+    } else if (rel <= ck.rtol) {
+      sc->mg_done = 1;
+    } else if (sc->mg_cycles >= ck.max_cycles) {
+      sc->err = AJ_ERR_NOT_CONVERGED;
+      sc->mg_done = 1;
+    }
+  }
+  sc->acc[0] = 0.0;
+  if (ck.use_handle) {
+    // independent bound on the while node: never more bodies than max_cycles + 1
+    sc->loops += 1;
+    if (sc->loops > ck.max_cycles + 1 && !sc->mg_done) {
+      sc->err = AJ_ERR_NOT_CONVERGED;
+      sc->mg_done = 1;
+    }
+    cudaGraphSetConditional(ck.h, sc->mg_done ? 0u : 1u);
+  }
+}
+
+// the pressure state: N hi values followed by N lo values
+struct PState {
+  float* a;   // buffer 0
+  float* b;   // buffer 1
+};
+
+// level 0: e + P(e_coarse), post-smoothing, p += e (double-FP32, ping-pong), the
+// residual of the reference operator for the next iteration (double-FP32), its
+// FP64 norm, and the convergence test in the last block to finish
+__global__ void __launch_bounds__(CV_THREADS) k_cv_up0(
+    CvLvl L, const float* __restrict__ r, const float* __restrict__ e_in,
+    const float* __restrict__ ec, int nc, int mc, float gc, PState ps, const float* __restrict__ b,
+    float* __restrict__ r_next, DevScalars* sc, DfCoef co, CvCheck ck, int profile) {
+  using TL = TileL0;
+  constexpr int TI = 32, TJ = 64, SJ = TL::SJ;
+  if (!profile && sc->mg_done) return;
+  __shared__ float E[TL::NT];
+  __shared__ float R[TL::NT];
+  constexpr int PI = TI + 2, PJ = TJ + 2;
+  __shared__ float PH[PI * PJ];
+  __shared__ float PL[PI * PJ];
+  __shared__ int am_last;
+  const int i0 = blockIdx.y * TI, j0 = blockIdx.x * TJ;
+  const int gi0 = i0 - CV_H, gj0 = j0 - CV_H;
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  const long N = (long)L.n * L.m;
+  const int cur = sc->pcur;
+  const float* __restrict__ pin = cur ? ps.b : ps.a;
+  float* __restrict__ pout = cur ? ps.a : ps.b;
+  cv_load<TL, false>(E, R, L, gi0, gj0, r, e_in, ec, nc, mc, gc);
+  cv_sweeps<TL>(E, R, L, gi0, gj0);
+  // new pressure on the interior and one cell around it
+  for (int t = tid; t < PI * PJ; t += CV_THREADS) {
+    const int pi = t / PJ, pj = t - pi * PJ;
+    const int gi = i0 - 1 + pi, gj = j0 - 1 + pj;
+    df v{0.f, 0.f};
+    if ((unsigned)gi < (unsigned)L.n && (unsigned)gj < (unsigned)L.m && gi != L.n - 1) {
+      const long k = (long)gi * L.m + gj;
+      v = df_add_f(df{pin[k], pin[N + k]}, E[(CV_H - 1 + pi) * SJ + (CV_H - 1 + pj)]);
+    }
+    PH[t] = v.hi;
+    PL[t] = v.lo;
+  }
+  __syncthreads();
+  const df ax{co.axh, co.axl}, ay{co.ayh, co.ayl};
+  float acc = 0.f;
+  for (int t = tid; t < TI * TJ; t += CV_THREADS) {
+    const int ti = t / TJ, tj = t % TJ;
+    const int gi = i0 + ti, gj = j0 + tj;
+    if (gi >= L.n || gj >= L.m) continue;
+    const long k = (long)gi * L.m + gj;
+    const int c = (ti + 1) * PJ + (tj + 1);
+    const df pc{PH[c], PL[c]};
+    pout[k] = pc.hi;
+    pout[N + k] = pc.lo;
+    float rr = 0.f;
+    if (gi != L.n - 1) {
+      const df xp{PH[c + PJ], PL[c + PJ]};                      // row n-1 holds the pinned 0
+      const df xm = gi > 0 ? df{PH[c - PJ], PL[c - PJ]} : pc;   // Neumann ghosts
+      const df yp = gj < L.m - 1 ? df{PH[c + 1], PL[c + 1]} : pc;
+      const df ym = gj > 0 ? df{PH[c - 1], PL[c - 1]} : pc;
+      const df res = df_residual(ldg(b + k), pc, xp, xm, yp, ym, ax, ay);
+      rr = res.hi + res.lo;
+    }
+    if (!profile) r_next[k] = rr;
+    acc = fmaf(rr, rr, acc);
+  }
+  if (profile) return;
+  block_sum_atomic((double)acc, &sc->acc[0]);
+  if (tid == 0) {
+    __threadfence();
+    unsigned int ticket = atomicAdd(&sc->red_count, 1u);
+    am_last = ticket == gridDim.x * gridDim.y - 1;
+  }
+  __syncthreads();
+  if (am_last && tid == 0) {
+    __threadfence();
+    sc->red_count = 0u;
+    sc->pcur = 1 - cur;
+    cv_check_body(sc, ck);
+  }
+}
+
+struct CvBlock {
+  int lc, D, ncoarse;
+  int n[AJ_MAX_LEVELS + 1], m[AJ_MAX_LEVELS + 1];
+  float ax[AJ_MAX_LEVELS + 1], ay[AJ_MAX_LEVELS + 1], g[AJ_MAX_LEVELS + 1];
+  const float* r_in;      // rhs of level lc (global)
+  float* e_out;           // correction of level lc (global)
+  const double* Ainv;     // coarsest inverse, row-major ncoarse^2
+  const int* done;
+};
+
+// shared-memory footprint of levels lc..D: e and r with a one-cell zero border
+// per level, plus the FP64 vector of the dense coarsest solve
+size_t converge_block_smem(const Layout& L, int lc) {
+  size_t s = 0;
+  for (int k = lc; k <= L.nlev; ++k) s += 2 * (size_t)(L.ln[k] + 2) * (L.lm[k] + 2) * 4;
+  s = (s + 15) & ~(size_t)15;
+  s += (size_t)L.ln[L.nlev] * L.lm[L.nlev] * 8;
+  return s;
+}
+
+__device__ __forceinline__ void blk_sweeps(float* E, const float* R, int n, int m, float ax,
+                                           float ay, float g) {
+  const int W = m + 2, hw = (m + 1) >> 1;
+  const float inv_int = 1.f / (-2.f * (ax + ay));
+  for (int h = 0; h < 2 * CV_NS; ++h) {
+    const int color = h & 1;
+    for (int t = threadIdx.x; t < n * hw; t += blockDim.x) {
+      const int i = t / hw;
+      const int j = ((color - i) & 1) + 2 * (t - i * hw);
+      if (j >= m) continue;
+      const int c = (i + 1) * W + (j + 1);
+      const float nb = ax * (E[c + W] + E[c - W]) + ay * (E[c + 1] + E[c - 1]);
+      float d;
+      if (i > 0 && i < n - 1 && j > 0 && j < m - 1) {
+        d = inv_int;
+      } else {
+        float dd = -2.f * (ax + ay);
+        if (i == 0) dd += ax;
+        if (j == 0) dd += ay;
+        if (j == m - 1) dd += ay;
+        if (i == n - 1) dd += ax * g;
+        d = 1.f / dd;
+      }
+      E[c] = (R[c] - nb) * d;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(CV_BLOCK_THREADS) k_cv_block(CvBlock a) {
+  if (*a.done) return;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  float* E[AJ_MAX_LEVELS + 1];
+  float* R[AJ_MAX_LEVELS + 1];
+  size_t off = 0, total_f = 0;
+  for (int k = a.lc; k <= a.D; ++k) {
+    size_t cnt = (size_t)(a.n[k] + 2) * (a.m[k] + 2);
+    E[k] = reinterpret_cast<float*>(smraw + off);
+    off += cnt * 4;
+    R[k] = reinterpret_cast<float*>(smraw + off);
+    off += cnt * 4;
+    total_f += 2 * cnt;
+  }
+  off = (off + 15) & ~(size_t)15;
+  double* V = reinterpret_cast<double*>(smraw + off);
+  float* all = reinterpret_cast<float*>(smraw);
+  for (size_t t = threadIdx.x; t < total_f; t += blockDim.x) all[t] = 0.f;
+  __syncthreads();
+  {
+    const int n = a.n[a.lc], m = a.m[a.lc], W = m + 2;
+    for (int t = threadIdx.x; t < n * m; t += blockDim.x) {
+      const int i = t / m, j = t - i * m;
+      R[a.lc][(i + 1) * W + (j + 1)] = ldg(a.r_in + t);
+    }
+  }
+  __syncthreads();
+  // down: smooth, residual, restrict
+  for (int k = a.lc; k < a.D; ++k) {
+    const int n = a.n[k], m = a.m[k], W = m + 2;
+    const float ax = a.ax[k], ay = a.ay[k], g = a.g[k];
+    blk_sweeps(E[k], R[k], n, m, ax, ay, g);
+    const int nc = n >> 1, mc = m >> 1, Wc = mc + 2;
+    for (int t = threadIdx.x; t < nc * mc; t += blockDim.x) {
+      const int I = t / mc, J = t - I * mc;
+      float s = 0.f;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int i = 2 * I + (q & 1), j = 2 * J + (q >> 1);
+        const int c = (i + 1) * W + (j + 1);
+        float dd = -2.f * (ax + ay);
+        if (i == 0) dd += ax;
+        if (j == 0) dd += ay;
+        if (j == m - 1) dd += ay;
+        if (i == n - 1) dd += ax * g;
+        const float Ae = ax * (E[k][c + W] + E[k][c - W]) + ay * (E[k][c + 1] + E[k][c - 1]) +
+                         dd * E[k][c];
+        s += R[k][c] - Ae;
+      }
+      R[k + 1][(I + 1) * Wc + (J + 1)] = 0.25f * s;
+    }
+    __syncthreads();
+  }
+  // coarsest: e = A^-1 r in FP64 (one warp per row)
+  {
+    const int n = a.n[a.D], m = a.m[a.D], W = m + 2, N = a.ncoarse;
+    for (int t = threadIdx.x; t < N; t += blockDim.x) {
+      const int i = t / m, j = t - i * m;
+      V[t] = (double)R[a.D][(i + 1) * W + (j + 1)];
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int row = warp; row < N; row += nw) {
+      const double* arow = a.Ainv + (long)row * N;
+      double s = 0.0;
+      for (int c = lane; c < N; c += 32) s += arow[c] * V[c];
+      s = warp_sum(s);
+      if (lane == 0) {
+        const int i = row / m, j = row - i * m;
+        E[a.D][(i + 1) * W + (j + 1)] = (float)s;
+      }
+    }
+    __syncthreads();
+  }
+  // up: prolong, smooth
+  for (int k = a.D - 1; k >= a.lc; --k) {
+    const int n = a.n[k], m = a.m[k], W = m + 2;
+    const int nc = a.n[k + 1], mc = a.m[k + 1], Wc = mc + 2;
+    const float gc = a.g[k + 1];
+    const float* Ec = E[k + 1];
+    for (int t = threadIdx.x; t < n * m; t += blockDim.x) {
+      const int gi = t / m, gj = t - gi * m;
+      const int I = gi >> 1, J = gj >> 1;
+      const int Ii = (gi & 1) ? I + 1 : I - 1;
+      int Jj = (gj & 1) ? J + 1 : J - 1;
+      Jj = Jj < 0 ? 0 : (Jj >= mc ? mc - 1 : Jj);
+      const float c0 = Ec[(I + 1) * Wc + (J + 1)], cy = Ec[(I + 1) * Wc + (Jj + 1)];
+      float cx, cxy;
+      if (Ii < 0) {
+        cx = c0;
+        cxy = cy;
+      } else if (Ii >= nc) {
+        cx = gc * c0;
+        cxy = gc * cy;
+      } else {
+        cx = Ec[(Ii + 1) * Wc + (J + 1)];
+        cxy = Ec[(Ii + 1) * Wc + (Jj + 1)];
+      }
+      E[k][(gi + 1) * W + (gj + 1)] += (9.f * c0 + 3.f * cx + 3.f * cy + cxy) * (1.f / 16.f);
+    }
+    __syncthreads();
+    blk_sweeps(E[k], R[k], n, m, a.ax[k], a.ay[k], a.g[k]);
+  }
+  {
+    const int n = a.n[a.lc], m = a.m[a.lc], W = m + 2;
+    for (int t = threadIdx.x; t < n * m; t += blockDim.x) {
+      const int i = t / m, j = t - i * m;
+      a.e_out[t] = E[a.lc][(i + 1) * W + (j + 1)];
+    }
+  }
+}
+
+// ---------------------------------------------------------------- set-up / solve
+// p = p0 (or 0) as hi, lo = 0, outlet row pinned
+__global__ void k_cv_init(const float* __restrict__ p0, float* __restrict__ ps, int n, int m) {
+  const long N = (long)n * m;
+  long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (k >= N) return;
+  int i = (int)(k / m);
+  ps[k] = (p0 && i != n - 1) ? p0[k] : 0.f;
+  ps[N + k] = 0.f;
+}
+
+// residual of the reference operator before the first cycle (double-FP32)
+// and the FP64 norms of r and b
+__global__ void __launch_bounds__(256) k_cv_resid(const float* __restrict__ ps,
+                                                  const float* __restrict__ b,
+                                                  float* __restrict__ r, int n, int m, DfCoef co,
+                                                  DevScalars* sc) {
+  const long N = (long)n * m;
+  const df ax{co.axh, co.axl}, ay{co.ayh, co.ayl};
+  float acc = 0.f, accb = 0.f;
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < N; k += (long)gridDim.x * blockDim.x) {
+    int i = (int)(k / m), j = (int)(k - (long)i * m);
+    float rr = 0.f;
+    if (i != n - 1) {
+      auto P = [&](long q) { return df{ps[q], ps[N + q]}; };
+      const df c = P(k);
+      const df xp = P((long)(i + 1) * m + j);
+      const df xm = i > 0 ? P((long)(i - 1) * m + j) : c;
+      const df yp = j + 1 < m ? P((long)i * m + j + 1) : c;
+      const df ym = j > 0 ? P((long)i * m + j - 1) : c;
+      const float bb = b[k];
+      const df res = df_residual(bb, c, xp, xm, yp, ym, ax, ay);
+      rr = res.hi + res.lo;
+      accb = fmaf(bb, bb, accb);
+    }
+    r[k] = rr;
+    acc = fmaf(rr, rr, acc);
+  }
+  block_sum_atomic((double)acc, &sc->acc[0]);
+  block_sum_atomic((double)accb, &sc->acc[1]);
+}
+
+__global__ void k_cv_begin(DevScalars* sc) {
+  sc->mg_done = 0;
+  sc->mg_cycles = 0;
+  sc->loops = 0;
+  sc->pcur = 0;
+  sc->red_count = 0u;
+  sc->acc[0] = 0.0;
+  sc->acc[1] = 0.0;
+  sc->err = AJ_OK;
+}
+
+// the test before the first cycle (the initial guess may already satisfy rtol)
+__global__ void k_cv_check0(DevScalars* sc, double rtol) {
+  sc->bnorm = sqrt(sc->acc[1]);
+  double nb = sc->bnorm > 0.0 ? sc->bnorm : 1.0;
+  double rel = sqrt(sc->acc[0]) / nb;
+  sc->rel = rel;
+  sc->abs_sq = sc->acc[0];
+  if (!isfinite(rel)) {
+    sc->err = AJ_ERR_NONFINITE;
+    sc->mg_done = 1;
+  } else if (rel <= rtol) {
+    sc->mg_done = 1;
+  }
+  sc->acc[0] = 0.0;
+  sc->acc[1] = 0.0;
+}
+
+__global__ void k_cv_out(PState ps, const DevScalars* sc, float* __restrict__ p, long N) {
+  long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const float* src = sc->pcur ? ps.b : ps.a;
+  if (k < N) p[k] = src[k] + src[N + k];
+}
+
+static CvBlock block_args(const AjStepParams& p, const Layout& L, void* ws, const int* done) {
+  CvBlock a;
+  memset(&a, 0, sizeof(a));
+  a.lc = L.lc;
+  a.D = L.nlev;
+  a.ncoarse = L.ncoarse;
+  for (int k = 0; k <= L.nlev; ++k) {
+    CvLvl c = cv_level(p, L, k);
+    a.n[k] = c.n;
+    a.m[k] = c.m;
+    a.ax[k] = c.ax;
+    a.ay[k] = c.ay;
+    a.g[k] = c.g;
+  }
+  a.r_in = at<float>(ws, L.B[L.lc]);
+  a.e_out = at<float>(ws, L.T[L.lc]);
+  a.Ainv = at<double>(ws, L.cinv);
+  a.done = done;
+  return a;
+}
+
+static PState pstate(const Layout& L, void* ws) {
+  return PState{at<float>(ws, L.p64), at<float>(ws, L.p64b)};
+}
+
+template <class TL, int TI, int TJ>
+static dim3 tiles(const CvLvl& c) {
+  return dim3(cdiv(c.m, TJ), cdiv(c.n, TI));
+}
+
+// one refinement iteration
+static void cv_body(const AjStepParams& p, const Layout& L, void* ws,
+                    cudaGraphConditionalHandle h, int use_handle, cudaStream_t st) {
+  DevScalars* sc = at<DevScalars>(ws, 0);
+  const int* done = &sc->mg_done;
+  const int lc = L.lc;
+  dim3 blk(32, 8);
+  for (int l = 0; l < lc; ++l) {
+    CvLvl c = cv_level(p, L, l);
+    if (l == 0)
+      k_cv_down<32, 64><<<tiles<TileL0, 32, 64>(c), blk, 0, st>>>(
+          c, at<float>(ws, L.B[l]), at<float>(ws, L.X[l]), at<float>(ws, L.B[l + 1]), done);
+    else
+      k_cv_down<16, 32><<<tiles<TileLc, 16, 32>(c), blk, 0, st>>>(
+          c, at<float>(ws, L.B[l]), at<float>(ws, L.X[l]), at<float>(ws, L.B[l + 1]), done);
+  }
+  k_cv_block<<<1, CV_BLOCK_THREADS, converge_block_smem(L, lc), st>>>(block_args(p, L, ws, done));
+  for (int l = lc - 1; l >= 1; --l) {
+    CvLvl c = cv_level(p, L, l);
+    k_cv_up<16, 32><<<tiles<TileLc, 16, 32>(c), blk, 0, st>>>(
+        c, at<float>(ws, L.B[l]), at<float>(ws, L.X[l]), at<float>(ws, L.T[l + 1]), L.ln[l + 1],
+        L.lm[l + 1], (float)ghost_factor(l + 1), at<float>(ws, L.T[l]), done);
+  }
+  CvLvl c0 = cv_level(p, L, 0);
+  CvCheck ck{p.mg_rtol, p.max_cycles, use_handle, h};
+  k_cv_up0<<<tiles<TileL0, 32, 64>(c0), blk, 0, st>>>(
+      c0, at<float>(ws, L.B[0]), at<float>(ws, L.X[0]), at<float>(ws, L.T[1]), L.ln[1], L.lm[1],
+      (float)ghost_factor(1), pstate(L, ws), at<float>(ws, L.b0), at<float>(ws, L.B[0]), sc,
+      df_coef(1.0 / (p.dx * p.dx), 1.0 / (p.dy * p.dy)), ck, 0);
+}
+
+static cudaStream_t side_stream() {
+  static cudaStream_t s = nullptr;
+  if (!s) cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  return s;
+}
+
+int converge_solve(const AjStepParams& p, const Layout& L, void* ws, const float* p0,
+                   float* pout, cudaStream_t st) {
+  DevScalars* sc = at<DevScalars>(ws, 0);
+  const long N = (long)p.nx * p.ny;
+  const PState ps = pstate(L, ws);
+  k_cv_begin<<<1, 1, 0, st>>>(sc);
+  k_cv_init<<<cdiv(N, 256), 256, 0, st>>>(p.warm_start ? p0 : nullptr, ps.a, p.nx, p.ny);
+  unsigned nb = cdiv(N, 256 * 4);
+  if (nb > 1216) nb = 1216;
+  k_cv_resid<<<nb, 256, 0, st>>>(ps.a, at<float>(ws, L.b0), at<float>(ws, L.B[0]), p.nx, p.ny,
+                                 df_coef(1.0 / (p.dx * p.dx), 1.0 / (p.dy * p.dy)), sc);
+  k_cv_check0<<<1, 1, 0, st>>>(sc, p.mg_rtol);
+
+  cudaStreamCaptureStatus cs;
+  unsigned long long id;
+  cudaGraph_t g;
+  const cudaGraphNode_t* deps;
+  const cudaGraphEdgeData* ed;
+  size_t nd;
+  if (cudaStreamGetCaptureInfo(st, &cs, &id, &g, &deps, &ed, &nd) != cudaSuccess)
+    return AJ_ERR_CUDA;
+  if (cs != cudaStreamCaptureStatusActive) {
+    // eager launches (profiling mode): a fixed number of loop bodies, each
+    // skipping its work once the target is met
+    int unroll = eager_unroll(p.max_cycles);
+    for (int k = 0; k < unroll; ++k) cv_body(p, L, ws, 0, 0, st);
+  } else {
+    // the refinement loop: a while node appended to the graph being captured
+    cudaGraphConditionalHandle h;
+    if (cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault) != cudaSuccess)
+      return AJ_ERR_CUDA;
+    // the params union has no default constructor: zero-initialised storage
+    alignas(cudaGraphNodeParams) unsigned char npbuf[sizeof(cudaGraphNodeParams)];
+    memset(npbuf, 0, sizeof(npbuf));
+    cudaGraphNodeParams& np = *reinterpret_cast<cudaGraphNodeParams*>(npbuf);
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    if (cudaGraphAddNode(&node, g, deps, ed, nd, &np) != cudaSuccess) return AJ_ERR_CUDA;
+    if (cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1,
+                                            cudaStreamSetCaptureDependencies) != cudaSuccess)
+      return AJ_ERR_CUDA;
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    cudaStream_t side = side_stream();
+    if (cudaStreamBeginCaptureToGraph(side, body, nullptr, nullptr, 0,
+                                      cudaStreamCaptureModeRelaxed) != cudaSuccess)
+      return AJ_ERR_CUDA;
+    cv_body(p, L, ws, h, 1, side);
+    cudaGraph_t out;
+    if (cudaStreamEndCapture(side, &out) != cudaSuccess) return AJ_ERR_CUDA;
+  }
+  k_cv_out<<<cdiv(N, 256), 256, 0, st>>>(ps, sc, pout, N);
+  return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+}
+
+// dense matrix of the coarsest converging-mode operator, inverted on the host
+static bool coarse_inverse(const AjStepParams& p, const Layout& L, std::vector<double>& inv) {
+  const int l = L.nlev, n = L.ln[l], m = L.lm[l], N = n * m;
+  double hx = p.dx * (double)(1 << l), hy = p.dy * (double)(1 << l);
+  double ax = 1.0 / (hx * hx), ay = 1.0 / (hy * hy), g = ghost_factor(l);
+  std::vector<double> A((size_t)N * N, 0.0);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < m; ++j) {
+      int r = i * m + j;
+      double d = -2.0 * (ax + ay);
+      if (i == 0) d += ax; else A[(size_t)r * N + (i - 1) * m + j] += ax;
+      if (i == n - 1) d += ax * g; else A[(size_t)r * N + (i + 1) * m + j] += ax;
+      if (j == 0) d += ay; else A[(size_t)r * N + i * m + j - 1] += ay;
+      if (j == m - 1) d += ay; else A[(size_t)r * N + i * m + j + 1] += ay;
+      A[(size_t)r * N + r] += d;
+    }
+  inv.assign((size_t)N * N, 0.0);
+  for (int i = 0; i < N; ++i) inv[(size_t)i * N + i] = 1.0;
+  for (int c = 0; c < N; ++c) {          // Gauss-Jordan with partial pivoting
+    int piv = c;
+    for (int r = c + 1; r < N; ++r)
+      if (fabs(A[(size_t)r * N + c]) > fabs(A[(size_t)piv * N + c])) piv = r;
+    if (fabs(A[(size_t)piv * N + c]) < 1e-300) return false;
+    if (piv != c)
+      for (int k = 0; k < N; ++k) {
+        std::swap(A[(size_t)c * N + k], A[(size_t)piv * N + k]);
+        std::swap(inv[(size_t)c * N + k], inv[(size_t)piv * N + k]);
+      }
+    double s = 1.0 / A[(size_t)c * N + c];
+    for (int k = 0; k < N; ++k) {
+      A[(size_t)c * N + k] *= s;
+      inv[(size_t)c * N + k] *= s;
+    }
+    for (int r = 0; r < N; ++r) {
+      if (r == c) continue;
+      double f = A[(size_t)r * N + c];
+      if (f == 0.0) continue;
+      for (int k = 0; k < N; ++k) {
+        A[(size_t)r * N + k] -= f * A[(size_t)c * N + k];
+        inv[(size_t)r * N + k] -= f * inv[(size_t)c * N + k];
+      }
+    }
+  }
+  return true;
+}
+
+int converge_first_block_level(const Layout& L) {
+  // the coarsest level always; finer ones while they are small enough and fit
+  int lc = L.nlev;
+  for (int l = L.nlev - 1; l >= 1; --l) {
+    if ((long)L.ln[l] * L.lm[l] > CV_BLOCK_MAX_CELLS) break;
+    if (converge_block_smem(L, l) > kBlockSmemMax) break;
+    lc = l;
+  }
+  return lc;
+}
+
+int converge_prepare(const AjStepParams& p, const Layout& L, void* ws, cudaStream_t st) {
+  std::vector<double> inv;
+  if (!coarse_inverse(p, L, inv)) return AJ_ERR_PARAM;
+  if (cudaFuncSetAttribute(k_cv_block, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)kBlockSmemMax + 1024) != cudaSuccess)
+    return AJ_ERR_CUDA;
+  if (cudaMemcpyAsync(at<double>(ws, L.cinv), inv.data(), inv.size() * sizeof(double),
+                      cudaMemcpyHostToDevice, st) != cudaSuccess)
+    return AJ_ERR_CUDA;
+  return cudaStreamSynchronize(st) == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+}
+
+// One launch of a converging-mode kernel on the workspace's current contents
+// (instrumentation: lets a caller time the kernel on its own).  which:
+// 0 = level-0 smoothing + residual + restriction, 1 = level-0 prolongation +
+// smoothing + pressure update + residual (the solver state is left untouched),
+// 2 = the one-block coarse-level kernel.
+int profile_pressure_kernel(const AjStepParams& p, const Layout& L, void* ws, int which,
+                            cudaStream_t st) {
+  if (p.mg_mode != AJ_MG_CONVERGE) return AJ_ERR_PARAM;
+  DevScalars* sc = at<DevScalars>(ws, 0);
+  const int* never = reinterpret_cast<const int*>(&sc->pad_[0]);   // always 0
+  dim3 blk(32, 8);
+  CvLvl c = cv_level(p, L, 0);
+  if (which == 0) {
+    k_cv_down<32, 64><<<tiles<TileL0, 32, 64>(c), blk, 0, st>>>(
+        c, at<float>(ws, L.B[0]), at<float>(ws, L.X[0]), at<float>(ws, L.B[1]), never);
+  } else if (which == 1) {
+    CvCheck ck{p.mg_rtol, p.max_cycles, 0, 0};
+    // profile mode reads the current state buffer and writes only the other one
+    k_cv_up0<<<tiles<TileL0, 32, 64>(c), blk, 0, st>>>(
+        c, at<float>(ws, L.B[0]), at<float>(ws, L.X[0]), at<float>(ws, L.T[1]), L.ln[1], L.lm[1],
+        (float)ghost_factor(1), pstate(L, ws), at<float>(ws, L.b0), at<float>(ws, L.B[0]), sc,
+        df_coef(1.0 / (p.dx * p.dx), 1.0 / (p.dy * p.dy)), ck, 1);
+  } else if (which == 2) {
+    k_cv_block<<<1, CV_BLOCK_THREADS, converge_block_smem(L, L.lc), st>>>(
+        block_args(p, L, ws, never));
+  } else {
+    return AJ_ERR_PARAM;
+  }
+  return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+}
+
+}  // namespace aj

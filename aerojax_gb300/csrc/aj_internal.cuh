@@ -7,7 +7,8 @@
 #include "../../include/aerojax_gb300.h"
 
 #define AJ_MAX_LEVELS 12
-#define AJ_MAX_COARSE 512          // cells of the converging-mode coarsest grid
+#define AJ_MAX_COARSE 64           // target cells of the converging-mode coarsest grid
+#define AJ_MAX_COARSE_HARD 1024    // largest coarsest grid accepted (odd-sized grids)
 #define AJ_PARITY_TOL_DEFAULT 1e-6
 
 namespace aj {
@@ -28,6 +29,7 @@ struct DevScalars {
   double abs_sq;       // sum r^2 dx dy
   unsigned int red_count;
   int loops;           // converging mode: executions of the while body
+  int pcur;            // converging mode: which FP64 pressure buffer is current
   unsigned int pad_[3];
 };
 
@@ -42,8 +44,9 @@ struct Layout {
   size_t b0 = 0, T0 = 0;                                // multigrid level-0 rhs, scratch
   size_t X[AJ_MAX_LEVELS + 1] = {0}, T[AJ_MAX_LEVELS + 1] = {0};
   size_t B[AJ_MAX_LEVELS + 1] = {0}, M[AJ_MAX_LEVELS + 1] = {0};
-  size_t p64 = 0;                                       // converging mode FP64 pressure
+  size_t p64 = 0, p64b = 0;                             // converging mode FP64 pressure (ping-pong)
   size_t cinv = 0;                                      // coarsest-grid inverse (FP64)
+  int lc = 0;                                           // first level of the one-block coarse kernel
   size_t part = 0;                                      // per-block partial sums (FP64)
   size_t total = 0;
   // multigrid hierarchy
@@ -77,6 +80,29 @@ __device__ __forceinline__ void atomic_max_nonneg(unsigned int* addr, float v) {
   atomicMax(addr, __float_as_uint(v));
 }
 
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block-wide sum of one double per thread, added atomically to *dst by one
+// thread.  Every thread of the block must call it (it synchronises).
+__device__ __forceinline__ void block_sum_atomic(double v, double* dst) {
+  __shared__ double ws_[32];
+  v = warp_sum(v);
+  const int nthreads = blockDim.x * blockDim.y;
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  const int lane = tid & 31, w = tid >> 5;
+  if (lane == 0) ws_[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    v = lane < (nthreads >> 5) ? ws_[lane] : 0.0;
+    v = warp_sum(v);
+    if (lane == 0) atomicAdd(dst, v);
+  }
+  __syncthreads();
+}
+
 // ------------------------------------------------------------------ launchers
 // predictor (aj_predictor.cu)
 int launch_predictor(const AjStepParams& p, const Layout& L, void* ws, const float* u,
@@ -104,6 +130,13 @@ int launch_pressure(const AjStepParams& p, const Layout& L, void* ws, const floa
                     const float* p0, float* pout, AjStats* stats, cudaStream_t st);
 int profile_pressure_kernel(const AjStepParams& p, const Layout& L, void* ws, int which,
                             cudaStream_t st);
+// converging multigrid (aj_converge.cu)
+int converge_prepare(const AjStepParams& p, const Layout& L, void* ws, cudaStream_t st);
+int converge_solve(const AjStepParams& p, const Layout& L, void* ws, const float* p0,
+                   float* pout, cudaStream_t st);
+size_t converge_block_smem(const Layout& L, int lc);
+int converge_first_block_level(const Layout& L);
+constexpr size_t kBlockSmemMax = 200 * 1024;   // coarse-level kernel shared memory budget
 
 inline unsigned cdiv(long a, long b) { return (unsigned)((a + b - 1) / b); }
 

@@ -9,42 +9,11 @@
 // The second post-smoothing sweep and the prolongation are fused (the sweep
 // evaluates p + P(e) on the fly), so each level costs five kernels.
 //
-// Converging mode (new) solves the same discrete operator to a relative
-// residual: FP64 iterative refinement (r = b - A p in FP64, one FP32 V-cycle on
-// A e = r, p += e) with red-black Gauss-Seidel smoothing in shared-memory tiles,
-// rediscretised coarse operators, cell-centred bilinear prolongation, an FP64
-// dense solve on the coarsest grid and FP64 norms.  The refinement loop is a
-// CUDA-graph while node whose condition the check kernel sets on the device.
+// The converging mode lives in aj_converge.cu; this file dispatches to it.
 #include "aj_internal.cuh"
 #include <math.h>
-#include <vector>
-#include <string.h>
 
 namespace aj {
-
-// ====================================================================== common
-__device__ __forceinline__ double warp_sum(double v) {
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
-// block-wide sum of one double into *dst (atomic); blockDim multiple of 32
-__device__ __forceinline__ void block_sum_atomic(double v, double* dst) {
-  __shared__ double ws_[32];
-  v = warp_sum(v);
-  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  int nthreads = blockDim.x * blockDim.y;
-  int tid = threadIdx.y * blockDim.x + threadIdx.x;
-  lane = tid & 31;
-  w = tid >> 5;
-  if (lane == 0) ws_[w] = v;
-  __syncthreads();
-  if (w == 0) {
-    v = lane < (nthreads >> 5) ? ws_[lane] : 0.0;
-    v = warp_sum(v);
-    if (lane == 0) atomicAdd(dst, v);
-  }
-}
 
 // b = rhs (* mask for MAC), b[-1, :] = 0 (multigrid_solver.py:75-77,
 // multigrid_solver_mac.py:78-83)
@@ -324,432 +293,6 @@ static int parity_solve(const AjStepParams& p, const Layout& L, void* ws, const 
   return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
 }
 
-// ==================================================================== converge
-// Tiles: 32 rows (x) by 64 columns (y); two red-black sweeps per smoothing phase.
-constexpr int CV_TI = 32, CV_TJ = 64, CV_NS = 2;
-constexpr int CV_HD = 2 * CV_NS + 1;   // down kernel halo (sweeps + residual)
-constexpr int CV_HU = 2 * CV_NS;       // up kernel halo
-constexpr int CV_SID = CV_TI + 2 * CV_HD, CV_SJD = CV_TJ + 2 * CV_HD;
-constexpr int CV_SIU = CV_TI + 2 * CV_HU, CV_SJU = CV_TJ + 2 * CV_HU;
-
-struct CvLvl {
-  int n, m, level;
-  float ax, ay, g;   // g: outlet ghost factor of this level (level >= 1)
-};
-
-__device__ __forceinline__ float cv_diag(const CvLvl& L, int gi, int gj) {
-  float d = -2.f * (L.ax + L.ay);
-  if (gi == 0) d += L.ax;
-  if (gj == 0) d += L.ay;
-  if (gj == L.m - 1) d += L.ay;
-  if (gi == L.n - 1) d += (L.level == 0) ? L.ax : L.ax * L.g;
-  return d;
-}
-
-// red-black half-sweeps over a shared-memory tile; cells outside the domain
-// hold zero and never change (the diagonal carries the ghost rule).  Every
-// half-sweep covers the whole tile: after half-sweep h the cells at distance
-// >= h+1 from the tile border hold exact red-black values, and the cells
-// nearer the border (stale neighbours) lie outside every value that is stored.
-template <int SI, int SJ>
-__device__ __forceinline__ void cv_sweeps(float* E, const float* R, const CvLvl& L, int gi0,
-                                          int gj0, int nhalf) {
-  constexpr int ROWS = SI - 2, HW = (SJ - 1) / 2;   // cells of one colour per row (upper bound)
-  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-  const int nth = blockDim.x * blockDim.y;
-  const float inv_int = 1.f / (-2.f * (L.ax + L.ay));
-  for (int h = 0; h < nhalf; ++h) {
-    const int color = h & 1;
-    for (int t = tid; t < ROWS * HW; t += nth) {
-      const int r = t / HW, kk = t - r * HW;
-      const int ti = 1 + r;
-      const int tj = 1 + ((color - ti - 1) & 1) + 2 * kk;
-      if (tj >= SJ - 1) continue;
-      const int gi = gi0 + ti, gj = gj0 + tj;
-      if ((unsigned)gi >= (unsigned)L.n || (unsigned)gj >= (unsigned)L.m) continue;
-      if (L.level == 0 && gi == L.n - 1) continue;          // pinned outlet row
-      const int c = ti * SJ + tj;
-      const float nb = L.ax * (E[c + SJ] + E[c - SJ]) + L.ay * (E[c + 1] + E[c - 1]);
-      const bool inner = gi > 0 && gi < L.n - 1 && gj > 0 && gj < L.m - 1;
-      E[c] = (R[c] - nb) * (inner ? inv_int : 1.f / cv_diag(L, gi, gj));
-    }
-    __syncthreads();
-  }
-}
-
-// pre-smoothing from e = 0, residual, 2x2 average onto the coarse rhs
-__global__ void __launch_bounds__(256) k_cv_down(CvLvl L, const float* __restrict__ r,
-                                                 float* __restrict__ e_out,
-                                                 float* __restrict__ rc, const int* done) {
-  if (*done) return;
-  __shared__ float E[CV_SID * CV_SJD];
-  __shared__ float R[CV_SID * CV_SJD];
-  const int i0 = blockIdx.y * CV_TI, j0 = blockIdx.x * CV_TJ;
-  const int gi0 = i0 - CV_HD, gj0 = j0 - CV_HD;
-  const int tid = threadIdx.y * blockDim.x + threadIdx.x, nth = blockDim.x * blockDim.y;
-  for (int t = tid; t < CV_SID * CV_SJD; t += nth) {
-    int ti = t / CV_SJD, tj = t - ti * CV_SJD;
-    int gi = gi0 + ti, gj = gj0 + tj;
-    bool in = gi >= 0 && gi < L.n && gj >= 0 && gj < L.m;
-    E[t] = 0.f;
-    R[t] = in ? ldg(r + (long)gi * L.m + gj) : 0.f;
-  }
-  __syncthreads();
-  cv_sweeps<CV_SID, CV_SJD>(E, R, L, gi0, gj0, 2 * CV_NS);
-  // store e and compute the residual on the tile interior (in place in R)
-  for (int t = tid; t < CV_TI * CV_TJ; t += nth) {
-    int ti = CV_HD + t / CV_TJ, tj = CV_HD + t % CV_TJ;
-    int gi = gi0 + ti, gj = gj0 + tj;
-    if (gi >= L.n || gj >= L.m) continue;
-    const int c = ti * CV_SJD + tj;
-    e_out[(long)gi * L.m + gj] = E[c];
-    float res = 0.f;
-    if (!(L.level == 0 && gi == L.n - 1)) {
-      float nb = L.ax * (E[c + CV_SJD] + E[c - CV_SJD]) + L.ay * (E[c + 1] + E[c - 1]);
-      res = R[c] - (nb + cv_diag(L, gi, gj) * E[c]);
-    }
-    R[c] = res;
-  }
-  __syncthreads();
-  const int mc = L.m >> 1, nc = L.n >> 1;
-  for (int t = tid; t < (CV_TI / 2) * (CV_TJ / 2); t += nth) {
-    int ci = t / (CV_TJ / 2), cj = t % (CV_TJ / 2);
-    int I = (i0 >> 1) + ci, J = (j0 >> 1) + cj;
-    if (I >= nc || J >= mc) continue;
-    int c = (CV_HD + 2 * ci) * CV_SJD + CV_HD + 2 * cj;
-    rc[(long)I * mc + J] = 0.25f * (R[c] + R[c + CV_SJD] + R[c + 1] + R[c + CV_SJD + 1]);
-  }
-}
-
-// cell-centred bilinear prolongation of the coarse correction (ghosts:
-// Neumann copies at inlet and walls, outlet ghost g * value)
-__device__ __forceinline__ float cv_prolong(const float* __restrict__ ec, int nc, int mc, float g,
-                                            int gi, int gj) {
-  int I = gi >> 1, J = gj >> 1;
-  int Ii = (gi & 1) ? I + 1 : I - 1;
-  int Jj = (gj & 1) ? J + 1 : J - 1;
-  Jj = Jj < 0 ? 0 : (Jj >= mc ? mc - 1 : Jj);
-  auto cval = [&](int a, int b) -> float {
-    if (a < 0) a = 0;
-    if (a >= nc) return g * ldg(ec + (long)(nc - 1) * mc + b);
-    return ldg(ec + (long)a * mc + b);
-  };
-  float c0 = ldg(ec + (long)I * mc + J);
-  return (9.f * c0 + 3.f * cval(Ii, J) + 3.f * cval(I, Jj) + cval(Ii, Jj)) * (1.f / 16.f);
-}
-
-// e + P(e_coarse), post-smoothing, store (level 0: p64 += e instead)
-__global__ void __launch_bounds__(256) k_cv_up(CvLvl L, const float* __restrict__ r,
-                                               const float* __restrict__ e_in,
-                                               const float* __restrict__ ec, int nc, int mc,
-                                               float gc, float* __restrict__ e_out,
-                                               double* __restrict__ p64, const int* done) {
-  if (*done) return;
-  __shared__ float E[CV_SIU * CV_SJU];
-  __shared__ float R[CV_SIU * CV_SJU];
-  const int i0 = blockIdx.y * CV_TI, j0 = blockIdx.x * CV_TJ;
-  const int gi0 = i0 - CV_HU, gj0 = j0 - CV_HU;
-  const int tid = threadIdx.y * blockDim.x + threadIdx.x, nth = blockDim.x * blockDim.y;
-  for (int t = tid; t < CV_SIU * CV_SJU; t += nth) {
-    int ti = t / CV_SJU, tj = t - ti * CV_SJU;
-    int gi = gi0 + ti, gj = gj0 + tj;
-    bool in = gi >= 0 && gi < L.n && gj >= 0 && gj < L.m;
-    float e = 0.f, rr = 0.f;
-    if (in) {
-      long k = (long)gi * L.m + gj;
-      rr = ldg(r + k);
-      if (!(L.level == 0 && gi == L.n - 1)) e = ldg(e_in + k) + cv_prolong(ec, nc, mc, gc, gi, gj);
-    }
-    E[t] = e;
-    R[t] = rr;
-  }
-  __syncthreads();
-  cv_sweeps<CV_SIU, CV_SJU>(E, R, L, gi0, gj0, 2 * CV_NS);
-  for (int t = tid; t < CV_TI * CV_TJ; t += nth) {
-    int ti = CV_HU + t / CV_TJ, tj = CV_HU + t % CV_TJ;
-    int gi = gi0 + ti, gj = gj0 + tj;
-    if (gi >= L.n || gj >= L.m) continue;
-    long k = (long)gi * L.m + gj;
-    float e = E[ti * CV_SJU + tj];
-    if (p64) p64[k] += (double)e;
-    else e_out[k] = e;
-  }
-}
-
-// coarsest grid: e = A^-1 r with the FP64 inverse (one warp per row)
-__global__ void k_cv_coarse(const double* __restrict__ Ainv, const float* __restrict__ rc,
-                            float* __restrict__ ec, int N, const int* done) {
-  if (*done) return;
-  extern __shared__ double rs[];
-  for (int t = threadIdx.x; t < N; t += blockDim.x) rs[t] = (double)rc[t];
-  __syncthreads();
-  int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  int row = blockIdx.x * (blockDim.x >> 5) + warp;
-  if (row >= N) return;
-  const double* a = Ainv + (long)row * N;
-  double s = 0.0;
-  for (int c = lane; c < N; c += 32) s += a[c] * rs[c];
-  s = warp_sum(s);
-  if (lane == 0) ec[row] = (float)s;
-}
-
-// p64 = p0 (or 0), outlet row pinned
-__global__ void k_cv_init(const float* __restrict__ p0, double* __restrict__ p64, int n, int m) {
-  long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (k >= (long)n * m) return;
-  int i = (int)(k / m);
-  p64[k] = (p0 && i != n - 1) ? (double)p0[k] : 0.0;
-}
-
-// FP64 residual of the reference operator: r = b - A p (edge ghosts, outlet
-// row pinned at 0 and excluded), stored as FP32 for the V-cycle; FP64 sums
-__global__ void __launch_bounds__(256) k_cv_resid(const double* __restrict__ p64,
-                                                  const float* __restrict__ b,
-                                                  float* __restrict__ r, int n, int m, double ax,
-                                                  double ay, DevScalars* sc, int first) {
-  if (!first && sc->mg_done) return;
-  double acc = 0.0, accb = 0.0;
-  long N = (long)n * m;
-  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < N; k += (long)gridDim.x * blockDim.x) {
-    int i = (int)(k / m), j = (int)(k - (long)i * m);
-    double rr = 0.0;
-    if (i != n - 1) {
-      double c = p64[k];
-      double xp = p64[(long)(i + 1) * m + j];
-      double xm = p64[(long)(i > 0 ? i - 1 : 0) * m + j];
-      double yp = p64[(long)i * m + (j + 1 < m ? j + 1 : m - 1)];
-      double ym = p64[(long)i * m + (j > 0 ? j - 1 : 0)];
-      double bb = (double)b[k];
-      rr = bb - (ax * (xp + xm - 2.0 * c) + ay * (yp + ym - 2.0 * c));
-      accb += bb * bb;
-    }
-    r[k] = (float)rr;
-    acc += rr * rr;
-  }
-  block_sum_atomic(acc, &sc->acc[0]);
-  if (first) {
-    __syncthreads();
-    block_sum_atomic(accb, &sc->acc[1]);
-  }
-}
-
-__global__ void k_cv_begin(DevScalars* sc) {
-  sc->mg_done = 0;
-  sc->loops = 0;
-  sc->mg_cycles = 0;
-  sc->acc[0] = 0.0;
-  sc->acc[1] = 0.0;
-  sc->err = AJ_OK;
-}
-
-// relative residual test; drives the graph's while node when h != 0
-__global__ void k_cv_check(DevScalars* sc, double rtol, int max_cycles, int first,
-                           cudaGraphConditionalHandle h, int use_handle) {
-  if (first) {
-    sc->bnorm = sqrt(sc->acc[1]);
-  } else if (!sc->mg_done) {
-    sc->mg_cycles += 1;
-  }
-  if (first || !sc->mg_done) {
-    double nb = sc->bnorm > 0.0 ? sc->bnorm : 1.0;
-    double rel = sqrt(sc->acc[0]) / nb;
-    sc->rel = rel;
-    sc->abs_sq = sc->acc[0];
-    if (!isfinite(rel)) {
-      sc->err = AJ_ERR_NONFINITE;
-      sc->mg_done = 1;
-    } else if (rel <= rtol) {
-      sc->mg_done = 1;
-    } else if (sc->mg_cycles >= max_cycles) {
-      sc->err = AJ_ERR_NOT_CONVERGED;
-      sc->mg_done = 1;
-    }
-  }
-  sc->acc[0] = 0.0;
-  sc->acc[1] = 0.0;
-  if (use_handle) {
-    // independent bound on the while node: never more bodies than max_cycles + 1
-    sc->loops += 1;
-    if (sc->loops > max_cycles + 1 && !sc->mg_done) {
-      sc->err = AJ_ERR_NOT_CONVERGED;
-      sc->mg_done = 1;
-    }
-    cudaGraphSetConditional(h, sc->mg_done ? 0u : 1u);
-  }
-}
-
-__global__ void k_cv_out(const double* __restrict__ p64, float* __restrict__ p, long N) {
-  long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (k < N) p[k] = (float)p64[k];
-}
-
-static double ghost_factor(int level) {
-  double th = 0.5 * (1.0 - pow(2.0, -level));
-  return (th - 1.0) / th;
-}
-
-static CvLvl cv_level(const AjStepParams& p, const Layout& L, int l) {
-  CvLvl c;
-  c.n = L.ln[l];
-  c.m = L.lm[l];
-  c.level = l;
-  double hx = p.dx * (double)(1 << l), hy = p.dy * (double)(1 << l);
-  c.ax = (float)(1.0 / (hx * hx));
-  c.ay = (float)(1.0 / (hy * hy));
-  c.g = l > 0 ? (float)ghost_factor(l) : 0.f;
-  return c;
-}
-
-// the body of one refinement iteration: V-cycle, then residual + check
-static void cv_body(const AjStepParams& p, const Layout& L, void* ws,
-                    cudaGraphConditionalHandle h, int use_handle, cudaStream_t st) {
-  DevScalars* sc = at<DevScalars>(ws, 0);
-  const int* done = &sc->mg_done;
-  const int D = L.nlev;
-  dim3 blk(32, 8);
-  double* p64 = at<double>(ws, L.p64);
-  for (int l = 0; l < D; ++l) {
-    CvLvl c = cv_level(p, L, l);
-    dim3 g(cdiv(c.m, CV_TJ), cdiv(c.n, CV_TI));
-    k_cv_down<<<g, blk, 0, st>>>(c, at<float>(ws, L.B[l]), at<float>(ws, L.X[l]),
-                                 at<float>(ws, L.B[l + 1]), done);
-  }
-  {
-    int N = L.ncoarse;
-    int rows_per_block = 8;
-    k_cv_coarse<<<cdiv(N, rows_per_block), 256, N * sizeof(double), st>>>(
-        at<double>(ws, L.cinv), at<float>(ws, L.B[D]), at<float>(ws, L.T[D]), N, done);
-  }
-  for (int l = D - 1; l >= 0; --l) {
-    CvLvl c = cv_level(p, L, l);
-    dim3 g(cdiv(c.m, CV_TJ), cdiv(c.n, CV_TI));
-    float gc = (float)ghost_factor(l + 1);
-    k_cv_up<<<g, blk, 0, st>>>(c, at<float>(ws, L.B[l]), at<float>(ws, L.X[l]),
-                               at<float>(ws, L.T[l + 1]), L.ln[l + 1], L.lm[l + 1], gc,
-                               l == 0 ? nullptr : at<float>(ws, L.T[l]), l == 0 ? p64 : nullptr,
-                               done);
-  }
-  long N = (long)p.nx * p.ny;
-  unsigned nb = cdiv(N, 256 * 4);
-  if (nb > 1216) nb = 1216;
-  k_cv_resid<<<nb, 256, 0, st>>>(p64, at<float>(ws, L.b0), at<float>(ws, L.B[0]), p.nx, p.ny,
-                                 1.0 / (p.dx * p.dx), 1.0 / (p.dy * p.dy), sc, 0);
-  k_cv_check<<<1, 1, 0, st>>>(sc, p.mg_rtol, p.max_cycles, 0, h, use_handle);
-}
-
-static cudaStream_t side_stream() {
-  static cudaStream_t s = nullptr;
-  if (!s) cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
-  return s;
-}
-
-static int converge_solve(const AjStepParams& p, const Layout& L, void* ws, const float* p0,
-                          float* pout, cudaStream_t st) {
-  DevScalars* sc = at<DevScalars>(ws, 0);
-  long N = (long)p.nx * p.ny;
-  double* p64 = at<double>(ws, L.p64);
-  k_cv_begin<<<1, 1, 0, st>>>(sc);
-  k_cv_init<<<cdiv(N, 256), 256, 0, st>>>(p.warm_start ? p0 : nullptr, p64, p.nx, p.ny);
-  unsigned nb = cdiv(N, 256 * 4);
-  if (nb > 1216) nb = 1216;
-  k_cv_resid<<<nb, 256, 0, st>>>(p64, at<float>(ws, L.b0), at<float>(ws, L.B[0]), p.nx, p.ny,
-                                 1.0 / (p.dx * p.dx), 1.0 / (p.dy * p.dy), sc, 1);
-  k_cv_check<<<1, 1, 0, st>>>(sc, p.mg_rtol, p.max_cycles, 1, 0, 0);
-
-  // the refinement loop: a while node appended to the graph being captured
-  cudaStreamCaptureStatus cs;
-  unsigned long long id;
-  cudaGraph_t g;
-  const cudaGraphNode_t* deps;
-  const cudaGraphEdgeData* ed;
-  size_t nd;
-  if (cudaStreamGetCaptureInfo(st, &cs, &id, &g, &deps, &ed, &nd) != cudaSuccess)
-    return AJ_ERR_CUDA;
-  if (cs != cudaStreamCaptureStatusActive) {
-    // eager launches (profiling mode, see aj_api.cu): a fixed number of loop
-    // bodies, each skipping its work once the target is met
-    int unroll = eager_unroll(p.max_cycles);
-    for (int k = 0; k < unroll; ++k) cv_body(p, L, ws, 0, 0, st);
-    k_cv_out<<<cdiv(N, 256), 256, 0, st>>>(p64, pout, N);
-    return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
-  }
-  cudaGraphConditionalHandle h;
-  if (cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault) != cudaSuccess)
-    return AJ_ERR_CUDA;
-  // the params union has no default constructor: zero-initialised storage
-  alignas(cudaGraphNodeParams) unsigned char npbuf[sizeof(cudaGraphNodeParams)];
-  memset(npbuf, 0, sizeof(npbuf));
-  cudaGraphNodeParams& np = *reinterpret_cast<cudaGraphNodeParams*>(npbuf);
-  np.type = cudaGraphNodeTypeConditional;
-  np.conditional.handle = h;
-  np.conditional.type = cudaGraphCondTypeWhile;
-  np.conditional.size = 1;
-  cudaGraphNode_t node;
-  if (cudaGraphAddNode(&node, g, deps, ed, nd, &np) != cudaSuccess) return AJ_ERR_CUDA;
-  if (cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies) !=
-      cudaSuccess)
-    return AJ_ERR_CUDA;
-  cudaGraph_t body = np.conditional.phGraph_out[0];
-  cudaStream_t side = side_stream();
-  if (cudaStreamBeginCaptureToGraph(side, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) !=
-      cudaSuccess)
-    return AJ_ERR_CUDA;
-  cv_body(p, L, ws, h, 1, side);
-  cudaGraph_t out;
-  if (cudaStreamEndCapture(side, &out) != cudaSuccess) return AJ_ERR_CUDA;
-
-  k_cv_out<<<cdiv(N, 256), 256, 0, st>>>(p64, pout, N);
-  return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
-}
-
-// ===================================================================== set-up
-// dense matrix of the coarsest converging-mode operator, inverted on the host
-static bool coarse_inverse(const AjStepParams& p, const Layout& L, std::vector<double>& inv) {
-  const int l = L.nlev, n = L.ln[l], m = L.lm[l], N = n * m;
-  double hx = p.dx * (double)(1 << l), hy = p.dy * (double)(1 << l);
-  double ax = 1.0 / (hx * hx), ay = 1.0 / (hy * hy), g = ghost_factor(l);
-  std::vector<double> A((size_t)N * N, 0.0);
-  for (int i = 0; i < n; ++i)
-    for (int j = 0; j < m; ++j) {
-      int r = i * m + j;
-      double d = -2.0 * (ax + ay);
-      if (i == 0) d += ax; else A[(size_t)r * N + (i - 1) * m + j] += ax;
-      if (i == n - 1) d += ax * g; else A[(size_t)r * N + (i + 1) * m + j] += ax;
-      if (j == 0) d += ay; else A[(size_t)r * N + i * m + j - 1] += ay;
-      if (j == m - 1) d += ay; else A[(size_t)r * N + i * m + j + 1] += ay;
-      A[(size_t)r * N + r] += d;
-    }
-  inv.assign((size_t)N * N, 0.0);
-  for (int i = 0; i < N; ++i) inv[(size_t)i * N + i] = 1.0;
-  // Gauss-Jordan with partial pivoting
-  for (int c = 0; c < N; ++c) {
-    int piv = c;
-    for (int r = c + 1; r < N; ++r)
-      if (fabs(A[(size_t)r * N + c]) > fabs(A[(size_t)piv * N + c])) piv = r;
-    if (fabs(A[(size_t)piv * N + c]) < 1e-300) return false;
-    if (piv != c)
-      for (int k = 0; k < N; ++k) {
-        std::swap(A[(size_t)c * N + k], A[(size_t)piv * N + k]);
-        std::swap(inv[(size_t)c * N + k], inv[(size_t)piv * N + k]);
-      }
-    double s = 1.0 / A[(size_t)c * N + c];
-    for (int k = 0; k < N; ++k) {
-      A[(size_t)c * N + k] *= s;
-      inv[(size_t)c * N + k] *= s;
-    }
-    for (int r = 0; r < N; ++r) {
-      if (r == c) continue;
-      double f = A[(size_t)r * N + c];
-      if (f == 0.0) continue;
-      for (int k = 0; k < N; ++k) {
-        A[(size_t)r * N + k] -= f * A[(size_t)c * N + k];
-        inv[(size_t)r * N + k] -= f * inv[(size_t)c * N + k];
-      }
-    }
-  }
-  return true;
-}
-
 int prepare_pressure(const AjStepParams& p, const Layout& L, void* ws, const float* mask,
                      cudaStream_t st) {
   if (p.mg_mode == AJ_MG_PARITY) {
@@ -763,44 +306,8 @@ int prepare_pressure(const AjStepParams& p, const Layout& L, void* ws, const flo
       }
     }
   } else {
-    std::vector<double> inv;
-    if (!coarse_inverse(p, L, inv)) return AJ_ERR_PARAM;
-    if (cudaMemcpyAsync(at<double>(ws, L.cinv), inv.data(), inv.size() * sizeof(double),
-                        cudaMemcpyHostToDevice, st) != cudaSuccess)
-      return AJ_ERR_CUDA;
-    if (cudaStreamSynchronize(st) != cudaSuccess) return AJ_ERR_CUDA;
-  }
-  return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
-}
-
-// One launch of a converging-mode level-0 kernel on the workspace's current
-// contents (instrumentation: lets a caller time the kernel on its own).
-// which: 0 = smoothing + residual + restriction, 1 = prolongation + smoothing +
-// FP64 update, 2 = FP64 residual and norms.
-int profile_pressure_kernel(const AjStepParams& p, const Layout& L, void* ws, int which,
-                            cudaStream_t st) {
-  if (p.mg_mode != AJ_MG_CONVERGE) return AJ_ERR_PARAM;
-  DevScalars* sc = at<DevScalars>(ws, 0);
-  const int* never = reinterpret_cast<const int*>(&sc->pad_[0]);   // always 0
-  dim3 blk(32, 8);
-  CvLvl c = cv_level(p, L, 0);
-  dim3 g(cdiv(c.m, CV_TJ), cdiv(c.n, CV_TI));
-  if (which == 0) {
-    k_cv_down<<<g, blk, 0, st>>>(c, at<float>(ws, L.B[0]), at<float>(ws, L.X[0]),
-                                 at<float>(ws, L.B[1]), never);
-  } else if (which == 1) {
-    k_cv_up<<<g, blk, 0, st>>>(c, at<float>(ws, L.B[0]), at<float>(ws, L.X[0]),
-                               at<float>(ws, L.T[1]), L.ln[1], L.lm[1], (float)ghost_factor(1),
-                               nullptr, at<double>(ws, L.p64), never);
-  } else if (which == 2) {
-    long N = (long)p.nx * p.ny;
-    unsigned nb = cdiv(N, 256 * 4);
-    if (nb > 1216) nb = 1216;
-    k_cv_resid<<<nb, 256, 0, st>>>(at<double>(ws, L.p64), at<float>(ws, L.b0),
-                                   at<float>(ws, L.B[0]), p.nx, p.ny, 1.0 / (p.dx * p.dx),
-                                   1.0 / (p.dy * p.dy), sc, 1);
-  } else {
-    return AJ_ERR_PARAM;
+    int rc = converge_prepare(p, L, ws, st);
+    if (rc != AJ_OK) return rc;
   }
   return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
 }

@@ -354,9 +354,12 @@ def gpu_arm(args):
 
 
 def roofline(args, plan, state, mask, flush, L):
-    """Times the converging level-0 prolongation/smoothing/update kernel alone:
-    per launch it reads r (4 B), e (4 B), the coarse correction (1 B) and
-    reads and writes the FP64 pressure (16 B): 25 algorithmic bytes per cell."""
+    """Times the converging multigrid's level-0 post-smoothing kernel alone
+    (k_cv_up0: prolongation, 2 red-black sweeps, FP64 pressure update, FP64
+    residual for the next cycle).  Per cell it reads r (4 B), e (4 B), the
+    coarse correction (4 B / 4 cells), the FP64 pressure (8 B) and b (4 B), and
+    writes the new FP64 pressure (8 B) and the next residual (4 B): 33
+    algorithmic bytes per cell.  The L2 is flushed before every launch."""
     import torch
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     peak, src = 6800.0, "fallback"
@@ -364,7 +367,7 @@ def roofline(args, plan, state, mask, flush, L):
         with open(peaks_path) as f:
             peak, src = float(json.load(f)["hbm_gbs"]), "measured"
     st = torch.cuda.current_stream()
-    which, bpc = 1, 25
+    which, bpc = 1, 33
     times = []
     for k in range(13):
         flush.zero_()
@@ -382,7 +385,8 @@ def roofline(args, plan, state, mask, flush, L):
     dur = statistics.mean(a.elapsed_time(b) for a, b in times) * 1e-3
     algo = bpc * args.nx * args.ny
     achieved = algo / dur / 1e9
-    return {"kernel": "k_cv_up (level 0: prolongation + 2 red-black sweeps + FP64 update)",
+    return {"kernel": "k_cv_up0 (level 0: prolongation + 2 red-black sweeps + FP64 update "
+                      "and residual)",
             "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_source": src, "traffic": None,
             "algorithmic_bytes_per_launch": algo, "launch_us": dur * 1e6}

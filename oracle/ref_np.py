@@ -883,7 +883,7 @@ def rel_residual(p, b, dx, dy):
     return float(np.sqrt(np.sum(r ** 2)) / (nb if nb > 0 else 1.0))
 
 
-def mg_depth(nx, ny, max_coarse=256):
+def mg_depth(nx, ny, max_coarse=64):
     """Number of coarsenings: halve while both sizes stay even and the halves
     keep >= 2 cells, until the coarse grid has <= max_coarse cells; always at
     least one coarsening when the grid allows it."""
@@ -1014,7 +1014,7 @@ def v_cycle_converge(r, dx, dy, depth, nu1=2, nu2=2):
     return cyc(r, 0)
 
 
-def mg_converge(b, dx, dy, rtol=1e-6, max_cycles=40, p0=None, nu1=2, nu2=2, max_coarse=256):
+def mg_converge(b, dx, dy, rtol=1e-6, max_cycles=40, p0=None, nu1=2, nu2=2, max_coarse=64):
     """Converging mode: iterative refinement around V-cycles.  Each outer
     iteration computes r = b - A p in float64, runs one V-cycle on A e = r and
     adds e.  Stops when ||r||/||b|| <= rtol.  Returns (p, info)."""

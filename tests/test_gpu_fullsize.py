@@ -117,8 +117,12 @@ def test_converging_poisson(cuda_lib, mac):
     assert st["err"] == 0 and st["converged"]
     assert st["rel_residual"] <= 1e-6
     bb = (b * mask if mac else b).astype(np.float32).astype(np.float64)
-    pref, info = R.mg_converge(bb, dx, dx, rtol=1e-10)
-    assert abs(st["cycles"] - R.mg_converge(bb, dx, dx, rtol=1e-6)[1]["cycles"]) <= 2
+    pref, info = R.mg_converge(bb, dx, dx, rtol=1e-12)
+    p6, info6 = R.mg_converge(bb, dx, dx, rtol=1e-6)
+    assert abs(st["cycles"] - info6["cycles"]) <= 2
+    # the GPU solve (FP32 V-cycles, double-FP32 refinement) is as close to the
+    # exact discrete solution as the all-FP64 oracle stopped at the same rtol
+    assert rel(p, pref) <= 2.0 * rel(p6, pref) + 2e-6
     assert rel(p, pref) < 1e-4
 
 
