@@ -5,7 +5,7 @@
 // Structure of one refinement iteration (one body of the graph's while node):
 //   levels 0 .. lc-1   k_cv_down: 2 red-black sweeps from e = 0 in a shared-
 //                      memory tile, residual, 2x2 restriction
-//   levels lc .. D     k_cv_block: one 1024-thread block holding the smallest
+//   levels lc .. D     k_cv_block: one 256-thread block holding the smallest
 //                      levels (<= 1024 cells) in shared memory: sweeps,
 //                      restriction, the FP64 dense solve of the coarsest grid,
 //                      prolongation, sweeps
@@ -39,15 +39,8 @@ namespace aj {
 constexpr int CV_NS = 2;                         // red-black sweeps per smoothing phase
 constexpr int CV_H = 2 * CV_NS + 1;              // tile halo: sweeps + one cell for the residual
 constexpr int CV_THREADS = 256;
-constexpr int CV_BLOCK_THREADS = 1024;
+constexpr int CV_BLOCK_THREADS = 256;
 constexpr int CV_BLOCK_MAX_CELLS = 1024;         // levels handled by the one-block kernel
-
-template <int TI, int TJ>
-struct Tile {
-  static constexpr int SI = TI + 2 * CV_H, SJ = TJ + 2 * CV_H, NT = SI * SJ;
-};
-using TileL0 = Tile<32, 64>;                     // level 0: 512 tiles at 2048x512
-using TileLc = Tile<16, 32>;                     // coarser levels: 4x more tiles
 
 struct CvLvl {
   int n, m, level;
@@ -133,6 +126,22 @@ static DfCoef df_coef(double ax, double ay) {
 }
 
 // ---------------------------------------------------------------- tiles
+// A tile is SI x SJ cells of shared memory: the TI x TJ interior plus a halo
+// of CV_H cells.  Threads form a (SJ/2) x RG grid: thread (tx, ty) owns the
+// column pair {2tx, 2tx+1} and walks the rows ty, ty+RG, ...; in a red-black
+// half-sweep exactly one cell of its pair per row has the colour being
+// updated, so no index needs a division.
+template <int SI_, int SJ_, int NTH_>
+struct TileCfg {
+  static constexpr int SI = SI_, SJ = SJ_, NTH = NTH_;
+  static constexpr int TI = SI - 2 * CV_H, TJ = SJ - 2 * CV_H;
+  static constexpr int PAIRS = SJ / 2, RG = NTH / PAIRS, NT = SI * SJ;
+  static_assert(TI % 2 == 0 && TJ % 2 == 0, "tile interiors must align with the coarse grid");
+  static_assert(NTH % PAIRS == 0, "threads must fill whole rows of column pairs");
+};
+using T0 = TileCfg<48, 64, 256>;   // level 0: 38 x 54 interior
+using T1 = TileCfg<32, 32, 128>;   // coarser levels: 22 x 22 interior
+
 __device__ __forceinline__ float cv_diag(const CvLvl& L, int gi, int gj) {
   float d = -2.f * (L.ax + L.ay);
   if (gi == 0) d += L.ax;
@@ -145,27 +154,29 @@ __device__ __forceinline__ float cv_diag(const CvLvl& L, int gi, int gj) {
 // red-black half-sweeps over the whole shared-memory tile; cells outside the
 // domain hold 0 and never change (the diagonal carries the ghost rule).  After
 // half-sweep h the cells at distance >= h+1 from the tile border hold exact
-// red-black values; the cells nearer the border are never stored.
-template <class TL>
+// red-black values; the cells nearer the border are never stored.  Tiles start
+// at even global coordinates, so a cell's colour is (ti + tj) & 1.
+template <class TC>
 __device__ __forceinline__ void cv_sweeps(float* E, const float* R, const CvLvl& L, int gi0,
                                           int gj0) {
-  constexpr int SJ = TL::SJ, ROWS = TL::SI - 2, HW = (SJ - 1) / 2;
-  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  constexpr int SJ = TC::SJ, SI = TC::SI;
+  const int tx = threadIdx.x, ty = threadIdx.y;
   const float inv_int = 1.f / (-2.f * (L.ax + L.ay));
   for (int h = 0; h < 2 * CV_NS; ++h) {
     const int color = h & 1;
-    for (int t = tid; t < ROWS * HW; t += CV_THREADS) {
-      const int r = t / HW, kk = t - r * HW;
-      const int ti = 1 + r;
-      const int tj = 1 + ((color - ti - 1) & 1) + 2 * kk;
-      if (tj >= SJ - 1) continue;
+#pragma unroll 4
+    for (int ti = 1 + ty; ti < SI - 1; ti += TC::RG) {
+      const int tj = 2 * tx + ((color + ti) & 1);
       const int gi = gi0 + ti, gj = gj0 + tj;
-      if ((unsigned)gi >= (unsigned)L.n || (unsigned)gj >= (unsigned)L.m) continue;
-      if (L.level == 0 && gi == L.n - 1) continue;          // pinned outlet row
-      const int c = ti * SJ + tj;
-      const float nb = L.ax * (E[c + SJ] + E[c - SJ]) + L.ay * (E[c + 1] + E[c - 1]);
-      const bool inner = gi > 0 && gi < L.n - 1 && gj > 0 && gj < L.m - 1;
-      E[c] = (R[c] - nb) * (inner ? inv_int : 1.f / cv_diag(L, gi, gj));
+      const bool upd = tj >= 1 && tj < SJ - 1 && (unsigned)gi < (unsigned)L.n &&
+                       (unsigned)gj < (unsigned)L.m && !(L.level == 0 && gi == L.n - 1);
+      if (upd) {
+        const int c = ti * SJ + tj;
+        const float nb = L.ax * (E[c + SJ] + E[c - SJ]) + L.ay * (E[c + 1] + E[c - 1]);
+        float inv = inv_int;
+        if (gi == 0 || gj == 0 || gi == L.n - 1 || gj == L.m - 1) inv = 1.f / cv_diag(L, gi, gj);
+        E[c] = (R[c] - nb) * inv;
+      }
     }
     __syncthreads();
   }
@@ -195,96 +206,110 @@ __device__ __forceinline__ float cv_prolong(const float* __restrict__ ec, int nc
   return (9.f * c0 + 3.f * cx + 3.f * cy + cxy) * (1.f / 16.f);
 }
 
-// tile + halo load: E = e_in + P(ec) (or 0), R = r; unrolled so the loads are
-// in flight together
-template <class TL, bool ZERO_E>
+// tile + halo load: E = e_in + P(ec) (or 0), R = r; each row is read as two
+// coalesced runs of SJ/2 floats
+template <class TC, bool ZERO_E>
 __device__ __forceinline__ void cv_load(float* E, float* R, const CvLvl& L, int gi0, int gj0,
                                         const float* __restrict__ r, const float* __restrict__ e_in,
                                         const float* __restrict__ ec, int nc, int mc, float gc) {
-  constexpr int NT = TL::NT, SJ = TL::SJ, IT = (NT + CV_THREADS - 1) / CV_THREADS;
-  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  constexpr int SJ = TC::SJ;
+  const int tx = threadIdx.x, ty = threadIdx.y;
 #pragma unroll
-  for (int it = 0; it < IT; ++it) {
-    const int t = tid + it * CV_THREADS;
-    if (t < NT) {
-      const int ti = t / SJ, tj = t - ti * SJ;
-      const int gi = gi0 + ti, gj = gj0 + tj;
-      const bool in = (unsigned)gi < (unsigned)L.n && (unsigned)gj < (unsigned)L.m;
+  for (int ti = ty; ti < TC::SI; ti += TC::RG) {
+    const int gi = gi0 + ti;
+    const bool row_in = (unsigned)gi < (unsigned)L.n;
+    const bool row_e = row_in && !ZERO_E && !(L.level == 0 && gi == L.n - 1);
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int tj = tx + q * TC::PAIRS;
+      const int gj = gj0 + tj;
+      const bool in = row_in && (unsigned)gj < (unsigned)L.m;
       float rr = 0.f, e = 0.f;
       if (in) {
         const long k = (long)gi * L.m + gj;
         rr = ldg(r + k);
-        if (!ZERO_E && !(L.level == 0 && gi == L.n - 1))
-          e = ldg(e_in + k) + cv_prolong(ec, nc, mc, gc, gi, gj);
+        if (row_e) e = ldg(e_in + k) + cv_prolong(ec, nc, mc, gc, gi, gj);
       }
-      E[t] = e;
-      R[t] = rr;
+      E[ti * SJ + tj] = e;
+      R[ti * SJ + tj] = rr;
     }
   }
   __syncthreads();
 }
 
 // pre-smoothing from e = 0, residual, 2x2 average onto the coarse rhs
-template <int TI, int TJ>
-__global__ void __launch_bounds__(CV_THREADS) k_cv_down(CvLvl L, const float* __restrict__ r,
-                                                        float* __restrict__ e_out,
-                                                        float* __restrict__ rc, const int* done) {
-  using TL = Tile<TI, TJ>;
-  constexpr int SJ = TL::SJ;
+template <class TC>
+__global__ void __launch_bounds__(TC::NTH) k_cv_down(CvLvl L, const float* __restrict__ r,
+                                                     float* __restrict__ e_out,
+                                                     float* __restrict__ rc, const int* done) {
+  constexpr int SJ = TC::SJ, TI = TC::TI, TJ = TC::TJ;
   if (*done) return;
-  __shared__ float E[TL::NT];
-  __shared__ float R[TL::NT];
+  __shared__ float E[TC::NT];
+  __shared__ float R[TC::NT];
   const int i0 = blockIdx.y * TI, j0 = blockIdx.x * TJ;
   const int gi0 = i0 - CV_H, gj0 = j0 - CV_H;
-  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-  cv_load<TL, true>(E, R, L, gi0, gj0, r, nullptr, nullptr, 0, 0, 0.f);
-  cv_sweeps<TL>(E, R, L, gi0, gj0);
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  cv_load<TC, true>(E, R, L, gi0, gj0, r, nullptr, nullptr, 0, 0, 0.f);
+  cv_sweeps<TC>(E, R, L, gi0, gj0);
   // store e and compute the residual on the tile interior (in place in R)
-  for (int t = tid; t < TI * TJ; t += CV_THREADS) {
-    const int ti = CV_H + t / TJ, tj = CV_H + t % TJ;
-    const int gi = gi0 + ti, gj = gj0 + tj;
-    if (gi >= L.n || gj >= L.m) continue;
-    const int c = ti * SJ + tj;
-    e_out[(long)gi * L.m + gj] = E[c];
-    float res = 0.f;
-    if (!(L.level == 0 && gi == L.n - 1)) {
-      const float nb = L.ax * (E[c + SJ] + E[c - SJ]) + L.ay * (E[c + 1] + E[c - 1]);
-      res = R[c] - (nb + cv_diag(L, gi, gj) * E[c]);
+  for (int ti = CV_H + ty; ti < CV_H + TI; ti += TC::RG) {
+    const int gi = gi0 + ti;
+    if (gi >= L.n) break;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int tj = CV_H + tx + q * TC::PAIRS;
+      const int gj = gj0 + tj;
+      if (tj >= CV_H + TJ || gj >= L.m) continue;
+      const int c = ti * SJ + tj;
+      e_out[(long)gi * L.m + gj] = E[c];
+      float res = 0.f;
+      if (!(L.level == 0 && gi == L.n - 1)) {
+        const float nb = L.ax * (E[c + SJ] + E[c - SJ]) + L.ay * (E[c + 1] + E[c - 1]);
+        res = R[c] - (nb + cv_diag(L, gi, gj) * E[c]);
+      }
+      R[c] = res;
     }
-    R[c] = res;
   }
   __syncthreads();
   const int mc = L.m >> 1, nc = L.n >> 1;
-  for (int t = tid; t < (TI / 2) * (TJ / 2); t += CV_THREADS) {
-    const int ci = t / (TJ / 2), cj = t % (TJ / 2);
-    const int I = (i0 >> 1) + ci, J = (j0 >> 1) + cj;
-    if (I >= nc || J >= mc) continue;
-    const int c = (CV_H + 2 * ci) * SJ + CV_H + 2 * cj;
-    rc[(long)I * mc + J] = 0.25f * (R[c] + R[c + SJ] + R[c + 1] + R[c + SJ + 1]);
+  for (int ci = ty; ci < TI / 2; ci += TC::RG) {
+    const int I = (i0 >> 1) + ci;
+    if (I >= nc) break;
+    for (int cj = tx; cj < TJ / 2; cj += TC::PAIRS) {
+      const int J = (j0 >> 1) + cj;
+      if (J >= mc) break;
+      const int c = (CV_H + 2 * ci) * SJ + CV_H + 2 * cj;
+      rc[(long)I * mc + J] = 0.25f * (R[c] + R[c + SJ] + R[c + 1] + R[c + SJ + 1]);
+    }
   }
 }
 
 // e + P(e_coarse), post-smoothing, store (levels >= 1)
-template <int TI, int TJ>
-__global__ void __launch_bounds__(CV_THREADS) k_cv_up(CvLvl L, const float* __restrict__ r,
-                                                      const float* __restrict__ e_in,
-                                                      const float* __restrict__ ec, int nc, int mc,
-                                                      float gc, float* __restrict__ e_out,
-                                                      const int* done) {
-  using TL = Tile<TI, TJ>;
+template <class TC>
+__global__ void __launch_bounds__(TC::NTH) k_cv_up(CvLvl L, const float* __restrict__ r,
+                                                   const float* __restrict__ e_in,
+                                                   const float* __restrict__ ec, int nc, int mc,
+                                                   float gc, float* __restrict__ e_out,
+                                                   const int* done) {
+  constexpr int SJ = TC::SJ, TI = TC::TI, TJ = TC::TJ;
   if (*done) return;
-  __shared__ float E[TL::NT];
-  __shared__ float R[TL::NT];
+  __shared__ float E[TC::NT];
+  __shared__ float R[TC::NT];
   const int i0 = blockIdx.y * TI, j0 = blockIdx.x * TJ;
   const int gi0 = i0 - CV_H, gj0 = j0 - CV_H;
-  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-  cv_load<TL, false>(E, R, L, gi0, gj0, r, e_in, ec, nc, mc, gc);
-  cv_sweeps<TL>(E, R, L, gi0, gj0);
-  for (int t = tid; t < TI * TJ; t += CV_THREADS) {
-    const int ti = CV_H + t / TJ, tj = CV_H + t % TJ;
-    const int gi = gi0 + ti, gj = gj0 + tj;
-    if (gi >= L.n || gj >= L.m) continue;
-    e_out[(long)gi * L.m + gj] = E[ti * TL::SJ + tj];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  cv_load<TC, false>(E, R, L, gi0, gj0, r, e_in, ec, nc, mc, gc);
+  cv_sweeps<TC>(E, R, L, gi0, gj0);
+  for (int ti = CV_H + ty; ti < CV_H + TI; ti += TC::RG) {
+    const int gi = gi0 + ti;
+    if (gi >= L.n) break;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int tj = CV_H + tx + q * TC::PAIRS;
+      const int gj = gj0 + tj;
+      if (tj >= CV_H + TJ || gj >= L.m) continue;
+      e_out[(long)gi * L.m + gj] = E[ti * SJ + tj];
+    }
   }
 }
 
@@ -334,63 +359,76 @@ struct PState {
 // level 0: e + P(e_coarse), post-smoothing, p += e (double-FP32, ping-pong), the
 // residual of the reference operator for the next iteration (double-FP32), its
 // FP64 norm, and the convergence test in the last block to finish
-__global__ void __launch_bounds__(CV_THREADS) k_cv_up0(
+__global__ void __launch_bounds__(T0::NTH) k_cv_up0(
     CvLvl L, const float* __restrict__ r, const float* __restrict__ e_in,
     const float* __restrict__ ec, int nc, int mc, float gc, PState ps, const float* __restrict__ b,
     float* __restrict__ r_next, DevScalars* sc, DfCoef co, CvCheck ck, int profile) {
-  using TL = TileL0;
-  constexpr int TI = 32, TJ = 64, SJ = TL::SJ;
-  if (!profile && sc->mg_done) return;
-  __shared__ float E[TL::NT];
-  __shared__ float R[TL::NT];
+  using TC = T0;
+  constexpr int TI = TC::TI, TJ = TC::TJ, SJ = TC::SJ;
   constexpr int PI = TI + 2, PJ = TJ + 2;
+  static_assert(PJ <= 2 * TC::PAIRS, "the pressure window must fit two column runs");
+  if (!profile && sc->mg_done) return;
+  __shared__ float E[TC::NT];
+  __shared__ float R[TC::NT];
   __shared__ float PH[PI * PJ];
   __shared__ float PL[PI * PJ];
   __shared__ int am_last;
   const int i0 = blockIdx.y * TI, j0 = blockIdx.x * TJ;
   const int gi0 = i0 - CV_H, gj0 = j0 - CV_H;
-  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int tid = ty * TC::PAIRS + tx;
   const long N = (long)L.n * L.m;
   const int cur = sc->pcur;
   const float* __restrict__ pin = cur ? ps.b : ps.a;
   float* __restrict__ pout = cur ? ps.a : ps.b;
-  cv_load<TL, false>(E, R, L, gi0, gj0, r, e_in, ec, nc, mc, gc);
-  cv_sweeps<TL>(E, R, L, gi0, gj0);
+  cv_load<TC, false>(E, R, L, gi0, gj0, r, e_in, ec, nc, mc, gc);
+  cv_sweeps<TC>(E, R, L, gi0, gj0);
   // new pressure on the interior and one cell around it
-  for (int t = tid; t < PI * PJ; t += CV_THREADS) {
-    const int pi = t / PJ, pj = t - pi * PJ;
-    const int gi = i0 - 1 + pi, gj = j0 - 1 + pj;
-    df v{0.f, 0.f};
-    if ((unsigned)gi < (unsigned)L.n && (unsigned)gj < (unsigned)L.m && gi != L.n - 1) {
-      const long k = (long)gi * L.m + gj;
-      v = df_add_f(df{pin[k], pin[N + k]}, E[(CV_H - 1 + pi) * SJ + (CV_H - 1 + pj)]);
+  for (int pi = ty; pi < PI; pi += TC::RG) {
+    const int gi = i0 - 1 + pi;
+    const bool row_in = (unsigned)gi < (unsigned)L.n && gi != L.n - 1;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int pj = tx + q * TC::PAIRS;
+      if (pj >= PJ) continue;
+      const int gj = j0 - 1 + pj;
+      df v{0.f, 0.f};
+      if (row_in && (unsigned)gj < (unsigned)L.m) {
+        const long k = (long)gi * L.m + gj;
+        v = df_add_f(df{pin[k], pin[N + k]}, E[(CV_H - 1 + pi) * SJ + (CV_H - 1 + pj)]);
+      }
+      PH[pi * PJ + pj] = v.hi;
+      PL[pi * PJ + pj] = v.lo;
     }
-    PH[t] = v.hi;
-    PL[t] = v.lo;
   }
   __syncthreads();
   const df ax{co.axh, co.axl}, ay{co.ayh, co.ayl};
   float acc = 0.f;
-  for (int t = tid; t < TI * TJ; t += CV_THREADS) {
-    const int ti = t / TJ, tj = t % TJ;
-    const int gi = i0 + ti, gj = j0 + tj;
-    if (gi >= L.n || gj >= L.m) continue;
-    const long k = (long)gi * L.m + gj;
-    const int c = (ti + 1) * PJ + (tj + 1);
-    const df pc{PH[c], PL[c]};
-    pout[k] = pc.hi;
-    pout[N + k] = pc.lo;
-    float rr = 0.f;
-    if (gi != L.n - 1) {
-      const df xp{PH[c + PJ], PL[c + PJ]};                      // row n-1 holds the pinned 0
-      const df xm = gi > 0 ? df{PH[c - PJ], PL[c - PJ]} : pc;   // Neumann ghosts
-      const df yp = gj < L.m - 1 ? df{PH[c + 1], PL[c + 1]} : pc;
-      const df ym = gj > 0 ? df{PH[c - 1], PL[c - 1]} : pc;
-      const df res = df_residual(ldg(b + k), pc, xp, xm, yp, ym, ax, ay);
-      rr = res.hi + res.lo;
+  for (int ti = ty; ti < TI; ti += TC::RG) {
+    const int gi = i0 + ti;
+    if (gi >= L.n) break;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int tj = tx + q * TC::PAIRS;
+      const int gj = j0 + tj;
+      if (tj >= TJ || gj >= L.m) continue;
+      const long k = (long)gi * L.m + gj;
+      const int c = (ti + 1) * PJ + (tj + 1);
+      const df pc{PH[c], PL[c]};
+      pout[k] = pc.hi;
+      pout[N + k] = pc.lo;
+      float rr = 0.f;
+      if (gi != L.n - 1) {
+        const df xp{PH[c + PJ], PL[c + PJ]};                      // row n-1 holds the pinned 0
+        const df xm = gi > 0 ? df{PH[c - PJ], PL[c - PJ]} : pc;   // Neumann ghosts
+        const df yp = gj < L.m - 1 ? df{PH[c + 1], PL[c + 1]} : pc;
+        const df ym = gj > 0 ? df{PH[c - 1], PL[c - 1]} : pc;
+        const df res = df_residual(ldg(b + k), pc, xp, xm, yp, ym, ax, ay);
+        rr = res.hi + res.lo;
+      }
+      if (!profile) r_next[k] = rr;
+      acc = fmaf(rr, rr, acc);
     }
-    if (!profile) r_next[k] = rr;
-    acc = fmaf(rr, rr, acc);
   }
   if (profile) return;
   block_sum_atomic((double)acc, &sc->acc[0]);
@@ -424,7 +462,9 @@ size_t converge_block_smem(const Layout& L, int lc) {
   size_t s = 0;
   for (int k = lc; k <= L.nlev; ++k) s += 2 * (size_t)(L.ln[k] + 2) * (L.lm[k] + 2) * 4;
   s = (s + 15) & ~(size_t)15;
-  s += (size_t)L.ln[L.nlev] * L.lm[L.nlev] * 8;
+  const size_t N = (size_t)L.ln[L.nlev] * L.lm[L.nlev];
+  s += N * 8;
+  if (N <= AJ_MAX_COARSE) s += N * N * 8;     // the coarsest inverse, prefetched
   return s;
 }
 
@@ -473,6 +513,12 @@ __global__ void __launch_bounds__(CV_BLOCK_THREADS) k_cv_block(CvBlock a) {
   }
   off = (off + 15) & ~(size_t)15;
   double* V = reinterpret_cast<double*>(smraw + off);
+  // small coarsest grids: start loading the inverse now, so its latency hides
+  // behind the smoothing of the finer levels
+  const bool pre = a.ncoarse <= AJ_MAX_COARSE;
+  double* Ainv_s = V + a.ncoarse;
+  if (pre)
+    for (int t = threadIdx.x; t < a.ncoarse * a.ncoarse; t += blockDim.x) Ainv_s[t] = a.Ainv[t];
   float* all = reinterpret_cast<float*>(smraw);
   for (size_t t = threadIdx.x; t < total_f; t += blockDim.x) all[t] = 0.f;
   __syncthreads();
@@ -520,7 +566,7 @@ __global__ void __launch_bounds__(CV_BLOCK_THREADS) k_cv_block(CvBlock a) {
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     for (int row = warp; row < N; row += nw) {
-      const double* arow = a.Ainv + (long)row * N;
+      const double* arow = (pre ? Ainv_s : a.Ainv) + (long)row * N;
       double s = 0.0;
       for (int c = lane; c < N; c += 32) s += arow[c] * V[c];
       s = warp_sum(s);
@@ -670,9 +716,13 @@ static PState pstate(const Layout& L, void* ws) {
   return PState{at<float>(ws, L.p64), at<float>(ws, L.p64b)};
 }
 
-template <class TL, int TI, int TJ>
+template <class TC>
 static dim3 tiles(const CvLvl& c) {
-  return dim3(cdiv(c.m, TJ), cdiv(c.n, TI));
+  return dim3(cdiv(c.m, TC::TJ), cdiv(c.n, TC::TI));
+}
+template <class TC>
+static dim3 tile_threads() {
+  return dim3(TC::PAIRS, TC::RG);
 }
 
 // one refinement iteration
@@ -681,26 +731,25 @@ static void cv_body(const AjStepParams& p, const Layout& L, void* ws,
   DevScalars* sc = at<DevScalars>(ws, 0);
   const int* done = &sc->mg_done;
   const int lc = L.lc;
-  dim3 blk(32, 8);
   for (int l = 0; l < lc; ++l) {
     CvLvl c = cv_level(p, L, l);
     if (l == 0)
-      k_cv_down<32, 64><<<tiles<TileL0, 32, 64>(c), blk, 0, st>>>(
+      k_cv_down<T0><<<tiles<T0>(c), tile_threads<T0>(), 0, st>>>(
           c, at<float>(ws, L.B[l]), at<float>(ws, L.X[l]), at<float>(ws, L.B[l + 1]), done);
     else
-      k_cv_down<16, 32><<<tiles<TileLc, 16, 32>(c), blk, 0, st>>>(
+      k_cv_down<T1><<<tiles<T1>(c), tile_threads<T1>(), 0, st>>>(
           c, at<float>(ws, L.B[l]), at<float>(ws, L.X[l]), at<float>(ws, L.B[l + 1]), done);
   }
   k_cv_block<<<1, CV_BLOCK_THREADS, converge_block_smem(L, lc), st>>>(block_args(p, L, ws, done));
   for (int l = lc - 1; l >= 1; --l) {
     CvLvl c = cv_level(p, L, l);
-    k_cv_up<16, 32><<<tiles<TileLc, 16, 32>(c), blk, 0, st>>>(
+    k_cv_up<T1><<<tiles<T1>(c), tile_threads<T1>(), 0, st>>>(
         c, at<float>(ws, L.B[l]), at<float>(ws, L.X[l]), at<float>(ws, L.T[l + 1]), L.ln[l + 1],
         L.lm[l + 1], (float)ghost_factor(l + 1), at<float>(ws, L.T[l]), done);
   }
   CvLvl c0 = cv_level(p, L, 0);
   CvCheck ck{p.mg_rtol, p.max_cycles, use_handle, h};
-  k_cv_up0<<<tiles<TileL0, 32, 64>(c0), blk, 0, st>>>(
+  k_cv_up0<<<tiles<T0>(c0), tile_threads<T0>(), 0, st>>>(
       c0, at<float>(ws, L.B[0]), at<float>(ws, L.X[0]), at<float>(ws, L.T[1]), L.ln[1], L.lm[1],
       (float)ghost_factor(1), pstate(L, ws), at<float>(ws, L.b0), at<float>(ws, L.B[0]), sc,
       df_coef(1.0 / (p.dx * p.dx), 1.0 / (p.dy * p.dy)), ck, 0);
@@ -848,15 +897,14 @@ int profile_pressure_kernel(const AjStepParams& p, const Layout& L, void* ws, in
   if (p.mg_mode != AJ_MG_CONVERGE) return AJ_ERR_PARAM;
   DevScalars* sc = at<DevScalars>(ws, 0);
   const int* never = reinterpret_cast<const int*>(&sc->pad_[0]);   // always 0
-  dim3 blk(32, 8);
   CvLvl c = cv_level(p, L, 0);
   if (which == 0) {
-    k_cv_down<32, 64><<<tiles<TileL0, 32, 64>(c), blk, 0, st>>>(
+    k_cv_down<T0><<<tiles<T0>(c), tile_threads<T0>(), 0, st>>>(
         c, at<float>(ws, L.B[0]), at<float>(ws, L.X[0]), at<float>(ws, L.B[1]), never);
   } else if (which == 1) {
     CvCheck ck{p.mg_rtol, p.max_cycles, 0, 0};
     // profile mode reads the current state buffer and writes only the other one
-    k_cv_up0<<<tiles<TileL0, 32, 64>(c), blk, 0, st>>>(
+    k_cv_up0<<<tiles<T0>(c), tile_threads<T0>(), 0, st>>>(
         c, at<float>(ws, L.B[0]), at<float>(ws, L.X[0]), at<float>(ws, L.T[1]), L.ln[1], L.lm[1],
         (float)ghost_factor(1), pstate(L, ws), at<float>(ws, L.b0), at<float>(ws, L.B[0]), sc,
         df_coef(1.0 / (p.dx * p.dx), 1.0 / (p.dy * p.dy)), ck, 1);
