@@ -34,7 +34,7 @@ class AjStepParams(ctypes.Structure):
     _fields_ = [(n, c_int32) for n in (
         "nx", "ny", "grid_type", "flow_type", "variant", "les_model", "advection", "mg_mode",
         "fast_mode", "slip_walls", "v_cycles", "levels", "max_cycles", "has_sdf", "cfl_dt",
-        "warm_start")] + [(n, c_double) for n in (
+        "warm_start", "nn_factor")] + [(n, c_double) for n in (
         "dx", "dy", "dt", "dt_correction", "nu", "U_inf", "brinkman_eta",
         "smagorinsky_constant", "nu_hyper_ratio", "mg_tolerance", "mg_rtol", "cfl_target",
         "dt_min", "dt_max", "les_delta")]
@@ -69,6 +69,27 @@ _SIGS = {
     "aj_poisson_mg_static": (c_int32, [POINTER(AjStepParams), c_void_p, c_void_p, c_void_p,
                                        c_void_p, c_void_p]),
     "aj_kernel_count": (c_int32, [POINTER(AjStepParams), c_int32]),
+    "aj_nn_param_count": (c_size_t, []),
+    "aj_nn_packed_count": (c_size_t, []),
+    "aj_nn_act_bytes": (c_size_t, [c_int32, c_int32, c_int32]),
+    "aj_nn_input": (c_void_p, [c_int32, c_int32, c_int32, c_void_p]),
+    "aj_nn_pack": (c_int32, [c_void_p, c_void_p, c_void_p]),
+    "aj_nn_forward": (c_int32, [c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_size_t,
+                                c_void_p, c_void_p]),
+    "aj_nn_backward": (c_int32, [c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p,
+                                 c_void_p, c_size_t, c_void_p, c_void_p]),
+    "aj_nn_loss": (c_int32, [c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_void_p,
+                             c_void_p]),
+    "aj_nn_adam": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_int32, ctypes.c_float,
+                             ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                             c_void_p]),
+    "aj_nn_expand": (c_int32, [c_int32, c_int32, c_int32, c_void_p, c_void_p, c_void_p]),
+    "aj_nn_features": (c_int32, [POINTER(AjStepParams), c_void_p, c_void_p, c_void_p, c_void_p,
+                                 c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
+    "aj_workspace_rhs": (c_void_p, [POINTER(AjStepParams), c_void_p]),
+    "aj_step_nn": (c_int32, [POINTER(AjStepParams), c_void_p, c_void_p, c_void_p, c_void_p,
+                             c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                             c_size_t, c_void_p, c_void_p]),
     "aj_profile_kernel": (c_int32, [POINTER(AjStepParams), c_int32, c_void_p, c_void_p, c_void_p,
                                     c_void_p, c_size_t, c_void_p]),
     "aj_release_graphs": (c_int32, []),
@@ -113,4 +134,5 @@ def header_symbols():
     """Names of every function the public header declares."""
     with open(HEADER) as f:
         text = f.read()
-    return sorted(set(re.findall(r"^\s*(?:int32_t|size_t)\s+(aj_\w+)\s*\(", text, re.M)))
+    return sorted(set(re.findall(
+        r"^\s*(?:const\s+)?(?:int32_t|size_t|float)\s*\*?\s*(aj_\w+)\s*\(", text, re.M)))

@@ -7,6 +7,7 @@
 // converging multigrid's refinement loop is a while node inside that graph,
 // so a step never waits on the host.
 #include "aj_internal.cuh"
+#include <deque>
 #include <mutex>
 #include <string>
 #include <unordered_map>
@@ -145,6 +146,10 @@ bool make_layout(const AjStepParams& p, Layout& L) {
     // levels lc..D run in one thread block with everything in shared memory
     L.lc = converge_first_block_level(L);
   }
+  if (p.nn_factor > 0 && p.mg_mode == AJ_MG_CONVERGE && nn_step_shape_ok(p)) {
+    L.nn_act = take(nn_step_act_bytes(p));
+    L.p_init = take(N * 4);
+  }
   L.part = take(kPartials * 8);
   L.total = off;
   return true;
@@ -168,7 +173,12 @@ static AjStepParams normalise(const AjStepParams& in) {
 namespace {
 std::mutex g_mu;
 std::unordered_map<std::string, cudaGraphExec_t> g_cache;
+std::deque<std::string> g_order;   // insertion order, for eviction
 cudaStream_t g_capture = nullptr;
+// Executable graphs kept at once.  Callers that allocate fresh output tensors
+// every step produce new pointer keys; the oldest graph is destroyed beyond
+// this count (an in-flight graph is freed by CUDA when it completes).
+constexpr size_t kMaxGraphs = 64;
 
 std::string make_key(int kind, const AjStepParams& p, std::initializer_list<const void*> ptrs) {
   std::string k;
@@ -205,7 +215,16 @@ int run_captured(const std::string& key, cudaStream_t user, F&& enqueue) {
       return AJ_ERR_CUDA;
     }
     cudaGraphDestroy(g);
+    while (g_cache.size() >= kMaxGraphs && !g_order.empty()) {
+      auto old = g_cache.find(g_order.front());
+      if (old != g_cache.end()) {
+        cudaGraphExecDestroy(old->second);
+        g_cache.erase(old);
+      }
+      g_order.pop_front();
+    }
     it = g_cache.emplace(key, ex).first;
+    g_order.push_back(key);
   }
   return cudaGraphLaunch(it->second, user) == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
 }
@@ -217,9 +236,15 @@ static int ws_ok(const Layout& L, void* ws, size_t bytes) {
   return AJ_OK;
 }
 
+struct NnRef {
+  const uint16_t* packed = nullptr;
+  const float* master = nullptr;
+};
+
 static int enqueue_step(const AjStepParams& p, const Layout& L, void* ws, const float* u,
                         const float* v, const float* mask, const float* p_guess, float* uo,
-                        float* vo, float* po, AjStats* stats, cudaStream_t st) {
+                        float* vo, float* po, AjStats* stats, cudaStream_t st,
+                        NnRef nn = NnRef()) {
   int rc = p.cfl_dt ? launch_cfl(p, ws, u, v, nullptr, st) : launch_set_dt(p, ws, st);
   if (rc != AJ_OK) return rc;
   const bool mac = p.grid_type == AJ_GRID_MAC;
@@ -240,6 +265,14 @@ static int enqueue_step(const AjStepParams& p, const Layout& L, void* ws, const 
   if (rc != AJ_OK) return rc;
   rc = launch_rhs(p, L, ws, us, vs, mask, at<float>(ws, L.b0), st);
   if (rc != AJ_OK) return rc;
+  if (nn.packed) {
+    // learned warm start: p_guess + the network's correction
+    float* pinit = at<float>(ws, L.p_init);
+    rc = nn_warm_start(p, L, ws, at<float>(ws, L.b0), mask, p_guess, nn.packed, nn.master, pinit,
+                       st);
+    if (rc != AJ_OK) return rc;
+    p_guess = pinit;
+  }
   rc = launch_pressure(p, L, ws, mask, p_guess, po, stats, st);
   if (rc != AJ_OK) return rc;
   return launch_correct(p, L, ws, us, vs, po, mask, uo, vo, st);
@@ -305,6 +338,39 @@ int32_t aj_step(const AjStepParams* prm, const float* u, const float* v, const f
   return run_captured(key, (cudaStream_t)stream, [&](cudaStream_t s) {
     return enqueue_step(p, L, ws, u, v, mask, pg, u_out, v_out, p_out, stats, s);
   });
+}
+
+int32_t aj_step_nn(const AjStepParams* prm, const float* u, const float* v, const float* mask,
+                   const float* p_prev, const uint16_t* nn_packed, const float* nn_master,
+                   float* u_out, float* v_out, float* p_out, void* ws, size_t bytes,
+                   AjStats* stats, void* stream) {
+  if (!prm || !u || !v || !mask || !p_prev || !nn_packed || !nn_master || !u_out || !v_out ||
+      !p_out)
+    return AJ_ERR_PARAM;
+  int rc = aj_check_params(prm);
+  if (rc != AJ_OK) return rc;
+  AjStepParams p = normalise(*prm);
+  if (p.mg_mode != AJ_MG_CONVERGE || p.nn_factor <= 0) return AJ_ERR_PARAM;
+  if (!nn_step_shape_ok(p)) return AJ_ERR_SHAPE;
+  p.warm_start = 1;
+  Layout L;
+  make_layout(p, L);
+  if ((rc = ws_ok(L, ws, bytes)) != AJ_OK) return rc;
+  std::string key = make_key(3, p, {ws, u, v, mask, p_prev, nn_packed, nn_master, u_out, v_out,
+                                    p_out, stats});
+  NnRef nn;
+  nn.packed = nn_packed;
+  nn.master = nn_master;
+  return run_captured(key, (cudaStream_t)stream, [&](cudaStream_t s) {
+    return enqueue_step(p, L, ws, u, v, mask, p_prev, u_out, v_out, p_out, stats, s, nn);
+  });
+}
+
+const float* aj_workspace_rhs(const AjStepParams* prm, void* ws) {
+  if (!prm || !ws) return nullptr;
+  Layout L;
+  if (!make_layout(normalise(*prm), L)) return nullptr;
+  return at<float>(ws, L.b0);
 }
 
 int32_t aj_poisson_mg(const AjStepParams* prm, const float* rhs, const float* mask,
@@ -412,6 +478,7 @@ int32_t aj_kernel_count(const AjStepParams* prm, int32_t cycles) {
   }
   n += 1;                                                       // stats
   n += 1;                                                       // correction
+  if (p.nn_factor > 0) n += 3 + 18 + 1;                         // features, network, p_init
   return n;
 }
 
@@ -419,6 +486,7 @@ int32_t aj_release_graphs(void) {
   std::lock_guard<std::mutex> lk(g_mu);
   for (auto& kv : g_cache) cudaGraphExecDestroy(kv.second);
   g_cache.clear();
+  g_order.clear();
   return AJ_OK;
 }
 

@@ -1,0 +1,825 @@
+// Learned pressure warm start: a 4-level convolutional encoder-decoder on the
+// tensor cores (BF16 operands, FP32 accumulation), its backward pass, MSE
+// loss and Adam - the network, training and inference kernels.
+//
+// The reference's learned operators (neural_operators/nn_pressure_operator_*.py)
+// replace the pressure solve; here the network predicts a correction to the
+// previous pressure on a grid F times coarser, and the converging multigrid
+// always finishes the solve.  Architecture (oracle/nn_np.py holds the same
+// table): e0a 16->32, e0b 32->32 (s0) | pool | e1a 32->64, e1b 64->64 (s1) |
+// pool | e2a 64->128, e2b 128->128 (s2) | pool | e3a, e3b 128->128 |
+// up + s2 | d2 128->64 | up + s1 | d1 64->32 | up + s0 | d0a 32->32 |
+// d0b 32->16 (linear; channel 0 is the prediction).  3x3 'SAME' convolutions
+// (zero padding, bias, ReLU), 2x2 average pooling, nearest 2x upsampling.
+// Activations are FP32 NHWC [n][h][w][c]; weights are kept as an FP32 master
+// copy (flat: per layer W[3][3][Cin][Cout] then b[Cout]) and packed to BF16
+// twice per layer: Wf[tap][Cin][Cout] for the forward pass and
+// Wb[8-tap][Cout][Cin] (the adjoint of a stride-1 'SAME' convolution is the
+// convolution with the flipped, channel-transposed kernel) for the input
+// gradient.
+#include "aj_internal.cuh"
+#include <cuda_bf16.h>
+#include <string.h>
+
+namespace aj {
+
+struct NnLayer {
+  int cin, cout, relu;
+};
+static const NnLayer kLayers[] = {
+    {16, 32, 1}, {32, 32, 1}, {32, 64, 1}, {64, 64, 1}, {64, 128, 1}, {128, 128, 1},
+    {128, 128, 1}, {128, 128, 1}, {128, 64, 1}, {64, 32, 1}, {32, 32, 1}, {32, 16, 0}};
+enum { E0A, E0B, E1A, E1B, E2A, E2B, E3A, E3B, D2, D1, D0A, D0B, NL };
+
+static size_t w_off(int l) {   // FP32 master offset of layer l's weights
+  size_t o = 0;
+  for (int k = 0; k < l; ++k) o += 9 * (size_t)kLayers[k].cin * kLayers[k].cout + kLayers[k].cout;
+  return o;
+}
+static size_t b_off(int l) { return w_off(l) + 9 * (size_t)kLayers[l].cin * kLayers[l].cout; }
+static size_t pk_off(int l) {  // packed BF16 offset of layer l (Wf then Wb)
+  size_t o = 0;
+  for (int k = 0; k < l; ++k) o += 2 * 9 * (size_t)kLayers[k].cin * kLayers[k].cout;
+  return o;
+}
+static size_t n_params() { return w_off(NL); }
+static size_t n_packed() { return pk_off(NL); }
+
+// ---------------------------------------------------------------- MMA helpers
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+  __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<uint32_t*>(&v);
+}
+
+// D = A (16x16 bf16, row) * B (16x8 bf16, col) + D (f32)
+__device__ __forceinline__ void mma_bf16(float* d, const uint32_t* a, const uint32_t* b) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+      "{%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// ---------------------------------------------------------------- convolution
+// Implicit GEMM: M = pixels (64 per block, 16 per warp), N = Cout (<= 128),
+// K = 9 taps x Cin (16 per step).  A = the input shifted by the tap (zero
+// outside the image), converted to BF16 on its way into shared memory;
+// B = Wf[tap][ci][co] held transposed in shared memory ([co][k]) so both
+// fragments are 32-bit shared loads.
+constexpr int CONV_BM = 64, CONV_THREADS = 128, CONV_BNMAX = 128;
+constexpr int CONV_AS = 16 + 8;     // bf16 row stride of the A tile (pad: no bank conflicts)
+constexpr int CONV_BS = 16 + 8;     // bf16 row stride of the transposed B tile
+
+template <int NT>   // NT = Cout / 8
+__global__ void __launch_bounds__(CONV_THREADS) k_conv3x3(const float* __restrict__ X, int N, int H,
+                                                          int W, int Cin,
+                                                          const __nv_bfloat16* __restrict__ Wt,
+                                                          const float* __restrict__ bias,
+                                                          float* __restrict__ Y, int relu) {
+  constexpr int Cout = NT * 8;
+  __shared__ __align__(16) __nv_bfloat16 As[CONV_BM * CONV_AS];
+  __shared__ __align__(16) __nv_bfloat16 Bs[CONV_BNMAX * CONV_BS];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int g = lane >> 2, tg = lane & 3;
+  const long P = (long)N * H * W;
+  const long p0 = (long)blockIdx.x * CONV_BM;
+  float acc[NT][4];
+#pragma unroll
+  for (int t = 0; t < NT; ++t) acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.f;
+  // the pixel this thread loads for A (two threads per pixel, 8 channels each)
+  const int apx = tid >> 1, ahalf = tid & 1;
+  const long ap = p0 + apx;
+  int an = 0, ah = 0, aw = 0;
+  if (ap < P) {
+    an = (int)(ap / ((long)H * W));
+    const int rem = (int)(ap - (long)an * H * W);
+    ah = rem / W;
+    aw = rem - ah * W;
+  }
+  for (int tap = 0; tap < 9; ++tap) {
+    const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+    const int hh = ah + dy, ww = aw + dx;
+    const bool inside = ap < P && hh >= 0 && hh < H && ww >= 0 && ww < W;
+    const float* src = X + (((long)an * H + hh) * W + ww) * Cin + ahalf * 8;
+    for (int c0 = 0; c0 < Cin; c0 += 16) {
+      // A: 64 pixels x 16 channels
+      float4 v0 = make_float4(0.f, 0.f, 0.f, 0.f), v1 = v0;
+      if (inside) {
+        v0 = *reinterpret_cast<const float4*>(src + c0);
+        v1 = *reinterpret_cast<const float4*>(src + c0 + 4);
+      }
+      uint4 pk;
+      pk.x = pack_bf16x2(v0.x, v0.y);
+      pk.y = pack_bf16x2(v0.z, v0.w);
+      pk.z = pack_bf16x2(v1.x, v1.y);
+      pk.w = pack_bf16x2(v1.z, v1.w);
+      *reinterpret_cast<uint4*>(&As[apx * CONV_AS + ahalf * 8]) = pk;
+      // B: 16 x Cout, stored transposed
+      const __nv_bfloat16* wsrc = Wt + ((long)tap * Cin + c0) * Cout;
+      for (int e = tid; e < 16 * Cout; e += CONV_THREADS) {
+        const int k = e / Cout, n = e - k * Cout;
+        Bs[n * CONV_BS + k] = wsrc[(long)k * Cout + n];
+      }
+      __syncthreads();
+      uint32_t a[4];
+      const int r = warp * 16 + g;
+      a[0] = *reinterpret_cast<const uint32_t*>(&As[r * CONV_AS + tg * 2]);
+      a[1] = *reinterpret_cast<const uint32_t*>(&As[(r + 8) * CONV_AS + tg * 2]);
+      a[2] = *reinterpret_cast<const uint32_t*>(&As[r * CONV_AS + tg * 2 + 8]);
+      a[3] = *reinterpret_cast<const uint32_t*>(&As[(r + 8) * CONV_AS + tg * 2 + 8]);
+#pragma unroll
+      for (int t = 0; t < NT; ++t) {
+        uint32_t b[2];
+        const int n = t * 8 + g;
+        b[0] = *reinterpret_cast<const uint32_t*>(&Bs[n * CONV_BS + tg * 2]);
+        b[1] = *reinterpret_cast<const uint32_t*>(&Bs[n * CONV_BS + tg * 2 + 8]);
+        mma_bf16(acc[t], a, b);
+      }
+      __syncthreads();
+    }
+  }
+  // epilogue: bias, ReLU, store
+#pragma unroll
+  for (int t = 0; t < NT; ++t) {
+    const int col = t * 8 + tg * 2;
+    const float b0 = bias ? bias[col] : 0.f, b1 = bias ? bias[col + 1] : 0.f;
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      const long p = p0 + warp * 16 + g + half * 8;
+      if (p >= P) continue;
+      float y0 = acc[t][half * 2] + b0, y1 = acc[t][half * 2 + 1] + b1;
+      if (relu) {
+        y0 = fmaxf(y0, 0.f);
+        y1 = fmaxf(y1, 0.f);
+      }
+      *reinterpret_cast<float2*>(&Y[p * Cout + col]) = make_float2(y0, y1);
+    }
+  }
+}
+
+static int conv3x3(const float* X, int N, int H, int W, int Cin, int Cout,
+                   const __nv_bfloat16* Wt, const float* bias, float* Y, int relu,
+                   cudaStream_t st) {
+  const long P = (long)N * H * W;
+  dim3 grid(cdiv(P, CONV_BM));
+  switch (Cout) {
+    case 8: k_conv3x3<1><<<grid, CONV_THREADS, 0, st>>>(X, N, H, W, Cin, Wt, bias, Y, relu); break;
+    case 16: k_conv3x3<2><<<grid, CONV_THREADS, 0, st>>>(X, N, H, W, Cin, Wt, bias, Y, relu); break;
+    case 32: k_conv3x3<4><<<grid, CONV_THREADS, 0, st>>>(X, N, H, W, Cin, Wt, bias, Y, relu); break;
+    case 64: k_conv3x3<8><<<grid, CONV_THREADS, 0, st>>>(X, N, H, W, Cin, Wt, bias, Y, relu); break;
+    case 128: k_conv3x3<16><<<grid, CONV_THREADS, 0, st>>>(X, N, H, W, Cin, Wt, bias, Y, relu); break;
+    default: return AJ_ERR_PARAM;
+  }
+  return AJ_OK;
+}
+
+// ---------------------------------------------------------------- weight gradient
+// dW[tap][ci][co] += sum_p Xshift(p)[ci] * dZ[p][co]: GEMM with M = Cin,
+// N = Cout, K = pixels.  One block per (tap, pixel chunk); 8 warps share the
+// (Cin/16) x (Cout/8) output tiles; the partial sums are added atomically.
+constexpr int DW_THREADS = 256, DW_KC = 64, DW_CHUNK = 4096;
+constexpr int DW_S = DW_KC + 8;     // bf16 row stride of the staged tiles
+
+__global__ void __launch_bounds__(DW_THREADS) k_conv_dw(const float* __restrict__ X,
+                                                        const float* __restrict__ dZ, int N, int H,
+                                                        int W, int Cin, int Cout,
+                                                        float* __restrict__ dW) {
+  __shared__ __align__(16) __nv_bfloat16 As[128 * DW_S];   // [ci][px]
+  __shared__ __align__(16) __nv_bfloat16 Bs[128 * DW_S];   // [co][px]
+  const int tap = blockIdx.y;
+  const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+  const long P = (long)N * H * W;
+  const long pbeg = (long)blockIdx.x * DW_CHUNK;
+  const long pend = pbeg + DW_CHUNK < P ? pbeg + DW_CHUNK : P;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int g = lane >> 2, tg = lane & 3;
+  const int MT = Cin / 16, NTt = Cout / 8, ntiles = MT * NTt;
+  constexpr int MAXT = 16;          // tiles per warp (128x128 / 8 warps / (16x8))
+  float acc[MAXT][4];
+#pragma unroll
+  for (int q = 0; q < MAXT; ++q) acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.f;
+  for (long pc = pbeg; pc < pend; pc += DW_KC) {
+    // stage X shifted (transposed to [ci][px]) and dZ (transposed to [co][px])
+    for (int e = tid; e < DW_KC * Cin; e += DW_THREADS) {
+      const int px = e / Cin, ci = e - px * Cin;
+      const long p = pc + px;
+      float v = 0.f;
+      if (p < pend) {
+        const int n = (int)(p / ((long)H * W));
+        const int rem = (int)(p - (long)n * H * W);
+        const int h = rem / W + dy, w = rem % W + dx;
+        if (h >= 0 && h < H && w >= 0 && w < W) v = X[(((long)n * H + h) * W + w) * Cin + ci];
+      }
+      As[ci * DW_S + px] = __float2bfloat16_rn(v);
+    }
+    for (int e = tid; e < DW_KC * Cout; e += DW_THREADS) {
+      const int px = e / Cout, co = e - px * Cout;
+      const long p = pc + px;
+      Bs[co * DW_S + px] = __float2bfloat16_rn(p < pend ? dZ[p * Cout + co] : 0.f);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int ks = 0; ks < DW_KC; ks += 16) {
+#pragma unroll
+      for (int q = 0; q < MAXT; ++q) {
+        const int tile = warp + q * 8;
+        if (tile >= ntiles) break;
+        const int mt = tile / NTt, nt = tile - mt * NTt;
+        const int r = mt * 16 + g;
+        uint32_t a[4], b[2];
+        a[0] = *reinterpret_cast<const uint32_t*>(&As[r * DW_S + ks + tg * 2]);
+        a[1] = *reinterpret_cast<const uint32_t*>(&As[(r + 8) * DW_S + ks + tg * 2]);
+        a[2] = *reinterpret_cast<const uint32_t*>(&As[r * DW_S + ks + tg * 2 + 8]);
+        a[3] = *reinterpret_cast<const uint32_t*>(&As[(r + 8) * DW_S + ks + tg * 2 + 8]);
+        const int n = nt * 8 + g;
+        b[0] = *reinterpret_cast<const uint32_t*>(&Bs[n * DW_S + ks + tg * 2]);
+        b[1] = *reinterpret_cast<const uint32_t*>(&Bs[n * DW_S + ks + tg * 2 + 8]);
+        mma_bf16(acc[q], a, b);
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int q = 0; q < MAXT; ++q) {
+    const int tile = warp + q * 8;
+    if (tile >= ntiles) break;
+    const int mt = tile / NTt, nt = tile - mt * NTt;
+    const int col = nt * 8 + tg * 2;
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      const int ci = mt * 16 + g + half * 8;
+      float* dst = dW + ((long)tap * Cin + ci) * Cout + col;
+      atomicAdd(dst, acc[q][half * 2]);
+      atomicAdd(dst + 1, acc[q][half * 2 + 1]);
+    }
+  }
+}
+
+// db[co] += sum_p dZ[p][co]
+__global__ void k_bias_grad(const float* __restrict__ dZ, long P, int C, float* __restrict__ db) {
+  const int co = threadIdx.x % C;
+  const int lanes = blockDim.x / C;
+  const int li = threadIdx.x / C;
+  if (li >= lanes) return;
+  float s = 0.f;
+  for (long p = (long)blockIdx.x * lanes + li; p < P; p += (long)gridDim.x * lanes) s += dZ[p * C + co];
+  atomicAdd(&db[co], s);
+}
+
+// ---------------------------------------------------------------- element-wise
+__global__ void k_pool2(const float* __restrict__ X, float* __restrict__ Y, int N, int H, int W,
+                        int C) {   // H, W of the output
+  long e = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const long T = (long)N * H * W * C;
+  if (e >= T) return;
+  const int c = (int)(e % C);
+  long q = e / C;
+  const int w = (int)(q % W);
+  q /= W;
+  const int h = (int)(q % H);
+  const int n = (int)(q / H);
+  const int W2 = 2 * W;
+  const long b = (((long)n * 2 * H + 2 * h) * W2 + 2 * w) * C + c;
+  Y[e] = 0.25f * (X[b] + X[b + (long)W2 * C] + X[b + C] + X[b + (long)W2 * C + C]);
+}
+
+// dX (fine, accumulated) += pool2 adjoint of dY (coarse)
+__global__ void k_pool2_bwd(const float* __restrict__ dY, float* __restrict__ dX, int N, int H,
+                            int W, int C) {   // H, W of dY
+  long e = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const long T = (long)N * 2 * H * 2 * W * C;
+  if (e >= T) return;
+  const int c = (int)(e % C);
+  long q = e / C;
+  const int w = (int)(q % (2 * W));
+  q /= 2 * W;
+  const int h = (int)(q % (2 * H));
+  const int n = (int)(q / (2 * H));
+  dX[e] += 0.25f * dY[(((long)n * H + h / 2) * W + w / 2) * C + c];
+}
+
+// Y (fine) = up2(X coarse) + S (fine)
+__global__ void k_up2_add(const float* __restrict__ X, const float* __restrict__ S,
+                          float* __restrict__ Y, int N, int H, int W, int C) {   // fine H, W
+  long e = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const long T = (long)N * H * W * C;
+  if (e >= T) return;
+  const int c = (int)(e % C);
+  long q = e / C;
+  const int w = (int)(q % W);
+  q /= W;
+  const int h = (int)(q % H);
+  const int n = (int)(q / H);
+  Y[e] = X[(((long)n * (H / 2) + h / 2) * (W / 2) + w / 2) * C + c] + S[e];
+}
+
+// dX (coarse) = adjoint of nearest up2 applied to dY (fine)
+__global__ void k_up2_bwd(const float* __restrict__ dY, float* __restrict__ dX, int N, int H,
+                          int W, int C) {   // coarse H, W
+  long e = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const long T = (long)N * H * W * C;
+  if (e >= T) return;
+  const int c = (int)(e % C);
+  long q = e / C;
+  const int w = (int)(q % W);
+  q /= W;
+  const int h = (int)(q % H);
+  const int n = (int)(q / H);
+  const int W2 = 2 * W;
+  const long b = (((long)n * 2 * H + 2 * h) * W2 + 2 * w) * C + c;
+  dX[e] = dY[b] + dY[b + (long)W2 * C] + dY[b + C] + dY[b + (long)W2 * C + C];
+}
+
+// dZ = dOut * (Y > 0)   (ReLU adjoint)
+__global__ void k_relu_gate(const float* __restrict__ dOut, const float* __restrict__ Y,
+                            float* __restrict__ dZ, long T) {
+  long e = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (e < T) dZ[e] = Y[e] > 0.f ? dOut[e] : 0.f;
+}
+
+// loss = mean over pixels of (y[.,0] - target)^2; dy = its gradient
+__global__ void k_mse(const float* __restrict__ y, const float* __restrict__ target,
+                      float* __restrict__ dy, long P, double* loss) {
+  float s = 0.f;
+  const float inv = 1.f / (float)P;
+  for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < P; p += (long)gridDim.x * blockDim.x) {
+    const float d = y[p * 16] - target[p];
+    s = fmaf(d, d, s);
+    dy[p * 16] = 2.f * d * inv;
+#pragma unroll
+    for (int c = 1; c < 16; ++c) dy[p * 16 + c] = 0.f;
+  }
+  block_sum_atomic((double)s * (double)inv, loss);
+}
+
+// Adam with element-wise clipping of the gradient to [-clip, clip]
+__global__ void k_adam(float* __restrict__ w, const float* __restrict__ gr, float* __restrict__ m,
+                       float* __restrict__ v, long n, float lr, float b1, float b2, float eps,
+                       float clip, float c1, float c2) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float g = fminf(fmaxf(gr[i], -clip), clip);
+  float mi = b1 * m[i] + (1.f - b1) * g;
+  float vi = b2 * v[i] + (1.f - b2) * g * g;
+  m[i] = mi;
+  v[i] = vi;
+  w[i] -= lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+}
+
+struct PackTab {
+  int nl;
+  long woff[NL], poff[NL];
+  int cin[NL], cout[NL];
+};
+
+// FP32 master weights -> BF16 Wf[tap][ci][co] and Wb[8-tap][co][ci]
+__global__ void k_pack(const float* __restrict__ master, __nv_bfloat16* __restrict__ packed,
+                       PackTab tab) {
+  const int l = blockIdx.y;
+  const int cin = tab.cin[l], cout = tab.cout[l];
+  const long nw = 9L * cin * cout;
+  const float* W = master + tab.woff[l];
+  __nv_bfloat16* Wf = packed + tab.poff[l];
+  __nv_bfloat16* Wb = Wf + nw;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < nw; e += (long)gridDim.x * blockDim.x) {
+    const int co = (int)(e % cout);
+    const long q = e / cout;
+    const int ci = (int)(q % cin);
+    const int tap = (int)(q / cin);
+    const __nv_bfloat16 b = __float2bfloat16_rn(W[e]);
+    Wf[e] = b;
+    Wb[((long)(8 - tap) * cout + co) * cin + ci] = b;
+  }
+}
+
+static PackTab pack_tab() {
+  PackTab t;
+  t.nl = NL;
+  for (int l = 0; l < NL; ++l) {
+    t.woff[l] = (long)w_off(l);
+    t.poff[l] = (long)pk_off(l);
+    t.cin[l] = kLayers[l].cin;
+    t.cout[l] = kLayers[l].cout;
+  }
+  return t;
+}
+
+// ---------------------------------------------------------------- activations
+// Every tensor the backward pass needs, for batch n at the network grid h x w.
+struct NnActs {
+  float *x, *a0, *s0, *p0, *a1, *s1, *p1, *a2, *s2, *p2, *a3, *bt;
+  float *u2, *o2, *u1, *o1, *u0, *o0, *y;
+  // backward: skip-connection gradients and two scratch buffers per resolution
+  float *ds0, *ds1, *ds2, *sa0, *sa1, *sb1, *sa2, *sb2, *sa3, *sb3;
+  size_t total;
+};
+
+static NnActs act_layout(int n, int h, int w, void* base) {
+  NnActs A;
+  size_t off = 0;
+  char* b = static_cast<char*>(base);
+  auto take = [&](long elems) {
+    float* p = reinterpret_cast<float*>(b ? b + off : nullptr);
+    off += ((size_t)elems * 4 + 255) & ~(size_t)255;
+    return p;
+  };
+  const long P0 = (long)n * h * w, P1 = P0 / 4, P2 = P0 / 16, P3 = P0 / 64;
+  A.x = take(P0 * 16);
+  A.a0 = take(P0 * 32);
+  A.s0 = take(P0 * 32);
+  A.p0 = take(P1 * 32);
+  A.a1 = take(P1 * 64);
+  A.s1 = take(P1 * 64);
+  A.p1 = take(P2 * 64);
+  A.a2 = take(P2 * 128);
+  A.s2 = take(P2 * 128);
+  A.p2 = take(P3 * 128);
+  A.a3 = take(P3 * 128);
+  A.bt = take(P3 * 128);
+  A.u2 = take(P2 * 128);
+  A.o2 = take(P2 * 64);
+  A.u1 = take(P1 * 64);
+  A.o1 = take(P1 * 32);
+  A.u0 = take(P0 * 32);
+  A.o0 = take(P0 * 32);
+  A.y = take(P0 * 16);
+  A.ds0 = take(P0 * 32);
+  A.sa0 = take(P0 * 32);
+  A.ds1 = take(P1 * 64);
+  A.sa1 = take(P1 * 64);
+  A.sb1 = take(P1 * 32);
+  A.ds2 = take(P2 * 128);
+  A.sa2 = take(P2 * 128);
+  A.sb2 = take(P2 * 64);
+  A.sa3 = take(P3 * 128);
+  A.sb3 = take(P3 * 128);
+  A.total = off;
+  return A;
+}
+
+struct NnW {
+  const __nv_bfloat16* packed;
+  const float* master;
+  const __nv_bfloat16* wf(int l) const { return packed + pk_off(l); }
+  const __nv_bfloat16* wb(int l) const {
+    return packed + pk_off(l) + 9 * (size_t)kLayers[l].cin * kLayers[l].cout;
+  }
+  const float* bias(int l) const { return master + b_off(l); }
+};
+
+static inline unsigned ew_blocks(long T) { return cdiv(T, 256); }
+
+int nn_forward(int n, int h, int w, const NnW& W, const NnActs& A, cudaStream_t st) {
+  const int H0 = h, W0 = w, H1 = h / 2, W1 = w / 2, H2 = h / 4, W2 = w / 4, H3 = h / 8, W3 = w / 8;
+  auto conv = [&](int l, const float* in, float* out, int H, int Wd) {
+    return conv3x3(in, n, H, Wd, kLayers[l].cin, kLayers[l].cout, W.wf(l), W.bias(l), out,
+                   kLayers[l].relu, st);
+  };
+  int rc = AJ_OK;
+  rc |= conv(E0A, A.x, A.a0, H0, W0);
+  rc |= conv(E0B, A.a0, A.s0, H0, W0);
+  k_pool2<<<ew_blocks((long)n * H1 * W1 * 32), 256, 0, st>>>(A.s0, A.p0, n, H1, W1, 32);
+  rc |= conv(E1A, A.p0, A.a1, H1, W1);
+  rc |= conv(E1B, A.a1, A.s1, H1, W1);
+  k_pool2<<<ew_blocks((long)n * H2 * W2 * 64), 256, 0, st>>>(A.s1, A.p1, n, H2, W2, 64);
+  rc |= conv(E2A, A.p1, A.a2, H2, W2);
+  rc |= conv(E2B, A.a2, A.s2, H2, W2);
+  k_pool2<<<ew_blocks((long)n * H3 * W3 * 128), 256, 0, st>>>(A.s2, A.p2, n, H3, W3, 128);
+  rc |= conv(E3A, A.p2, A.a3, H3, W3);
+  rc |= conv(E3B, A.a3, A.bt, H3, W3);
+  k_up2_add<<<ew_blocks((long)n * H2 * W2 * 128), 256, 0, st>>>(A.bt, A.s2, A.u2, n, H2, W2, 128);
+  rc |= conv(D2, A.u2, A.o2, H2, W2);
+  k_up2_add<<<ew_blocks((long)n * H1 * W1 * 64), 256, 0, st>>>(A.o2, A.s1, A.u1, n, H1, W1, 64);
+  rc |= conv(D1, A.u1, A.o1, H1, W1);
+  k_up2_add<<<ew_blocks((long)n * H0 * W0 * 32), 256, 0, st>>>(A.o1, A.s0, A.u0, n, H0, W0, 32);
+  rc |= conv(D0A, A.u0, A.o0, H0, W0);
+  rc |= conv(D0B, A.o0, A.y, H0, W0);
+  if (rc != AJ_OK) return AJ_ERR_PARAM;
+  return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+}
+
+// gradient of one conv layer: dz = dout (* ReLU gate), dW, db, and (if dx) the
+// input gradient
+static void layer_bwd(int l, int n, int H, int Wd, const float* in, const float* out,
+                      const float* dout, float* dz, float* dx, const NnW& W, float* grad,
+                      cudaStream_t st) {
+  const int cin = kLayers[l].cin, cout = kLayers[l].cout;
+  const long P = (long)n * H * Wd;
+  const float* g = dout;
+  if (kLayers[l].relu) {
+    k_relu_gate<<<ew_blocks(P * cout), 256, 0, st>>>(dout, out, dz, P * cout);
+    g = dz;
+  }
+  dim3 gdw(cdiv(P, DW_CHUNK), 9);
+  k_conv_dw<<<gdw, DW_THREADS, 0, st>>>(in, g, n, H, Wd, cin, cout, grad + w_off(l));
+  const int lanes = 256 / cout;
+  unsigned nb = cdiv(P, (long)lanes * 64);
+  if (nb > 512) nb = 512;
+  k_bias_grad<<<nb, lanes * cout, 0, st>>>(g, P, cout, grad + b_off(l));
+  if (dx) conv3x3(g, n, H, Wd, cout, cin, W.wb(l), nullptr, dx, 0, st);
+}
+
+int nn_backward(int n, int h, int w, const float* dy, const NnW& W, const NnActs& A, float* grad,
+                cudaStream_t st) {
+  const int H0 = h, W0 = w, H1 = h / 2, W1 = w / 2, H2 = h / 4, W2 = w / 4, H3 = h / 8, W3 = w / 8;
+  const long P0 = (long)n * H0 * W0, P1 = P0 / 4, P2 = P0 / 16, P3 = P0 / 64;
+  if (cudaMemsetAsync(grad, 0, n_params() * 4, st) != cudaSuccess) return AJ_ERR_CUDA;
+  // Each layer_bwd gates its incoming gradient in place and writes the input
+  // gradient to a different buffer.  Decoder first: y = d0b(o0),
+  // o0 = d0a(u0), u0 = up(o1) + s0, ...
+  layer_bwd(D0B, n, H0, W0, A.o0, A.y, dy, nullptr, A.sa0, W, grad, st);        // sa0 = d o0
+  layer_bwd(D0A, n, H0, W0, A.u0, A.o0, A.sa0, A.sa0, A.ds0, W, grad, st);      // ds0 = d u0
+  k_up2_bwd<<<ew_blocks(P1 * 32), 256, 0, st>>>(A.ds0, A.sa1, n, H1, W1, 32);   // sa1 = d o1
+  layer_bwd(D1, n, H1, W1, A.u1, A.o1, A.sa1, A.sa1, A.ds1, W, grad, st);       // ds1 = d u1
+  k_up2_bwd<<<ew_blocks(P2 * 64), 256, 0, st>>>(A.ds1, A.sa2, n, H2, W2, 64);   // sa2 = d o2
+  layer_bwd(D2, n, H2, W2, A.u2, A.o2, A.sa2, A.sa2, A.ds2, W, grad, st);       // ds2 = d u2
+  k_up2_bwd<<<ew_blocks(P3 * 128), 256, 0, st>>>(A.ds2, A.sa3, n, H3, W3, 128); // sa3 = d bt
+  // encoder: the skip gradients ds* accumulate the pooled paths
+  layer_bwd(E3B, n, H3, W3, A.a3, A.bt, A.sa3, A.sa3, A.sb3, W, grad, st);      // sb3 = d a3
+  layer_bwd(E3A, n, H3, W3, A.p2, A.a3, A.sb3, A.sb3, A.sa3, W, grad, st);      // sa3 = d p2
+  k_pool2_bwd<<<ew_blocks(P2 * 128), 256, 0, st>>>(A.sa3, A.ds2, n, H3, W3, 128);   // ds2 = d s2
+  layer_bwd(E2B, n, H2, W2, A.a2, A.s2, A.ds2, A.ds2, A.sa2, W, grad, st);      // sa2 = d a2
+  layer_bwd(E2A, n, H2, W2, A.p1, A.a2, A.sa2, A.sa2, A.sb2, W, grad, st);      // sb2 = d p1
+  k_pool2_bwd<<<ew_blocks(P1 * 64), 256, 0, st>>>(A.sb2, A.ds1, n, H2, W2, 64);     // ds1 = d s1
+  layer_bwd(E1B, n, H1, W1, A.a1, A.s1, A.ds1, A.ds1, A.sa1, W, grad, st);      // sa1 = d a1
+  layer_bwd(E1A, n, H1, W1, A.p0, A.a1, A.sa1, A.sa1, A.sb1, W, grad, st);      // sb1 = d p0
+  k_pool2_bwd<<<ew_blocks(P0 * 32), 256, 0, st>>>(A.sb1, A.ds0, n, H1, W1, 32);     // ds0 = d s0
+  layer_bwd(E0B, n, H0, W0, A.a0, A.s0, A.ds0, A.ds0, A.sa0, W, grad, st);      // sa0 = d a0
+  layer_bwd(E0A, n, H0, W0, A.x, A.a0, A.sa0, A.sa0, nullptr, W, grad, st);
+  return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+}
+
+static bool nn_shape_ok(int n, int h, int w) { return n >= 1 && h >= 8 && w >= 8 && h % 8 == 0 && w % 8 == 0; }
+
+// ---------------------------------------------------------------- warm start
+// Network inputs on the grid F times coarser than the pressure grid:
+//   channel 0: F x F average of the previous pressure's residual b - A p_prev
+//              (the reference operator: edge ghosts, outlet row pinned)
+//   channel 1: F x F average of the mask
+//   channel 2: F x F average of p_prev
+// channels 3..15 are zero.  Also the FP64 sums of channel 0^2 and 2^2.
+__global__ void __launch_bounds__(256) k_nn_feat(const float* __restrict__ b,
+                                                 const float* __restrict__ mask,
+                                                 const float* __restrict__ pp, int nx, int ny,
+                                                 int F, float ax, float ay, float* __restrict__ x,
+                                                 DevScalars* sc) {
+  const int J = blockIdx.x * blockDim.x + threadIdx.x;
+  const int I = blockIdx.y * blockDim.y + threadIdx.y;
+  const int h = nx / F, w = ny / F;
+  float sr = 0.f, sp = 0.f;
+  if (I < h && J < w) {
+    float ar = 0.f, am = 0.f, ap = 0.f;
+    for (int di = 0; di < F; ++di) {
+      const int i = I * F + di;
+      for (int dj = 0; dj < F; ++dj) {
+        const int j = J * F + dj;
+        const long k = (long)i * ny + j;
+        const float c = pp[k];
+        float r = 0.f;
+        if (i != nx - 1) {
+          const float xp = pp[k + ny];
+          const float xm = i > 0 ? pp[k - ny] : c;
+          const float yp = j + 1 < ny ? pp[k + 1] : c;
+          const float ym = j > 0 ? pp[k - 1] : c;
+          r = b[k] - (ax * ((xp - c) + (xm - c)) + ay * ((yp - c) + (ym - c)));
+        }
+        ar += r;
+        am += mask[k];
+        ap += c;
+      }
+    }
+    const float inv = 1.f / (float)(F * F);
+    ar *= inv;
+    am *= inv;
+    ap *= inv;
+    float* o = x + ((long)I * w + J) * 16;
+    o[0] = ar;
+    o[1] = am;
+    o[2] = ap;
+#pragma unroll
+    for (int c = 3; c < 16; ++c) o[c] = 0.f;
+    sr = ar * ar;
+    sp = ap * ap;
+  }
+  block_sum_atomic((double)sr, &sc->acc[2]);
+  block_sum_atomic((double)sp, &sc->acc[3]);
+}
+
+// per-sample scales: channel RMS values and the output scale
+// rms_r * lmin^2 / 10 (a correction solving A dp = r has that magnitude)
+__global__ void k_nn_scale(DevScalars* sc, long cells, double lmin2) {
+  const double rr = sqrt(sc->acc[2] / (double)cells), rp = sqrt(sc->acc[3] / (double)cells);
+  sc->nn_rms_r = rr > 1e-30 ? rr : 1e-30;
+  sc->nn_rms_p = rp > 1e-30 ? rp : 1e-30;
+  sc->nn_out_scale = sc->nn_rms_r * lmin2 / 10.0;
+  sc->acc[2] = 0.0;
+  sc->acc[3] = 0.0;
+}
+
+// normalise channels 0 and 2 in place; optionally copy the 3 features out
+__global__ void k_nn_norm(float* __restrict__ x, float* __restrict__ x3, long cells,
+                          const DevScalars* sc) {
+  const long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (c >= cells) return;
+  const float ir = (float)(1.0 / sc->nn_rms_r), ip = (float)(1.0 / sc->nn_rms_p);
+  float* o = x + c * 16;
+  o[0] *= ir;
+  o[2] *= ip;
+  if (x3) {
+    x3[c * 3] = o[0];
+    x3[c * 3 + 1] = o[1];
+    x3[c * 3 + 2] = o[2];
+  }
+}
+
+// training target: F x F average of (p_true - p_prev) / out_scale
+__global__ void k_nn_target(const float* __restrict__ pt, const float* __restrict__ pp, int nx,
+                            int ny, int F, float* __restrict__ target, const DevScalars* sc) {
+  const int J = blockIdx.x * blockDim.x + threadIdx.x;
+  const int I = blockIdx.y * blockDim.y + threadIdx.y;
+  const int h = nx / F, w = ny / F;
+  if (I >= h || J >= w) return;
+  float a = 0.f;
+  for (int di = 0; di < F; ++di)
+    for (int dj = 0; dj < F; ++dj) {
+      const long k = (long)(I * F + di) * ny + J * F + dj;
+      a += pt[k] - pp[k];
+    }
+  target[(long)I * w + J] = (float)((double)(a / (float)(F * F)) / sc->nn_out_scale);
+}
+
+// p_init = p_prev + bilinear prolongation of (prediction * out_scale); the
+// outlet row stays pinned at 0
+__global__ void k_nn_apply(const float* __restrict__ y, const float* __restrict__ pp, int nx,
+                           int ny, int F, float* __restrict__ pinit, const DevScalars* sc) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= nx || j >= ny) return;
+  const long k = (long)i * ny + j;
+  if (i == nx - 1) {
+    pinit[k] = 0.f;
+    return;
+  }
+  const int h = nx / F, w = ny / F;
+  const float xi = (i + 0.5f) / F - 0.5f, xj = (j + 0.5f) / F - 0.5f;
+  int i0 = (int)floorf(xi), j0 = (int)floorf(xj);
+  const float ti = xi - i0, tj = xj - j0;
+  const int i1 = min(max(i0 + 1, 0), h - 1), j1 = min(max(j0 + 1, 0), w - 1);
+  i0 = min(max(i0, 0), h - 1);
+  j0 = min(max(j0, 0), w - 1);
+  const float v00 = y[((long)i0 * w + j0) * 16], v01 = y[((long)i0 * w + j1) * 16];
+  const float v10 = y[((long)i1 * w + j0) * 16], v11 = y[((long)i1 * w + j1) * 16];
+  const float v = (1.f - ti) * ((1.f - tj) * v00 + tj * v01) + ti * ((1.f - tj) * v10 + tj * v11);
+  pinit[k] = pp[k] + (float)(v * sc->nn_out_scale);
+}
+
+// [n][h][w][3] -> [n][h][w][16] (zeros beyond the features)
+__global__ void k_nn_expand(const float* __restrict__ x3, float* __restrict__ x16, long cells) {
+  const long e = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (e >= cells * 16) return;
+  const long c = e / 16;
+  const int ch = (int)(e - c * 16);
+  x16[e] = ch < 3 ? x3[c * 3 + ch] : 0.f;
+}
+
+// features (+ optional dataset copy and target) for one step's pressure solve
+int nn_features(const AjStepParams& p, void* ws, const float* b, const float* mask,
+                const float* pp, const float* pt, float* x16, float* x3, float* target,
+                cudaStream_t st) {
+  const int F = p.nn_factor, h = p.nx / F, w = p.ny / F;
+  DevScalars* sc = at<DevScalars>(ws, 0);
+  dim3 blk(32, 8), grd(cdiv(w, 32), cdiv(h, 8));
+  k_nn_feat<<<grd, blk, 0, st>>>(b, mask, pp, p.nx, p.ny, F, (float)(1.0 / (p.dx * p.dx)),
+                                 (float)(1.0 / (p.dy * p.dy)), x16, sc);
+  const double lx = p.nx * p.dx, ly = p.ny * p.dy, lmin = lx < ly ? lx : ly;
+  k_nn_scale<<<1, 1, 0, st>>>(sc, (long)h * w, lmin * lmin);
+  k_nn_norm<<<cdiv((long)h * w, 256), 256, 0, st>>>(x16, x3, (long)h * w, sc);
+  if (pt && target) k_nn_target<<<grd, blk, 0, st>>>(pt, pp, p.nx, p.ny, F, target, sc);
+  return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+}
+
+// the learned warm start inside a step: features, network, p_init
+int nn_warm_start(const AjStepParams& p, const Layout& L, void* ws, const float* b,
+                  const float* mask, const float* pp, const uint16_t* packed, const float* master,
+                  float* pinit, cudaStream_t st) {
+  const int F = p.nn_factor, h = p.nx / F, w = p.ny / F;
+  NnActs A = act_layout(1, h, w, at<char>(ws, L.nn_act));
+  int rc = nn_features(p, ws, b, mask, pp, nullptr, A.x, nullptr, nullptr, st);
+  if (rc != AJ_OK) return rc;
+  NnW W{reinterpret_cast<const __nv_bfloat16*>(packed), master};
+  rc = nn_forward(1, h, w, W, A, st);
+  if (rc != AJ_OK) return rc;
+  dim3 blk(32, 8), grd(cdiv(p.ny, 32), cdiv(p.nx, 8));
+  k_nn_apply<<<grd, blk, 0, st>>>(A.y, pp, p.nx, p.ny, F, pinit, at<DevScalars>(ws, 0));
+  return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+}
+
+size_t nn_step_act_bytes(const AjStepParams& p) {
+  if (p.nn_factor <= 0) return 0;
+  return act_layout(1, p.nx / p.nn_factor, p.ny / p.nn_factor, nullptr).total;
+}
+
+bool nn_step_shape_ok(const AjStepParams& p) {
+  const int F = p.nn_factor;
+  if (F <= 0) return true;
+  if (p.nx % F || p.ny % F) return false;
+  return nn_shape_ok(1, p.nx / F, p.ny / F);
+}
+
+}  // namespace aj
+
+using namespace aj;
+
+extern "C" {
+
+size_t aj_nn_param_count(void) { return n_params(); }
+size_t aj_nn_packed_count(void) { return n_packed(); }
+
+size_t aj_nn_act_bytes(int32_t n, int32_t h, int32_t w) {
+  if (!nn_shape_ok(n, h, w)) return 0;
+  return act_layout(n, h, w, nullptr).total;
+}
+
+// the network input [n][h][w][16] inside the activation buffer
+float* aj_nn_input(int32_t n, int32_t h, int32_t w, void* act) {
+  if (!nn_shape_ok(n, h, w) || !act) return nullptr;
+  return act_layout(n, h, w, act).x;
+}
+
+int32_t aj_nn_pack(const float* master, uint16_t* packed, void* stream) {
+  if (!master || !packed) return AJ_ERR_PARAM;
+  dim3 grid(64, NL);
+  k_pack<<<grid, 256, 0, (cudaStream_t)stream>>>(master, reinterpret_cast<__nv_bfloat16*>(packed),
+                                                   pack_tab());
+  return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+}
+
+int32_t aj_nn_forward(int32_t n, int32_t h, int32_t w, const uint16_t* packed, const float* master,
+                      void* act, size_t act_bytes, float* y_out, void* stream) {
+  if (!nn_shape_ok(n, h, w) || !packed || !master || !act) return AJ_ERR_PARAM;
+  NnActs A = act_layout(n, h, w, act);
+  if (act_bytes < A.total) return AJ_ERR_WORKSPACE;
+  NnW W{reinterpret_cast<const __nv_bfloat16*>(packed), master};
+  cudaStream_t st = (cudaStream_t)stream;
+  int rc = nn_forward(n, h, w, W, A, st);
+  if (rc != AJ_OK) return rc;
+  if (y_out && cudaMemcpyAsync(y_out, A.y, (size_t)n * h * w * 16 * 4, cudaMemcpyDeviceToDevice,
+                               st) != cudaSuccess)
+    return AJ_ERR_CUDA;
+  return AJ_OK;
+}
+
+int32_t aj_nn_backward(int32_t n, int32_t h, int32_t w, const float* dy, const uint16_t* packed,
+                       const float* master, void* act, size_t act_bytes, float* grad,
+                       void* stream) {
+  if (!nn_shape_ok(n, h, w) || !dy || !packed || !master || !act || !grad) return AJ_ERR_PARAM;
+  NnActs A = act_layout(n, h, w, act);
+  if (act_bytes < A.total) return AJ_ERR_WORKSPACE;
+  NnW W{reinterpret_cast<const __nv_bfloat16*>(packed), master};
+  return nn_backward(n, h, w, dy, W, A, grad, (cudaStream_t)stream);
+}
+
+int32_t aj_nn_loss(int32_t n, int32_t h, int32_t w, const float* y, const float* target, float* dy,
+                   double* loss, void* stream) {
+  if (!nn_shape_ok(n, h, w) || !y || !target || !dy || !loss) return AJ_ERR_PARAM;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (cudaMemsetAsync(loss, 0, sizeof(double), st) != cudaSuccess) return AJ_ERR_CUDA;
+  const long P = (long)n * h * w;
+  unsigned nb = cdiv(P, 256 * 4);
+  if (nb > 1216) nb = 1216;
+  k_mse<<<nb, 256, 0, st>>>(y, target, dy, P, loss);
+  return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+}
+
+int32_t aj_nn_expand(int32_t n, int32_t h, int32_t w, const float* x3, float* x16, void* stream) {
+  if (!nn_shape_ok(n, h, w) || !x3 || !x16) return AJ_ERR_PARAM;
+  const long cells = (long)n * h * w;
+  k_nn_expand<<<cdiv(cells * 16, 256), 256, 0, (cudaStream_t)stream>>>(x3, x16, cells);
+  return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+}
+
+int32_t aj_nn_features(const AjStepParams* prm, const float* b, const float* mask,
+                       const float* p_prev, const float* p_true, float* x3_out, float* target_out,
+                       void* ws, size_t ws_bytes, void* stream) {
+  if (!prm || !b || !mask || !p_prev || prm->nn_factor <= 0) return AJ_ERR_PARAM;
+  Layout L;
+  if (!make_layout(*prm, L) || !nn_step_shape_ok(*prm)) return AJ_ERR_SHAPE;
+  if (!ws || ws_bytes < L.total) return AJ_ERR_WORKSPACE;
+  const int F = prm->nn_factor;
+  NnActs A = act_layout(1, prm->nx / F, prm->ny / F, at<char>(ws, L.nn_act));
+  return nn_features(*prm, ws, b, mask, p_prev, p_true, A.x, x3_out, target_out,
+                     (cudaStream_t)stream);
+}
+
+int32_t aj_nn_adam(float* master, const float* grad, float* m, float* v, int32_t step, float lr,
+                   float beta1, float beta2, float eps, float clip, void* stream) {
+  if (!master || !grad || !m || !v || step < 1) return AJ_ERR_PARAM;
+  const long n = (long)n_params();
+  const float c1 = (float)(1.0 / (1.0 - pow((double)beta1, step)));
+  const float c2 = (float)(1.0 / (1.0 - pow((double)beta2, step)));
+  k_adam<<<cdiv(n, 256), 256, 0, (cudaStream_t)stream>>>(master, grad, m, v, n, lr, beta1, beta2,
+                                                         eps, clip, c1, c2);
+  return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+}
+
+}  // extern "C"

@@ -124,6 +124,7 @@ class StepConfig:
     mg_tolerance: float = 1e-6
     max_cycles: int = 40
     warm_start: bool = False
+    nn_factor: int = 0
     has_sdf: bool = False
     cfl_dt: bool = False
     dt: float = 1e-3

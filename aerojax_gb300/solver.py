@@ -67,6 +67,7 @@ def make_params(cfg: StepConfig) -> AjStepParams:
     p.has_sdf = int(cfg.has_sdf)
     p.cfl_dt = int(cfg.cfl_dt)
     p.warm_start = int(cfg.warm_start)
+    p.nn_factor = int(cfg.nn_factor)
     p.dx, p.dy = cfg.dx, cfg.dy
     p.dt = cfg.dt
     p.dt_correction = cfg.dt_correction

@@ -74,6 +74,8 @@ typedef struct {
   int32_t has_sdf;               /* collocated: chi from sdf (rk3_simple_new.py:194)  */
   int32_t cfl_dt;                /* 1 = dt from the CFL rule on the device each step  */
   int32_t warm_start;            /* converging mode: start from p_guess               */
+  int32_t nn_factor;             /* learned warm start: network grid is nx/F x ny/F
+                                    (0 = off; aj_step_nn only)                        */
   double dx, dy;
   double dt;                     /* used when cfl_dt == 0                             */
   double dt_correction;          /* GUI: trace-time self.dt (step_handlers.py:139);
@@ -170,6 +172,58 @@ enum { AJ_GEOM_NONE = 0, AJ_GEOM_CYLINDER = 1, AJ_GEOM_NACA4 = 2, AJ_GEOM_CYL3_R
        AJ_GEOM_CYL3_TRI = 4 };
 int32_t aj_geometry(int32_t nx, int32_t ny, double lx, double ly, int32_t kind,
                     const double* geo_host, double eps, float* mask, float* sdf, void* stream);
+
+/* ---------------------------------------------------------------------------
+   Learned pressure warm start.  The reference's learned operators
+   (neural_operators/nn_pressure_operator_*.py, trained by
+   neural_operators/training_utils.py:84-253) replace the pressure solve
+   (step_handlers.py:101-107); here a 4-level convolutional encoder-decoder
+   (3x3 convs, base 32 channels, ~0.69 M parameters, BF16 tensor-core
+   operands with FP32 accumulation) predicts a correction to the previous
+   pressure on a grid nn_factor times coarser, and the converging multigrid
+   always finishes the solve to mg_rtol.  Parameters: one flat FP32 master
+   vector (per layer W[3][3][Cin][Cout] then b[Cout]) plus a BF16 packed copy
+   made by aj_nn_pack.  Activations: NHWC [n][h][w][c], h and w multiples of 8. */
+size_t aj_nn_param_count(void);
+size_t aj_nn_packed_count(void);
+size_t aj_nn_act_bytes(int32_t n, int32_t h, int32_t w);
+/* Device pointer of the network input [n][h][w][16] inside an activation buffer. */
+float* aj_nn_input(int32_t n, int32_t h, int32_t w, void* act);
+int32_t aj_nn_pack(const float* master, uint16_t* packed, void* stream);
+/* Forward pass; activations stay in `act` for the backward pass; y_out
+   ([n][h][w][16], channel 0 = prediction) may be NULL. */
+int32_t aj_nn_forward(int32_t n, int32_t h, int32_t w, const uint16_t* packed, const float* master,
+                      void* act, size_t act_bytes, float* y_out, void* stream);
+/* Gradient of sum(dy * y) w.r.t. the master parameters (grad is overwritten). */
+int32_t aj_nn_backward(int32_t n, int32_t h, int32_t w, const float* dy, const uint16_t* packed,
+                       const float* master, void* act, size_t act_bytes, float* grad,
+                       void* stream);
+/* MSE of channel 0 against target [n][h][w] (loss: one double, device), and dy. */
+int32_t aj_nn_loss(int32_t n, int32_t h, int32_t w, const float* y, const float* target, float* dy,
+                   double* loss, void* stream);
+/* Adam on the master parameters with gradients clipped to [-clip, clip]
+   (training_utils.py:162-188); step is 1-based. */
+int32_t aj_nn_adam(float* master, const float* grad, float* m, float* v, int32_t step, float lr,
+                   float beta1, float beta2, float eps, float clip, void* stream);
+/* [n][h][w][3] features -> [n][h][w][16] network input. */
+int32_t aj_nn_expand(int32_t n, int32_t h, int32_t w, const float* x3, float* x16, void* stream);
+/* Training data for one solve (prm->nn_factor > 0): features x3_out
+   [h][w][3] from the pressure rhs b (nx*ny, e.g. aj_workspace_rhs after a
+   step), the mask and the previous pressure; with p_true the target
+   [h][w] (nullable outputs).  Mirrors the reference's dataset contract
+   (training_utils.py:35-51). */
+int32_t aj_nn_features(const AjStepParams* prm, const float* b, const float* mask,
+                       const float* p_prev, const float* p_true, float* x3_out, float* target_out,
+                       void* workspace, size_t workspace_bytes, void* stream);
+/* The pressure right-hand side of the last aj_step / aj_step_nn on this
+   workspace (device pointer, nx*ny). */
+const float* aj_workspace_rhs(const AjStepParams* prm, void* workspace);
+/* One projection step (as aj_step, converging multigrid) whose pressure solve
+   starts from p_prev + the network's correction. */
+int32_t aj_step_nn(const AjStepParams* prm, const float* u, const float* v, const float* mask,
+                   const float* p_prev, const uint16_t* nn_packed, const float* nn_master,
+                   float* u_out, float* v_out, float* p_out, void* workspace,
+                   size_t workspace_bytes, AjStats* stats, void* stream);
 
 /* Allocation-free pressure solve, for callers that cannot allocate device
    memory: hosts that own every device byte through their own allocator (a

@@ -1,0 +1,242 @@
+"""Learned warm start on the GPU against the CPU oracle (oracle/nn_np.py):
+BF16 tensor-core forward and backward, loss, Adam, the solver-side features
+and the warm-started step."""
+import ctypes
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from oracle import nn_np as N
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def dev():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch.device("cuda:0")
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(np.ravel(a - b)) / max(np.linalg.norm(np.ravel(b)), 1e-30))
+
+
+def _live_params(seed):
+    """Oracle initialisation plus a little noise, so that every weight
+    (including the padded channels) and every bias carries signal."""
+    rng = np.random.default_rng(seed + 100)
+    flat = N.init_params(seed)
+    return (flat + 0.01 * rng.standard_normal(flat.shape)).astype(np.float32)
+
+
+def _routing_params(seed):
+    """Random first and last layers; every other layer moves each output
+    channel from one input channel at one random tap (weight 1, no bias).
+    The BF16 rounding of the FP32 accumulation is then the only difference
+    from the FP64 oracle in the first and last layers, and the routing layers,
+    pooling, up-sampling and skip additions are exact, so every index of
+    every level (taps, zero padding, batch boundaries) is checked tightly."""
+    rng = np.random.default_rng(seed)
+    d = {}
+    for name, cin, cout, _ in N.LAYERS:
+        W, b = np.zeros((3, 3, cin, cout)), np.zeros(cout)
+        if name in ("e0a", "d0b"):
+            W, b = 0.25 * rng.standard_normal((3, 3, cin, cout)), 0.1 * rng.standard_normal(cout)
+        else:
+            tap, perm = int(rng.integers(9)), rng.permutation(max(cin, cout))
+            for co in range(cout):
+                W[tap // 3, tap % 3, perm[co] % cin, co] = 1.0
+        d[name] = (W, b)
+    return N.flatten(d).astype(np.float32)
+
+
+def test_param_count_matches_oracle(dev):
+    from aerojax_gb300._lib import lib
+    assert int(lib().aj_nn_param_count()) == N.num_params()
+
+
+@pytest.mark.parametrize("n,h,w", [(2, 16, 16), (3, 32, 8), (1, 8, 24)])
+def test_forward_routing_network_exact(dev, n, h, w):
+    from aerojax_gb300.nn import WarmStartNet
+    flat = _routing_params(n * 100 + h)
+    net = WarmStartNet(device=dev, params=flat)
+    x = np.random.default_rng(2).standard_normal((n, h, w, 16)).astype(np.float32)
+    y = net.forward(torch.as_tensor(x, device=dev), n, h, w).cpu().numpy()
+    for s in range(n):
+        ref = N.forward(flat.astype(np.float64), x[s].astype(np.float64), emulate_bf16=True)
+        assert _rel(y[s], ref) < 1e-4, (s, _rel(y[s], ref))
+
+
+def test_forward_matches_oracle(dev):
+    """A He-initialised network: BF16 operands, FP32 accumulation.  The
+    oracle rounds the same operands to BF16 and accumulates in FP64; a
+    handful of BF16 rounding ties that FP32 and FP64 sums resolve differently
+    move the output by a few 1e-3 (an FP64 oracle with 1e-7 relative noise
+    in its sums moves by 2.5e-3)."""
+    from aerojax_gb300.nn import WarmStartNet
+    n, h, w = 2, 16, 16
+    flat = _live_params(1)
+    net = WarmStartNet(device=dev, params=flat)
+    rng = np.random.default_rng(2)
+    x = np.zeros((n, h, w, 16), np.float32)
+    x[..., :3] = rng.standard_normal((n, h, w, 3))
+    y = net.forward(torch.as_tensor(x, device=dev), n, h, w).cpu().numpy()
+    for s in range(n):
+        ref = N.forward(flat.astype(np.float64), x[s].astype(np.float64), emulate_bf16=True)
+        assert _rel(y[s], ref) < 1.5e-2, _rel(y[s], ref)
+
+
+def test_backward_routing_network(dev):
+    from aerojax_gb300.nn import WarmStartNet
+    n, h, w = 2, 16, 16
+    flat = _routing_params(3)
+    net = WarmStartNet(device=dev, params=flat)
+    rng = np.random.default_rng(4)
+    x = rng.standard_normal((n, h, w, 16)).astype(np.float32)
+    dy = rng.standard_normal((n, h, w, 16)).astype(np.float32)
+    net.forward(torch.as_tensor(x, device=dev), n, h, w)
+    g = net.backward(torch.as_tensor(dy, device=dev), n, h, w).cpu().numpy().astype(np.float64)
+    ref = sum(N.backward(flat.astype(np.float64), x[s].astype(np.float64),
+                         dy[s].astype(np.float64), emulate_bf16=True) for s in range(n))
+    gp, rp = N.unflatten(g), N.unflatten(ref)
+    for name, _, _, _ in N.LAYERS:
+        assert _rel(gp[name][0], rp[name][0]) < 1e-4, (name, "W", _rel(gp[name][0], rp[name][0]))
+        assert _rel(gp[name][1], rp[name][1]) < 1e-4, (name, "b", _rel(gp[name][1], rp[name][1]))
+
+
+def test_backward_matches_oracle(dev):
+    from aerojax_gb300.nn import WarmStartNet
+    n, h, w = 2, 16, 16
+    flat = _live_params(3)
+    net = WarmStartNet(device=dev, params=flat)
+    rng = np.random.default_rng(4)
+    x = np.zeros((n, h, w, 16), np.float32)
+    x[..., :3] = rng.standard_normal((n, h, w, 3))
+    dy = rng.standard_normal((n, h, w, 16)).astype(np.float32)
+    net.forward(torch.as_tensor(x, device=dev), n, h, w)
+    g = net.backward(torch.as_tensor(dy, device=dev), n, h, w).cpu().numpy().astype(np.float64)
+    ref = sum(N.backward(flat.astype(np.float64), x[s].astype(np.float64),
+                         dy[s].astype(np.float64), emulate_bf16=True) for s in range(n))
+    gp, rp = N.unflatten(g), N.unflatten(ref)
+    # BF16 rounding ties resolved differently by FP32 and FP64 sums weigh most
+    # on the 2x2 bottleneck (8 pixels per bias gradient); the routing-network
+    # test above pins every index to 1e-4
+    for name, _, _, _ in N.LAYERS:
+        assert _rel(gp[name][0], rp[name][0]) < 1e-1, (name, "W", _rel(gp[name][0], rp[name][0]))
+        assert _rel(gp[name][1], rp[name][1]) < 1e-1, (name, "b", _rel(gp[name][1], rp[name][1]))
+    assert _rel(g, ref) < 2e-2, _rel(g, ref)
+
+
+def test_gradient_descends_the_loss(dev):
+    """A small step against the GPU gradient lowers the oracle's (float64,
+    unrounded) loss by about the predicted amount."""
+    from aerojax_gb300.nn import WarmStartNet
+    n, h, w = 1, 16, 8
+    flat = _live_params(5)
+    rng = np.random.default_rng(6)
+    x = np.zeros((n, h, w, 16), np.float32)
+    x[..., :3] = rng.standard_normal((n, h, w, 3))
+    tgt = rng.standard_normal((n, h, w)).astype(np.float32)
+    net = WarmStartNet(device=dev, params=flat)
+    y = net.forward(torch.as_tensor(x, device=dev), n, h, w)
+    loss, dy = net.loss(y, torch.as_tensor(tgt, device=dev), n, h, w)
+    g = net.backward(dy, n, h, w).cpu().numpy().astype(np.float64)
+    f64 = flat.astype(np.float64)
+    l0, _ = N.mse_loss(N.forward(f64, x[0].astype(np.float64)), tgt[0])
+    assert abs(float(loss.item()) - l0) < 1e-2 * l0
+    eps = 1e-3 / np.linalg.norm(g)
+    l1, _ = N.mse_loss(N.forward(f64 - eps * g, x[0].astype(np.float64)), tgt[0])
+    predicted = eps * float(g @ g)
+    assert l0 - l1 > 0.5 * predicted, (l0, l1, predicted)
+
+
+def test_loss_and_adam_match_oracle(dev):
+    from aerojax_gb300._lib import check, lib
+    n, h, w = 2, 8, 8
+    rng = np.random.default_rng(7)
+    y = rng.standard_normal((n, h, w, 16)).astype(np.float32)
+    t = rng.standard_normal((n, h, w)).astype(np.float32)
+    yd, td = torch.as_tensor(y, device=dev), torch.as_tensor(t, device=dev)
+    dy = torch.empty_like(yd)
+    loss = torch.zeros(1, dtype=torch.float64, device=dev)
+    check("aj_nn_loss", lib().aj_nn_loss(n, h, w, yd.data_ptr(), td.data_ptr(), dy.data_ptr(),
+                                         loss.data_ptr(), torch.cuda.current_stream().cuda_stream))
+    ref_l, ref_dy = N.mse_loss(y.reshape(n * h, w, 16).astype(np.float64), t.reshape(n * h, w))
+    assert abs(loss.item() - ref_l) < 1e-5 * ref_l
+    assert np.allclose(dy.cpu().numpy().reshape(n * h, w, 16), ref_dy, rtol=1e-5, atol=1e-9)
+
+    P = N.num_params()
+    wv = rng.standard_normal(P).astype(np.float32)
+    gv = (3 * rng.standard_normal(P)).astype(np.float32)
+    mv = (0.1 * rng.standard_normal(P)).astype(np.float32)
+    vv = (0.1 * rng.random(P)).astype(np.float32)
+    T = [torch.as_tensor(a.copy(), device=dev) for a in (wv, gv, mv, vv)]
+    check("aj_nn_adam", lib().aj_nn_adam(T[0].data_ptr(), T[1].data_ptr(), T[2].data_ptr(),
+                                         T[3].data_ptr(), 3, ctypes.c_float(1e-3),
+                                         ctypes.c_float(0.9), ctypes.c_float(0.999),
+                                         ctypes.c_float(1e-8), ctypes.c_float(1.0),
+                                         torch.cuda.current_stream().cuda_stream))
+    rw, rm, rv = N.adam_step(wv.astype(np.float64), gv.astype(np.float64), mv.astype(np.float64),
+                             vv.astype(np.float64), 3, 1e-3)
+    assert np.allclose(T[0].cpu().numpy(), rw, rtol=0, atol=1e-6)
+    # the hyper-parameters are FP32 (1 - 0.999f differs from 0.001 by 1.3e-5)
+    assert np.allclose(T[2].cpu().numpy(), rm, rtol=1e-5, atol=1e-7)
+    assert np.allclose(T[3].cpu().numpy(), rv, rtol=5e-5, atol=1e-9)
+
+
+def _nn_plan(dev, nx=256, ny=64, F=4):
+    from aerojax_gb300 import configs
+    from aerojax_gb300.solver import Plan
+    from dataclasses import replace
+    case = configs.naca_mac_2048x512(device=dev, nx=nx, ny=ny, mg_mode="converge")
+    cfg = replace(case["cfg"], nn_factor=F)
+    plan = Plan(cfg, dev)
+    plan.prepare(case["mask"])
+    return case, plan
+
+
+def test_features_match_oracle(dev):
+    from aerojax_gb300._lib import check, lib
+    case, plan = _nn_plan(dev)
+    c = plan.cfg
+    F = c.nn_factor
+    rng = np.random.default_rng(8)
+    b = rng.standard_normal((c.nx, c.ny)).astype(np.float32)
+    pp = rng.standard_normal((c.nx, c.ny)).astype(np.float32)
+    pt = (pp + 0.01 * rng.standard_normal((c.nx, c.ny))).astype(np.float32)
+    bd, ppd, ptd = (torch.as_tensor(a, device=dev) for a in (b, pp, pt))
+    h, w = c.nx // F, c.ny // F
+    x3 = torch.empty((h, w, 3), dtype=torch.float32, device=dev)
+    tg = torch.empty((h, w), dtype=torch.float32, device=dev)
+    check("aj_nn_features", lib().aj_nn_features(
+        ctypes.byref(plan.params), bd.data_ptr(), case["mask"].data_ptr(), ppd.data_ptr(),
+        ptd.data_ptr(), x3.data_ptr(), tg.data_ptr(), plan.ws.data_ptr(), plan.nbytes,
+        torch.cuda.current_stream().cuda_stream))
+    rx, rt, _ = N.features(b, case["mask"].cpu().numpy(), pp, c.dx, c.dy, F, p_true=pt)
+    assert _rel(x3.cpu().numpy(), rx) < 1e-5
+    assert _rel(tg.cpu().numpy(), rt) < 1e-4
+
+
+def test_step_nn_converges_to_the_same_solution(dev):
+    """The learned warm start changes only where the multigrid starts: the
+    step's result matches the plain step to the solver tolerance."""
+    from aerojax_gb300.nn import WarmStartNet, run_step_nn
+    from aerojax_gb300.solver import run_step
+    case, plan = _nn_plan(dev)
+    net = WarmStartNet(device=dev, params=_live_params(9))
+    u, v, m = case["u"], case["v"], case["mask"]
+    p0 = torch.zeros((plan.cfg.nx, plan.cfg.ny), dtype=torch.float32, device=dev)
+    u1, v1, p1 = run_step(plan, u, v, m, p_guess=p0)
+    u2, v2, p2 = run_step_nn(plan, net, u1, v1, m, p1)
+    s_nn = plan.stats()
+    u3, v3, p3 = run_step(plan, u1, v1, m, p_guess=p1)
+    s_pl = plan.stats()
+    assert s_nn["converged"] and s_pl["converged"]
+    assert s_nn["rel_residual"] <= plan.cfg.mg_rtol and s_pl["rel_residual"] <= plan.cfg.mg_rtol
+    scale = float(p3.abs().max())
+    assert float((p2 - p3).abs().max()) < 1e-3 * scale
+    assert float((u2 - u3).abs().max()) < 1e-4
+    assert float((v2 - v3).abs().max()) < 1e-4
