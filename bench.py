@@ -34,6 +34,8 @@ sys.path.insert(0, ROOT)
 METRIC = "Mcell-steps/s at 2048×512 FP32, NN-warm-start+MG vs plain MG at equal div tol"
 UNIT = "Mcell-steps/s"
 FLUSH_BYTES = 256 << 20          # larger than the 126 MB L2
+# DRAM bytes of one k_cv_up0 launch at 2048x512 from an ncu capture
+TRAFFIC_UP0 = 22056192
 
 
 def parse():
@@ -47,7 +49,10 @@ def parse():
     ap.add_argument("--cpu-sample-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quick", action="store_true",
-                    help="timed GPU arms only (no clock soak, e2e or CPU leg): for profiling")
+                    help="timed GPU arms only (no clock soak, e2e or CPU leg)")
+    ap.add_argument("--profile", action="store_true",
+                    help="warm-up and timed steps of the method arm only, then exit "
+                         "(the command a kernel profiler wraps)")
     return ap.parse_args()
 
 
@@ -238,6 +243,15 @@ def gpu_arm(args):
         while time.perf_counter() - t0 < seconds:
             run(plan, bufs, 20, False, warm)
 
+    if args.profile:
+        plan, bufs = make_arm(True)
+        run(plan, bufs, max(3, args.warmup), False, True)
+        ms, cyc = run(plan, bufs, args.steps, True, True)
+        if rank == 0:
+            print(json.dumps({"profile_steps": args.steps, "ms_per_step": ms / args.steps,
+                              "cycles": [c[0] for c in cyc], "errors": [c[2] for c in cyc]}))
+        return
+
     results = {}
     clocks = ClockSampler(local)
     for name, warm in (("plain", False), ("method", True)):
@@ -330,8 +344,8 @@ def gpu_arm(args):
         "data": "synthetic (seeded NACA 0012 flow; the solver generates every step)",
         "config": {
             "workload": case["name"], "nx": args.nx, "ny": args.ny, "grid": "mac",
-            "method": "converging MG (FP32 red-black V-cycles, FP64 refinement, coarsest and "
-                      "norms) warm-started from the previous pressure; NN warm start not built yet",
+            "method": "converging MG (FP32 red-black V-cycles, double-FP32 refinement, FP64 coarsest "
+                      "and norms) warm-started from the previous pressure",
             "rel_residual_target": 1e-6, "rel_residual_max": rel_m,
             "mg_cycles_mean": statistics.mean(cyc_m) if cyc_m else None,
             "plain_mg_value": plain_value, "plain_mg_ms_per_step": plain_ms,
@@ -388,7 +402,9 @@ def roofline(args, plan, state, mask, flush, L):
     return {"kernel": "k_cv_up0 (level 0: prolongation + 2 red-black sweeps + FP64 update "
                       "and residual)",
             "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "peak_source": src, "traffic": None,
+            "frac": achieved / peak, "peak_source": src, "traffic": TRAFFIC_UP0,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch "
+                              "(profiles/k_cv_up0_naca0012_mac_2048x512.md)",
             "algorithmic_bytes_per_launch": algo, "launch_us": dur * 1e6}
 
 
