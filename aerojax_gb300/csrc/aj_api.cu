@@ -143,8 +143,17 @@ bool make_layout(const AjStepParams& p, Layout& L) {
     L.p64 = take(N * 8);
     L.p64b = take(N * 8);
     L.cinv = take((size_t)L.ncoarse * L.ncoarse * 8);
-    // levels lc..D run in one thread block with everything in shared memory
-    L.lc = converge_first_block_level(L);
+    // the coarse solve: an exact separable solve at level ld when one fits,
+    // else levels lc..D in one thread block with everything in shared memory
+    L.ld = converge_direct_level(L);
+    if (L.ld > 0) {
+      L.lc = L.ld;
+      L.dcy = take((size_t)L.lm[L.ld] * L.lm[L.ld] * 4);
+      L.dly = take((size_t)L.lm[L.ld] * 4);
+      L.dtmp = take((size_t)L.ln[L.ld] * L.lm[L.ld] * 4);
+    } else {
+      L.lc = converge_first_block_level(L);
+    }
   }
   if (p.nn_factor > 0 && p.mg_mode == AJ_MG_CONVERGE && nn_step_shape_ok(p)) {
     L.nn_act = take(nn_step_act_bytes(p));
@@ -473,7 +482,7 @@ int32_t aj_kernel_count(const AjStepParams* prm, int32_t cycles) {
     int per_cycle = 5 * L.nlev + 10 + 2;                        // 5 per level, coarsest, norm
     n += 1 + p.v_cycles * per_cycle;                            // begin + cycles
   } else {
-    int body = 2 * L.lc + 1;                                    // downs, one-block coarse, ups
+    int body = 2 * L.lc + 1 + (L.ld > 0 ? 2 : 0);               // downs, coarse solve, ups
     n += 4 + (cycles > 1 ? cycles : 1) * body + 1;              // begin/init/resid/check, loop, out
   }
   n += 1;                                                       // stats

@@ -5,8 +5,8 @@
 // Structure of one refinement iteration (one body of the graph's while node):
 //   levels 0 .. lc-1   k_cv_down: 2 red-black sweeps from e = 0 in a shared-
 //                      memory tile, residual, 2x2 restriction
-//   levels lc .. D     k_cv_block: one 256-thread block holding the smallest
-//                      levels (<= 1024 cells) in shared memory: sweeps,
+//   levels lc .. D     k_cv_block: one 1024-thread block holding the smallest
+//                      levels (<= 16384 cells) in shared memory: sweeps,
 //                      restriction, the FP64 dense solve of the coarsest grid,
 //                      prolongation, sweeps
 //   levels lc-1 .. 1   k_cv_up: e += P(e_coarse), 2 red-black sweeps
@@ -39,8 +39,8 @@ namespace aj {
 constexpr int CV_NS = 2;                         // red-black sweeps per smoothing phase
 constexpr int CV_H = 2 * CV_NS + 1;              // tile halo: sweeps + one cell for the residual
 constexpr int CV_THREADS = 256;
-constexpr int CV_BLOCK_THREADS = 256;
-constexpr int CV_BLOCK_MAX_CELLS = 1024;         // levels handled by the one-block kernel
+constexpr int CV_BLOCK_THREADS = 1024;
+constexpr int CV_BLOCK_MAX_CELLS = 16384;        // levels handled by the one-block kernel
 
 struct CvLvl {
   int n, m, level;
@@ -447,8 +447,9 @@ __global__ void __launch_bounds__(T0::NTH) k_cv_up0(
 }
 
 struct CvBlock {
-  int lc, D, ncoarse;
+  int lc, D, ncoarse, pre;
   int n[AJ_MAX_LEVELS + 1], m[AJ_MAX_LEVELS + 1];
+  int eoff[AJ_MAX_LEVELS + 1], roff[AJ_MAX_LEVELS + 1], voff;   // shared-memory float offsets
   float ax[AJ_MAX_LEVELS + 1], ay[AJ_MAX_LEVELS + 1], g[AJ_MAX_LEVELS + 1];
   const float* r_in;      // rhs of level lc (global)
   float* e_out;           // correction of level lc (global)
@@ -456,123 +457,146 @@ struct CvBlock {
   const int* done;
 };
 
-// shared-memory footprint of levels lc..D: e and r with a one-cell zero border
-// per level, plus the FP64 vector of the dense coarsest solve
-size_t converge_block_smem(const Layout& L, int lc) {
+// shared-memory footprint of levels lc..D: e with a one-cell zero border and
+// r, per level, plus the FP64 vector of the dense coarsest solve
+static size_t block_levels_smem(const Layout& L, int lc) {
   size_t s = 0;
-  for (int k = lc; k <= L.nlev; ++k) s += 2 * (size_t)(L.ln[k] + 2) * (L.lm[k] + 2) * 4;
+  for (int k = lc; k <= L.nlev; ++k)
+    s += ((size_t)(L.ln[k] + 2) * (L.lm[k] + 2) + (size_t)L.ln[k] * L.lm[k]) * 4;
   s = (s + 15) & ~(size_t)15;
   const size_t N = (size_t)L.ln[L.nlev] * L.lm[L.nlev];
-  s += N * 8;
-  if (N <= AJ_MAX_COARSE) s += N * N * 8;     // the coarsest inverse, prefetched
-  return s;
+  return s + N * 8;
+}
+// whether the coarsest inverse is copied to shared memory (when it fits)
+static bool block_prefetch(const Layout& L, int lc) {
+  const size_t N = (size_t)L.ln[L.nlev] * L.lm[L.nlev];
+  return N <= AJ_MAX_COARSE && block_levels_smem(L, lc) + N * N * 8 <= kBlockSmemMax;
+}
+size_t converge_block_smem(const Layout& L, int lc) {
+  const size_t N = (size_t)L.ln[L.nlev] * L.lm[L.nlev];
+  return block_levels_smem(L, lc) + (block_prefetch(L, lc) ? N * N * 8 : 0);
 }
 
+// A thread's place in a (rows x w) sweep of the block: column tx, first row
+// ty, row stride rs (threads beyond rs * w rows idle).
+struct Lane2 {
+  int tx, ty, rs;
+};
+__device__ __forceinline__ Lane2 lane2(int w) {
+  Lane2 l;
+  l.tx = threadIdx.x % w;
+  l.ty = threadIdx.x / w;
+  l.rs = blockDim.x / w;
+  return l;
+}
+
+__device__ __forceinline__ float blk_inv_diag(int i, int j, int n, int m, float ax, float ay,
+                                              float g, float inv_int) {
+  if (i > 0 && i < n - 1 && j > 0 && j < m - 1) return inv_int;
+  float dd = -2.f * (ax + ay);
+  if (i == 0) dd += ax;
+  if (j == 0) dd += ay;
+  if (j == m - 1) dd += ay;
+  if (i == n - 1) dd += ax * g;
+  return __frcp_rn(dd);
+}
+
+// red-black sweeps of one level held in shared memory (E bordered, R not)
 __device__ __forceinline__ void blk_sweeps(float* E, const float* R, int n, int m, float ax,
                                            float ay, float g) {
   const int W = m + 2, hw = (m + 1) >> 1;
+  const Lane2 q = lane2(hw);
   const float inv_int = 1.f / (-2.f * (ax + ay));
   for (int h = 0; h < 2 * CV_NS; ++h) {
     const int color = h & 1;
-    for (int t = threadIdx.x; t < n * hw; t += blockDim.x) {
-      const int i = t / hw;
-      const int j = ((color - i) & 1) + 2 * (t - i * hw);
-      if (j >= m) continue;
-      const int c = (i + 1) * W + (j + 1);
-      const float nb = ax * (E[c + W] + E[c - W]) + ay * (E[c + 1] + E[c - 1]);
-      float d;
-      if (i > 0 && i < n - 1 && j > 0 && j < m - 1) {
-        d = inv_int;
-      } else {
-        float dd = -2.f * (ax + ay);
-        if (i == 0) dd += ax;
-        if (j == 0) dd += ay;
-        if (j == m - 1) dd += ay;
-        if (i == n - 1) dd += ax * g;
-        d = 1.f / dd;
+    if (q.ty < q.rs) {
+      for (int i = q.ty; i < n; i += q.rs) {
+        const int j = ((color + i) & 1) + 2 * q.tx;
+        if (j >= m) continue;
+        const int c = (i + 1) * W + (j + 1);
+        const float nb = ax * (E[c + W] + E[c - W]) + ay * (E[c + 1] + E[c - 1]);
+        E[c] = (R[i * m + j] - nb) * blk_inv_diag(i, j, n, m, ax, ay, g, inv_int);
       }
-      E[c] = (R[c] - nb) * d;
     }
     __syncthreads();
   }
 }
 
+// Levels lc..D in one block of CV_BLOCK_THREADS threads, every level resident
+// in shared memory: pre-smoothing, residual and restriction down to the
+// coarsest grid, its FP64 dense solve, prolongation and post-smoothing back
+// to level lc.  Replaces 2 (D - lc) launches of the tile kernels by one.
 __global__ void __launch_bounds__(CV_BLOCK_THREADS) k_cv_block(CvBlock a) {
   if (*a.done) return;
-  extern __shared__ __align__(16) unsigned char smraw[];
-  float* E[AJ_MAX_LEVELS + 1];
-  float* R[AJ_MAX_LEVELS + 1];
-  size_t off = 0, total_f = 0;
-  for (int k = a.lc; k <= a.D; ++k) {
-    size_t cnt = (size_t)(a.n[k] + 2) * (a.m[k] + 2);
-    E[k] = reinterpret_cast<float*>(smraw + off);
-    off += cnt * 4;
-    R[k] = reinterpret_cast<float*>(smraw + off);
-    off += cnt * 4;
-    total_f += 2 * cnt;
-  }
-  off = (off + 15) & ~(size_t)15;
-  double* V = reinterpret_cast<double*>(smraw + off);
-  // small coarsest grids: start loading the inverse now, so its latency hides
-  // behind the smoothing of the finer levels
-  const bool pre = a.ncoarse <= AJ_MAX_COARSE;
+  extern __shared__ __align__(16) float smf[];
+  // level arrays are addressed from smf directly so that every access is a
+  // shared-memory access
+  auto E = [&](int k) { return smf + a.eoff[k]; };
+  auto R = [&](int k) { return smf + a.roff[k]; };
+  double* V = reinterpret_cast<double*>(smf + a.voff);
   double* Ainv_s = V + a.ncoarse;
-  if (pre)
+  // start loading the coarsest inverse now, so its latency hides behind the
+  // smoothing of the finer levels
+  if (a.pre)
     for (int t = threadIdx.x; t < a.ncoarse * a.ncoarse; t += blockDim.x) Ainv_s[t] = a.Ainv[t];
-  float* all = reinterpret_cast<float*>(smraw);
-  for (size_t t = threadIdx.x; t < total_f; t += blockDim.x) all[t] = 0.f;
-  __syncthreads();
+  for (int k = a.lc; k <= a.D; ++k) {
+    float* e = E(k);
+    const int cnt = (a.n[k] + 2) * (a.m[k] + 2);
+    for (int t = threadIdx.x; t < cnt; t += blockDim.x) e[t] = 0.f;
+  }
   {
-    const int n = a.n[a.lc], m = a.m[a.lc], W = m + 2;
-    for (int t = threadIdx.x; t < n * m; t += blockDim.x) {
-      const int i = t / m, j = t - i * m;
-      R[a.lc][(i + 1) * W + (j + 1)] = ldg(a.r_in + t);
-    }
+    const int cnt = a.n[a.lc] * a.m[a.lc];
+    float* r0 = R(a.lc);
+    for (int t = threadIdx.x; t < cnt; t += blockDim.x) r0[t] = ldg(a.r_in + t);
   }
   __syncthreads();
-  // down: smooth, residual, restrict
+  // down: smooth, residual, restrict (coarse cell = average of 4 fine residuals)
   for (int k = a.lc; k < a.D; ++k) {
     const int n = a.n[k], m = a.m[k], W = m + 2;
     const float ax = a.ax[k], ay = a.ay[k], g = a.g[k];
-    blk_sweeps(E[k], R[k], n, m, ax, ay, g);
-    const int nc = n >> 1, mc = m >> 1, Wc = mc + 2;
-    for (int t = threadIdx.x; t < nc * mc; t += blockDim.x) {
-      const int I = t / mc, J = t - I * mc;
-      float s = 0.f;
+    blk_sweeps(E(k), R(k), n, m, ax, ay, g);
+    const int nc = n >> 1, mc = m >> 1;
+    const Lane2 q = lane2(mc);
+    const float* e = E(k);
+    const float* rk = R(k);
+    float* rk1 = R(k + 1);
+    if (q.ty < q.rs) {
+      for (int I = q.ty; I < nc; I += q.rs) {
+        const int J = q.tx;
+        float s = 0.f;
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int i = 2 * I + (q & 1), j = 2 * J + (q >> 1);
-        const int c = (i + 1) * W + (j + 1);
-        float dd = -2.f * (ax + ay);
-        if (i == 0) dd += ax;
-        if (j == 0) dd += ay;
-        if (j == m - 1) dd += ay;
-        if (i == n - 1) dd += ax * g;
-        const float Ae = ax * (E[k][c + W] + E[k][c - W]) + ay * (E[k][c + 1] + E[k][c - 1]) +
-                         dd * E[k][c];
-        s += R[k][c] - Ae;
+        for (int u = 0; u < 4; ++u) {
+          const int i = 2 * I + (u & 1), j = 2 * J + (u >> 1);
+          const int c = (i + 1) * W + (j + 1);
+          float dd = -2.f * (ax + ay);
+          if (i == 0) dd += ax;
+          if (j == 0) dd += ay;
+          if (j == m - 1) dd += ay;
+          if (i == n - 1) dd += ax * g;
+          const float Ae = ax * (e[c + W] + e[c - W]) + ay * (e[c + 1] + e[c - 1]) + dd * e[c];
+          s += rk[i * m + j] - Ae;
+        }
+        rk1[I * mc + J] = 0.25f * s;
       }
-      R[k + 1][(I + 1) * Wc + (J + 1)] = 0.25f * s;
     }
     __syncthreads();
   }
   // coarsest: e = A^-1 r in FP64 (one warp per row)
   {
-    const int n = a.n[a.D], m = a.m[a.D], W = m + 2, N = a.ncoarse;
-    for (int t = threadIdx.x; t < N; t += blockDim.x) {
-      const int i = t / m, j = t - i * m;
-      V[t] = (double)R[a.D][(i + 1) * W + (j + 1)];
-    }
+    const int m = a.m[a.D], W = m + 2, N = a.ncoarse;
+    const float* rD = R(a.D);
+    float* eD = E(a.D);
+    for (int t = threadIdx.x; t < N; t += blockDim.x) V[t] = (double)rD[t];
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     for (int row = warp; row < N; row += nw) {
-      const double* arow = (pre ? Ainv_s : a.Ainv) + (long)row * N;
+      const double* arow = (a.pre ? Ainv_s : a.Ainv) + (long)row * N;
       double s = 0.0;
       for (int c = lane; c < N; c += 32) s += arow[c] * V[c];
       s = warp_sum(s);
       if (lane == 0) {
         const int i = row / m, j = row - i * m;
-        E[a.D][(i + 1) * W + (j + 1)] = (float)s;
+        eD[(i + 1) * W + (j + 1)] = (float)s;
       }
     }
     __syncthreads();
@@ -582,38 +606,217 @@ __global__ void __launch_bounds__(CV_BLOCK_THREADS) k_cv_block(CvBlock a) {
     const int n = a.n[k], m = a.m[k], W = m + 2;
     const int nc = a.n[k + 1], mc = a.m[k + 1], Wc = mc + 2;
     const float gc = a.g[k + 1];
-    const float* Ec = E[k + 1];
-    for (int t = threadIdx.x; t < n * m; t += blockDim.x) {
-      const int gi = t / m, gj = t - gi * m;
-      const int I = gi >> 1, J = gj >> 1;
-      const int Ii = (gi & 1) ? I + 1 : I - 1;
-      int Jj = (gj & 1) ? J + 1 : J - 1;
-      Jj = Jj < 0 ? 0 : (Jj >= mc ? mc - 1 : Jj);
-      const float c0 = Ec[(I + 1) * Wc + (J + 1)], cy = Ec[(I + 1) * Wc + (Jj + 1)];
-      float cx, cxy;
-      if (Ii < 0) {
-        cx = c0;
-        cxy = cy;
-      } else if (Ii >= nc) {
-        cx = gc * c0;
-        cxy = gc * cy;
-      } else {
-        cx = Ec[(Ii + 1) * Wc + (J + 1)];
-        cxy = Ec[(Ii + 1) * Wc + (Jj + 1)];
+    const float* Ec = E(k + 1);
+    float* Ek = E(k);
+    const Lane2 q = lane2(m);
+    if (q.ty < q.rs) {
+      for (int gi = q.ty; gi < n; gi += q.rs) {
+        const int gj = q.tx;
+        const int I = gi >> 1, J = gj >> 1;
+        const int Ii = (gi & 1) ? I + 1 : I - 1;
+        int Jj = (gj & 1) ? J + 1 : J - 1;
+        Jj = Jj < 0 ? 0 : (Jj >= mc ? mc - 1 : Jj);
+        const float c0 = Ec[(I + 1) * Wc + (J + 1)], cy = Ec[(I + 1) * Wc + (Jj + 1)];
+        float cx, cxy;
+        if (Ii < 0) {
+          cx = c0;
+          cxy = cy;
+        } else if (Ii >= nc) {
+          cx = gc * c0;
+          cxy = gc * cy;
+        } else {
+          cx = Ec[(Ii + 1) * Wc + (J + 1)];
+          cxy = Ec[(Ii + 1) * Wc + (Jj + 1)];
+        }
+        Ek[(gi + 1) * W + (gj + 1)] += (9.f * c0 + 3.f * cx + 3.f * cy + cxy) * (1.f / 16.f);
       }
-      E[k][(gi + 1) * W + (gj + 1)] += (9.f * c0 + 3.f * cx + 3.f * cy + cxy) * (1.f / 16.f);
     }
     __syncthreads();
-    blk_sweeps(E[k], R[k], n, m, a.ax[k], a.ay[k], a.g[k]);
+    blk_sweeps(Ek, R(k), n, m, a.ax[k], a.ay[k], a.g[k]);
   }
   {
     const int n = a.n[a.lc], m = a.m[a.lc], W = m + 2;
-    for (int t = threadIdx.x; t < n * m; t += blockDim.x) {
-      const int i = t / m, j = t - i * m;
-      a.e_out[t] = E[a.lc][(i + 1) * W + (j + 1)];
-    }
+    const Lane2 q = lane2(m);
+    const float* e0 = E(a.lc);
+    if (q.ty < q.rs)
+      for (int i = q.ty; i < n; i += q.rs) a.e_out[(long)i * m + q.tx] = e0[(i + 1) * W + q.tx + 1];
   }
 }
+
+// ---------------------------------------------------------------- direct coarse solve
+// The rediscretised operator of level ld is separable: A = ax Tx (x) I +
+// ay I (x) Ty, with Ty the 1-D Neumann-Neumann Laplacian (edge ghosts at both
+// walls) and Tx the 1-D operator with an edge ghost at the inlet and the
+// outlet ghost g * e_last.  The orthonormal DCT-II basis diagonalises Ty
+// (eigenvalues -4 sin^2(pi k / 2m)), so A e = r splits into m independent
+// tridiagonal systems (ax Tx + ay lambda_k) e_k = r_k in x, one per cosine
+// mode, solved here by parallel cyclic reduction.  The whole coarse part of
+// the V-cycle below level ld is replaced by this exact solve: a cosine
+// transform (k_cv_dfwd), the m tridiagonal solves (k_cv_dpcr) and the inverse
+// transform (k_cv_dbwd).
+constexpr int CV_DIRECT_MAX_CELLS = 65536;
+constexpr int CV_DIRECT_MAX_M = 128;
+constexpr int CV_DIRECT_MAX_N = 1024;
+
+struct CvDirect {
+  int n, m;
+  float ax, g;
+  const float* r;      // level-ld rhs [n][m]
+  const float* cy;     // cosine basis Cy[k][j] (orthonormal DCT-II)
+  const float* ly;     // ay * lambda_k
+  float* rhat;         // mode coefficients of r, transposed [m][n]
+  float* ehat;         // mode coefficients of e, transposed [m][n]
+  float* e;            // level-ld correction [n][m]
+  const int* done;
+};
+
+int converge_direct_level(const Layout& L) {
+  for (int l = 1; l <= L.nlev; ++l) {
+    const long cells = (long)L.ln[l] * L.lm[l];
+    if (cells <= CV_DIRECT_MAX_CELLS && L.lm[l] <= CV_DIRECT_MAX_M && L.ln[l] <= CV_DIRECT_MAX_N &&
+        L.ln[l] >= 2)
+      return l;
+  }
+  return 0;
+}
+
+// rhat[k][i] = sum_j Cy[k][j] r[i][j]: 32 x 32 output tiles, 32-wide slices
+// of j staged in shared memory; thread (tx, ty) owns i = i0 + tx and the
+// modes k0 + ty + 8q
+constexpr int CV_DT = 32;
+__global__ void __launch_bounds__(256) k_cv_dfwd(CvDirect a) {
+  if (*a.done) return;
+  __shared__ float Cs[CV_DT][CV_DT + 1];
+  __shared__ float Rs[CV_DT][CV_DT + 1];
+  const int n = a.n, m = a.m;
+  const int i0 = blockIdx.x * CV_DT, k0 = blockIdx.y * CV_DT;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  float acc[4] = {0.f, 0.f, 0.f, 0.f};
+  for (int j0 = 0; j0 < m; j0 += CV_DT) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int rr = ty + 8 * q, j = j0 + tx;
+      const int k = k0 + rr, i = i0 + rr;
+      Cs[rr][tx] = (k < m && j < m) ? ldg(a.cy + (long)k * m + j) : 0.f;
+      Rs[rr][tx] = (i < n && j < m) ? ldg(a.r + (long)i * m + j) : 0.f;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int jj = 0; jj < CV_DT; ++jj) {
+      const float rv = Rs[tx][jj];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc[q] = fmaf(Cs[ty + 8 * q][jj], rv, acc[q]);
+    }
+    __syncthreads();
+  }
+  const int i = i0 + tx;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int k = k0 + ty + 8 * q;
+    if (i < n && k < m) a.rhat[(long)k * n + i] = acc[q];
+  }
+}
+
+// one block per cosine mode k: parallel cyclic reduction of
+// (ax Tx + ay lambda_k) ehat_k = rhat_k, n unknowns along x
+__global__ void __launch_bounds__(1024) k_cv_dpcr(CvDirect a) {
+  if (*a.done) return;
+  extern __shared__ __align__(16) float sh[];
+  const int n = a.n, k = blockIdx.x;
+  float* A0 = sh;
+  float* B0 = A0 + n;
+  float* C0 = B0 + n;
+  float* D0 = C0 + n;
+  float* A1 = D0 + n;
+  float* B1 = A1 + n;
+  float* C1 = B1 + n;
+  float* D1 = C1 + n;
+  const int i = threadIdx.x;
+  const float lyk = ldg(a.ly + k);
+  if (i < n) {
+    float dx = -2.f;
+    if (i == 0) dx += 1.f;
+    if (i == n - 1) dx += a.g;
+    A0[i] = i > 0 ? a.ax : 0.f;
+    C0[i] = i < n - 1 ? a.ax : 0.f;
+    B0[i] = fmaf(a.ax, dx, lyk);
+    D0[i] = ldg(a.rhat + (long)k * n + i);
+  }
+  __syncthreads();
+  float *Ac = A0, *Bc = B0, *Cc = C0, *Dc = D0, *An = A1, *Bn = B1, *Cn = C1, *Dn = D1;
+  for (int st = 1; st < n; st <<= 1) {
+    if (i < n) {
+      const float ai = Ac[i], bi = Bc[i], ci = Cc[i], di = Dc[i];
+      float an = 0.f, bn = bi, cn = 0.f, dn = di;
+      if (i - st >= 0) {
+        const float k1 = ai / Bc[i - st];
+        an = -Ac[i - st] * k1;
+        bn -= Cc[i - st] * k1;
+        dn -= Dc[i - st] * k1;
+      }
+      if (i + st < n) {
+        const float k2 = ci / Bc[i + st];
+        cn = -Cc[i + st] * k2;
+        bn -= Ac[i + st] * k2;
+        dn -= Dc[i + st] * k2;
+      }
+      An[i] = an;
+      Bn[i] = bn;
+      Cn[i] = cn;
+      Dn[i] = dn;
+    }
+    __syncthreads();
+    float* t;
+    t = Ac; Ac = An; An = t;
+    t = Bc; Bc = Bn; Bn = t;
+    t = Cc; Cc = Cn; Cn = t;
+    t = Dc; Dc = Dn; Dn = t;
+  }
+  if (i < n) a.ehat[(long)k * n + i] = Dc[i] / Bc[i];
+}
+
+// e[i][j] = sum_k ehat[k][i] Cy[k][j]: 32 x 32 output tiles; thread (tx, ty)
+// owns j = j0 + tx and the rows i0 + ty + 8q
+__global__ void __launch_bounds__(256) k_cv_dbwd(CvDirect a) {
+  if (*a.done) return;
+  __shared__ float Es[CV_DT][CV_DT + 1];
+  __shared__ float Cs[CV_DT][CV_DT + 1];
+  const int n = a.n, m = a.m;
+  const int j0 = blockIdx.x * CV_DT, i0 = blockIdx.y * CV_DT;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  float acc[4] = {0.f, 0.f, 0.f, 0.f};
+  for (int kb = 0; kb < m; kb += CV_DT) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int kk = ty + 8 * q, k = kb + kk;
+      const int i = i0 + tx, j = j0 + tx;
+      Es[kk][tx] = (k < m && i < n) ? ldg(a.ehat + (long)k * n + i) : 0.f;
+      Cs[kk][tx] = (k < m && j < m) ? ldg(a.cy + (long)k * m + j) : 0.f;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int kk = 0; kk < CV_DT; ++kk) {
+      const float cv = Cs[kk][tx];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc[q] = fmaf(Es[kk][ty + 8 * q], cv, acc[q]);
+    }
+    __syncthreads();
+  }
+  const int j = j0 + tx;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int i = i0 + ty + 8 * q;
+    if (i < n && j < m) a.e[(long)i * m + j] = acc[q];
+  }
+}
+
+static void direct_launch(const CvDirect& d, cudaStream_t st) {
+  k_cv_dfwd<<<dim3(cdiv(d.n, CV_DT), cdiv(d.m, CV_DT)), dim3(CV_DT, 8), 0, st>>>(d);
+  k_cv_dpcr<<<d.m, cdiv(d.n, 32) * 32, 8 * d.n * sizeof(float), st>>>(d);
+  k_cv_dbwd<<<dim3(cdiv(d.m, CV_DT), cdiv(d.n, CV_DT)), dim3(CV_DT, 8), 0, st>>>(d);
+}
+
+static CvDirect direct_args(const AjStepParams& p, const Layout& L, void* ws, const int* done);
 
 // ---------------------------------------------------------------- set-up / solve
 // p = p0 (or 0) as hi, lo = 0, outlet row pinned
@@ -697,6 +900,15 @@ static CvBlock block_args(const AjStepParams& p, const Layout& L, void* ws, cons
   a.lc = L.lc;
   a.D = L.nlev;
   a.ncoarse = L.ncoarse;
+  a.pre = block_prefetch(L, L.lc) ? 1 : 0;
+  size_t off = 0;   // floats; the same order as block_levels_smem
+  for (int k = L.lc; k <= L.nlev; ++k) {
+    a.eoff[k] = (int)off;
+    off += (size_t)(L.ln[k] + 2) * (L.lm[k] + 2);
+    a.roff[k] = (int)off;
+    off += (size_t)L.ln[k] * L.lm[k];
+  }
+  a.voff = (int)((off + 3) & ~(size_t)3);
   for (int k = 0; k <= L.nlev; ++k) {
     CvLvl c = cv_level(p, L, k);
     a.n[k] = c.n;
@@ -710,6 +922,23 @@ static CvBlock block_args(const AjStepParams& p, const Layout& L, void* ws, cons
   a.Ainv = at<double>(ws, L.cinv);
   a.done = done;
   return a;
+}
+
+static CvDirect direct_args(const AjStepParams& p, const Layout& L, void* ws, const int* done) {
+  CvDirect d;
+  const CvLvl c = cv_level(p, L, L.ld);
+  d.n = c.n;
+  d.m = c.m;
+  d.ax = c.ax;
+  d.g = c.g;
+  d.r = at<float>(ws, L.B[L.ld]);
+  d.cy = at<float>(ws, L.dcy);
+  d.ly = at<float>(ws, L.dly);
+  d.rhat = at<float>(ws, L.X[L.ld]);
+  d.ehat = at<float>(ws, L.dtmp);
+  d.e = at<float>(ws, L.T[L.ld]);
+  d.done = done;
+  return d;
 }
 
 static PState pstate(const Layout& L, void* ws) {
@@ -740,7 +969,11 @@ static void cv_body(const AjStepParams& p, const Layout& L, void* ws,
       k_cv_down<T1><<<tiles<T1>(c), tile_threads<T1>(), 0, st>>>(
           c, at<float>(ws, L.B[l]), at<float>(ws, L.X[l]), at<float>(ws, L.B[l + 1]), done);
   }
-  k_cv_block<<<1, CV_BLOCK_THREADS, converge_block_smem(L, lc), st>>>(block_args(p, L, ws, done));
+  if (L.ld > 0) {
+    direct_launch(direct_args(p, L, ws, done), st);
+  } else {
+    k_cv_block<<<1, CV_BLOCK_THREADS, converge_block_smem(L, lc), st>>>(block_args(p, L, ws, done));
+  }
   for (int l = lc - 1; l >= 1; --l) {
     CvLvl c = cv_level(p, L, l);
     k_cv_up<T1><<<tiles<T1>(c), tile_threads<T1>(), 0, st>>>(
@@ -869,6 +1102,7 @@ int converge_first_block_level(const Layout& L) {
   int lc = L.nlev;
   for (int l = L.nlev - 1; l >= 1; --l) {
     if ((long)L.ln[l] * L.lm[l] > CV_BLOCK_MAX_CELLS) break;
+    if (L.lm[l] > CV_BLOCK_THREADS) break;      // one row per pass of the block
     if (converge_block_smem(L, l) > kBlockSmemMax) break;
     lc = l;
   }
@@ -878,6 +1112,27 @@ int converge_first_block_level(const Layout& L) {
 int converge_prepare(const AjStepParams& p, const Layout& L, void* ws, cudaStream_t st) {
   std::vector<double> inv;
   if (!coarse_inverse(p, L, inv)) return AJ_ERR_PARAM;
+  std::vector<float> cy, ly;
+  if (L.ld > 0) {
+    // orthonormal DCT-II basis of the level-ld Neumann-Neumann y operator and
+    // its eigenvalues times 1/hy^2
+    const int m = L.lm[L.ld];
+    const double hy = p.dy * (double)(1 << L.ld), ay = 1.0 / (hy * hy);
+    const double pi = 3.14159265358979323846;
+    cy.resize((size_t)m * m);
+    ly.resize(m);
+    for (int k = 0; k < m; ++k) {
+      const double sk = k == 0 ? sqrt(1.0 / m) : sqrt(2.0 / m);
+      for (int j = 0; j < m; ++j) cy[(size_t)k * m + j] = (float)(sk * cos(pi * k * (2 * j + 1) / (2.0 * m)));
+      const double sn = sin(pi * k / (2.0 * m));
+      ly[k] = (float)(-4.0 * ay * sn * sn);
+    }
+    if (cudaMemcpyAsync(at<float>(ws, L.dcy), cy.data(), cy.size() * 4, cudaMemcpyHostToDevice,
+                        st) != cudaSuccess ||
+        cudaMemcpyAsync(at<float>(ws, L.dly), ly.data(), ly.size() * 4, cudaMemcpyHostToDevice,
+                        st) != cudaSuccess)
+      return AJ_ERR_CUDA;
+  }
   if (cudaFuncSetAttribute(k_cv_block, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)kBlockSmemMax + 1024) != cudaSuccess)
     return AJ_ERR_CUDA;
@@ -891,7 +1146,7 @@ int converge_prepare(const AjStepParams& p, const Layout& L, void* ws, cudaStrea
 // (instrumentation: lets a caller time the kernel on its own).  which:
 // 0 = level-0 smoothing + residual + restriction, 1 = level-0 prolongation +
 // smoothing + pressure update + residual (the solver state is left untouched),
-// 2 = the one-block coarse-level kernel.
+// 2 = the coarse solve (the separable direct solve, or the one-block kernel).
 int profile_pressure_kernel(const AjStepParams& p, const Layout& L, void* ws, int which,
                             cudaStream_t st) {
   if (p.mg_mode != AJ_MG_CONVERGE) return AJ_ERR_PARAM;
@@ -909,8 +1164,12 @@ int profile_pressure_kernel(const AjStepParams& p, const Layout& L, void* ws, in
         (float)ghost_factor(1), pstate(L, ws), at<float>(ws, L.b0), at<float>(ws, L.B[0]), sc,
         df_coef(1.0 / (p.dx * p.dx), 1.0 / (p.dy * p.dy)), ck, 1);
   } else if (which == 2) {
-    k_cv_block<<<1, CV_BLOCK_THREADS, converge_block_smem(L, L.lc), st>>>(
-        block_args(p, L, ws, never));
+    if (L.ld > 0) {
+      direct_launch(direct_args(p, L, ws, never), st);
+    } else {
+      k_cv_block<<<1, CV_BLOCK_THREADS, converge_block_smem(L, L.lc), st>>>(
+          block_args(p, L, ws, never));
+    }
   } else {
     return AJ_ERR_PARAM;
   }

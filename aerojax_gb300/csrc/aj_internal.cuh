@@ -47,7 +47,9 @@ struct Layout {
   size_t B[AJ_MAX_LEVELS + 1] = {0}, M[AJ_MAX_LEVELS + 1] = {0};
   size_t p64 = 0, p64b = 0;                             // converging mode FP64 pressure (ping-pong)
   size_t cinv = 0;                                      // coarsest-grid inverse (FP64)
-  int lc = 0;                                           // first level of the one-block coarse kernel
+  int lc = 0;                                           // first level of the coarse solve
+  int ld = 0;                                           // level of the separable direct solve (0: none)
+  size_t dcy = 0, dly = 0, dtmp = 0;                    // its cosine basis, y eigenvalues, scratch
   size_t nn_act = 0, p_init = 0;                        // learned warm start: activations, p guess
   size_t part = 0;                                      // per-block partial sums (FP64)
   size_t total = 0;
@@ -138,13 +140,14 @@ int converge_solve(const AjStepParams& p, const Layout& L, void* ws, const float
                    float* pout, cudaStream_t st);
 size_t converge_block_smem(const Layout& L, int lc);
 int converge_first_block_level(const Layout& L);
+int converge_direct_level(const Layout& L);
 // learned warm start (aj_nn.cu)
 size_t nn_step_act_bytes(const AjStepParams& p);
 bool nn_step_shape_ok(const AjStepParams& p);
 int nn_warm_start(const AjStepParams& p, const Layout& L, void* ws, const float* b,
                   const float* mask, const float* pp, const uint16_t* packed, const float* master,
                   float* pinit, cudaStream_t st);
-constexpr size_t kBlockSmemMax = 200 * 1024;   // coarse-level kernel shared memory budget
+constexpr size_t kBlockSmemMax = 220 * 1024;   // coarse-level kernel shared memory budget
 
 inline unsigned cdiv(long a, long b) { return (unsigned)((a + b - 1) / b); }
 

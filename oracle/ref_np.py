@@ -996,9 +996,53 @@ def coarse_matrix(shape, level, dx, dy):
     return A
 
 
-def v_cycle_converge(r, dx, dy, depth, nu1=2, nu2=2):
-    """One V(nu1,nu2) cycle for A e = r from e = 0; returns e (level 0)."""
+def direct_level(nx, ny, depth, max_cells=65536, max_m=128, max_n=1024):
+    """Level of the separable direct coarse solve: the first level >= 1 with at
+    most max_cells cells, at most max_m cells across and max_n along the
+    channel (0: none; the V-cycle then runs down to the dense coarsest grid)."""
+    for level in range(1, depth + 1):
+        n, m = nx >> level, ny >> level
+        if n * m <= max_cells and m <= max_m and n <= max_n and n >= 2:
+            return level
+    return 0
+
+
+def coarse_solve_separable(r, level, dx, dy):
+    """Exact solve of the level-l operator (level >= 1).  It is separable:
+    A = ax Tx (x) I + ay I (x) Ty with Ty the Neumann-Neumann 1-D Laplacian,
+    diagonalised by the orthonormal DCT-II (eigenvalues -4 sin^2(pi k/2m)),
+    and Tx tridiagonal with an edge ghost at the inlet and the outlet ghost
+    g * e_last; one tridiagonal solve in x per cosine mode."""
+    from scipy.linalg import solve_banded
+    n, m = r.shape
+    hx, hy = dx * 2 ** level, dy * 2 ** level
+    ax, ay = 1.0 / hx ** 2, 1.0 / hy ** 2
+    kk = np.arange(m)[:, None]
+    jj = np.arange(m)[None, :]
+    C = np.sqrt(2.0 / m) * np.cos(np.pi * kk * (2 * jj + 1) / (2.0 * m))
+    C[0, :] = np.sqrt(1.0 / m)
+    ly = -4.0 * ay * np.sin(np.pi * np.arange(m) / (2.0 * m)) ** 2
+    rh = r @ C.T
+    dxv = np.full(n, -2.0)
+    dxv[0] += 1.0
+    dxv[-1] += outlet_ghost_factor(level)
+    eh = np.empty_like(rh)
+    for k in range(m):
+        ab = np.zeros((3, n))
+        ab[0, 1:] = ax
+        ab[1] = ax * dxv + ly[k]
+        ab[2, :-1] = ax
+        eh[:, k] = solve_banded((1, 1), ab, rh[:, k])
+    return eh @ C
+
+
+def v_cycle_converge(r, dx, dy, depth, nu1=2, nu2=2, direct=0):
+    """One V(nu1,nu2) cycle for A e = r from e = 0; returns e (level 0).
+    With direct > 0 the cycle stops at that level with the separable exact
+    solve; else it descends to the dense coarsest grid."""
     def cyc(rl, level):
+        if direct and level == direct:
+            return coarse_solve_separable(rl, level, dx, dy)
         if level == depth:
             A = coarse_matrix(rl.shape, level, dx, dy)
             return np.linalg.solve(A, rl.ravel()).reshape(rl.shape)
@@ -1010,18 +1054,22 @@ def v_cycle_converge(r, dx, dy, depth, nu1=2, nu2=2):
         e = e + prolong_bilinear(ec, level + 1)
         if level == 0:
             e[-1, :] = 0.0
-        return rbgs(e, rl, level, dx, dy, nu2, reverse=True)
+        return rbgs(e, rl, level, dx, dy, nu2)
     return cyc(r, 0)
 
 
-def mg_converge(b, dx, dy, rtol=1e-6, max_cycles=40, p0=None, nu1=2, nu2=2, max_coarse=64):
+def mg_converge(b, dx, dy, rtol=1e-6, max_cycles=40, p0=None, nu1=2, nu2=2, max_coarse=64,
+                direct=True):
     """Converging mode: iterative refinement around V-cycles.  Each outer
     iteration computes r = b - A p in float64, runs one V-cycle on A e = r and
-    adds e.  Stops when ||r||/||b|| <= rtol.  Returns (p, info)."""
+    adds e.  Stops when ||r||/||b|| <= rtol.  Returns (p, info).  The V-cycle
+    ends in the separable direct solve at direct_level() when direct is True
+    (as on the GPU), else at the dense coarsest grid."""
     b = np.asarray(b, np.float64).copy()
     b[-1, :] = 0.0
     nx, ny = b.shape
     depth = mg_depth(nx, ny, max_coarse)
+    dlev = direct_level(nx, ny, depth) if direct else 0
     p = np.zeros_like(b) if p0 is None else np.asarray(p0, np.float64).copy()
     p[-1, :] = 0.0
     nb = np.sqrt(np.sum(b ** 2))
@@ -1034,10 +1082,11 @@ def mg_converge(b, dx, dy, rtol=1e-6, max_cycles=40, p0=None, nu1=2, nu2=2, max_
         hist.append(float(rel))
         if rel <= rtol or cycles >= max_cycles:
             break
-        p = p + v_cycle_converge(r, dx, dy, depth, nu1, nu2)
+        p = p + v_cycle_converge(r, dx, dy, depth, nu1, nu2, dlev)
         p[-1, :] = 0.0
         cycles += 1
-    return p, {"cycles": cycles, "rel_residual": hist[-1], "history": hist, "depth": depth}
+    return p, {"cycles": cycles, "rel_residual": hist[-1], "history": hist, "depth": depth,
+               "direct_level": dlev}
 
 
 # ---------------------------------------------------------------------------
