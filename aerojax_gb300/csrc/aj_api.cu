@@ -83,6 +83,8 @@ int check_params(const AjStepParams& p) {
     if (nc > AJ_MAX_COARSE_HARD) return AJ_ERR_SHAPE;
     if (p.mg_rtol <= 0 || p.max_cycles < 1) return AJ_ERR_PARAM;
   }
+  if (p.warm_start < AJ_WARM_ZERO || p.warm_start > AJ_WARM_EXTRAPOLATE) return AJ_ERR_PARAM;
+  if (p.warm_start == AJ_WARM_EXTRAPOLATE && p.mg_mode != AJ_MG_CONVERGE) return AJ_ERR_PARAM;
   if (p.cfl_dt && (p.cfl_target <= 0 || p.dt_max <= 0)) return AJ_ERR_PARAM;
   if (!p.cfl_dt && p.dt <= 0) return AJ_ERR_PARAM;
   return AJ_OK;
@@ -142,6 +144,7 @@ bool make_layout(const AjStepParams& p, Layout& L) {
     L.ncoarse = L.ln[D] * L.lm[D];
     L.p64 = take(N * 8);
     L.p64b = take(N * 8);
+    if (p.warm_start == AJ_WARM_EXTRAPOLATE) L.hist = take(2 * N * 8);
     L.cinv = take((size_t)L.ncoarse * L.ncoarse * 8);
     // the coarse solve: an exact separable solve at level ld when one fits,
     // else levels lc..D in one thread block with everything in shared memory
@@ -157,7 +160,6 @@ bool make_layout(const AjStepParams& p, Layout& L) {
   }
   if (p.nn_factor > 0 && p.mg_mode == AJ_MG_CONVERGE && nn_step_shape_ok(p)) {
     L.nn_act = take(nn_step_act_bytes(p));
-    L.p_init = take(N * 4);
   }
   L.part = take(kPartials * 8);
   L.total = off;
@@ -274,15 +276,11 @@ static int enqueue_step(const AjStepParams& p, const Layout& L, void* ws, const 
   if (rc != AJ_OK) return rc;
   rc = launch_rhs(p, L, ws, us, vs, mask, at<float>(ws, L.b0), st);
   if (rc != AJ_OK) return rc;
-  if (nn.packed) {
-    // learned warm start: p_guess + the network's correction
-    float* pinit = at<float>(ws, L.p_init);
-    rc = nn_warm_start(p, L, ws, at<float>(ws, L.b0), mask, p_guess, nn.packed, nn.master, pinit,
-                       st);
-    if (rc != AJ_OK) return rc;
-    p_guess = pinit;
-  }
-  rc = launch_pressure(p, L, ws, mask, p_guess, po, stats, st);
+  NnWarm nw;
+  nw.packed = nn.packed;
+  nw.master = nn.master;
+  nw.mask = mask;
+  rc = launch_pressure(p, L, ws, mask, p_guess, po, stats, st, nn.packed ? &nw : nullptr);
   if (rc != AJ_OK) return rc;
   return launch_correct(p, L, ws, us, vs, po, mask, uo, vo, st);
 }
@@ -338,7 +336,7 @@ int32_t aj_step(const AjStepParams* prm, const float* u, const float* v, const f
   int rc = aj_check_params(prm);
   if (rc != AJ_OK) return rc;
   AjStepParams p = normalise(*prm);
-  if (p.warm_start && !p_guess) return AJ_ERR_PARAM;
+  if (p.warm_start == AJ_WARM_GUESS && !p_guess) return AJ_ERR_PARAM;
   Layout L;
   make_layout(p, L);
   if ((rc = ws_ok(L, ws, bytes)) != AJ_OK) return rc;
@@ -361,7 +359,7 @@ int32_t aj_step_nn(const AjStepParams* prm, const float* u, const float* v, cons
   AjStepParams p = normalise(*prm);
   if (p.mg_mode != AJ_MG_CONVERGE || p.nn_factor <= 0) return AJ_ERR_PARAM;
   if (!nn_step_shape_ok(p)) return AJ_ERR_SHAPE;
-  p.warm_start = 1;
+  if (p.warm_start != AJ_WARM_EXTRAPOLATE) p.warm_start = AJ_WARM_GUESS;
   Layout L;
   make_layout(p, L);
   if ((rc = ws_ok(L, ws, bytes)) != AJ_OK) return rc;
@@ -393,7 +391,8 @@ int32_t aj_poisson_mg(const AjStepParams* prm, const float* rhs, const float* ma
   Layout L;
   make_layout(p, L);
   if ((rc = ws_ok(L, ws, bytes)) != AJ_OK) return rc;
-  if (p.mg_mode == AJ_MG_CONVERGE) p.warm_start = p0 ? 1 : 0;
+  if (p.mg_mode == AJ_MG_CONVERGE && p.warm_start != AJ_WARM_EXTRAPOLATE)
+    p.warm_start = p0 ? AJ_WARM_GUESS : AJ_WARM_ZERO;
   std::string key = make_key(2, p, {ws, rhs, mask, p0, p_out, stats});
   return run_captured(key, (cudaStream_t)stream, [&](cudaStream_t s) {
     int r = launch_mg_rhs(p, L, ws, rhs, mask, s);
@@ -487,7 +486,7 @@ int32_t aj_kernel_count(const AjStepParams* prm, int32_t cycles) {
   }
   n += 1;                                                       // stats
   n += 1;                                                       // correction
-  if (p.nn_factor > 0) n += 3 + 18 + 1;                         // features, network, p_init
+  if (p.nn_factor > 0) n += 3 + 18 + 1;                         // features, network, correction
   return n;
 }
 

@@ -819,18 +819,46 @@ static void direct_launch(const CvDirect& d, cudaStream_t st) {
 static CvDirect direct_args(const AjStepParams& p, const Layout& L, void* ws, const int* done);
 
 // ---------------------------------------------------------------- set-up / solve
-// p = p0 (or 0) as hi, lo = 0, outlet row pinned
-__global__ void k_cv_init(const float* __restrict__ p0, float* __restrict__ ps, int n, int m) {
+// The initial double-FP32 state, outlet row pinned; a block per 8 rows.
+// With a history (warm start AJ_WARM_EXTRAPOLATE) of two solutions
+// p = p1 + (dt / dt1) (p1 - p2), of one solution p = p1; else p0 (or 0).
+struct CvHist {
+  const float* h;   // two slots of N hi values followed by N lo values; null: none
+  long N;
+};
+constexpr int CV_ROWS = 8;
+__global__ void __launch_bounds__(256) k_cv_init(const float* __restrict__ p0,
+                                                 float* __restrict__ ps, int n, int m, CvHist hs,
+                                                 const DevScalars* sc) {
   const long N = (long)n * m;
-  long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (k >= N) return;
-  int i = (int)(k / m);
-  ps[k] = (p0 && i != n - 1) ? p0[k] : 0.f;
-  ps[N + k] = 0.f;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= m) return;
+  const int hn = hs.h ? sc->hist_n : 0;
+  const float* h1 = hs.h ? hs.h + (long)sc->hist_cur * 2 * N : nullptr;
+  const float* h2 = hs.h ? hs.h + (long)(1 - sc->hist_cur) * 2 * N : nullptr;
+  float ratio = 1.f;
+  if (hn >= 2 && sc->dt > 0.f && sc->dt_prev > 0.f) ratio = sc->dt / sc->dt_prev;
+  const int i1 = min(n, (int)(blockIdx.y + 1) * CV_ROWS);
+  for (int i = blockIdx.y * CV_ROWS; i < i1; ++i) {
+    const long k = (long)i * m + j;
+    df v{0.f, 0.f};
+    if (i != n - 1) {
+      if (hn >= 2) {
+        const df a{h1[k], h1[N + k]}, b{h2[k], h2[N + k]};
+        v = df_add(a, df_mul(df{ratio, 0.f}, df_add(a, df_neg(b))));
+      } else if (hn == 1) {
+        v = df{h1[k], h1[N + k]};
+      } else if (p0) {
+        v.hi = p0[k];
+      }
+    }
+    ps[k] = v.hi;
+    ps[N + k] = v.lo;
+  }
 }
 
 // residual of the reference operator before the first cycle (double-FP32)
-// and the FP64 norms of r and b
+// and the FP64 norms of r and b; a block per 8 rows
 __global__ void __launch_bounds__(256) k_cv_resid(const float* __restrict__ ps,
                                                   const float* __restrict__ b,
                                                   float* __restrict__ r, int n, int m, DfCoef co,
@@ -838,29 +866,39 @@ __global__ void __launch_bounds__(256) k_cv_resid(const float* __restrict__ ps,
   const long N = (long)n * m;
   const df ax{co.axh, co.axl}, ay{co.ayh, co.ayl};
   float acc = 0.f, accb = 0.f;
-  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < N; k += (long)gridDim.x * blockDim.x) {
-    int i = (int)(k / m), j = (int)(k - (long)i * m);
-    float rr = 0.f;
-    if (i != n - 1) {
-      auto P = [&](long q) { return df{ps[q], ps[N + q]}; };
-      const df c = P(k);
-      const df xp = P((long)(i + 1) * m + j);
-      const df xm = i > 0 ? P((long)(i - 1) * m + j) : c;
-      const df yp = j + 1 < m ? P((long)i * m + j + 1) : c;
-      const df ym = j > 0 ? P((long)i * m + j - 1) : c;
-      const float bb = b[k];
-      const df res = df_residual(bb, c, xp, xm, yp, ym, ax, ay);
-      rr = res.hi + res.lo;
-      accb = fmaf(bb, bb, accb);
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < m) {
+    const int i1 = min(n, (int)(blockIdx.y + 1) * CV_ROWS);
+    for (int i = blockIdx.y * CV_ROWS; i < i1; ++i) {
+      const long k = (long)i * m + j;
+      float rr = 0.f;
+      if (i != n - 1) {
+        auto P = [&](long q) { return df{ps[q], ps[N + q]}; };
+        const df c = P(k);
+        const df xp = P(k + m);
+        const df xm = i > 0 ? P(k - m) : c;
+        const df yp = j + 1 < m ? P(k + 1) : c;
+        const df ym = j > 0 ? P(k - 1) : c;
+        const float bb = b[k];
+        const df res = df_residual(bb, c, xp, xm, yp, ym, ax, ay);
+        rr = res.hi + res.lo;
+        accb = fmaf(bb, bb, accb);
+      }
+      r[k] = rr;
+      acc = fmaf(rr, rr, acc);
     }
-    r[k] = rr;
-    acc = fmaf(rr, rr, acc);
   }
   block_sum_atomic((double)acc, &sc->acc[0]);
   block_sum_atomic((double)accb, &sc->acc[1]);
 }
 
 __global__ void k_cv_begin(DevScalars* sc) {
+  if (sc->hist_pending) {       // the last solve's state went to the other slot
+    sc->hist_cur = 1 - sc->hist_cur;
+    sc->hist_n = sc->hist_n < 2 ? sc->hist_n + 1 : 2;
+    sc->dt_prev = sc->dt_last;
+    sc->hist_pending = 0;
+  }
   sc->mg_done = 0;
   sc->mg_cycles = 0;
   sc->loops = 0;
@@ -888,10 +926,24 @@ __global__ void k_cv_check0(DevScalars* sc, double rtol) {
   sc->acc[1] = 0.0;
 }
 
-__global__ void k_cv_out(PState ps, const DevScalars* sc, float* __restrict__ p, long N) {
+// p = hi + lo; with a history, the state also goes to the free slot (the
+// next k_cv_begin makes it the latest)
+__global__ void k_cv_out(PState ps, DevScalars* sc, float* __restrict__ p, long N, float* hist) {
   long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
   const float* src = sc->pcur ? ps.b : ps.a;
-  if (k < N) p[k] = src[k] + src[N + k];
+  if (k < N) {
+    const float hi = src[k], lo = src[N + k];
+    p[k] = hi + lo;
+    if (hist) {
+      float* dst = hist + (long)(1 - sc->hist_cur) * 2 * N;
+      dst[k] = hi;
+      dst[N + k] = lo;
+    }
+  }
+  if (hist && k == 0) {
+    sc->hist_pending = 1;
+    sc->dt_last = sc->dt;
+  }
 }
 
 static CvBlock block_args(const AjStepParams& p, const Layout& L, void* ws, const int* done) {
@@ -995,16 +1047,21 @@ static cudaStream_t side_stream() {
 }
 
 int converge_solve(const AjStepParams& p, const Layout& L, void* ws, const float* p0,
-                   float* pout, cudaStream_t st) {
+                   float* pout, cudaStream_t st, const NnWarm* nn) {
   DevScalars* sc = at<DevScalars>(ws, 0);
   const long N = (long)p.nx * p.ny;
   const PState ps = pstate(L, ws);
   k_cv_begin<<<1, 1, 0, st>>>(sc);
-  k_cv_init<<<cdiv(N, 256), 256, 0, st>>>(p.warm_start ? p0 : nullptr, ps.a, p.nx, p.ny);
-  unsigned nb = cdiv(N, 256 * 4);
-  if (nb > 1216) nb = 1216;
-  k_cv_resid<<<nb, 256, 0, st>>>(ps.a, at<float>(ws, L.b0), at<float>(ws, L.B[0]), p.nx, p.ny,
-                                 df_coef(1.0 / (p.dx * p.dx), 1.0 / (p.dy * p.dy)), sc);
+  const dim3 rgrid(cdiv(p.ny, 256), cdiv(p.nx, CV_ROWS));
+  const bool extrap = p.warm_start == AJ_WARM_EXTRAPOLATE && L.hist;
+  CvHist hs{extrap ? at<float>(ws, L.hist) : nullptr, N};
+  k_cv_init<<<rgrid, 256, 0, st>>>(p.warm_start ? p0 : nullptr, ps.a, p.nx, p.ny, hs, sc);
+  if (nn && nn->packed) {
+    const int rc = nn_correct_state(p, L, ws, at<float>(ws, L.b0), *nn, ps.a, st);
+    if (rc != AJ_OK) return rc;
+  }
+  k_cv_resid<<<rgrid, 256, 0, st>>>(ps.a, at<float>(ws, L.b0), at<float>(ws, L.B[0]), p.nx, p.ny,
+                                    df_coef(1.0 / (p.dx * p.dx), 1.0 / (p.dy * p.dy)), sc);
   k_cv_check0<<<1, 1, 0, st>>>(sc, p.mg_rtol);
 
   cudaStreamCaptureStatus cs;
@@ -1047,7 +1104,7 @@ int converge_solve(const AjStepParams& p, const Layout& L, void* ws, const float
     cudaGraph_t out;
     if (cudaStreamEndCapture(side, &out) != cudaSuccess) return AJ_ERR_CUDA;
   }
-  k_cv_out<<<cdiv(N, 256), 256, 0, st>>>(ps, sc, pout, N);
+  k_cv_out<<<cdiv(N, 256), 256, 0, st>>>(ps, sc, pout, N, extrap ? at<float>(ws, L.hist) : nullptr);
   return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
 }
 

@@ -31,6 +31,11 @@ struct DevScalars {
   int loops;           // converging mode: executions of the while body
   int pcur;            // converging mode: which FP64 pressure buffer is current
   double nn_rms_r, nn_rms_p, nn_out_scale;   // learned warm start: per-sample scales
+  int hist_n;          // converging mode: solutions held in the history (0..2)
+  int hist_cur;        // history slot of the latest solution
+  int hist_pending;    // a solve finished since the last k_cv_begin
+  float dt_last;       // dt of the last finished solve
+  float dt_prev;       // dt of the latest solution in the history
   unsigned int pad_[3];
 };
 
@@ -46,11 +51,12 @@ struct Layout {
   size_t X[AJ_MAX_LEVELS + 1] = {0}, T[AJ_MAX_LEVELS + 1] = {0};
   size_t B[AJ_MAX_LEVELS + 1] = {0}, M[AJ_MAX_LEVELS + 1] = {0};
   size_t p64 = 0, p64b = 0;                             // converging mode FP64 pressure (ping-pong)
+  size_t hist = 0;                                      // extrapolation history: 2 double-FP32 solutions
   size_t cinv = 0;                                      // coarsest-grid inverse (FP64)
   int lc = 0;                                           // first level of the coarse solve
   int ld = 0;                                           // level of the separable direct solve (0: none)
   size_t dcy = 0, dly = 0, dtmp = 0;                    // its cosine basis, y eigenvalues, scratch
-  size_t nn_act = 0, p_init = 0;                        // learned warm start: activations, p guess
+  size_t nn_act = 0;                                    // learned warm start: activations
   size_t part = 0;                                      // per-block partial sums (FP64)
   size_t total = 0;
   // multigrid hierarchy
@@ -130,23 +136,31 @@ int prepare_pressure(const AjStepParams& p, const Layout& L, void* ws, const flo
                      cudaStream_t st);
 int launch_mg_rhs(const AjStepParams& p, const Layout& L, void* ws, const float* rhs,
                   const float* mask, cudaStream_t st);
+// the learned warm start inside a converging solve (null pointers: off)
+struct NnWarm {
+  const uint16_t* packed = nullptr;
+  const float* master = nullptr;
+  const float* mask = nullptr;
+};
 int launch_pressure(const AjStepParams& p, const Layout& L, void* ws, const float* mask,
-                    const float* p0, float* pout, AjStats* stats, cudaStream_t st);
+                    const float* p0, float* pout, AjStats* stats, cudaStream_t st,
+                    const NnWarm* nn = nullptr);
 int profile_pressure_kernel(const AjStepParams& p, const Layout& L, void* ws, int which,
                             cudaStream_t st);
 // converging multigrid (aj_converge.cu)
 int converge_prepare(const AjStepParams& p, const Layout& L, void* ws, cudaStream_t st);
 int converge_solve(const AjStepParams& p, const Layout& L, void* ws, const float* p0,
-                   float* pout, cudaStream_t st);
+                   float* pout, cudaStream_t st, const NnWarm* nn = nullptr);
 size_t converge_block_smem(const Layout& L, int lc);
 int converge_first_block_level(const Layout& L);
 int converge_direct_level(const Layout& L);
 // learned warm start (aj_nn.cu)
 size_t nn_step_act_bytes(const AjStepParams& p);
 bool nn_step_shape_ok(const AjStepParams& p);
-int nn_warm_start(const AjStepParams& p, const Layout& L, void* ws, const float* b,
-                  const float* mask, const float* pp, const uint16_t* packed, const float* master,
-                  float* pinit, cudaStream_t st);
+// adds the network's correction to the initial double-FP32 state (hi: N
+// floats, lo: N floats) of a converging solve with right-hand side b
+int nn_correct_state(const AjStepParams& p, const Layout& L, void* ws, const float* b,
+                     const NnWarm& nn, float* state, cudaStream_t st);
 constexpr size_t kBlockSmemMax = 220 * 1024;   // coarse-level kernel shared memory budget
 
 inline unsigned cdiv(long a, long b) { return (unsigned)((a + b - 1) / b); }

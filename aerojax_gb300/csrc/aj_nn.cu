@@ -13,8 +13,8 @@
 // (zero padding, bias, ReLU), 2x2 average pooling, nearest 2x upsampling.
 // Activations are FP32 NHWC [n][h][w][c]; weights are kept as an FP32 master
 // copy (flat: per layer W[3][3][Cin][Cout] then b[Cout]) and packed to BF16
-// twice per layer: Wf[tap][Cin][Cout] for the forward pass and
-// Wb[8-tap][Cout][Cin] (the adjoint of a stride-1 'SAME' convolution is the
+// twice per layer: WfT[tap][Cout][Cin] for the forward pass and
+// WbT[8-tap][Cin][Cout] (the adjoint of a stride-1 'SAME' convolution is the
 // convolution with the flipped, channel-transposed kernel) for the input
 // gradient.
 #include "aj_internal.cuh"
@@ -61,116 +61,176 @@ __device__ __forceinline__ void mma_bf16(float* d, const uint32_t* a, const uint
 }
 
 // ---------------------------------------------------------------- convolution
-// Implicit GEMM: M = pixels (64 per block, 16 per warp), N = Cout (<= 128),
-// K = 9 taps x Cin (16 per step).  A = the input shifted by the tap (zero
-// outside the image), converted to BF16 on its way into shared memory;
-// B = Wf[tap][ci][co] held transposed in shared memory ([co][k]) so both
-// fragments are 32-bit shared loads.
-constexpr int CONV_BM = 64, CONV_THREADS = 128, CONV_BNMAX = 128;
-constexpr int CONV_AS = 16 + 8;     // bf16 row stride of the A tile (pad: no bank conflicts)
-constexpr int CONV_BS = 16 + 8;     // bf16 row stride of the transposed B tile
+// Implicit GEMM on 8 x 8 pixel tiles: M = 64 pixels (16 per warp: two tile
+// rows), N = BN output channels of the block, K = 9 taps x Cin.  The block
+// stages the 10 x 10 x Cin halo of its tile once, converted to BF16, so that
+// every tap is an offset into shared memory, and the weights of all 9 taps
+// for its BN channels (WT[tap][co][ci]) with cp.async: one wait, one barrier,
+// then the whole K loop runs from shared memory.  Row strides of Cin + 8 BF16
+// keep the fragment loads free of bank conflicts.
+constexpr int CT = 8;                       // pixel tile edge
+constexpr int CT_HALO = (CT + 2) * (CT + 2);
+constexpr int CONV_THREADS = 128;
 
-template <int NT>   // NT = Cout / 8
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int NPEND>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(NPEND));
+}
+
+template <int CIN, int NT>
+struct ConvSmem {
+  static constexpr int AS = CIN + 8, BN = NT * 8;
+  static constexpr size_t bytes = (size_t)(CT_HALO * AS + 9 * BN * AS) * 2;
+};
+
+template <int CIN, int NT>   // BN = NT * 8 output channels per block
 __global__ void __launch_bounds__(CONV_THREADS) k_conv3x3(const float* __restrict__ X, int N, int H,
-                                                          int W, int Cin,
-                                                          const __nv_bfloat16* __restrict__ Wt,
+                                                          int W, int Cout,
+                                                          const __nv_bfloat16* __restrict__ WT,
                                                           const float* __restrict__ bias,
                                                           float* __restrict__ Y, int relu) {
-  constexpr int Cout = NT * 8;
-  __shared__ __align__(16) __nv_bfloat16 As[CONV_BM * CONV_AS];
-  __shared__ __align__(16) __nv_bfloat16 Bs[CONV_BNMAX * CONV_BS];
+  using S = ConvSmem<CIN, NT>;
+  constexpr int AS = S::AS, BN = S::BN;
+  extern __shared__ __align__(16) unsigned char conv_sm[];
+  __nv_bfloat16* As = reinterpret_cast<__nv_bfloat16*>(conv_sm);
+  __nv_bfloat16* Bs = As + CT_HALO * AS;     // [tap][BN][AS]
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int g = lane >> 2, tg = lane & 3;
-  const long P = (long)N * H * W;
-  const long p0 = (long)blockIdx.x * CONV_BM;
+  const int tilesW = (W + CT - 1) / CT, tilesH = (H + CT - 1) / CT;
+  int t = blockIdx.x;
+  const int tw = t % tilesW;
+  t /= tilesW;
+  const int th = t % tilesH;
+  const int n = t / tilesH;
+  const int h0 = th * CT, w0 = tw * CT, co0 = blockIdx.y * BN;
+  {  // weights of the 9 taps: 9 * BN rows of CIN BF16, CIN / 8 16-byte pieces each
+    constexpr int PR = CIN / 8;
+    for (int e = tid; e < 9 * BN * PR; e += CONV_THREADS) {
+      const int row = e / PR, q = e - row * PR;
+      const int tap = row / BN, r = row - tap * BN;
+      cp_async16(Bs + row * AS + q * 8, WT + ((long)tap * Cout + co0 + r) * CIN + q * 8);
+    }
+    cp_async_commit();
+  }
+  {  // the halo tile, FP32 -> BF16
+    constexpr int C4 = CIN / 4;
+    for (int e = tid; e < CT_HALO * C4; e += CONV_THREADS) {
+      const int px = e / C4, q = e - px * C4;
+      const int hy = px / (CT + 2), hx = px - hy * (CT + 2);
+      const int gh = h0 - 1 + hy, gw = w0 - 1 + hx;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (gh >= 0 && gh < H && gw >= 0 && gw < W)
+        v = *reinterpret_cast<const float4*>(X + (((long)n * H + gh) * W + gw) * CIN + q * 4);
+      uint2 pk;
+      pk.x = pack_bf16x2(v.x, v.y);
+      pk.y = pack_bf16x2(v.z, v.w);
+      *reinterpret_cast<uint2*>(As + px * AS + q * 4) = pk;
+    }
+  }
+  cp_async_wait<0>();
+  __syncthreads();
   float acc[NT][4];
 #pragma unroll
-  for (int t = 0; t < NT; ++t) acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.f;
-  // the pixel this thread loads for A (two threads per pixel, 8 channels each)
-  const int apx = tid >> 1, ahalf = tid & 1;
-  const long ap = p0 + apx;
-  int an = 0, ah = 0, aw = 0;
-  if (ap < P) {
-    an = (int)(ap / ((long)H * W));
-    const int rem = (int)(ap - (long)an * H * W);
-    ah = rem / W;
-    aw = rem - ah * W;
-  }
+  for (int q = 0; q < NT; ++q) acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.f;
+  const int ty0 = 2 * warp;   // this warp's tile rows: ty0 (fragment rows g) and ty0 + 1 (g + 8)
+#pragma unroll 1
   for (int tap = 0; tap < 9; ++tap) {
-    const int dy = tap / 3 - 1, dx = tap % 3 - 1;
-    const int hh = ah + dy, ww = aw + dx;
-    const bool inside = ap < P && hh >= 0 && hh < H && ww >= 0 && ww < W;
-    const float* src = X + (((long)an * H + hh) * W + ww) * Cin + ahalf * 8;
-    for (int c0 = 0; c0 < Cin; c0 += 16) {
-      // A: 64 pixels x 16 channels
-      float4 v0 = make_float4(0.f, 0.f, 0.f, 0.f), v1 = v0;
-      if (inside) {
-        v0 = *reinterpret_cast<const float4*>(src + c0);
-        v1 = *reinterpret_cast<const float4*>(src + c0 + 4);
-      }
-      uint4 pk;
-      pk.x = pack_bf16x2(v0.x, v0.y);
-      pk.y = pack_bf16x2(v0.z, v0.w);
-      pk.z = pack_bf16x2(v1.x, v1.y);
-      pk.w = pack_bf16x2(v1.z, v1.w);
-      *reinterpret_cast<uint4*>(&As[apx * CONV_AS + ahalf * 8]) = pk;
-      // B: 16 x Cout, stored transposed
-      const __nv_bfloat16* wsrc = Wt + ((long)tap * Cin + c0) * Cout;
-      for (int e = tid; e < 16 * Cout; e += CONV_THREADS) {
-        const int k = e / Cout, n = e - k * Cout;
-        Bs[n * CONV_BS + k] = wsrc[(long)k * Cout + n];
-      }
-      __syncthreads();
-      uint32_t a[4];
-      const int r = warp * 16 + g;
-      a[0] = *reinterpret_cast<const uint32_t*>(&As[r * CONV_AS + tg * 2]);
-      a[1] = *reinterpret_cast<const uint32_t*>(&As[(r + 8) * CONV_AS + tg * 2]);
-      a[2] = *reinterpret_cast<const uint32_t*>(&As[r * CONV_AS + tg * 2 + 8]);
-      a[3] = *reinterpret_cast<const uint32_t*>(&As[(r + 8) * CONV_AS + tg * 2 + 8]);
+    const int dy = tap / 3, dx = tap % 3;   // halo offsets (tap - centre + 1)
+    const __nv_bfloat16* a0p = As + ((ty0 + dy) * (CT + 2) + g + dx) * AS + tg * 2;
+    const __nv_bfloat16* a1p = a0p + (CT + 2) * AS;
+    const __nv_bfloat16* Bt = Bs + tap * BN * AS;
 #pragma unroll
-      for (int t = 0; t < NT; ++t) {
+    for (int ks = 0; ks < CIN / 16; ++ks) {
+      uint32_t a[4];
+      a[0] = *reinterpret_cast<const uint32_t*>(a0p + ks * 16);
+      a[1] = *reinterpret_cast<const uint32_t*>(a1p + ks * 16);
+      a[2] = *reinterpret_cast<const uint32_t*>(a0p + ks * 16 + 8);
+      a[3] = *reinterpret_cast<const uint32_t*>(a1p + ks * 16 + 8);
+#pragma unroll
+      for (int q = 0; q < NT; ++q) {
+        const __nv_bfloat16* bp = Bt + (q * 8 + g) * AS + ks * 16 + tg * 2;
         uint32_t b[2];
-        const int n = t * 8 + g;
-        b[0] = *reinterpret_cast<const uint32_t*>(&Bs[n * CONV_BS + tg * 2]);
-        b[1] = *reinterpret_cast<const uint32_t*>(&Bs[n * CONV_BS + tg * 2 + 8]);
-        mma_bf16(acc[t], a, b);
+        b[0] = *reinterpret_cast<const uint32_t*>(bp);
+        b[1] = *reinterpret_cast<const uint32_t*>(bp + 8);
+        mma_bf16(acc[q], a, b);
       }
-      __syncthreads();
     }
   }
   // epilogue: bias, ReLU, store
 #pragma unroll
-  for (int t = 0; t < NT; ++t) {
-    const int col = t * 8 + tg * 2;
+  for (int q = 0; q < NT; ++q) {
+    const int col = co0 + q * 8 + tg * 2;
     const float b0 = bias ? bias[col] : 0.f, b1 = bias ? bias[col + 1] : 0.f;
 #pragma unroll
     for (int half = 0; half < 2; ++half) {
-      const long p = p0 + warp * 16 + g + half * 8;
-      if (p >= P) continue;
-      float y0 = acc[t][half * 2] + b0, y1 = acc[t][half * 2 + 1] + b1;
+      const int gh = h0 + ty0 + half, gw = w0 + g;
+      if (gh >= H || gw >= W) continue;
+      float y0 = acc[q][half * 2] + b0, y1 = acc[q][half * 2 + 1] + b1;
       if (relu) {
         y0 = fmaxf(y0, 0.f);
         y1 = fmaxf(y1, 0.f);
       }
-      *reinterpret_cast<float2*>(&Y[p * Cout + col]) = make_float2(y0, y1);
+      *reinterpret_cast<float2*>(&Y[(((long)n * H + gh) * W + gw) * Cout + col]) =
+          make_float2(y0, y1);
     }
   }
 }
 
-static int conv3x3(const float* X, int N, int H, int W, int Cin, int Cout,
-                   const __nv_bfloat16* Wt, const float* bias, float* Y, int relu,
-                   cudaStream_t st) {
-  const long P = (long)N * H * W;
-  dim3 grid(cdiv(P, CONV_BM));
+template <int CIN, int NT>
+static void conv_launch(const float* X, int N, int H, int W, int Cout, const __nv_bfloat16* WT,
+                        const float* bias, float* Y, int relu, cudaStream_t st) {
+  using S = ConvSmem<CIN, NT>;
+  const int tiles = ((W + CT - 1) / CT) * ((H + CT - 1) / CT) * N;
+  dim3 grid(tiles, Cout / S::BN);
+  k_conv3x3<CIN, NT><<<grid, CONV_THREADS, S::bytes, st>>>(X, N, H, W, Cout, WT, bias, Y, relu);
+}
+
+template <int CIN, int NT>
+static void conv_attr() {
+  cudaFuncSetAttribute(k_conv3x3<CIN, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)ConvSmem<CIN, NT>::bytes);
+}
+// the dynamic shared-memory opt-in of every convolution instance (once, before
+// any launch or capture)
+static void conv_attrs() {
+  static bool done = false;
+  if (done) return;
+  conv_attr<16, 2>(); conv_attr<16, 4>();
+  conv_attr<32, 2>(); conv_attr<32, 4>();
+  conv_attr<64, 2>(); conv_attr<64, 4>();
+  conv_attr<128, 2>(); conv_attr<128, 4>();
+  done = true;
+}
+
+template <int CIN>
+static int conv_cin(const float* X, int N, int H, int W, int Cout, const __nv_bfloat16* WT,
+                    const float* bias, float* Y, int relu, cudaStream_t st) {
   switch (Cout) {
-    case 8: k_conv3x3<1><<<grid, CONV_THREADS, 0, st>>>(X, N, H, W, Cin, Wt, bias, Y, relu); break;
-    case 16: k_conv3x3<2><<<grid, CONV_THREADS, 0, st>>>(X, N, H, W, Cin, Wt, bias, Y, relu); break;
-    case 32: k_conv3x3<4><<<grid, CONV_THREADS, 0, st>>>(X, N, H, W, Cin, Wt, bias, Y, relu); break;
-    case 64: k_conv3x3<8><<<grid, CONV_THREADS, 0, st>>>(X, N, H, W, Cin, Wt, bias, Y, relu); break;
-    case 128: k_conv3x3<16><<<grid, CONV_THREADS, 0, st>>>(X, N, H, W, Cin, Wt, bias, Y, relu); break;
+    case 16: conv_launch<CIN, 2>(X, N, H, W, Cout, WT, bias, Y, relu, st); break;
+    case 32:
+    case 64:
+    case 128: conv_launch<CIN, 4>(X, N, H, W, Cout, WT, bias, Y, relu, st); break;
     default: return AJ_ERR_PARAM;
   }
   return AJ_OK;
+}
+
+// Y = conv(X, WT) (+ bias, ReLU); WT[tap][Cout][Cin] BF16
+static int conv3x3(const float* X, int N, int H, int W, int Cin, int Cout,
+                   const __nv_bfloat16* WT, const float* bias, float* Y, int relu,
+                   cudaStream_t st) {
+  switch (Cin) {
+    case 16: return conv_cin<16>(X, N, H, W, Cout, WT, bias, Y, relu, st);
+    case 32: return conv_cin<32>(X, N, H, W, Cout, WT, bias, Y, relu, st);
+    case 64: return conv_cin<64>(X, N, H, W, Cout, WT, bias, Y, relu, st);
+    case 128: return conv_cin<128>(X, N, H, W, Cout, WT, bias, Y, relu, st);
+    default: return AJ_ERR_PARAM;
+  }
 }
 
 // ---------------------------------------------------------------- weight gradient
@@ -372,7 +432,8 @@ struct PackTab {
   int cin[NL], cout[NL];
 };
 
-// FP32 master weights -> BF16 Wf[tap][ci][co] and Wb[8-tap][co][ci]
+// FP32 master weights -> BF16 WfT[tap][co][ci] (forward) and
+// WbT[8-tap][ci][co] (the adjoint: output channel ci, input channel co)
 __global__ void k_pack(const float* __restrict__ master, __nv_bfloat16* __restrict__ packed,
                        PackTab tab) {
   const int l = blockIdx.y;
@@ -387,8 +448,8 @@ __global__ void k_pack(const float* __restrict__ master, __nv_bfloat16* __restri
     const int ci = (int)(q % cin);
     const int tap = (int)(q / cin);
     const __nv_bfloat16 b = __float2bfloat16_rn(W[e]);
-    Wf[e] = b;
-    Wb[((long)(8 - tap) * cout + co) * cin + ci] = b;
+    Wf[((long)tap * cout + co) * cin + ci] = b;
+    Wb[((long)(8 - tap) * cin + ci) * cout + co] = b;
   }
 }
 
@@ -648,18 +709,16 @@ __global__ void k_nn_target(const float* __restrict__ pt, const float* __restric
   target[(long)I * w + J] = (float)((double)(a / (float)(F * F)) / sc->nn_out_scale);
 }
 
-// p_init = p_prev + bilinear prolongation of (prediction * out_scale); the
+// state += bilinear prolongation of (prediction * out_scale), added to the
+// double-FP32 state (hi: N floats, lo: N floats) with Knuth's TwoSum; the
 // outlet row stays pinned at 0
-__global__ void k_nn_apply(const float* __restrict__ y, const float* __restrict__ pp, int nx,
-                           int ny, int F, float* __restrict__ pinit, const DevScalars* sc) {
+__global__ void k_nn_apply(const float* __restrict__ y, int nx, int ny, int F,
+                           float* __restrict__ state, const DevScalars* sc) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= nx || j >= ny) return;
+  if (i >= nx - 1 || j >= ny) return;
+  const long N = (long)nx * ny;
   const long k = (long)i * ny + j;
-  if (i == nx - 1) {
-    pinit[k] = 0.f;
-    return;
-  }
   const int h = nx / F, w = ny / F;
   const float xi = (i + 0.5f) / F - 0.5f, xj = (j + 0.5f) / F - 0.5f;
   int i0 = (int)floorf(xi), j0 = (int)floorf(xj);
@@ -670,7 +729,13 @@ __global__ void k_nn_apply(const float* __restrict__ y, const float* __restrict_
   const float v00 = y[((long)i0 * w + j0) * 16], v01 = y[((long)i0 * w + j1) * 16];
   const float v10 = y[((long)i1 * w + j0) * 16], v11 = y[((long)i1 * w + j1) * 16];
   const float v = (1.f - ti) * ((1.f - tj) * v00 + tj * v01) + ti * ((1.f - tj) * v10 + tj * v11);
-  pinit[k] = pp[k] + (float)(v * sc->nn_out_scale);
+  const float c = (float)(v * sc->nn_out_scale);
+  const float hi = state[k], lo = state[N + k];
+  const float s = hi + c, bb = s - hi;
+  const float e = (hi - (s - bb)) + (c - bb) + lo;
+  const float s2 = s + e;
+  state[k] = s2;
+  state[N + k] = e - (s2 - s);
 }
 
 // [n][h][w][3] -> [n][h][w][16] (zeros beyond the features)
@@ -698,19 +763,21 @@ int nn_features(const AjStepParams& p, void* ws, const float* b, const float* ma
   return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
 }
 
-// the learned warm start inside a step: features, network, p_init
-int nn_warm_start(const AjStepParams& p, const Layout& L, void* ws, const float* b,
-                  const float* mask, const float* pp, const uint16_t* packed, const float* master,
-                  float* pinit, cudaStream_t st) {
+// the learned warm start inside a converging solve: features of the initial
+// state, the network, the correction added to the state
+int nn_correct_state(const AjStepParams& p, const Layout& L, void* ws, const float* b,
+                     const NnWarm& nn, float* state, cudaStream_t st) {
+  conv_attrs();
   const int F = p.nn_factor, h = p.nx / F, w = p.ny / F;
+  if (F <= 0 || !L.nn_act) return AJ_ERR_PARAM;
   NnActs A = act_layout(1, h, w, at<char>(ws, L.nn_act));
-  int rc = nn_features(p, ws, b, mask, pp, nullptr, A.x, nullptr, nullptr, st);
+  int rc = nn_features(p, ws, b, nn.mask, state, nullptr, A.x, nullptr, nullptr, st);
   if (rc != AJ_OK) return rc;
-  NnW W{reinterpret_cast<const __nv_bfloat16*>(packed), master};
+  NnW W{reinterpret_cast<const __nv_bfloat16*>(nn.packed), nn.master};
   rc = nn_forward(1, h, w, W, A, st);
   if (rc != AJ_OK) return rc;
   dim3 blk(32, 8), grd(cdiv(p.ny, 32), cdiv(p.nx, 8));
-  k_nn_apply<<<grd, blk, 0, st>>>(A.y, pp, p.nx, p.ny, F, pinit, at<DevScalars>(ws, 0));
+  k_nn_apply<<<grd, blk, 0, st>>>(A.y, p.nx, p.ny, F, state, at<DevScalars>(ws, 0));
   return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
 }
 
@@ -748,6 +815,7 @@ float* aj_nn_input(int32_t n, int32_t h, int32_t w, void* act) {
 
 int32_t aj_nn_pack(const float* master, uint16_t* packed, void* stream) {
   if (!master || !packed) return AJ_ERR_PARAM;
+  conv_attrs();
   dim3 grid(64, NL);
   k_pack<<<grid, 256, 0, (cudaStream_t)stream>>>(master, reinterpret_cast<__nv_bfloat16*>(packed),
                                                    pack_tab());
@@ -757,6 +825,7 @@ int32_t aj_nn_pack(const float* master, uint16_t* packed, void* stream) {
 int32_t aj_nn_forward(int32_t n, int32_t h, int32_t w, const uint16_t* packed, const float* master,
                       void* act, size_t act_bytes, float* y_out, void* stream) {
   if (!nn_shape_ok(n, h, w) || !packed || !master || !act) return AJ_ERR_PARAM;
+  conv_attrs();
   NnActs A = act_layout(n, h, w, act);
   if (act_bytes < A.total) return AJ_ERR_WORKSPACE;
   NnW W{reinterpret_cast<const __nv_bfloat16*>(packed), master};
@@ -773,6 +842,7 @@ int32_t aj_nn_backward(int32_t n, int32_t h, int32_t w, const float* dy, const u
                        const float* master, void* act, size_t act_bytes, float* grad,
                        void* stream) {
   if (!nn_shape_ok(n, h, w) || !dy || !packed || !master || !act || !grad) return AJ_ERR_PARAM;
+  conv_attrs();
   NnActs A = act_layout(n, h, w, act);
   if (act_bytes < A.total) return AJ_ERR_WORKSPACE;
   NnW W{reinterpret_cast<const __nv_bfloat16*>(packed), master};

@@ -313,10 +313,11 @@ int prepare_pressure(const AjStepParams& p, const Layout& L, void* ws, const flo
 }
 
 int launch_pressure(const AjStepParams& p, const Layout& L, void* ws, const float* mask,
-                    const float* p0, float* pout, AjStats* stats, cudaStream_t st) {
+                    const float* p0, float* pout, AjStats* stats, cudaStream_t st,
+                    const NnWarm* nn) {
   int rc;
   if (p.mg_mode == AJ_MG_PARITY) rc = parity_solve(p, L, ws, mask, p0, pout, st);
-  else rc = converge_solve(p, L, ws, p0, pout, st);
+  else rc = converge_solve(p, L, ws, p0, pout, st, nn);
   if (rc != AJ_OK) return rc;
   if (stats) k_stats<<<1, 1, 0, st>>>(at<DevScalars>(ws, 0), stats, p.mg_mode == AJ_MG_CONVERGE);
   return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;

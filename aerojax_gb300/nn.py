@@ -4,16 +4,17 @@ and training — every computation runs in libaerojax_gb300.so.
 The reference trains its learned pressure operators on snapshots the GUI
 solver writes (neural_operators/training_utils.py:12-81) with MSE, Adam and
 gradients clipped to [-1, 1], keeping the best epoch (:162-248).  Here the
-network predicts a correction to the previous pressure on a grid ``factor``
-times coarser; the converging multigrid then finishes every solve to the same
-relative residual, so the network only ever changes how many V-cycles a step
-needs.  Snapshots are produced on the GPU by the solver itself and kept in
-device memory.
+network predicts a correction to the converging solve's initial guess on a
+grid ``factor`` times coarser; the multigrid then finishes every solve to the
+same relative residual, so the network only ever changes how many V-cycles a
+step needs.  Snapshots are produced on the GPU by the solver itself and kept
+in device memory.
 """
 from __future__ import annotations
 
 import ctypes
 import math
+import os
 from dataclasses import dataclass, replace
 from typing import List, Optional
 
@@ -29,6 +30,9 @@ from .solver import Plan, _stream, get_plan, make_geometry, make_params, run_ste
 LAYERS = [(16, 32, 1), (32, 32, 1), (32, 64, 1), (64, 64, 1), (64, 128, 1), (128, 128, 1),
           (128, 128, 1), (128, 128, 1), (128, 64, 1), (64, 32, 1), (32, 32, 1), (32, 16, 0)]
 FEATURES = 3
+# trained weights for the NACA 0012 MAC 2048x512 workload (network grid 256x64)
+WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights",
+                       "warmstart_naca0012_2048x512_f8.npz")
 
 
 def init_params(seed: int = 0) -> np.ndarray:
@@ -79,6 +83,7 @@ class WarmStartNet:
     def load(cls, path: str, device="cuda"):
         with np.load(path) as z:
             return cls(device=device, params=z["master"])
+
 
     # -- passes --------------------------------------------------------------
     def acts(self, n, h, w):
@@ -149,7 +154,8 @@ class Snapshots:
     cfgs: list                # (geometry parameters) per snapshot
 
 
-def naca_case(nx, ny, aoa_deg, le_shift_cells, device, factor=4, rtol=1e-6, seed=0):
+def naca_case(nx, ny, aoa_deg, le_shift_cells, device, factor=8, rtol=1e-6, seed=0,
+              warm_start="extrapolate"):
     """The NACA 0012 MAC workload family with a given angle of attack and
     leading-edge shift (cells): the learned warm start's training geometry."""
     from . import configs
@@ -163,16 +169,26 @@ def naca_case(nx, ny, aoa_deg, le_shift_cells, device, factor=4, rtol=1e-6, seed
     eps = 0.05 * c.dx
     mask, _ = make_geometry("naca4", nx, ny, lx, ly, (chord, aoa_deg, xle, yle, 0.0, 0.0, 0.12),
                             eps, device)
-    cfg = replace(c, nn_factor=factor, warm_start=True)
+    cfg = replace(c, nn_factor=factor, warm_start=warm_start)
     return dict(cfg=cfg, mask=mask, u=base["u"], v=base["v"])
 
 
-def generate_snapshots(nx=2048, ny=512, n_geoms=40, steps=500, warmup=20, factor=4, seed=0,
+def initial_guess(p1, p2, dt, dt1, n_hist):
+    """The converging solve's initial guess under AJ_WARM_EXTRAPOLATE, in FP32:
+    p1 + (dt / dt1)(p1 - p2) with two solutions in the history, p1 with one."""
+    if n_hist >= 2:
+        return p1 + (dt / dt1) * (p1 - p2)
+    return p1.clone()
+
+
+def generate_snapshots(nx=2048, ny=512, n_geoms=40, steps=500, warmup=2, factor=8, seed=0,
                        device="cuda", aoa_range=(0.0, 15.0), shift_cells=64, log=None) -> Snapshots:
-    """Runs the solver on randomly drawn geometries (angle of attack uniform in
-    aoa_range, leading edge shifted uniformly by +-shift_cells) and records, for
-    every step after the warm-up, the network features of the step's pressure
-    solve and the target correction (converged p minus previous p)."""
+    """Runs the solver (extrapolated warm start) on randomly drawn geometries
+    (angle of attack uniform in aoa_range, leading edge shifted uniformly by
+    +-shift_cells at 2048 cells) and records, for every step after the
+    warm-up, the network features of the step's pressure solve (its rhs, the
+    mask and its initial guess) and the target correction (converged p minus
+    the initial guess)."""
     rng = np.random.default_rng(seed)
     h, w = nx // factor, ny // factor
     N = n_geoms * steps
@@ -190,21 +206,25 @@ def generate_snapshots(nx=2048, ny=512, n_geoms=40, steps=500, warmup=20, factor
         bufs = [(case["u"].clone(), case["v"].clone(),
                  torch.zeros((nx, ny), dtype=torch.float32, device=device)) for _ in range(2)]
         cur = 0
+        hist, dts = [], []
         for s in range(warmup + steps):
             src, dst = bufs[cur], bufs[1 - cur]
             run_step(plan, src[0], src[1], case["mask"], p_guess=src[2], out=dst)
-            if s >= warmup:
+            dts.append(plan.stats()["dt"])
+            if s >= max(warmup, 2):
+                p_init = initial_guess(hist[-1], hist[-2], dts[-1], dts[-2], 2)
                 rhs = L.aj_workspace_rhs(ctypes.byref(plan.params), plan.ws.data_ptr())
                 check("aj_nn_features", L.aj_nn_features(
-                    ctypes.byref(plan.params), rhs, case["mask"].data_ptr(), src[2].data_ptr(),
+                    ctypes.byref(plan.params), rhs, case["mask"].data_ptr(), p_init.data_ptr(),
                     dst[2].data_ptr(), x3[k].data_ptr(), tgt[k].data_ptr(), plan.ws.data_ptr(),
                     plan.nbytes, _stream(None)))
                 meta.append((aoa, shift, s))
                 k += 1
+            hist = (hist + [dst[2].clone()])[-2:]
             cur = 1 - cur
         if log:
             log(f"geometry {gidx + 1}/{n_geoms}: aoa={aoa:.2f} shift={shift} cells")
-    return Snapshots(x3=x3, target=tgt, factor=factor, cfgs=meta)
+    return Snapshots(x3=x3[:k], target=tgt[:k], factor=factor, cfgs=meta)
 
 
 def train(net: WarmStartNet, data: Snapshots, epochs=3, batch=16, lr=1e-3, holdout=0.1, seed=0,
@@ -256,8 +276,9 @@ def train(net: WarmStartNet, data: Snapshots, epochs=3, batch=16, lr=1e-3, holdo
 
 
 def run_step_nn(plan: Plan, net: WarmStartNet, u, v, mask, p_prev, out=None, stream=None):
-    """One step whose pressure solve starts from p_prev + the network's
-    correction (aj_step_nn); returns (u, v, p)."""
+    """One step whose pressure solve starts from the plan's initial guess
+    (p_prev, or the extrapolation of the workspace's history) plus the
+    network's correction (aj_step_nn); returns (u, v, p)."""
     cfg = plan.cfg
     if out is None:
         out = (torch.empty_like(u), torch.empty_like(v),

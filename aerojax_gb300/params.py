@@ -123,7 +123,7 @@ class StepConfig:
     mg_rtol: float = 1e-6
     mg_tolerance: float = 1e-6
     max_cycles: int = 40
-    warm_start: bool = False
+    warm_start: Any = False       # False/True (p_guess) or "extrapolate"
     nn_factor: int = 0
     has_sdf: bool = False
     cfl_dt: bool = False

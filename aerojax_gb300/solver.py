@@ -50,6 +50,16 @@ def _f32(t, name, shape=None, device=None):
     return t
 
 
+def warm_mode(w) -> int:
+    """StepConfig.warm_start -> AJ_WARM_*: False 0 (zero guess), True 1
+    (p_guess), "extrapolate" 2 (the workspace's last two solutions)."""
+    if isinstance(w, str):
+        if w != "extrapolate":
+            raise ValueError(f"warm_start={w!r}: expected a bool or 'extrapolate'")
+        return 2
+    return int(bool(w))
+
+
 def make_params(cfg: StepConfig) -> AjStepParams:
     p = AjStepParams()
     p.nx, p.ny = cfg.nx, cfg.ny
@@ -66,7 +76,7 @@ def make_params(cfg: StepConfig) -> AjStepParams:
     p.max_cycles = cfg.max_cycles
     p.has_sdf = int(cfg.has_sdf)
     p.cfl_dt = int(cfg.cfl_dt)
-    p.warm_start = int(cfg.warm_start)
+    p.warm_start = warm_mode(cfg.warm_start)
     p.nn_factor = int(cfg.nn_factor)
     p.dx, p.dy = cfg.dx, cfg.dy
     p.dt = cfg.dt
@@ -233,7 +243,7 @@ class StepHandler:
         _f32(mask, "mask", (nx, ny))
         plan = self.plan(u.device)
         plan.prepare(mask, self.sdf if self.cfg.has_sdf else None, stream)
-        if self.cfg.warm_start and p_guess is None:
+        if warm_mode(self.cfg.warm_start) == 1 and p_guess is None:
             raise ValueError("warm_start needs p_guess")
         return run_step(plan, u, v, mask, p_guess if self.cfg.warm_start else None, out=out,
                         stream=stream, dt=dt if dt is not None else self.dt)

@@ -8,10 +8,14 @@ residual (FP64 norm) by the converging multigrid.  One "step" is one full
 projection step (LES, RK3 predictor, divergence, pressure solve, correction,
 boundary conditions).
 
-Arms on the GPU (all through aj_step, whole step captured in one CUDA graph):
-  method   pressure warm-started from the previous step's pressure
+Arms on the GPU (whole step captured in one CUDA graph each):
+  nn       aj_step_nn: the learned warm start (trained weights in
+           aerojax_gb300/weights) corrects the double-FP32 extrapolation of the
+           last two pressures, then the converging multigrid
+  extrap   aj_step with the extrapolated warm start alone
   plain    the plain GPU multigrid step: zero initial guess, same tolerance
-value = cell-steps/s of `method`; the plain arm is reported next to it.
+value = cell-steps/s of `nn` (the metric's arm); the others are reported in
+config.arms.
 
 `python bench.py --impl reference` times the reference algorithm's CPU path
 (the NumPy port of the reference GUI step, float32, 5 reference V-cycles) on
@@ -34,6 +38,7 @@ sys.path.insert(0, ROOT)
 METRIC = "Mcell-steps/s at 2048×512 FP32, NN-warm-start+MG vs plain MG at equal div tol"
 UNIT = "Mcell-steps/s"
 FLUSH_BYTES = 256 << 20          # larger than the 126 MB L2
+NN_FACTOR = 8                    # network grid 256x64 at 2048x512
 # DRAM bytes of one k_cv_up0 launch at 2048x512 from an ncu capture
 TRAFFIC_UP0 = 22056192
 
@@ -174,6 +179,7 @@ def gpu_arm(args):
     import torch
     import aerojax_gb300 as aj
     from aerojax_gb300 import _lib, configs
+    from aerojax_gb300 import nn as NNW
     from aerojax_gb300.build import build
 
     world, rank, local = dist_env()
@@ -191,16 +197,30 @@ def gpu_arm(args):
     mask = case["mask"]
     flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=dev)
 
-    def make_arm(warm):
+    net = None
+    if os.path.exists(NNW.WEIGHTS):
+        net = NNW.WarmStartNet.load(NNW.WEIGHTS, device=dev)
+
+    def make_arm(kind):
+        """plain: zero initial guess; extrap: double-FP32 extrapolation of the
+        last two solutions; nn: the extrapolation plus the network's
+        correction (the metric's arm)."""
         from dataclasses import replace
-        cfg = replace(case["cfg"], warm_start=warm)
+        warm = {"plain": False, "extrap": "extrapolate", "nn": "extrapolate"}[kind]
+        cfg = replace(case["cfg"], warm_start=warm, nn_factor=NN_FACTOR if kind == "nn" else 0)
         plan = aj.get_plan(cfg, dev)
         plan.prepare(mask)
         bufs = [(case["u"].clone(), case["v"].clone(), torch.zeros((args.nx, args.ny), device=dev))
                 for _ in range(2)]
         return plan, bufs
 
-    def run(plan, bufs, k, timed, warm):
+    def step(plan, kind, src, dst):
+        if kind == "nn":
+            NNW.run_step_nn(plan, net, src[0], src[1], mask, src[2], out=dst)
+        else:
+            aj.run_step(plan, src[0], src[1], mask, p_guess=src[2], out=dst)
+
+    def run(plan, bufs, k, timed, kind):
         """k steps, ping-ponging two state buffers; per-step CUDA events."""
         st = torch.cuda.current_stream()
         times, cycles = [], []
@@ -210,7 +230,7 @@ def gpu_arm(args):
             flush.zero_()                               # evict the working set from L2
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(st)
-            aj.run_step(plan, src[0], src[1], mask, p_guess=src[2] if warm else None, out=dst)
+            step(plan, kind, src, dst)
             e1.record(st)
             times.append((e0, e1))
             cur = 1 - cur
@@ -238,50 +258,56 @@ def gpu_arm(args):
             return float(t.item())
         return x
 
-    def soak(plan, bufs, warm, seconds):
+    def soak(plan, bufs, kind, seconds):
         t0 = time.perf_counter()
         while time.perf_counter() - t0 < seconds:
-            run(plan, bufs, 20, False, warm)
+            run(plan, bufs, 20, False, kind)
 
+    head = "nn" if net is not None else "extrap"
     if args.profile:
-        plan, bufs = make_arm(True)
-        run(plan, bufs, max(3, args.warmup), False, True)
-        ms, cyc = run(plan, bufs, args.steps, True, True)
+        plan, bufs = make_arm(head)
+        run(plan, bufs, max(3, args.warmup), False, head)
+        ms, cyc = run(plan, bufs, args.steps, True, head)
         if rank == 0:
-            print(json.dumps({"profile_steps": args.steps, "ms_per_step": ms / args.steps,
+            print(json.dumps({"profile_steps": args.steps, "arm": head,
+                              "ms_per_step": ms / args.steps,
                               "cycles": [c[0] for c in cyc], "errors": [c[2] for c in cyc]}))
         return
 
     results = {}
     clocks = ClockSampler(local)
-    for name, warm in (("plain", False), ("method", True)):
-        plan, bufs = make_arm(warm)
-        run(plan, bufs, max(3, args.warmup), False, warm)
+    clk = None
+    for kind in ("plain", "extrap", "nn"):
+        if kind == "nn" and net is None:
+            continue
+        plan, bufs = make_arm(kind)
+        run(plan, bufs, max(3, args.warmup), False, kind)
         barrier()
-        sample_clocks = name == "method" and not args.quick
+        sample_clocks = kind == head and not args.quick
         if sample_clocks:
             clocks.start()                      # sample clocks over >= 1.5 s of load
-            soak(plan, bufs, warm, 1.0)
-        ms, cyc = run(plan, bufs, args.steps, True, warm)
+        soak(plan, bufs, kind, 0.0 if args.quick else 1.0)   # the same flow stage for every arm
+        ms, cyc = run(plan, bufs, args.steps, True, kind)
         if sample_clocks:
-            soak(plan, bufs, warm, 0.5)
+            soak(plan, bufs, kind, 0.5)
             clk = clocks.stop()
-        elif name == "method":
-            clk = None
         barrier()
         ms = max_over_ranks(ms)
-        results[name] = dict(ms=ms, cycles=cyc, plan=plan, bufs=bufs)
+        results[kind] = dict(ms=ms, cycles=cyc, plan=plan, bufs=bufs)
 
-    meth = results["method"]
+    def arm_summary(r):
+        ms = r["ms"] / args.steps
+        return {"value": world * cells / (ms * 1e-3) / 1e6, "ms_per_step": ms,
+                "mg_cycles_mean": statistics.mean(c[0] for c in r["cycles"]),
+                "rel_residual_max": max(c[1] for c in r["cycles"]),
+                "device_errors": sorted({c[2] for c in r["cycles"]})}
+
+    arms = {k: arm_summary(r) for k, r in results.items()}
+    meth = results[head]
     ms_step = meth["ms"] / args.steps
     value = world * cells / (ms_step * 1e-3) / 1e6
-    plain_ms = results["plain"]["ms"] / args.steps
-    plain_value = world * cells / (plain_ms * 1e-3) / 1e6
+    plain_value = arms["plain"]["value"]
     cyc_m = [c[0] for c in meth["cycles"]]
-    cyc_p = [c[0] for c in results["plain"]["cycles"]]
-    rel_m = max(c[1] for c in meth["cycles"])
-    rel_p = max(c[1] for c in results["plain"]["cycles"])
-    errs = sorted({c[2] for c in meth["cycles"] + results["plain"]["cycles"]})
     plan = meth["plan"]
     launches = sum(int(L.aj_kernel_count(ctypes.byref(plan.params), c)) for c in cyc_m)
 
@@ -303,7 +329,7 @@ def gpu_arm(args):
             e0.record(st)
             for d, h in zip(d_in, h_in):
                 d.copy_(h, non_blocking=True)
-            aj.run_step(plan, d_in[0], d_in[1], mask, p_guess=d_in[2], out=tuple(d_out))
+            step(plan, head, d_in, tuple(d_out))
             for h, d in zip(h_out, d_out):
                 h.copy_(d, non_blocking=True)
             e1.record(st)
@@ -344,14 +370,13 @@ def gpu_arm(args):
         "data": "synthetic (seeded NACA 0012 flow; the solver generates every step)",
         "config": {
             "workload": case["name"], "nx": args.nx, "ny": args.ny, "grid": "mac",
-            "method": "converging MG (FP32 red-black V-cycles, double-FP32 refinement, FP64 coarsest "
-                      "and norms) warm-started from the previous pressure",
-            "rel_residual_target": 1e-6, "rel_residual_max": rel_m,
-            "mg_cycles_mean": statistics.mean(cyc_m) if cyc_m else None,
-            "plain_mg_value": plain_value, "plain_mg_ms_per_step": plain_ms,
-            "plain_mg_cycles_mean": statistics.mean(cyc_p) if cyc_p else None,
-            "plain_rel_residual_max": rel_p, "device_errors": errs,
-            "speedup_vs_plain": value / plain_value,
+            "method": ("learned warm start (4-level BF16 conv encoder-decoder on the 256x64 grid, "
+                       "correction to the double-FP32 extrapolation of the last two pressures), "
+                       "then converging MG (FP32 red-black V-cycles, exact separable coarse solve, "
+                       "double-FP32 refinement, FP64 norms)") if head == "nn" else
+                      "converging MG warm-started from the double-FP32 extrapolation",
+            "rel_residual_target": 1e-6, "arms": arms,
+            "plain_mg_value": plain_value, "speedup_vs_plain": value / plain_value,
             "l2": "flushed before every step (256 MiB write outside the timed events)",
             "parallelism": "replicas only" if world > 1 else "single GPU",
         },

@@ -54,6 +54,14 @@ enum { AJ_ADV_UPWIND = 0, AJ_ADV_WENO5 = 1 };
    CONVERGE = red-black Gauss-Seidel V-cycles inside FP64 iterative
               refinement, FP64 coarsest solve and norms, relative stop. */
 enum { AJ_MG_PARITY = 0, AJ_MG_CONVERGE = 1 };
+/* Initial guess of the converging solve (no reference counterpart: the
+   reference always starts from p = 0, multigrid_solver.py:219).
+   ZERO        p = 0
+   GUESS       p = p_guess (float, caller-owned)
+   EXTRAPOLATE p = p1 + (dt / dt1) (p1 - p2) from the last two solutions of
+               this workspace, kept in double-FP32 by the library; p_guess
+               (nullable) seeds the first two steps. */
+enum { AJ_WARM_ZERO = 0, AJ_WARM_GUESS = 1, AJ_WARM_EXTRAPOLATE = 2 };
 
 /* Every scalar and static option of one step.  Mirrors the keyword arguments
    of step_pure (solver/pure_functions/step.py:50-66) plus the attributes the
@@ -73,7 +81,7 @@ typedef struct {
   int32_t max_cycles;            /* converging mode: cap on refinement cycles         */
   int32_t has_sdf;               /* collocated: chi from sdf (rk3_simple_new.py:194)  */
   int32_t cfl_dt;                /* 1 = dt from the CFL rule on the device each step  */
-  int32_t warm_start;            /* converging mode: start from p_guess               */
+  int32_t warm_start;            /* converging mode initial guess: AJ_WARM_*          */
   int32_t nn_factor;             /* learned warm start: network grid is nx/F x ny/F
                                     (0 = off; aj_step_nn only)                        */
   double dx, dy;

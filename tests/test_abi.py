@@ -70,6 +70,21 @@ def test_param_errors(L):
     assert L.aj_check_params(ctypes.byref(_params(grid_type="mac", variant="gui"))) == 0
     assert L.aj_check_params(ctypes.byref(_params(mg_mode="converge", mg_rtol=0.0))) == 2
     assert L.aj_check_params(ctypes.byref(_params(mg_mode="converge"))) == 0
+    # AJ_WARM_EXTRAPOLATE exists for the converging solve only
+    assert L.aj_check_params(ctypes.byref(_params(mg_mode="converge",
+                                                  warm_start="extrapolate"))) == 0
+    assert L.aj_check_params(ctypes.byref(_params(warm_start="extrapolate"))) == 2
+    p = _params(mg_mode="converge")
+    p.warm_start = 3
+    assert L.aj_check_params(ctypes.byref(p)) == 2
+
+
+def test_extrapolation_history_in_workspace(L):
+    """The extrapolation warm start keeps two double-FP32 solutions (16 bytes
+    per cell) in the workspace."""
+    a = L.aj_workspace_size(ctypes.byref(_params(mg_mode="converge", warm_start=True)))
+    b = L.aj_workspace_size(ctypes.byref(_params(mg_mode="converge", warm_start="extrapolate")))
+    assert b - a >= 16 * 512 * 96
 
 
 def test_workspace_grows_with_grid(L):

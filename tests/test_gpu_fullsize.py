@@ -155,3 +155,34 @@ def test_naca_converge_step(cuda_lib):
         assert st["err"] == 0, st
         assert st["rel_residual"] <= 1e-6, st
     assert torch.isfinite(u).all() and torch.isfinite(v).all()
+
+
+def test_extrapolated_warm_start(cuda_lib):
+    """AJ_WARM_EXTRAPOLATE starts each solve from p1 + (dt/dt1)(p1 - p2) of the
+    workspace's own double-FP32 history: the same converged steps as the
+    previous-pressure warm start, in no more V-cycles."""
+    from dataclasses import replace
+    import torch
+    import aerojax_gb300 as aj
+    from aerojax_gb300 import configs
+    from aerojax_gb300.solver import Plan
+    case = configs.naca_mac_2048x512(nx=512, ny=128, mg_mode="converge")
+    m = case["mask"]
+    res = {}
+    for mode in (True, "extrapolate"):
+        plan = Plan(replace(case["cfg"], warm_start=mode), m.device)
+        plan.prepare(m)
+        u, v = case["u"].clone(), case["v"].clone()
+        p = torch.zeros((512, 128), device="cuda")
+        cyc = []
+        for _ in range(40):
+            u, v, p = aj.run_step(plan, u, v, m, p_guess=p)
+            st = plan.stats()
+            assert st["err"] == 0 and st["rel_residual"] <= 1e-6, st
+            cyc.append(st["cycles"])
+        res[mode] = (u, v, p, cyc)
+    ue, ve, pe, ce = res["extrapolate"]
+    up, vp, pp, cp = res[True]
+    assert sum(ce[10:]) <= sum(cp[10:])
+    assert float((ue - up).abs().max()) < 1e-3
+    assert float((pe - pp).abs().max()) < 1e-2 * float(pp.abs().max())

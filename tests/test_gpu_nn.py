@@ -240,3 +240,58 @@ def test_step_nn_converges_to_the_same_solution(dev):
     assert float((p2 - p3).abs().max()) < 1e-3 * scale
     assert float((u2 - u3).abs().max()) < 1e-4
     assert float((v2 - v3).abs().max()) < 1e-4
+
+
+def test_trained_warm_start_gain(dev):
+    """What the trained network (aerojax_gb300/weights) gains, on a geometry
+    outside its training draws (angle of attack 7.3 deg, leading edge +17
+    cells) of the 2048x512 NACA workload:
+      - its correction explains most of the extrapolation error it is given
+        (held-out MSE well below the zero-correction MSE);
+      - V-cycles per step against the plain multigrid (zero guess), the FP32
+        previous-pressure guess and the double-FP32 extrapolation it corrects.
+    The multigrid finishes every solve to 1e-6 in all arms."""
+    import os
+    from dataclasses import replace
+    from aerojax_gb300 import nn as NN
+    from aerojax_gb300.solver import Plan, run_step
+    assert os.path.exists(NN.WEIGHTS), "trained weights missing"
+    net = NN.WarmStartNet.load(NN.WEIGHTS, device=dev)
+    aoa, shift = 7.3, 17
+    # prediction quality on snapshots of the held-out geometry
+    data = NN.generate_snapshots(2048, 512, n_geoms=1, steps=30, factor=8, device=dev,
+                                 aoa_range=(aoa, aoa), shift_cells=0)
+    n, h, w, _ = data.x3.shape
+    net.expand(data.x3.contiguous(), n, h, w)
+    y = net.forward(None, n, h, w)
+    loss, _ = net.loss(y, data.target.contiguous(), n, h, w)
+    zero = float(data.target.pow(2).mean())
+    assert float(loss.item()) < 0.6 * zero, (float(loss.item()), zero)
+    # V-cycles per step, 60 steps from the same initial state
+    case = NN.naca_case(2048, 512, aoa, shift, dev, factor=8)
+    cyc = {}
+    for arm, warm in (("zero", False), ("prev", True), ("extrap", "extrapolate"),
+                      ("nn", "extrapolate")):
+        cfg = replace(case["cfg"], warm_start=warm, nn_factor=8 if arm == "nn" else 0)
+        plan = Plan(cfg, dev)
+        plan.prepare(case["mask"])
+        u, v = case["u"].clone(), case["v"].clone()
+        p = torch.zeros((2048, 512), device=dev)
+        c = []
+        for _ in range(60):
+            if arm == "nn":
+                u, v, p = NN.run_step_nn(plan, net, u, v, case["mask"], p)
+            else:
+                u, v, p = run_step(plan, u, v, case["mask"], p_guess=p)
+            st = plan.stats()
+            assert st["err"] == 0 and st["rel_residual"] <= 1e-6, (arm, st)
+            c.append(st["cycles"])
+        cyc[arm] = float(np.mean(c[5:]))
+    print("mean V-cycles per step:", cyc, "held-out MSE", float(loss.item()), "zero", zero)
+    # measured on GB300: zero 5.0, prev 3.96, extrap 2.89, nn 3.11 (the
+    # correction removes ~94% of the error energy it sees, but what sets the
+    # residual after the first V-cycle is error below the 8-cell scale of the
+    # network grid, which no coarse correction carries)
+    assert cyc["nn"] <= cyc["zero"] - 1.5
+    assert cyc["nn"] <= cyc["prev"] - 0.5
+    assert cyc["nn"] <= cyc["extrap"] + 0.5

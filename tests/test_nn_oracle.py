@@ -58,3 +58,13 @@ def test_adam_matches_closed_form_first_step():
     w1, m, v = N.adam_step(w, g, np.zeros(3), np.zeros(3), 1, lr=0.1)
     # first step: m_hat = clip(g), v_hat = clip(g)^2  ->  w - lr * sign(g)
     assert np.allclose(w1, w - 0.1 * np.sign(np.clip(g, -1, 1)) * (np.abs(g) > 0), atol=1e-6)
+
+
+def test_package_network_table_matches_oracle():
+    """The host package (aerojax_gb300.nn) describes the same network as the
+    oracle: layer table, parameter count and initialisation."""
+    from aerojax_gb300 import nn as P
+    assert [(a, b, int(r)) for a, b, r in P.LAYERS] == [(a, b, int(r)) for _, a, b, r in N.LAYERS]
+    flat = P.init_params(3)
+    assert flat.size == N.num_params()
+    assert np.allclose(flat, N.init_params(3).astype(np.float32))
