@@ -486,7 +486,7 @@ int32_t aj_kernel_count(const AjStepParams* prm, int32_t cycles) {
   }
   n += 1;                                                       // stats
   n += 1;                                                       // correction
-  if (p.nn_factor > 0) n += 3 + 18 + 1;                         // features, network, correction
+  if (p.nn_factor > 0) n += 3 + 15 + 1;                         // features, network, correction
   return n;
 }
 

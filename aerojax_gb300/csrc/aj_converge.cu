@@ -140,7 +140,7 @@ struct TileCfg {
   static_assert(NTH % PAIRS == 0, "threads must fill whole rows of column pairs");
 };
 using T0 = TileCfg<48, 64, 256>;   // level 0: 38 x 54 interior
-using T1 = TileCfg<32, 32, 128>;   // coarser levels: 22 x 22 interior
+using T1 = TileCfg<32, 32, 256>;   // coarser levels: 22 x 22 interior
 
 __device__ __forceinline__ float cv_diag(const CvLvl& L, int gi, int gj) {
   float d = -2.f * (L.ax + L.ay);
@@ -680,34 +680,32 @@ int converge_direct_level(const Layout& L) {
   return 0;
 }
 
-// rhat[k][i] = sum_j Cy[k][j] r[i][j]: 32 x 32 output tiles, 32-wide slices
-// of j staged in shared memory; thread (tx, ty) owns i = i0 + tx and the
-// modes k0 + ty + 8q
+// rhat[k][i] = sum_j Cy[k][j] r[i][j]: 32 x 32 output tiles; both operand
+// panels (32 x m, m <= 128) are staged whole, so the block waits for global
+// memory once; thread (tx, ty) owns i = i0 + tx and the modes k0 + ty + 8q
 constexpr int CV_DT = 32;
+constexpr int CV_DK = CV_DIRECT_MAX_M + 1;
 __global__ void __launch_bounds__(256) k_cv_dfwd(CvDirect a) {
   if (*a.done) return;
-  __shared__ float Cs[CV_DT][CV_DT + 1];
-  __shared__ float Rs[CV_DT][CV_DT + 1];
+  __shared__ float Cs[CV_DT][CV_DK];
+  __shared__ float Rs[CV_DT][CV_DK];
   const int n = a.n, m = a.m;
   const int i0 = blockIdx.x * CV_DT, k0 = blockIdx.y * CV_DT;
   const int tx = threadIdx.x, ty = threadIdx.y;
+  for (int rr = ty; rr < CV_DT; rr += 8) {
+    const int k = k0 + rr, i = i0 + rr;
+    for (int j = tx; j < m; j += CV_DT) {
+      Cs[rr][j] = k < m ? ldg(a.cy + (long)k * m + j) : 0.f;
+      Rs[rr][j] = i < n ? ldg(a.r + (long)i * m + j) : 0.f;
+    }
+  }
+  __syncthreads();
   float acc[4] = {0.f, 0.f, 0.f, 0.f};
-  for (int j0 = 0; j0 < m; j0 += CV_DT) {
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int rr = ty + 8 * q, j = j0 + tx;
-      const int k = k0 + rr, i = i0 + rr;
-      Cs[rr][tx] = (k < m && j < m) ? ldg(a.cy + (long)k * m + j) : 0.f;
-      Rs[rr][tx] = (i < n && j < m) ? ldg(a.r + (long)i * m + j) : 0.f;
-    }
-    __syncthreads();
 #pragma unroll 8
-    for (int jj = 0; jj < CV_DT; ++jj) {
-      const float rv = Rs[tx][jj];
+  for (int j = 0; j < m; ++j) {
+    const float rv = Rs[tx][j];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) acc[q] = fmaf(Cs[ty + 8 * q][jj], rv, acc[q]);
-    }
-    __syncthreads();
+    for (int q = 0; q < 4; ++q) acc[q] = fmaf(Cs[ty + 8 * q][j], rv, acc[q]);
   }
   const int i = i0 + tx;
 #pragma unroll
@@ -775,32 +773,28 @@ __global__ void __launch_bounds__(1024) k_cv_dpcr(CvDirect a) {
   if (i < n) a.ehat[(long)k * n + i] = Dc[i] / Bc[i];
 }
 
-// e[i][j] = sum_k ehat[k][i] Cy[k][j]: 32 x 32 output tiles; thread (tx, ty)
-// owns j = j0 + tx and the rows i0 + ty + 8q
+// e[i][j] = sum_k ehat[k][i] Cy[k][j]: 32 x 32 output tiles, both m x 32
+// operand panels staged whole; thread (tx, ty) owns j = j0 + tx and the rows
+// i0 + ty + 8q
 __global__ void __launch_bounds__(256) k_cv_dbwd(CvDirect a) {
   if (*a.done) return;
-  __shared__ float Es[CV_DT][CV_DT + 1];
-  __shared__ float Cs[CV_DT][CV_DT + 1];
+  __shared__ float Es[CV_DIRECT_MAX_M][CV_DT + 1];
+  __shared__ float Cs[CV_DIRECT_MAX_M][CV_DT + 1];
   const int n = a.n, m = a.m;
   const int j0 = blockIdx.x * CV_DT, i0 = blockIdx.y * CV_DT;
   const int tx = threadIdx.x, ty = threadIdx.y;
+  for (int k = ty; k < m; k += 8) {
+    const int i = i0 + tx, j = j0 + tx;
+    Es[k][tx] = i < n ? ldg(a.ehat + (long)k * n + i) : 0.f;
+    Cs[k][tx] = j < m ? ldg(a.cy + (long)k * m + j) : 0.f;
+  }
+  __syncthreads();
   float acc[4] = {0.f, 0.f, 0.f, 0.f};
-  for (int kb = 0; kb < m; kb += CV_DT) {
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int kk = ty + 8 * q, k = kb + kk;
-      const int i = i0 + tx, j = j0 + tx;
-      Es[kk][tx] = (k < m && i < n) ? ldg(a.ehat + (long)k * n + i) : 0.f;
-      Cs[kk][tx] = (k < m && j < m) ? ldg(a.cy + (long)k * m + j) : 0.f;
-    }
-    __syncthreads();
 #pragma unroll 8
-    for (int kk = 0; kk < CV_DT; ++kk) {
-      const float cv = Cs[kk][tx];
+  for (int k = 0; k < m; ++k) {
+    const float cv = Cs[k][tx];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) acc[q] = fmaf(Es[kk][ty + 8 * q], cv, acc[q]);
-    }
-    __syncthreads();
+    for (int q = 0; q < 4; ++q) acc[q] = fmaf(Es[k][ty + 8 * q], cv, acc[q]);
   }
   const int j = j0 + tx;
 #pragma unroll
@@ -826,7 +820,7 @@ struct CvHist {
   const float* h;   // two slots of N hi values followed by N lo values; null: none
   long N;
 };
-constexpr int CV_ROWS = 8;
+constexpr int CV_ROWS = 8;   // rows per block of the whole-grid kernels (unrolled)
 __global__ void __launch_bounds__(256) k_cv_init(const float* __restrict__ p0,
                                                  float* __restrict__ ps, int n, int m, CvHist hs,
                                                  const DevScalars* sc) {
@@ -838,8 +832,10 @@ __global__ void __launch_bounds__(256) k_cv_init(const float* __restrict__ p0,
   const float* h2 = hs.h ? hs.h + (long)(1 - sc->hist_cur) * 2 * N : nullptr;
   float ratio = 1.f;
   if (hn >= 2 && sc->dt > 0.f && sc->dt_prev > 0.f) ratio = sc->dt / sc->dt_prev;
-  const int i1 = min(n, (int)(blockIdx.y + 1) * CV_ROWS);
-  for (int i = blockIdx.y * CV_ROWS; i < i1; ++i) {
+#pragma unroll
+  for (int r = 0; r < CV_ROWS; ++r) {
+    const int i = blockIdx.y * CV_ROWS + r;
+    if (i >= n) break;
     const long k = (long)i * m + j;
     df v{0.f, 0.f};
     if (i != n - 1) {
@@ -868,8 +864,10 @@ __global__ void __launch_bounds__(256) k_cv_resid(const float* __restrict__ ps,
   float acc = 0.f, accb = 0.f;
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j < m) {
-    const int i1 = min(n, (int)(blockIdx.y + 1) * CV_ROWS);
-    for (int i = blockIdx.y * CV_ROWS; i < i1; ++i) {
+#pragma unroll
+    for (int rr_ = 0; rr_ < CV_ROWS; ++rr_) {
+      const int i = blockIdx.y * CV_ROWS + rr_;
+      if (i >= n) break;
       const long k = (long)i * m + j;
       float rr = 0.f;
       if (i != n - 1) {

@@ -63,10 +63,11 @@ __device__ __forceinline__ void mma_bf16(float* d, const uint32_t* a, const uint
 // ---------------------------------------------------------------- convolution
 // Implicit GEMM on 8 x 8 pixel tiles: M = 64 pixels (16 per warp: two tile
 // rows), N = BN output channels of the block, K = 9 taps x Cin.  The block
-// stages the 10 x 10 x Cin halo of its tile once, converted to BF16, so that
-// every tap is an offset into shared memory, and the weights of all 9 taps
-// for its BN channels (WT[tap][co][ci]) with cp.async: one wait, one barrier,
-// then the whole K loop runs from shared memory.  Row strides of Cin + 8 BF16
+// stages the 10 x 10 x Cin FP32 halo of its tile (zero-filled outside the
+// image) and the BF16 weights of all 9 taps for its BN channels
+// (WT[tap][co][ci]) with cp.async: one wait, one barrier, then the whole K
+// loop runs from shared memory, every tap an offset into the halo; operands
+// are rounded to BF16 as the fragments are built.  Row strides of Cin + 8
 // keep the fragment loads free of bank conflicts.
 constexpr int CT = 8;                       // pixel tile edge
 constexpr int CT_HALO = (CT + 2) * (CT + 2);
@@ -76,6 +77,11 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
 }
+// 16 bytes, or zeros when src_bytes == 0 (the source is then not read)
+__device__ __forceinline__ void cp_async16z(void* smem, const void* gmem, int src_bytes) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(src_bytes));
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
 template <int NPEND>
 __device__ __forceinline__ void cp_async_wait() {
@@ -84,8 +90,8 @@ __device__ __forceinline__ void cp_async_wait() {
 
 template <int CIN, int NT>
 struct ConvSmem {
-  static constexpr int AS = CIN + 8, BN = NT * 8;
-  static constexpr size_t bytes = (size_t)(CT_HALO * AS + 9 * BN * AS) * 2;
+  static constexpr int AS = CIN + 8, BN = NT * 8;   // AS: FP32 halo stride, BF16 weight stride
+  static constexpr size_t bytes = (size_t)CT_HALO * AS * 4 + (size_t)9 * BN * AS * 2;
 };
 
 template <int CIN, int NT>   // BN = NT * 8 output channels per block
@@ -93,12 +99,13 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv3x3(const float* __restric
                                                           int W, int Cout,
                                                           const __nv_bfloat16* __restrict__ WT,
                                                           const float* __restrict__ bias,
-                                                          float* __restrict__ Y, int relu) {
+                                                          float* __restrict__ Y, int relu,
+                                                          float* __restrict__ Yp) {
   using S = ConvSmem<CIN, NT>;
   constexpr int AS = S::AS, BN = S::BN;
   extern __shared__ __align__(16) unsigned char conv_sm[];
-  __nv_bfloat16* As = reinterpret_cast<__nv_bfloat16*>(conv_sm);
-  __nv_bfloat16* Bs = As + CT_HALO * AS;     // [tap][BN][AS]
+  float* As = reinterpret_cast<float*>(conv_sm);                              // [px][AS] FP32
+  __nv_bfloat16* Bs = reinterpret_cast<__nv_bfloat16*>(As + CT_HALO * AS);   // [tap][BN][AS]
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int g = lane >> 2, tg = lane & 3;
   const int tilesW = (W + CT - 1) / CT, tilesH = (H + CT - 1) / CT;
@@ -117,20 +124,17 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv3x3(const float* __restric
     }
     cp_async_commit();
   }
-  {  // the halo tile, FP32 -> BF16
+  {  // the halo tile, FP32, zeros outside the image
     constexpr int C4 = CIN / 4;
     for (int e = tid; e < CT_HALO * C4; e += CONV_THREADS) {
       const int px = e / C4, q = e - px * C4;
       const int hy = px / (CT + 2), hx = px - hy * (CT + 2);
       const int gh = h0 - 1 + hy, gw = w0 - 1 + hx;
-      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (gh >= 0 && gh < H && gw >= 0 && gw < W)
-        v = *reinterpret_cast<const float4*>(X + (((long)n * H + gh) * W + gw) * CIN + q * 4);
-      uint2 pk;
-      pk.x = pack_bf16x2(v.x, v.y);
-      pk.y = pack_bf16x2(v.z, v.w);
-      *reinterpret_cast<uint2*>(As + px * AS + q * 4) = pk;
+      const bool in = gh >= 0 && gh < H && gw >= 0 && gw < W;
+      const float* src = in ? X + (((long)n * H + gh) * W + gw) * CIN + q * 4 : X;
+      cp_async16z(As + px * AS + q * 4, src, in ? 16 : 0);
     }
+    cp_async_commit();
   }
   cp_async_wait<0>();
   __syncthreads();
@@ -141,16 +145,20 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv3x3(const float* __restric
 #pragma unroll 1
   for (int tap = 0; tap < 9; ++tap) {
     const int dy = tap / 3, dx = tap % 3;   // halo offsets (tap - centre + 1)
-    const __nv_bfloat16* a0p = As + ((ty0 + dy) * (CT + 2) + g + dx) * AS + tg * 2;
-    const __nv_bfloat16* a1p = a0p + (CT + 2) * AS;
+    const float* a0p = As + ((ty0 + dy) * (CT + 2) + g + dx) * AS + tg * 2;
+    const float* a1p = a0p + (CT + 2) * AS;
     const __nv_bfloat16* Bt = Bs + tap * BN * AS;
 #pragma unroll
     for (int ks = 0; ks < CIN / 16; ++ks) {
       uint32_t a[4];
-      a[0] = *reinterpret_cast<const uint32_t*>(a0p + ks * 16);
-      a[1] = *reinterpret_cast<const uint32_t*>(a1p + ks * 16);
-      a[2] = *reinterpret_cast<const uint32_t*>(a0p + ks * 16 + 8);
-      a[3] = *reinterpret_cast<const uint32_t*>(a1p + ks * 16 + 8);
+      const float2 f0 = *reinterpret_cast<const float2*>(a0p + ks * 16);
+      const float2 f1 = *reinterpret_cast<const float2*>(a1p + ks * 16);
+      const float2 f2 = *reinterpret_cast<const float2*>(a0p + ks * 16 + 8);
+      const float2 f3 = *reinterpret_cast<const float2*>(a1p + ks * 16 + 8);
+      a[0] = pack_bf16x2(f0.x, f0.y);
+      a[1] = pack_bf16x2(f1.x, f1.y);
+      a[2] = pack_bf16x2(f2.x, f2.y);
+      a[3] = pack_bf16x2(f3.x, f3.y);
 #pragma unroll
       for (int q = 0; q < NT; ++q) {
         const __nv_bfloat16* bp = Bt + (q * 8 + g) * AS + ks * 16 + tg * 2;
@@ -161,33 +169,53 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv3x3(const float* __restric
       }
     }
   }
-  // epilogue: bias, ReLU, store
+  // epilogue: bias, ReLU, store; with Yp also the 2x2 average pool of the
+  // output (the warp holds both rows of a pooling window; the column
+  // neighbour is 4 lanes up), summed in the order s00 + s10 + s01 + s11 of the
+  // oracle's pool2
+  const int gw = w0 + g;
 #pragma unroll
   for (int q = 0; q < NT; ++q) {
     const int col = co0 + q * 8 + tg * 2;
     const float b0 = bias ? bias[col] : 0.f, b1 = bias ? bias[col + 1] : 0.f;
+    float y[2][2];
 #pragma unroll
     for (int half = 0; half < 2; ++half) {
-      const int gh = h0 + ty0 + half, gw = w0 + g;
-      if (gh >= H || gw >= W) continue;
-      float y0 = acc[q][half * 2] + b0, y1 = acc[q][half * 2 + 1] + b1;
+      y[half][0] = acc[q][half * 2] + b0;
+      y[half][1] = acc[q][half * 2 + 1] + b1;
       if (relu) {
-        y0 = fmaxf(y0, 0.f);
-        y1 = fmaxf(y1, 0.f);
+        y[half][0] = fmaxf(y[half][0], 0.f);
+        y[half][1] = fmaxf(y[half][1], 0.f);
       }
-      *reinterpret_cast<float2*>(&Y[(((long)n * H + gh) * W + gw) * Cout + col]) =
-          make_float2(y0, y1);
+      const int gh = h0 + ty0 + half;
+      if (gh < H && gw < W)
+        *reinterpret_cast<float2*>(&Y[(((long)n * H + gh) * W + gw) * Cout + col]) =
+            make_float2(y[half][0], y[half][1]);
+    }
+    if (Yp) {
+      float pv[2];
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        const float s01 = __shfl_down_sync(0xffffffffu, y[0][c], 4);
+        const float s11 = __shfl_down_sync(0xffffffffu, y[1][c], 4);
+        pv[c] = 0.25f * (((y[0][c] + y[1][c]) + s01) + s11);
+      }
+      const int ph = (h0 + ty0) >> 1, pw = gw >> 1;
+      if (!(g & 1) && h0 + ty0 + 1 < H && gw + 1 < W)
+        *reinterpret_cast<float2*>(&Yp[(((long)n * (H / 2) + ph) * (W / 2) + pw) * Cout + col]) =
+            make_float2(pv[0], pv[1]);
     }
   }
 }
 
 template <int CIN, int NT>
 static void conv_launch(const float* X, int N, int H, int W, int Cout, const __nv_bfloat16* WT,
-                        const float* bias, float* Y, int relu, cudaStream_t st) {
+                        const float* bias, float* Y, int relu, float* Yp, cudaStream_t st) {
   using S = ConvSmem<CIN, NT>;
   const int tiles = ((W + CT - 1) / CT) * ((H + CT - 1) / CT) * N;
   dim3 grid(tiles, Cout / S::BN);
-  k_conv3x3<CIN, NT><<<grid, CONV_THREADS, S::bytes, st>>>(X, N, H, W, Cout, WT, bias, Y, relu);
+  k_conv3x3<CIN, NT><<<grid, CONV_THREADS, S::bytes, st>>>(X, N, H, W, Cout, WT, bias, Y, relu,
+                                                            Yp);
 }
 
 template <int CIN, int NT>
@@ -209,26 +237,27 @@ static void conv_attrs() {
 
 template <int CIN>
 static int conv_cin(const float* X, int N, int H, int W, int Cout, const __nv_bfloat16* WT,
-                    const float* bias, float* Y, int relu, cudaStream_t st) {
+                    const float* bias, float* Y, int relu, float* Yp, cudaStream_t st) {
   switch (Cout) {
-    case 16: conv_launch<CIN, 2>(X, N, H, W, Cout, WT, bias, Y, relu, st); break;
+    case 16: conv_launch<CIN, 2>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, st); break;
     case 32:
     case 64:
-    case 128: conv_launch<CIN, 4>(X, N, H, W, Cout, WT, bias, Y, relu, st); break;
+    case 128: conv_launch<CIN, 4>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, st); break;
     default: return AJ_ERR_PARAM;
   }
   return AJ_OK;
 }
 
-// Y = conv(X, WT) (+ bias, ReLU); WT[tap][Cout][Cin] BF16
+// Y = conv(X, WT) (+ bias, ReLU); WT[tap][Cout][Cin] BF16; Yp (nullable,
+// H and W even) receives the 2x2 average pool of Y
 static int conv3x3(const float* X, int N, int H, int W, int Cin, int Cout,
                    const __nv_bfloat16* WT, const float* bias, float* Y, int relu,
-                   cudaStream_t st) {
+                   cudaStream_t st, float* Yp = nullptr) {
   switch (Cin) {
-    case 16: return conv_cin<16>(X, N, H, W, Cout, WT, bias, Y, relu, st);
-    case 32: return conv_cin<32>(X, N, H, W, Cout, WT, bias, Y, relu, st);
-    case 64: return conv_cin<64>(X, N, H, W, Cout, WT, bias, Y, relu, st);
-    case 128: return conv_cin<128>(X, N, H, W, Cout, WT, bias, Y, relu, st);
+    case 16: return conv_cin<16>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, st);
+    case 32: return conv_cin<32>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, st);
+    case 64: return conv_cin<64>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, st);
+    case 128: return conv_cin<128>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, st);
     default: return AJ_ERR_PARAM;
   }
 }
@@ -327,22 +356,6 @@ __global__ void k_bias_grad(const float* __restrict__ dZ, long P, int C, float* 
 }
 
 // ---------------------------------------------------------------- element-wise
-__global__ void k_pool2(const float* __restrict__ X, float* __restrict__ Y, int N, int H, int W,
-                        int C) {   // H, W of the output
-  long e = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  const long T = (long)N * H * W * C;
-  if (e >= T) return;
-  const int c = (int)(e % C);
-  long q = e / C;
-  const int w = (int)(q % W);
-  q /= W;
-  const int h = (int)(q % H);
-  const int n = (int)(q / H);
-  const int W2 = 2 * W;
-  const long b = (((long)n * 2 * H + 2 * h) * W2 + 2 * w) * C + c;
-  Y[e] = 0.25f * (X[b] + X[b + (long)W2 * C] + X[b + C] + X[b + (long)W2 * C + C]);
-}
-
 // dX (fine, accumulated) += pool2 adjoint of dY (coarse)
 __global__ void k_pool2_bwd(const float* __restrict__ dY, float* __restrict__ dX, int N, int H,
                             int W, int C) {   // H, W of dY
@@ -532,20 +545,17 @@ static inline unsigned ew_blocks(long T) { return cdiv(T, 256); }
 
 int nn_forward(int n, int h, int w, const NnW& W, const NnActs& A, cudaStream_t st) {
   const int H0 = h, W0 = w, H1 = h / 2, W1 = w / 2, H2 = h / 4, W2 = w / 4, H3 = h / 8, W3 = w / 8;
-  auto conv = [&](int l, const float* in, float* out, int H, int Wd) {
+  auto conv = [&](int l, const float* in, float* out, int H, int Wd, float* pooled = nullptr) {
     return conv3x3(in, n, H, Wd, kLayers[l].cin, kLayers[l].cout, W.wf(l), W.bias(l), out,
-                   kLayers[l].relu, st);
+                   kLayers[l].relu, st, pooled);
   };
   int rc = AJ_OK;
   rc |= conv(E0A, A.x, A.a0, H0, W0);
-  rc |= conv(E0B, A.a0, A.s0, H0, W0);
-  k_pool2<<<ew_blocks((long)n * H1 * W1 * 32), 256, 0, st>>>(A.s0, A.p0, n, H1, W1, 32);
+  rc |= conv(E0B, A.a0, A.s0, H0, W0, A.p0);     // s0 and its pool p0
   rc |= conv(E1A, A.p0, A.a1, H1, W1);
-  rc |= conv(E1B, A.a1, A.s1, H1, W1);
-  k_pool2<<<ew_blocks((long)n * H2 * W2 * 64), 256, 0, st>>>(A.s1, A.p1, n, H2, W2, 64);
+  rc |= conv(E1B, A.a1, A.s1, H1, W1, A.p1);
   rc |= conv(E2A, A.p1, A.a2, H2, W2);
-  rc |= conv(E2B, A.a2, A.s2, H2, W2);
-  k_pool2<<<ew_blocks((long)n * H3 * W3 * 128), 256, 0, st>>>(A.s2, A.p2, n, H3, W3, 128);
+  rc |= conv(E2B, A.a2, A.s2, H2, W2, A.p2);
   rc |= conv(E3A, A.p2, A.a3, H3, W3);
   rc |= conv(E3B, A.a3, A.bt, H3, W3);
   k_up2_add<<<ew_blocks((long)n * H2 * W2 * 128), 256, 0, st>>>(A.bt, A.s2, A.u2, n, H2, W2, 128);
@@ -619,62 +629,91 @@ static bool nn_shape_ok(int n, int h, int w) { return n >= 1 && h >= 8 && w >= 8
 //   channel 1: F x F average of the mask
 //   channel 2: F x F average of p_prev
 // channels 3..15 are zero.  Also the FP64 sums of channel 0^2 and 2^2.
+// one thread per fine cell: the F x F window sums reduce across F lanes with
+// shuffles and across F rows through shared memory (F in {2, 4, 8}; a
+// 32 x 8 block holds whole windows)
 __global__ void __launch_bounds__(256) k_nn_feat(const float* __restrict__ b,
                                                  const float* __restrict__ mask,
                                                  const float* __restrict__ pp, int nx, int ny,
-                                                 int F, float ax, float ay, float* __restrict__ x,
-                                                 DevScalars* sc) {
-  const int J = blockIdx.x * blockDim.x + threadIdx.x;
-  const int I = blockIdx.y * blockDim.y + threadIdx.y;
-  const int h = nx / F, w = ny / F;
-  float sr = 0.f, sp = 0.f;
-  if (I < h && J < w) {
+                                                 int F, float ax, float ay, float* __restrict__ x) {
+  __shared__ float red[3][8][32];
+  const int lane = threadIdx.x, row = threadIdx.y;
+  const int j = blockIdx.x * 32 + lane, i = blockIdx.y * 8 + row;
+  float vr = 0.f, vm = 0.f, vp = 0.f;
+  if (i < nx && j < ny) {
+    const long k = (long)i * ny + j;
+    const float c = pp[k];
+    if (i != nx - 1) {
+      const float xp = pp[k + ny];
+      const float xm = i > 0 ? pp[k - ny] : c;
+      const float yp = j + 1 < ny ? pp[k + 1] : c;
+      const float ym = j > 0 ? pp[k - 1] : c;
+      vr = b[k] - (ax * ((xp - c) + (xm - c)) + ay * ((yp - c) + (ym - c)));
+    }
+    vm = mask[k];
+    vp = c;
+  }
+  for (int o = 1; o < F; o <<= 1) {
+    vr += __shfl_xor_sync(0xffffffffu, vr, o);
+    vm += __shfl_xor_sync(0xffffffffu, vm, o);
+    vp += __shfl_xor_sync(0xffffffffu, vp, o);
+  }
+  red[0][row][lane] = vr;
+  red[1][row][lane] = vm;
+  red[2][row][lane] = vp;
+  __syncthreads();
+  if ((row % F) == 0 && (lane % F) == 0 && i < nx && j < ny) {
     float ar = 0.f, am = 0.f, ap = 0.f;
-    for (int di = 0; di < F; ++di) {
-      const int i = I * F + di;
-      for (int dj = 0; dj < F; ++dj) {
-        const int j = J * F + dj;
-        const long k = (long)i * ny + j;
-        const float c = pp[k];
-        float r = 0.f;
-        if (i != nx - 1) {
-          const float xp = pp[k + ny];
-          const float xm = i > 0 ? pp[k - ny] : c;
-          const float yp = j + 1 < ny ? pp[k + 1] : c;
-          const float ym = j > 0 ? pp[k - 1] : c;
-          r = b[k] - (ax * ((xp - c) + (xm - c)) + ay * ((yp - c) + (ym - c)));
-        }
-        ar += r;
-        am += mask[k];
-        ap += c;
-      }
+    for (int q = 0; q < F; ++q) {
+      ar += red[0][row + q][lane];
+      am += red[1][row + q][lane];
+      ap += red[2][row + q][lane];
     }
     const float inv = 1.f / (float)(F * F);
     ar *= inv;
     am *= inv;
     ap *= inv;
-    float* o = x + ((long)I * w + J) * 16;
+    const int w = ny / F;
+    float* o = x + ((long)(i / F) * w + j / F) * 16;
     o[0] = ar;
     o[1] = am;
     o[2] = ap;
 #pragma unroll
     for (int c = 3; c < 16; ++c) o[c] = 0.f;
-    sr = ar * ar;
-    sp = ap * ap;
   }
-  block_sum_atomic((double)sr, &sc->acc[2]);
-  block_sum_atomic((double)sp, &sc->acc[3]);
 }
 
-// per-sample scales: channel RMS values and the output scale
-// rms_r * lmin^2 / 10 (a correction solving A dp = r has that magnitude)
-__global__ void k_nn_scale(DevScalars* sc, long cells, double lmin2) {
-  const double rr = sqrt(sc->acc[2] / (double)cells), rp = sqrt(sc->acc[3] / (double)cells);
-  sc->nn_rms_r = rr > 1e-30 ? rr : 1e-30;
-  sc->nn_rms_p = rp > 1e-30 ? rp : 1e-30;
-  sc->nn_out_scale = sc->nn_rms_r * lmin2 / 10.0;
-  sc->acc[2] = 0.0;
-  sc->acc[3] = 0.0;
+// per-sample scales (one block): RMS of channels 0 and 2 over the network
+// grid (FP64 sums) and the output scale rms_r * lmin^2 / 10 (a correction
+// solving A dp = r has that magnitude)
+__global__ void __launch_bounds__(1024) k_nn_scale(const float* __restrict__ x, long cells,
+                                                   DevScalars* sc, double lmin2) {
+  double sr = 0.0, sp = 0.0;
+  for (long c = threadIdx.x; c < cells; c += blockDim.x) {
+    const float r = x[c * 16], q = x[c * 16 + 2];
+    sr += (double)r * r;
+    sp += (double)q * q;
+  }
+  __shared__ double red[2][32];
+  sr = warp_sum(sr);
+  sp = warp_sum(sp);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) {
+    red[0][w] = sr;
+    red[1][w] = sp;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+      a += red[0][k];
+      b += red[1][k];
+    }
+    const double rr = sqrt(a / (double)cells), rp = sqrt(b / (double)cells);
+    sc->nn_rms_r = rr > 1e-30 ? rr : 1e-30;
+    sc->nn_rms_p = rp > 1e-30 ? rp : 1e-30;
+    sc->nn_out_scale = sc->nn_rms_r * lmin2 / 10.0;
+  }
 }
 
 // normalise channels 0 and 2 in place; optionally copy the 3 features out
@@ -754,10 +793,11 @@ int nn_features(const AjStepParams& p, void* ws, const float* b, const float* ma
   const int F = p.nn_factor, h = p.nx / F, w = p.ny / F;
   DevScalars* sc = at<DevScalars>(ws, 0);
   dim3 blk(32, 8), grd(cdiv(w, 32), cdiv(h, 8));
-  k_nn_feat<<<grd, blk, 0, st>>>(b, mask, pp, p.nx, p.ny, F, (float)(1.0 / (p.dx * p.dx)),
-                                 (float)(1.0 / (p.dy * p.dy)), x16, sc);
+  k_nn_feat<<<dim3(cdiv(p.ny, 32), cdiv(p.nx, 8)), blk, 0, st>>>(
+      b, mask, pp, p.nx, p.ny, F, (float)(1.0 / (p.dx * p.dx)), (float)(1.0 / (p.dy * p.dy)),
+      x16);
   const double lx = p.nx * p.dx, ly = p.ny * p.dy, lmin = lx < ly ? lx : ly;
-  k_nn_scale<<<1, 1, 0, st>>>(sc, (long)h * w, lmin * lmin);
+  k_nn_scale<<<1, 1024, 0, st>>>(x16, (long)h * w, sc, lmin * lmin);
   k_nn_norm<<<cdiv((long)h * w, 256), 256, 0, st>>>(x16, x3, (long)h * w, sc);
   if (pt && target) k_nn_target<<<grd, blk, 0, st>>>(pt, pp, p.nx, p.ny, F, target, sc);
   return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
@@ -789,6 +829,7 @@ size_t nn_step_act_bytes(const AjStepParams& p) {
 bool nn_step_shape_ok(const AjStepParams& p) {
   const int F = p.nn_factor;
   if (F <= 0) return true;
+  if (F != 2 && F != 4 && F != 8) return false;   // whole windows in a 32 x 8 block
   if (p.nx % F || p.ny % F) return false;
   return nn_shape_ok(1, p.nx / F, p.ny / F);
 }

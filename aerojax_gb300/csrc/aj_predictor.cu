@@ -596,7 +596,8 @@ __device__ float rhs_mac_u(const RkMac& a, int i, int j) {
   float uxm = uw_at(a, a.uin, i > 0 ? i - 1 : 0, j);
   float uxp = uw_at(a, a.uin, i < nx ? i + 1 : nx, j);
   float back = (uw - uxm) * a.idx, fwd = (uxp - uw) * a.idx;
-  float al = 0.5f * (1.f + tanhf(uw / 0.05f));
+  // upwind blend 0.5 (1 + tanh(u / 0.05)) of rk3_mac.py, the argument formed as 20 u
+  float al = 0.5f * (1.f + tanhf(uw * 20.f));
   float adv_x = uw * (al * back + (1.f - al) * fwd);
   float du_dy;
   if (j == 0) du_dy = (uw_at(a, a.uin, i, 1) - uw) * a.idy;
@@ -622,7 +623,7 @@ __device__ float rhs_mac_v(const RkMac& a, int i, int j) {
   float vym = vw_at(a, a.vin, i, j > 0 ? j - 1 : 0);
   float vyp = vw_at(a, a.vin, i, j < ny ? j + 1 : ny);
   float back = (vw - vym) * a.idy, fwd = (vyp - vw) * a.idy;
-  float al = 0.5f * (1.f + tanhf(vw / 0.05f));
+  float al = 0.5f * (1.f + tanhf(vw * 20.f));
   float adv_y = vw * (al * back + (1.f - al) * fwd);
   float dv_dx;
   if (i == 0) dv_dx = (vw_at(a, a.vin, 1, j) - vw) * a.idx;
@@ -692,7 +693,7 @@ __device__ __forceinline__ float stage_mac_u_int(const RkMac& a, int i, int j, f
   const float vc_m = 0.5f * (ldg(v - nyv + 1) + ldg(v - nyv));
   const float v_at_u = 0.5f * (vc_i + vc_m);
   const float back = (uw - uxm) * a.idx, fwd = (uxp - uw) * a.idx;
-  const float al = 0.5f * (1.f + tanhf(uw / 0.05f));
+  const float al = 0.5f * (1.f + tanhf(uw * 20.f));
   const float adv_x = uw * (al * back + (1.f - al) * fwd);
   const float du_dy = (uyp - uym) * (0.5f * a.idy);
   const float m_i = ldg(a.mask + k), m_im = ldg(a.mask + k - ny);
@@ -726,7 +727,7 @@ __device__ __forceinline__ float stage_mac_v_int(const RkMac& a, int i, int j, f
   const float uc_m = 0.5f * (ldg(u + ny - 1) + ldg(u - 1));
   const float u_at_v = 0.5f * (uc_j + uc_m);
   const float back = (vw - vym) * a.idy, fwd = (vyp - vw) * a.idy;
-  const float al = 0.5f * (1.f + tanhf(vw / 0.05f));
+  const float al = 0.5f * (1.f + tanhf(vw * 20.f));
   const float adv_y = vw * (al * back + (1.f - al) * fwd);
   const float dv_dx = (vxp - vxm) * (0.5f * a.idx);
   const long c = (long)i * ny + j;

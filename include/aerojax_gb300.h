@@ -82,7 +82,8 @@ typedef struct {
   int32_t has_sdf;               /* collocated: chi from sdf (rk3_simple_new.py:194)  */
   int32_t cfl_dt;                /* 1 = dt from the CFL rule on the device each step  */
   int32_t warm_start;            /* converging mode initial guess: AJ_WARM_*          */
-  int32_t nn_factor;             /* learned warm start: network grid is nx/F x ny/F
+  int32_t nn_factor;             /* learned warm start: network grid is nx/F x ny/F,
+                                    F in {2, 4, 8}, both multiples of 8
                                     (0 = off; aj_step_nn only)                        */
   double dx, dy;
   double dt;                     /* used when cfl_dt == 0                             */
