@@ -11,6 +11,7 @@
 #include <mutex>
 #include <string>
 #include <unordered_map>
+#include <vector>
 #include <string.h>
 #include <stdlib.h>
 
@@ -193,10 +194,32 @@ constexpr size_t kMaxGraphs = 64;
 
 std::string make_key(int kind, const AjStepParams& p, std::initializer_list<const void*> ptrs) {
   std::string k;
+  const int tv = tile_variant(p.nx, p.ny);   // the autotuned level-0 tiles are baked in
   k.append(reinterpret_cast<const char*>(&kind), sizeof(kind));
+  k.append(reinterpret_cast<const char*>(&tv), sizeof(tv));
   k.append(reinterpret_cast<const char*>(&p), sizeof(p));
   for (const void* q : ptrs) k.append(reinterpret_cast<const char*>(&q), sizeof(q));
   return k;
+}
+
+// branch streams and fork/join events of the ensemble capture (created once)
+cudaStream_t* ensemble_streams(int n) {
+  static std::vector<cudaStream_t> v;
+  while ((int)v.size() < n) {
+    cudaStream_t s;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return nullptr;
+    v.push_back(s);
+  }
+  return v.data();
+}
+cudaEvent_t* ensemble_events(int n) {
+  static std::vector<cudaEvent_t> v;
+  while ((int)v.size() < n) {
+    cudaEvent_t e;
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return nullptr;
+    v.push_back(e);
+  }
+  return v.data();
 }
 
 template <typename F>
@@ -488,6 +511,66 @@ int32_t aj_kernel_count(const AjStepParams* prm, int32_t cycles) {
   n += 1;                                                       // correction
   if (p.nn_factor > 0) n += 3 + 15 + 1;                         // features, network, correction
   return n;
+}
+
+int32_t aj_autotune(const AjStepParams* prm, void* ws, size_t bytes, int32_t reps,
+                    float* times_ms, int32_t* chosen, void* stream) {
+  if (!prm) return AJ_ERR_PARAM;
+  AjStepParams p = normalise(*prm);
+  int rc = check_params(p);
+  if (rc != AJ_OK) return rc;
+  if (p.mg_mode != AJ_MG_CONVERGE) return AJ_ERR_PARAM;
+  Layout L;
+  make_layout(p, L);
+  if ((rc = ws_ok(L, ws, bytes)) != AJ_OK) return rc;
+  int ch = 0;
+  rc = converge_autotune(p, L, ws, reps > 0 ? reps : 10, times_ms, &ch, (cudaStream_t)stream);
+  if (chosen) *chosen = ch;
+  return rc;
+}
+
+int32_t aj_ensemble_step(int32_t n, const AjStepParams* prms, const float* const* u,
+                         const float* const* v, const float* const* mask,
+                         const float* const* p_guess, float* const* u_out, float* const* v_out,
+                         float* const* p_out, void* const* ws, const size_t* ws_bytes,
+                         AjStats* stats, void* stream) {
+  if (n < 1 || n > AJ_ENSEMBLE_MAX || !prms || !u || !v || !mask || !u_out || !v_out || !p_out ||
+      !ws || !ws_bytes)
+    return AJ_ERR_PARAM;
+  std::vector<AjStepParams> P(n);
+  std::vector<Layout> Ls(n);
+  std::string key;
+  for (int i = 0; i < n; ++i) {
+    int rc = aj_check_params(&prms[i]);
+    if (rc != AJ_OK) return rc;
+    P[i] = normalise(prms[i]);
+    if (P[i].warm_start == AJ_WARM_GUESS && !(p_guess && p_guess[i])) return AJ_ERR_PARAM;
+    if (!u[i] || !v[i] || !mask[i] || !u_out[i] || !v_out[i] || !p_out[i]) return AJ_ERR_PARAM;
+    make_layout(P[i], Ls[i]);
+    if ((rc = ws_ok(Ls[i], ws[i], ws_bytes[i])) != AJ_OK) return rc;
+    const float* pg = (P[i].warm_start && p_guess) ? p_guess[i] : nullptr;
+    key += make_key(4, P[i], {ws[i], u[i], v[i], mask[i], pg, u_out[i], v_out[i], p_out[i],
+                              stats ? (const void*)(stats + i) : nullptr});
+  }
+  // one graph: the instances are independent branches forked from the
+  // capturing stream and joined back, so they run concurrently
+  return run_captured(key, (cudaStream_t)stream, [&](cudaStream_t s) {
+    cudaStream_t* br = ensemble_streams(n);
+    cudaEvent_t* ev = ensemble_events(n + 1);
+    if (!br || !ev) return (int)AJ_ERR_CUDA;
+    if (cudaEventRecord(ev[n], s) != cudaSuccess) return (int)AJ_ERR_CUDA;
+    for (int i = 0; i < n; ++i) {
+      if (cudaStreamWaitEvent(br[i], ev[n], 0) != cudaSuccess) return (int)AJ_ERR_CUDA;
+      const float* pg = (P[i].warm_start && p_guess) ? p_guess[i] : nullptr;
+      int rc = enqueue_step(P[i], Ls[i], ws[i], u[i], v[i], mask[i], pg, u_out[i], v_out[i],
+                            p_out[i], stats ? stats + i : nullptr, br[i]);
+      if (rc != AJ_OK) return rc;
+      if (cudaEventRecord(ev[i], br[i]) != cudaSuccess) return (int)AJ_ERR_CUDA;
+    }
+    for (int i = 0; i < n; ++i)
+      if (cudaStreamWaitEvent(s, ev[i], 0) != cudaSuccess) return (int)AJ_ERR_CUDA;
+    return (int)AJ_OK;
+  });
 }
 
 int32_t aj_release_graphs(void) {

@@ -32,6 +32,9 @@
 #include "aj_internal.cuh"
 #include <math.h>
 #include <string.h>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <vector>
 
 namespace aj {
@@ -139,8 +142,11 @@ struct TileCfg {
   static_assert(TI % 2 == 0 && TJ % 2 == 0, "tile interiors must align with the coarse grid");
   static_assert(NTH % PAIRS == 0, "threads must fill whole rows of column pairs");
 };
-using T0 = TileCfg<48, 64, 256>;   // level 0: 38 x 54 interior
+using T0 = TileCfg<48, 64, 256>;   // level 0: 38 x 54 interior (default)
+using T0b = TileCfg<32, 64, 256>;  // level 0: 22 x 54 interior (more, shorter tiles)
+using T0c = TileCfg<64, 32, 256>;  // level 0: 54 x 22 interior (narrow tiles)
 using T1 = TileCfg<32, 32, 256>;   // coarser levels: 22 x 22 interior
+constexpr int CV_TILE_VARIANTS = 3;
 
 __device__ __forceinline__ float cv_diag(const CvLvl& L, int gi, int gj) {
   float d = -2.f * (L.ax + L.ay);
@@ -359,11 +365,11 @@ struct PState {
 // level 0: e + P(e_coarse), post-smoothing, p += e (double-FP32, ping-pong), the
 // residual of the reference operator for the next iteration (double-FP32), its
 // FP64 norm, and the convergence test in the last block to finish
-__global__ void __launch_bounds__(T0::NTH) k_cv_up0(
+template <class TC>
+__global__ void __launch_bounds__(TC::NTH) k_cv_up0(
     CvLvl L, const float* __restrict__ r, const float* __restrict__ e_in,
     const float* __restrict__ ec, int nc, int mc, float gc, PState ps, const float* __restrict__ b,
     float* __restrict__ r_next, DevScalars* sc, DfCoef co, CvCheck ck, int profile) {
-  using TC = T0;
   constexpr int TI = TC::TI, TJ = TC::TJ, SJ = TC::SJ;
   constexpr int PI = TI + 2, PJ = TJ + 2;
   static_assert(PJ <= 2 * TC::PAIRS, "the pressure window must fit two column runs");
@@ -1004,6 +1010,34 @@ static dim3 tile_threads() {
   return dim3(TC::PAIRS, TC::RG);
 }
 
+// level-0 kernels of tile variant v (chosen per grid shape by the autotuner)
+template <class TC>
+static void level0_down(const CvLvl& c, const Layout& L, void* ws, const int* done,
+                        cudaStream_t st) {
+  k_cv_down<TC><<<tiles<TC>(c), tile_threads<TC>(), 0, st>>>(
+      c, at<float>(ws, L.B[0]), at<float>(ws, L.X[0]), at<float>(ws, L.B[1]), done);
+}
+template <class TC>
+static void level0_up(const AjStepParams& p, const CvLvl& c, const Layout& L, void* ws,
+                      DevScalars* sc, const CvCheck& ck, int profile, cudaStream_t st) {
+  k_cv_up0<TC><<<tiles<TC>(c), tile_threads<TC>(), 0, st>>>(
+      c, at<float>(ws, L.B[0]), at<float>(ws, L.X[0]), at<float>(ws, L.T[1]), L.ln[1], L.lm[1],
+      (float)ghost_factor(1), pstate(L, ws), at<float>(ws, L.b0), at<float>(ws, L.B[0]), sc,
+      df_coef(1.0 / (p.dx * p.dx), 1.0 / (p.dy * p.dy)), ck, profile);
+}
+static void level0_down_v(int v, const CvLvl& c, const Layout& L, void* ws, const int* done,
+                          cudaStream_t st) {
+  if (v == 1) level0_down<T0b>(c, L, ws, done, st);
+  else if (v == 2) level0_down<T0c>(c, L, ws, done, st);
+  else level0_down<T0>(c, L, ws, done, st);
+}
+static void level0_up_v(int v, const AjStepParams& p, const CvLvl& c, const Layout& L, void* ws,
+                        DevScalars* sc, const CvCheck& ck, int profile, cudaStream_t st) {
+  if (v == 1) level0_up<T0b>(p, c, L, ws, sc, ck, profile, st);
+  else if (v == 2) level0_up<T0c>(p, c, L, ws, sc, ck, profile, st);
+  else level0_up<T0>(p, c, L, ws, sc, ck, profile, st);
+}
+
 // one refinement iteration
 static void cv_body(const AjStepParams& p, const Layout& L, void* ws,
                     cudaGraphConditionalHandle h, int use_handle, cudaStream_t st) {
@@ -1013,8 +1047,7 @@ static void cv_body(const AjStepParams& p, const Layout& L, void* ws,
   for (int l = 0; l < lc; ++l) {
     CvLvl c = cv_level(p, L, l);
     if (l == 0)
-      k_cv_down<T0><<<tiles<T0>(c), tile_threads<T0>(), 0, st>>>(
-          c, at<float>(ws, L.B[l]), at<float>(ws, L.X[l]), at<float>(ws, L.B[l + 1]), done);
+      level0_down_v(tile_variant(p.nx, p.ny), c, L, ws, done, st);
     else
       k_cv_down<T1><<<tiles<T1>(c), tile_threads<T1>(), 0, st>>>(
           c, at<float>(ws, L.B[l]), at<float>(ws, L.X[l]), at<float>(ws, L.B[l + 1]), done);
@@ -1032,10 +1065,7 @@ static void cv_body(const AjStepParams& p, const Layout& L, void* ws,
   }
   CvLvl c0 = cv_level(p, L, 0);
   CvCheck ck{p.mg_rtol, p.max_cycles, use_handle, h};
-  k_cv_up0<<<tiles<T0>(c0), tile_threads<T0>(), 0, st>>>(
-      c0, at<float>(ws, L.B[0]), at<float>(ws, L.X[0]), at<float>(ws, L.T[1]), L.ln[1], L.lm[1],
-      (float)ghost_factor(1), pstate(L, ws), at<float>(ws, L.b0), at<float>(ws, L.B[0]), sc,
-      df_coef(1.0 / (p.dx * p.dx), 1.0 / (p.dy * p.dy)), ck, 0);
+  level0_up_v(tile_variant(p.nx, p.ny), p, c0, L, ws, sc, ck, 0, st);
 }
 
 static cudaStream_t side_stream() {
@@ -1208,16 +1238,13 @@ int profile_pressure_kernel(const AjStepParams& p, const Layout& L, void* ws, in
   DevScalars* sc = at<DevScalars>(ws, 0);
   const int* never = reinterpret_cast<const int*>(&sc->pad_[0]);   // always 0
   CvLvl c = cv_level(p, L, 0);
+  const int v = tile_variant(p.nx, p.ny);
   if (which == 0) {
-    k_cv_down<T0><<<tiles<T0>(c), tile_threads<T0>(), 0, st>>>(
-        c, at<float>(ws, L.B[0]), at<float>(ws, L.X[0]), at<float>(ws, L.B[1]), never);
+    level0_down_v(v, c, L, ws, never, st);
   } else if (which == 1) {
     CvCheck ck{p.mg_rtol, p.max_cycles, 0, 0};
     // profile mode reads the current state buffer and writes only the other one
-    k_cv_up0<<<tiles<T0>(c), tile_threads<T0>(), 0, st>>>(
-        c, at<float>(ws, L.B[0]), at<float>(ws, L.X[0]), at<float>(ws, L.T[1]), L.ln[1], L.lm[1],
-        (float)ghost_factor(1), pstate(L, ws), at<float>(ws, L.b0), at<float>(ws, L.B[0]), sc,
-        df_coef(1.0 / (p.dx * p.dx), 1.0 / (p.dy * p.dy)), ck, 1);
+    level0_up_v(v, p, c, L, ws, sc, ck, 1, st);
   } else if (which == 2) {
     if (L.ld > 0) {
       direct_launch(direct_args(p, L, ws, never), st);
@@ -1231,4 +1258,78 @@ int profile_pressure_kernel(const AjStepParams& p, const Layout& L, void* ws, in
   return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
 }
 
+// ---------------------------------------------------------------- autotuner
+// The level-0 tile shape per grid shape.  converge_autotune times every
+// candidate (level-0 pre-smoothing + post-smoothing kernels, profile mode, on
+// a prepared workspace) and keeps the fastest; the choice is cached per
+// (nx, ny, SM count) for the life of the process and is part of every graph
+// key, so graphs captured before and after a tuning never mix.
+namespace {
+std::mutex g_tune_mu;
+std::map<std::tuple<int, int, int>, int> g_tune;
+int sm_count() {
+  static int n = -1;
+  if (n < 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) n = 0;
+  }
+  return n;
+}
+}  // namespace
+
+int tile_variant(int nx, int ny) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  auto it = g_tune.find({nx, ny, sm_count()});
+  return it == g_tune.end() ? 0 : it->second;
+}
+
+int converge_autotune(const AjStepParams& p, const Layout& L, void* ws, int reps, float* times_ms,
+                      int* chosen, cudaStream_t st) {
+  if (p.mg_mode != AJ_MG_CONVERGE) return AJ_ERR_PARAM;
+  DevScalars* sc = at<DevScalars>(ws, 0);
+  const int* never = reinterpret_cast<const int*>(&sc->pad_[0]);   // always 0
+  const CvLvl c = cv_level(p, L, 0);
+  const CvCheck ck{p.mg_rtol, p.max_cycles, 0, 0};
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+    return AJ_ERR_CUDA;
+  int best = 0;
+  float best_ms = 1e30f;
+  for (int v = 0; v < CV_TILE_VARIANTS; ++v) {
+    for (int w = 0; w < 2; ++w) {   // warm-up
+      level0_down_v(v, c, L, ws, never, st);
+      level0_up_v(v, p, c, L, ws, sc, ck, 1, st);
+    }
+    cudaEventRecord(e0, st);
+    for (int r = 0; r < reps; ++r) {
+      level0_down_v(v, c, L, ws, never, st);
+      level0_up_v(v, p, c, L, ws, sc, ck, 1, st);
+    }
+    cudaEventRecord(e1, st);
+    if (cudaEventSynchronize(e1) != cudaSuccess) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      return AJ_ERR_CUDA;
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    ms /= (float)(reps > 0 ? reps : 1);
+    if (times_ms) times_ms[v] = ms;
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = v;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune[{p.nx, p.ny, sm_count()}] = best;
+  }
+  if (chosen) *chosen = best;
+  return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+}
+
 }  // namespace aj
+

@@ -154,6 +154,10 @@ int converge_solve(const AjStepParams& p, const Layout& L, void* ws, const float
 size_t converge_block_smem(const Layout& L, int lc);
 int converge_first_block_level(const Layout& L);
 int converge_direct_level(const Layout& L);
+// level-0 tile shape of a grid (0 until converge_autotune has run for it)
+int tile_variant(int nx, int ny);
+int converge_autotune(const AjStepParams& p, const Layout& L, void* ws, int reps, float* times_ms,
+                      int* chosen, cudaStream_t st);
 // learned warm start (aj_nn.cu)
 size_t nn_step_act_bytes(const AjStepParams& p);
 bool nn_step_shape_ok(const AjStepParams& p);

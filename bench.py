@@ -49,6 +49,10 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="naca", choices=["naca", "ensemble", "tri4096"],
+                    help="naca: the metric's workload (default); ensemble: 64 cylinder "
+                         "channels of uneven sizes in one graph launch; tri4096: the "
+                         "4096x2048 three-cylinder dynamic-LES flow")
     ap.add_argument("--nx", type=int, default=2048)
     ap.add_argument("--ny", type=int, default=512)
     ap.add_argument("--cpu-sample-steps", type=int, default=20)
@@ -197,6 +201,7 @@ def gpu_arm(args):
     mask = case["mask"]
     flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=dev)
 
+    tuned = []
     net = None
     if os.path.exists(NNW.WEIGHTS):
         net = NNW.WarmStartNet.load(NNW.WEIGHTS, device=dev)
@@ -210,6 +215,9 @@ def gpu_arm(args):
         cfg = replace(case["cfg"], warm_start=warm, nn_factor=NN_FACTOR if kind == "nn" else 0)
         plan = aj.get_plan(cfg, dev)
         plan.prepare(mask)
+        if not tuned:                       # the level-0 tile shape of this grid, once
+            from aerojax_gb300.ensemble import autotune
+            tuned.append(autotune(plan))
         bufs = [(case["u"].clone(), case["v"].clone(), torch.zeros((args.nx, args.ny), device=dev))
                 for _ in range(2)]
         return plan, bufs
@@ -376,6 +384,7 @@ def gpu_arm(args):
                        "double-FP32 refinement, FP64 norms)") if head == "nn" else
                       "converging MG warm-started from the double-FP32 extrapolation",
             "rel_residual_target": 1e-6, "arms": arms,
+            "autotuned_level0_tiles": tuned[0] if tuned else None,
             "plain_mg_value": plain_value, "speedup_vs_plain": value / plain_value,
             "l2": "flushed before every step (256 MiB write outside the timed events)",
             "parallelism": "replicas only" if world > 1 else "single GPU",
@@ -433,10 +442,82 @@ def roofline(args, plan, state, mask, flush, L):
             "algorithmic_bytes_per_launch": algo, "launch_us": dur * 1e6}
 
 
+def side_workload(args):
+    """Lines for the ensemble and the 4096x2048 workloads (not the metric's
+    configuration): cell-steps/s of the GPU path, CUDA-event timed."""
+    import torch
+    from dataclasses import replace
+    import aerojax_gb300 as aj
+    from aerojax_gb300.build import build
+    build()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    st = torch.cuda.current_stream()
+    if args.workload == "ensemble":
+        from aerojax_gb300 import ensemble as E
+        ens = E.Ensemble(E.draw_instances(64, seed=0), device=dev)
+        for _ in range(max(3, args.warmup)):
+            ens.step()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(args.steps):
+            ens.step()
+        e1.record(st)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        sts = ens.stats()
+        print(json.dumps({
+            "metric": "aggregate Mcell-steps/s, 64-instance cylinder-channel ensemble",
+            "value": ens.cells / (ms * 1e-3) / 1e6, "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded draws)",
+            "config": {"workload": "ensemble64_cylinders", "cells_per_step": ens.cells,
+                       "instances": 64, "graph_launches_per_step": 1,
+                       "autotuned_tiles": {f"{k[0]}x{k[1]}": v for k, v in ens.tuned.items()},
+                       "mg_cycles_mean": statistics.mean(s["cycles"] for s in sts),
+                       "rel_residual_max": max(s["rel_residual"] for s in sts),
+                       "l2": "working set above the L2 size (no flush)"}}))
+        return
+    from aerojax_gb300 import configs
+    case = configs.tri_cyl_4096x2048(device=dev)
+    out = {}
+    for arm, warm in (("plain", False), ("extrap", "extrapolate")):
+        plan = aj.get_plan(replace(case["cfg"], warm_start=warm), dev)
+        plan.prepare(case["mask"], case["sdf"])
+        u, v = case["u"].clone(), case["v"].clone()
+        p = torch.zeros_like(u)
+        for _ in range(max(3, args.warmup)):
+            u, v, p = aj.run_step(plan, u, v, case["mask"], p_guess=p)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        cyc = []
+        for _ in range(args.steps):
+            u, v, p = aj.run_step(plan, u, v, case["mask"], p_guess=p)
+            cyc.append(plan.stats_buf.clone())
+        e1.record(st)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        from aerojax_gb300 import _lib
+        c = [_lib.AjStats.from_buffer_copy(bytes(x.cpu().numpy().tobytes())).cycles for x in cyc]
+        out[arm] = {"value": 4096 * 2048 / (ms * 1e-3) / 1e6, "ms_per_step": ms,
+                    "mg_cycles_mean": statistics.mean(c)}
+    print(json.dumps({
+        "metric": "Mcell-steps/s, 4096x2048 three-cylinder dynamic-LES step",
+        "value": out["extrap"]["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": out["extrap"]["ms_per_step"],
+        "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": case["name"], "arms": out,
+                   "l2": "working set (~1 GB) above the L2 size (no flush)"}}))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         reference_arm(args)
+    elif args.workload != "naca":
+        side_workload(args)
     else:
         gpu_arm(args)
 

@@ -268,6 +268,32 @@ int32_t aj_kernel_count(const AjStepParams* prm, int32_t cycles);
    Call only while none of them is executing.  No reference counterpart. */
 int32_t aj_release_graphs(void);
 
+/* Autotuner of the converging multigrid's level-0 tile shape for prm's grid
+   (converging mode, after aj_prepare on this workspace): times each
+   candidate `reps` times (level-0 pre- and post-smoothing kernels on the
+   workspace's current contents), keeps the fastest for every later call on
+   this grid shape in this process, and returns the per-candidate times (host
+   array of AJ_TILE_VARIANTS floats, ms, nullable) and the choice (host,
+   nullable).  Synchronises the stream.  No reference counterpart. */
+#define AJ_TILE_VARIANTS 3
+int32_t aj_autotune(const AjStepParams* prm, void* workspace, size_t workspace_bytes,
+                    int32_t reps, float* times_ms, int32_t* chosen, void* stream);
+
+/* Batched ensemble: one step of n independent simulations (each with its own
+   parameters - grid sizes may differ -, fields and prepared workspace) as a
+   single CUDA graph launch whose n branches run concurrently on the GPU.
+   Every array is a host array of n entries; the pointers in them are device
+   pointers (p_guess entries may be NULL where warm_start is not
+   AJ_WARM_GUESS; stats: device array of n AjStats or NULL).  Instance i gets
+   exactly what aj_step would give it.  No reference counterpart (the
+   reference steps one simulation at a time). */
+#define AJ_ENSEMBLE_MAX 256
+int32_t aj_ensemble_step(int32_t n, const AjStepParams* prms, const float* const* u,
+                         const float* const* v, const float* const* mask,
+                         const float* const* p_guess, float* const* u_out, float* const* v_out,
+                         float* const* p_out, void* const* workspaces,
+                         const size_t* workspace_bytes, AjStats* stats, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -109,3 +109,15 @@ def test_float32_oracle_close_to_float64():
     for x, y in zip(a, b):
         assert y.dtype == np.float32
         assert np.max(np.abs(x - y)) / np.max(np.abs(x)) < 1e-4
+
+
+def test_ensemble_draws_follow_the_workload():
+    """The ensemble's instances: sizes from the four grids, diameter 8-32
+    cells, centre at 10-20 % / 40-60 %, Re log-uniform in [100, 1000]."""
+    from aerojax_gb300 import ensemble as E
+    specs = E.draw_instances(256, seed=1)
+    assert {(s.nx, s.ny) for s in specs} == set(E.SIZES)
+    assert all(8 <= s.d_cells <= 32 and 0.1 <= s.cx_frac <= 0.2 and 0.4 <= s.cy_frac <= 0.6
+               and 100 <= s.re <= 1000 for s in specs)
+    logs = np.log([s.re for s in specs])
+    assert abs(logs.mean() - 0.5 * (np.log(100) + np.log(1000))) < 0.15
