@@ -497,7 +497,7 @@ int32_t aj_kernel_count(const AjStepParams* prm, int32_t cycles) {
   const bool mac = p.grid_type == AJ_GRID_MAC;
   int n = 1;                                                    // cfl or set-dt
   if (p.les_model != AJ_LES_NONE && (p.variant == AJ_VARIANT_GUI || mac))
-    n += (mac ? 1 : 0) + (p.les_model == AJ_LES_DYNAMIC ? 4 : 1);
+    n += p.les_model == AJ_LES_DYNAMIC ? (mac ? 1 : 0) + 4 : 1;
   n += p.fast_mode ? 2 : 3;                                     // predictor stages
   n += 1;                                                       // rhs
   if (p.mg_mode == AJ_MG_PARITY) {
@@ -505,11 +505,11 @@ int32_t aj_kernel_count(const AjStepParams* prm, int32_t cycles) {
     n += 1 + p.v_cycles * per_cycle;                            // begin + cycles
   } else {
     int body = 2 * L.lc + 1 + (L.ld > 0 ? 2 : 0);               // downs, coarse solve, ups
-    n += 4 + (cycles > 1 ? cycles : 1) * body + 1;              // begin/init/resid/check, loop, out
+    n += 2 + (cycles > 1 ? cycles : 1) * body + 1;              // init, resid, loop, out+stats
   }
-  n += 1;                                                       // stats
+  if (p.mg_mode == AJ_MG_PARITY) n += 1;                        // stats
   n += 1;                                                       // correction
-  if (p.nn_factor > 0) n += 3 + 15 + 1;                         // features, network, correction
+  if (p.nn_factor > 0) n += 3 + 12 + 1;                         // features, network, correction
   return n;
 }
 

@@ -107,12 +107,19 @@ __device__ __forceinline__ df df_add_f(df a, float b) {
   s.lo += a.lo;
   return quick_two_sum(s.hi, s.lo);
 }
+// Dekker's addition with one TwoSum: error <= ~2^-47 max(|a|, |b|), which in
+// the residual below stays ~1e-14 |p| ax, far under the 1e-6 |b| targets
+__device__ __forceinline__ df df_add_s(df a, df b) {
+  df s = two_sum(a.hi, b.hi);
+  s.lo += a.lo + b.lo;
+  return quick_two_sum(s.hi, s.lo);
+}
 // r = b - (ax ((xp - c) + (xm - c)) + ay ((yp - c) + (ym - c))), all double-FP32
 __device__ __forceinline__ df df_residual(float b, df c, df xp, df xm, df yp, df ym, df ax, df ay) {
   const df nc = df_neg(c);
-  const df sx = df_add(df_add(xp, nc), df_add(xm, nc));
-  const df sy = df_add(df_add(yp, nc), df_add(ym, nc));
-  const df ap = df_add(df_mul(ax, sx), df_mul(ay, sy));
+  const df sx = df_add_s(df_add_s(xp, nc), df_add_s(xm, nc));
+  const df sy = df_add_s(df_add_s(yp, nc), df_add_s(ym, nc));
+  const df ap = df_add_s(df_mul(ax, sx), df_mul(ay, sy));
   return df_add_f(df_neg(ap), b);
 }
 
@@ -827,17 +834,39 @@ struct CvHist {
   long N;
 };
 constexpr int CV_ROWS = 8;   // rows per block of the whole-grid kernels (unrolled)
+
+// The extrapolation history as this solve sees it: a solve that finished
+// since the last commit (hist_pending) has filed its solution in the other
+// slot.  The last block of k_cv_resid commits the rotation.
+struct HistView {
+  int cur, n;
+  float dtp;
+};
+__device__ __forceinline__ HistView hist_view(const DevScalars* sc) {
+  HistView h;
+  if (sc->hist_pending) {
+    h.cur = 1 - sc->hist_cur;
+    h.n = sc->hist_n < 2 ? sc->hist_n + 1 : 2;
+    h.dtp = sc->dt_last;
+  } else {
+    h.cur = sc->hist_cur;
+    h.n = sc->hist_n;
+    h.dtp = sc->dt_prev;
+  }
+  return h;
+}
 __global__ void __launch_bounds__(256) k_cv_init(const float* __restrict__ p0,
                                                  float* __restrict__ ps, int n, int m, CvHist hs,
                                                  const DevScalars* sc) {
   const long N = (long)n * m;
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= m) return;
-  const int hn = hs.h ? sc->hist_n : 0;
-  const float* h1 = hs.h ? hs.h + (long)sc->hist_cur * 2 * N : nullptr;
-  const float* h2 = hs.h ? hs.h + (long)(1 - sc->hist_cur) * 2 * N : nullptr;
+  const HistView hv = hist_view(sc);
+  const int hn = hs.h ? hv.n : 0;
+  const float* h1 = hs.h ? hs.h + (long)hv.cur * 2 * N : nullptr;
+  const float* h2 = hs.h ? hs.h + (long)(1 - hv.cur) * 2 * N : nullptr;
   float ratio = 1.f;
-  if (hn >= 2 && sc->dt > 0.f && sc->dt_prev > 0.f) ratio = sc->dt / sc->dt_prev;
+  if (hn >= 2 && sc->dt > 0.f && hv.dtp > 0.f) ratio = sc->dt / hv.dtp;
 #pragma unroll
   for (int r = 0; r < CV_ROWS; ++r) {
     const int i = blockIdx.y * CV_ROWS + r;
@@ -864,7 +893,7 @@ __global__ void __launch_bounds__(256) k_cv_init(const float* __restrict__ p0,
 __global__ void __launch_bounds__(256) k_cv_resid(const float* __restrict__ ps,
                                                   const float* __restrict__ b,
                                                   float* __restrict__ r, int n, int m, DfCoef co,
-                                                  DevScalars* sc) {
+                                                  DevScalars* sc, double rtol) {
   const long N = (long)n * m;
   const df ax{co.axh, co.axl}, ay{co.ayh, co.ayl};
   float acc = 0.f, accb = 0.f;
@@ -894,45 +923,48 @@ __global__ void __launch_bounds__(256) k_cv_resid(const float* __restrict__ ps,
   }
   block_sum_atomic((double)acc, &sc->acc[0]);
   block_sum_atomic((double)accb, &sc->acc[1]);
-}
-
-__global__ void k_cv_begin(DevScalars* sc) {
-  if (sc->hist_pending) {       // the last solve's state went to the other slot
-    sc->hist_cur = 1 - sc->hist_cur;
-    sc->hist_n = sc->hist_n < 2 ? sc->hist_n + 1 : 2;
-    sc->dt_prev = sc->dt_last;
+  // the last block: commit the history rotation, reset the solve's counters
+  // and run the test before the first cycle (the guess may already satisfy rtol)
+  __shared__ int am_last;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned int ticket = atomicAdd(&sc->red_count, 1u);
+    am_last = ticket == gridDim.x * gridDim.y - 1;
+  }
+  __syncthreads();
+  if (am_last && threadIdx.x == 0) {
+    __threadfence();
+    const HistView hv = hist_view(sc);
+    sc->hist_cur = hv.cur;
+    sc->hist_n = hv.n;
+    sc->dt_prev = hv.dtp;
     sc->hist_pending = 0;
+    sc->red_count = 0u;
+    sc->mg_cycles = 0;
+    sc->loops = 0;
+    sc->pcur = 0;
+    sc->err = AJ_OK;
+    sc->mg_done = 0;
+    sc->bnorm = sqrt(sc->acc[1]);
+    const double nb = sc->bnorm > 0.0 ? sc->bnorm : 1.0;
+    const double rel = sqrt(sc->acc[0]) / nb;
+    sc->rel = rel;
+    sc->abs_sq = sc->acc[0];
+    if (!isfinite(rel)) {
+      sc->err = AJ_ERR_NONFINITE;
+      sc->mg_done = 1;
+    } else if (rel <= rtol) {
+      sc->mg_done = 1;
+    }
+    sc->acc[0] = 0.0;
+    sc->acc[1] = 0.0;
   }
-  sc->mg_done = 0;
-  sc->mg_cycles = 0;
-  sc->loops = 0;
-  sc->pcur = 0;
-  sc->red_count = 0u;
-  sc->acc[0] = 0.0;
-  sc->acc[1] = 0.0;
-  sc->err = AJ_OK;
-}
-
-// the test before the first cycle (the initial guess may already satisfy rtol)
-__global__ void k_cv_check0(DevScalars* sc, double rtol) {
-  sc->bnorm = sqrt(sc->acc[1]);
-  double nb = sc->bnorm > 0.0 ? sc->bnorm : 1.0;
-  double rel = sqrt(sc->acc[0]) / nb;
-  sc->rel = rel;
-  sc->abs_sq = sc->acc[0];
-  if (!isfinite(rel)) {
-    sc->err = AJ_ERR_NONFINITE;
-    sc->mg_done = 1;
-  } else if (rel <= rtol) {
-    sc->mg_done = 1;
-  }
-  sc->acc[0] = 0.0;
-  sc->acc[1] = 0.0;
 }
 
 // p = hi + lo; with a history, the state also goes to the free slot (the
-// next k_cv_begin makes it the latest)
-__global__ void k_cv_out(PState ps, DevScalars* sc, float* __restrict__ p, long N, float* hist) {
+// next solve's k_cv_resid makes it the latest); thread 0 files the statistics
+__global__ void k_cv_out(PState ps, DevScalars* sc, float* __restrict__ p, long N, float* hist,
+                         AjStats* stats) {
   long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
   const float* src = sc->pcur ? ps.b : ps.a;
   if (k < N) {
@@ -944,9 +976,21 @@ __global__ void k_cv_out(PState ps, DevScalars* sc, float* __restrict__ p, long 
       dst[N + k] = lo;
     }
   }
-  if (hist && k == 0) {
-    sc->hist_pending = 1;
-    sc->dt_last = sc->dt;
+  if (k == 0) {
+    if (hist) {
+      sc->hist_pending = 1;
+      sc->dt_last = sc->dt;
+    }
+    if (stats) {
+      stats->cycles = sc->mg_cycles;
+      stats->converged = sc->mg_done;
+      stats->err = sc->err;
+      stats->pad = 0;
+      stats->rel_residual = sc->rel;
+      stats->rhs_norm = sc->bnorm;
+      stats->dt = sc->dt;
+      stats->abs_residual_sq = sc->abs_sq;
+    }
   }
 }
 
@@ -1075,11 +1119,10 @@ static cudaStream_t side_stream() {
 }
 
 int converge_solve(const AjStepParams& p, const Layout& L, void* ws, const float* p0,
-                   float* pout, cudaStream_t st, const NnWarm* nn) {
+                   float* pout, cudaStream_t st, const NnWarm* nn, AjStats* stats) {
   DevScalars* sc = at<DevScalars>(ws, 0);
   const long N = (long)p.nx * p.ny;
   const PState ps = pstate(L, ws);
-  k_cv_begin<<<1, 1, 0, st>>>(sc);
   const dim3 rgrid(cdiv(p.ny, 256), cdiv(p.nx, CV_ROWS));
   const bool extrap = p.warm_start == AJ_WARM_EXTRAPOLATE && L.hist;
   CvHist hs{extrap ? at<float>(ws, L.hist) : nullptr, N};
@@ -1089,8 +1132,8 @@ int converge_solve(const AjStepParams& p, const Layout& L, void* ws, const float
     if (rc != AJ_OK) return rc;
   }
   k_cv_resid<<<rgrid, 256, 0, st>>>(ps.a, at<float>(ws, L.b0), at<float>(ws, L.B[0]), p.nx, p.ny,
-                                    df_coef(1.0 / (p.dx * p.dx), 1.0 / (p.dy * p.dy)), sc);
-  k_cv_check0<<<1, 1, 0, st>>>(sc, p.mg_rtol);
+                                    df_coef(1.0 / (p.dx * p.dx), 1.0 / (p.dy * p.dy)), sc,
+                                    p.mg_rtol);
 
   cudaStreamCaptureStatus cs;
   unsigned long long id;
@@ -1132,7 +1175,8 @@ int converge_solve(const AjStepParams& p, const Layout& L, void* ws, const float
     cudaGraph_t out;
     if (cudaStreamEndCapture(side, &out) != cudaSuccess) return AJ_ERR_CUDA;
   }
-  k_cv_out<<<cdiv(N, 256), 256, 0, st>>>(ps, sc, pout, N, extrap ? at<float>(ws, L.hist) : nullptr);
+  k_cv_out<<<cdiv(N, 256), 256, 0, st>>>(ps, sc, pout, N, extrap ? at<float>(ws, L.hist) : nullptr,
+                                         stats);
   return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
 }
 

@@ -150,7 +150,8 @@ int profile_pressure_kernel(const AjStepParams& p, const Layout& L, void* ws, in
 // converging multigrid (aj_converge.cu)
 int converge_prepare(const AjStepParams& p, const Layout& L, void* ws, cudaStream_t st);
 int converge_solve(const AjStepParams& p, const Layout& L, void* ws, const float* p0,
-                   float* pout, cudaStream_t st, const NnWarm* nn = nullptr);
+                   float* pout, cudaStream_t st, const NnWarm* nn = nullptr,
+                   AjStats* stats = nullptr);
 size_t converge_block_smem(const Layout& L, int lc);
 int converge_first_block_level(const Layout& L);
 int converge_direct_level(const Layout& L);

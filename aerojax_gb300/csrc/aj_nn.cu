@@ -100,7 +100,8 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv3x3(const float* __restric
                                                           const __nv_bfloat16* __restrict__ WT,
                                                           const float* __restrict__ bias,
                                                           float* __restrict__ Y, int relu,
-                                                          float* __restrict__ Yp) {
+                                                          float* __restrict__ Yp,
+                                                          const float* __restrict__ Xc) {
   using S = ConvSmem<CIN, NT>;
   constexpr int AS = S::AS, BN = S::BN;
   extern __shared__ __align__(16) unsigned char conv_sm[];
@@ -138,6 +139,27 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv3x3(const float* __restric
   }
   cp_async_wait<0>();
   __syncthreads();
+  if (Xc) {   // input = nearest 2x up-sampling of Xc (H/2 x W/2) + X
+    constexpr int C4 = CIN / 4;
+    const int Hc = H >> 1, Wc = W >> 1;
+    for (int e = tid; e < CT_HALO * C4; e += CONV_THREADS) {
+      const int px = e / C4, q = e - px * C4;
+      const int hy = px / (CT + 2), hx = px - hy * (CT + 2);
+      const int gh = h0 - 1 + hy, gw = w0 - 1 + hx;
+      if (gh >= 0 && gh < H && gw >= 0 && gw < W) {
+        const float4 c = *reinterpret_cast<const float4*>(
+            Xc + (((long)n * Hc + (gh >> 1)) * Wc + (gw >> 1)) * CIN + q * 4);
+        float4* a = reinterpret_cast<float4*>(As + px * AS + q * 4);
+        float4 v = *a;
+        v.x = c.x + v.x;
+        v.y = c.y + v.y;
+        v.z = c.z + v.z;
+        v.w = c.w + v.w;
+        *a = v;
+      }
+    }
+    __syncthreads();
+  }
   float acc[NT][4];
 #pragma unroll
   for (int q = 0; q < NT; ++q) acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.f;
@@ -210,12 +232,13 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv3x3(const float* __restric
 
 template <int CIN, int NT>
 static void conv_launch(const float* X, int N, int H, int W, int Cout, const __nv_bfloat16* WT,
-                        const float* bias, float* Y, int relu, float* Yp, cudaStream_t st) {
+                        const float* bias, float* Y, int relu, float* Yp, const float* Xc,
+                        cudaStream_t st) {
   using S = ConvSmem<CIN, NT>;
   const int tiles = ((W + CT - 1) / CT) * ((H + CT - 1) / CT) * N;
   dim3 grid(tiles, Cout / S::BN);
   k_conv3x3<CIN, NT><<<grid, CONV_THREADS, S::bytes, st>>>(X, N, H, W, Cout, WT, bias, Y, relu,
-                                                            Yp);
+                                                            Yp, Xc);
 }
 
 template <int CIN, int NT>
@@ -237,27 +260,29 @@ static void conv_attrs() {
 
 template <int CIN>
 static int conv_cin(const float* X, int N, int H, int W, int Cout, const __nv_bfloat16* WT,
-                    const float* bias, float* Y, int relu, float* Yp, cudaStream_t st) {
+                    const float* bias, float* Y, int relu, float* Yp, const float* Xc,
+                    cudaStream_t st) {
   switch (Cout) {
-    case 16: conv_launch<CIN, 2>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, st); break;
+    case 16: conv_launch<CIN, 2>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, Xc, st); break;
     case 32:
     case 64:
-    case 128: conv_launch<CIN, 4>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, st); break;
+    case 128: conv_launch<CIN, 4>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, Xc, st); break;
     default: return AJ_ERR_PARAM;
   }
   return AJ_OK;
 }
 
 // Y = conv(X, WT) (+ bias, ReLU); WT[tap][Cout][Cin] BF16; Yp (nullable,
-// H and W even) receives the 2x2 average pool of Y
+// H and W even) receives the 2x2 average pool of Y; with Xc (nullable) the
+// input is up2(Xc) + X
 static int conv3x3(const float* X, int N, int H, int W, int Cin, int Cout,
                    const __nv_bfloat16* WT, const float* bias, float* Y, int relu,
-                   cudaStream_t st, float* Yp = nullptr) {
+                   cudaStream_t st, float* Yp = nullptr, const float* Xc = nullptr) {
   switch (Cin) {
-    case 16: return conv_cin<16>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, st);
-    case 32: return conv_cin<32>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, st);
-    case 64: return conv_cin<64>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, st);
-    case 128: return conv_cin<128>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, st);
+    case 16: return conv_cin<16>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, Xc, st);
+    case 32: return conv_cin<32>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, Xc, st);
+    case 64: return conv_cin<64>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, Xc, st);
+    case 128: return conv_cin<128>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, Xc, st);
     default: return AJ_ERR_PARAM;
   }
 }
@@ -543,11 +568,16 @@ struct NnW {
 
 static inline unsigned ew_blocks(long T) { return cdiv(T, 256); }
 
-int nn_forward(int n, int h, int w, const NnW& W, const NnActs& A, cudaStream_t st) {
+// The forward pass.  keep: materialise the decoder inputs u = up2(o) + s
+// (the backward pass needs them); else the decoder convolutions add the
+// up-sampled coarse input while staging their halo (inference).
+int nn_forward(int n, int h, int w, const NnW& W, const NnActs& A, cudaStream_t st,
+               bool keep = true) {
   const int H0 = h, W0 = w, H1 = h / 2, W1 = w / 2, H2 = h / 4, W2 = w / 4, H3 = h / 8, W3 = w / 8;
-  auto conv = [&](int l, const float* in, float* out, int H, int Wd, float* pooled = nullptr) {
+  auto conv = [&](int l, const float* in, float* out, int H, int Wd, float* pooled = nullptr,
+                  const float* coarse = nullptr) {
     return conv3x3(in, n, H, Wd, kLayers[l].cin, kLayers[l].cout, W.wf(l), W.bias(l), out,
-                   kLayers[l].relu, st, pooled);
+                   kLayers[l].relu, st, pooled, coarse);
   };
   int rc = AJ_OK;
   rc |= conv(E0A, A.x, A.a0, H0, W0);
@@ -558,12 +588,18 @@ int nn_forward(int n, int h, int w, const NnW& W, const NnActs& A, cudaStream_t 
   rc |= conv(E2B, A.a2, A.s2, H2, W2, A.p2);
   rc |= conv(E3A, A.p2, A.a3, H3, W3);
   rc |= conv(E3B, A.a3, A.bt, H3, W3);
-  k_up2_add<<<ew_blocks((long)n * H2 * W2 * 128), 256, 0, st>>>(A.bt, A.s2, A.u2, n, H2, W2, 128);
-  rc |= conv(D2, A.u2, A.o2, H2, W2);
-  k_up2_add<<<ew_blocks((long)n * H1 * W1 * 64), 256, 0, st>>>(A.o2, A.s1, A.u1, n, H1, W1, 64);
-  rc |= conv(D1, A.u1, A.o1, H1, W1);
-  k_up2_add<<<ew_blocks((long)n * H0 * W0 * 32), 256, 0, st>>>(A.o1, A.s0, A.u0, n, H0, W0, 32);
-  rc |= conv(D0A, A.u0, A.o0, H0, W0);
+  if (keep) {
+    k_up2_add<<<ew_blocks((long)n * H2 * W2 * 128), 256, 0, st>>>(A.bt, A.s2, A.u2, n, H2, W2, 128);
+    rc |= conv(D2, A.u2, A.o2, H2, W2);
+    k_up2_add<<<ew_blocks((long)n * H1 * W1 * 64), 256, 0, st>>>(A.o2, A.s1, A.u1, n, H1, W1, 64);
+    rc |= conv(D1, A.u1, A.o1, H1, W1);
+    k_up2_add<<<ew_blocks((long)n * H0 * W0 * 32), 256, 0, st>>>(A.o1, A.s0, A.u0, n, H0, W0, 32);
+    rc |= conv(D0A, A.u0, A.o0, H0, W0);
+  } else {
+    rc |= conv(D2, A.s2, A.o2, H2, W2, nullptr, A.bt);
+    rc |= conv(D1, A.s1, A.o1, H1, W1, nullptr, A.o2);
+    rc |= conv(D0A, A.s0, A.o0, H0, W0, nullptr, A.o1);
+  }
   rc |= conv(D0B, A.o0, A.y, H0, W0);
   if (rc != AJ_OK) return AJ_ERR_PARAM;
   return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
@@ -683,36 +719,38 @@ __global__ void __launch_bounds__(256) k_nn_feat(const float* __restrict__ b,
   }
 }
 
-// per-sample scales (one block): RMS of channels 0 and 2 over the network
-// grid (FP64 sums) and the output scale rms_r * lmin^2 / 10 (a correction
-// solving A dp = r has that magnitude)
-__global__ void __launch_bounds__(1024) k_nn_scale(const float* __restrict__ x, long cells,
-                                                   DevScalars* sc, double lmin2) {
-  double sr = 0.0, sp = 0.0;
-  for (long c = threadIdx.x; c < cells; c += blockDim.x) {
+// per-sample scales: RMS of channels 0 and 2 over the network grid (FP64
+// sums of a few blocks, the last block to finish turns them into scales) and
+// the output scale rms_r * lmin^2 / 10 (a correction solving A dp = r has
+// that magnitude)
+constexpr int NN_SCALE_BLOCKS = 32;
+__global__ void __launch_bounds__(512) k_nn_scale(const float* __restrict__ x, long cells,
+                                                  DevScalars* sc, double lmin2) {
+  float sr = 0.f, sp = 0.f;
+  const long stride = (long)gridDim.x * blockDim.x;
+#pragma unroll 4
+  for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < cells; c += stride) {
     const float r = x[c * 16], q = x[c * 16 + 2];
-    sr += (double)r * r;
-    sp += (double)q * q;
+    sr = fmaf(r, r, sr);
+    sp = fmaf(q, q, sp);
   }
-  __shared__ double red[2][32];
-  sr = warp_sum(sr);
-  sp = warp_sum(sp);
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  if (lane == 0) {
-    red[0][w] = sr;
-    red[1][w] = sp;
+  block_sum_atomic((double)sr, &sc->acc[2]);
+  block_sum_atomic((double)sp, &sc->acc[3]);
+  __shared__ int am_last;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    am_last = atomicAdd(&sc->red_count, 1u) == gridDim.x - 1;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    double a = 0.0, b = 0.0;
-    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
-      a += red[0][k];
-      b += red[1][k];
-    }
-    const double rr = sqrt(a / (double)cells), rp = sqrt(b / (double)cells);
+  if (am_last && threadIdx.x == 0) {
+    __threadfence();
+    const double rr = sqrt(sc->acc[2] / (double)cells), rp = sqrt(sc->acc[3] / (double)cells);
     sc->nn_rms_r = rr > 1e-30 ? rr : 1e-30;
     sc->nn_rms_p = rp > 1e-30 ? rp : 1e-30;
     sc->nn_out_scale = sc->nn_rms_r * lmin2 / 10.0;
+    sc->acc[2] = 0.0;
+    sc->acc[3] = 0.0;
+    sc->red_count = 0u;
   }
 }
 
@@ -797,7 +835,7 @@ int nn_features(const AjStepParams& p, void* ws, const float* b, const float* ma
       b, mask, pp, p.nx, p.ny, F, (float)(1.0 / (p.dx * p.dx)), (float)(1.0 / (p.dy * p.dy)),
       x16);
   const double lx = p.nx * p.dx, ly = p.ny * p.dy, lmin = lx < ly ? lx : ly;
-  k_nn_scale<<<1, 1024, 0, st>>>(x16, (long)h * w, sc, lmin * lmin);
+  k_nn_scale<<<NN_SCALE_BLOCKS, 512, 0, st>>>(x16, (long)h * w, sc, lmin * lmin);
   k_nn_norm<<<cdiv((long)h * w, 256), 256, 0, st>>>(x16, x3, (long)h * w, sc);
   if (pt && target) k_nn_target<<<grd, blk, 0, st>>>(pt, pp, p.nx, p.ny, F, target, sc);
   return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
@@ -814,7 +852,7 @@ int nn_correct_state(const AjStepParams& p, const Layout& L, void* ws, const flo
   int rc = nn_features(p, ws, b, nn.mask, state, nullptr, A.x, nullptr, nullptr, st);
   if (rc != AJ_OK) return rc;
   NnW W{reinterpret_cast<const __nv_bfloat16*>(nn.packed), nn.master};
-  rc = nn_forward(1, h, w, W, A, st);
+  rc = nn_forward(1, h, w, W, A, st, false);
   if (rc != AJ_OK) return rc;
   dim3 blk(32, 8), grd(cdiv(p.ny, 32), cdiv(p.nx, 8));
   k_nn_apply<<<grd, blk, 0, st>>>(A.y, p.nx, p.ny, F, state, at<DevScalars>(ws, 0));

@@ -148,6 +148,34 @@ __global__ void k_les_const(const float* __restrict__ u, const float* __restrict
   nsg[(long)i * ny + j] = coef * s.smag;
 }
 
+// constant Smagorinsky on the MAC grid: the strain of the cell-centred
+// velocities (solver/operators_mac.py:118-127) formed from the faces on the fly,
+// the same arithmetic as k_mac_to_center followed by k_les_const
+__global__ void k_les_const_mac(const float* __restrict__ u, const float* __restrict__ v,
+                                float* __restrict__ nsg, int nx, int ny, float h2x, float h2y,
+                                float coef) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= nx || j >= ny) return;
+  // rounded like the stored centre values (no contraction into the gradients)
+  auto uc = [&](int a, int b) {
+    return __fmul_rn(0.5f, __fadd_rn(ldg(u + (long)(a + 1) * ny + b), ldg(u + (long)a * ny + b)));
+  };
+  auto vc = [&](int a, int b) {
+    return __fmul_rn(0.5f,
+                     __fadd_rn(ldg(v + (long)a * (ny + 1) + b + 1), ldg(v + (long)a * (ny + 1) + b)));
+  };
+  const int ip = wrapi(i + 1, nx), im = wrapi(i - 1, nx), jp = wrapi(j + 1, ny),
+            jm = wrapi(j - 1, ny);
+  const float du_dx = (uc(ip, j) - uc(im, j)) * h2x;
+  const float du_dy = (uc(i, jp) - uc(i, jm)) * h2y;
+  const float dv_dx = (vc(ip, j) - vc(im, j)) * h2x;
+  const float dv_dy = (vc(i, jp) - vc(i, jm)) * h2y;
+  const float sxx = du_dx, syy = dv_dy, sxy = 0.5f * (du_dy + dv_dx);
+  const float smag = sqrtf(2.0f * (sxx * sxx + syy * syy + 2.0f * sxy * sxy) + 1e-10f);
+  nsg[(long)i * ny + j] = coef * smag;
+}
+
 // MAC faces to cell centres (solver/operators_mac.py:118-127)
 __global__ void k_mac_to_center(const float* __restrict__ u, const float* __restrict__ v,
                                 float* __restrict__ uc, float* __restrict__ vc, int nx, int ny) {
@@ -271,6 +299,11 @@ int launch_les(const AjStepParams& p, const Layout& L, void* ws, int model, cons
   long n = (long)nx * ny;
   float* D = at<float>(ws, L.dyn);
   const float *uu = u, *vv = v;
+  if (mac_input && model == AJ_LES_SMAGORINSKY) {
+    double c = p.smagorinsky_constant * delta;
+    k_les_const_mac<<<grd, blk, 0, st>>>(u, v, nsg, nx, ny, h2x, h2y, (float)(c * c));
+    return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+  }
   if (mac_input) {
     float* uc = D + 14 * n;
     float* vc = D + 15 * n;
@@ -757,6 +790,16 @@ __global__ void __launch_bounds__(256) k_rk_mac(RkMac a) {
   const float dt = a.sc->dt;
   bool last = a.rk2 ? a.stage == 2 : a.stage == 3;
   const bool fast = a.flow == AJ_FLOW_VON_KARMAN && a.slip;
+  if (fast && i >= 2 && i <= nx - 3 && j >= 2 && j <= ny - 3) {
+    // both faces of the cell interior: one scope, so the loads they share
+    // (u at (i,j), (i+1,j), (i,j-1); v at (i,j), (i,j+1), (i-1,j); mask and
+    // nu_sgs at (i,j)) are issued once
+    const float uo = stage_mac_u_int<HYPER>(a, i, j, dt, last ? nullptr : a.k1u_out);
+    const float vo = stage_mac_v_int<HYPER>(a, i, j, dt, last ? nullptr : a.k1v_out);
+    a.uout[(long)i * ny + j] = uo;
+    a.vout[(long)i * (ny + 1) + j] = vo;
+    return;
+  }
   // u faces
   if (i <= nx && j < ny) {
     long k = (long)i * ny + j;
