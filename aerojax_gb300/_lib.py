@@ -93,6 +93,8 @@ _SIGS = {
     "aj_profile_kernel": (c_int32, [POINTER(AjStepParams), c_int32, c_void_p, c_void_p, c_void_p,
                                     c_void_p, c_size_t, c_void_p]),
     "aj_release_graphs": (c_int32, []),
+    "aj_diagnostics": (c_int32, [POINTER(AjStepParams), c_void_p, c_void_p, c_void_p, c_void_p,
+                                 c_void_p, c_void_p]),
     "aj_autotune": (c_int32, [POINTER(AjStepParams), c_void_p, c_size_t, c_int32,
                               POINTER(ctypes.c_float), POINTER(c_int32), c_void_p]),
     "aj_ensemble_step": (c_int32, [c_int32, POINTER(AjStepParams), POINTER(c_void_p),

@@ -292,3 +292,94 @@ extern "C" int32_t aj_geometry(int32_t nx, int32_t ny, double lx, double ly, int
                                                      1.0 / eps, mask, sdf);
   return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
 }
+
+// ---------------------------------------------------------------- diagnostics
+// The post-step fields of step_for_visualization
+// (solver/simulation/visualization_step.py:224-256) into headless device
+// buffers: vorticity and divergence (solver/operators.py:75-108,
+// solver/operators_mac.py:58-115; non-periodic for the von Karman channel,
+// periodic otherwise) and the speed of the cell-centred velocity.  On the MAC
+// grid the reference's vorticity differentiates the centred u in x and the
+// centred v in y (its names say dv/dx and du/dy); that is reproduced.
+namespace aj {
+
+template <bool MAC, bool PER>
+__global__ void k_diagnostics(const float* __restrict__ u, const float* __restrict__ v, int nx,
+                              int ny, float dx, float dy, float* __restrict__ vort,
+                              float* __restrict__ div, float* __restrict__ speed) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= nx || j >= ny) return;
+  const long k = (long)i * ny + j;
+  const float h2x = 2.f * dx, h2y = 2.f * dy;
+  if (MAC) {
+    const int nyv = ny + 1;
+    auto uc = [&](int a, int b) {
+      return __fmul_rn(0.5f, __fadd_rn(u[(long)(a + 1) * ny + b], u[(long)a * ny + b]));
+    };
+    auto vc = [&](int a, int b) {
+      return __fmul_rn(0.5f, __fadd_rn(v[(long)a * nyv + b + 1], v[(long)a * nyv + b]));
+    };
+    int ip, im, jp, jm;
+    if (PER) {
+      ip = wrapi(i + 1, nx), im = wrapi(i - 1, nx), jp = wrapi(j + 1, ny), jm = wrapi(j - 1, ny);
+    } else {
+      ip = clampi(i + 1, nx), im = clampi(i - 1, nx), jp = clampi(j + 1, ny), jm = clampi(j - 1, ny);
+    }
+    if (vort) vort[k] = (uc(ip, j) - uc(im, j)) / h2x - (vc(i, jp) - vc(i, jm)) / h2y;
+    if (div)
+      div[k] = (u[(long)(i + 1) * ny + j] - u[(long)i * ny + j]) / dx +
+               (v[(long)i * nyv + j + 1] - v[(long)i * nyv + j]) / dy;
+    if (speed) {
+      const float a = uc(i, j), b = vc(i, j);
+      speed[k] = sqrtf(a * a + b * b);
+    }
+  } else {
+    if (vort) {
+      float gx, gy;
+      if (PER) {
+        gx = (v[(long)wrapi(i + 1, nx) * ny + j] - v[(long)wrapi(i - 1, nx) * ny + j]) / h2x;
+        gy = (u[(long)i * ny + wrapi(j + 1, ny)] - u[(long)i * ny + wrapi(j - 1, ny)]) / h2y;
+      } else {
+        if (i == 0) gx = (v[k + ny] - v[k]) / dx;
+        else if (i == nx - 1) gx = (v[k] - v[k - ny]) / dx;
+        else gx = (v[k + ny] - v[k - ny]) / h2x;
+        if (j == 0) gy = (u[k + 1] - u[k]) / dy;
+        else if (j == ny - 1) gy = (u[k] - u[k - 1]) / dy;
+        else gy = (u[k + 1] - u[k - 1]) / h2y;
+      }
+      vort[k] = gx - gy;
+    }
+    if (div) {
+      float d = 0.f;
+      if (PER) {
+        d = (u[(long)wrapi(i + 1, nx) * ny + j] - u[(long)wrapi(i - 1, nx) * ny + j]) / h2x +
+            (v[(long)i * ny + wrapi(j + 1, ny)] - v[(long)i * ny + wrapi(j - 1, ny)]) / h2y;
+      } else if (i > 0 && i < nx - 1 && j > 0 && j < ny - 1) {
+        d = (u[k + ny] - u[k - ny]) / h2x + (v[k + 1] - v[k - 1]) / h2y;
+      }
+      div[k] = d;
+    }
+    if (speed) speed[k] = sqrtf(u[k] * u[k] + v[k] * v[k]);
+  }
+}
+
+}  // namespace aj
+
+extern "C" int32_t aj_diagnostics(const AjStepParams* prm, const float* u, const float* v,
+                                  float* vort, float* div, float* speed, void* stream) {
+  using namespace aj;
+  if (!prm || !u || !v || prm->nx < 2 || prm->ny < 2 || prm->dx <= 0 || prm->dy <= 0)
+    return AJ_ERR_PARAM;
+  const int nx = prm->nx, ny = prm->ny;
+  const bool mac = prm->grid_type == AJ_GRID_MAC;
+  const bool per = prm->flow_type != AJ_FLOW_VON_KARMAN;
+  const float dx = (float)prm->dx, dy = (float)prm->dy;
+  dim3 blk(32, 8), grd(cdiv(ny, 32), cdiv(nx, 8));
+  cudaStream_t st = (cudaStream_t)stream;
+  if (mac && per) k_diagnostics<true, true><<<grd, blk, 0, st>>>(u, v, nx, ny, dx, dy, vort, div, speed);
+  else if (mac) k_diagnostics<true, false><<<grd, blk, 0, st>>>(u, v, nx, ny, dx, dy, vort, div, speed);
+  else if (per) k_diagnostics<false, true><<<grd, blk, 0, st>>>(u, v, nx, ny, dx, dy, vort, div, speed);
+  else k_diagnostics<false, false><<<grd, blk, 0, st>>>(u, v, nx, ny, dx, dy, vort, div, speed);
+  return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+}

@@ -396,6 +396,24 @@ def compute_cfl_timestep(u, v, dx, dy, nu, mask=None, cfl_target=0.3, dt_min=1e-
     return out
 
 
+def diagnostics(u, v, dx, dy, grid_type="collocated", flow_type="von_karman", stream=None):
+    """The post-step fields of step_for_visualization
+    (solver/simulation/visualization_step.py:224-256): (vorticity, divergence,
+    speed), each (nx, ny), computed on the device."""
+    mac = grid_type == "mac"
+    nx = v.shape[0]
+    ny = u.shape[1]
+    _f32(u, "u", (nx + 1, ny) if mac else (nx, ny))
+    _f32(v, "v", (nx, ny + 1) if mac else (nx, ny))
+    p = make_params(StepConfig(nx=nx, ny=ny, dx=float(dx), dy=float(dy), nu=1.0,
+                               grid_type=grid_type, flow_type=flow_type))
+    out = [torch.empty((nx, ny), dtype=torch.float32, device=u.device) for _ in range(3)]
+    check("aj_diagnostics", lib().aj_diagnostics(ctypes.byref(p), u.data_ptr(), v.data_ptr(),
+                                                 out[0].data_ptr(), out[1].data_ptr(),
+                                                 out[2].data_ptr(), _stream(stream)))
+    return tuple(out)
+
+
 def make_geometry(kind, nx, ny, lx, ly, geo, eps, device="cuda", stream=None):
     """Obstacle SDF and mask = 1 - sigmoid(-sdf/eps) on the device
     (solver/simulation/mask_generator.py:10-160).  kind: 'cylinder' (cx, cy, r),

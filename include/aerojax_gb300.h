@@ -51,8 +51,9 @@ enum { AJ_VARIANT_PURE = 0, AJ_VARIANT_GUI = 1 };
 enum { AJ_LES_NONE = 0, AJ_LES_SMAGORINSKY = 1, AJ_LES_DYNAMIC = 2 };
 enum { AJ_ADV_UPWIND = 0, AJ_ADV_WENO5 = 1 };
 /* PARITY   = the reference V-cycle, fixed v_cycles, absolute early exit;
-   CONVERGE = red-black Gauss-Seidel V-cycles inside FP64 iterative
-              refinement, FP64 coarsest solve and norms, relative stop. */
+   CONVERGE = FP32 red-black Gauss-Seidel V-cycles inside double-FP32
+              iterative refinement, an exact separable coarse solve (or an FP64
+              dense one), FP64 norms, relative stop. */
 enum { AJ_MG_PARITY = 0, AJ_MG_CONVERGE = 1 };
 /* Initial guess of the converging solve (no reference counterpart: the
    reference always starts from p = 0, multigrid_solver.py:219).
@@ -233,6 +234,16 @@ int32_t aj_step_nn(const AjStepParams* prm, const float* u, const float* v, cons
                    const float* p_prev, const uint16_t* nn_packed, const float* nn_master,
                    float* u_out, float* v_out, float* p_out, void* workspace,
                    size_t workspace_bytes, AjStats* stats, void* stream);
+
+/* Post-step fields of step_for_visualization (visualization_step.py:224-256)
+   into caller buffers (each nx*ny, nullable): vorticity
+   (operators.py:105-108 / operators_mac.py:101-115; the periodic forms
+   operators.py:99-102 / operators_mac.py:83-98 when flow_type is not von
+   Karman), divergence (operators.py:75-96 / operators_mac.py:58-80) and the
+   speed of the cell-centred velocity.  Reads prm->nx, ny, dx, dy, grid_type,
+   flow_type. */
+int32_t aj_diagnostics(const AjStepParams* prm, const float* u, const float* v, float* vort,
+                       float* div, float* speed, void* stream);
 
 /* Allocation-free pressure solve, for callers that cannot allocate device
    memory: hosts that own every device byte through their own allocator (a

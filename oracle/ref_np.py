@@ -129,6 +129,43 @@ def interpolate_to_cell_center(u, v):
     return 0.5 * (u[1:, :] + u[:-1, :]), 0.5 * (v[:, 1:] + v[:, :-1])
 
 
+def vorticity(u, v, dx, dy):
+    """solver/operators.py:99-102 (periodic)."""
+    return grad_x(v, dx) - grad_y(u, dy)
+
+
+def vorticity_staggered(u, v, dx, dy):
+    """solver/operators_mac.py:83-98, as written: d(u_centre)/dx - d(v_centre)/dy
+    with periodic central differences (the names say dv/dx and du/dy, the
+    arrays are the other velocity component)."""
+    uc, vc = interpolate_to_cell_center(u, v)
+    return ((np.roll(uc, -1, axis=0) - np.roll(uc, 1, axis=0)) / (2.0 * dx)
+            - (np.roll(vc, -1, axis=1) - np.roll(vc, 1, axis=1)) / (2.0 * dy))
+
+
+def vorticity_nonperiodic_staggered(u, v, dx, dy):
+    """solver/operators_mac.py:101-115, the same pairing with edge padding."""
+    uc, vc = interpolate_to_cell_center(u, v)
+    up = np.pad(uc, ((1, 1), (0, 0)), mode="edge")
+    vp = np.pad(vc, ((0, 0), (1, 1)), mode="edge")
+    return (up[2:, :] - up[:-2, :]) / (2.0 * dx) - (vp[:, 2:] - vp[:, :-2]) / (2.0 * dy)
+
+
+def diagnostics(u, v, dx, dy, mac=False, periodic=False):
+    """Post-step fields of step_for_visualization
+    (solver/simulation/visualization_step.py:224-256): vorticity, divergence
+    and the speed |u| of the cell-centred velocity."""
+    if mac:
+        vort = (vorticity_staggered if periodic else vorticity_nonperiodic_staggered)(u, v, dx, dy)
+        div = divergence_staggered(u, v, dx, dy)
+        uc, vc = interpolate_to_cell_center(u, v)
+    else:
+        vort = (vorticity if periodic else vorticity_nonperiodic)(u, v, dx, dy)
+        div = (divergence if periodic else divergence_nonperiodic)(u, v, dx, dy)
+        uc, vc = u, v
+    return vort, div, np.sqrt(uc * uc + vc * vc)
+
+
 def interpolate_to_x_face(c):
     """solver/operators_mac.py:130-137."""
     cp = np.pad(c, ((1, 1), (0, 0)), mode="edge")

@@ -224,6 +224,18 @@ def main(root):
                                    use_les=int(kw["use_les"]), dynamic=0, cs=kw["cs"],
                                    hyper=kw["hyper"], u_new=A(un), v_new=A(vn), p=A(p))
 
+    # --- post-step diagnostics (visualization_step.py:224-256) ------------------
+    out["diagnostics"] = dict(
+        u=c["u"], v=c["v"], um=um, vm=vm, dx=c["dx"], dy=c["dy"],
+        vort_np=A(R.ops.vorticity_nonperiodic(c["u"], c["v"], c["dx"], c["dy"])),
+        div_np=A(R.ops.divergence_nonperiodic(c["u"], c["v"], c["dx"], c["dy"])),
+        vort_per=A(R.ops.vorticity(c["u"], c["v"], c["dx"], c["dy"])),
+        div_per=A(R.ops.divergence(c["u"], c["v"], c["dx"], c["dy"])),
+        vort_mac_np=A(R.opsm.vorticity_nonperiodic_staggered(um, vm, c["dx"], c["dy"])),
+        div_mac_np=A(R.opsm.divergence_nonperiodic_staggered(um, vm, c["dx"], c["dy"])),
+        vort_mac_per=A(R.opsm.vorticity_staggered(um, vm, c["dx"], c["dy"])),
+        div_mac_per=A(R.opsm.divergence_staggered(um, vm, c["dx"], c["dy"])))
+
     # --- time step and geometry ---------------------------------------------------
     dtc = R.cfl.compute_cfl_timestep(c["u"], c["v"], c["dx"], c["dy"], nu, cfl_target=0.5,
                                      dt_min=1e-5, dt_max=0.05)

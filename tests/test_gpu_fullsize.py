@@ -186,3 +186,52 @@ def test_extrapolated_warm_start(cuda_lib):
     assert sum(ce[10:]) <= sum(cp[10:])
     assert float((ue - up).abs().max()) < 1e-3
     assert float((pe - pp).abs().max()) < 1e-2 * float(pp.abs().max())
+
+
+def test_diagnostics_match_reference(cuda_lib):
+    """aj_diagnostics against the reference's own operators (golden), all four
+    grid/flow variants, plus the speed against the oracle."""
+    import torch
+    import aerojax_gb300 as aj
+    from conftest import golden
+    from oracle import ref_np as R
+    z = golden("diagnostics")
+    dx, dy = float(z["dx"]), float(z["dy"])
+    for mac, u, v in ((False, z["u"], z["v"]), (True, z["um"], z["vm"])):
+        ut = torch.as_tensor(u.astype(np.float32), device="cuda")
+        vt = torch.as_tensor(v.astype(np.float32), device="cuda")
+        for per in (False, True):
+            vort, div, speed = aj.diagnostics(ut, vt, dx, dy, grid_type="mac" if mac else "collocated",
+                                              flow_type="taylor_green" if per else "von_karman")
+            tag = ("mac_" if mac else "") + ("per" if per else "np")
+            for got, ref in ((vort, z["vort_" + tag]), (div, z["div_" + tag])):
+                g = got.cpu().numpy()
+                assert np.max(np.abs(g - ref)) <= 1e-5 * max(1.0, np.max(np.abs(ref))), tag
+            _, _, sp = R.diagnostics(u.astype(np.float32).astype(np.float64),
+                                     v.astype(np.float32).astype(np.float64), dx, dy, mac=mac)
+            assert np.max(np.abs(speed.cpu().numpy() - sp)) <= 1e-6 * np.max(sp)
+
+
+def test_training_data_file(cuda_lib, tmp_path):
+    """generate_training_data writes the reference's .npz layout
+    (training_utils.py:12-81) and the recorded fields are the solver's."""
+    import torch
+    import aerojax_gb300 as aj
+    from aerojax_gb300 import configs, snapshots
+    case = configs.cylinder_512x96(nx=128, ny=48, mg_mode="parity", cfl_dt=False)
+    plan = aj.get_plan(case["cfg"], "cuda")
+    plan.prepare(case["mask"], case["sdf"])
+    path = snapshots.generate_training_data(
+        plan, case["u"].clone(), case["v"].clone(), case["mask"], 3,
+        {"u": True, "v": True, "p": True, "mask": True, "divergence": True},
+        str(tmp_path / "td.npz"))
+    d = snapshots.load_training_data(path)
+    assert d["u"].shape == (3, 128, 48) and d["p"].dtype == np.float64
+    assert int(d["nx"]) == 128 and int(d["ny"]) == 48 and float(d["dx"]) == case["cfg"].dx
+    u, v, p = case["u"].clone(), case["v"].clone(), torch.zeros((128, 48), device="cuda")
+    for _ in range(3):
+        u, v, p = aj.run_step(plan, u, v, case["mask"], p_guess=p)
+    assert np.array_equal(d["u"][-1], u.cpu().numpy().astype(np.float64))
+    assert np.array_equal(d["p"][-1], p.cpu().numpy().astype(np.float64))
+    _, div, _ = aj.diagnostics(u, v, case["cfg"].dx, case["cfg"].dy, flow_type="taylor_green")
+    assert np.array_equal(d["divergence"][-1], div.cpu().numpy().astype(np.float64))

@@ -99,3 +99,16 @@ def test_geometry():
     assert np.nanmax(np.abs(s2 - g["sdf_naca2412"])) < 1e-13
     s3 = R.sdf_three_cylinders_inline(g["X"], g["Y"], 2.0, 1.5, 0.5, 0.8)
     assert np.max(np.abs(s3 - g["sdf_three"])) < 1e-13
+
+
+def test_diagnostics_match_reference():
+    """Vorticity and divergence of step_for_visualization
+    (visualization_step.py:224-256), all four grid/flow variants."""
+    z = golden("diagnostics")
+    dx, dy = float(z["dx"]), float(z["dy"])
+    for mac, u, v in ((False, z["u"], z["v"]), (True, z["um"], z["vm"])):
+        for per in (False, True):
+            vort, div, _ = R.diagnostics(u, v, dx, dy, mac=mac, periodic=per)
+            tag = ("mac_" if mac else "") + ("per" if per else "np")
+            assert np.array_equal(vort, z["vort_" + tag]), tag
+            assert np.allclose(div, z["div_" + tag], rtol=0, atol=1e-12), tag
