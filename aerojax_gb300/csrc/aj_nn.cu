@@ -262,11 +262,19 @@ template <int CIN>
 static int conv_cin(const float* X, int N, int H, int W, int Cout, const __nv_bfloat16* WT,
                     const float* bias, float* Y, int relu, float* Yp, const float* Xc,
                     cudaStream_t st) {
+  // 32 output channels per block, or 16 when that leaves fewer blocks than
+  // SMs (the small grids of the deep layers are latency-bound: more, lighter
+  // blocks load their weights sooner)
+  const long tiles = (long)((W + CT - 1) / CT) * ((H + CT - 1) / CT) * N;
+  const bool narrow = Cout == 16 || tiles * (Cout / 32) < 152;
   switch (Cout) {
-    case 16: conv_launch<CIN, 2>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, Xc, st); break;
+    case 16:
     case 32:
     case 64:
-    case 128: conv_launch<CIN, 4>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, Xc, st); break;
+    case 128:
+      if (narrow) conv_launch<CIN, 2>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, Xc, st);
+      else conv_launch<CIN, 4>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, Xc, st);
+      break;
     default: return AJ_ERR_PARAM;
   }
   return AJ_OK;

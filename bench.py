@@ -317,6 +317,14 @@ def gpu_arm(args):
     plain_value = arms["plain"]["value"]
     cyc_m = [c[0] for c in meth["cycles"]]
     plan = meth["plan"]
+    bpc = step_bytes_per_cell(statistics.mean(cyc_m))
+    hbm = 6800.0
+    if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")):
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            hbm = float(json.load(f)["hbm_gbs"])
+    step_roofline = {"bytes_per_cell": bpc, "bytes_per_step": bpc * cells,
+                     "achieved_gbs": bpc * cells / (ms_step * 1e-3) / 1e9,
+                     "frac_of_measured_hbm": bpc * cells / (ms_step * 1e-3) / 1e9 / hbm}
     launches = sum(int(L.aj_kernel_count(ctypes.byref(plan.params), c)) for c in cyc_m)
 
     # ---- e2e: host buffers, H2D of the step's inputs, D2H of its result
@@ -385,6 +393,7 @@ def gpu_arm(args):
                       "converging MG warm-started from the double-FP32 extrapolation",
             "rel_residual_target": 1e-6, "arms": arms,
             "autotuned_level0_tiles": tuned[0] if tuned else None,
+            "step_roofline": step_roofline,
             "plain_mg_value": plain_value, "speedup_vs_plain": value / plain_value,
             "l2": "flushed before every step (256 MiB write outside the timed events)",
             "parallelism": "replicas only" if world > 1 else "single GPU",
@@ -399,6 +408,17 @@ def gpu_arm(args):
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def step_bytes_per_cell(n_cycles, les=True):
+    """Algorithmic bytes per cell of one projection step (FP32, each logical
+    phase reading its inputs and writing its outputs once): RK3 stages
+    20 + 28 + 32 = 80 B, LES 12 B plus 4 B per stage = 24 B, divergence and
+    right-hand side 16 B, projection and boundary rows 24 B, and per V-cycle
+    96 B (two pre and two post sweeps 2 x 12 B each, residual and restriction
+    9 B, prolongation 9 B at the fine level times sum 4^-l = 1.328, plus the
+    coarse solve and the residual norm)."""
+    return 120 + (24 if les else 0) + 96 * n_cycles
 
 
 def roofline(args, plan, state, mask, flush, L):
