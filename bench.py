@@ -186,11 +186,10 @@ def gpu_arm(args):
     from aerojax_gb300 import nn as NNW
     from aerojax_gb300.build import build
 
-    world, rank, local = dist_env()
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", rank=rank, world_size=world)
+    from aerojax_gb300 import replicas
+    world, rank, local = replicas.dist_env()
     torch.cuda.set_device(local)
+    replicas.init()
     build()
     dev = torch.device("cuda", local)
     L = _lib.lib()
@@ -252,19 +251,8 @@ def gpu_arm(args):
             cyc.append((raw.cycles, raw.rel_residual, raw.err))
         return ms, cyc
 
-    def barrier():
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
-        torch.cuda.synchronize()
-
-    def max_over_ranks(x):
-        if world > 1:
-            import torch.distributed as dist
-            t = torch.tensor([x], device=dev, dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            return float(t.item())
-        return x
+    barrier = replicas.barrier
+    max_over_ranks = replicas.max_over_ranks
 
     def soak(plan, bufs, kind, seconds):
         t0 = time.perf_counter()
@@ -305,7 +293,7 @@ def gpu_arm(args):
 
     def arm_summary(r):
         ms = r["ms"] / args.steps
-        return {"value": world * cells / (ms * 1e-3) / 1e6, "ms_per_step": ms,
+        return {"value": replicas.throughput(cells, args.steps, r["ms"], world), "ms_per_step": ms,
                 "mg_cycles_mean": statistics.mean(c[0] for c in r["cycles"]),
                 "rel_residual_max": max(c[1] for c in r["cycles"]),
                 "device_errors": sorted({c[2] for c in r["cycles"]})}
@@ -313,7 +301,7 @@ def gpu_arm(args):
     arms = {k: arm_summary(r) for k, r in results.items()}
     meth = results[head]
     ms_step = meth["ms"] / args.steps
-    value = world * cells / (ms_step * 1e-3) / 1e6
+    value = replicas.throughput(cells, args.steps, meth["ms"], world)
     plain_value = arms["plain"]["value"]
     cyc_m = [c[0] for c in meth["cycles"]]
     plan = meth["plan"]
@@ -368,9 +356,7 @@ def gpu_arm(args):
     roof = roofline(args, plan, meth["bufs"][0], mask, flush, L)
 
     if rank != 0:
-        if world > 1:
-            import torch.distributed as dist
-            dist.destroy_process_group()
+        replicas.finalize()
         return
     cpu = None
     if not args.no_cpu_baseline and not args.quick:
@@ -405,9 +391,7 @@ def gpu_arm(args):
         "clocks": clk,
     }
     print(json.dumps(line))
-    if world > 1:
-        import torch.distributed as dist
-        dist.destroy_process_group()
+    replicas.finalize()
 
 
 def step_bytes_per_cell(n_cycles, les=True):

@@ -25,7 +25,12 @@ def test_autotune_choice(dev):
     r = E.autotune(plan, reps=5)
     assert r["chosen"] in (0, 1, 2)
     assert all(t > 0 for t in r["times_ms"])
-    assert r["times_ms"][r["chosen"]] == min(r["times_ms"])
+    t = r["times_ms"]
+    # the default shape unless another one is 5 % faster
+    if r["chosen"] == 0:
+        assert min(t[1:]) >= 0.95 * t[0] or min(t) == t[0]
+    else:
+        assert t[r["chosen"]] < 0.95 * t[0]
 
 
 def test_ensemble_matches_single_steps(dev):
