@@ -24,6 +24,7 @@ import torch
 from . import _lib
 from ._lib import check, lib
 from .params import StepConfig
+from .params import compute_eps_multiplier
 from .solver import Plan, _stream, get_plan, make_geometry, make_params, run_step
 
 # the architecture table of csrc/aj_nn.cu: (Cin, Cout, relu)
@@ -33,6 +34,9 @@ FEATURES = 3
 # trained weights for the NACA 0012 MAC 2048x512 workload (network grid 256x64)
 WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights",
                        "warmstart_naca0012_2048x512_f8.npz")
+# trained weights for the 4096x2048 three-cylinder workload (network grid 512x256)
+WEIGHTS_TRI = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights",
+                           "warmstart_tri_cylinders_4096x2048_f8.npz")
 
 
 def init_params(seed: int = 0) -> np.ndarray:
@@ -181,28 +185,43 @@ def initial_guess(p1, p2, dt, dt1, n_hist):
     return p1.clone()
 
 
-def generate_snapshots(nx=2048, ny=512, n_geoms=40, steps=500, warmup=2, factor=8, seed=0,
-                       device="cuda", aoa_range=(0.0, 15.0), shift_cells=64, log=None) -> Snapshots:
-    """Runs the solver (extrapolated warm start) on randomly drawn geometries
-    (angle of attack uniform in aoa_range, leading edge shifted uniformly by
-    +-shift_cells at 2048 cells) and records, for every step after the
-    warm-up, the network features of the step's pressure solve (its rhs, the
-    mask and its initial guess) and the target correction (converged p minus
-    the initial guess)."""
-    rng = np.random.default_rng(seed)
-    h, w = nx // factor, ny // factor
-    N = n_geoms * steps
-    x3 = torch.empty((N, h, w, 3), dtype=torch.float32, device=device)
-    tgt = torch.empty((N, h, w), dtype=torch.float32, device=device)
+def tri_case(shift_x_cells, shift_y_cells, device, factor=8, seed=0, nx=4096, ny=2048,
+             warm_start="extrapolate"):
+    """The 4096x2048 three-cylinder (triangle) dynamic-LES workload with the
+    triangle's centre shifted by whole cells (at 4096 cells): the second
+    learned warm start's training family."""
+    from . import configs
+    base = configs.tri_cyl_4096x2048(device=device, nx=nx, ny=ny, seed=seed)
+    c = base["cfg"]
+    lx, ly = base["lx"], base["ly"]
+    D = 64 * c.dx * nx / 4096
+    cx = ((800 + shift_x_cells) * nx // 4096) * lx / (nx - 1)
+    cy = ((ny // 2) + shift_y_cells * ny // 2048) * ly / (ny - 1)
+    eps = compute_eps_multiplier(3000.0) * c.dx
+    mask, sdf = make_geometry("cyl3_tri", nx, ny, lx, ly, (cx, cy, D, 160 * c.dx * nx / 4096),
+                              eps, device)
+    cfg = replace(c, nn_factor=factor, warm_start=warm_start)
+    return dict(cfg=cfg, mask=mask, sdf=sdf, u=base["u"], v=base["v"])
+
+
+def _snapshots_from(cases, n_geoms, steps, warmup, factor, device, log=None) -> Snapshots:
+    """Runs the solver (extrapolated warm start) on each case and records, for
+    every step after the warm-up, the network features of the step's pressure
+    solve (its rhs, the mask and its initial guess) and the target correction
+    (converged p minus the initial guess)."""
+    x3 = tgt = None
     meta = []
     L = lib()
     k = 0
-    for gidx in range(n_geoms):
-        aoa = float(rng.uniform(*aoa_range))
-        shift = int(rng.integers(-shift_cells, shift_cells + 1)) * nx // 2048
-        case = naca_case(nx, ny, aoa, shift, device, factor, seed=seed + gidx)
-        plan = Plan(case["cfg"], device)
-        plan.prepare(case["mask"])
+    for gidx, (case, info) in enumerate(cases):
+        cfg = case["cfg"]
+        nx, ny = cfg.nx, cfg.ny
+        if x3 is None:
+            h, w = nx // factor, ny // factor
+            x3 = torch.empty((n_geoms * steps, h, w, 3), dtype=torch.float32, device=device)
+            tgt = torch.empty((n_geoms * steps, h, w), dtype=torch.float32, device=device)
+        plan = Plan(cfg, device)
+        plan.prepare(case["mask"], case.get("sdf"))
         bufs = [(case["u"].clone(), case["v"].clone(),
                  torch.zeros((nx, ny), dtype=torch.float32, device=device)) for _ in range(2)]
         cur = 0
@@ -211,32 +230,83 @@ def generate_snapshots(nx=2048, ny=512, n_geoms=40, steps=500, warmup=2, factor=
             src, dst = bufs[cur], bufs[1 - cur]
             run_step(plan, src[0], src[1], case["mask"], p_guess=src[2], out=dst)
             dts.append(plan.stats()["dt"])
-            if s >= max(warmup, 2):
+            if s >= max(warmup, 2) and k < x3.shape[0]:
                 p_init = initial_guess(hist[-1], hist[-2], dts[-1], dts[-2], 2)
                 rhs = L.aj_workspace_rhs(ctypes.byref(plan.params), plan.ws.data_ptr())
                 check("aj_nn_features", L.aj_nn_features(
                     ctypes.byref(plan.params), rhs, case["mask"].data_ptr(), p_init.data_ptr(),
                     dst[2].data_ptr(), x3[k].data_ptr(), tgt[k].data_ptr(), plan.ws.data_ptr(),
                     plan.nbytes, _stream(None)))
-                meta.append((aoa, shift, s))
+                meta.append(info + (s,))
                 k += 1
             hist = (hist + [dst[2].clone()])[-2:]
             cur = 1 - cur
+        del plan
         if log:
-            log(f"geometry {gidx + 1}/{n_geoms}: aoa={aoa:.2f} shift={shift} cells")
+            log(f"geometry {gidx + 1}/{n_geoms}: {info}")
     return Snapshots(x3=x3[:k], target=tgt[:k], factor=factor, cfgs=meta)
 
 
+def generate_snapshots(nx=2048, ny=512, n_geoms=40, steps=500, warmup=2, factor=8, seed=0,
+                       device="cuda", aoa_range=(0.0, 15.0), shift_cells=64, log=None) -> Snapshots:
+    """NACA 0012 MAC snapshots: angle of attack uniform in aoa_range, leading
+    edge shifted uniformly by +-shift_cells (at 2048 cells)."""
+    rng = np.random.default_rng(seed)
+
+    def cases():
+        for gidx in range(n_geoms):
+            aoa = float(rng.uniform(*aoa_range))
+            shift = int(rng.integers(-shift_cells, shift_cells + 1)) * nx // 2048
+            yield naca_case(nx, ny, aoa, shift, device, factor, seed=seed + gidx), (aoa, shift)
+    return _snapshots_from(cases(), n_geoms, steps, warmup, factor, device, log)
+
+
+def generate_snapshots_tri(n_geoms=8, steps=250, warmup=2, factor=8, seed=0, device="cuda",
+                           shift_cells=64, nx=4096, ny=2048, log=None) -> Snapshots:
+    """Three-cylinder snapshots: the triangle's centre shifted uniformly by
+    +-shift_cells in x and y."""
+    rng = np.random.default_rng(seed)
+
+    def cases():
+        for gidx in range(n_geoms):
+            sx = int(rng.integers(-shift_cells, shift_cells + 1))
+            sy = int(rng.integers(-shift_cells, shift_cells + 1))
+            yield tri_case(sx, sy, device, factor, seed=seed + gidx, nx=nx, ny=ny), (sx, sy)
+    return _snapshots_from(cases(), n_geoms, steps, warmup, factor, device, log)
+
+
+def _last_layer_slice():
+    """Offsets of the output layer's weights W[3][3][Cin][Cout] and bias in the
+    flat parameter vector."""
+    off = 0
+    for cin, cout, _ in LAYERS[:-1]:
+        off += 9 * cin * cout + cout
+    cin, cout, _ = LAYERS[-1]
+    return off, off + 9 * cin * cout, cin, cout
+
+
 def train(net: WarmStartNet, data: Snapshots, epochs=3, batch=16, lr=1e-3, holdout=0.1, seed=0,
-          log=None):
+          log=None, normalize_target=True):
     """Adam on the MSE of the predicted correction; 10% of the snapshots held
-    out; the parameters of the best held-out epoch are kept.  Returns the
-    per-epoch (train, held-out) losses."""
+    out; the parameters of the best held-out epoch are kept.
+
+    normalize_target: train on target / g, g the RMS of the training targets,
+    then fold g into the output layer's channel 0, so that the network
+    predicts the correction in the features' units whatever its magnitude.
+    If no epoch beats the zero correction on the held-out snapshots, the
+    output layer is zeroed: the warm start then adds nothing (the multigrid
+    judges the network's error and it has none to add).
+    Returns the per-epoch (train, held-out) losses in the targets' units."""
     N, h, w, _ = data.x3.shape
-    g = torch.Generator(device="cpu").manual_seed(seed)
-    perm = torch.randperm(N, generator=g)
+    gen = torch.Generator(device="cpu").manual_seed(seed)
+    perm = torch.randperm(N, generator=gen)
     n_val = max(1, int(round(N * holdout)))
     val_idx, tr_idx = perm[:n_val].to(net.device), perm[n_val:].to(net.device)
+    gain = 1.0
+    if normalize_target:
+        gain = max(float(data.target[tr_idx].pow(2).mean().sqrt()), 1e-30)
+    inv = 1.0 / gain
+    zero_val = float(data.target[val_idx].pow(2).mean())
     hist = []
     best = (float("inf"), net.master.clone())
 
@@ -247,30 +317,43 @@ def train(net: WarmStartNet, data: Snapshots, epochs=3, batch=16, lr=1e-3, holdo
             n = len(b)
             net.expand(data.x3[b].contiguous(), n, h, w)
             y = net.forward(None, n, h, w)
-            loss, _ = net.loss(y, data.target[b].contiguous(), n, h, w)
+            loss, _ = net.loss(y, (data.target[b] * inv).contiguous(), n, h, w)
             tot += float(loss.item()) * n
             cnt += n
-        return tot / max(cnt, 1)
+        return tot / max(cnt, 1) * gain * gain
 
     for ep in range(epochs):
-        order = tr_idx[torch.randperm(len(tr_idx), generator=g).to(net.device)]
+        order = tr_idx[torch.randperm(len(tr_idx), generator=gen).to(net.device)]
         tl, tn = 0.0, 0
         for i in range(0, len(order) - batch + 1, batch):
             b = order[i:i + batch]
             net.expand(data.x3[b].contiguous(), batch, h, w)
             y = net.forward(None, batch, h, w)
-            loss, dy = net.loss(y, data.target[b].contiguous(), batch, h, w)
+            loss, dy = net.loss(y, (data.target[b] * inv).contiguous(), batch, h, w)
             net.backward(dy, batch, h, w)
             net.adam(lr=lr)
             tl += float(loss.item())
             tn += 1
         vl = eval_loss(val_idx)
-        hist.append((tl / max(tn, 1), vl))
+        hist.append((tl / max(tn, 1) * gain * gain, vl))
         if vl < best[0]:
             best = (vl, net.master.clone())
         if log:
-            log(f"epoch {ep + 1}/{epochs}: train {hist[-1][0]:.4e}  held-out {vl:.4e}")
-    net.master.copy_(best[1])
+            log(f"epoch {ep + 1}/{epochs}: train {hist[-1][0]:.4e}  held-out {vl:.4e}  "
+                f"(zero correction {zero_val:.4e})")
+    master = best[1].cpu().numpy().copy()
+    w0, b0, cin, cout = _last_layer_slice()
+    W = master[w0:b0].reshape(3, 3, cin, cout)
+    if best[0] >= zero_val:
+        W[..., 0] = 0.0
+        master[b0] = 0.0
+        if log:
+            log("no epoch beats the zero correction on the held-out snapshots: output layer zeroed")
+    else:
+        W[..., 0] *= gain
+        master[b0] *= gain
+    master[w0:b0] = W.ravel()
+    net.master.copy_(torch.as_tensor(master, device=net.device))
     net.pack()
     return hist
 

@@ -484,21 +484,32 @@ def side_workload(args):
                        "l2": "working set above the L2 size (no flush)"}}))
         return
     from aerojax_gb300 import configs
+    from aerojax_gb300 import nn as NNW
     case = configs.tri_cyl_4096x2048(device=dev)
+    net = NNW.WarmStartNet.load(NNW.WEIGHTS_TRI, device=dev) \
+        if os.path.exists(NNW.WEIGHTS_TRI) else None
     out = {}
-    for arm, warm in (("plain", False), ("extrap", "extrapolate")):
-        plan = aj.get_plan(replace(case["cfg"], warm_start=warm), dev)
+    for arm, warm in (("plain", False), ("extrap", "extrapolate"), ("nn", "extrapolate")):
+        if arm == "nn" and net is None:
+            continue
+        plan = aj.get_plan(replace(case["cfg"], warm_start=warm,
+                                   nn_factor=NN_FACTOR if arm == "nn" else 0), dev)
         plan.prepare(case["mask"], case["sdf"])
         u, v = case["u"].clone(), case["v"].clone()
         p = torch.zeros_like(u)
+
+        def step(u, v, p):
+            if arm == "nn":
+                return NNW.run_step_nn(plan, net, u, v, case["mask"], p)
+            return aj.run_step(plan, u, v, case["mask"], p_guess=p)
         for _ in range(max(3, args.warmup)):
-            u, v, p = aj.run_step(plan, u, v, case["mask"], p_guess=p)
+            u, v, p = step(u, v, p)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(st)
         cyc = []
         for _ in range(args.steps):
-            u, v, p = aj.run_step(plan, u, v, case["mask"], p_guess=p)
+            u, v, p = step(u, v, p)
             cyc.append(plan.stats_buf.clone())
         e1.record(st)
         torch.cuda.synchronize()
@@ -507,10 +518,11 @@ def side_workload(args):
         c = [_lib.AjStats.from_buffer_copy(bytes(x.cpu().numpy().tobytes())).cycles for x in cyc]
         out[arm] = {"value": 4096 * 2048 / (ms * 1e-3) / 1e6, "ms_per_step": ms,
                     "mg_cycles_mean": statistics.mean(c)}
+    head = "nn" if "nn" in out else "extrap"
     print(json.dumps({
         "metric": "Mcell-steps/s, 4096x2048 three-cylinder dynamic-LES step",
-        "value": out["extrap"]["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": out["extrap"]["ms_per_step"],
+        "value": out[head]["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": out[head]["ms_per_step"],
         "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": case["name"], "arms": out,
                    "l2": "working set (~1 GB) above the L2 size (no flush)"}}))

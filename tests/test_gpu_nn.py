@@ -288,8 +288,8 @@ def test_trained_warm_start_gain(dev):
             c.append(st["cycles"])
         cyc[arm] = float(np.mean(c[5:]))
     print("mean V-cycles per step:", cyc, "held-out MSE", float(loss.item()), "zero", zero)
-    # measured on GB300: zero 5.0, prev 3.96, extrap 2.89, nn 3.11 (the
-    # correction removes ~94% of the error energy it sees, but what sets the
+    # measured on GB300: zero 5.0, prev 3.96, extrap 2.89, nn 2.96 (the
+    # correction removes ~95% of the error energy it sees, but what sets the
     # residual after the first V-cycle is error below the 8-cell scale of the
     # network grid, which no coarse correction carries)
     assert cyc["nn"] <= cyc["zero"] - 1.5
