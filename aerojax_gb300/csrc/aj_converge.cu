@@ -195,43 +195,54 @@ __device__ __forceinline__ void cv_sweeps(float* E, const float* R, const CvLvl&
   }
 }
 
-// cell-centred bilinear prolongation of the coarse correction (ghosts:
-// Neumann copies at inlet and walls, outlet ghost g * value)
-__device__ __forceinline__ float cv_prolong(const float* __restrict__ ec, int nc, int mc, float g,
-                                            int gi, int gj) {
-  const int I = gi >> 1, J = gj >> 1;
-  const int Ii = (gi & 1) ? I + 1 : I - 1;
-  int Jj = (gj & 1) ? J + 1 : J - 1;
-  Jj = Jj < 0 ? 0 : (Jj >= mc ? mc - 1 : Jj);
-  const float c0 = ldg(ec + (long)I * mc + J);
-  const float cy = ldg(ec + (long)I * mc + Jj);
-  float cx, cxy;
-  if (Ii < 0) {
-    cx = c0;
-    cxy = cy;
-  } else if (Ii >= nc) {
-    cx = g * c0;
-    cxy = g * cy;
-  } else {
-    cx = ldg(ec + (long)Ii * mc + J);
-    cxy = ldg(ec + (long)Ii * mc + Jj);
+// The coarse cells a tile's cell-centred bilinear prolongation reads, with the
+// ghost rules folded in: row -1 copies row 0 (inlet Neumann), row nc is
+// g * row nc-1 (outlet ghost), columns clamp (wall Neumann).
+template <class TC>
+struct CoarseWin {
+  static constexpr int R = TC::SI / 2 + 3, C = TC::SJ / 2 + 3;
+};
+
+template <class TC>
+__device__ __forceinline__ void cv_load_coarse(float* W, int gi0, int gj0,
+                                               const float* __restrict__ ec, int nc, int mc,
+                                               float g) {
+  using CW = CoarseWin<TC>;
+  const int I0 = (gi0 >> 1) - 1, J0 = (gj0 >> 1) - 1;
+  for (int t = threadIdx.y * blockDim.x + threadIdx.x; t < CW::R * CW::C;
+       t += blockDim.x * blockDim.y) {
+    const int a = t / CW::C, b = t - a * CW::C;
+    int I = I0 + a;
+    const int J = min(max(J0 + b, 0), mc - 1);
+    float f = 1.f;
+    if (I < 0) I = 0;
+    if (I >= nc) {
+      I = nc - 1;
+      f = g;
+    }
+    float v = 0.f;
+    if (I0 + a >= -1 && I0 + a <= nc) v = ldg(ec + (long)I * mc + J);
+    W[t] = f == 1.f ? v : f * v;
   }
-  return (9.f * c0 + 3.f * cx + 3.f * cy + cxy) * (1.f / 16.f);
 }
 
 // tile + halo load: E = e_in + P(ec) (or 0), R = r; each row is read as two
-// coalesced runs of SJ/2 floats
+// coalesced runs of SJ/2 floats.  W (nullable when ZERO_E) holds the coarse
+// window after a cv_load_coarse and a barrier.
 template <class TC, bool ZERO_E>
 __device__ __forceinline__ void cv_load(float* E, float* R, const CvLvl& L, int gi0, int gj0,
                                         const float* __restrict__ r, const float* __restrict__ e_in,
-                                        const float* __restrict__ ec, int nc, int mc, float gc) {
+                                        const float* W) {
   constexpr int SJ = TC::SJ;
+  using CW = CoarseWin<TC>;
   const int tx = threadIdx.x, ty = threadIdx.y;
+  const int I0 = (gi0 >> 1) - 1, J0 = (gj0 >> 1) - 1;
 #pragma unroll
   for (int ti = ty; ti < TC::SI; ti += TC::RG) {
     const int gi = gi0 + ti;
     const bool row_in = (unsigned)gi < (unsigned)L.n;
     const bool row_e = row_in && !ZERO_E && !(L.level == 0 && gi == L.n - 1);
+    const int a = (gi >> 1) - I0, ai = (gi & 1) ? a + 1 : a - 1;
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
       const int tj = tx + q * TC::PAIRS;
@@ -241,7 +252,13 @@ __device__ __forceinline__ void cv_load(float* E, float* R, const CvLvl& L, int 
       if (in) {
         const long k = (long)gi * L.m + gj;
         rr = ldg(r + k);
-        if (row_e) e = ldg(e_in + k) + cv_prolong(ec, nc, mc, gc, gi, gj);
+        if (row_e) {
+          // cell-centred bilinear prolongation (weights 9/16, 3/16, 3/16, 1/16)
+          const int b = (gj >> 1) - J0, bj = (gj & 1) ? b + 1 : b - 1;
+          const float c0 = W[a * CW::C + b], cx = W[ai * CW::C + b];
+          const float cy = W[a * CW::C + bj], cxy = W[ai * CW::C + bj];
+          e = ldg(e_in + k) + (9.f * c0 + 3.f * cx + 3.f * cy + cxy) * (1.f / 16.f);
+        }
       }
       E[ti * SJ + tj] = e;
       R[ti * SJ + tj] = rr;
@@ -250,10 +267,12 @@ __device__ __forceinline__ void cv_load(float* E, float* R, const CvLvl& L, int 
   __syncthreads();
 }
 
-// pre-smoothing from e = 0, residual, 2x2 average onto the coarse rhs
+// pre-smoothing from e = 0, residual, 2x2 average onto the coarse rhs.  On
+// level 0 the residual alternates between two buffers (r0, r1) with the
+// pressure state: *cur selects the one the last iteration wrote.
 template <class TC>
-__global__ void __launch_bounds__(TC::NTH) k_cv_down(CvLvl L, const float* __restrict__ r,
-                                                     float* __restrict__ e_out,
+__global__ void __launch_bounds__(TC::NTH) k_cv_down(CvLvl L, const float* r0, const float* r1,
+                                                     const int* cur, float* __restrict__ e_out,
                                                      float* __restrict__ rc, const int* done) {
   constexpr int SJ = TC::SJ, TI = TC::TI, TJ = TC::TJ;
   if (*done) return;
@@ -262,7 +281,8 @@ __global__ void __launch_bounds__(TC::NTH) k_cv_down(CvLvl L, const float* __res
   const int i0 = blockIdx.y * TI, j0 = blockIdx.x * TJ;
   const int gi0 = i0 - CV_H, gj0 = j0 - CV_H;
   const int tx = threadIdx.x, ty = threadIdx.y;
-  cv_load<TC, true>(E, R, L, gi0, gj0, r, nullptr, nullptr, 0, 0, 0.f);
+  const float* r = (r1 && *cur) ? r1 : r0;
+  cv_load<TC, true>(E, R, L, gi0, gj0, r, nullptr, nullptr);
   cv_sweeps<TC>(E, R, L, gi0, gj0);
   // store e and compute the residual on the tile interior (in place in R)
   for (int ti = CV_H + ty; ti < CV_H + TI; ti += TC::RG) {
@@ -311,7 +331,10 @@ __global__ void __launch_bounds__(TC::NTH) k_cv_up(CvLvl L, const float* __restr
   const int i0 = blockIdx.y * TI, j0 = blockIdx.x * TJ;
   const int gi0 = i0 - CV_H, gj0 = j0 - CV_H;
   const int tx = threadIdx.x, ty = threadIdx.y;
-  cv_load<TC, false>(E, R, L, gi0, gj0, r, e_in, ec, nc, mc, gc);
+  __shared__ float W[CoarseWin<TC>::R * CoarseWin<TC>::C];
+  cv_load_coarse<TC>(W, gi0, gj0, ec, nc, mc, gc);
+  __syncthreads();
+  cv_load<TC, false>(E, R, L, gi0, gj0, r, e_in, W);
   cv_sweeps<TC>(E, R, L, gi0, gj0);
   for (int ti = CV_H + ty; ti < CV_H + TI; ti += TC::RG) {
     const int gi = gi0 + ti;
@@ -363,7 +386,8 @@ __device__ void cv_check_body(DevScalars* sc, const CvCheck& ck) {
   }
 }
 
-// the pressure state: N hi values followed by N lo values
+// a ping-pong pair: the pressure state (each buffer N hi values followed by N
+// lo values) or the level-0 residual (N floats each)
 struct PState {
   float* a;   // buffer 0
   float* b;   // buffer 1
@@ -371,12 +395,15 @@ struct PState {
 
 // level 0: e + P(e_coarse), post-smoothing, p += e (double-FP32, ping-pong), the
 // residual of the reference operator for the next iteration (double-FP32), its
-// FP64 norm, and the convergence test in the last block to finish
+// FP64 norm, and the convergence test in the last block to finish.  The
+// residual ping-pongs with the pressure (rs.a pairs with ps.a): a block reads
+// the current residual over its tile and halo while its neighbours write the
+// next one, so the two must never share a buffer.
 template <class TC>
 __global__ void __launch_bounds__(TC::NTH) k_cv_up0(
-    CvLvl L, const float* __restrict__ r, const float* __restrict__ e_in,
+    CvLvl L, PState rs, const float* __restrict__ e_in,
     const float* __restrict__ ec, int nc, int mc, float gc, PState ps, const float* __restrict__ b,
-    float* __restrict__ r_next, DevScalars* sc, DfCoef co, CvCheck ck, int profile) {
+    DevScalars* sc, DfCoef co, CvCheck ck, int profile) {
   constexpr int TI = TC::TI, TJ = TC::TJ, SJ = TC::SJ;
   constexpr int PI = TI + 2, PJ = TJ + 2;
   static_assert(PJ <= 2 * TC::PAIRS, "the pressure window must fit two column runs");
@@ -394,7 +421,12 @@ __global__ void __launch_bounds__(TC::NTH) k_cv_up0(
   const int cur = sc->pcur;
   const float* __restrict__ pin = cur ? ps.b : ps.a;
   float* __restrict__ pout = cur ? ps.a : ps.b;
-  cv_load<TC, false>(E, R, L, gi0, gj0, r, e_in, ec, nc, mc, gc);
+  const float* __restrict__ r = cur ? rs.b : rs.a;
+  float* __restrict__ r_next = cur ? rs.a : rs.b;
+  __shared__ float W[CoarseWin<TC>::R * CoarseWin<TC>::C];
+  cv_load_coarse<TC>(W, gi0, gj0, ec, nc, mc, gc);
+  __syncthreads();
+  cv_load<TC, false>(E, R, L, gi0, gj0, r, e_in, W);
   cv_sweeps<TC>(E, R, L, gi0, gj0);
   // new pressure on the interior and one cell around it
   for (int pi = ty; pi < PI; pi += TC::RG) {
@@ -1058,16 +1090,18 @@ static dim3 tile_threads() {
 template <class TC>
 static void level0_down(const CvLvl& c, const Layout& L, void* ws, const int* done,
                         cudaStream_t st) {
+  const DevScalars* sc = at<DevScalars>(ws, 0);
   k_cv_down<TC><<<tiles<TC>(c), tile_threads<TC>(), 0, st>>>(
-      c, at<float>(ws, L.B[0]), at<float>(ws, L.X[0]), at<float>(ws, L.B[1]), done);
+      c, at<float>(ws, L.B[0]), at<float>(ws, L.T[0]), &sc->pcur, at<float>(ws, L.X[0]),
+      at<float>(ws, L.B[1]), done);
 }
 template <class TC>
 static void level0_up(const AjStepParams& p, const CvLvl& c, const Layout& L, void* ws,
                       DevScalars* sc, const CvCheck& ck, int profile, cudaStream_t st) {
   k_cv_up0<TC><<<tiles<TC>(c), tile_threads<TC>(), 0, st>>>(
-      c, at<float>(ws, L.B[0]), at<float>(ws, L.X[0]), at<float>(ws, L.T[1]), L.ln[1], L.lm[1],
-      (float)ghost_factor(1), pstate(L, ws), at<float>(ws, L.b0), at<float>(ws, L.B[0]), sc,
-      df_coef(1.0 / (p.dx * p.dx), 1.0 / (p.dy * p.dy)), ck, profile);
+      c, PState{at<float>(ws, L.B[0]), at<float>(ws, L.T[0])}, at<float>(ws, L.X[0]),
+      at<float>(ws, L.T[1]), L.ln[1], L.lm[1], (float)ghost_factor(1), pstate(L, ws),
+      at<float>(ws, L.b0), sc, df_coef(1.0 / (p.dx * p.dx), 1.0 / (p.dy * p.dy)), ck, profile);
 }
 static void level0_down_v(int v, const CvLvl& c, const Layout& L, void* ws, const int* done,
                           cudaStream_t st) {
@@ -1094,7 +1128,8 @@ static void cv_body(const AjStepParams& p, const Layout& L, void* ws,
       level0_down_v(tile_variant(p.nx, p.ny), c, L, ws, done, st);
     else
       k_cv_down<T1><<<tiles<T1>(c), tile_threads<T1>(), 0, st>>>(
-          c, at<float>(ws, L.B[l]), at<float>(ws, L.X[l]), at<float>(ws, L.B[l + 1]), done);
+          c, at<float>(ws, L.B[l]), nullptr, done, at<float>(ws, L.X[l]), at<float>(ws, L.B[l + 1]),
+          done);
   }
   if (L.ld > 0) {
     direct_launch(direct_args(p, L, ws, done), st);

@@ -35,7 +35,10 @@ def test_autotune_choice(dev):
 
 def test_ensemble_matches_single_steps(dev):
     """Six instances of mixed grid sizes, five steps: the batched graph gives
-    every instance the same fields as stepping it alone."""
+    every instance bit for bit the fields of stepping it alone.  The branches
+    run concurrently, so block scheduling differs from the standalone launch:
+    any kernel whose blocks read what their neighbours write in the same
+    launch shows up here as a mismatch."""
     from aerojax_gb300 import ensemble as E
     from aerojax_gb300.solver import Plan, run_step
     specs = E.draw_instances(6, seed=3)
@@ -53,9 +56,9 @@ def test_ensemble_matches_single_steps(dev):
         for _ in range(5):
             u, v, p = run_step(plan, u, v, mask, p_guess=p)
         ue, ve, pe = ens.state(k)
-        assert float((ue - u).abs().max()) <= 1e-6, k
-        assert float((ve - v).abs().max()) <= 1e-6, k
-        assert float((pe - p).abs().max()) <= 1e-6 * max(1.0, float(p.abs().max())), k
+        assert torch.equal(ue, u), (k, float((ue - u).abs().max()))
+        assert torch.equal(ve, v), (k, float((ve - v).abs().max()))
+        assert torch.equal(pe, p), (k, float((pe - p).abs().max()))
 
 
 def test_full_ensemble_steps(dev):
