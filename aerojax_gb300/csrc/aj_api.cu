@@ -59,6 +59,15 @@ bool eager_mode() {
   return v == 1;
 }
 
+bool pdl_enabled() {
+  static int v = -1;
+  if (v < 0) {
+    const char* e = getenv("AEROJAX_PDL");
+    v = (e && e[0] == '0') ? 0 : 1;
+  }
+  return v == 1;
+}
+
 int eager_unroll(int max_cycles) {
   const char* e = getenv("AEROJAX_UNROLL");
   int n = e ? atoi(e) : max_cycles;

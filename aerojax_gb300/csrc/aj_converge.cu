@@ -274,6 +274,7 @@ template <class TC>
 __global__ void __launch_bounds__(TC::NTH) k_cv_down(CvLvl L, const float* r0, const float* r1,
                                                      const int* cur, float* __restrict__ e_out,
                                                      float* __restrict__ rc, const int* done) {
+  pdl_wait();
   constexpr int SJ = TC::SJ, TI = TC::TI, TJ = TC::TJ;
   if (*done) return;
   __shared__ float E[TC::NT];
@@ -324,6 +325,7 @@ __global__ void __launch_bounds__(TC::NTH) k_cv_up(CvLvl L, const float* __restr
                                                    const float* __restrict__ ec, int nc, int mc,
                                                    float gc, float* __restrict__ e_out,
                                                    const int* done) {
+  pdl_wait();
   constexpr int SJ = TC::SJ, TI = TC::TI, TJ = TC::TJ;
   if (*done) return;
   __shared__ float E[TC::NT];
@@ -404,6 +406,7 @@ __global__ void __launch_bounds__(TC::NTH) k_cv_up0(
     CvLvl L, PState rs, const float* __restrict__ e_in,
     const float* __restrict__ ec, int nc, int mc, float gc, PState ps, const float* __restrict__ b,
     DevScalars* sc, DfCoef co, CvCheck ck, int profile) {
+  pdl_wait();
   constexpr int TI = TC::TI, TJ = TC::TJ, SJ = TC::SJ;
   constexpr int PI = TI + 2, PJ = TJ + 2;
   static_assert(PJ <= 2 * TC::PAIRS, "the pressure window must fit two column runs");
@@ -572,6 +575,7 @@ __device__ __forceinline__ void blk_sweeps(float* E, const float* R, int n, int 
 // coarsest grid, its FP64 dense solve, prolongation and post-smoothing back
 // to level lc.  Replaces 2 (D - lc) launches of the tile kernels by one.
 __global__ void __launch_bounds__(CV_BLOCK_THREADS) k_cv_block(CvBlock a) {
+  pdl_wait();
   if (*a.done) return;
   extern __shared__ __align__(16) float smf[];
   // level arrays are addressed from smf directly so that every access is a
@@ -731,6 +735,7 @@ int converge_direct_level(const Layout& L) {
 constexpr int CV_DT = 32;
 constexpr int CV_DK = CV_DIRECT_MAX_M + 1;
 __global__ void __launch_bounds__(256) k_cv_dfwd(CvDirect a) {
+  pdl_wait();
   if (*a.done) return;
   __shared__ float Cs[CV_DT][CV_DK];
   __shared__ float Rs[CV_DT][CV_DK];
@@ -763,6 +768,7 @@ __global__ void __launch_bounds__(256) k_cv_dfwd(CvDirect a) {
 // one block per cosine mode k: parallel cyclic reduction of
 // (ax Tx + ay lambda_k) ehat_k = rhat_k, n unknowns along x
 __global__ void __launch_bounds__(1024) k_cv_dpcr(CvDirect a) {
+  pdl_wait();
   if (*a.done) return;
   extern __shared__ __align__(16) float sh[];
   const int n = a.n, k = blockIdx.x;
@@ -822,6 +828,7 @@ __global__ void __launch_bounds__(1024) k_cv_dpcr(CvDirect a) {
 // operand panels staged whole; thread (tx, ty) owns j = j0 + tx and the rows
 // i0 + ty + 8q
 __global__ void __launch_bounds__(256) k_cv_dbwd(CvDirect a) {
+  pdl_wait();
   if (*a.done) return;
   __shared__ float Es[CV_DIRECT_MAX_M][CV_DT + 1];
   __shared__ float Cs[CV_DIRECT_MAX_M][CV_DT + 1];
@@ -850,9 +857,9 @@ __global__ void __launch_bounds__(256) k_cv_dbwd(CvDirect a) {
 }
 
 static void direct_launch(const CvDirect& d, cudaStream_t st) {
-  k_cv_dfwd<<<dim3(cdiv(d.n, CV_DT), cdiv(d.m, CV_DT)), dim3(CV_DT, 8), 0, st>>>(d);
-  k_cv_dpcr<<<d.m, cdiv(d.n, 32) * 32, 8 * d.n * sizeof(float), st>>>(d);
-  k_cv_dbwd<<<dim3(cdiv(d.m, CV_DT), cdiv(d.n, CV_DT)), dim3(CV_DT, 8), 0, st>>>(d);
+  launch_pdl(true, k_cv_dfwd, dim3(cdiv(d.n, CV_DT), cdiv(d.m, CV_DT)), dim3(CV_DT, 8), 0, st, d);
+  launch_pdl(true, k_cv_dpcr, dim3(d.m), dim3(cdiv(d.n, 32) * 32), 8 * d.n * sizeof(float), st, d);
+  launch_pdl(true, k_cv_dbwd, dim3(cdiv(d.m, CV_DT), cdiv(d.n, CV_DT)), dim3(CV_DT, 8), 0, st, d);
 }
 
 static CvDirect direct_args(const AjStepParams& p, const Layout& L, void* ws, const int* done);
@@ -890,6 +897,7 @@ __device__ __forceinline__ HistView hist_view(const DevScalars* sc) {
 __global__ void __launch_bounds__(256) k_cv_init(const float* __restrict__ p0,
                                                  float* __restrict__ ps, int n, int m, CvHist hs,
                                                  const DevScalars* sc) {
+  pdl_wait();
   const long N = (long)n * m;
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= m) return;
@@ -926,6 +934,7 @@ __global__ void __launch_bounds__(256) k_cv_resid(const float* __restrict__ ps,
                                                   const float* __restrict__ b,
                                                   float* __restrict__ r, int n, int m, DfCoef co,
                                                   DevScalars* sc, double rtol) {
+  pdl_wait();
   const long N = (long)n * m;
   const df ax{co.axh, co.axl}, ay{co.ayh, co.ayl};
   float acc = 0.f, accb = 0.f;
@@ -997,6 +1006,7 @@ __global__ void __launch_bounds__(256) k_cv_resid(const float* __restrict__ ps,
 // next solve's k_cv_resid makes it the latest); thread 0 files the statistics
 __global__ void k_cv_out(PState ps, DevScalars* sc, float* __restrict__ p, long N, float* hist,
                          AjStats* stats) {
+  pdl_wait();
   long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
   const float* src = sc->pcur ? ps.b : ps.a;
   if (k < N) {
@@ -1091,17 +1101,18 @@ template <class TC>
 static void level0_down(const CvLvl& c, const Layout& L, void* ws, const int* done,
                         cudaStream_t st) {
   const DevScalars* sc = at<DevScalars>(ws, 0);
-  k_cv_down<TC><<<tiles<TC>(c), tile_threads<TC>(), 0, st>>>(
-      c, at<float>(ws, L.B[0]), at<float>(ws, L.T[0]), &sc->pcur, at<float>(ws, L.X[0]),
-      at<float>(ws, L.B[1]), done);
+  launch_pdl(true, k_cv_down<TC>, dim3(tiles<TC>(c)), dim3(tile_threads<TC>()), 0, st, c,
+             at<float>(ws, L.B[0]), at<float>(ws, L.T[0]), &sc->pcur, at<float>(ws, L.X[0]),
+             at<float>(ws, L.B[1]), done);
 }
 template <class TC>
 static void level0_up(const AjStepParams& p, const CvLvl& c, const Layout& L, void* ws,
                       DevScalars* sc, const CvCheck& ck, int profile, cudaStream_t st) {
-  k_cv_up0<TC><<<tiles<TC>(c), tile_threads<TC>(), 0, st>>>(
-      c, PState{at<float>(ws, L.B[0]), at<float>(ws, L.T[0])}, at<float>(ws, L.X[0]),
-      at<float>(ws, L.T[1]), L.ln[1], L.lm[1], (float)ghost_factor(1), pstate(L, ws),
-      at<float>(ws, L.b0), sc, df_coef(1.0 / (p.dx * p.dx), 1.0 / (p.dy * p.dy)), ck, profile);
+  launch_pdl(true, k_cv_up0<TC>, dim3(tiles<TC>(c)), dim3(tile_threads<TC>()), 0, st, c,
+             PState{at<float>(ws, L.B[0]), at<float>(ws, L.T[0])}, at<float>(ws, L.X[0]),
+             at<float>(ws, L.T[1]), L.ln[1], L.lm[1], (float)ghost_factor(1), pstate(L, ws),
+             at<float>(ws, L.b0), sc, df_coef(1.0 / (p.dx * p.dx), 1.0 / (p.dy * p.dy)), ck,
+             profile);
 }
 static void level0_down_v(int v, const CvLvl& c, const Layout& L, void* ws, const int* done,
                           cudaStream_t st) {
@@ -1127,9 +1138,9 @@ static void cv_body(const AjStepParams& p, const Layout& L, void* ws,
     if (l == 0)
       level0_down_v(tile_variant(p.nx, p.ny), c, L, ws, done, st);
     else
-      k_cv_down<T1><<<tiles<T1>(c), tile_threads<T1>(), 0, st>>>(
-          c, at<float>(ws, L.B[l]), nullptr, done, at<float>(ws, L.X[l]), at<float>(ws, L.B[l + 1]),
-          done);
+      launch_pdl(true, k_cv_down<T1>, dim3(tiles<T1>(c)), dim3(tile_threads<T1>()), 0, st, c,
+                 at<float>(ws, L.B[l]), nullptr, done, at<float>(ws, L.X[l]),
+                 at<float>(ws, L.B[l + 1]), done);
   }
   if (L.ld > 0) {
     direct_launch(direct_args(p, L, ws, done), st);
@@ -1138,9 +1149,9 @@ static void cv_body(const AjStepParams& p, const Layout& L, void* ws,
   }
   for (int l = lc - 1; l >= 1; --l) {
     CvLvl c = cv_level(p, L, l);
-    k_cv_up<T1><<<tiles<T1>(c), tile_threads<T1>(), 0, st>>>(
-        c, at<float>(ws, L.B[l]), at<float>(ws, L.X[l]), at<float>(ws, L.T[l + 1]), L.ln[l + 1],
-        L.lm[l + 1], (float)ghost_factor(l + 1), at<float>(ws, L.T[l]), done);
+    launch_pdl(true, k_cv_up<T1>, dim3(tiles<T1>(c)), dim3(tile_threads<T1>()), 0, st, c,
+               at<float>(ws, L.B[l]), at<float>(ws, L.X[l]), at<float>(ws, L.T[l + 1]), L.ln[l + 1],
+               L.lm[l + 1], (float)ghost_factor(l + 1), at<float>(ws, L.T[l]), done);
   }
   CvLvl c0 = cv_level(p, L, 0);
   CvCheck ck{p.mg_rtol, p.max_cycles, use_handle, h};
@@ -1161,14 +1172,15 @@ int converge_solve(const AjStepParams& p, const Layout& L, void* ws, const float
   const dim3 rgrid(cdiv(p.ny, 256), cdiv(p.nx, CV_ROWS));
   const bool extrap = p.warm_start == AJ_WARM_EXTRAPOLATE && L.hist;
   CvHist hs{extrap ? at<float>(ws, L.hist) : nullptr, N};
-  k_cv_init<<<rgrid, 256, 0, st>>>(p.warm_start ? p0 : nullptr, ps.a, p.nx, p.ny, hs, sc);
+  launch_pdl(true, k_cv_init, dim3(rgrid), dim3(256), 0, st, p.warm_start ? p0 : nullptr, ps.a,
+             p.nx, p.ny, hs, sc);
   if (nn && nn->packed) {
     const int rc = nn_correct_state(p, L, ws, at<float>(ws, L.b0), *nn, ps.a, st);
     if (rc != AJ_OK) return rc;
   }
-  k_cv_resid<<<rgrid, 256, 0, st>>>(ps.a, at<float>(ws, L.b0), at<float>(ws, L.B[0]), p.nx, p.ny,
-                                    df_coef(1.0 / (p.dx * p.dx), 1.0 / (p.dy * p.dy)), sc,
-                                    p.mg_rtol);
+  launch_pdl(true, k_cv_resid, dim3(rgrid), dim3(256), 0, st, ps.a, at<float>(ws, L.b0),
+             at<float>(ws, L.B[0]), p.nx, p.ny, df_coef(1.0 / (p.dx * p.dx), 1.0 / (p.dy * p.dy)),
+             sc, p.mg_rtol);
 
   cudaStreamCaptureStatus cs;
   unsigned long long id;
@@ -1210,8 +1222,8 @@ int converge_solve(const AjStepParams& p, const Layout& L, void* ws, const float
     cudaGraph_t out;
     if (cudaStreamEndCapture(side, &out) != cudaSuccess) return AJ_ERR_CUDA;
   }
-  k_cv_out<<<cdiv(N, 256), 256, 0, st>>>(ps, sc, pout, N, extrap ? at<float>(ws, L.hist) : nullptr,
-                                         stats);
+  launch_pdl(true, k_cv_out, dim3(cdiv(N, 256)), dim3(256), 0, st, ps, sc, pout, N,
+             extrap ? at<float>(ws, L.hist) : nullptr, stats);
   return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
 }
 

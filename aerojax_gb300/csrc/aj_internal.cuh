@@ -113,6 +113,36 @@ __device__ __forceinline__ void block_sum_atomic(double v, double* dst) {
   __syncthreads();
 }
 
+// ------------------------------------------------------------------ dependent launch
+// Programmatic dependent launch: a kernel started with launch_pdl may be
+// scheduled as its predecessor on the stream drains (the launch latency
+// overlaps the predecessor's tail; ~5 us per 2048x512 step).  It must execute
+// pdl_wait() - which returns once the predecessor grid has completed and its
+// writes are visible - before it reads or writes anything a predecessor
+// touches, on every path (early returns included), so that its own completion
+// still implies its predecessors'.  A no-op in a kernel launched normally.
+// (Early triggers, griddepcontrol.launch_dependents at the start of the
+// network's convolutions so that the next layer stages its weights sooner,
+// measured slower and are not used.)
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+// AEROJAX_PDL=0 turns dependent launches off (read once)
+bool pdl_enabled();
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(bool pdl, void (*kernel)(KArgs...), dim3 grid, dim3 block,
+                              size_t smem, cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = (pdl && pdl_enabled()) ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 // ------------------------------------------------------------------ launchers
 // predictor (aj_predictor.cu)
 int launch_predictor(const AjStepParams& p, const Layout& L, void* ws, const float* u,

@@ -125,6 +125,9 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv3x3(const float* __restric
     }
     cp_async_commit();
   }
+  // the weights do not depend on the previous layer: staged before the wait
+  // for the previous layer's output
+  pdl_wait();
   {  // the halo tile, FP32, zeros outside the image
     constexpr int C4 = CIN / 4;
     for (int e = tid; e < CT_HALO * C4; e += CONV_THREADS) {
@@ -233,12 +236,12 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv3x3(const float* __restric
 template <int CIN, int NT>
 static void conv_launch(const float* X, int N, int H, int W, int Cout, const __nv_bfloat16* WT,
                         const float* bias, float* Y, int relu, float* Yp, const float* Xc,
-                        cudaStream_t st) {
+                        cudaStream_t st, bool pdl) {
   using S = ConvSmem<CIN, NT>;
   const int tiles = ((W + CT - 1) / CT) * ((H + CT - 1) / CT) * N;
   dim3 grid(tiles, Cout / S::BN);
-  k_conv3x3<CIN, NT><<<grid, CONV_THREADS, S::bytes, st>>>(X, N, H, W, Cout, WT, bias, Y, relu,
-                                                            Yp, Xc);
+  launch_pdl(pdl, k_conv3x3<CIN, NT>, grid, dim3(CONV_THREADS), S::bytes, st, X, N, H, W, Cout,
+             WT, bias, Y, relu, Yp, Xc);
 }
 
 template <int CIN, int NT>
@@ -261,7 +264,7 @@ static void conv_attrs() {
 template <int CIN>
 static int conv_cin(const float* X, int N, int H, int W, int Cout, const __nv_bfloat16* WT,
                     const float* bias, float* Y, int relu, float* Yp, const float* Xc,
-                    cudaStream_t st) {
+                    cudaStream_t st, bool pdl) {
   // 32 output channels per block, or 16 when that leaves fewer blocks than
   // SMs (the small grids of the deep layers are latency-bound: more, lighter
   // blocks load their weights sooner)
@@ -272,8 +275,8 @@ static int conv_cin(const float* X, int N, int H, int W, int Cout, const __nv_bf
     case 32:
     case 64:
     case 128:
-      if (narrow) conv_launch<CIN, 2>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, Xc, st);
-      else conv_launch<CIN, 4>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, Xc, st);
+      if (narrow) conv_launch<CIN, 2>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, Xc, st, pdl);
+      else conv_launch<CIN, 4>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, Xc, st, pdl);
       break;
     default: return AJ_ERR_PARAM;
   }
@@ -282,15 +285,17 @@ static int conv_cin(const float* X, int N, int H, int W, int Cout, const __nv_bf
 
 // Y = conv(X, WT) (+ bias, ReLU); WT[tap][Cout][Cin] BF16; Yp (nullable,
 // H and W even) receives the 2x2 average pool of Y; with Xc (nullable) the
-// input is up2(Xc) + X
+// input is up2(Xc) + X.  pdl: dependent launch (the weights WT must be
+// complete before the chain of dependent launches started)
 static int conv3x3(const float* X, int N, int H, int W, int Cin, int Cout,
                    const __nv_bfloat16* WT, const float* bias, float* Y, int relu,
-                   cudaStream_t st, float* Yp = nullptr, const float* Xc = nullptr) {
+                   cudaStream_t st, float* Yp = nullptr, const float* Xc = nullptr,
+                   bool pdl = false) {
   switch (Cin) {
-    case 16: return conv_cin<16>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, Xc, st);
-    case 32: return conv_cin<32>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, Xc, st);
-    case 64: return conv_cin<64>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, Xc, st);
-    case 128: return conv_cin<128>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, Xc, st);
+    case 16: return conv_cin<16>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, Xc, st, pdl);
+    case 32: return conv_cin<32>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, Xc, st, pdl);
+    case 64: return conv_cin<64>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, Xc, st, pdl);
+    case 128: return conv_cin<128>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, Xc, st, pdl);
     default: return AJ_ERR_PARAM;
   }
 }
@@ -582,10 +587,11 @@ static inline unsigned ew_blocks(long T) { return cdiv(T, 256); }
 int nn_forward(int n, int h, int w, const NnW& W, const NnActs& A, cudaStream_t st,
                bool keep = true) {
   const int H0 = h, W0 = w, H1 = h / 2, W1 = w / 2, H2 = h / 4, W2 = w / 4, H3 = h / 8, W3 = w / 8;
+  // inference launches the convolutions as one chain of dependent launches
   auto conv = [&](int l, const float* in, float* out, int H, int Wd, float* pooled = nullptr,
                   const float* coarse = nullptr) {
     return conv3x3(in, n, H, Wd, kLayers[l].cin, kLayers[l].cout, W.wf(l), W.bias(l), out,
-                   kLayers[l].relu, st, pooled, coarse);
+                   kLayers[l].relu, st, pooled, coarse, !keep);
   };
   int rc = AJ_OK;
   rc |= conv(E0A, A.x, A.a0, H0, W0);
@@ -680,6 +686,7 @@ __global__ void __launch_bounds__(256) k_nn_feat(const float* __restrict__ b,
                                                  const float* __restrict__ mask,
                                                  const float* __restrict__ pp, int nx, int ny,
                                                  int F, float ax, float ay, float* __restrict__ x) {
+  pdl_wait();
   __shared__ float red[3][8][32];
   const int lane = threadIdx.x, row = threadIdx.y;
   const int j = blockIdx.x * 32 + lane, i = blockIdx.y * 8 + row;
@@ -734,6 +741,7 @@ __global__ void __launch_bounds__(256) k_nn_feat(const float* __restrict__ b,
 constexpr int NN_SCALE_BLOCKS = 32;
 __global__ void __launch_bounds__(512) k_nn_scale(const float* __restrict__ x, long cells,
                                                   DevScalars* sc, double lmin2) {
+  pdl_wait();
   float sr = 0.f, sp = 0.f;
   const long stride = (long)gridDim.x * blockDim.x;
 #pragma unroll 4
@@ -765,6 +773,7 @@ __global__ void __launch_bounds__(512) k_nn_scale(const float* __restrict__ x, l
 // normalise channels 0 and 2 in place; optionally copy the 3 features out
 __global__ void k_nn_norm(float* __restrict__ x, float* __restrict__ x3, long cells,
                           const DevScalars* sc) {
+  pdl_wait();
   const long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (c >= cells) return;
   const float ir = (float)(1.0 / sc->nn_rms_r), ip = (float)(1.0 / sc->nn_rms_p);
@@ -799,6 +808,7 @@ __global__ void k_nn_target(const float* __restrict__ pt, const float* __restric
 // outlet row stays pinned at 0
 __global__ void k_nn_apply(const float* __restrict__ y, int nx, int ny, int F,
                            float* __restrict__ state, const DevScalars* sc) {
+  pdl_wait();
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= nx - 1 || j >= ny) return;
@@ -835,16 +845,17 @@ __global__ void k_nn_expand(const float* __restrict__ x3, float* __restrict__ x1
 // features (+ optional dataset copy and target) for one step's pressure solve
 int nn_features(const AjStepParams& p, void* ws, const float* b, const float* mask,
                 const float* pp, const float* pt, float* x16, float* x3, float* target,
-                cudaStream_t st) {
+                cudaStream_t st, bool pdl) {
   const int F = p.nn_factor, h = p.nx / F, w = p.ny / F;
   DevScalars* sc = at<DevScalars>(ws, 0);
   dim3 blk(32, 8), grd(cdiv(w, 32), cdiv(h, 8));
-  k_nn_feat<<<dim3(cdiv(p.ny, 32), cdiv(p.nx, 8)), blk, 0, st>>>(
-      b, mask, pp, p.nx, p.ny, F, (float)(1.0 / (p.dx * p.dx)), (float)(1.0 / (p.dy * p.dy)),
-      x16);
+  launch_pdl(pdl, k_nn_feat, dim3(cdiv(p.ny, 32), cdiv(p.nx, 8)), blk, 0, st, b, mask, pp, p.nx,
+             p.ny, F, (float)(1.0 / (p.dx * p.dx)), (float)(1.0 / (p.dy * p.dy)), x16);
   const double lx = p.nx * p.dx, ly = p.ny * p.dy, lmin = lx < ly ? lx : ly;
-  k_nn_scale<<<NN_SCALE_BLOCKS, 512, 0, st>>>(x16, (long)h * w, sc, lmin * lmin);
-  k_nn_norm<<<cdiv((long)h * w, 256), 256, 0, st>>>(x16, x3, (long)h * w, sc);
+  launch_pdl(pdl, k_nn_scale, dim3(NN_SCALE_BLOCKS), dim3(512), 0, st, x16, (long)h * w, sc,
+             lmin * lmin);
+  launch_pdl(pdl, k_nn_norm, dim3(cdiv((long)h * w, 256)), dim3(256), 0, st, x16, x3,
+             (long)h * w, (const DevScalars*)sc);
   if (pt && target) k_nn_target<<<grd, blk, 0, st>>>(pt, pp, p.nx, p.ny, F, target, sc);
   return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
 }
@@ -857,13 +868,16 @@ int nn_correct_state(const AjStepParams& p, const Layout& L, void* ws, const flo
   const int F = p.nn_factor, h = p.nx / F, w = p.ny / F;
   if (F <= 0 || !L.nn_act) return AJ_ERR_PARAM;
   NnActs A = act_layout(1, h, w, at<char>(ws, L.nn_act));
-  int rc = nn_features(p, ws, b, nn.mask, state, nullptr, A.x, nullptr, nullptr, st);
+  // features, network and correction: one chain of dependent launches (the
+  // packed weights were written before the step began)
+  int rc = nn_features(p, ws, b, nn.mask, state, nullptr, A.x, nullptr, nullptr, st, true);
   if (rc != AJ_OK) return rc;
   NnW W{reinterpret_cast<const __nv_bfloat16*>(nn.packed), nn.master};
   rc = nn_forward(1, h, w, W, A, st, false);
   if (rc != AJ_OK) return rc;
   dim3 blk(32, 8), grd(cdiv(p.ny, 32), cdiv(p.nx, 8));
-  k_nn_apply<<<grd, blk, 0, st>>>(A.y, p.nx, p.ny, F, state, at<DevScalars>(ws, 0));
+  launch_pdl(true, k_nn_apply, grd, blk, 0, st, (const float*)A.y, p.nx, p.ny, F, state,
+             (const DevScalars*)at<DevScalars>(ws, 0));
   return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
 }
 
@@ -965,7 +979,7 @@ int32_t aj_nn_features(const AjStepParams* prm, const float* b, const float* mas
   const int F = prm->nn_factor;
   NnActs A = act_layout(1, prm->nx / F, prm->ny / F, at<char>(ws, L.nn_act));
   return nn_features(*prm, ws, b, mask, p_prev, p_true, A.x, x3_out, target_out,
-                     (cudaStream_t)stream);
+                     (cudaStream_t)stream, false);
 }
 
 int32_t aj_nn_adam(float* master, const float* grad, float* m, float* v, int32_t step, float lr,

@@ -42,12 +42,14 @@ int launch_chi(const AjStepParams& p, const Layout& L, void* ws, const float* ma
 
 // ============================================================ dt
 __global__ void k_set_dt(DevScalars* sc, float dt, float dtc) {
+  pdl_wait();
   sc->dt = dt;
   sc->dt_corr = dtc > 0.f ? dtc : dt;
 }
 
 int launch_set_dt(const AjStepParams& p, void* ws, cudaStream_t st) {
-  k_set_dt<<<1, 1, 0, st>>>(at<DevScalars>(ws, 0), (float)p.dt, (float)p.dt_correction);
+  launch_pdl(true, k_set_dt, dim3(1), dim3(1), 0, st, at<DevScalars>(ws, 0), (float)p.dt,
+             (float)p.dt_correction);
   return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
 }
 
@@ -56,6 +58,7 @@ int launch_set_dt(const AjStepParams& p, void* ws, cudaStream_t st) {
 __global__ void k_cfl(const float* __restrict__ u, const float* __restrict__ v, long nu_,
                       long nv_, int mac, DevScalars* sc, float* dt_out, double h, double nu,
                       double cfl, double dt_min, double dt_max, float dtc_host) {
+  pdl_wait();
   float m = 0.f;
   long stride = (long)gridDim.x * blockDim.x;
   long n = nu_ > nv_ ? nu_ : nv_;
@@ -108,9 +111,9 @@ int launch_cfl(const AjStepParams& p, void* ws, const float* u, const float* v, 
   unsigned blocks = cdiv(n, 256 * 8);
   if (blocks > 1216) blocks = 1216;
   if (blocks < 1) blocks = 1;
-  k_cfl<<<blocks, 256, 0, st>>>(u, v, nu_, nv_, mac, at<DevScalars>(ws, 0), dt_out,
-                                p.dx < p.dy ? p.dx : p.dy, p.nu, p.cfl_target, p.dt_min,
-                                p.dt_max, (float)p.dt_correction);
+  launch_pdl(true, k_cfl, dim3(blocks), dim3(256), 0, st, u, v, nu_, nv_, mac,
+             at<DevScalars>(ws, 0), dt_out, p.dx < p.dy ? p.dx : p.dy, p.nu, p.cfl_target,
+             p.dt_min, p.dt_max, (float)p.dt_correction);
   return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
 }
 
@@ -141,6 +144,7 @@ __device__ __forceinline__ Strain strain_at(const float* __restrict__ u,
 __global__ void k_les_const(const float* __restrict__ u, const float* __restrict__ v,
                             float* __restrict__ nsg, int nx, int ny, float h2x, float h2y,
                             float coef) {
+  pdl_wait();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= nx || j >= ny) return;
@@ -154,6 +158,7 @@ __global__ void k_les_const(const float* __restrict__ u, const float* __restrict
 __global__ void k_les_const_mac(const float* __restrict__ u, const float* __restrict__ v,
                                 float* __restrict__ nsg, int nx, int ny, float h2x, float h2y,
                                 float coef) {
+  pdl_wait();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= nx || j >= ny) return;
@@ -179,6 +184,7 @@ __global__ void k_les_const_mac(const float* __restrict__ u, const float* __rest
 // MAC faces to cell centres (solver/operators_mac.py:118-127)
 __global__ void k_mac_to_center(const float* __restrict__ u, const float* __restrict__ v,
                                 float* __restrict__ uc, float* __restrict__ vc, int nx, int ny) {
+  pdl_wait();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= nx || j >= ny) return;
@@ -192,6 +198,7 @@ __global__ void k_dyn_strain(const float* __restrict__ u, const float* __restric
                              int ny, float h2x, float h2y, float* __restrict__ smag,
                              float* __restrict__ ssxx, float* __restrict__ ssxy,
                              float* __restrict__ ssyy) {
+  pdl_wait();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= nx || j >= ny) return;
@@ -212,6 +219,7 @@ __global__ void k_dyn_filter(const float* __restrict__ u, const float* __restric
                              float* __restrict__ uut, float* __restrict__ uvt,
                              float* __restrict__ vvt, float* __restrict__ fxx,
                              float* __restrict__ fxy, float* __restrict__ fyy) {
+  pdl_wait();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= nx || j >= ny) return;
@@ -250,6 +258,7 @@ __global__ void k_dyn_lm(const float* __restrict__ ut, const float* __restrict__
                          const float* __restrict__ fxy, const float* __restrict__ fyy, int nx,
                          int ny, float h2x, float h2y, float a2, float* __restrict__ lm,
                          float* __restrict__ mm) {
+  pdl_wait();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= nx || j >= ny) return;
@@ -269,6 +278,7 @@ __global__ void k_dyn_lm(const float* __restrict__ ut, const float* __restrict__
 __global__ void k_dyn_final(const float* __restrict__ lm, const float* __restrict__ mm,
                             const float* __restrict__ smag, int nx, int ny, float delta2,
                             float* __restrict__ nsg, float* __restrict__ cd) {
+  pdl_wait();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= nx || j >= ny) return;
@@ -301,30 +311,34 @@ int launch_les(const AjStepParams& p, const Layout& L, void* ws, int model, cons
   const float *uu = u, *vv = v;
   if (mac_input && model == AJ_LES_SMAGORINSKY) {
     double c = p.smagorinsky_constant * delta;
-    k_les_const_mac<<<grd, blk, 0, st>>>(u, v, nsg, nx, ny, h2x, h2y, (float)(c * c));
+    launch_pdl(true, k_les_const_mac, dim3(grd), dim3(blk), 0, st, u, v, nsg, nx, ny, h2x, h2y,
+               (float)(c * c));
     return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
   }
   if (mac_input) {
     float* uc = D + 14 * n;
     float* vc = D + 15 * n;
-    k_mac_to_center<<<grd, blk, 0, st>>>(u, v, uc, vc, nx, ny);
+    launch_pdl(true, k_mac_to_center, dim3(grd), dim3(blk), 0, st, u, v, uc, vc, nx, ny);
     uu = uc;
     vv = vc;
   }
   if (model == AJ_LES_SMAGORINSKY) {
     double c = p.smagorinsky_constant * delta;
-    k_les_const<<<grd, blk, 0, st>>>(uu, vv, nsg, nx, ny, h2x, h2y, (float)(c * c));
+    launch_pdl(true, k_les_const, dim3(grd), dim3(blk), 0, st, uu, vv, nsg, nx, ny, h2x, h2y,
+               (float)(c * c));
   } else if (model == AJ_LES_DYNAMIC) {
     float *smag = D, *sxx = D + n, *sxy = D + 2 * n, *syy = D + 3 * n;
     float *ut = D + 4 * n, *vt = D + 5 * n, *uut = D + 6 * n, *uvt = D + 7 * n, *vvt = D + 8 * n;
     float *fxx = D + 9 * n, *fxy = D + 10 * n, *fyy = D + 11 * n;
     float *lm = D + 12 * n, *mm = D + 13 * n;
-    k_dyn_strain<<<grd, blk, 0, st>>>(uu, vv, nx, ny, h2x, h2y, smag, sxx, sxy, syy);
-    k_dyn_filter<<<grd, blk, 0, st>>>(uu, vv, sxx, sxy, syy, nx, ny, ut, vt, uut, uvt, vvt, fxx,
-                                      fxy, fyy);
-    k_dyn_lm<<<grd, blk, 0, st>>>(ut, vt, uut, uvt, vvt, fxx, fxy, fyy, nx, ny, h2x, h2y, 4.0f,
-                                  lm, mm);
-    k_dyn_final<<<grd, blk, 0, st>>>(lm, mm, smag, nx, ny, (float)(delta * delta), nsg, cd);
+    launch_pdl(true, k_dyn_strain, dim3(grd), dim3(blk), 0, st, uu, vv, nx, ny, h2x, h2y, smag, sxx,
+               sxy, syy);
+    launch_pdl(true, k_dyn_filter, dim3(grd), dim3(blk), 0, st, uu, vv, sxx, sxy, syy, nx, ny, ut,
+               vt, uut, uvt, vvt, fxx, fxy, fyy);
+    launch_pdl(true, k_dyn_lm, dim3(grd), dim3(blk), 0, st, ut, vt, uut, uvt, vvt, fxx, fxy, fyy,
+               nx, ny, h2x, h2y, 4.0f, lm, mm);
+    launch_pdl(true, k_dyn_final, dim3(grd), dim3(blk), 0, st, lm, mm, smag, nx, ny,
+               (float)(delta * delta), nsg, cd);
   } else {
     return AJ_ERR_PARAM;
   }
@@ -452,6 +466,7 @@ __device__ __forceinline__ float stage_val(const RkArgs& a, const float* f, cons
 
 template <bool PER, bool HYPER, int ADV>
 __global__ void __launch_bounds__(256) k_rk_col(RkArgs a) {
+  pdl_wait();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   const int nx = a.nx, ny = a.ny;
@@ -500,11 +515,13 @@ __global__ void __launch_bounds__(256) k_rk_col(RkArgs a) {
 template <bool PER>
 static void dispatch_rk_col(const RkArgs& a, bool hyper, int adv, dim3 g, dim3 b, cudaStream_t st) {
   if (hyper) {
-    if (adv == AJ_ADV_WENO5) k_rk_col<PER, true, AJ_ADV_WENO5><<<g, b, 0, st>>>(a);
-    else k_rk_col<PER, true, AJ_ADV_UPWIND><<<g, b, 0, st>>>(a);
+    if (adv == AJ_ADV_WENO5) launch_pdl(true, k_rk_col<PER, true, AJ_ADV_WENO5>, dim3(g), dim3(b),
+                                        0, st, a);
+    else launch_pdl(true, k_rk_col<PER, true, AJ_ADV_UPWIND>, dim3(g), dim3(b), 0, st, a);
   } else {
-    if (adv == AJ_ADV_WENO5) k_rk_col<PER, false, AJ_ADV_WENO5><<<g, b, 0, st>>>(a);
-    else k_rk_col<PER, false, AJ_ADV_UPWIND><<<g, b, 0, st>>>(a);
+    if (adv == AJ_ADV_WENO5) launch_pdl(true, k_rk_col<PER, false, AJ_ADV_WENO5>, dim3(g), dim3(b),
+                                        0, st, a);
+    else launch_pdl(true, k_rk_col<PER, false, AJ_ADV_UPWIND>, dim3(g), dim3(b), 0, st, a);
   }
 }
 
@@ -784,6 +801,7 @@ __device__ __forceinline__ float stage_mac_v_int(const RkMac& a, int i, int j, f
 
 template <bool HYPER>
 __global__ void __launch_bounds__(256) k_rk_mac(RkMac a) {
+  pdl_wait();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   const int nx = a.nx, ny = a.ny;
@@ -939,8 +957,8 @@ int launch_predictor(const AjStepParams& p, const Layout& L, void* ws, const flo
       a.vout = last ? vs : dst[1];
       a.k1u_out = (rk2 && s == 1) ? K[0] : nullptr;
       a.k1v_out = (rk2 && s == 1) ? K[1] : nullptr;
-      if (hyper) k_rk_mac<true><<<grd, blk, 0, st>>>(a);
-      else k_rk_mac<false><<<grd, blk, 0, st>>>(a);
+      if (hyper) launch_pdl(true, k_rk_mac<true>, dim3(grd), dim3(blk), 0, st, a);
+      else launch_pdl(true, k_rk_mac<false>, dim3(grd), dim3(blk), 0, st, a);
       in_u = a.uout;
       in_v = a.vout;
     }

@@ -178,6 +178,7 @@ __global__ void k_copy(const float* __restrict__ s, float* __restrict__ d, long 
 }
 
 __global__ void k_stats(const DevScalars* sc, AjStats* st, int converge_mode) {
+  pdl_wait();
   st->cycles = sc->mg_cycles;
   st->converged = converge_mode ? sc->mg_done : sc->mg_skip;
   st->err = sc->err;

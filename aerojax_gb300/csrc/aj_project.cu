@@ -25,6 +25,7 @@ __global__ void __launch_bounds__(256) k_rhs(const float* __restrict__ us,
                                              float* __restrict__ b, int nx, int ny, float h2x,
                                              float h2y, float idx, float idy, int mac, int pure,
                                              int outlet, const DevScalars* sc) {
+  pdl_wait();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= nx || j >= ny) return;
@@ -49,11 +50,10 @@ __global__ void __launch_bounds__(256) k_rhs(const float* __restrict__ us,
 int launch_rhs(const AjStepParams& p, const Layout& L, void* ws, const float* us,
                const float* vs, const float* mask, float* b, cudaStream_t st) {
   dim3 blk(32, 8), grd(cdiv(p.ny, 32), cdiv(p.nx, 8));
-  k_rhs<<<grd, blk, 0, st>>>(us, vs, mask, b, p.nx, p.ny, (float)(1.0 / (2.0 * p.dx)),
-                             (float)(1.0 / (2.0 * p.dy)), (float)(1.0 / p.dx),
-                             (float)(1.0 / p.dy), p.grid_type == AJ_GRID_MAC,
-                             p.variant == AJ_VARIANT_PURE, p.flow_type == AJ_FLOW_VON_KARMAN,
-                             at<DevScalars>(ws, 0));
+  launch_pdl(true, k_rhs, dim3(grd), dim3(blk), 0, st, us, vs, mask, b, p.nx, p.ny,
+             (float)(1.0 / (2.0 * p.dx)), (float)(1.0 / (2.0 * p.dy)), (float)(1.0 / p.dx),
+             (float)(1.0 / p.dy), p.grid_type == AJ_GRID_MAC, p.variant == AJ_VARIANT_PURE,
+             p.flow_type == AJ_FLOW_VON_KARMAN, at<DevScalars>(ws, 0));
   return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
 }
 
@@ -112,6 +112,7 @@ __device__ __forceinline__ float w_gui(const Corr& c, int a, int b, float dt) {
 }
 
 __global__ void __launch_bounds__(256) k_correct_col(Corr c) {
+  pdl_wait();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   const int nx = c.nx, ny = c.ny;
@@ -139,6 +140,7 @@ __global__ void __launch_bounds__(256) k_correct_col(Corr c) {
 // MAC GUI correction: staggered gradients (operators_mac.py:40-55; the face
 // gradient on the boundary faces is 0), BC of step_handlers.py:256-274
 __global__ void __launch_bounds__(256) k_correct_mac(Corr c) {
+  pdl_wait();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   const int nx = c.nx, ny = c.ny;
@@ -190,10 +192,10 @@ int launch_correct(const AjStepParams& p, const Layout& L, void* ws, const float
   dim3 blk(32, 8);
   if (p.grid_type == AJ_GRID_MAC) {
     dim3 grd(cdiv(p.ny + 1, 32), cdiv(p.nx + 1, 8));
-    k_correct_mac<<<grd, blk, 0, st>>>(c);
+    launch_pdl(true, k_correct_mac, dim3(grd), dim3(blk), 0, st, c);
   } else {
     dim3 grd(cdiv(p.ny, 32), cdiv(p.nx, 8));
-    k_correct_col<<<grd, blk, 0, st>>>(c);
+    launch_pdl(true, k_correct_col, dim3(grd), dim3(blk), 0, st, c);
   }
   return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
 }
