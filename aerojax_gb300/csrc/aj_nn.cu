@@ -94,28 +94,46 @@ struct ConvSmem {
   static constexpr size_t bytes = (size_t)CT_HALO * AS * 4 + (size_t)9 * BN * AS * 2;
 };
 
-template <int CIN, int NT>   // BN = NT * 8 output channels per block
-__global__ void __launch_bounds__(CONV_THREADS) k_conv3x3(const float* __restrict__ X, int N, int H,
-                                                          int W, int Cout,
-                                                          const __nv_bfloat16* __restrict__ WT,
-                                                          const float* __restrict__ bias,
-                                                          float* __restrict__ Y, int relu,
-                                                          float* __restrict__ Yp,
-                                                          const float* __restrict__ Xc) {
+// One convolution's operands (NHWC activations, WT[tap][Cout][Cin] BF16).
+struct ConvArgs {
+  const float* X;
+  int N, H, W, Cout;
+  const __nv_bfloat16* WT;
+  const float* bias;
+  float* Y;
+  int relu;
+  float* Yp;         // nullable: 2x2 average pool of Y
+  const float* Xc;   // nullable: the input is up2(Xc) + X
+};
+
+// One 8 x 8 pixel tile t (tiles ordered w fastest, then h, then sample) and
+// the BN = NT * 8 output channels from co0.  PDL: dependent launch (wait for
+// the previous layer after staging the weights).  A caller that runs several
+// tiles in a row puts a block barrier between them (the next staging
+// overwrites shared memory that other warps may still be reading).
+template <int CIN, int NT, bool PDL>
+__device__ __forceinline__ void conv_tile(const ConvArgs& cv, int t, int co0,
+                                          unsigned char* conv_sm) {
+  const float* __restrict__ X = cv.X;
+  const int H = cv.H, W = cv.W, Cout = cv.Cout;
+  const __nv_bfloat16* __restrict__ WT = cv.WT;
+  const float* __restrict__ bias = cv.bias;
+  float* __restrict__ Y = cv.Y;
+  const int relu = cv.relu;
+  float* __restrict__ Yp = cv.Yp;
+  const float* __restrict__ Xc = cv.Xc;
   using S = ConvSmem<CIN, NT>;
   constexpr int AS = S::AS, BN = S::BN;
-  extern __shared__ __align__(16) unsigned char conv_sm[];
   float* As = reinterpret_cast<float*>(conv_sm);                              // [px][AS] FP32
   __nv_bfloat16* Bs = reinterpret_cast<__nv_bfloat16*>(As + CT_HALO * AS);   // [tap][BN][AS]
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int g = lane >> 2, tg = lane & 3;
   const int tilesW = (W + CT - 1) / CT, tilesH = (H + CT - 1) / CT;
-  int t = blockIdx.x;
   const int tw = t % tilesW;
   t /= tilesW;
   const int th = t % tilesH;
   const int n = t / tilesH;
-  const int h0 = th * CT, w0 = tw * CT, co0 = blockIdx.y * BN;
+  const int h0 = th * CT, w0 = tw * CT;
   {  // weights of the 9 taps: 9 * BN rows of CIN BF16, CIN / 8 16-byte pieces each
     constexpr int PR = CIN / 8;
     for (int e = tid; e < 9 * BN * PR; e += CONV_THREADS) {
@@ -127,7 +145,7 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv3x3(const float* __restric
   }
   // the weights do not depend on the previous layer: staged before the wait
   // for the previous layer's output
-  pdl_wait();
+  if (PDL) pdl_wait();
   {  // the halo tile, FP32, zeros outside the image
     constexpr int C4 = CIN / 4;
     for (int e = tid; e < CT_HALO * C4; e += CONV_THREADS) {
@@ -150,14 +168,14 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv3x3(const float* __restric
       const int hy = px / (CT + 2), hx = px - hy * (CT + 2);
       const int gh = h0 - 1 + hy, gw = w0 - 1 + hx;
       if (gh >= 0 && gh < H && gw >= 0 && gw < W) {
-        const float4 c = *reinterpret_cast<const float4*>(
-            Xc + (((long)n * Hc + (gh >> 1)) * Wc + (gw >> 1)) * CIN + q * 4);
+        const float4 u = __ldcg(reinterpret_cast<const float4*>(
+            Xc + (((long)n * Hc + (gh >> 1)) * Wc + (gw >> 1)) * CIN + q * 4));
         float4* a = reinterpret_cast<float4*>(As + px * AS + q * 4);
         float4 v = *a;
-        v.x = c.x + v.x;
-        v.y = c.y + v.y;
-        v.z = c.z + v.z;
-        v.w = c.w + v.w;
+        v.x = u.x + v.x;
+        v.y = u.y + v.y;
+        v.z = u.z + v.z;
+        v.w = u.w + v.w;
         *a = v;
       }
     }
@@ -234,14 +252,20 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv3x3(const float* __restric
 }
 
 template <int CIN, int NT>
+__global__ void __launch_bounds__(CONV_THREADS) k_conv3x3(ConvArgs a) {
+  extern __shared__ __align__(16) unsigned char conv_sm[];
+  conv_tile<CIN, NT, true>(a, blockIdx.x, blockIdx.y * NT * 8, conv_sm);
+}
+
+template <int CIN, int NT>
 static void conv_launch(const float* X, int N, int H, int W, int Cout, const __nv_bfloat16* WT,
                         const float* bias, float* Y, int relu, float* Yp, const float* Xc,
                         cudaStream_t st, bool pdl) {
   using S = ConvSmem<CIN, NT>;
   const int tiles = ((W + CT - 1) / CT) * ((H + CT - 1) / CT) * N;
   dim3 grid(tiles, Cout / S::BN);
-  launch_pdl(pdl, k_conv3x3<CIN, NT>, grid, dim3(CONV_THREADS), S::bytes, st, X, N, H, W, Cout,
-             WT, bias, Y, relu, Yp, Xc);
+  launch_pdl(pdl, k_conv3x3<CIN, NT>, grid, dim3(CONV_THREADS), S::bytes, st,
+             ConvArgs{X, N, H, W, Cout, WT, bias, Y, relu, Yp, Xc});
 }
 
 template <int CIN, int NT>
