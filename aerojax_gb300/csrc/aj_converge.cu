@@ -358,34 +358,44 @@ struct CvCheck {
   cudaGraphConditionalHandle h;
 };
 
-// convergence bookkeeping after a V-cycle (device scalars; one thread)
+// convergence bookkeeping after a V-cycle (device scalars; one thread).  All
+// fields are loaded before any is stored: interleaved, every load waited for
+// the store before it (a chain of dependent round trips at the end of the
+// cycle's last kernel).
 __device__ void cv_check_body(DevScalars* sc, const CvCheck& ck) {
-  if (!sc->mg_done) {
-    sc->mg_cycles += 1;
-    double nb = sc->bnorm > 0.0 ? sc->bnorm : 1.0;
-    double rel = sqrt(sc->acc[0]) / nb;
+  int done = sc->mg_done, cycles = sc->mg_cycles, err = sc->err, loops = sc->loops;
+  const double bnorm = sc->bnorm, a0 = sc->acc[0];
+  const int was_done = done;
+  if (!was_done) {
+    cycles += 1;
+    const double nb = bnorm > 0.0 ? bnorm : 1.0;
+    const double rel = sqrt(a0) / nb;
     sc->rel = rel;
-    sc->abs_sq = sc->acc[0];
+    sc->abs_sq = a0;
     if (!isfinite(rel)) {
-      sc->err = AJ_ERR_NONFINITE;
-      sc->mg_done = 1;
+      err = AJ_ERR_NONFINITE;
+      done = 1;
     } else if (rel <= ck.rtol) {
-      sc->mg_done = 1;
-    } else if (sc->mg_cycles >= ck.max_cycles) {
-      sc->err = AJ_ERR_NOT_CONVERGED;
-      sc->mg_done = 1;
+      done = 1;
+    } else if (cycles >= ck.max_cycles) {
+      err = AJ_ERR_NOT_CONVERGED;
+      done = 1;
     }
   }
   sc->acc[0] = 0.0;
   if (ck.use_handle) {
     // independent bound on the while node: never more bodies than max_cycles + 1
-    sc->loops += 1;
-    if (sc->loops > ck.max_cycles + 1 && !sc->mg_done) {
-      sc->err = AJ_ERR_NOT_CONVERGED;
-      sc->mg_done = 1;
+    loops += 1;
+    if (loops > ck.max_cycles + 1 && !done) {
+      err = AJ_ERR_NOT_CONVERGED;
+      done = 1;
     }
-    cudaGraphSetConditional(ck.h, sc->mg_done ? 0u : 1u);
+    sc->loops = loops;
   }
+  sc->mg_cycles = cycles;
+  sc->err = err;
+  sc->mg_done = done;
+  if (ck.use_handle) cudaGraphSetConditional(ck.h, done ? 0u : 1u);
 }
 
 // a ping-pong pair: the pressure state (each buffer N hi values followed by N
@@ -882,15 +892,18 @@ struct HistView {
   float dtp;
 };
 __device__ __forceinline__ HistView hist_view(const DevScalars* sc) {
+  // all five fields loaded unconditionally (one round trip), then selected
+  const int pend = sc->hist_pending, cur = sc->hist_cur, n = sc->hist_n;
+  const float dtl = sc->dt_last, dtp = sc->dt_prev;
   HistView h;
-  if (sc->hist_pending) {
-    h.cur = 1 - sc->hist_cur;
-    h.n = sc->hist_n < 2 ? sc->hist_n + 1 : 2;
-    h.dtp = sc->dt_last;
+  if (pend) {
+    h.cur = 1 - cur;
+    h.n = n < 2 ? n + 1 : 2;
+    h.dtp = dtl;
   } else {
-    h.cur = sc->hist_cur;
-    h.n = sc->hist_n;
-    h.dtp = sc->dt_prev;
+    h.cur = cur;
+    h.n = n;
+    h.dtp = dtp;
   }
   return h;
 }
@@ -903,28 +916,45 @@ __global__ void __launch_bounds__(256) k_cv_init(const float* __restrict__ p0,
   if (j >= m) return;
   const HistView hv = hist_view(sc);
   const int hn = hs.h ? hv.n : 0;
-  const float* h1 = hs.h ? hs.h + (long)hv.cur * 2 * N : nullptr;
-  const float* h2 = hs.h ? hs.h + (long)(1 - hv.cur) * 2 * N : nullptr;
+  const float* __restrict__ h1 = hs.h ? hs.h + (long)hv.cur * 2 * N : nullptr;
+  const float* __restrict__ h2 = hs.h ? hs.h + (long)(1 - hv.cur) * 2 * N : nullptr;
   float ratio = 1.f;
   if (hn >= 2 && sc->dt > 0.f && hv.dtp > 0.f) ratio = sc->dt / hv.dtp;
+  const int i0 = blockIdx.y * CV_ROWS;
+  // every row's loads first (the stores below would otherwise hold each
+  // row's loads back behind the previous row's stores)
+  float a_hi[CV_ROWS], a_lo[CV_ROWS], b_hi[CV_ROWS], b_lo[CV_ROWS];
 #pragma unroll
   for (int r = 0; r < CV_ROWS; ++r) {
-    const int i = blockIdx.y * CV_ROWS + r;
-    if (i >= n) break;
+    const int i = i0 + r;
     const long k = (long)i * m + j;
-    df v{0.f, 0.f};
-    if (i != n - 1) {
-      if (hn >= 2) {
-        const df a{h1[k], h1[N + k]}, b{h2[k], h2[N + k]};
-        v = df_add(a, df_mul(df{ratio, 0.f}, df_add(a, df_neg(b))));
-      } else if (hn == 1) {
-        v = df{h1[k], h1[N + k]};
+    a_hi[r] = a_lo[r] = b_hi[r] = b_lo[r] = 0.f;
+    if (i < n - 1) {
+      if (hn >= 1) {
+        a_hi[r] = h1[k];
+        a_lo[r] = h1[N + k];
       } else if (p0) {
-        v.hi = p0[k];
+        a_hi[r] = p0[k];
+      }
+      if (hn >= 2) {
+        b_hi[r] = h2[k];
+        b_lo[r] = h2[N + k];
       }
     }
-    ps[k] = v.hi;
-    ps[N + k] = v.lo;
+  }
+#pragma unroll
+  for (int r = 0; r < CV_ROWS; ++r) {
+    const int i = i0 + r;
+    if (i < n) {
+      const long k = (long)i * m + j;
+      df v{a_hi[r], a_lo[r]};
+      if (hn >= 2 && i != n - 1) {
+        const df a = v, b{b_hi[r], b_lo[r]};
+        v = df_add(a, df_mul(df{ratio, 0.f}, df_add(a, df_neg(b))));
+      }
+      ps[k] = v.hi;
+      ps[N + k] = v.lo;
+    }
   }
 }
 
@@ -940,23 +970,53 @@ __global__ void __launch_bounds__(256) k_cv_resid(const float* __restrict__ ps,
   float acc = 0.f, accb = 0.f;
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j < m) {
+    const int i0 = blockIdx.y * CV_ROWS;
+    // all loads first: the state at rows i0-1 .. i0+CV_ROWS (column j), the
+    // column neighbours j-1, j+1 and b at rows i0 .. i0+CV_ROWS-1
+    float ch[CV_ROWS + 2], cl[CV_ROWS + 2], yph[CV_ROWS], ypl[CV_ROWS], ymh[CV_ROWS],
+        yml[CV_ROWS], bv[CV_ROWS];
 #pragma unroll
-    for (int rr_ = 0; rr_ < CV_ROWS; ++rr_) {
-      const int i = blockIdx.y * CV_ROWS + rr_;
+    for (int q = 0; q < CV_ROWS + 2; ++q) {
+      const int i = i0 - 1 + q;
+      ch[q] = cl[q] = 0.f;
+      if (i >= 0 && i < n) {
+        const long k = (long)i * m + j;
+        ch[q] = ps[k];
+        cl[q] = ps[N + k];
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < CV_ROWS; ++q) {
+      const int i = i0 + q;
+      yph[q] = ypl[q] = ymh[q] = yml[q] = bv[q] = 0.f;
+      if (i < n - 1) {
+        const long k = (long)i * m + j;
+        if (j + 1 < m) {
+          yph[q] = ps[k + 1];
+          ypl[q] = ps[N + k + 1];
+        }
+        if (j > 0) {
+          ymh[q] = ps[k - 1];
+          yml[q] = ps[N + k - 1];
+        }
+        bv[q] = b[k];
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < CV_ROWS; ++q) {
+      const int i = i0 + q;
       if (i >= n) break;
       const long k = (long)i * m + j;
       float rr = 0.f;
       if (i != n - 1) {
-        auto P = [&](long q) { return df{ps[q], ps[N + q]}; };
-        const df c = P(k);
-        const df xp = P(k + m);
-        const df xm = i > 0 ? P(k - m) : c;
-        const df yp = j + 1 < m ? P(k + 1) : c;
-        const df ym = j > 0 ? P(k - 1) : c;
-        const float bb = b[k];
-        const df res = df_residual(bb, c, xp, xm, yp, ym, ax, ay);
+        const df c{ch[q + 1], cl[q + 1]};
+        const df xp{ch[q + 2], cl[q + 2]};
+        const df xm = i > 0 ? df{ch[q], cl[q]} : c;
+        const df yp = j + 1 < m ? df{yph[q], ypl[q]} : c;
+        const df ym = j > 0 ? df{ymh[q], yml[q]} : c;
+        const df res = df_residual(bv[q], c, xp, xm, yp, ym, ax, ay);
         rr = res.hi + res.lo;
-        accb = fmaf(bb, bb, accb);
+        accb = fmaf(bv[q], bv[q], accb);
       }
       r[k] = rr;
       acc = fmaf(rr, rr, acc);
@@ -975,7 +1035,19 @@ __global__ void __launch_bounds__(256) k_cv_resid(const float* __restrict__ ps,
   __syncthreads();
   if (am_last && threadIdx.x == 0) {
     __threadfence();
+    // every field first, then the stores (see cv_check_body)
     const HistView hv = hist_view(sc);
+    const double a0 = sc->acc[0], a1 = sc->acc[1];
+    const double bnorm = sqrt(a1);
+    const double nb = bnorm > 0.0 ? bnorm : 1.0;
+    const double rel = sqrt(a0) / nb;
+    int err = AJ_OK, done = 0;
+    if (!isfinite(rel)) {
+      err = AJ_ERR_NONFINITE;
+      done = 1;
+    } else if (rel <= rtol) {
+      done = 1;
+    }
     sc->hist_cur = hv.cur;
     sc->hist_n = hv.n;
     sc->dt_prev = hv.dtp;
@@ -984,21 +1056,13 @@ __global__ void __launch_bounds__(256) k_cv_resid(const float* __restrict__ ps,
     sc->mg_cycles = 0;
     sc->loops = 0;
     sc->pcur = 0;
-    sc->err = AJ_OK;
-    sc->mg_done = 0;
-    sc->bnorm = sqrt(sc->acc[1]);
-    const double nb = sc->bnorm > 0.0 ? sc->bnorm : 1.0;
-    const double rel = sqrt(sc->acc[0]) / nb;
+    sc->bnorm = bnorm;
     sc->rel = rel;
-    sc->abs_sq = sc->acc[0];
-    if (!isfinite(rel)) {
-      sc->err = AJ_ERR_NONFINITE;
-      sc->mg_done = 1;
-    } else if (rel <= rtol) {
-      sc->mg_done = 1;
-    }
+    sc->abs_sq = a0;
     sc->acc[0] = 0.0;
     sc->acc[1] = 0.0;
+    sc->err = err;
+    sc->mg_done = done;
   }
 }
 
@@ -1019,19 +1083,24 @@ __global__ void k_cv_out(PState ps, DevScalars* sc, float* __restrict__ p, long 
     }
   }
   if (k == 0) {
+    // every field first, then the stores (stats may alias nothing the
+    // compiler can prove, so interleaved each load waited for a store)
+    const int cycles = sc->mg_cycles, done = sc->mg_done, err = sc->err;
+    const double rel = sc->rel, bnorm = sc->bnorm, abs_sq = sc->abs_sq;
+    const float dt = sc->dt;
     if (hist) {
       sc->hist_pending = 1;
-      sc->dt_last = sc->dt;
+      sc->dt_last = dt;
     }
     if (stats) {
-      stats->cycles = sc->mg_cycles;
-      stats->converged = sc->mg_done;
-      stats->err = sc->err;
+      stats->cycles = cycles;
+      stats->converged = done;
+      stats->err = err;
       stats->pad = 0;
-      stats->rel_residual = sc->rel;
-      stats->rhs_norm = sc->bnorm;
-      stats->dt = sc->dt;
-      stats->abs_residual_sq = sc->abs_sq;
+      stats->rel_residual = rel;
+      stats->rhs_norm = bnorm;
+      stats->dt = dt;
+      stats->abs_residual_sq = abs_sq;
     }
   }
 }

@@ -60,15 +60,28 @@ __global__ void k_cfl(const float* __restrict__ u, const float* __restrict__ v, 
                       double cfl, double dt_min, double dt_max, float dtc_host) {
   pdl_wait();
   float m = 0.f;
-  long stride = (long)gridDim.x * blockDim.x;
-  long n = nu_ > nv_ ? nu_ : nv_;
-  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += stride) {
-    if (mac) {
-      if (k < nu_) m = fmaxf(m, fabsf(u[k]));
-      if (k < nv_) m = fmaxf(m, fabsf(v[k]));
-    } else {
-      float a = u[k], b = v[k];
-      m = fmaxf(m, sqrtf(a * a + b * b));
+  const long stride = (long)gridDim.x * blockDim.x;
+  const long n = nu_ > nv_ ? nu_ : nv_;
+  // grid-stride in batches of CFL_BATCH: a batch's loads are all issued
+  // before its maxima
+  constexpr int CFL_BATCH = 8;
+  for (long k0 = blockIdx.x * (long)blockDim.x + threadIdx.x; k0 < n;
+       k0 += CFL_BATCH * stride) {
+    float a[CFL_BATCH], b[CFL_BATCH];
+#pragma unroll
+    for (int q = 0; q < CFL_BATCH; ++q) {
+      const long k = k0 + q * stride;
+      a[q] = k < nu_ ? u[k] : 0.f;
+      b[q] = k < nv_ ? v[k] : 0.f;
+    }
+#pragma unroll
+    for (int q = 0; q < CFL_BATCH; ++q) {
+      if (mac) {
+        m = fmaxf(m, fabsf(a[q]));
+        m = fmaxf(m, fabsf(b[q]));
+      } else {
+        m = fmaxf(m, sqrtf(a[q] * a[q] + b[q] * b[q]));
+      }
     }
   }
   for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));

@@ -179,14 +179,19 @@ __global__ void k_copy(const float* __restrict__ s, float* __restrict__ d, long 
 
 __global__ void k_stats(const DevScalars* sc, AjStats* st, int converge_mode) {
   pdl_wait();
-  st->cycles = sc->mg_cycles;
-  st->converged = converge_mode ? sc->mg_done : sc->mg_skip;
-  st->err = sc->err;
+  // all loads before the stores (interleaved, each load waits for a store)
+  const int cycles = sc->mg_cycles, conv = converge_mode ? sc->mg_done : sc->mg_skip;
+  const int err = sc->err;
+  const double rel = sc->rel, bnorm = sc->bnorm, abs_sq = sc->abs_sq;
+  const float dt = sc->dt;
+  st->cycles = cycles;
+  st->converged = conv;
+  st->err = err;
   st->pad = 0;
-  st->rel_residual = sc->rel;
-  st->rhs_norm = sc->bnorm;
-  st->dt = sc->dt;
-  st->abs_residual_sq = sc->abs_sq;
+  st->rel_residual = rel;
+  st->rhs_norm = bnorm;
+  st->dt = dt;
+  st->abs_residual_sq = abs_sq;
 }
 
 static int parity_solve(const AjStepParams& p, const Layout& L, void* ws, const float* mask,
