@@ -114,11 +114,12 @@ __device__ __forceinline__ df df_add_s(df a, df b) {
   s.lo += a.lo + b.lo;
   return quick_two_sum(s.hi, s.lo);
 }
-// r = b - (ax ((xp - c) + (xm - c)) + ay ((yp - c) + (ym - c))), all double-FP32
+// r = b - (ax ((xp + xm) - 2c) + ay ((yp + ym) - 2c)), all double-FP32 (-2c is
+// exact, so each second difference costs two additions, not three)
 __device__ __forceinline__ df df_residual(float b, df c, df xp, df xm, df yp, df ym, df ax, df ay) {
-  const df nc = df_neg(c);
-  const df sx = df_add_s(df_add_s(xp, nc), df_add_s(xm, nc));
-  const df sy = df_add_s(df_add_s(yp, nc), df_add_s(ym, nc));
+  const df c2{-2.f * c.hi, -2.f * c.lo};
+  const df sx = df_add_s(df_add_s(xp, xm), c2);
+  const df sy = df_add_s(df_add_s(yp, ym), c2);
   const df ap = df_add_s(df_mul(ax, sx), df_mul(ay, sy));
   return df_add_f(df_neg(ap), b);
 }
@@ -169,9 +170,9 @@ __device__ __forceinline__ float cv_diag(const CvLvl& L, int gi, int gj) {
 // half-sweep h the cells at distance >= h+1 from the tile border hold exact
 // red-black values; the cells nearer the border are never stored.  Tiles start
 // at even global coordinates, so a cell's colour is (ti + tj) & 1.
-template <class TC>
-__device__ __forceinline__ void cv_sweeps(float* E, const float* R, const CvLvl& L, int gi0,
-                                          int gj0) {
+template <class TC, bool INTERIOR>
+__device__ __forceinline__ void cv_sweeps_t(float* E, const float* R, const CvLvl& L, int gi0,
+                                            int gj0) {
   constexpr int SJ = TC::SJ, SI = TC::SI;
   const int tx = threadIdx.x, ty = threadIdx.y;
   const float inv_int = 1.f / (-2.f * (L.ax + L.ay));
@@ -181,18 +182,31 @@ __device__ __forceinline__ void cv_sweeps(float* E, const float* R, const CvLvl&
     for (int ti = 1 + ty; ti < SI - 1; ti += TC::RG) {
       const int tj = 2 * tx + ((color + ti) & 1);
       const int gi = gi0 + ti, gj = gj0 + tj;
-      const bool upd = tj >= 1 && tj < SJ - 1 && (unsigned)gi < (unsigned)L.n &&
-                       (unsigned)gj < (unsigned)L.m && !(L.level == 0 && gi == L.n - 1);
+      const bool upd = INTERIOR ? (tj >= 1 && tj < SJ - 1)
+                                : (tj >= 1 && tj < SJ - 1 && (unsigned)gi < (unsigned)L.n &&
+                                   (unsigned)gj < (unsigned)L.m &&
+                                   !(L.level == 0 && gi == L.n - 1));
       if (upd) {
         const int c = ti * SJ + tj;
         const float nb = L.ax * (E[c + SJ] + E[c - SJ]) + L.ay * (E[c + 1] + E[c - 1]);
         float inv = inv_int;
-        if (gi == 0 || gj == 0 || gi == L.n - 1 || gj == L.m - 1) inv = 1.f / cv_diag(L, gi, gj);
+        if (!INTERIOR && (gi == 0 || gj == 0 || gi == L.n - 1 || gj == L.m - 1))
+          inv = 1.f / cv_diag(L, gi, gj);
         E[c] = (R[c] - nb) * inv;
       }
     }
     __syncthreads();
   }
+}
+// A tile whose every cell is an interior cell of the level (no boundary row
+// or column, not the pinned outlet row) takes the sweep without the checks.
+template <class TC>
+__device__ __forceinline__ void cv_sweeps(float* E, const float* R, const CvLvl& L, int gi0,
+                                          int gj0) {
+  if (gi0 >= 1 && gj0 >= 1 && gi0 + TC::SI <= L.n - 1 && gj0 + TC::SJ <= L.m - 1)
+    cv_sweeps_t<TC, true>(E, R, L, gi0, gj0);
+  else
+    cv_sweeps_t<TC, false>(E, R, L, gi0, gj0);
 }
 
 // The coarse cells a tile's cell-centred bilinear prolongation reads, with the
