@@ -419,6 +419,14 @@ struct PState {
   float* b;   // buffer 1
 };
 
+// 4-byte asynchronous global-to-shared copy; zero-fill when !in (the source
+// is then not read)
+__device__ __forceinline__ void cv_cp4(float* dst, const float* src, bool in) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(src),
+               "r"(in ? 4 : 0));
+}
+
 // level 0: e + P(e_coarse), post-smoothing, p += e (double-FP32, ping-pong), the
 // residual of the reference operator for the next iteration (double-FP32), its
 // FP64 norm, and the convergence test in the last block to finish.  The
@@ -426,7 +434,7 @@ struct PState {
 // the current residual over its tile and halo while its neighbours write the
 // next one, so the two must never share a buffer.
 template <class TC>
-__global__ void __launch_bounds__(TC::NTH) k_cv_up0(
+__global__ void __launch_bounds__(TC::NTH, 4) k_cv_up0(
     CvLvl L, PState rs, const float* __restrict__ e_in,
     const float* __restrict__ ec, int nc, int mc, float gc, PState ps, const float* __restrict__ b,
     DevScalars* sc, DfCoef co, CvCheck ck, int profile) {
@@ -450,11 +458,43 @@ __global__ void __launch_bounds__(TC::NTH) k_cv_up0(
   float* __restrict__ pout = cur ? ps.a : ps.b;
   const float* __restrict__ r = cur ? rs.b : rs.a;
   float* __restrict__ r_next = cur ? rs.a : rs.b;
+  // the pressure window (interior + 1) and b are requested first, so that
+  // their latency overlaps the prolongation and the sweeps: the window by
+  // cp.async straight into PH/PL, b into registers (this thread's residual
+  // cells: rows ty + RG q, columns tx and tx + PAIRS)
+  for (int pi = ty; pi < PI; pi += TC::RG) {
+    const int gi = i0 - 1 + pi;
+    const bool row_in = (unsigned)gi < (unsigned)L.n && gi != L.n - 1;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int pj = tx + q * TC::PAIRS;
+      if (pj >= PJ) continue;
+      const int gj = j0 - 1 + pj;
+      const bool in = row_in && (unsigned)gj < (unsigned)L.m;
+      const long k = in ? (long)gi * L.m + gj : 0;
+      cv_cp4(PH + pi * PJ + pj, pin + k, in);
+      cv_cp4(PL + pi * PJ + pj, pin + N + k, in);
+    }
+  }
+  asm volatile("cp.async.commit_group;\n" ::);
+  constexpr int RQ = (TI + TC::RG - 1) / TC::RG;
+  float bpre[RQ][2];
+#pragma unroll
+  for (int it = 0; it < RQ; ++it) {
+    const int ti = ty + it * TC::RG, gi = i0 + ti;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int tj = tx + q * TC::PAIRS, gj = j0 + tj;
+      bpre[it][q] = (ti < TI && gi < L.n && tj < TJ && gj < L.m) ? ldg(b + (long)gi * L.m + gj) : 0.f;
+    }
+  }
   __shared__ float W[CoarseWin<TC>::R * CoarseWin<TC>::C];
   cv_load_coarse<TC>(W, gi0, gj0, ec, nc, mc, gc);
   __syncthreads();
   cv_load<TC, false>(E, R, L, gi0, gj0, r, e_in, W);
   cv_sweeps<TC>(E, R, L, gi0, gj0);
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+  __syncthreads();
   // new pressure on the interior and one cell around it
   for (int pi = ty; pi < PI; pi += TC::RG) {
     const int gi = i0 - 1 + pi;
@@ -464,21 +504,22 @@ __global__ void __launch_bounds__(TC::NTH) k_cv_up0(
       const int pj = tx + q * TC::PAIRS;
       if (pj >= PJ) continue;
       const int gj = j0 - 1 + pj;
-      df v{0.f, 0.f};
       if (row_in && (unsigned)gj < (unsigned)L.m) {
-        const long k = (long)gi * L.m + gj;
-        v = df_add_f(df{pin[k], pin[N + k]}, E[(CV_H - 1 + pi) * SJ + (CV_H - 1 + pj)]);
+        const int t = pi * PJ + pj;
+        const df v = df_add_f(df{PH[t], PL[t]}, E[(CV_H - 1 + pi) * SJ + (CV_H - 1 + pj)]);
+        PH[t] = v.hi;
+        PL[t] = v.lo;
       }
-      PH[pi * PJ + pj] = v.hi;
-      PL[pi * PJ + pj] = v.lo;
     }
   }
   __syncthreads();
   const df ax{co.axh, co.axl}, ay{co.ayh, co.ayl};
   float acc = 0.f;
-  for (int ti = ty; ti < TI; ti += TC::RG) {
+#pragma unroll
+  for (int it = 0; it < RQ; ++it) {
+    const int ti = ty + it * TC::RG;
     const int gi = i0 + ti;
-    if (gi >= L.n) break;
+    if (ti >= TI || gi >= L.n) break;
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
       const int tj = tx + q * TC::PAIRS;
@@ -495,7 +536,7 @@ __global__ void __launch_bounds__(TC::NTH) k_cv_up0(
         const df xm = gi > 0 ? df{PH[c - PJ], PL[c - PJ]} : pc;   // Neumann ghosts
         const df yp = gj < L.m - 1 ? df{PH[c + 1], PL[c + 1]} : pc;
         const df ym = gj > 0 ? df{PH[c - 1], PL[c - 1]} : pc;
-        const df res = df_residual(ldg(b + k), pc, xp, xm, yp, ym, ax, ay);
+        const df res = df_residual(bpre[it][q], pc, xp, xm, yp, ym, ax, ay);
         rr = res.hi + res.lo;
       }
       if (!profile) r_next[k] = rr;
