@@ -113,6 +113,24 @@ __device__ __forceinline__ void block_sum_atomic(double v, double* dst) {
   __syncthreads();
 }
 
+// Block-wide sum of one double per thread in a fixed order (the result is
+// bit-reproducible); the total is returned to thread 0.  Every thread of the
+// block must call it (it synchronises).
+__device__ __forceinline__ double block_sum(double v) {
+  __shared__ double wb_[32];
+  v = warp_sum(v);
+  const int nthreads = blockDim.x * blockDim.y;
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  const int lane = tid & 31, w = tid >> 5;
+  if (lane == 0) wb_[w] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (tid == 0)
+    for (int k = 0; k < (nthreads >> 5); ++k) t += wb_[k];
+  __syncthreads();
+  return t;
+}
+
 // ------------------------------------------------------------------ dependent launch
 // Programmatic dependent launch: a kernel started with launch_pdl may be
 // scheduled as its predecessor on the stream drains (the launch latency

@@ -758,13 +758,15 @@ __global__ void __launch_bounds__(256) k_nn_feat(const float* __restrict__ b,
   }
 }
 
-// per-sample scales: RMS of channels 0 and 2 over the network grid (FP64
-// sums of a few blocks, the last block to finish turns them into scales) and
-// the output scale rms_r * lmin^2 / 10 (a correction solving A dp = r has
-// that magnitude)
+// per-sample scales: RMS of channels 0 and 2 over the network grid and the
+// output scale rms_r * lmin^2 / 10 (a correction solving A dp = r has that
+// magnitude).  Each block files its FP64 partial sums in part[2 b], part[2 b
+// + 1]; the last block to finish adds them in block order, so the scales -
+// and the correction - are bit-reproducible.
 constexpr int NN_SCALE_BLOCKS = 32;
+static_assert(2 * NN_SCALE_BLOCKS <= kPartials, "the partial sums live in the workspace's part");
 __global__ void __launch_bounds__(512) k_nn_scale(const float* __restrict__ x, long cells,
-                                                  DevScalars* sc, double lmin2) {
+                                                  DevScalars* sc, double lmin2, double* part) {
   pdl_wait();
   float sr = 0.f, sp = 0.f;
   const long stride = (long)gridDim.x * blockDim.x;
@@ -774,22 +776,28 @@ __global__ void __launch_bounds__(512) k_nn_scale(const float* __restrict__ x, l
     sr = fmaf(r, r, sr);
     sp = fmaf(q, q, sp);
   }
-  block_sum_atomic((double)sr, &sc->acc[2]);
-  block_sum_atomic((double)sp, &sc->acc[3]);
+  const double br = block_sum((double)sr);
+  const double bp = block_sum((double)sp);
   __shared__ int am_last;
   if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = br;
+    part[2 * blockIdx.x + 1] = bp;
     __threadfence();
     am_last = atomicAdd(&sc->red_count, 1u) == gridDim.x - 1;
   }
   __syncthreads();
   if (am_last && threadIdx.x == 0) {
     __threadfence();
-    const double rr = sqrt(sc->acc[2] / (double)cells), rp = sqrt(sc->acc[3] / (double)cells);
-    sc->nn_rms_r = rr > 1e-30 ? rr : 1e-30;
-    sc->nn_rms_p = rp > 1e-30 ? rp : 1e-30;
-    sc->nn_out_scale = sc->nn_rms_r * lmin2 / 10.0;
-    sc->acc[2] = 0.0;
-    sc->acc[3] = 0.0;
+    double tr = 0.0, tp = 0.0;
+    for (unsigned b = 0; b < gridDim.x; ++b) {
+      tr += __ldcg(part + 2 * b);
+      tp += __ldcg(part + 2 * b + 1);
+    }
+    const double rr = sqrt(tr / (double)cells), rp = sqrt(tp / (double)cells);
+    const double rrc = rr > 1e-30 ? rr : 1e-30, rpc = rp > 1e-30 ? rp : 1e-30;
+    sc->nn_rms_r = rrc;
+    sc->nn_rms_p = rpc;
+    sc->nn_out_scale = rrc * lmin2 / 10.0;
     sc->red_count = 0u;
   }
 }
@@ -867,7 +875,7 @@ __global__ void k_nn_expand(const float* __restrict__ x3, float* __restrict__ x1
 }
 
 // features (+ optional dataset copy and target) for one step's pressure solve
-int nn_features(const AjStepParams& p, void* ws, const float* b, const float* mask,
+int nn_features(const AjStepParams& p, void* ws, double* part, const float* b, const float* mask,
                 const float* pp, const float* pt, float* x16, float* x3, float* target,
                 cudaStream_t st, bool pdl) {
   const int F = p.nn_factor, h = p.nx / F, w = p.ny / F;
@@ -877,7 +885,7 @@ int nn_features(const AjStepParams& p, void* ws, const float* b, const float* ma
              p.ny, F, (float)(1.0 / (p.dx * p.dx)), (float)(1.0 / (p.dy * p.dy)), x16);
   const double lx = p.nx * p.dx, ly = p.ny * p.dy, lmin = lx < ly ? lx : ly;
   launch_pdl(pdl, k_nn_scale, dim3(NN_SCALE_BLOCKS), dim3(512), 0, st, x16, (long)h * w, sc,
-             lmin * lmin);
+             lmin * lmin, part);
   launch_pdl(pdl, k_nn_norm, dim3(cdiv((long)h * w, 256)), dim3(256), 0, st, x16, x3,
              (long)h * w, (const DevScalars*)sc);
   if (pt && target) k_nn_target<<<grd, blk, 0, st>>>(pt, pp, p.nx, p.ny, F, target, sc);
@@ -894,7 +902,8 @@ int nn_correct_state(const AjStepParams& p, const Layout& L, void* ws, const flo
   NnActs A = act_layout(1, h, w, at<char>(ws, L.nn_act));
   // features, network and correction: one chain of dependent launches (the
   // packed weights were written before the step began)
-  int rc = nn_features(p, ws, b, nn.mask, state, nullptr, A.x, nullptr, nullptr, st, true);
+  int rc = nn_features(p, ws, at<double>(ws, L.part), b, nn.mask, state, nullptr, A.x, nullptr,
+                       nullptr, st, true);
   if (rc != AJ_OK) return rc;
   NnW W{reinterpret_cast<const __nv_bfloat16*>(nn.packed), nn.master};
   rc = nn_forward(1, h, w, W, A, st, false);
@@ -1002,8 +1011,8 @@ int32_t aj_nn_features(const AjStepParams* prm, const float* b, const float* mas
   if (!ws || ws_bytes < L.total) return AJ_ERR_WORKSPACE;
   const int F = prm->nn_factor;
   NnActs A = act_layout(1, prm->nx / F, prm->ny / F, at<char>(ws, L.nn_act));
-  return nn_features(*prm, ws, b, mask, p_prev, p_true, A.x, x3_out, target_out,
-                     (cudaStream_t)stream, false);
+  return nn_features(*prm, ws, at<double>(ws, L.part), b, mask, p_prev, p_true, A.x, x3_out,
+                     target_out, (cudaStream_t)stream, false);
 }
 
 int32_t aj_nn_adam(float* master, const float* grad, float* m, float* v, int32_t step, float lr,

@@ -261,3 +261,48 @@ def test_converging_shapes(cuda_lib, shape):
     p6, info6 = R.mg_converge(bb, dx, dx, rtol=1e-6, max_cycles=80)
     assert abs(st["cycles"] - info6["cycles"]) <= 2, (st["cycles"], info6["cycles"])
     assert rel(p, pref) <= 2.0 * rel(p6, pref) + 2e-6
+
+
+_PDL_SCRIPT = r"""
+import sys, numpy as np, torch
+sys.path.insert(0, sys.argv[1])
+from dataclasses import replace
+from aerojax_gb300 import configs, nn
+import aerojax_gb300 as aj
+c = configs.naca_mac_2048x512(nx=1024, ny=256, mg_mode="converge")
+net = nn.WarmStartNet.load(nn.WEIGHTS, device="cuda")
+out = {}
+for arm in ("extrap", "nn"):
+    plan = aj.get_plan(replace(c["cfg"], warm_start="extrapolate",
+                               nn_factor=8 if arm == "nn" else 0), "cuda")
+    plan.prepare(c["mask"])
+    u, v, p = c["u"].clone(), c["v"].clone(), torch.zeros((1024, 256), device="cuda")
+    for _ in range(4):
+        if arm == "nn":
+            u, v, p = nn.run_step_nn(plan, net, u, v, c["mask"], p)
+        else:
+            u, v, p = aj.run_step(plan, u, v, c["mask"], p_guess=p)
+        assert plan.stats()["err"] == 0
+    out[arm + "_u"], out[arm + "_v"], out[arm + "_p"] = (t.cpu().numpy() for t in (u, v, p))
+np.savez(sys.argv[2], **out)
+"""
+
+
+def test_dependent_launches_change_nothing(cuda_lib, tmp_path):
+    """Programmatic dependent launch only moves when a kernel is scheduled:
+    four steps of the extrapolation and learned-warm-start arms are bit for
+    bit the same with it (the default) and without it (AEROJAX_PDL=0)."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    res = {}
+    for mode in ("1", "0"):
+        f = tmp_path / f"pdl{mode}.npz"
+        env = dict(os.environ, AEROJAX_PDL=mode)
+        r = subprocess.run([sys.executable, "-c", _PDL_SCRIPT, root, str(f)], env=env,
+                           capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stderr[-2000:]
+        res[mode] = np.load(f)
+    for k in res["1"].files:
+        assert np.array_equal(res["1"][k], res["0"][k]), k
