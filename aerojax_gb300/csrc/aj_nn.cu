@@ -71,7 +71,7 @@ __device__ __forceinline__ void mma_bf16(float* d, const uint32_t* a, const uint
 // keep the fragment loads free of bank conflicts.
 constexpr int CT = 8;                       // pixel tile edge
 constexpr int CT_HALO = (CT + 2) * (CT + 2);
-constexpr int CONV_THREADS = 128;
+constexpr int CONV_THREADS = 256;   // 8 warps: 4 pixel-row pairs x 2 halves of K
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
@@ -108,9 +108,8 @@ struct ConvArgs {
 
 // One 8 x 8 pixel tile t (tiles ordered w fastest, then h, then sample) and
 // the BN = NT * 8 output channels from co0.  PDL: dependent launch (wait for
-// the previous layer after staging the weights).  A caller that runs several
-// tiles in a row puts a block barrier between them (the next staging
-// overwrites shared memory that other warps may still be reading).
+// the previous layer after staging the weights).  Warps 4-7 return before the
+// epilogue: nothing after the K halves' hand-over may synchronise the block.
 template <int CIN, int NT, bool PDL>
 __device__ __forceinline__ void conv_tile(const ConvArgs& cv, int t, int co0,
                                           unsigned char* conv_sm) {
@@ -184,9 +183,13 @@ __device__ __forceinline__ void conv_tile(const ConvArgs& cv, int t, int co0,
   float acc[NT][4];
 #pragma unroll
   for (int q = 0; q < NT; ++q) acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.f;
-  const int ty0 = 2 * warp;   // this warp's tile rows: ty0 (fragment rows g) and ty0 + 1 (g + 8)
+  // warp w: tile rows 2 (w & 3) and 2 (w & 3) + 1 (fragment rows g, g + 8);
+  // warps 0-3 run taps 0-4 and warps 4-7 taps 5-8, which halves each chain
+  // of dependent MMAs (9 Cin / 16 of them in one warp before)
+  const int prow = warp & 3, kh = warp >> 2;
+  const int ty0 = 2 * prow;
 #pragma unroll 1
-  for (int tap = 0; tap < 9; ++tap) {
+  for (int tap = kh ? 5 : 0; tap < (kh ? 9 : 5); ++tap) {
     const int dy = tap / 3, dx = tap % 3;   // halo offsets (tap - centre + 1)
     const float* a0p = As + ((ty0 + dy) * (CT + 2) + g + dx) * AS + tg * 2;
     const float* a1p = a0p + (CT + 2) * AS;
@@ -212,6 +215,23 @@ __device__ __forceinline__ void conv_tile(const ConvArgs& cv, int t, int co0,
       }
     }
   }
+  // warps 4-7 hand their partial sums to warps 0-3 through the (now free)
+  // halo buffer; the sum is (taps 0-4) + (taps 5-8)
+  static_assert(4 * NT * 4 * 32 <= CT_HALO * AS, "the hand-over must fit the halo buffer");
+  __syncthreads();
+  float* red = As;   // 4 x NT x 4 x 32 floats <= the halo buffer for every CIN
+  if (kh) {
+#pragma unroll
+    for (int q = 0; q < NT; ++q)
+#pragma unroll
+      for (int e = 0; e < 4; ++e) red[((prow * NT + q) * 4 + e) * 32 + lane] = acc[q][e];
+  }
+  __syncthreads();
+  if (kh) return;
+#pragma unroll
+  for (int q = 0; q < NT; ++q)
+#pragma unroll
+    for (int e = 0; e < 4; ++e) acc[q][e] += red[((prow * NT + q) * 4 + e) * 32 + lane];
   // epilogue: bias, ReLU, store; with Yp also the 2x2 average pool of the
   // output (the warp holds both rows of a pooling window; the column
   // neighbour is 4 lanes up), summed in the order s00 + s10 + s01 + s11 of the
