@@ -13,6 +13,8 @@ Arms on the GPU (whole step captured in one CUDA graph each):
            aerojax_gb300/weights) corrects the double-FP32 extrapolation of the
            last two pressures, then the converging multigrid
   extrap   aj_step with the extrapolated warm start alone
+  prev     aj_step warm-started from the previous step's FP32 pressure (the
+           "without network" baseline of the learned warm start)
   plain    the plain GPU multigrid step: zero initial guess, same tolerance
 value = cell-steps/s of `nn` (the metric's arm); the others are reported in
 config.arms.
@@ -206,11 +208,11 @@ def gpu_arm(args):
         net = NNW.WarmStartNet.load(NNW.WEIGHTS, device=dev)
 
     def make_arm(kind):
-        """plain: zero initial guess; extrap: double-FP32 extrapolation of the
-        last two solutions; nn: the extrapolation plus the network's
-        correction (the metric's arm)."""
+        """plain: zero initial guess; prev: the previous step's FP32 pressure;
+        extrap: double-FP32 extrapolation of the last two solutions; nn: the
+        extrapolation plus the network's correction (the metric's arm)."""
         from dataclasses import replace
-        warm = {"plain": False, "extrap": "extrapolate", "nn": "extrapolate"}[kind]
+        warm = {"plain": False, "prev": True, "extrap": "extrapolate", "nn": "extrapolate"}[kind]
         cfg = replace(case["cfg"], warm_start=warm, nn_factor=NN_FACTOR if kind == "nn" else 0)
         plan = aj.get_plan(cfg, dev)
         plan.prepare(mask)
@@ -273,8 +275,10 @@ def gpu_arm(args):
     results = {}
     clocks = ClockSampler(local)
     clk = None
-    for kind in ("plain", "extrap", "nn"):
+    for kind in ("plain", "prev", "extrap", "nn"):
         if kind == "nn" and net is None:
+            continue
+        if kind == "prev" and args.quick:
             continue
         plan, bufs = make_arm(kind)
         run(plan, bufs, max(3, args.warmup), False, kind)
