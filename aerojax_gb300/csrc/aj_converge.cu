@@ -174,27 +174,41 @@ template <class TC, bool INTERIOR>
 __device__ __forceinline__ void cv_sweeps_t(float* E, const float* R, const CvLvl& L, int gi0,
                                             int gj0) {
   constexpr int SJ = TC::SJ, SI = TC::SI;
+  constexpr int ROWS = (SI - 2 + TC::RG - 1) / TC::RG;   // rows of a thread per half-sweep
   const int tx = threadIdx.x, ty = threadIdx.y;
   const float inv_int = 1.f / (-2.f * (L.ax + L.ay));
   for (int h = 0; h < 2 * CV_NS; ++h) {
     const int color = h & 1;
-#pragma unroll 4
-    for (int ti = 1 + ty; ti < SI - 1; ti += TC::RG) {
+    // every new value of this thread's rows first, then the stores: a
+    // half-sweep reads only the other colour, so no store can feed a load of
+    // the same half-sweep, and the loads of all rows are in flight together
+    float val[ROWS];
+    int cc[ROWS];
+#pragma unroll
+    for (int q = 0; q < ROWS; ++q) {
+      const int ti = 1 + ty + q * TC::RG;
       const int tj = 2 * tx + ((color + ti) & 1);
       const int gi = gi0 + ti, gj = gj0 + tj;
-      const bool upd = INTERIOR ? (tj >= 1 && tj < SJ - 1)
-                                : (tj >= 1 && tj < SJ - 1 && (unsigned)gi < (unsigned)L.n &&
-                                   (unsigned)gj < (unsigned)L.m &&
-                                   !(L.level == 0 && gi == L.n - 1));
+      const bool upd = ti < SI - 1 &&
+                       (INTERIOR ? (tj >= 1 && tj < SJ - 1)
+                                 : (tj >= 1 && tj < SJ - 1 && (unsigned)gi < (unsigned)L.n &&
+                                    (unsigned)gj < (unsigned)L.m &&
+                                    !(L.level == 0 && gi == L.n - 1)));
+      cc[q] = -1;
+      val[q] = 0.f;
       if (upd) {
         const int c = ti * SJ + tj;
         const float nb = L.ax * (E[c + SJ] + E[c - SJ]) + L.ay * (E[c + 1] + E[c - 1]);
         float inv = inv_int;
         if (!INTERIOR && (gi == 0 || gj == 0 || gi == L.n - 1 || gj == L.m - 1))
           inv = 1.f / cv_diag(L, gi, gj);
-        E[c] = (R[c] - nb) * inv;
+        val[q] = (R[c] - nb) * inv;
+        cc[q] = c;
       }
     }
+#pragma unroll
+    for (int q = 0; q < ROWS; ++q)
+      if (cc[q] >= 0) E[cc[q]] = val[q];
     __syncthreads();
   }
 }
