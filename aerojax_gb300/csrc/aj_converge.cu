@@ -313,25 +313,37 @@ __global__ void __launch_bounds__(TC::NTH) k_cv_down(CvLvl L, const float* r0, c
   const float* r = (r1 && *cur) ? r1 : r0;
   cv_load<TC, true>(E, R, L, gi0, gj0, r, nullptr, nullptr);
   cv_sweeps<TC>(E, R, L, gi0, gj0);
-  // store e and compute the residual on the tile interior (in place in R)
-  for (int ti = CV_H + ty; ti < CV_H + TI; ti += TC::RG) {
+  // store e and compute the residual on the tile interior (in place in R:
+  // every residual of this thread first, then the stores, so that no store
+  // holds back the next cell's loads)
+  constexpr int DR = (TI + TC::RG - 1) / TC::RG;
+  float res[DR][2];
+  int rc_[DR][2];
+#pragma unroll
+  for (int it = 0; it < DR; ++it) {
+    const int ti = CV_H + ty + it * TC::RG;
     const int gi = gi0 + ti;
-    if (gi >= L.n) break;
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
       const int tj = CV_H + tx + q * TC::PAIRS;
       const int gj = gj0 + tj;
-      if (tj >= CV_H + TJ || gj >= L.m) continue;
+      rc_[it][q] = -1;
+      res[it][q] = 0.f;
+      if (ti >= CV_H + TI || gi >= L.n || tj >= CV_H + TJ || gj >= L.m) continue;
       const int c = ti * SJ + tj;
       e_out[(long)gi * L.m + gj] = E[c];
-      float res = 0.f;
       if (!(L.level == 0 && gi == L.n - 1)) {
         const float nb = L.ax * (E[c + SJ] + E[c - SJ]) + L.ay * (E[c + 1] + E[c - 1]);
-        res = R[c] - (nb + cv_diag(L, gi, gj) * E[c]);
+        res[it][q] = R[c] - (nb + cv_diag(L, gi, gj) * E[c]);
       }
-      R[c] = res;
+      rc_[it][q] = c;
     }
   }
+#pragma unroll
+  for (int it = 0; it < DR; ++it)
+#pragma unroll
+    for (int q = 0; q < 2; ++q)
+      if (rc_[it][q] >= 0) R[rc_[it][q]] = res[it][q];
   __syncthreads();
   const int mc = L.m >> 1, nc = L.n >> 1;
   for (int ci = ty; ci < TI / 2; ci += TC::RG) {
@@ -509,23 +521,37 @@ __global__ void __launch_bounds__(TC::NTH, 4) k_cv_up0(
   cv_sweeps<TC>(E, R, L, gi0, gj0);
   asm volatile("cp.async.wait_group 0;\n" ::: "memory");
   __syncthreads();
-  // new pressure on the interior and one cell around it
-  for (int pi = ty; pi < PI; pi += TC::RG) {
+  // new pressure on the interior and one cell around it (all of this
+  // thread's sums first, then the stores)
+  constexpr int PR = (PI + TC::RG - 1) / TC::RG;
+  df pv[PR][2];
+  int pt[PR][2];
+#pragma unroll
+  for (int it = 0; it < PR; ++it) {
+    const int pi = ty + it * TC::RG;
     const int gi = i0 - 1 + pi;
-    const bool row_in = (unsigned)gi < (unsigned)L.n && gi != L.n - 1;
+    const bool row_in = pi < PI && (unsigned)gi < (unsigned)L.n && gi != L.n - 1;
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
       const int pj = tx + q * TC::PAIRS;
-      if (pj >= PJ) continue;
       const int gj = j0 - 1 + pj;
-      if (row_in && (unsigned)gj < (unsigned)L.m) {
+      pt[it][q] = -1;
+      pv[it][q] = df{0.f, 0.f};
+      if (row_in && pj < PJ && (unsigned)gj < (unsigned)L.m) {
         const int t = pi * PJ + pj;
-        const df v = df_add_f(df{PH[t], PL[t]}, E[(CV_H - 1 + pi) * SJ + (CV_H - 1 + pj)]);
-        PH[t] = v.hi;
-        PL[t] = v.lo;
+        pv[it][q] = df_add_f(df{PH[t], PL[t]}, E[(CV_H - 1 + pi) * SJ + (CV_H - 1 + pj)]);
+        pt[it][q] = t;
       }
     }
   }
+#pragma unroll
+  for (int it = 0; it < PR; ++it)
+#pragma unroll
+    for (int q = 0; q < 2; ++q)
+      if (pt[it][q] >= 0) {
+        PH[pt[it][q]] = pv[it][q].hi;
+        PL[pt[it][q]] = pv[it][q].lo;
+      }
   __syncthreads();
   const df ax{co.axh, co.axl}, ay{co.ayh, co.ayl};
   float acc = 0.f;
