@@ -284,35 +284,82 @@ struct NnRef {
   const float* master = nullptr;
 };
 
+// Side branches of a step (two streams, four events) per lane: lane i of an
+// ensemble capture uses its own, so that no two instances' branches chain.
+// Captures are serialised by g_mu; eager launches use the same objects.
+struct StepForks {
+  cudaStream_t les, init;
+  cudaEvent_t start, les_done, dt_done, init_done;
+};
+static const StepForks* step_forks(int lane) {
+  static std::vector<StepForks> v;
+  static std::mutex mu;
+  std::lock_guard<std::mutex> lk(mu);
+  while ((int)v.size() <= lane) {
+    StepForks f;
+    if (cudaStreamCreateWithFlags(&f.les, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&f.init, cudaStreamNonBlocking) != cudaSuccess)
+      return nullptr;
+    cudaEvent_t* e[4] = {&f.start, &f.les_done, &f.dt_done, &f.init_done};
+    for (cudaEvent_t* q : e)
+      if (cudaEventCreateWithFlags(q, cudaEventDisableTiming) != cudaSuccess) return nullptr;
+    v.push_back(f);
+  }
+  return &v[lane];
+}
+
+// One step.  Two pieces of work run beside the main chain: the LES viscosity
+// (it reads only the input velocities) beside the CFL reduction, and the
+// converging solve's initial state (it needs dt and the history, not the
+// rhs) beside the predictor and the divergence.
 static int enqueue_step(const AjStepParams& p, const Layout& L, void* ws, const float* u,
                         const float* v, const float* mask, const float* p_guess, float* uo,
                         float* vo, float* po, AjStats* stats, cudaStream_t st,
-                        NnRef nn = NnRef()) {
-  int rc = p.cfl_dt ? launch_cfl(p, ws, u, v, nullptr, st) : launch_set_dt(p, ws, st);
-  if (rc != AJ_OK) return rc;
+                        NnRef nn = NnRef(), int lane = 0) {
+  const StepForks* fk = step_forks(lane);
+  if (!fk) return AJ_ERR_CUDA;
   const bool mac = p.grid_type == AJ_GRID_MAC;
-  const float* nsg = nullptr;
-  int dc = 0;
   // step_pure computes the LES field on the collocated path but never passes it
   // on (step.py:177-180): nothing to do.  The GUI step and MAC use it.
-  if (p.les_model != AJ_LES_NONE && (p.variant == AJ_VARIANT_GUI || mac)) {
+  const bool les = p.les_model != AJ_LES_NONE && (p.variant == AJ_VARIANT_GUI || mac);
+  const bool conv = p.mg_mode == AJ_MG_CONVERGE;
+  const float* nsg = nullptr;
+  int dc = 0;
+  int rc;
+  if (les) {
     float* f = at<float>(ws, L.nu_sgs);
-    rc = launch_les(p, L, ws, p.les_model, u, v, mac, f, nullptr, st);
+    if (cudaEventRecord(fk->start, st) != cudaSuccess ||
+        cudaStreamWaitEvent(fk->les, fk->start, 0) != cudaSuccess)
+      return AJ_ERR_CUDA;
+    rc = launch_les(p, L, ws, p.les_model, u, v, mac, f, nullptr, fk->les);
     if (rc != AJ_OK) return rc;
+    if (cudaEventRecord(fk->les_done, fk->les) != cudaSuccess) return AJ_ERR_CUDA;
     nsg = f;
     dc = (p.variant == AJ_VARIANT_GUI && !mac) ? 1 : 0;
   }
+  rc = p.cfl_dt ? launch_cfl(p, ws, u, v, nullptr, st) : launch_set_dt(p, ws, st);
+  if (rc != AJ_OK) return rc;
+  if (conv) {
+    if (cudaEventRecord(fk->dt_done, st) != cudaSuccess ||
+        cudaStreamWaitEvent(fk->init, fk->dt_done, 0) != cudaSuccess)
+      return AJ_ERR_CUDA;
+    rc = converge_init(p, L, ws, p_guess, fk->init);
+    if (rc != AJ_OK) return rc;
+    if (cudaEventRecord(fk->init_done, fk->init) != cudaSuccess) return AJ_ERR_CUDA;
+  }
+  if (les && cudaStreamWaitEvent(st, fk->les_done, 0) != cudaSuccess) return AJ_ERR_CUDA;
   float* us = at<float>(ws, L.sS_u);
   float* vs = at<float>(ws, L.sS_v);
   rc = launch_predictor(p, L, ws, u, v, mask, nsg, dc, us, vs, st);
   if (rc != AJ_OK) return rc;
   rc = launch_rhs(p, L, ws, us, vs, mask, at<float>(ws, L.b0), st);
   if (rc != AJ_OK) return rc;
+  if (conv && cudaStreamWaitEvent(st, fk->init_done, 0) != cudaSuccess) return AJ_ERR_CUDA;
   NnWarm nw;
   nw.packed = nn.packed;
   nw.master = nn.master;
   nw.mask = mask;
-  rc = launch_pressure(p, L, ws, mask, p_guess, po, stats, st, nn.packed ? &nw : nullptr);
+  rc = launch_pressure(p, L, ws, mask, p_guess, po, stats, st, nn.packed ? &nw : nullptr, conv);
   if (rc != AJ_OK) return rc;
   return launch_correct(p, L, ws, us, vs, po, mask, uo, vo, st);
 }
@@ -572,7 +619,7 @@ int32_t aj_ensemble_step(int32_t n, const AjStepParams* prms, const float* const
       if (cudaStreamWaitEvent(br[i], ev[n], 0) != cudaSuccess) return (int)AJ_ERR_CUDA;
       const float* pg = (P[i].warm_start && p_guess) ? p_guess[i] : nullptr;
       int rc = enqueue_step(P[i], Ls[i], ws[i], u[i], v[i], mask[i], pg, u_out[i], v_out[i],
-                            p_out[i], stats ? stats + i : nullptr, br[i]);
+                            p_out[i], stats ? stats + i : nullptr, br[i], NnRef(), i);
       if (rc != AJ_OK) return rc;
       if (cudaEventRecord(ev[i], br[i]) != cudaSuccess) return (int)AJ_ERR_CUDA;
     }

@@ -1328,8 +1328,10 @@ static cudaStream_t side_stream() {
   return s;
 }
 
-int converge_solve(const AjStepParams& p, const Layout& L, void* ws, const float* p0,
-                   float* pout, cudaStream_t st, const NnWarm* nn, AjStats* stats) {
+// the initial double-FP32 state (needs the step's dt and the history, not
+// the rhs: the step runs it beside the predictor)
+int converge_init(const AjStepParams& p, const Layout& L, void* ws, const float* p0,
+                  cudaStream_t st) {
   DevScalars* sc = at<DevScalars>(ws, 0);
   const long N = (long)p.nx * p.ny;
   const PState ps = pstate(L, ws);
@@ -1337,7 +1339,22 @@ int converge_solve(const AjStepParams& p, const Layout& L, void* ws, const float
   const bool extrap = p.warm_start == AJ_WARM_EXTRAPOLATE && L.hist;
   CvHist hs{extrap ? at<float>(ws, L.hist) : nullptr, N};
   launch_pdl(true, k_cv_init, dim3(rgrid), dim3(256), 0, st, p.warm_start ? p0 : nullptr, ps.a,
-             p.nx, p.ny, hs, sc);
+             p.nx, p.ny, hs, (const DevScalars*)sc);
+  return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+}
+
+int converge_solve(const AjStepParams& p, const Layout& L, void* ws, const float* p0,
+                   float* pout, cudaStream_t st, const NnWarm* nn, AjStats* stats,
+                   bool init_done) {
+  DevScalars* sc = at<DevScalars>(ws, 0);
+  const long N = (long)p.nx * p.ny;
+  const PState ps = pstate(L, ws);
+  const dim3 rgrid(cdiv(p.ny, 256), cdiv(p.nx, CV_ROWS));
+  const bool extrap = p.warm_start == AJ_WARM_EXTRAPOLATE && L.hist;
+  if (!init_done) {
+    const int rc = converge_init(p, L, ws, p0, st);
+    if (rc != AJ_OK) return rc;
+  }
   if (nn && nn->packed) {
     const int rc = nn_correct_state(p, L, ws, at<float>(ws, L.b0), *nn, ps.a, st);
     if (rc != AJ_OK) return rc;

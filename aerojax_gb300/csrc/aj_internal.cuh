@@ -190,16 +190,20 @@ struct NnWarm {
   const float* master = nullptr;
   const float* mask = nullptr;
 };
+// init_done: converge_init already ran (the step launches it beside the
+// predictor)
 int launch_pressure(const AjStepParams& p, const Layout& L, void* ws, const float* mask,
                     const float* p0, float* pout, AjStats* stats, cudaStream_t st,
-                    const NnWarm* nn = nullptr);
+                    const NnWarm* nn = nullptr, bool init_done = false);
 int profile_pressure_kernel(const AjStepParams& p, const Layout& L, void* ws, int which,
                             cudaStream_t st);
 // converging multigrid (aj_converge.cu)
 int converge_prepare(const AjStepParams& p, const Layout& L, void* ws, cudaStream_t st);
 int converge_solve(const AjStepParams& p, const Layout& L, void* ws, const float* p0,
                    float* pout, cudaStream_t st, const NnWarm* nn = nullptr,
-                   AjStats* stats = nullptr);
+                   AjStats* stats = nullptr, bool init_done = false);
+int converge_init(const AjStepParams& p, const Layout& L, void* ws, const float* p0,
+                  cudaStream_t st);
 size_t converge_block_smem(const Layout& L, int lc);
 int converge_first_block_level(const Layout& L);
 int converge_direct_level(const Layout& L);

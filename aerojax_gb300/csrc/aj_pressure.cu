@@ -320,14 +320,14 @@ int prepare_pressure(const AjStepParams& p, const Layout& L, void* ws, const flo
 
 int launch_pressure(const AjStepParams& p, const Layout& L, void* ws, const float* mask,
                     const float* p0, float* pout, AjStats* stats, cudaStream_t st,
-                    const NnWarm* nn) {
+                    const NnWarm* nn, bool init_done) {
   int rc;
   if (p.mg_mode == AJ_MG_PARITY) {
     rc = parity_solve(p, L, ws, mask, p0, pout, st);
     if (rc != AJ_OK) return rc;
     if (stats) k_stats<<<1, 1, 0, st>>>(at<DevScalars>(ws, 0), stats, 0);
   } else {
-    rc = converge_solve(p, L, ws, p0, pout, st, nn, stats);   // k_cv_out files the stats
+    rc = converge_solve(p, L, ws, p0, pout, st, nn, stats, init_done);   // k_cv_out: stats
     if (rc != AJ_OK) return rc;
   }
   return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
