@@ -104,6 +104,8 @@ struct ConvArgs {
   int relu;
   float* Yp;         // nullable: 2x2 average pool of Y
   const float* Xc;   // nullable: the input is up2(Xc) + X
+  const DevScalars* norm;   // nullable: scale input channels 0 and 2 by 1 / the
+                            // sample's RMS (the features' normalisation)
 };
 
 // One 8 x 8 pixel tile t (tiles ordered w fastest, then h, then sample) and
@@ -159,6 +161,14 @@ __device__ __forceinline__ void conv_tile(const ConvArgs& cv, int t, int co0,
   }
   cp_async_wait<0>();
   __syncthreads();
+  if (cv.norm) {   // k_nn_norm's scaling of the staged features (same arithmetic)
+    const float ir = (float)(1.0 / cv.norm->nn_rms_r), ip = (float)(1.0 / cv.norm->nn_rms_p);
+    for (int px = tid; px < CT_HALO; px += CONV_THREADS) {
+      As[px * AS] *= ir;
+      As[px * AS + 2] *= ip;
+    }
+    __syncthreads();
+  }
   if (Xc) {   // input = nearest 2x up-sampling of Xc (H/2 x W/2) + X
     constexpr int C4 = CIN / 4;
     const int Hc = H >> 1, Wc = W >> 1;
@@ -280,12 +290,12 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv3x3(ConvArgs a) {
 template <int CIN, int NT>
 static void conv_launch(const float* X, int N, int H, int W, int Cout, const __nv_bfloat16* WT,
                         const float* bias, float* Y, int relu, float* Yp, const float* Xc,
-                        cudaStream_t st, bool pdl) {
+                        cudaStream_t st, bool pdl, const DevScalars* norm) {
   using S = ConvSmem<CIN, NT>;
   const int tiles = ((W + CT - 1) / CT) * ((H + CT - 1) / CT) * N;
   dim3 grid(tiles, Cout / S::BN);
   launch_pdl(pdl, k_conv3x3<CIN, NT>, grid, dim3(CONV_THREADS), S::bytes, st,
-             ConvArgs{X, N, H, W, Cout, WT, bias, Y, relu, Yp, Xc});
+             ConvArgs{X, N, H, W, Cout, WT, bias, Y, relu, Yp, Xc, norm});
 }
 
 template <int CIN, int NT>
@@ -308,7 +318,7 @@ static void conv_attrs() {
 template <int CIN>
 static int conv_cin(const float* X, int N, int H, int W, int Cout, const __nv_bfloat16* WT,
                     const float* bias, float* Y, int relu, float* Yp, const float* Xc,
-                    cudaStream_t st, bool pdl) {
+                    cudaStream_t st, bool pdl, const DevScalars* norm) {
   // 32 output channels per block, or 16 when that leaves fewer blocks than
   // SMs (the small grids of the deep layers are latency-bound: more, lighter
   // blocks load their weights sooner)
@@ -319,8 +329,8 @@ static int conv_cin(const float* X, int N, int H, int W, int Cout, const __nv_bf
     case 32:
     case 64:
     case 128:
-      if (narrow) conv_launch<CIN, 2>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, Xc, st, pdl);
-      else conv_launch<CIN, 4>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, Xc, st, pdl);
+      if (narrow) conv_launch<CIN, 2>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, Xc, st, pdl, norm);
+      else conv_launch<CIN, 4>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, Xc, st, pdl, norm);
       break;
     default: return AJ_ERR_PARAM;
   }
@@ -334,12 +344,12 @@ static int conv_cin(const float* X, int N, int H, int W, int Cout, const __nv_bf
 static int conv3x3(const float* X, int N, int H, int W, int Cin, int Cout,
                    const __nv_bfloat16* WT, const float* bias, float* Y, int relu,
                    cudaStream_t st, float* Yp = nullptr, const float* Xc = nullptr,
-                   bool pdl = false) {
+                   bool pdl = false, const DevScalars* norm = nullptr) {
   switch (Cin) {
-    case 16: return conv_cin<16>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, Xc, st, pdl);
-    case 32: return conv_cin<32>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, Xc, st, pdl);
-    case 64: return conv_cin<64>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, Xc, st, pdl);
-    case 128: return conv_cin<128>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, Xc, st, pdl);
+    case 16: return conv_cin<16>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, Xc, st, pdl, norm);
+    case 32: return conv_cin<32>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, Xc, st, pdl, norm);
+    case 64: return conv_cin<64>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, Xc, st, pdl, norm);
+    case 128: return conv_cin<128>(X, N, H, W, Cout, WT, bias, Y, relu, Yp, Xc, st, pdl, norm);
     default: return AJ_ERR_PARAM;
   }
 }
@@ -629,13 +639,13 @@ static inline unsigned ew_blocks(long T) { return cdiv(T, 256); }
 // (the backward pass needs them); else the decoder convolutions add the
 // up-sampled coarse input while staging their halo (inference).
 int nn_forward(int n, int h, int w, const NnW& W, const NnActs& A, cudaStream_t st,
-               bool keep = true) {
+               bool keep = true, const DevScalars* norm = nullptr) {
   const int H0 = h, W0 = w, H1 = h / 2, W1 = w / 2, H2 = h / 4, W2 = w / 4, H3 = h / 8, W3 = w / 8;
   // inference launches the convolutions as one chain of dependent launches
   auto conv = [&](int l, const float* in, float* out, int H, int Wd, float* pooled = nullptr,
                   const float* coarse = nullptr) {
     return conv3x3(in, n, H, Wd, kLayers[l].cin, kLayers[l].cout, W.wf(l), W.bias(l), out,
-                   kLayers[l].relu, st, pooled, coarse, !keep);
+                   kLayers[l].relu, st, pooled, coarse, !keep, l == E0A ? norm : nullptr);
   };
   int rc = AJ_OK;
   rc |= conv(E0A, A.x, A.a0, H0, W0);
@@ -897,7 +907,7 @@ __global__ void k_nn_expand(const float* __restrict__ x3, float* __restrict__ x1
 // features (+ optional dataset copy and target) for one step's pressure solve
 int nn_features(const AjStepParams& p, void* ws, double* part, const float* b, const float* mask,
                 const float* pp, const float* pt, float* x16, float* x3, float* target,
-                cudaStream_t st, bool pdl) {
+                cudaStream_t st, bool pdl, bool normalise) {
   const int F = p.nn_factor, h = p.nx / F, w = p.ny / F;
   DevScalars* sc = at<DevScalars>(ws, 0);
   dim3 blk(32, 8), grd(cdiv(w, 32), cdiv(h, 8));
@@ -906,8 +916,9 @@ int nn_features(const AjStepParams& p, void* ws, double* part, const float* b, c
   const double lx = p.nx * p.dx, ly = p.ny * p.dy, lmin = lx < ly ? lx : ly;
   launch_pdl(pdl, k_nn_scale, dim3(NN_SCALE_BLOCKS), dim3(512), 0, st, x16, (long)h * w, sc,
              lmin * lmin, part);
-  launch_pdl(pdl, k_nn_norm, dim3(cdiv((long)h * w, 256)), dim3(256), 0, st, x16, x3,
-             (long)h * w, (const DevScalars*)sc);
+  if (normalise)
+    launch_pdl(pdl, k_nn_norm, dim3(cdiv((long)h * w, 256)), dim3(256), 0, st, x16, x3,
+               (long)h * w, (const DevScalars*)sc);
   if (pt && target) k_nn_target<<<grd, blk, 0, st>>>(pt, pp, p.nx, p.ny, F, target, sc);
   return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
 }
@@ -922,11 +933,12 @@ int nn_correct_state(const AjStepParams& p, const Layout& L, void* ws, const flo
   NnActs A = act_layout(1, h, w, at<char>(ws, L.nn_act));
   // features, network and correction: one chain of dependent launches (the
   // packed weights were written before the step began)
+  // (the first convolution normalises the features as it stages them)
   int rc = nn_features(p, ws, at<double>(ws, L.part), b, nn.mask, state, nullptr, A.x, nullptr,
-                       nullptr, st, true);
+                       nullptr, st, true, false);
   if (rc != AJ_OK) return rc;
   NnW W{reinterpret_cast<const __nv_bfloat16*>(nn.packed), nn.master};
-  rc = nn_forward(1, h, w, W, A, st, false);
+  rc = nn_forward(1, h, w, W, A, st, false, at<DevScalars>(ws, 0));
   if (rc != AJ_OK) return rc;
   dim3 blk(32, 8), grd(cdiv(p.ny, 32), cdiv(p.nx, 8));
   launch_pdl(true, k_nn_apply, grd, blk, 0, st, (const float*)A.y, p.nx, p.ny, F, state,
@@ -1032,7 +1044,7 @@ int32_t aj_nn_features(const AjStepParams* prm, const float* b, const float* mas
   const int F = prm->nn_factor;
   NnActs A = act_layout(1, prm->nx / F, prm->ny / F, at<char>(ws, L.nn_act));
   return nn_features(*prm, ws, at<double>(ws, L.part), b, mask, p_prev, p_true, A.x, x3_out,
-                     target_out, (cudaStream_t)stream, false);
+                     target_out, (cudaStream_t)stream, false, true);
 }
 
 int32_t aj_nn_adam(float* master, const float* grad, float* m, float* v, int32_t step, float lr,
