@@ -286,7 +286,10 @@ struct NnRef {
 
 // Side branches of a step (two streams, four events) per lane: lane i of an
 // ensemble capture uses its own, so that no two instances' branches chain.
-// Captures are serialised by g_mu; eager launches use the same objects.
+// enqueue_step holds g_forks_mu while it records, so that two host threads
+// (each capturing into its own graph, or launching eagerly) never interleave
+// records of the same events.
+std::mutex g_forks_mu;
 struct StepForks {
   cudaStream_t les, init;
   cudaEvent_t start, les_done, dt_done, init_done;
@@ -316,6 +319,7 @@ static int enqueue_step(const AjStepParams& p, const Layout& L, void* ws, const 
                         const float* v, const float* mask, const float* p_guess, float* uo,
                         float* vo, float* po, AjStats* stats, cudaStream_t st,
                         NnRef nn = NnRef(), int lane = 0) {
+  std::lock_guard<std::mutex> forks_lock(g_forks_mu);
   const StepForks* fk = step_forks(lane);
   if (!fk) return AJ_ERR_CUDA;
   const bool mac = p.grid_type == AJ_GRID_MAC;
