@@ -569,7 +569,8 @@ int32_t aj_kernel_count(const AjStepParams* prm, int32_t cycles) {
   }
   if (p.mg_mode == AJ_MG_PARITY) n += 1;                        // stats
   n += 1;                                                       // correction
-  if (p.nn_factor > 0) n += 3 + 12 + 1;                         // features, network, correction
+  // features and scales, 12 convolutions (the first normalises), correction
+  if (p.nn_factor > 0) n += 2 + 12 + 1;
   return n;
 }
 
