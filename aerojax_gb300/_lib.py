@@ -95,6 +95,9 @@ _SIGS = {
     "aj_release_graphs": (c_int32, []),
     "aj_diagnostics": (c_int32, [POINTER(AjStepParams), c_void_p, c_void_p, c_void_p, c_void_p,
                                  c_void_p, c_void_p]),
+    "aj_post_step": (c_int32, [POINTER(AjStepParams), c_void_p, c_void_p, c_void_p, c_void_p,
+                               ctypes.c_float, ctypes.c_float, c_void_p, c_void_p, c_void_p,
+                               c_void_p]),
     "aj_autotune": (c_int32, [POINTER(AjStepParams), c_void_p, c_size_t, c_int32,
                               POINTER(ctypes.c_float), POINTER(c_int32), c_void_p]),
     "aj_ensemble_step": (c_int32, [c_int32, POINTER(AjStepParams), POINTER(c_void_p),

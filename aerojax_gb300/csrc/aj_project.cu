@@ -305,10 +305,64 @@ extern "C" int32_t aj_geometry(int32_t nx, int32_t ny, double lx, double ly, int
 // centred v in y (its names say dv/dx and du/dy); that is reproduced.
 namespace aj {
 
+// Dye (passive scalar) step at cell (i, j), the reference's four variants
+// (operators.py:111-150, operators_mac.py:161-215): c + dt (-(uc dc/dx +
+// vc dc/dy) + kappa lap c), clipped to [0, 1]; (uc, vc) is the cell's velocity.
+struct Dye {
+  const float* c;
+  float* c_out;
+  float dt, kappa, dx2, dy2;   // dx2, dy2: dx*dx and dy*dy rounded once to FP32
+};
+template <bool MAC, bool PER>
+__device__ __forceinline__ float dye_at(const Dye& d, int i, int j, int nx, int ny, float h2x,
+                                        float h2y, float dx, float uc, float vc) {
+  const float* c = d.c;
+  const float cc = c[(long)i * ny + j];
+  // only the neighbours each variant reads: edge-padded (clamped) x and y for
+  // MAC; wrapped for the collocated periodic one; clamped x (which also gives
+  // the one-sided inlet/outlet differences) and wrapped y for the collocated
+  // non-periodic one; MAC periodic differences wrap but its Laplacian clamps
+  const int ipx = PER && !MAC ? wrapi(i + 1, nx) : clampi(i + 1, nx);
+  const int imx = PER && !MAC ? wrapi(i - 1, nx) : clampi(i - 1, nx);
+  const int jpy = (MAC && !PER) ? clampi(j + 1, ny) : wrapi(j + 1, ny);
+  const int jmy = (MAC && !PER) ? clampi(j - 1, ny) : wrapi(j - 1, ny);
+  const float xp = c[(long)ipx * ny + j], xm = c[(long)imx * ny + j];
+  const float yp = c[(long)i * ny + jpy], ym = c[(long)i * ny + jmy];
+  float dcx, dcy, lap;
+  if (MAC && PER) {
+    // periodic central differences, edge-padded Laplacian (laplacian_staggered)
+    const float xwp = c[(long)wrapi(i + 1, nx) * ny + j], xwm = c[(long)wrapi(i - 1, nx) * ny + j];
+    const float yep = c[(long)i * ny + clampi(j + 1, ny)], yem = c[(long)i * ny + clampi(j - 1, ny)];
+    dcx = (xwp - xwm) / h2x;
+    dcy = (yp - ym) / h2y;
+    lap = (xp + xm - 2.f * cc) / d.dx2 + (yep + yem - 2.f * cc) / d.dy2;
+  } else if (MAC) {
+    dcx = (xp - xm) / h2x;
+    dcy = (yp - ym) / h2y;
+    lap = (xp + xm - 2.f * cc) / d.dx2 + (yp + ym - 2.f * cc) / d.dy2;
+  } else if (PER) {
+    dcx = (xp - xm) / h2x;
+    dcy = (yp - ym) / h2y;
+    lap = ((((xm + xp) + ym) + yp) - 4.f * cc) / d.dx2;   // dx^2 for all five points
+  } else {
+    if (i == 0) dcx = (xp - cc) / dx;   // one-sided at the inlet and outlet rows
+    else if (i == nx - 1) dcx = (cc - xm) / dx;
+    else dcx = (xp - xm) / h2x;
+    dcy = (yp - ym) / h2y;   // periodic in y
+    lap = ((xp - 2.f * cc) + xm) / d.dx2 + ((ym + yp) - 2.f * cc) / d.dy2;
+  }
+  const float adv = uc * dcx + vc * dcy;
+  const float cn = cc + d.dt * (-adv + d.kappa * lap);
+  return fminf(fmaxf(cn, 0.f), 1.f);
+}
+
+// The post-step epilogue, one read of the new velocity: vorticity,
+// divergence, speed (step_for_visualization, visualization_step.py:224-256)
+// and the dye step, each optional (null output: not computed).
 template <bool MAC, bool PER>
 __global__ void k_diagnostics(const float* __restrict__ u, const float* __restrict__ v, int nx,
                               int ny, float dx, float dy, float* __restrict__ vort,
-                              float* __restrict__ div, float* __restrict__ speed) {
+                              float* __restrict__ div, float* __restrict__ speed, Dye dye) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= nx || j >= ny) return;
@@ -332,9 +386,10 @@ __global__ void k_diagnostics(const float* __restrict__ u, const float* __restri
     if (div)
       div[k] = (u[(long)(i + 1) * ny + j] - u[(long)i * ny + j]) / dx +
                (v[(long)i * nyv + j + 1] - v[(long)i * nyv + j]) / dy;
-    if (speed) {
+    if (speed || dye.c) {
       const float a = uc(i, j), b = vc(i, j);
-      speed[k] = sqrtf(a * a + b * b);
+      if (speed) speed[k] = sqrtf(a * a + b * b);
+      if (dye.c) dye.c_out[k] = dye_at<true, PER>(dye, i, j, nx, ny, h2x, h2y, dx, a, b);
     }
   } else {
     if (vort) {
@@ -363,25 +418,43 @@ __global__ void k_diagnostics(const float* __restrict__ u, const float* __restri
       div[k] = d;
     }
     if (speed) speed[k] = sqrtf(u[k] * u[k] + v[k] * v[k]);
+    if (dye.c) dye.c_out[k] = dye_at<false, PER>(dye, i, j, nx, ny, h2x, h2y, dx, u[k], v[k]);
   }
 }
 
-}  // namespace aj
-
-extern "C" int32_t aj_diagnostics(const AjStepParams* prm, const float* u, const float* v,
-                                  float* vort, float* div, float* speed, void* stream) {
-  using namespace aj;
+static int post_step(const AjStepParams* prm, const float* u, const float* v, const float* c_in,
+                     float* c_out, float dt, float diffusivity, float* vort, float* div,
+                     float* speed, void* stream) {
   if (!prm || !u || !v || prm->nx < 2 || prm->ny < 2 || prm->dx <= 0 || prm->dy <= 0)
     return AJ_ERR_PARAM;
+  if ((c_in == nullptr) != (c_out == nullptr) || (c_in && c_in == c_out)) return AJ_ERR_PARAM;
   const int nx = prm->nx, ny = prm->ny;
   const bool mac = prm->grid_type == AJ_GRID_MAC;
   const bool per = prm->flow_type != AJ_FLOW_VON_KARMAN;
   const float dx = (float)prm->dx, dy = (float)prm->dy;
+  const Dye dye{c_in, c_out, dt, diffusivity, (float)(prm->dx * prm->dx),
+                (float)(prm->dy * prm->dy)};
   dim3 blk(32, 8), grd(cdiv(ny, 32), cdiv(nx, 8));
   cudaStream_t st = (cudaStream_t)stream;
-  if (mac && per) k_diagnostics<true, true><<<grd, blk, 0, st>>>(u, v, nx, ny, dx, dy, vort, div, speed);
-  else if (mac) k_diagnostics<true, false><<<grd, blk, 0, st>>>(u, v, nx, ny, dx, dy, vort, div, speed);
-  else if (per) k_diagnostics<false, true><<<grd, blk, 0, st>>>(u, v, nx, ny, dx, dy, vort, div, speed);
-  else k_diagnostics<false, false><<<grd, blk, 0, st>>>(u, v, nx, ny, dx, dy, vort, div, speed);
+  if (mac && per)
+    k_diagnostics<true, true><<<grd, blk, 0, st>>>(u, v, nx, ny, dx, dy, vort, div, speed, dye);
+  else if (mac)
+    k_diagnostics<true, false><<<grd, blk, 0, st>>>(u, v, nx, ny, dx, dy, vort, div, speed, dye);
+  else if (per)
+    k_diagnostics<false, true><<<grd, blk, 0, st>>>(u, v, nx, ny, dx, dy, vort, div, speed, dye);
+  else
+    k_diagnostics<false, false><<<grd, blk, 0, st>>>(u, v, nx, ny, dx, dy, vort, div, speed, dye);
   return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+}
+}  // namespace aj
+
+extern "C" int32_t aj_diagnostics(const AjStepParams* prm, const float* u, const float* v,
+                                  float* vort, float* div, float* speed, void* stream) {
+  return aj::post_step(prm, u, v, nullptr, nullptr, 0.f, 0.f, vort, div, speed, stream);
+}
+
+extern "C" int32_t aj_post_step(const AjStepParams* prm, const float* u, const float* v,
+                                const float* c_in, float* c_out, float dt, float diffusivity,
+                                float* vort, float* div, float* speed, void* stream) {
+  return aj::post_step(prm, u, v, c_in, c_out, dt, diffusivity, vort, div, speed, stream);
 }

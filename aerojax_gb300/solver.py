@@ -414,6 +414,31 @@ def diagnostics(u, v, dx, dy, grid_type="collocated", flow_type="von_karman", st
     return tuple(out)
 
 
+def post_step(u, v, c, dt, dx, dy, diffusivity, grid_type="collocated", flow_type="von_karman",
+              diagnostics=True, stream=None):
+    """The post-step epilogue in one kernel: the dye c advanced one step with
+    the new velocity (scalar_advection_diffusion_*, solver/operators.py:111-150,
+    solver/operators_mac.py:161-215; clipped to [0, 1]) and, with
+    diagnostics, the fields of step_for_visualization.  Returns c_new, or
+    (c_new, vorticity, divergence, speed)."""
+    mac = grid_type == "mac"
+    nx, ny = c.shape
+    _f32(u, "u", (nx + 1, ny) if mac else (nx, ny))
+    _f32(v, "v", (nx, ny + 1) if mac else (nx, ny))
+    _f32(c, "c", (nx, ny))
+    p = make_params(StepConfig(nx=nx, ny=ny, dx=float(dx), dy=float(dy), nu=1.0,
+                               grid_type=grid_type, flow_type=flow_type))
+    c_new = torch.empty_like(c)
+    d = [torch.empty((nx, ny), dtype=torch.float32, device=u.device) for _ in range(3)] \
+        if diagnostics else [None, None, None]
+    ptr = lambda t: None if t is None else t.data_ptr()
+    check("aj_post_step", lib().aj_post_step(ctypes.byref(p), u.data_ptr(), v.data_ptr(),
+                                             c.data_ptr(), c_new.data_ptr(), float(dt),
+                                             float(diffusivity), ptr(d[0]), ptr(d[1]), ptr(d[2]),
+                                             _stream(stream)))
+    return (c_new, *d) if diagnostics else c_new
+
+
 def make_geometry(kind, nx, ny, lx, ly, geo, eps, device="cuda", stream=None):
     """Obstacle SDF and mask = 1 - sigmoid(-sdf/eps) on the device
     (solver/simulation/mask_generator.py:10-160).  kind: 'cylinder' (cx, cy, r),

@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="naca", choices=["naca", "ensemble", "tri4096"],
+    ap.add_argument("--workload", default="naca", choices=["naca", "ensemble", "tri4096", "post"],
                     help="naca: the metric's workload (default); ensemble: 64 cylinder "
                          "channels of uneven sizes in one graph launch; tri4096: the "
                          "4096x2048 three-cylinder dynamic-LES flow")
@@ -486,6 +486,62 @@ def side_workload(args):
                        "mg_cycles_mean": statistics.mean(s["cycles"] for s in sts),
                        "rel_residual_max": max(s["rel_residual"] for s in sts),
                        "l2": "working set above the L2 size (no flush)"}}))
+        return
+    if args.workload == "post":
+        # the post-step epilogue (vorticity, divergence, speed and the dye step
+        # in one kernel): 2048x512 MAC and 4096x2048 collocated, inputs larger
+        # than L2 at the larger size; algorithmic bytes = read u, v, c + write
+        # c_new, vorticity, divergence, speed
+        out = {}
+        for name, nx, ny, grid in (("mac_2048x512", 2048, 512, "mac"),
+                                   ("collocated_4096x2048", 4096, 2048, "collocated")):
+            g = torch.Generator(device=dev).manual_seed(0)
+            mac = grid == "mac"
+            u = torch.rand(((nx + 1) if mac else nx, ny), device=dev, generator=g)
+            v = torch.rand((nx, (ny + 1) if mac else ny), device=dev, generator=g)
+            c = torch.rand((nx, ny), device=dev, generator=g)
+            outs = [torch.empty((nx, ny), device=dev) for _ in range(4)]
+            from aerojax_gb300 import _lib
+            from aerojax_gb300.solver import make_params, StepConfig
+            prm = make_params(StepConfig(nx=nx, ny=ny, dx=1 / 64, dy=1 / 64, nu=1.0,
+                                         grid_type=grid))
+            L = _lib.lib()
+
+            def call(s_):
+                rc = L.aj_post_step(ctypes.byref(prm), u.data_ptr(), v.data_ptr(), c.data_ptr(),
+                                    outs[0].data_ptr(), 1e-3, 1e-3, outs[1].data_ptr(),
+                                    outs[2].data_ptr(), outs[3].data_ptr(), s_)
+                assert rc == 0, rc
+            for _ in range(max(3, args.warmup)):
+                call(torch.cuda.current_stream().cuda_stream)
+            # the launches in a CUDA graph, so that host overhead cannot pad the time
+            graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(graph):
+                for _ in range(10):
+                    call(torch.cuda.current_stream().cuda_stream)
+            graph.replay()
+            torch.cuda.synchronize()
+            reps = max(1, args.steps // 10)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            for _ in range(reps):
+                graph.replay()
+            e1.record(st)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / (10 * reps)
+            nbytes = 4 * (u.numel() + v.numel() + c.numel() + 4 * nx * ny)
+            out[name] = {"ms_per_call": ms, "value": nx * ny / (ms * 1e-3) / 1e6,
+                         "achieved_gbs": nbytes / (ms * 1e-3) / 1e9,
+                         "algorithmic_bytes": nbytes}
+        big = out["collocated_4096x2048"]
+        print(json.dumps({
+            "metric": "Mcell/s of the post-step epilogue (diagnostics + dye step, one kernel)",
+            "value": big["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": big["ms_per_call"], "higher_is_better": True,
+            "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": "post_step_epilogue", "sizes": out,
+                       "l2": "4096x2048 inputs above the L2 size (no flush); launches "
+                             "replayed from a CUDA graph of 10"}}))
         return
     from aerojax_gb300 import configs
     from aerojax_gb300 import nn as NNW

@@ -245,6 +245,20 @@ int32_t aj_step_nn(const AjStepParams* prm, const float* u, const float* v, cons
 int32_t aj_diagnostics(const AjStepParams* prm, const float* u, const float* v, float* vort,
                        float* div, float* speed, void* stream);
 
+/* The post-step epilogue in one kernel that reads the new velocity once:
+   the diagnostics of aj_diagnostics and one explicit step of the passive
+   scalar (dye) c (nx*ny, cell-centred): c_out = clip(c_in + dt (-(u, v).grad
+   c_in + diffusivity lap c_in), 0, 1) with the reference's four variants
+   (scalar_advection_diffusion_periodic / _nonperiodic, operators.py:111-150;
+   the _staggered pair for MAC, operators_mac.py:161-215; non-periodic for the
+   von Karman flow).  Every output is optional (NULL: not computed); c_in and
+   c_out come together and must not alias.  Replaces the dye update and the
+   step_for_visualization fields of the GUI loop
+   (visualization_step.py:224-256). */
+int32_t aj_post_step(const AjStepParams* prm, const float* u, const float* v, const float* c_in,
+                     float* c_out, float dt, float diffusivity, float* vort, float* div,
+                     float* speed, void* stream);
+
 /* Allocation-free pressure solve, for callers that cannot allocate device
    memory: hosts that own every device byte through their own allocator (a
    framework's caching allocator, an XLA custom call without a scratch

@@ -166,6 +166,50 @@ def diagnostics(u, v, dx, dy, mac=False, periodic=False):
     return vort, div, np.sqrt(uc * uc + vc * vc)
 
 
+def scalar_advection_diffusion(c, u, v, dt, dx, dy, kappa, mac=False, periodic=False):
+    """One explicit step of the passive scalar (dye): c + dt (-(u, v).grad c +
+    kappa lap c), clipped to [0, 1].  The four variants of the reference:
+      collocated, periodic      solver/operators.py:111-129 (the Laplacian
+                                divides all five points by dx^2)
+      collocated, non-periodic  solver/operators.py:132-150 (one-sided d/dx at
+                                the inlet and outlet rows, periodic d/dy;
+                                Laplacian edge-padded in x, periodic in y)
+      MAC, periodic             solver/operators_mac.py:161-187 (face-averaged
+                                velocities, periodic central differences,
+                                edge-padded Laplacian)
+      MAC, non-periodic         solver/operators_mac.py:189-215 (central
+                                differences and Laplacian edge-padded)"""
+    c = np.asarray(c)
+    if mac:
+        uc, vc = interpolate_to_cell_center(u, v)
+        if periodic:
+            dcx = (np.roll(c, -1, 0) - np.roll(c, 1, 0)) / (2.0 * dx)
+            dcy = (np.roll(c, -1, 1) - np.roll(c, 1, 1)) / (2.0 * dy)
+        else:
+            px = np.pad(c, ((1, 1), (0, 0)), mode="edge")
+            py = np.pad(c, ((0, 0), (1, 1)), mode="edge")
+            dcx = (px[2:, :] - px[:-2, :]) / (2.0 * dx)
+            dcy = (py[:, 2:] - py[:, :-2]) / (2.0 * dy)
+        pe = np.pad(c, ((1, 1), (1, 1)), mode="edge")
+        lap = ((pe[2:, 1:-1] + pe[:-2, 1:-1] - 2 * c) / dx ** 2
+               + (pe[1:-1, 2:] + pe[1:-1, :-2] - 2 * c) / dy ** 2)
+        adv = uc * dcx + vc * dcy
+    elif periodic:
+        dcx = (np.roll(c, -1, 0) - np.roll(c, 1, 0)) / (2.0 * dx)
+        dcy = (np.roll(c, -1, 1) - np.roll(c, 1, 1)) / (2.0 * dy)
+        lap = (np.roll(c, 1, 0) + np.roll(c, -1, 0) + np.roll(c, 1, 1) + np.roll(c, -1, 1)
+               - 4 * c) / dx ** 2
+        adv = u * dcx + v * dcy
+    else:
+        dcx = grad_x_nonperiodic(c, dx)
+        dcy = (np.roll(c, -1, 1) - np.roll(c, 1, 1)) / (2.0 * dy)
+        px = np.pad(c, ((1, 1), (0, 0)), mode="edge")
+        lap = ((px[2:, :] - 2 * c + px[:-2, :]) / (dx * dx)
+               + (np.roll(c, 1, 1) + np.roll(c, -1, 1) - 2 * c) / (dy * dy))
+        adv = u * dcx + v * dcy
+    return np.clip(c + dt * (-adv + kappa * lap), 0.0, 1.0)
+
+
 def interpolate_to_x_face(c):
     """solver/operators_mac.py:130-137."""
     cp = np.pad(c, ((1, 1), (0, 0)), mode="edge")

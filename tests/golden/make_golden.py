@@ -236,6 +236,25 @@ def main(root):
         vort_mac_per=A(R.opsm.vorticity_staggered(um, vm, c["dx"], c["dy"])),
         div_mac_per=A(R.opsm.divergence_staggered(um, vm, c["dx"], c["dy"])))
 
+    # --- passive scalar (dye) advection-diffusion (operators.py:111-150,
+    # operators_mac.py:161-215) --------------------------------------------------
+    rng = np.random.default_rng(7)
+    nxs, nys = c["u"].shape
+    X, Y = np.meshgrid(np.linspace(0, 1, nxs), np.linspace(0, 1, nys), indexing="ij")
+    dye = np.clip(np.exp(-((X - 0.3) ** 2 + (Y - 0.5) ** 2) / 0.02)
+                  + 0.05 * rng.standard_normal(X.shape), 0.0, 1.0)
+    dts, kap = 0.004, 0.002
+    out["scalar"] = dict(
+        c=dye, u=c["u"], v=c["v"], um=um, vm=vm, dx=c["dx"], dy=c["dy"], dt=dts, kappa=kap,
+        col_per=A(R.ops.scalar_advection_diffusion_periodic(dye, c["u"], c["v"], dts, c["dx"],
+                                                            c["dy"], kap)),
+        col_np=A(R.ops.scalar_advection_diffusion_nonperiodic(dye, c["u"], c["v"], dts, c["dx"],
+                                                              c["dy"], kap)),
+        mac_per=A(R.opsm.scalar_advection_diffusion_periodic_staggered(dye, um, vm, dts, c["dx"],
+                                                                       c["dy"], kap)),
+        mac_np=A(R.opsm.scalar_advection_diffusion_nonperiodic_staggered(dye, um, vm, dts,
+                                                                         c["dx"], c["dy"], kap)))
+
     # --- time step and geometry ---------------------------------------------------
     dtc = R.cfl.compute_cfl_timestep(c["u"], c["v"], c["dx"], c["dy"], nu, cfl_target=0.5,
                                      dt_min=1e-5, dt_max=0.05)

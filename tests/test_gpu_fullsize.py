@@ -212,6 +212,34 @@ def test_diagnostics_match_reference(cuda_lib):
             assert np.max(np.abs(speed.cpu().numpy() - sp)) <= 1e-6 * np.max(sp)
 
 
+def test_post_step_dye_matches_reference(cuda_lib):
+    """aj_post_step: the dye step against the reference's own four
+    scalar_advection_diffusion variants (golden), and its diagnostics equal to
+    aj_diagnostics' (the same kernel reads the velocity once for both)."""
+    import torch
+    import aerojax_gb300 as aj
+    from conftest import golden
+    z = golden("scalar")
+    dt, dx, dy, kap = (float(z[k]) for k in ("dt", "dx", "dy", "kappa"))
+    c = torch.as_tensor(z["c"].astype(np.float32), device="cuda")
+    for mac, u, v in ((False, z["u"], z["v"]), (True, z["um"], z["vm"])):
+        ut = torch.as_tensor(u.astype(np.float32), device="cuda")
+        vt = torch.as_tensor(v.astype(np.float32), device="cuda")
+        for per in (False, True):
+            g, f = ("mac" if mac else "collocated"), ("taylor_green" if per else "von_karman")
+            cn, vort, div, speed = aj.post_step(ut, vt, c, dt, dx, dy, kap, grid_type=g,
+                                                flow_type=f)
+            tag = ("mac_" if mac else "col_") + ("per" if per else "np")
+            ref = z[tag]
+            assert np.max(np.abs(cn.cpu().numpy() - ref)) <= 1e-6, tag
+            assert float(cn.min()) >= 0.0 and float(cn.max()) <= 1.0
+            d = aj.diagnostics(ut, vt, dx, dy, grid_type=g, flow_type=f)
+            for a, b in zip((vort, div, speed), d):
+                assert torch.equal(a, b), tag
+            assert torch.equal(aj.post_step(ut, vt, c, dt, dx, dy, kap, grid_type=g, flow_type=f,
+                                            diagnostics=False), cn)
+
+
 def test_training_data_file(cuda_lib, tmp_path):
     """generate_training_data writes the reference's .npz layout
     (training_utils.py:12-81) and the recorded fields are the solver's."""

@@ -101,6 +101,19 @@ def test_geometry():
     assert np.max(np.abs(s3 - g["sdf_three"])) < 1e-13
 
 
+def test_scalar_advection_matches_reference():
+    """The dye step (operators.py:111-150, operators_mac.py:161-215), all four
+    grid/flow variants, bit for bit in float64."""
+    z = golden("scalar")
+    a = (float(z["dt"]), float(z["dx"]), float(z["dy"]), float(z["kappa"]))
+    for mac, u, v in ((False, z["u"], z["v"]), (True, z["um"], z["vm"])):
+        for per in (False, True):
+            c = R.scalar_advection_diffusion(z["c"], u, v, a[0], a[1], a[2], a[3], mac=mac,
+                                             periodic=per)
+            tag = ("mac_" if mac else "col_") + ("per" if per else "np")
+            assert np.array_equal(c, z[tag]), tag
+
+
 def test_diagnostics_match_reference():
     """Vorticity and divergence of step_for_visualization
     (visualization_step.py:224-256), all four grid/flow variants."""
