@@ -286,9 +286,10 @@ struct NnRef {
 
 // Side branches of a step (two streams, four events) per lane: lane i of an
 // ensemble capture uses its own, so that no two instances' branches chain.
-// enqueue_step holds g_forks_mu while it records, so that two host threads
-// (each capturing into its own graph, or launching eagerly) never interleave
-// records of the same events.
+// enqueue_step (and aj_poisson_mg) hold g_forks_mu while they record, so that
+// two host threads (each capturing into its own graph, or launching eagerly)
+// never interleave records of the same events or of the converging solve's
+// loop-body stream.
 std::mutex g_forks_mu;
 struct StepForks {
   cudaStream_t les, init;
@@ -478,6 +479,9 @@ int32_t aj_poisson_mg(const AjStepParams* prm, const float* rhs, const float* ma
     p.warm_start = p0 ? AJ_WARM_GUESS : AJ_WARM_ZERO;
   std::string key = make_key(2, p, {ws, rhs, mask, p0, p_out, stats});
   return run_captured(key, (cudaStream_t)stream, [&](cudaStream_t s) {
+    // the converging solve records its loop body through a shared side
+    // stream: the same lock as a step's enqueue
+    std::lock_guard<std::mutex> forks_lock(g_forks_mu);
     int r = launch_mg_rhs(p, L, ws, rhs, mask, s);
     if (r != AJ_OK) return r;
     return launch_pressure(p, L, ws, mask, p0, p_out, stats, s);
