@@ -12,7 +12,7 @@ from .solver import (Plan, StepHandler, compute_cfl_timestep, constant_smagorins
                      diagnostics, dynamic_smagorinsky, get_plan, make_geometry, poisson_multigrid,
                      post_step,
                      poisson_multigrid_converge, poisson_multigrid_mac, rk_step_unified,
-                     rk_step_unified_mac, run_step, step_pure)
+                     rk_step_unified_mac, run_step, run_step_host, step_pure)
 
 __all__ = [
     "GridParams", "SimState", "StepConfig", "compute_eps_multiplier", "get_re_parameters",
@@ -20,5 +20,6 @@ __all__ = [
     "post_step",
     "dynamic_smagorinsky",
     "get_plan", "make_geometry", "poisson_multigrid", "poisson_multigrid_converge",
-    "poisson_multigrid_mac", "rk_step_unified", "rk_step_unified_mac", "run_step", "step_pure",
+    "poisson_multigrid_mac", "rk_step_unified", "rk_step_unified_mac", "run_step",
+    "run_step_host", "step_pure",
 ]

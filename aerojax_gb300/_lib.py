@@ -95,6 +95,9 @@ _SIGS = {
     "aj_release_graphs": (c_int32, []),
     "aj_diagnostics": (c_int32, [POINTER(AjStepParams), c_void_p, c_void_p, c_void_p, c_void_p,
                                  c_void_p, c_void_p]),
+    "aj_step_host": (c_int32, [POINTER(AjStepParams), c_void_p, c_void_p, c_void_p, c_void_p,
+                               c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                               c_void_p, c_void_p, c_size_t, c_void_p, c_void_p]),
     "aj_post_step": (c_int32, [POINTER(AjStepParams), c_void_p, c_void_p, c_void_p, c_void_p,
                                ctypes.c_float, ctypes.c_float, c_void_p, c_void_p, c_void_p,
                                c_void_p]),

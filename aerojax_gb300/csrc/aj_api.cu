@@ -292,8 +292,8 @@ struct NnRef {
 // loop-body stream.
 std::mutex g_forks_mu;
 struct StepForks {
-  cudaStream_t les, init;
-  cudaEvent_t start, les_done, dt_done, init_done;
+  cudaStream_t les, init, io;
+  cudaEvent_t start, les_done, dt_done, init_done, io_p_in, io_p_ready, io_p_done;
 };
 static const StepForks* step_forks(int lane) {
   static std::vector<StepForks> v;
@@ -302,15 +302,26 @@ static const StepForks* step_forks(int lane) {
   while ((int)v.size() <= lane) {
     StepForks f;
     if (cudaStreamCreateWithFlags(&f.les, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&f.init, cudaStreamNonBlocking) != cudaSuccess)
+        cudaStreamCreateWithFlags(&f.init, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&f.io, cudaStreamNonBlocking) != cudaSuccess)
       return nullptr;
-    cudaEvent_t* e[4] = {&f.start, &f.les_done, &f.dt_done, &f.init_done};
+    cudaEvent_t* e[7] = {&f.start,   &f.les_done,   &f.dt_done,  &f.init_done,
+                         &f.io_p_in, &f.io_p_ready, &f.io_p_done};
     for (cudaEvent_t* q : e)
       if (cudaEventCreateWithFlags(q, cudaEventDisableTiming) != cudaSuccess) return nullptr;
     v.push_back(f);
   }
   return &v[lane];
 }
+
+// Host buffers of a step (aj_step_host): the pressure guess is uploaded on a
+// side branch that only the pressure solve waits for, and the new pressure
+// is downloaded on that branch while the correction runs.
+struct HostIO {
+  const float* h_p = nullptr;   // host pressure guess (nullable)
+  float* h_po = nullptr;        // host pressure result
+  size_t p_bytes = 0;
+};
 
 // One step.  Two pieces of work run beside the main chain: the LES viscosity
 // (it reads only the input velocities) beside the CFL reduction, and the
@@ -319,10 +330,18 @@ static const StepForks* step_forks(int lane) {
 static int enqueue_step(const AjStepParams& p, const Layout& L, void* ws, const float* u,
                         const float* v, const float* mask, const float* p_guess, float* uo,
                         float* vo, float* po, AjStats* stats, cudaStream_t st,
-                        NnRef nn = NnRef(), int lane = 0) {
+                        NnRef nn = NnRef(), int lane = 0, const HostIO* io = nullptr) {
   std::lock_guard<std::mutex> forks_lock(g_forks_mu);
   const StepForks* fk = step_forks(lane);
   if (!fk) return AJ_ERR_CUDA;
+  if (io && io->h_p) {   // the guess's upload, beside everything up to the solve
+    if (cudaEventRecord(fk->start, st) != cudaSuccess ||
+        cudaStreamWaitEvent(fk->io, fk->start, 0) != cudaSuccess ||
+        cudaMemcpyAsync(const_cast<float*>(p_guess), io->h_p, io->p_bytes,
+                        cudaMemcpyHostToDevice, fk->io) != cudaSuccess ||
+        cudaEventRecord(fk->io_p_in, fk->io) != cudaSuccess)
+      return AJ_ERR_CUDA;
+  }
   const bool mac = p.grid_type == AJ_GRID_MAC;
   // step_pure computes the LES field on the collocated path but never passes it
   // on (step.py:177-180): nothing to do.  The GUI step and MAC use it.
@@ -348,6 +367,9 @@ static int enqueue_step(const AjStepParams& p, const Layout& L, void* ws, const 
     if (cudaEventRecord(fk->dt_done, st) != cudaSuccess ||
         cudaStreamWaitEvent(fk->init, fk->dt_done, 0) != cudaSuccess)
       return AJ_ERR_CUDA;
+    // the initial state may read the guess: after its upload
+    if (io && io->h_p && cudaStreamWaitEvent(fk->init, fk->io_p_in, 0) != cudaSuccess)
+      return AJ_ERR_CUDA;
     rc = converge_init(p, L, ws, p_guess, fk->init);
     if (rc != AJ_OK) return rc;
     if (cudaEventRecord(fk->init_done, fk->init) != cudaSuccess) return AJ_ERR_CUDA;
@@ -360,13 +382,26 @@ static int enqueue_step(const AjStepParams& p, const Layout& L, void* ws, const 
   rc = launch_rhs(p, L, ws, us, vs, mask, at<float>(ws, L.b0), st);
   if (rc != AJ_OK) return rc;
   if (conv && cudaStreamWaitEvent(st, fk->init_done, 0) != cudaSuccess) return AJ_ERR_CUDA;
+  if (io && io->h_p && cudaStreamWaitEvent(st, fk->io_p_in, 0) != cudaSuccess)
+    return AJ_ERR_CUDA;
   NnWarm nw;
   nw.packed = nn.packed;
   nw.master = nn.master;
   nw.mask = mask;
   rc = launch_pressure(p, L, ws, mask, p_guess, po, stats, st, nn.packed ? &nw : nullptr, conv);
   if (rc != AJ_OK) return rc;
-  return launch_correct(p, L, ws, us, vs, po, mask, uo, vo, st);
+  if (io) {   // the pressure's download, beside the correction
+    if (cudaEventRecord(fk->io_p_ready, st) != cudaSuccess ||
+        cudaStreamWaitEvent(fk->io, fk->io_p_ready, 0) != cudaSuccess ||
+        cudaMemcpyAsync(io->h_po, po, io->p_bytes, cudaMemcpyDeviceToHost, fk->io) !=
+            cudaSuccess ||
+        cudaEventRecord(fk->io_p_done, fk->io) != cudaSuccess)
+      return AJ_ERR_CUDA;
+  }
+  rc = launch_correct(p, L, ws, us, vs, po, mask, uo, vo, st);
+  if (rc != AJ_OK) return rc;
+  if (io && cudaStreamWaitEvent(st, fk->io_p_done, 0) != cudaSuccess) return AJ_ERR_CUDA;
+  return AJ_OK;
 }
 
 }  // namespace aj
@@ -454,6 +489,58 @@ int32_t aj_step_nn(const AjStepParams* prm, const float* u, const float* v, cons
   nn.master = nn_master;
   return run_captured(key, (cudaStream_t)stream, [&](cudaStream_t s) {
     return enqueue_step(p, L, ws, u, v, mask, p_prev, u_out, v_out, p_out, stats, s, nn);
+  });
+}
+
+int32_t aj_step_host(const AjStepParams* prm, const float* h_u, const float* h_v,
+                     const float* mask, const float* h_p, float* h_u_out, float* h_v_out,
+                     float* h_p_out, float* d_in, float* d_out, const uint16_t* nn_packed,
+                     const float* nn_master, void* ws, size_t bytes, AjStats* stats,
+                     void* stream) {
+  if (!prm || !h_u || !h_v || !mask || !h_u_out || !h_v_out || !h_p_out || !d_in || !d_out)
+    return AJ_ERR_PARAM;
+  if ((nn_packed == nullptr) != (nn_master == nullptr)) return AJ_ERR_PARAM;
+  int rc = aj_check_params(prm);
+  if (rc != AJ_OK) return rc;
+  AjStepParams p = normalise(*prm);
+  if (nn_packed) {
+    if (p.mg_mode != AJ_MG_CONVERGE || p.nn_factor <= 0 || !h_p) return AJ_ERR_PARAM;
+    if (!nn_step_shape_ok(p)) return AJ_ERR_SHAPE;
+    if (p.warm_start != AJ_WARM_EXTRAPOLATE) p.warm_start = AJ_WARM_GUESS;
+  }
+  if (p.warm_start == AJ_WARM_GUESS && !h_p) return AJ_ERR_PARAM;
+  Layout L;
+  make_layout(p, L);
+  if ((rc = ws_ok(L, ws, bytes)) != AJ_OK) return rc;
+  const bool mac = p.grid_type == AJ_GRID_MAC;
+  const size_t nu = mac ? (size_t)(p.nx + 1) * p.ny : (size_t)p.nx * p.ny;
+  const size_t nv = mac ? (size_t)p.nx * (p.ny + 1) : (size_t)p.nx * p.ny;
+  const size_t np = (size_t)p.nx * p.ny;
+  float *du = d_in, *dv = d_in + nu, *dp = d_in + nu + nv;
+  float *duo = d_out, *dvo = d_out + nu, *dpo = d_out + nu + nv;
+  const float* hp = p.warm_start ? h_p : nullptr;
+  HostIO io;
+  io.h_p = hp;
+  io.h_po = h_p_out;
+  io.p_bytes = np * 4;
+  NnRef nn;
+  nn.packed = nn_packed;
+  nn.master = nn_master;
+  std::string key = make_key(5, p, {ws, h_u, h_v, mask, hp, h_u_out, h_v_out, h_p_out, d_in,
+                                    d_out, nn_packed, nn_master, stats});
+  return run_captured(key, (cudaStream_t)stream, [&](cudaStream_t s) {
+    if (cudaMemcpyAsync(du, h_u, nu * 4, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemcpyAsync(dv, h_v, nv * 4, cudaMemcpyHostToDevice, s) != cudaSuccess)
+      return (int)AJ_ERR_CUDA;
+    // the pressure guess goes up, and the new pressure comes down, on the
+    // step's io stream (enqueue_step), beside the predictor and the correction
+    int r = enqueue_step(p, L, ws, du, dv, mask, hp ? dp : nullptr, duo, dvo, dpo, stats, s, nn,
+                         0, &io);
+    if (r != AJ_OK) return r;
+    if (cudaMemcpyAsync(h_u_out, duo, nu * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaMemcpyAsync(h_v_out, dvo, nv * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+      return (int)AJ_ERR_CUDA;
+    return (int)AJ_OK;
   });
 }
 

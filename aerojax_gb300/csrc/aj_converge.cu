@@ -468,7 +468,16 @@ __global__ void __launch_bounds__(TC::NTH, 4) k_cv_up0(
   constexpr int TI = TC::TI, TJ = TC::TJ, SJ = TC::SJ;
   constexpr int PI = TI + 2, PJ = TJ + 2;
   static_assert(PJ <= 2 * TC::PAIRS, "the pressure window must fit two column runs");
-  if (!profile && sc->mg_done) return;
+  if (!profile && sc->mg_done) {
+    // met before this body ran (the initial guess already satisfied the
+    // tolerance, or the rhs is zero): every kernel of the body skipped its
+    // work and no block reaches the convergence test, so end the loop here
+    // (a body after a converged one never runs: the test set the condition)
+    if (ck.use_handle && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 &&
+        threadIdx.y == 0)
+      cudaGraphSetConditional(ck.h, 0u);
+    return;
+  }
   __shared__ float E[TC::NT];
   __shared__ float R[TC::NT];
   __shared__ float PH[PI * PJ];

@@ -156,6 +156,40 @@ def run_step(plan: Plan, u, v, mask, p_guess=None, out=None, stream=None, dt=Non
     return uo, vo, po
 
 
+def run_step_host(plan: Plan, h_u, h_v, mask, h_p=None, h_out=None, net=None, stream=None):
+    """One step with the fields in pinned HOST memory (aj_step_host): the
+    uploads, the step (the learned warm start with ``net``) and the downloads
+    in one graph launch, the pressure's transfers overlapped with the
+    predictor and the correction.  Returns (u_new, v_new, p) as host tensors
+    (``h_out`` if given)."""
+    cfg = plan.cfg
+    mac = cfg.grid_type == "mac"
+    nu = (cfg.nx + 1) * cfg.ny if mac else cfg.nx * cfg.ny
+    nv = cfg.nx * (cfg.ny + 1) if mac else cfg.nx * cfg.ny
+    n = nu + nv + cfg.nx * cfg.ny
+    dev = plan.ws.device
+    stage = getattr(plan, "_host_stage", None)
+    if stage is None or stage[0].numel() != n:
+        stage = (torch.empty(n, dtype=torch.float32, device=dev),
+                 torch.empty(n, dtype=torch.float32, device=dev))
+        plan._host_stage = stage
+    for t, name in ((h_u, "h_u"), (h_v, "h_v")):
+        if t.is_cuda or not t.is_pinned():
+            raise ValueError(f"{name} must be a pinned host tensor")
+    if h_out is None:
+        h_out = (torch.empty_like(h_u).pin_memory(), torch.empty_like(h_v).pin_memory(),
+                 torch.empty((cfg.nx, cfg.ny), dtype=torch.float32).pin_memory())
+    packed = master = None
+    if net is not None:   # an aerojax_gb300.nn.WarmStartNet (its packed BF16 weights current)
+        packed, master = net.packed.data_ptr(), net.master.data_ptr()
+    check("aj_step_host", lib().aj_step_host(
+        ctypes.byref(plan.params), h_u.data_ptr(), h_v.data_ptr(), mask.data_ptr(), _ptr(h_p),
+        h_out[0].data_ptr(), h_out[1].data_ptr(), h_out[2].data_ptr(), stage[0].data_ptr(),
+        stage[1].data_ptr(), packed, master, plan.ws.data_ptr(), plan.nbytes,
+        plan.stats_buf.data_ptr(), _stream(stream)))
+    return h_out
+
+
 # ----------------------------------------------------------------- step_pure
 def step_pure(state: SimState, mask, sdf, dx, dy, nu, U_inf, use_les=False,
               smagorinsky_constant=0.1, weno_epsilon=1e-6, eps=0.01, adaptive_dt=False,

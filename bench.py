@@ -319,14 +319,13 @@ def gpu_arm(args):
                      "frac_of_measured_hbm": bpc * cells / (ms_step * 1e-3) / 1e9 / hbm}
     launches = sum(int(L.aj_kernel_count(ctypes.byref(plan.params), c)) for c in cyc_m)
 
-    # ---- e2e: host buffers, H2D of the step's inputs, D2H of its result
+    # ---- e2e: host buffers through aj_step_host (one graph launch: the H2D of
+    # the step's inputs, the step, the D2H of its result)
     nxu, nyv = (args.nx + 1) * args.ny, args.nx * (args.ny + 1)
     pin = lambda t: t.detach().cpu().pin_memory()
     h_in = [pin(meth["bufs"][0][0]), pin(meth["bufs"][0][1]), pin(meth["bufs"][0][2])]
-    h_out = [torch.empty_like(h_in[0]).pin_memory(), torch.empty_like(h_in[1]).pin_memory(),
-             torch.empty_like(h_in[2]).pin_memory()]
-    d_in = [t.clone() for t in meth["bufs"][0]]
-    d_out = [t.clone() for t in meth["bufs"][1]]
+    h_out = (torch.empty_like(h_in[0]).pin_memory(), torch.empty_like(h_in[1]).pin_memory(),
+             torch.empty_like(h_in[2]).pin_memory())
     st = torch.cuda.current_stream()
 
     def e2e_steps(k):
@@ -335,11 +334,8 @@ def gpu_arm(args):
             flush.zero_()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(st)
-            for d, h in zip(d_in, h_in):
-                d.copy_(h, non_blocking=True)
-            step(plan, head, d_in, tuple(d_out))
-            for h, d in zip(h_out, d_out):
-                h.copy_(d, non_blocking=True)
+            aj.run_step_host(plan, h_in[0], h_in[1], mask, h_in[2], h_out=h_out,
+                             net=net if head == "nn" else None)
             e1.record(st)
             ev.append((e0, e1))
             torch.cuda.synchronize()                 # the host owns the result now
@@ -386,6 +382,8 @@ def gpu_arm(args):
             "step_roofline": step_roofline,
             "plain_mg_value": plain_value, "speedup_vs_plain": value / plain_value,
             "l2": "flushed before every step (256 MiB write outside the timed events)",
+            "e2e_api": "aj_step_host: pinned host u, v, p in; u, v, p out; copies inside the "
+                       "step's graph",
             "parallelism": "replicas only" if world > 1 else "single GPU",
         },
         "roofline": roof,

@@ -235,6 +235,22 @@ int32_t aj_step_nn(const AjStepParams* prm, const float* u, const float* v, cons
                    float* u_out, float* v_out, float* p_out, void* workspace,
                    size_t workspace_bytes, AjStats* stats, void* stream);
 
+/* One step with the fields in (pinned) HOST memory - the call a host-driven
+   loop makes (the reference's BaselineSolver._step hands back NumPy-visible
+   arrays every step, step_handlers.py:296-301).  One graph launch: the
+   upload of u, v, the step (aj_step, or aj_step_nn when nn_packed/nn_master
+   are given), the download of u, v and p.  The pressure guess h_p is uploaded
+   on a side branch that only the pressure solve waits for, and the new
+   pressure is downloaded while the velocity correction runs.  d_in and
+   d_out are device buffers of (nu + nv + nx*ny) floats each (nu, nv: the u
+   and v sizes of the grid) that the call uses for the device copies; h_p
+   may be NULL when the step ignores the guess. */
+int32_t aj_step_host(const AjStepParams* prm, const float* h_u, const float* h_v,
+                     const float* mask, const float* h_p, float* h_u_out, float* h_v_out,
+                     float* h_p_out, float* d_in, float* d_out, const uint16_t* nn_packed,
+                     const float* nn_master, void* ws, size_t bytes, AjStats* stats,
+                     void* stream);
+
 /* Post-step fields of step_for_visualization (visualization_step.py:224-256)
    into caller buffers (each nx*ny, nullable): vorticity
    (operators.py:105-108 / operators_mac.py:101-115; the periodic forms

@@ -139,6 +139,31 @@ def test_converging_warm_start_fewer_cycles(cuda_lib):
     assert st2["cycles"] < st["cycles"]
 
 
+def test_converging_solve_met_by_initial_state(cuda_lib):
+    """The initial state already meets the tolerance: a zero rhs (zero and
+    guessed initial state), and a guess that is the rhs's own converged
+    solution under a looser tolerance.  The graph's refinement loop must end
+    after its first (skipped) body with zero cycles counted."""
+    import torch
+    import aerojax_gb300 as aj
+    nx, ny, dx = 512, 128, 1 / 64
+    m = torch.ones((nx, ny), device="cuda")
+    z = torch.zeros((nx, ny), device="cuda")
+    for p0 in (None, z):
+        p, st = aj.poisson_multigrid_converge(z, m, dx, dx, rtol=1e-6, p0=p0)
+        torch.cuda.synchronize()
+        assert st["err"] == 0 and st["converged"] and st["cycles"] == 0, st
+        assert int(torch.count_nonzero(p)) == 0
+    rng = np.random.default_rng(8)
+    b = torch.as_tensor(rng.standard_normal((nx, ny)).astype(np.float32), device="cuda")
+    p, st = aj.poisson_multigrid_converge(b, m, dx, dx, rtol=1e-6)
+    assert st["err"] == 0 and st["cycles"] > 0
+    p2, st2 = aj.poisson_multigrid_converge(b, m, dx, dx, rtol=1e-3, p0=p)
+    assert st2["err"] == 0 and st2["converged"] and st2["cycles"] == 0, st2
+    assert st2["rel_residual"] <= 1e-3
+    assert torch.equal(p2, p)
+
+
 def test_naca_converge_step(cuda_lib):
     import aerojax_gb300 as aj
     from aerojax_gb300 import configs
@@ -334,3 +359,42 @@ def test_dependent_launches_change_nothing(cuda_lib, tmp_path):
         res[mode] = np.load(f)
     for k in res["1"].files:
         assert np.array_equal(res["1"][k], res["0"][k]), k
+
+
+@pytest.mark.parametrize("learned", [False, True])
+def test_host_buffer_step_matches_device_step(cuda_lib, learned):
+    """aj_step_host (fields in pinned host memory, the copies inside the step's
+    graph, the pressure's transfers on a side branch) gives bit for bit the
+    fields of the device-buffer step, with and without the learned warm
+    start, over five steps of the 512x128 NACA workload."""
+    from dataclasses import replace
+    import torch
+    import aerojax_gb300 as aj
+    from aerojax_gb300 import configs, nn
+    c = configs.naca_mac_2048x512(nx=512, ny=128, mg_mode="converge")
+    cfg = replace(c["cfg"], warm_start="extrapolate", nn_factor=8 if learned else 0)
+    net = nn.WarmStartNet.load(nn.WEIGHTS, device="cuda") if learned else None
+    res = []
+    for host in (False, True):
+        # a fresh plan for each arm: both start from an empty pressure history
+        plan = aj.Plan(cfg, torch.device("cuda"))
+        plan.prepare(c["mask"])
+        u, v = c["u"].clone(), c["v"].clone()
+        p = torch.zeros((512, 128), device="cuda")
+        if host:
+            hu, hv, hp = (t.cpu().pin_memory() for t in (u, v, p))
+            for _ in range(5):
+                ou, ov, op = aj.run_step_host(plan, hu, hv, c["mask"], hp, net=net)
+                torch.cuda.synchronize()
+                hu, hv, hp = ou.clone().pin_memory(), ov.clone().pin_memory(), op.clone().pin_memory()
+            res.append((hu, hv, hp))
+        else:
+            for _ in range(5):
+                if learned:
+                    u, v, p = nn.run_step_nn(plan, net, u, v, c["mask"], p)
+                else:
+                    u, v, p = aj.run_step(plan, u, v, c["mask"], p_guess=p)
+            res.append((u.cpu(), v.cpu(), p.cpu()))
+        assert plan.stats()["err"] == 0
+    for a, b in zip(*res):
+        assert torch.equal(a, b)
