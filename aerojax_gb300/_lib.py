@@ -101,6 +101,11 @@ _SIGS = {
     "aj_post_step": (c_int32, [POINTER(AjStepParams), c_void_p, c_void_p, c_void_p, c_void_p,
                                ctypes.c_float, ctypes.c_float, c_void_p, c_void_p, c_void_p,
                                c_void_p]),
+    "aj_step_vjp_workspace_size": (c_size_t, [POINTER(AjStepParams)]),
+    "aj_step_vjp": (c_int32, [POINTER(AjStepParams), c_void_p, c_void_p, c_void_p, c_void_p,
+                              c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                              c_void_p, c_size_t, c_void_p, c_size_t, c_void_p]),
+    "aj_step_vjp_kernel_count": (c_int32, [POINTER(AjStepParams)]),
     "aj_autotune": (c_int32, [POINTER(AjStepParams), c_void_p, c_size_t, c_int32,
                               POINTER(ctypes.c_float), POINTER(c_int32), c_void_p]),
     "aj_ensemble_step": (c_int32, [c_int32, POINTER(AjStepParams), POINTER(c_void_p),

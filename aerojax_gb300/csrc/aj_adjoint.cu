@@ -1,0 +1,609 @@
+// Reverse mode (vector-Jacobian product) of the collocated step_pure: what
+// jax.grad computes through the reference's rollouts (solver/solver.py:34-114;
+// inverse_design_WIP/optimizer_autodiff.py:113-205 differentiates the same
+// scan).  From cotangents of the step's outputs (u, v, p) it produces the
+// cotangents of its inputs (u, v) and of the parameters a design loss
+// differentiates: the SDF (through the Brinkman chi), nu and U_inf.
+//
+// The reverse pass follows the forward in reverse order:
+//   correction + interface projection + boundary rows + hard masks
+//     (solver/pure_functions/step.py:259-397)       -> k_adj_correct, k_adj_grad
+//   parity multigrid (pressure_solvers/multigrid_solver.py:173-241)
+//                                                    -> k_adj_jac/prolong/restrict
+//   rhs = div*mask/dt (step.py:182-199)              -> k_adj_div
+//   RK3/RK2 upwind predictor with implicit Brinkman (rk3_simple_new.py:284-358)
+//                                                    -> k_adj_rk_out, k_adj_rk_stage
+// JAX's rules: where(c, x, y) sends the cotangent to the selected branch (the
+// condition has none), .at[].set drops the overwritten entries' cotangent,
+// lax.cond in the V-cycle scan differentiates only the cycles that ran.
+//
+// Structure: the Jacobi sweep (p <- (N p - b)/d) and the edge-ghost Laplacian
+// are symmetric, so each reversed sweep is h = pbar/d, bbar -= h, pbar = N h;
+// restriction and prolongation swap into each other's transposes.  The
+// boundary rows are gathers (each output cell copies one source cell), so
+// their transposes are gathers at the source.  The two boundary passes of the
+// predictor (rk3_simple_new.py:262-275, then step.py:182-191) compose to the
+// first, so one transpose covers both.  Forward stage states are recomputed
+// by the forward predictor kernels (stage buffers of the step workspace).
+#include "aj_internal.cuh"
+
+namespace aj {
+
+// ------------------------------------------------------------------ layout
+struct AdjLayout {
+  size_t gus = 0, gvs = 0;           // cotangent of the predictor output
+  size_t gdpx = 0, gdpy = 0;         // cotangent of the projected pressure gradient
+  size_t wnu = 0, wnv = 0;           // forward predictor output (recomputed)
+  size_t kAu = 0, kAv = 0, kBu = 0, kBv = 0, kEu = 0, kEv = 0;   // stage-slope cotangents
+  size_t w1u = 0, w1v = 0, dbar = 0; // cotangent of u, v through the stages; of den
+  size_t pscr = 0;                   // forward pressure (only to count V-cycles)
+  size_t GX[AJ_MAX_LEVELS + 1] = {0}, GT[AJ_MAX_LEVELS + 1] = {0}, GB[AJ_MAX_LEVELS + 1] = {0};
+  size_t part = 0;                   // per-block FP64 partial sums of d/d nu
+  int nblk = 0;                      // blocks of one cell kernel
+  size_t total = 0;
+};
+
+constexpr int kAdjBX = 32, kAdjBY = 8;
+
+static bool make_adj_layout(const AjStepParams& p, const Layout& L, AdjLayout& A) {
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    size_t o = off;
+    off += (bytes + 255) & ~(size_t)255;
+    return o;
+  };
+  const size_t N = (size_t)p.nx * p.ny * 4;
+  A.gus = take(N);
+  A.gvs = take(N);
+  A.gdpx = take(N);
+  A.gdpy = take(N);
+  A.wnu = take(N);
+  A.wnv = take(N);
+  A.kAu = take(N);
+  A.kAv = take(N);
+  A.kBu = take(N);
+  A.kBv = take(N);
+  if (p.fast_mode) {
+    A.kEu = take(N);
+    A.kEv = take(N);
+  }
+  A.w1u = take(N);
+  A.w1v = take(N);
+  A.dbar = take(N);
+  if (p.v_cycles > 1) A.pscr = take(N);
+  for (int l = 0; l <= L.nlev; ++l) {
+    const size_t n = (size_t)L.ln[l] * L.lm[l] * 4;
+    A.GX[l] = take(n);
+    A.GT[l] = take(n);
+    A.GB[l] = take(n);
+  }
+  A.nblk = cdiv(p.ny, kAdjBX) * cdiv(p.nx, kAdjBY);
+  A.part = take((size_t)A.nblk * 3 * 8);
+  A.total = off;
+  return true;
+}
+
+// ------------------------------------------------------------------ helpers
+__device__ __forceinline__ bool live_at(const float* __restrict__ mask, long k) {
+  return ldg(mask + k) > 0.5f;
+}
+__device__ __forceinline__ bool interior(int i, int j, int nx, int ny) {
+  return i >= 1 && i <= nx - 2 && j >= 1 && j <= ny - 2;
+}
+
+// one-sided mask gradients of the interface projection (operators.py:17-56)
+__device__ __forceinline__ float gx_nonper(const float* __restrict__ f, int a, int b, int nx,
+                                           int ny, float idx, float h2x) {
+  if (a == 0) return (ldg(f + (long)ny + b) - ldg(f + b)) * idx;
+  if (a == nx - 1) return (ldg(f + (long)(nx - 1) * ny + b) - ldg(f + (long)(nx - 2) * ny + b)) * idx;
+  return (ldg(f + (long)(a + 1) * ny + b) - ldg(f + (long)(a - 1) * ny + b)) * h2x;
+}
+__device__ __forceinline__ float gy_nonper(const float* __restrict__ f, int a, int b, int ny,
+                                           float idy, float h2y) {
+  const float* r = f + (long)a * ny;
+  if (b == 0) return (ldg(r + 1) - ldg(r)) * idy;
+  if (b == ny - 1) return (ldg(r + ny - 1) - ldg(r + ny - 2)) * idy;
+  return (ldg(r + b + 1) - ldg(r + b - 1)) * h2y;
+}
+
+// transpose of the non-periodic gradient along one axis at index i of n
+// (stride between neighbours s): central rows 1..n-2, one-sided rows 0, n-1
+__device__ __forceinline__ float grad_T(const float* __restrict__ g, long s, int i, int n,
+                                        float ih, float h2) {
+  float r = 0.f;
+  if (i - 1 >= 1 && i - 1 <= n - 2) r += h2 * ldg(g + (long)(i - 1) * s);
+  if (i + 1 >= 1 && i + 1 <= n - 2) r -= h2 * ldg(g + (long)(i + 1) * s);
+  if (i == 1) r += ih * ldg(g);
+  if (i == 0) r -= ih * ldg(g);
+  if (i == n - 1) r += ih * ldg(g + (long)(n - 1) * s);
+  if (i == n - 2) r -= ih * ldg(g + (long)(n - 1) * s);
+  return r;
+}
+
+// Transpose of the von Karman slip-wall boundary gather at source (a, b):
+// output u(i, j) copies u(ci(i), cj(j)) (i > 0; ci(nx-1) = nx-2, cj(0) = 1,
+// cj(ny-1) = ny-2) and v(i, j) copies v(ci(i), j) (0 < j < ny-1); the inlet
+// row and the wall columns of v are constants.  Each output may be weighted
+// by its hard mask (the correction's last mask, step.py:396-397).
+template <bool MASKED>
+__device__ __forceinline__ void bc_gather_T(const float* __restrict__ gu_o,
+                                            const float* __restrict__ gv_o,
+                                            const float* __restrict__ mask, int a, int b, int nx,
+                                            int ny, float& gu, float& gv) {
+  gu = 0.f;
+  gv = 0.f;
+  if (!interior(a, b, nx, ny)) return;
+  const int nrow = a == nx - 2 ? 2 : 1;
+  for (int r = 0; r < nrow; ++r) {
+    const long base = (long)(r == 0 ? a : nx - 1) * ny;
+    auto take = [&](const float* g, long q) { return MASKED ? (live_at(mask, q) ? ldg(g + q) : 0.f) : ldg(g + q); };
+    gu += take(gu_o, base + b);
+    if (b == 1) gu += take(gu_o, base);
+    if (b == ny - 2) gu += take(gu_o, base + ny - 1);
+    gv += take(gv_o, base + b);
+  }
+}
+
+// ------------------------------------------------------------------ correction
+struct AdjCorr {
+  const float *gu_o, *gv_o, *gp_o, *mask;
+  float *gus, *gvs, *gdpx, *gdpy, *pbar;
+  const DevScalars* sc;
+  int nx, ny;
+  float idx, idy, h2x, h2y, thresh;
+};
+
+// cotangents of u*, v* and of the projected gradient at source (a, b)
+// (step.py:341-397 reversed)
+__global__ void __launch_bounds__(256) k_adj_correct(AdjCorr c) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  const int nx = c.nx, ny = c.ny;
+  if (i >= nx || j >= ny) return;
+  const long k = (long)i * ny + j;
+  float gu, gv;
+  bc_gather_T<true>(c.gu_o, c.gv_o, c.mask, i, j, nx, ny, gu, gv);
+  if (!live_at(c.mask, k)) gu = gv = 0.f;                      // step.py:348-349
+  c.gus[k] = gu;
+  c.gvs[k] = gv;
+  const float dt = c.sc->dt_corr;
+  float ax = -dt * gu, ay = -dt * gv;                           // (row 0: gu = 0, :341)
+  const float dmx = gx_nonper(c.mask, i, j, nx, ny, c.idx, c.h2x);
+  const float dmy = gy_nonper(c.mask, i, j, ny, c.idy, c.h2y);
+  const float gm = sqrtf(dmx * dmx + dmy * dmy);
+  if (gm > c.thresh) {                                          // step.py:313-335 (symmetric)
+    const float nxv = dmx / (gm + 1e-8f), nyv = dmy / (gm + 1e-8f);
+    const float dn = -(ax * nxv + ay * nyv);
+    ax = ax + dn * nxv;
+    ay = ay + dn * nyv;
+  }
+  c.gdpx[k] = ax;
+  c.gdpy[k] = ay;
+}
+
+// cotangent of p: the output's own cotangent plus the gradient's transpose
+__global__ void __launch_bounds__(256) k_adj_grad(AdjCorr c) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  const int nx = c.nx, ny = c.ny;
+  if (i >= nx || j >= ny) return;
+  const long k = (long)i * ny + j;
+  float r = c.gp_o ? ldg(c.gp_o + k) : 0.f;
+  r += grad_T(c.gdpx + j, ny, i, nx, c.idx, c.h2x);
+  r += grad_T(c.gdpy + (long)i * ny, 1, j, ny, c.idy, c.h2y);
+  c.pbar[k] = r;
+}
+
+// ------------------------------------------------------------------ multigrid
+// reversed Jacobi sweep: h = (gin with the outlet row zeroed when the forward
+// sweep reset it)/d; gb -= h (or = -h); gout = N h
+__global__ void __launch_bounds__(256) k_adj_jac(const float* __restrict__ gin,
+                                                 float* __restrict__ gout, float* __restrict__ gb,
+                                                 int n, int m, float ax, float ay, float d,
+                                                 int zero_last, int assign, const int* ncyc,
+                                                 int cyc) {
+  if (ncyc && cyc >= *ncyc) return;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= n || j >= m) return;
+  auto h = [&](int ii, int jj) -> float {
+    return (zero_last && ii == n - 1) ? 0.f : ldg(gin + (long)ii * m + jj) / d;
+  };
+  const long k = (long)i * m + j;
+  const float hc = h(i, j);
+  gb[k] = assign ? -hc : gb[k] - hc;
+  if (gout) {
+    const int ip = i + 1 < n ? i + 1 : n - 1, im = i > 0 ? i - 1 : 0;
+    const int jp = j + 1 < m ? j + 1 : m - 1, jm = j > 0 ? j - 1 : 0;
+    gout[k] = ax * (h(ip, j) + h(im, j)) + ay * (h(i, jp) + h(i, jm));
+  }
+}
+
+// transpose of the reference prolongation (multigrid_solver.py:134-156) onto
+// the coarse cell (I, J): even fine cells inject, odd interior ones average
+__global__ void __launch_bounds__(256) k_adj_prolong(const float* __restrict__ gf,
+                                                     float* __restrict__ gc, int nc, int mc,
+                                                     const int* ncyc, int cyc) {
+  if (ncyc && cyc >= *ncyc) return;
+  const int J = blockIdx.x * blockDim.x + threadIdx.x;
+  const int I = blockIdx.y * blockDim.y + threadIdx.y;
+  if (I >= nc || J >= mc) return;
+  const int mf = 2 * mc;
+  auto F = [&](int a, int b) { return ldg(gf + (long)a * mf + b); };
+  const bool iu = I <= nc - 2, id = I >= 1, ju = J <= mc - 2, jd = J >= 1;
+  float r = F(2 * I, 2 * J);
+  float s = 0.f;
+  if (iu) s += F(2 * I + 1, 2 * J);
+  if (id) s += F(2 * I - 1, 2 * J);
+  if (ju) s += F(2 * I, 2 * J + 1);
+  if (jd) s += F(2 * I, 2 * J - 1);
+  float q = 0.f;
+  if (iu && ju) q += F(2 * I + 1, 2 * J + 1);
+  if (id && ju) q += F(2 * I - 1, 2 * J + 1);
+  if (iu && jd) q += F(2 * I + 1, 2 * J - 1);
+  if (id && jd) q += F(2 * I - 1, 2 * J - 1);
+  gc[(long)I * mc + J] = r + 0.5f * s + 0.25f * q;
+}
+
+// transpose of rc = R(b - A p): s = R^T rc_bar (a quarter to each child);
+// gb += s, gx -= A s (A symmetric with edge ghosts)
+__global__ void __launch_bounds__(256) k_adj_restrict(const float* __restrict__ gbc,
+                                                      float* __restrict__ gb,
+                                                      float* __restrict__ gx, int n, int m,
+                                                      float ax, float ay, const int* ncyc,
+                                                      int cyc) {
+  if (ncyc && cyc >= *ncyc) return;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= n || j >= m) return;
+  const int mc = m / 2;
+  auto s = [&](int ii, int jj) { return 0.25f * ldg(gbc + (long)(ii >> 1) * mc + (jj >> 1)); };
+  const int ip = i + 1 < n ? i + 1 : n - 1, im = i > 0 ? i - 1 : 0;
+  const int jp = j + 1 < m ? j + 1 : m - 1, jm = j > 0 ? j - 1 : 0;
+  const float sc = s(i, j);
+  const long k = (long)i * m + j;
+  gb[k] += sc;
+  gx[k] -= ax * (s(ip, j) + s(im, j) - 2.f * sc) + ay * (s(i, jp) + s(i, jm) - 2.f * sc);
+}
+
+// ------------------------------------------------------------------ rhs
+// rhs = (div * mask)/dt with b[-1] = 0 (step.py:199, multigrid_solver.py:75-77);
+// div = central differences on the interior (operators.py:81-96): adds the
+// transpose to the predictor-output cotangent
+__global__ void __launch_bounds__(256) k_adj_div(const float* __restrict__ gb0,
+                                                 const float* __restrict__ mask,
+                                                 float* __restrict__ gus, float* __restrict__ gvs,
+                                                 const DevScalars* sc, int nx, int ny, float h2x,
+                                                 float h2y) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= nx || j >= ny) return;
+  const float dt = sc->dt;
+  auto dv = [&](int a, int b) -> float {
+    if (!interior(a, b, nx, ny)) return 0.f;                  // (a <= nx-2: never the zeroed row)
+    const long q = (long)a * ny + b;
+    return (ldg(gb0 + q) * ldg(mask + q)) / dt;
+  };
+  const long k = (long)i * ny + j;
+  gus[k] += h2x * (dv(i - 1, j) - dv(i + 1, j));
+  gvs[k] += h2y * (dv(i, j - 1) - dv(i, j + 1));
+}
+
+// ------------------------------------------------------------------ predictor
+struct AdjRk {
+  const float *gus, *gvs;          // k_adj_rk_out: cotangent of the predictor output
+  const float *kin_u, *kin_v;      // stages: cotangent of this stage's slope
+  const float *wu, *wv;            // stages: the stage state; k_adj_rk_out: predictor output
+  const float *chi;
+  float *w1u, *w1v, *dbar;
+  float *kout_u, *kout_v;          // cotangent of the previous stage's slope
+  float *kext_u, *kext_v;          // RK2: 0.5 dt x_n (part of k1's cotangent)
+  float *gu, *gv;                  // last stage: cotangents of the step's u, v
+  float *gsdf;                     // accumulated (nullable)
+  double* part;                    // per-block d/d nu
+  const float* mask;
+  const DevScalars* sc;
+  int nx, ny, last;
+  float idx, idy, idx2, idy2, nu, inv_eta, cn, sdf_fac;
+};
+
+// cotangent of the final combination x_n / den, through the predictor's hard
+// mask and boundary rows (rk3_simple_new.py:332-337, 262-275; step.py:182-191)
+__global__ void __launch_bounds__(256) k_adj_rk_out(AdjRk a) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  const int nx = a.nx, ny = a.ny;
+  if (i >= nx || j >= ny) return;
+  const long k = (long)i * ny + j;
+  float gu, gv;
+  bc_gather_T<false>(a.gus, a.gvs, nullptr, i, j, nx, ny, gu, gv);
+  if (!live_at(a.mask, k)) gu = gv = 0.f;
+  const float dt = a.sc->dt;
+  const float den = 1.f + dt * ldg(a.chi + k) * a.inv_eta;
+  const float xu = gu / den, xv = gv / den;
+  // where x != 0 the output cell is interior and live: it holds x_n/den itself
+  a.dbar[k] = -(xu * ldg(a.wu + k) + xv * ldg(a.wv + k));
+  a.w1u[k] = xu;                                                // 1/3 + 2/3 (RK2: 1)
+  a.w1v[k] = xv;
+  a.kout_u[k] = a.cn * dt * xu;
+  a.kout_v[k] = a.cn * dt * xv;
+  if (a.kext_u) {
+    a.kext_u[k] = 0.5f * dt * xu;
+    a.kext_v[k] = 0.5f * dt * xv;
+  }
+}
+
+// One reversed stage: the transpose of the explicit right-hand side
+// (rk3_simple_new.py:284-313; first-order upwind, edge ghosts) at the stage
+// state w, applied to the slope cotangent kbar, then the stage's
+// combination.  For target cell c the upwind difference of cell q reads
+// +f(q) - f(W(q)) when its velocity is positive, else -f(q) + f(E(q)): the
+// gather visits q = c and its four neighbours.
+__global__ void __launch_bounds__(256) k_adj_rk_stage(AdjRk a) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  const int nx = a.nx, ny = a.ny;
+  const bool valid = i < nx && j < ny;
+  double nub = 0.0;
+  if (valid) {
+    const long k = (long)i * ny + j;
+    const int im = i > 0 ? i - 1 : 0, ip = i < nx - 1 ? i + 1 : nx - 1;
+    const int jm = j > 0 ? j - 1 : 0, jp = j < ny - 1 ? j + 1 : ny - 1;
+    const long kxm = (long)im * ny + j, kxp = (long)ip * ny + j;
+    const long kym = (long)i * ny + jm, kyp = (long)i * ny + jp;
+    const float U = ldg(a.wu + k), V = ldg(a.wv + k);
+    const float uxm = ldg(a.wu + kxm), uxp = ldg(a.wu + kxp), uym = ldg(a.wu + kym), uyp = ldg(a.wu + kyp);
+    const float vxm = ldg(a.wv + kxm), vxp = ldg(a.wv + kxp), vym = ldg(a.wv + kym), vyp = ldg(a.wv + kyp);
+    const float ku = ldg(a.kin_u + k), kv = ldg(a.kin_v + k);
+    const float kuxm = ldg(a.kin_u + kxm), kuxp = ldg(a.kin_u + kxp);
+    const float kuym = ldg(a.kin_u + kym), kuyp = ldg(a.kin_u + kyp);
+    const float kvxm = ldg(a.kin_v + kxm), kvxp = ldg(a.kin_v + kxp);
+    const float kvym = ldg(a.kin_v + kym), kvyp = ldg(a.kin_v + kyp);
+    const float A = -ku, B = -kv;                  // cotangents of the advection terms
+    const bool px = U > 0.f, py = V > 0.f;
+    // velocity roles: d(adv)/d(velocity) = the upwind difference itself
+    const float fxu = px ? (U - uxm) * a.idx : (uxp - U) * a.idx;
+    const float fxv = px ? (V - vxm) * a.idx : (vxp - V) * a.idx;
+    const float fyu = py ? (U - uym) * a.idy : (uyp - U) * a.idy;
+    const float fyv = py ? (V - vym) * a.idy : (vyp - V) * a.idy;
+    float gu = A * fxu + B * fxv;
+    float gv = A * fyu + B * fyv;
+    // diffusion (the edge Laplacian is symmetric)
+    gu += a.nu * ((kuxp + kuxm - 2.f * ku) * a.idx2 + (kuyp + kuym - 2.f * ku) * a.idy2);
+    gv += a.nu * ((kvxp + kvxm - 2.f * kv) * a.idx2 + (kvyp + kvym - 2.f * kv) * a.idy2);
+    // field roles, centre cell (its own ghost at the edges)
+    {
+      const float al = A * U * a.idx, be = B * U * a.idx;
+      float cu = px ? al : -al, cv = px ? be : -be;
+      if (i == 0 && px) { cu -= al; cv -= be; }
+      if (i == nx - 1 && !px) { cu += al; cv += be; }
+      const float ay_ = A * V * a.idy, by_ = B * V * a.idy;
+      float du = py ? ay_ : -ay_, dv = py ? by_ : -by_;
+      if (j == 0 && py) { du -= ay_; dv -= by_; }
+      if (j == ny - 1 && !py) { du += ay_; dv += by_; }
+      gu += cu + du;
+      gv += cv + dv;
+    }
+    // field roles, neighbours: q = c + x reads f(c) as its W when U(q) > 0,
+    // q = c - x reads f(c) as its E when U(q) <= 0 (likewise in y with V)
+    if (i + 1 <= nx - 1 && uxp > 0.f) { gu += kuxp * uxp * a.idx; gv += kvxp * uxp * a.idx; }
+    if (i - 1 >= 0 && !(uxm > 0.f)) { gu -= kuxm * uxm * a.idx; gv -= kvxm * uxm * a.idx; }
+    if (j + 1 <= ny - 1 && vyp > 0.f) { gu += kuyp * vyp * a.idy; gv += kvyp * vyp * a.idy; }
+    if (j - 1 >= 0 && !(vym > 0.f)) { gu -= kuym * vym * a.idy; gv -= kvym * vym * a.idy; }
+    // d/d nu: kbar . lap(w)
+    const float lu = (uxp + uxm - 2.f * U) * a.idx2 + (uyp + uym - 2.f * U) * a.idy2;
+    const float lv = (vxp + vxm - 2.f * V) * a.idx2 + (vyp + vym - 2.f * V) * a.idy2;
+    nub = (double)ku * lu + (double)kv * lv;
+    const float dt = a.sc->dt;
+    if (!a.last) {
+      const float den = 1.f + dt * ldg(a.chi + k) * a.inv_eta;
+      const float xu = gu / den, xv = gv / den;
+      a.dbar[k] -= xu * U + xv * V;
+      a.w1u[k] += xu;
+      a.w1v[k] += xv;
+      float nku = a.cn * dt * xu, nkv = a.cn * dt * xv;
+      if (a.kext_u) {
+        nku += a.kext_u[k];
+        nkv += a.kext_v[k];
+      }
+      a.kout_u[k] = nku;
+      a.kout_v[k] = nkv;
+    } else {
+      a.gu[k] = a.w1u[k] + gu;
+      a.gv[k] = a.w1v[k] + gv;
+      if (a.gsdf) {
+        // den = 1 + dt chi/eta, chi = sigmoid(-sdf/(0.1 dx)) (rk3_simple_new.py:194-198)
+        const float c = ldg(a.chi + k);
+        a.gsdf[k] += a.dbar[k] * dt * a.inv_eta * c * (1.f - c) * a.sdf_fac;
+      }
+    }
+  }
+  const double t = block_sum(nub);
+  if (threadIdx.x == 0 && threadIdx.y == 0) a.part[blockIdx.y * gridDim.x + blockIdx.x] = t;
+}
+
+// d/d nu from the stage partials and d/d U_inf from the inlet rows (the
+// correction's final row 0 where live, and the predictor output's row 0),
+// summed in a fixed order and added to gscal[0], gscal[1]
+__global__ void k_adj_scalars(const double* __restrict__ part, int nparts,
+                              const float* __restrict__ gu_o, const float* __restrict__ gus,
+                              const float* __restrict__ mask, int ny, double* gscal) {
+  double s = 0.0, u = 0.0;
+  for (int q = threadIdx.x; q < nparts; q += blockDim.x) s += part[q];
+  for (int q = threadIdx.x; q < ny; q += blockDim.x) {
+    u += (double)ldg(gus + q);
+    if (live_at(mask, q)) u += (double)ldg(gu_o + q);
+  }
+  s = block_sum(s);
+  u = block_sum(u);
+  if (threadIdx.x == 0) {
+    gscal[0] += s;
+    gscal[1] += u;
+  }
+}
+
+// ------------------------------------------------------------------ driver
+size_t step_vjp_workspace(const AjStepParams& p, const Layout& L) {
+  AdjLayout A;
+  make_adj_layout(p, L, A);
+  return A.total;
+}
+
+int launch_step_vjp(const AjStepParams& p, const Layout& L, void* ws, void* aws, const float* u,
+                    const float* v, const float* mask, const float* gu_o, const float* gv_o,
+                    const float* gp_o, float* gu, float* gv, float* gsdf, double* gscal,
+                    cudaStream_t st) {
+  AdjLayout A;
+  make_adj_layout(p, L, A);
+  DevScalars* sc = at<DevScalars>(ws, 0);
+  const int nx = p.nx, ny = p.ny;
+  const long N = (long)nx * ny;
+  auto F = [&](size_t off) { return at<float>(aws, off); };
+  const dim3 blk(kAdjBX, kAdjBY), grd(cdiv(ny, kAdjBX), cdiv(nx, kAdjBY));
+  int rc;
+  // ---- forward: dt and the predictor's stage states
+  if ((rc = launch_set_dt(p, ws, st)) != AJ_OK) return rc;
+  if ((rc = launch_predictor(p, L, ws, u, v, mask, nullptr, 0, F(A.wnu), F(A.wnv), st)) != AJ_OK)
+    return rc;
+  const int* ncyc = nullptr;
+  if (p.v_cycles > 1) {
+    // the V-cycles the forward ran (the reference skips cycles once converged)
+    if ((rc = launch_rhs(p, L, ws, F(A.wnu), F(A.wnv), mask, at<float>(ws, L.b0), st)) != AJ_OK)
+      return rc;
+    if ((rc = launch_pressure(p, L, ws, mask, nullptr, F(A.pscr), nullptr, st)) != AJ_OK) return rc;
+    ncyc = &sc->mg_cycles;
+  }
+  // ---- correction, reversed
+  AdjCorr c{};
+  c.gu_o = gu_o;
+  c.gv_o = gv_o;
+  c.gp_o = gp_o;
+  c.mask = mask;
+  c.gus = F(A.gus);
+  c.gvs = F(A.gvs);
+  c.gdpx = F(A.gdpx);
+  c.gdpy = F(A.gdpy);
+  c.pbar = F(A.GX[0]);
+  c.sc = sc;
+  c.nx = nx;
+  c.ny = ny;
+  c.idx = (float)(1.0 / p.dx);
+  c.idy = (float)(1.0 / p.dy);
+  c.h2x = (float)(1.0 / (2.0 * p.dx));
+  c.h2y = (float)(1.0 / (2.0 * p.dy));
+  c.thresh = (float)(0.1 / p.dx);
+  k_adj_correct<<<grd, blk, 0, st>>>(c);
+  k_adj_grad<<<grd, blk, 0, st>>>(c);
+  // ---- multigrid, reversed (cycles from the last to the first)
+  if (cudaMemsetAsync(F(A.GB[0]), 0, (size_t)N * 4, st) != cudaSuccess) return AJ_ERR_CUDA;
+  const float ax = (float)(1.0 / (p.dx * p.dx)), ay = (float)(1.0 / (p.dy * p.dy));
+  const float den = (float)(2.0 * (1.0 / (p.dx * p.dx) + 1.0 / (p.dy * p.dy)));
+  const int nl = L.nlev;
+  auto lg = [&](int l) { return dim3(cdiv(L.lm[l], kAdjBX), cdiv(L.ln[l], kAdjBY)); };
+  for (int cyc = p.v_cycles - 1; cyc >= 0; --cyc) {
+    const int* nc = cyc == 0 ? nullptr : ncyc;                 // cycle 0 always ran
+    for (int l = 0; l < nl; ++l) {                             // up-sweep, reversed
+      const int n = L.ln[l], m = L.lm[l];
+      k_adj_jac<<<lg(l), blk, 0, st>>>(F(A.GX[l]), F(A.GT[l]), F(A.GB[l]), n, m, ax, ay, den, 1,
+                                       l > 0, nc, cyc);
+      k_adj_jac<<<lg(l), blk, 0, st>>>(F(A.GT[l]), F(A.GX[l]), F(A.GB[l]), n, m, ax, ay, den, 0, 0,
+                                       nc, cyc);
+      k_adj_prolong<<<lg(l + 1), blk, 0, st>>>(F(A.GX[l]), F(A.GX[l + 1]), L.ln[l + 1],
+                                               L.lm[l + 1], nc, cyc);
+    }
+    {                                                          // coarsest: 10 sweeps from zero
+      const int n = L.ln[nl], m = L.lm[nl];
+      for (int s = 9; s >= 0; --s) {
+        const float* gin = (s % 2 == 1) ? F(A.GX[nl]) : F(A.GT[nl]);
+        float* gout = s == 0 ? nullptr : ((s % 2 == 1) ? F(A.GT[nl]) : F(A.GX[nl]));
+        k_adj_jac<<<lg(nl), blk, 0, st>>>(gin, gout, F(A.GB[nl]), n, m, ax, ay, den, 0, s == 9,
+                                          nc, cyc);
+      }
+    }
+    for (int l = nl - 1; l >= 0; --l) {                        // down-sweep, reversed
+      const int n = L.ln[l], m = L.lm[l];
+      k_adj_restrict<<<lg(l), blk, 0, st>>>(F(A.GB[l + 1]), F(A.GB[l]), F(A.GX[l]), n, m, ax, ay,
+                                            nc, cyc);
+      k_adj_jac<<<lg(l), blk, 0, st>>>(F(A.GX[l]), F(A.GT[l]), F(A.GB[l]), n, m, ax, ay, den, 1, 0,
+                                       nc, cyc);
+      // the first pre-sweep's input: zero below level 0 and in the first cycle
+      float* gout = (l == 0 && cyc > 0) ? F(A.GX[0]) : nullptr;
+      k_adj_jac<<<lg(l), blk, 0, st>>>(F(A.GT[l]), gout, F(A.GB[l]), n, m, ax, ay, den, 0, 0, nc,
+                                       cyc);
+    }
+  }
+  // ---- rhs and divergence, reversed
+  k_adj_div<<<grd, blk, 0, st>>>(F(A.GB[0]), mask, F(A.gus), F(A.gvs), sc, nx, ny,
+                                 (float)(1.0 / (2.0 * p.dx)), (float)(1.0 / (2.0 * p.dy)));
+  // ---- predictor, reversed
+  const bool rk2 = p.fast_mode != 0;
+  AdjRk r{};
+  r.gus = F(A.gus);
+  r.gvs = F(A.gvs);
+  r.wu = F(A.wnu);
+  r.wv = F(A.wnv);
+  r.chi = at<float>(ws, L.chi);
+  r.w1u = F(A.w1u);
+  r.w1v = F(A.w1v);
+  r.dbar = F(A.dbar);
+  r.kout_u = F(A.kAu);
+  r.kout_v = F(A.kAv);
+  r.kext_u = rk2 ? F(A.kEu) : nullptr;
+  r.kext_v = rk2 ? F(A.kEv) : nullptr;
+  r.part = at<double>(aws, A.part);
+  r.mask = mask;
+  r.sc = sc;
+  r.nx = nx;
+  r.ny = ny;
+  r.idx = (float)(1.0 / p.dx);
+  r.idy = (float)(1.0 / p.dy);
+  r.idx2 = (float)(1.0 / (p.dx * p.dx));
+  r.idy2 = (float)(1.0 / (p.dy * p.dy));
+  r.nu = (float)p.nu;
+  r.inv_eta = (float)(1.0 / p.brinkman_eta);
+  r.sdf_fac = (float)(-1.0 / (0.1 * p.dx));
+  r.cn = rk2 ? 0.5f : (float)(2.0 / 3.0);
+  k_adj_rk_out<<<grd, blk, 0, st>>>(r);
+  // stage states: RK3 w3 = sB, w2 = sA; RK2 w2 = sA; stage 1 is the input
+  const float* Wu[3] = {u, at<float>(ws, L.sA_u), at<float>(ws, L.sB_u)};
+  const float* Wv[3] = {v, at<float>(ws, L.sA_v), at<float>(ws, L.sB_v)};
+  const float cn3[3] = {0.f, 1.f, 0.25f};     // RK3: slope of stage s-1 from x_s
+  float* KU[2] = {F(A.kAu), F(A.kBu)};
+  float* KV[2] = {F(A.kAv), F(A.kBv)};
+  const int nst = rk2 ? 2 : 3;
+  int cur = 0;
+  for (int s = nst; s >= 1; --s) {
+    r.kin_u = KU[cur];
+    r.kin_v = KV[cur];
+    r.kout_u = KU[1 - cur];
+    r.kout_v = KV[1 - cur];
+    r.wu = Wu[s - 1];
+    r.wv = Wv[s - 1];
+    r.last = s == 1;
+    r.cn = rk2 ? 1.f : cn3[s - 1];
+    r.kext_u = (rk2 && s == 2) ? F(A.kEu) : nullptr;
+    r.kext_v = (rk2 && s == 2) ? F(A.kEv) : nullptr;
+    r.gu = gu;
+    r.gv = gv;
+    r.gsdf = (s == 1 && p.has_sdf) ? gsdf : nullptr;
+    r.part = at<double>(aws, A.part) + (size_t)(nst - s) * A.nblk;
+    k_adj_rk_stage<<<grd, blk, 0, st>>>(r);
+    cur = 1 - cur;
+  }
+  if (gscal)
+    k_adj_scalars<<<1, 256, 0, st>>>(at<double>(aws, A.part), nst * A.nblk, gu_o, F(A.gus), mask,
+                                     ny, gscal);
+  return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+}
+
+int step_vjp_kernel_count(const AjStepParams& p, const Layout& L) {
+  const int nst = p.fast_mode ? 2 : 3;
+  int n = 1 + nst;                                  // dt + forward predictor stages
+  if (p.v_cycles > 1) n += 1 + 1 + p.v_cycles * (5 * L.nlev + 12);   // rhs, forward solve
+  n += 2;                                           // correction, gradient
+  n += p.v_cycles * (6 * L.nlev + 10);              // reversed V-cycles
+  n += 1 + 1 + nst + 1;                             // divergence, output, stages, scalars
+  return n;
+}
+
+}  // namespace aj

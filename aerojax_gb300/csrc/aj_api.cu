@@ -544,6 +544,54 @@ int32_t aj_step_host(const AjStepParams* prm, const float* h_u, const float* h_v
   });
 }
 
+// the configurations the reverse pass covers: the collocated step_pure with
+// the von Karman boundaries, upwind RK3/RK2, a fixed dt and the parity V-cycle
+static int vjp_params_ok(const AjStepParams& p) {
+  if (p.variant != AJ_VARIANT_PURE || p.grid_type != AJ_GRID_COLLOCATED ||
+      p.flow_type != AJ_FLOW_VON_KARMAN || p.mg_mode != AJ_MG_PARITY ||
+      p.advection != AJ_ADV_UPWIND || p.cfl_dt || p.warm_start || p.nn_factor > 0)
+    return AJ_ERR_PARAM;
+  if (p.nx < 3 || p.ny < 3) return AJ_ERR_SHAPE;
+  return AJ_OK;
+}
+
+size_t aj_step_vjp_workspace_size(const AjStepParams* prm) {
+  if (!prm) return 0;
+  AjStepParams p = normalise(*prm);
+  Layout L;
+  if (vjp_params_ok(p) != AJ_OK || !make_layout(p, L)) return 0;
+  return step_vjp_workspace(p, L);
+}
+
+int32_t aj_step_vjp(const AjStepParams* prm, const float* u, const float* v, const float* mask,
+                    const float* gu_out, const float* gv_out, const float* gp_out, float* gu,
+                    float* gv, float* gsdf, double* gscal, void* ws, size_t bytes, void* aws,
+                    size_t adj_bytes, void* stream) {
+  if (!prm || !u || !v || !mask || !gu_out || !gv_out || !gu || !gv || !aws) return AJ_ERR_PARAM;
+  int rc = aj_check_params(prm);
+  if (rc != AJ_OK) return rc;
+  AjStepParams p = normalise(*prm);
+  if ((rc = vjp_params_ok(p)) != AJ_OK) return rc;
+  Layout L;
+  make_layout(p, L);
+  if ((rc = ws_ok(L, ws, bytes)) != AJ_OK) return rc;
+  if (adj_bytes < step_vjp_workspace(p, L)) return AJ_ERR_WORKSPACE;
+  std::string key = make_key(6, p, {ws, aws, u, v, mask, gu_out, gv_out, gp_out, gu, gv, gsdf,
+                                    gscal});
+  return run_captured(key, (cudaStream_t)stream, [&](cudaStream_t s) {
+    return launch_step_vjp(p, L, ws, aws, u, v, mask, gu_out, gv_out, gp_out, gu, gv, gsdf,
+                           gscal, s);
+  });
+}
+
+int32_t aj_step_vjp_kernel_count(const AjStepParams* prm) {
+  if (!prm) return -1;
+  AjStepParams p = normalise(*prm);
+  Layout L;
+  if (vjp_params_ok(p) != AJ_OK || !make_layout(p, L)) return -1;
+  return step_vjp_kernel_count(p, L);
+}
+
 const float* aj_workspace_rhs(const AjStepParams* prm, void* ws) {
   if (!prm || !ws) return nullptr;
   Layout L;

@@ -171,6 +171,13 @@ int launch_les(const AjStepParams& p, const Layout& L, void* ws, int model, cons
 int launch_cfl(const AjStepParams& p, void* ws, const float* u, const float* v,
                float* dt_out, cudaStream_t st);
 int launch_set_dt(const AjStepParams& p, void* ws, cudaStream_t st);
+// reverse mode of the collocated step_pure (aj_adjoint.cu)
+size_t step_vjp_workspace(const AjStepParams& p, const Layout& L);
+int launch_step_vjp(const AjStepParams& p, const Layout& L, void* ws, void* aws, const float* u,
+                    const float* v, const float* mask, const float* gu_o, const float* gv_o,
+                    const float* gp_o, float* gu, float* gv, float* gsdf, double* gscal,
+                    cudaStream_t st);
+int step_vjp_kernel_count(const AjStepParams& p, const Layout& L);
 int launch_chi(const AjStepParams& p, const Layout& L, void* ws, const float* mask,
                const float* sdf, cudaStream_t st);
 // projection (aj_project.cu)

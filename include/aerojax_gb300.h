@@ -138,6 +138,27 @@ int32_t aj_step(const AjStepParams* prm, const float* u, const float* v, const f
                 const float* p_guess, float* u_out, float* v_out, float* p_out,
                 void* workspace, size_t workspace_bytes, AjStats* stats, void* stream);
 
+/* Reverse mode of one step_pure: the vector-Jacobian product that jax.grad
+   evaluates through the reference's differentiable rollouts
+   (solver/solver.py:34-75 differentiable_rollout, :78-114 design_loss /
+   grad_design_loss; inverse_design_WIP/optimizer_autodiff.py:113-205).
+   Covers the collocated von Karman step_pure with upwind RK3/RK2, a fixed dt
+   (cfl_dt = 0) and the parity V-cycle (AJ_ERR_PARAM otherwise).
+   Inputs: the step's inputs u, v (nx*ny) and the mask of aj_prepare on this
+   workspace (prepared with the SDF when has_sdf), and the cotangents of the
+   step's outputs gu_out, gv_out and gp_out (nullable: zero).  Writes the
+   cotangents of the inputs gu, gv; adds the SDF's cotangent into gsdf
+   (nullable; nothing is added without an SDF) and (d/d nu, d/d U_inf) into
+   gscal[0..1] (nullable, FP64).  adj_workspace: aj_step_vjp_workspace_size
+   bytes.  The forward stage states are recomputed inside the call. */
+size_t aj_step_vjp_workspace_size(const AjStepParams* prm);
+int32_t aj_step_vjp(const AjStepParams* prm, const float* u, const float* v, const float* mask,
+                    const float* gu_out, const float* gv_out, const float* gp_out, float* gu,
+                    float* gv, float* gsdf, double* gscal, void* workspace,
+                    size_t workspace_bytes, void* adj_workspace, size_t adj_bytes, void* stream);
+/* Kernels one aj_step_vjp launches (-1 on unsupported parameters). */
+int32_t aj_step_vjp_kernel_count(const AjStepParams* prm);
+
 /* The pressure solve alone.  Replaces poisson_multigrid
    (pressure_solvers/multigrid_solver.py:55-241) for grid_type COLLOCATED and
    poisson_multigrid_mac (pressure_solvers/multigrid_solver_mac.py:59-246) for

@@ -1,0 +1,145 @@
+"""aj_step_vjp (reverse mode of step_pure) on the GPU against the FP64 oracle
+(oracle/adjoint_np.py, itself pinned by finite differences), through the
+C ABI; linearity and determinism at 2048x512; the rollout's reverse scan."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+DX, DT, NU, U = 0.05, 0.004, 0.02, 1.0
+
+
+@pytest.fixture(scope="module")
+def dev():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch.device("cuda:0")
+
+
+def _case(nx, ny, seed, dx=DX):
+    from oracle import ref_np as R
+    rng = np.random.default_rng(seed)
+    X, Y = np.meshgrid((np.arange(nx) + 0.5) * dx, (np.arange(ny) + 0.5) * dx, indexing="ij")
+    s = R.sdf_cylinder(X, Y, 0.28 * nx * dx, 0.5 * ny * dx, 0.08 * ny * dx)
+    mask = R.mask_from_sdf(s, 0.5 * dx)
+    u = U + 0.3 * rng.standard_normal((nx, ny))
+    v = 0.3 * rng.standard_normal((nx, ny))
+    f32 = lambda a: np.asarray(a, np.float32)
+    return f32(u), f32(v), f32(mask), f32(s), rng
+
+
+def _rel(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+
+
+def _t(a, dev):
+    return torch.as_tensor(np.asarray(a, np.float32), device=dev)
+
+
+@pytest.mark.parametrize("fast,use_sdf,cycles", [(False, True, 1), (True, True, 1),
+                                                 (False, False, 1), (False, True, 3)])
+def test_step_vjp_matches_oracle(dev, fast, use_sdf, cycles):
+    """Every cotangent within 1e-4 (relative L2; FP32 reverse pass against
+    FP64) of the oracle's on a 128x64 cylinder case."""
+    from oracle import adjoint_np as A
+    from aerojax_gb300 import adjoint as ADJ
+    from aerojax_gb300.params import SimState
+    nx, ny = 128, 64
+    u, v, mask, s, rng = _case(nx, ny, 11)
+    sdf = s if use_sdf else None
+    gu, gv, gp = (rng.standard_normal((nx, ny)).astype(np.float32) for _ in range(3))
+    ref = A.step_pure_vjp(u, v, DT, mask, sdf, DX, DX, NU, U, gu, gv, gp, v_cycles=cycles,
+                          fast_mode=fast)
+    st = SimState(u=_t(u, dev), v=_t(v, dev), p=None, u_prev=None, v_prev=None, c=None, dt=DT,
+                  iteration=0)
+    got = ADJ.step_pure_vjp(st, _t(mask, dev), None if sdf is None else _t(sdf, dev), DX, DX, NU,
+                            U, _t(gu, dev), _t(gv, dev), _t(gp, dev), v_cycles=cycles,
+                            fast_mode=fast)
+    assert _rel(got["u"].cpu(), ref["u"]) <= 1e-4
+    assert _rel(got["v"].cpu(), ref["v"]) <= 1e-4
+    if use_sdf:
+        assert _rel(got["sdf"].cpu(), ref["sdf"]) <= 1e-4
+    else:
+        assert got["sdf"] is None and ref["sdf"] is None
+    assert abs(got["nu"] - ref["nu"]) <= 1e-4 * abs(ref["nu"])
+    assert abs(got["U_inf"] - ref["U_inf"]) <= 1e-4 * max(abs(ref["U_inf"]), 1.0)
+
+
+def test_step_vjp_full_size(dev):
+    """2048x512: against the oracle, linear in the cotangent, and bit-for-bit
+    repeatable."""
+    from oracle import adjoint_np as A
+    from aerojax_gb300.adjoint import StepVjp, _config
+    nx, ny, dx = 2048, 512, 1.0 / 128
+    u, v, mask, s, rng = _case(nx, ny, 12, dx)
+    dt = 2e-4
+    cfg = _config(nx, ny, dx, dx, 1e-3, U, dt, True)
+    op = StepVjp(cfg, dev)
+    M, S = _t(mask, dev), _t(s, dev)
+    op.prepare(M, S)
+    ud, vd = _t(u, dev), _t(v, dev)
+    g1 = [rng.standard_normal((nx, ny)).astype(np.float32) for _ in range(3)]
+    g2 = [rng.standard_normal((nx, ny)).astype(np.float32) for _ in range(3)]
+
+    def run(g):
+        op.zero_grad()
+        gu, gv = op(ud, vd, M, *(_t(x, dev) for x in g))
+        return gu.cpu().numpy().copy(), gv.cpu().numpy().copy(), op.gsdf.cpu().numpy().copy(), \
+            op.gscal.cpu().numpy().copy()
+
+    r1 = run(g1)
+    r1b = run(g1)
+    for a, b in zip(r1, r1b):
+        assert np.array_equal(a, b)                   # deterministic
+    r2 = run(g2)
+    r12 = run([2.0 * a - 0.5 * b for a, b in zip(g1, g2)])
+    for a, b, c in zip(r1[:3], r2[:3], r12[:3]):
+        assert _rel(c, 2.0 * a - 0.5 * b) <= 1e-5
+    ref = A.step_pure_vjp(u, v, dt, mask, s, dx, dx, 1e-3, U, *g1)
+    assert _rel(r1[0], ref["u"]) <= 1e-4
+    assert _rel(r1[1], ref["v"]) <= 1e-4
+    assert _rel(r1[2], ref["sdf"]) <= 1e-4
+    assert abs(r1[3][0] - ref["nu"]) <= 1e-4 * abs(ref["nu"])
+    assert abs(r1[3][1] - ref["U_inf"]) <= 1e-4 * max(abs(ref["U_inf"]), 1.0)
+
+
+def test_rollout_vjp_matches_oracle(dev):
+    """Four steps forward (history kept on the device) and the reverse scan:
+    the initial state's, the SDF's and nu's cotangents match the oracle's."""
+    from oracle import adjoint_np as A
+    from aerojax_gb300 import adjoint as ADJ
+    from aerojax_gb300.params import SimState
+    nx, ny, n = 128, 64, 4
+    u, v, mask, s, rng = _case(nx, ny, 13)
+    gu, gv = (rng.standard_normal((nx, ny)).astype(np.float32) for _ in range(2))
+    params = {"dx": DX, "dy": DX, "nu": NU, "U_inf": U, "sdf": _t(s, dev)}
+    st = SimState(u=_t(u, dev), v=_t(v, dev), p=None, u_prev=None, v_prev=None, c=None, dt=DT,
+                  iteration=0)
+    final, hist = ADJ.differentiable_rollout(st, _t(mask, dev), params, n)
+    assert hist[0].shape == (n, nx, ny) and final.iteration == n
+    (ru, rv), _ = A.rollout(u, v, DT, mask, s, DX, DX, NU, U, n)
+    assert _rel(final.u.cpu(), ru) <= 1e-5
+    got = ADJ.rollout_vjp(st, _t(mask, dev), params, n, _t(gu, dev), _t(gv, dev), history=hist)
+    ref = A.rollout_vjp(u, v, DT, mask, s, DX, DX, NU, U, n, gu, gv)
+    assert _rel(got["u"].cpu(), ref["u"]) <= 2e-4
+    assert _rel(got["v"].cpu(), ref["v"]) <= 2e-4
+    assert _rel(got["sdf"].cpu(), ref["sdf"]) <= 2e-4
+    assert abs(got["nu"] - ref["nu"]) <= 2e-4 * abs(ref["nu"])
+    assert abs(got["U_inf"] - ref["U_inf"]) <= 2e-4 * max(abs(ref["U_inf"]), 1.0)
+
+
+def test_step_vjp_rejects_uncovered_configurations(dev):
+    import ctypes
+    from dataclasses import replace
+    from aerojax_gb300 import _lib
+    from aerojax_gb300.adjoint import _config
+    from aerojax_gb300.solver import make_params
+    base = _config(128, 64, DX, DX, NU, U, DT, False)
+    for bad in (replace(base, grid_type="mac", variant="gui"), replace(base, mg_mode="converge"),
+                replace(base, cfl_dt=True), replace(base, advection_scheme="weno5")):
+        p = make_params(bad)
+        assert _lib.lib().aj_step_vjp_workspace_size(ctypes.byref(p)) == 0
+        assert _lib.lib().aj_step_vjp_kernel_count(ctypes.byref(p)) == -1
