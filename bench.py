@@ -51,7 +51,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="naca", choices=["naca", "ensemble", "tri4096", "post"],
+    ap.add_argument("--workload", default="naca",
+                    choices=["naca", "ensemble", "tri4096", "post", "adjoint"],
                     help="naca: the metric's workload (default); ensemble: 64 cylinder "
                          "channels of uneven sizes in one graph launch; tri4096: the "
                          "4096x2048 three-cylinder dynamic-LES flow")
@@ -541,6 +542,9 @@ def side_workload(args):
                        "l2": "4096x2048 inputs above the L2 size (no flush); launches "
                              "replayed from a CUDA graph of 10"}}))
         return
+    if args.workload == "adjoint":
+        adjoint_workload(args, dev, st)
+        return
     from aerojax_gb300 import configs
     from aerojax_gb300 import nn as NNW
     case = configs.tri_cyl_4096x2048(device=dev)
@@ -584,6 +588,110 @@ def side_workload(args):
         "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": case["name"], "arms": out,
                    "l2": "working set (~1 GB) above the L2 size (no flush)"}}))
+
+
+# algorithmic bytes per cell of one aj_step_vjp (RK3, one V-cycle, four
+# coarser levels): each array read or written once per kernel, FP32
+#   forward predictor: stage 1 reads u, v, chi, writes 2; stages 2, 3 read
+#     the stage state, u, v, chi, write 2                              20+28+28
+#   correction: reads gu, gv, mask, writes gu*, gv*, gdpx, gdpy            28
+#   gradient transpose: reads gdpx, gdpy, gp, writes pbar                  16
+#   level-0 multigrid: 4 reversed sweeps (read 1, update b 2, write 1),
+#     restriction transpose (update b and x: 4), prolongation read 1       88
+#   levels 1-4 of the V-cycle: a third of level 0 (1/4 + 1/16 + ...)      29
+#   divergence transpose: reads b, mask, updates gu*, gv*                  24
+#   output stage: reads gu*, gv*, mask, chi, u*, v*, writes 5 fields       44
+#   three reversed stages: read slope 2, state 2, chi, update w1 2 and
+#     den 1, write slope 2 (the last writes gu, gv, updates gsdf)   52+52+52
+VJP_BYTES_PER_CELL = 20 + 28 + 28 + 28 + 16 + 88 + 29 + 24 + 44 + 3 * 52
+
+
+def adjoint_workload(args, dev, st):
+    """Reverse mode of step_pure (aj_step_vjp) on a 2048x512 collocated
+    cylinder channel: RK3, one parity V-cycle (the defaults of the
+    reference's differentiable rollout), gradients w.r.t. u, v, the SDF, nu
+    and U_inf.  The forward step is timed beside it."""
+    import torch
+    from aerojax_gb300 import _lib
+    from aerojax_gb300.adjoint import StepVjp, _config
+    nx, ny, dx, dt = 2048, 512, 1.0 / 128, 2e-4
+    cells = nx * ny
+    g = torch.Generator(device=dev).manual_seed(0)
+    X = (torch.arange(nx, device=dev, dtype=torch.float32)[:, None] + 0.5) * dx
+    Y = (torch.arange(ny, device=dev, dtype=torch.float32)[None, :] + 0.5) * dx
+    sdf = torch.sqrt((X - 0.28 * nx * dx) ** 2 + (Y - 0.5 * ny * dx) ** 2) - 0.08 * ny * dx
+    mask = 1.0 - torch.sigmoid(-sdf / (0.5 * dx))
+    u = 1.0 + 0.3 * torch.randn((nx, ny), device=dev, generator=g)
+    v = 0.3 * torch.randn((nx, ny), device=dev, generator=g)
+    op = StepVjp(_config(nx, ny, dx, dx, 1e-3, 1.0, dt, True), dev)
+    op.prepare(mask, sdf)
+    op.u_in.copy_(u)
+    op.v_in.copy_(v)
+    for t in op.g_in:
+        t.copy_(torch.randn((nx, ny), device=dev, generator=g))
+    flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    L = _lib.lib()
+    P = op.plan
+    uo, vo, po = (torch.empty((nx, ny), device=dev) for _ in range(3))
+
+    def fwd():
+        rc = L.aj_step(ctypes.byref(P.params), op.u_in.data_ptr(), op.v_in.data_ptr(),
+                       mask.data_ptr(), None, uo.data_ptr(), vo.data_ptr(), po.data_ptr(),
+                       P.ws.data_ptr(), P.nbytes, P.stats_buf.data_ptr(), st.cuda_stream)
+        assert rc == 0, rc
+
+    def vjp():
+        op(op.u_in, op.v_in, mask, op.g_in[0], op.g_in[1], op.g_in[2], stream=st)
+
+    def timed(fn, k):
+        ev = []
+        for _ in range(k):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            fn()
+            e1.record(st)
+            ev.append((e0, e1))
+        torch.cuda.synchronize()
+        return sum(a.elapsed_time(b) for a, b in ev) / k
+
+    for _ in range(max(3, args.warmup)):
+        fwd()
+        vjp()
+    torch.cuda.synchronize()
+    fwd_ms = timed(fwd, args.steps)
+    vjp_ms = timed(vjp, args.steps)
+    kc = int(L.aj_step_vjp_kernel_count(ctypes.byref(P.params)))
+    hbm = 6800.0
+    if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")):
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            hbm = float(json.load(f)["hbm_gbs"])
+    gbs = VJP_BYTES_PER_CELL * cells / (vjp_ms * 1e-3) / 1e9
+    cpu = None
+    if not args.no_cpu_baseline and not args.quick:
+        import numpy as np
+        from oracle import adjoint_np as A
+        h = lambda t: t.detach().cpu().numpy().astype(np.float64)
+        t0 = time.perf_counter()
+        A.step_pure_vjp(h(op.u_in), h(op.v_in), dt, h(mask), h(sdf), dx, dx, 1e-3, 1.0,
+                        h(op.g_in[0]), h(op.g_in[1]), h(op.g_in[2]))
+        el = time.perf_counter() - t0
+        cpu = {"value": cells / el / 1e6, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"one 2048x512 reverse-mode step ({el:.1f} s), NumPy FP64 oracle "
+                         "(forward recomputation included)"}
+    print(json.dumps({
+        "metric": "Mcell-steps/s of the reverse-mode step_pure (aj_step_vjp), 2048x512",
+        "value": cells / (vjp_ms * 1e-3) / 1e6, "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": vjp_ms,
+        "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded cylinder channel)",
+        "config": {"workload": "step_pure_vjp_cylinder_2048x512", "rk": "rk3", "v_cycles": 1,
+                   "gradients": ["u", "v", "sdf", "nu", "U_inf"],
+                   "forward_ms_per_step": fwd_ms, "vjp_over_forward": vjp_ms / fwd_ms,
+                   "kernels_per_vjp": kc, "algorithmic_bytes_per_cell": VJP_BYTES_PER_CELL,
+                   "achieved_gbs": gbs, "frac_of_measured_hbm": gbs / hbm,
+                   "l2": "flushed before every call (256 MiB write outside the timed events)"},
+        "cpu_baseline": cpu,
+        "gpu_launches": kc * args.steps}))
 
 
 def main():
