@@ -156,6 +156,7 @@ struct AdjCorr {
 // cotangents of u*, v* and of the projected gradient at source (a, b)
 // (step.py:341-397 reversed)
 __global__ void __launch_bounds__(256) k_adj_correct(AdjCorr c) {
+  pdl_wait();
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = blockIdx.y * blockDim.y + threadIdx.y;
   const int nx = c.nx, ny = c.ny;
@@ -183,6 +184,7 @@ __global__ void __launch_bounds__(256) k_adj_correct(AdjCorr c) {
 
 // cotangent of p: the output's own cotangent plus the gradient's transpose
 __global__ void __launch_bounds__(256) k_adj_grad(AdjCorr c) {
+  pdl_wait();
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = blockIdx.y * blockDim.y + threadIdx.y;
   const int nx = c.nx, ny = c.ny;
@@ -202,6 +204,7 @@ __global__ void __launch_bounds__(256) k_adj_jac(const float* __restrict__ gin,
                                                  int n, int m, float ax, float ay, float d,
                                                  int zero_last, int assign, const int* ncyc,
                                                  int cyc) {
+  pdl_wait();
   if (ncyc && cyc >= *ncyc) return;
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = blockIdx.y * blockDim.y + threadIdx.y;
@@ -219,11 +222,51 @@ __global__ void __launch_bounds__(256) k_adj_jac(const float* __restrict__ gin,
   }
 }
 
+// the ten reversed coarsest-grid sweeps (the forward smooths 10 times from a
+// zero guess, multigrid_solver.py:186-187) in one block: the cotangent
+// ping-pongs in shared memory, b's cotangent accumulates in a third array.
+// Used when 3 arrays of the level fit the block's shared memory.
+constexpr int kCoarsestThreads = 1024;
+__global__ void __launch_bounds__(kCoarsestThreads) k_adj_coarsest(const float* __restrict__ gin,
+                                                                   float* __restrict__ gb, int n,
+                                                                   int m, float ax, float ay,
+                                                                   float d, const int* ncyc,
+                                                                   int cyc) {
+  pdl_wait();
+  if (ncyc && cyc >= *ncyc) return;
+  extern __shared__ float csm[];
+  const int nm = n * m;
+  float* A = csm;
+  float* B = csm + nm;
+  float* G = csm + 2 * nm;
+  for (int c = threadIdx.x; c < nm; c += blockDim.x) A[c] = gin[c];
+  __syncthreads();
+  for (int s = 9; s >= 0; --s) {
+    for (int c = threadIdx.x; c < nm; c += blockDim.x) {
+      const int i = c / m, j = c - i * m;
+      const float hc = A[c] / d;
+      G[c] = s == 9 ? -hc : G[c] - hc;
+      if (s > 0) {
+        const int ip = i + 1 < n ? i + 1 : n - 1, im = i > 0 ? i - 1 : 0;
+        const int jp = j + 1 < m ? j + 1 : m - 1, jm = j > 0 ? j - 1 : 0;
+        B[c] = ax * (A[ip * m + j] / d + A[im * m + j] / d) +
+               ay * (A[i * m + jp] / d + A[i * m + jm] / d);
+      }
+    }
+    __syncthreads();
+    float* t = A;
+    A = B;
+    B = t;
+  }
+  for (int c = threadIdx.x; c < nm; c += blockDim.x) gb[c] = G[c];
+}
+
 // transpose of the reference prolongation (multigrid_solver.py:134-156) onto
 // the coarse cell (I, J): even fine cells inject, odd interior ones average
 __global__ void __launch_bounds__(256) k_adj_prolong(const float* __restrict__ gf,
                                                      float* __restrict__ gc, int nc, int mc,
                                                      const int* ncyc, int cyc) {
+  pdl_wait();
   if (ncyc && cyc >= *ncyc) return;
   const int J = blockIdx.x * blockDim.x + threadIdx.x;
   const int I = blockIdx.y * blockDim.y + threadIdx.y;
@@ -252,6 +295,7 @@ __global__ void __launch_bounds__(256) k_adj_restrict(const float* __restrict__ 
                                                       float* __restrict__ gx, int n, int m,
                                                       float ax, float ay, const int* ncyc,
                                                       int cyc) {
+  pdl_wait();
   if (ncyc && cyc >= *ncyc) return;
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = blockIdx.y * blockDim.y + threadIdx.y;
@@ -275,6 +319,7 @@ __global__ void __launch_bounds__(256) k_adj_div(const float* __restrict__ gb0,
                                                  float* __restrict__ gus, float* __restrict__ gvs,
                                                  const DevScalars* sc, int nx, int ny, float h2x,
                                                  float h2y) {
+  pdl_wait();
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= nx || j >= ny) return;
@@ -310,6 +355,7 @@ struct AdjRk {
 // cotangent of the final combination x_n / den, through the predictor's hard
 // mask and boundary rows (rk3_simple_new.py:332-337, 262-275; step.py:182-191)
 __global__ void __launch_bounds__(256) k_adj_rk_out(AdjRk a) {
+  pdl_wait();
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = blockIdx.y * blockDim.y + threadIdx.y;
   const int nx = a.nx, ny = a.ny;
@@ -319,8 +365,8 @@ __global__ void __launch_bounds__(256) k_adj_rk_out(AdjRk a) {
   bc_gather_T<false>(a.gus, a.gvs, nullptr, i, j, nx, ny, gu, gv);
   if (!live_at(a.mask, k)) gu = gv = 0.f;
   const float dt = a.sc->dt;
-  const float den = 1.f + dt * ldg(a.chi + k) * a.inv_eta;
-  const float xu = gu / den, xv = gv / den;
+  const float rden = 1.f / (1.f + dt * ldg(a.chi + k) * a.inv_eta);
+  const float xu = gu * rden, xv = gv * rden;
   // where x != 0 the output cell is interior and live: it holds x_n/den itself
   a.dbar[k] = -(xu * ldg(a.wu + k) + xv * ldg(a.wv + k));
   a.w1u[k] = xu;                                                // 1/3 + 2/3 (RK2: 1)
@@ -340,11 +386,12 @@ __global__ void __launch_bounds__(256) k_adj_rk_out(AdjRk a) {
 // +f(q) - f(W(q)) when its velocity is positive, else -f(q) + f(E(q)): the
 // gather visits q = c and its four neighbours.
 __global__ void __launch_bounds__(256) k_adj_rk_stage(AdjRk a) {
+  pdl_wait();
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = blockIdx.y * blockDim.y + threadIdx.y;
   const int nx = a.nx, ny = a.ny;
   const bool valid = i < nx && j < ny;
-  double nub = 0.0;
+  df nub{0.f, 0.f};
   if (valid) {
     const long k = (long)i * ny + j;
     const int im = i > 0 ? i - 1 : 0, ip = i < nx - 1 ? i + 1 : nx - 1;
@@ -393,11 +440,12 @@ __global__ void __launch_bounds__(256) k_adj_rk_stage(AdjRk a) {
     // d/d nu: kbar . lap(w)
     const float lu = (uxp + uxm - 2.f * U) * a.idx2 + (uyp + uym - 2.f * U) * a.idy2;
     const float lv = (vxp + vxm - 2.f * V) * a.idx2 + (vyp + vym - 2.f * V) * a.idy2;
-    nub = (double)ku * lu + (double)kv * lv;
+    // exact products, summed in double-FP32 (the sum cancels heavily)
+    nub = df_add(two_prod(ku, lu), two_prod(kv, lv));
     const float dt = a.sc->dt;
     if (!a.last) {
-      const float den = 1.f + dt * ldg(a.chi + k) * a.inv_eta;
-      const float xu = gu / den, xv = gv / den;
+      const float rden = 1.f / (1.f + dt * ldg(a.chi + k) * a.inv_eta);
+      const float xu = gu * rden, xv = gv * rden;
       a.dbar[k] -= xu * U + xv * V;
       a.w1u[k] += xu;
       a.w1v[k] += xv;
@@ -418,18 +466,33 @@ __global__ void __launch_bounds__(256) k_adj_rk_stage(AdjRk a) {
       }
     }
   }
-  const double t = block_sum(nub);
+  const double t = block_sum_df(nub);
   if (threadIdx.x == 0 && threadIdx.y == 0) a.part[blockIdx.y * gridDim.x + blockIdx.x] = t;
 }
 
 // d/d nu from the stage partials and d/d U_inf from the inlet rows (the
 // correction's final row 0 where live, and the predictor output's row 0),
 // summed in a fixed order and added to gscal[0], gscal[1]
-__global__ void k_adj_scalars(const double* __restrict__ part, int nparts,
-                              const float* __restrict__ gu_o, const float* __restrict__ gus,
-                              const float* __restrict__ mask, int ny, double* gscal) {
-  double s = 0.0, u = 0.0;
-  for (int q = threadIdx.x; q < nparts; q += blockDim.x) s += part[q];
+// (four independent accumulators per thread keep four loads in flight: one
+// accumulator left the block waiting on one partial at a time, 28 us)
+__global__ void __launch_bounds__(1024) k_adj_scalars(const double* __restrict__ part, int nparts,
+                                                      const float* __restrict__ gu_o,
+                                                      const float* __restrict__ gus,
+                                                      const float* __restrict__ mask, int ny,
+                                                      double* gscal) {
+  pdl_wait();
+  const int bd = blockDim.x;
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0, u = 0.0;
+  int q = threadIdx.x;
+  for (; q + 3 * bd < nparts; q += 4 * bd) {
+    const double a = part[q], b = part[q + bd], c = part[q + 2 * bd], d = part[q + 3 * bd];
+    s0 += a;
+    s1 += b;
+    s2 += c;
+    s3 += d;
+  }
+  for (; q < nparts; q += bd) s0 += part[q];
+  double s = (s0 + s1) + (s2 + s3);
   for (int q = threadIdx.x; q < ny; q += blockDim.x) {
     u += (double)ldg(gus + q);
     if (live_at(mask, q)) u += (double)ldg(gu_o + q);
@@ -492,49 +555,52 @@ int launch_step_vjp(const AjStepParams& p, const Layout& L, void* ws, void* aws,
   c.h2x = (float)(1.0 / (2.0 * p.dx));
   c.h2y = (float)(1.0 / (2.0 * p.dy));
   c.thresh = (float)(0.1 / p.dx);
-  k_adj_correct<<<grd, blk, 0, st>>>(c);
-  k_adj_grad<<<grd, blk, 0, st>>>(c);
+  launch_pdl(true, k_adj_correct, grd, blk, 0, st, c);
+  launch_pdl(true, k_adj_grad, grd, blk, 0, st, c);
   // ---- multigrid, reversed (cycles from the last to the first)
   if (cudaMemsetAsync(F(A.GB[0]), 0, (size_t)N * 4, st) != cudaSuccess) return AJ_ERR_CUDA;
   const float ax = (float)(1.0 / (p.dx * p.dx)), ay = (float)(1.0 / (p.dy * p.dy));
   const float den = (float)(2.0 * (1.0 / (p.dx * p.dx) + 1.0 / (p.dy * p.dy)));
   const int nl = L.nlev;
   auto lg = [&](int l) { return dim3(cdiv(L.lm[l], kAdjBX), cdiv(L.ln[l], kAdjBY)); };
+  // one reversed sweep at level l (b's cotangent: level l's GB)
+  auto jac = [&](int l, const float* gin, float* gout, int zero_last, int assign, const int* nc,
+                 int cyc) {
+    launch_pdl(true, k_adj_jac, lg(l), blk, 0, st, gin, gout, F(A.GB[l]), L.ln[l], L.lm[l], ax,
+               ay, den, zero_last, assign, nc, cyc);
+  };
   for (int cyc = p.v_cycles - 1; cyc >= 0; --cyc) {
     const int* nc = cyc == 0 ? nullptr : ncyc;                 // cycle 0 always ran
     for (int l = 0; l < nl; ++l) {                             // up-sweep, reversed
-      const int n = L.ln[l], m = L.lm[l];
-      k_adj_jac<<<lg(l), blk, 0, st>>>(F(A.GX[l]), F(A.GT[l]), F(A.GB[l]), n, m, ax, ay, den, 1,
-                                       l > 0, nc, cyc);
-      k_adj_jac<<<lg(l), blk, 0, st>>>(F(A.GT[l]), F(A.GX[l]), F(A.GB[l]), n, m, ax, ay, den, 0, 0,
-                                       nc, cyc);
-      k_adj_prolong<<<lg(l + 1), blk, 0, st>>>(F(A.GX[l]), F(A.GX[l + 1]), L.ln[l + 1],
-                                               L.lm[l + 1], nc, cyc);
+      jac(l, F(A.GX[l]), F(A.GT[l]), 1, l > 0, nc, cyc);
+      jac(l, F(A.GT[l]), F(A.GX[l]), 0, 0, nc, cyc);
+      launch_pdl(true, k_adj_prolong, lg(l + 1), blk, 0, st, F(A.GX[l]), F(A.GX[l + 1]),
+                 L.ln[l + 1], L.lm[l + 1], nc, cyc);
     }
-    {                                                          // coarsest: 10 sweeps from zero
+    if (parity_coarsest_fused(L)) {                            // coarsest: 10 sweeps from zero
       const int n = L.ln[nl], m = L.lm[nl];
+      cudaFuncSetAttribute(k_adj_coarsest, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)kBlockSmemMax);
+      launch_pdl(true, k_adj_coarsest, dim3(1), dim3(kCoarsestThreads), (size_t)n * m * 12, st,
+                 F(A.GX[nl]), F(A.GB[nl]), n, m, ax, ay, den, nc, cyc);
+    } else {
       for (int s = 9; s >= 0; --s) {
         const float* gin = (s % 2 == 1) ? F(A.GX[nl]) : F(A.GT[nl]);
         float* gout = s == 0 ? nullptr : ((s % 2 == 1) ? F(A.GT[nl]) : F(A.GX[nl]));
-        k_adj_jac<<<lg(nl), blk, 0, st>>>(gin, gout, F(A.GB[nl]), n, m, ax, ay, den, 0, s == 9,
-                                          nc, cyc);
+        jac(nl, gin, gout, 0, s == 9, nc, cyc);
       }
     }
     for (int l = nl - 1; l >= 0; --l) {                        // down-sweep, reversed
-      const int n = L.ln[l], m = L.lm[l];
-      k_adj_restrict<<<lg(l), blk, 0, st>>>(F(A.GB[l + 1]), F(A.GB[l]), F(A.GX[l]), n, m, ax, ay,
-                                            nc, cyc);
-      k_adj_jac<<<lg(l), blk, 0, st>>>(F(A.GX[l]), F(A.GT[l]), F(A.GB[l]), n, m, ax, ay, den, 1, 0,
-                                       nc, cyc);
+      launch_pdl(true, k_adj_restrict, lg(l), blk, 0, st, F(A.GB[l + 1]), F(A.GB[l]), F(A.GX[l]),
+                 L.ln[l], L.lm[l], ax, ay, nc, cyc);
+      jac(l, F(A.GX[l]), F(A.GT[l]), 1, 0, nc, cyc);
       // the first pre-sweep's input: zero below level 0 and in the first cycle
-      float* gout = (l == 0 && cyc > 0) ? F(A.GX[0]) : nullptr;
-      k_adj_jac<<<lg(l), blk, 0, st>>>(F(A.GT[l]), gout, F(A.GB[l]), n, m, ax, ay, den, 0, 0, nc,
-                                       cyc);
+      jac(l, F(A.GT[l]), (l == 0 && cyc > 0) ? F(A.GX[0]) : nullptr, 0, 0, nc, cyc);
     }
   }
   // ---- rhs and divergence, reversed
-  k_adj_div<<<grd, blk, 0, st>>>(F(A.GB[0]), mask, F(A.gus), F(A.gvs), sc, nx, ny,
-                                 (float)(1.0 / (2.0 * p.dx)), (float)(1.0 / (2.0 * p.dy)));
+  launch_pdl(true, k_adj_div, grd, blk, 0, st, F(A.GB[0]), mask, F(A.gus), F(A.gvs), sc, nx, ny,
+             (float)(1.0 / (2.0 * p.dx)), (float)(1.0 / (2.0 * p.dy)));
   // ---- predictor, reversed
   const bool rk2 = p.fast_mode != 0;
   AdjRk r{};
@@ -563,7 +629,7 @@ int launch_step_vjp(const AjStepParams& p, const Layout& L, void* ws, void* aws,
   r.inv_eta = (float)(1.0 / p.brinkman_eta);
   r.sdf_fac = (float)(-1.0 / (0.1 * p.dx));
   r.cn = rk2 ? 0.5f : (float)(2.0 / 3.0);
-  k_adj_rk_out<<<grd, blk, 0, st>>>(r);
+  launch_pdl(true, k_adj_rk_out, grd, blk, 0, st, r);
   // stage states: RK3 w3 = sB, w2 = sA; RK2 w2 = sA; stage 1 is the input
   const float* Wu[3] = {u, at<float>(ws, L.sA_u), at<float>(ws, L.sB_u)};
   const float* Wv[3] = {v, at<float>(ws, L.sA_v), at<float>(ws, L.sB_v)};
@@ -587,21 +653,23 @@ int launch_step_vjp(const AjStepParams& p, const Layout& L, void* ws, void* aws,
     r.gv = gv;
     r.gsdf = (s == 1 && p.has_sdf) ? gsdf : nullptr;
     r.part = at<double>(aws, A.part) + (size_t)(nst - s) * A.nblk;
-    k_adj_rk_stage<<<grd, blk, 0, st>>>(r);
+    launch_pdl(true, k_adj_rk_stage, grd, blk, 0, st, r);
     cur = 1 - cur;
   }
   if (gscal)
-    k_adj_scalars<<<1, 256, 0, st>>>(at<double>(aws, A.part), nst * A.nblk, gu_o, F(A.gus), mask,
-                                     ny, gscal);
+    launch_pdl(true, k_adj_scalars, dim3(1), dim3(1024), 0, st, at<double>(aws, A.part),
+               nst * A.nblk, gu_o, F(A.gus), mask, ny, gscal);
   return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
 }
 
 int step_vjp_kernel_count(const AjStepParams& p, const Layout& L) {
   const int nst = p.fast_mode ? 2 : 3;
   int n = 1 + nst;                                  // dt + forward predictor stages
-  if (p.v_cycles > 1) n += 1 + 1 + p.v_cycles * (5 * L.nlev + 12);   // rhs, forward solve
+  const bool fused = parity_coarsest_fused(L);
+  if (p.v_cycles > 1)                               // rhs, forward solve
+    n += 1 + 1 + p.v_cycles * (5 * L.nlev + (fused ? 1 : 10) + 2);
   n += 2;                                           // correction, gradient
-  n += p.v_cycles * (6 * L.nlev + 10);              // reversed V-cycles
+  n += p.v_cycles * (6 * L.nlev + (fused ? 1 : 10));  // reversed V-cycles
   n += 1 + 1 + nst + 1;                             // divergence, output, stages, scalars
   return n;
 }

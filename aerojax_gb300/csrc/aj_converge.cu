@@ -68,34 +68,7 @@ static CvLvl cv_level(const AjStepParams& p, const Layout& L, int l) {
 }
 
 // ---------------------------------------------------------------- double-FP32
-struct df {
-  float hi, lo;
-};
-// Knuth's TwoSum: s + e == a + b exactly
-__device__ __forceinline__ df two_sum(float a, float b) {
-  float s = a + b;
-  float bb = s - a;
-  float e = (a - (s - bb)) + (b - bb);
-  return {s, e};
-}
-// Dekker's FastTwoSum, valid for |a| >= |b|
-__device__ __forceinline__ df quick_two_sum(float a, float b) {
-  float s = a + b;
-  return {s, b - (s - a)};
-}
-// Dekker's TwoProd with a fused multiply-add: p + e == a * b exactly
-__device__ __forceinline__ df two_prod(float a, float b) {
-  float p = a * b;
-  return {p, fmaf(a, b, -p)};
-}
-__device__ __forceinline__ df df_add(df a, df b) {
-  df s = two_sum(a.hi, b.hi);
-  df t = two_sum(a.lo, b.lo);
-  s.lo += t.hi;
-  s = quick_two_sum(s.hi, s.lo);
-  s.lo += t.lo;
-  return quick_two_sum(s.hi, s.lo);
-}
+// (df, two_sum, quick_two_sum, two_prod, df_add: aj_internal.cuh)
 __device__ __forceinline__ df df_neg(df a) { return {-a.hi, -a.lo}; }
 __device__ __forceinline__ df df_mul(df a, df b) {
   df p = two_prod(a.hi, b.hi);

@@ -113,6 +113,61 @@ __device__ __forceinline__ void block_sum_atomic(double v, double* dst) {
   __syncthreads();
 }
 
+// ------------------------------------------------------------------ double-FP32
+// an unevaluated sum hi + lo of two floats (~48-bit significand on the FP32
+// pipes; GB300 runs FP64 at 1/64 of the FP32 rate)
+struct df {
+  float hi, lo;
+};
+// Knuth's TwoSum: s + e == a + b exactly
+__device__ __forceinline__ df two_sum(float a, float b) {
+  float s = a + b;
+  float bb = s - a;
+  float e = (a - (s - bb)) + (b - bb);
+  return {s, e};
+}
+// Dekker's FastTwoSum, valid for |a| >= |b|
+__device__ __forceinline__ df quick_two_sum(float a, float b) {
+  float s = a + b;
+  return {s, b - (s - a)};
+}
+// Dekker's TwoProd with a fused multiply-add: p + e == a * b exactly
+__device__ __forceinline__ df two_prod(float a, float b) {
+  float p = a * b;
+  return {p, fmaf(a, b, -p)};
+}
+__device__ __forceinline__ df df_add(df a, df b) {
+  df s = two_sum(a.hi, b.hi);
+  df t = two_sum(a.lo, b.lo);
+  s.lo += t.hi;
+  s = quick_two_sum(s.hi, s.lo);
+  s.lo += t.lo;
+  return quick_two_sum(s.hi, s.lo);
+}
+
+// Block-wide sum of one double-FP32 value per thread, in a fixed order (the
+// result is bit-reproducible): a TwoSum butterfly inside each warp, one FP64
+// value per warp, the warps summed by thread 0, which gets the total.  Every
+// thread of the block must call it (it synchronises).
+__device__ __forceinline__ double block_sum_df(df v) {
+  __shared__ double wd_[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float h = __shfl_xor_sync(0xffffffffu, v.hi, o);
+    const float l = __shfl_xor_sync(0xffffffffu, v.lo, o);
+    v = df_add(v, df{h, l});
+  }
+  const int nthreads = blockDim.x * blockDim.y;
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  if ((tid & 31) == 0) wd_[tid >> 5] = (double)v.hi + (double)v.lo;
+  __syncthreads();
+  double t = 0.0;
+  if (tid == 0)
+    for (int k = 0; k < (nthreads >> 5); ++k) t += wd_[k];
+  __syncthreads();
+  return t;
+}
+
 // Block-wide sum of one double per thread in a fixed order (the result is
 // bit-reproducible); the total is returned to thread 0.  Every thread of the
 // block must call it (it synchronises).
@@ -171,6 +226,7 @@ int launch_les(const AjStepParams& p, const Layout& L, void* ws, int model, cons
 int launch_cfl(const AjStepParams& p, void* ws, const float* u, const float* v,
                float* dt_out, cudaStream_t st);
 int launch_set_dt(const AjStepParams& p, void* ws, cudaStream_t st);
+bool parity_coarsest_fused(const Layout& L);   // coarsest sweeps in one block (aj_pressure.cu)
 // reverse mode of the collocated step_pure (aj_adjoint.cu)
 size_t step_vjp_workspace(const AjStepParams& p, const Layout& L);
 int launch_step_vjp(const AjStepParams& p, const Layout& L, void* ws, void* aws, const float* u,

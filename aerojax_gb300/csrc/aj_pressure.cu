@@ -172,6 +172,45 @@ __global__ void k_par_check(DevScalars* sc, double dxdy, double tol2, int first)
   sc->acc[1] = 0.0;
 }
 
+// the coarsest level's 10 Jacobi sweeps from a zero guess
+// (multigrid_solver.py:186-187) in one block: the iterate ping-pongs in
+// shared memory, b is staged once.  Same arithmetic as k_par_jacobi; used
+// when three arrays of the level fit the block's shared memory.
+constexpr int kParCoarsestThreads = 1024;
+__global__ void __launch_bounds__(kParCoarsestThreads) k_par_coarsest(
+    const float* __restrict__ b, const float* __restrict__ mask, float* __restrict__ x, int n,
+    int m, float ax, float ay, float den, const int* skip) {
+  if (skip && *skip) return;
+  extern __shared__ float psm[];
+  const int nm = n * m;
+  float* P = psm;
+  float* Q = psm + nm;
+  float* Bs = psm + 2 * nm;
+  for (int c = threadIdx.x; c < nm; c += blockDim.x) Bs[c] = b[c];
+  __syncthreads();
+  for (int s = 0; s < 10; ++s) {
+    for (int c = threadIdx.x; c < nm; c += blockDim.x) {
+      const int i = c / m, j = c - i * m;
+      const int ip = i + 1 < n ? i + 1 : n - 1, im = i > 0 ? i - 1 : 0;
+      const int jp = j + 1 < m ? j + 1 : m - 1, jm = j > 0 ? j - 1 : 0;
+      auto pv = [&](int ii, int jj) -> float { return s == 0 ? 0.f : P[ii * m + jj]; };
+      float pn = (ax * (pv(ip, j) + pv(im, j)) + ay * (pv(i, jp) + pv(i, jm)) - Bs[c]) / den;
+      if (mask) pn = pn * mask[c];
+      Q[c] = pn;
+    }
+    __syncthreads();
+    float* t = P;
+    P = Q;
+    Q = t;
+  }
+  for (int c = threadIdx.x; c < nm; c += blockDim.x) x[c] = P[c];
+}
+
+// whether the coarsest level's sweeps run as one k_par_coarsest block
+bool parity_coarsest_fused(const Layout& L) {
+  return (size_t)L.ln[L.nlev] * L.lm[L.nlev] * 12 <= kBlockSmemMax;
+}
+
 __global__ void k_copy(const float* __restrict__ s, float* __restrict__ d, long n) {
   long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (k < n) d[k] = s[k];
@@ -247,7 +286,14 @@ static int parity_solve(const AjStepParams& p, const Layout& L, void* ws, const 
                                                mac && p.flow_type == AJ_FLOW_VON_KARMAN, sk);
     }
     // coarsest: 10 sweeps from zero, ending in X
-    {
+    if (parity_coarsest_fused(L)) {
+      const int n = L.ln[nl], m = L.lm[nl];
+      const size_t csm = (size_t)n * m * 12;
+      cudaFuncSetAttribute(k_par_coarsest, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)kBlockSmemMax);
+      k_par_coarsest<<<1, kParCoarsestThreads, csm, st>>>(B(nl), M(nl), X(nl), n, m, ax, ay, den,
+                                                           sk);
+    } else {
       int n = L.ln[nl], m = L.lm[nl];
       dim3 g(cdiv(m, 32), cdiv(n, 8));
       ParJac a{};

@@ -87,8 +87,10 @@ def _rhs_T(ku_bar, kv_bar, u, v, nu, dx, dy):
     # field roles (velocities fixed)
     ub += _one_sided_T(a * u, u, dx, 0) + _one_sided_T(a * v, v, dy, 1)
     vb += _one_sided_T(b * u, u, dx, 0) + _one_sided_T(b * v, v, dy, 1)
-    nu_bar = float(np.sum(ku_bar * _lap(u, dx, dy)) + np.sum(kv_bar * _lap(v, dx, dy)))
-    return ub, vb, nu_bar
+    tu, tv = ku_bar * _lap(u, dx, dy), kv_bar * _lap(v, dx, dy)
+    nu_bar = float(np.sum(tu) + np.sum(tv))
+    nu_abs = float(np.sum(np.abs(tu)) + np.sum(np.abs(tv)))   # the sum's magnitude scale
+    return ub, vb, nu_bar, nu_abs
 
 
 def _bc_T(gu, gv):
@@ -96,7 +98,7 @@ def _bc_T(gu, gv):
     (rk3_simple_new.py:262-275 and step.py:365-377, the same statements):
     u[0]=U, v[0]=0, u[-1]=u[-2], v[-1]=v[-2], u[:,0]=u[:,1], u[:,-1]=u[:,-2],
     v[:,0]=0, v[:,-1]=0, undone in reverse order.  Returns the cotangent of
-    U_inf as well."""
+    U_inf as well, and the sum of the magnitudes it adds up."""
     gu, gv = gu.copy(), gv.copy()
     gv[:, -1] = 0.0
     gv[:, 0] = 0.0
@@ -110,8 +112,9 @@ def _bc_T(gu, gv):
     gu[-1, :] = 0.0
     gv[0, :] = 0.0
     U_bar = float(np.sum(gu[0, :]))
+    U_abs = float(np.sum(np.abs(gu[0, :])))
     gu[0, :] = 0.0
-    return gu, gv, U_bar
+    return gu, gv, U_bar, U_abs
 
 
 def _bc_inlet_T(gu, gv):
@@ -126,8 +129,9 @@ def _bc_inlet_T(gu, gv):
     gu[:, 0] = 0.0
     gv[0, :] = 0.0
     U_bar = float(np.sum(gu[0, :]))
+    U_abs = float(np.sum(np.abs(gu[0, :])))
     gu[0, :] = 0.0
-    return gu, gv, U_bar
+    return gu, gv, U_bar, U_abs
 
 
 def _gx_T(g, dx):
@@ -305,8 +309,9 @@ def step_pure_vjp(u, v, dt, mask, sdf, dx, dy, nu, U_inf, gu, gv, gp=None, *, v_
     # ---- correction (step.py:259-397), reversed
     g_u = np.where(live, gu, 0.0)                               # :396-397
     g_v = np.where(live, gv, 0.0)
-    g_u, g_v, ub = _bc_T(g_u, g_v)                              # :365-377
+    g_u, g_v, ub, ua = _bc_T(g_u, g_v)                          # :365-377
     U_bar += ub
+    U_abs = ua
     g_u = np.where(live, g_u, 0.0)                              # :348-349
     g_v = np.where(live, g_v, 0.0)
     us_bar, vs_bar = g_u.copy(), g_v.copy()
@@ -322,28 +327,32 @@ def step_pure_vjp(u, v, dt, mask, sdf, dx, dy, nu, U_inf, gu, gv, gp=None, *, v_
     dub, dvb = _div_T(div_bar, dx, dy)
     us_bar += dub
     vs_bar += dvb
-    us_bar, vs_bar, ub = _bc_inlet_T(us_bar, vs_bar)
+    us_bar, vs_bar, ub, ua = _bc_inlet_T(us_bar, vs_bar)
     U_bar += ub
+    U_abs += ua
     # ---- predictor, reversed
-    us_bar, vs_bar, ub = _bc_T(us_bar, vs_bar)
+    us_bar, vs_bar, ub, ua = _bc_T(us_bar, vs_bar)
     U_bar += ub
+    U_abs += ua
     xu = np.where(live, us_bar, 0.0) / den
     xv = np.where(live, vs_bar, 0.0) / den
     den_bar = -(xu * un_pre + xv * vn_pre)
-    nu_bar = 0.0
+    nu_bar = nu_abs = 0.0
     if not fast_mode:
         (u1, v1), (u2, v2), (u3, v3) = stages
         w1u, w1v = xu.copy(), xv.copy()                         # (1/3 + 2/3) of x_n
         ku, kv = (2 / 3) * dt * xu, (2 / 3) * dt * xv
-        a, b, nb = _rhs_T(ku, kv, u3, v3, nu, dx, dy)
+        a, b, nb, na = _rhs_T(ku, kv, u3, v3, nu, dx, dy)
         nu_bar += nb
+        nu_abs += na
         xu, xv = a / den, b / den
         den_bar -= xu * u3 + xv * v3
         w1u += xu                                               # 0.75 + 0.25
         w1v += xv
         ku, kv = 0.25 * dt * xu, 0.25 * dt * xv
-        a, b, nb = _rhs_T(ku, kv, u2, v2, nu, dx, dy)
+        a, b, nb, na = _rhs_T(ku, kv, u2, v2, nu, dx, dy)
         nu_bar += nb
+        nu_abs += na
         xu, xv = a / den, b / den
         den_bar -= xu * u2 + xv * v2
         w1u += xu
@@ -353,15 +362,17 @@ def step_pure_vjp(u, v, dt, mask, sdf, dx, dy, nu, U_inf, gu, gv, gp=None, *, v_
         (u1, v1), (u2, v2) = stages
         w1u, w1v = xu.copy(), xv.copy()
         k1u, k1v = 0.5 * dt * xu, 0.5 * dt * xv
-        a, b, nb = _rhs_T(0.5 * dt * xu, 0.5 * dt * xv, u2, v2, nu, dx, dy)
+        a, b, nb, na = _rhs_T(0.5 * dt * xu, 0.5 * dt * xv, u2, v2, nu, dx, dy)
         nu_bar += nb
+        nu_abs += na
         xu, xv = a / den, b / den
         den_bar -= xu * u2 + xv * v2
         w1u += xu
         w1v += xv
         ku, kv = k1u + dt * xu, k1v + dt * xv
-    a, b, nb = _rhs_T(ku, kv, u1, v1, nu, dx, dy)
+    a, b, nb, na = _rhs_T(ku, kv, u1, v1, nu, dx, dy)
     nu_bar += nb
+    nu_abs += na
     sdf_bar = None
     if sdf is not None:
         chi_bar = den_bar * dt / brinkman_eta
@@ -371,7 +382,7 @@ def step_pure_vjp(u, v, dt, mask, sdf, dx, dy, nu, U_inf, gu, gv, gp=None, *, v_
                              fast_mode=fast_mode, brinkman_eta=brinkman_eta,
                              mg=R.MGConfig(mode="parity", v_cycles=v_cycles, levels=levels))
     return {"u": w1u + a, "v": w1v + b, "sdf": sdf_bar, "nu": nu_bar, "U_inf": U_bar,
-            "cycles": info["cycles"], "out": (un, vn, pp)}
+            "nu_abs": nu_abs, "U_inf_abs": U_abs, "cycles": info["cycles"], "out": (un, vn, pp)}
 
 
 # ------------------------------------------------------------------ rollouts
@@ -395,14 +406,15 @@ def rollout_vjp(u0, v0, dt, mask, sdf, dx, dy, nu, U_inf, num_steps, gu, gv, *, 
         u, v, _ = R.step_pure(*states[-1], dt, mask, sdf, dx, dy, nu, U_inf, v_cycles=v_cycles,
                               fast_mode=fast_mode, brinkman_eta=brinkman_eta)
         states.append((u, v))
-    acc = {"sdf": None if sdf is None else np.zeros_like(states[0][0]), "nu": 0.0, "U_inf": 0.0}
+    acc = {"sdf": None if sdf is None else np.zeros_like(states[0][0]), "nu": 0.0, "U_inf": 0.0,
+           "nu_abs": 0.0, "U_inf_abs": 0.0}
     for (u, v) in reversed(states):
         r = step_pure_vjp(u, v, dt, mask, sdf, dx, dy, nu, U_inf, gu, gv, None, v_cycles=v_cycles,
                           fast_mode=fast_mode, brinkman_eta=brinkman_eta)
         gu, gv = r["u"], r["v"]
         if sdf is not None:
             acc["sdf"] += r["sdf"]
-        acc["nu"] += r["nu"]
-        acc["U_inf"] += r["U_inf"]
+        for key in ("nu", "U_inf", "nu_abs", "U_inf_abs"):
+            acc[key] += r[key]
     acc["u"], acc["v"] = gu, gv
     return acc

@@ -39,6 +39,15 @@ def _t(a, dev):
     return torch.as_tensor(np.asarray(a, np.float32), device=dev)
 
 
+def _scalar_ok(got, ref, key, rel):
+    """d/d nu and d/d U_inf are sums of many terms that largely cancel (for
+    d/d nu on random fields |sum| can be 1e-5 of sum |terms|): the FP32
+    error is bounded against the oracle's magnitude scale of the sum, or
+    ``rel`` of the value, whichever is larger."""
+    tol = max(rel * abs(ref[key]), 1e-7 * ref[key + "_abs"])
+    return abs(got - ref[key]) <= tol
+
+
 @pytest.mark.parametrize("fast,use_sdf,cycles", [(False, True, 1), (True, True, 1),
                                                  (False, False, 1), (False, True, 3)])
 def test_step_vjp_matches_oracle(dev, fast, use_sdf, cycles):
@@ -64,8 +73,8 @@ def test_step_vjp_matches_oracle(dev, fast, use_sdf, cycles):
         assert _rel(got["sdf"].cpu(), ref["sdf"]) <= 1e-4
     else:
         assert got["sdf"] is None and ref["sdf"] is None
-    assert abs(got["nu"] - ref["nu"]) <= 1e-4 * abs(ref["nu"])
-    assert abs(got["U_inf"] - ref["U_inf"]) <= 1e-4 * max(abs(ref["U_inf"]), 1.0)
+    assert _scalar_ok(got["nu"], ref, "nu", 1e-4), (got["nu"], ref["nu"], ref["nu_abs"])
+    assert _scalar_ok(got["U_inf"], ref, "U_inf", 1e-4), (got["U_inf"], ref["U_inf"])
 
 
 def test_step_vjp_full_size(dev):
@@ -102,8 +111,8 @@ def test_step_vjp_full_size(dev):
     assert _rel(r1[0], ref["u"]) <= 1e-4
     assert _rel(r1[1], ref["v"]) <= 1e-4
     assert _rel(r1[2], ref["sdf"]) <= 1e-4
-    assert abs(r1[3][0] - ref["nu"]) <= 1e-4 * abs(ref["nu"])
-    assert abs(r1[3][1] - ref["U_inf"]) <= 1e-4 * max(abs(ref["U_inf"]), 1.0)
+    assert _scalar_ok(r1[3][0], ref, "nu", 1e-4), (r1[3][0], ref["nu"], ref["nu_abs"])
+    assert _scalar_ok(r1[3][1], ref, "U_inf", 1e-4), (r1[3][1], ref["U_inf"])
 
 
 def test_rollout_vjp_matches_oracle(dev):
@@ -127,8 +136,8 @@ def test_rollout_vjp_matches_oracle(dev):
     assert _rel(got["u"].cpu(), ref["u"]) <= 2e-4
     assert _rel(got["v"].cpu(), ref["v"]) <= 2e-4
     assert _rel(got["sdf"].cpu(), ref["sdf"]) <= 2e-4
-    assert abs(got["nu"] - ref["nu"]) <= 2e-4 * abs(ref["nu"])
-    assert abs(got["U_inf"] - ref["U_inf"]) <= 2e-4 * max(abs(ref["U_inf"]), 1.0)
+    assert _scalar_ok(got["nu"], ref, "nu", 2e-4), (got["nu"], ref["nu"], ref["nu_abs"])
+    assert _scalar_ok(got["U_inf"], ref, "U_inf", 2e-4), (got["U_inf"], ref["U_inf"])
 
 
 def test_step_vjp_rejects_uncovered_configurations(dev):
