@@ -9,7 +9,7 @@
 //   correction + interface projection + boundary rows + hard masks
 //     (solver/pure_functions/step.py:259-397)       -> k_adj_correct, k_adj_grad
 //   parity multigrid (pressure_solvers/multigrid_solver.py:173-241)
-//                                                    -> k_adj_jac/prolong/restrict
+//                                                    -> k_adj_pair/prolong/coarsest
 //   rhs = div*mask/dt (step.py:182-199)              -> k_adj_div
 //   RK3/RK2 upwind predictor with implicit Brinkman (rk3_simple_new.py:284-358)
 //                                                    -> k_adj_rk_out, k_adj_rk_stage
@@ -19,13 +19,16 @@
 //
 // Structure: the Jacobi sweep (p <- (N p - b)/d) and the edge-ghost Laplacian
 // are symmetric, so each reversed sweep is h = pbar/d, bbar -= h, pbar = N h;
-// restriction and prolongation swap into each other's transposes.  The
+// restriction and prolongation swap into each other's transposes; each
+// level's two reversed pre- or post-sweeps run as one tiled kernel.  The
 // boundary rows are gathers (each output cell copies one source cell), so
 // their transposes are gathers at the source.  The two boundary passes of the
 // predictor (rk3_simple_new.py:262-275, then step.py:182-191) compose to the
 // first, so one transpose covers both.  Forward stage states are recomputed
 // by the forward predictor kernels (stage buffers of the step workspace).
 #include "aj_internal.cuh"
+
+#include <mutex>
 
 namespace aj {
 
@@ -222,6 +225,69 @@ __global__ void __launch_bounds__(256) k_adj_jac(const float* __restrict__ gin,
   }
 }
 
+// Two consecutive reversed sweeps of one level in one kernel (the forward's
+// two pre- or two post-smoothing sweeps, multigrid_solver.py:182-201):
+//   [down side only] x = gin - A s, gb += s, s = R^T(coarse b cotangent)
+//   h1 = (x with the outlet row zeroed)/d,  gb -= h1,  t = N h1
+//   h2 = t/d,                               gb -= h2,  gout = N h2
+// on an 8 x 32 output tile: h1 is staged on the tile and a halo of 2, h2 on a
+// halo of 1.  gb is read and written only at the block's own cells; gout
+// must not alias gin (neighbouring blocks read gin's halo).
+constexpr int kPairBX = 32, kPairBY = 8, kPairH = 2;
+constexpr int kPairRI = kPairBY + 2 * kPairH, kPairRJ = kPairBX + 2 * kPairH;
+__global__ void __launch_bounds__(kPairBX * kPairBY) k_adj_pair(
+    const float* __restrict__ gin, float* __restrict__ gout, float* __restrict__ gb,
+    const float* __restrict__ gbc, int n, int m, float ax, float ay, float d, int assign,
+    const int* ncyc, int cyc) {
+  pdl_wait();
+  if (ncyc && cyc >= *ncyc) return;
+  __shared__ float H1[kPairRI][kPairRJ];
+  __shared__ float H2[kPairRI][kPairRJ];
+  const int i0 = blockIdx.y * kPairBY - kPairH, j0 = blockIdx.x * kPairBX - kPairH;
+  const int tid = threadIdx.y * kPairBX + threadIdx.x;
+  const int mc = m / 2;
+  auto sres = [&](int gi, int gj) { return 0.25f * ldg(gbc + (long)(gi >> 1) * mc + (gj >> 1)); };
+  for (int q = tid; q < kPairRI * kPairRJ; q += kPairBX * kPairBY) {
+    const int r = q / kPairRJ, c = q - r * kPairRJ;
+    const int gi = i0 + r, gj = j0 + c;
+    float h = 0.f;
+    if (gi >= 0 && gi < n && gj >= 0 && gj < m) {
+      float x = ldg(gin + (long)gi * m + gj);
+      if (gbc) {
+        const int ip = gi + 1 < n ? gi + 1 : n - 1, im = gi > 0 ? gi - 1 : 0;
+        const int jp = gj + 1 < m ? gj + 1 : m - 1, jm = gj > 0 ? gj - 1 : 0;
+        const float sc = sres(gi, gj);
+        x -= ax * (sres(ip, gj) + sres(im, gj) - 2.f * sc) + ay * (sres(gi, jp) + sres(gi, jm) - 2.f * sc);
+      }
+      h = gi == n - 1 ? 0.f : x / d;
+    }
+    H1[r][c] = h;
+  }
+  __syncthreads();
+  // neighbours with edge ghosts, in tile coordinates (a domain edge maps to the cell itself)
+  auto nsum = [&](float (*S)[kPairRJ], int r, int c, int gi, int gj) {
+    const int rp = gi + 1 < n ? r + 1 : r, rm = gi > 0 ? r - 1 : r;
+    const int cp = gj + 1 < m ? c + 1 : c, cm = gj > 0 ? c - 1 : c;
+    return ax * (S[rp][c] + S[rm][c]) + ay * (S[r][cp] + S[r][cm]);
+  };
+  for (int q = tid; q < (kPairRI - 2) * (kPairRJ - 2); q += kPairBX * kPairBY) {
+    const int r = q / (kPairRJ - 2) + 1, c = q % (kPairRJ - 2) + 1;
+    const int gi = i0 + r, gj = j0 + c;
+    float h = 0.f;
+    if (gi >= 0 && gi < n && gj >= 0 && gj < m) h = nsum(H1, r, c, gi, gj) / d;
+    H2[r][c] = h;
+  }
+  __syncthreads();
+  const int r = threadIdx.y + kPairH, c = threadIdx.x + kPairH;
+  const int gi = i0 + r, gj = j0 + c;
+  if (gi >= n || gj >= m) return;
+  const long k = (long)gi * m + gj;
+  float acc = assign ? 0.f : gb[k];
+  if (gbc) acc += sres(gi, gj);
+  gb[k] = acc - H1[r][c] - H2[r][c];
+  if (gout) gout[k] = nsum(H2, r, c, gi, gj);
+}
+
 // the ten reversed coarsest-grid sweeps (the forward smooths 10 times from a
 // zero guess, multigrid_solver.py:186-187) in one block: the cotangent
 // ping-pongs in shared memory, b's cotangent accumulates in a third array.
@@ -286,28 +352,6 @@ __global__ void __launch_bounds__(256) k_adj_prolong(const float* __restrict__ g
   if (iu && jd) q += F(2 * I + 1, 2 * J - 1);
   if (id && jd) q += F(2 * I - 1, 2 * J - 1);
   gc[(long)I * mc + J] = r + 0.5f * s + 0.25f * q;
-}
-
-// transpose of rc = R(b - A p): s = R^T rc_bar (a quarter to each child);
-// gb += s, gx -= A s (A symmetric with edge ghosts)
-__global__ void __launch_bounds__(256) k_adj_restrict(const float* __restrict__ gbc,
-                                                      float* __restrict__ gb,
-                                                      float* __restrict__ gx, int n, int m,
-                                                      float ax, float ay, const int* ncyc,
-                                                      int cyc) {
-  pdl_wait();
-  if (ncyc && cyc >= *ncyc) return;
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= n || j >= m) return;
-  const int mc = m / 2;
-  auto s = [&](int ii, int jj) { return 0.25f * ldg(gbc + (long)(ii >> 1) * mc + (jj >> 1)); };
-  const int ip = i + 1 < n ? i + 1 : n - 1, im = i > 0 ? i - 1 : 0;
-  const int jp = j + 1 < m ? j + 1 : m - 1, jm = j > 0 ? j - 1 : 0;
-  const float sc = s(i, j);
-  const long k = (long)i * m + j;
-  gb[k] += sc;
-  gx[k] -= ax * (s(ip, j) + s(im, j) - 2.f * sc) + ay * (s(i, jp) + s(i, jm) - 2.f * sc);
 }
 
 // ------------------------------------------------------------------ rhs
@@ -512,6 +556,30 @@ size_t step_vjp_workspace(const AjStepParams& p, const Layout& L) {
   return A.total;
 }
 
+// The side branch that recomputes the forward predictor beside the reverse
+// pass of the correction and the multigrid (created once; its use is
+// serialised: a capture into a caller's graph does not hold the library's
+// graph-cache lock).
+namespace {
+std::mutex g_vjp_mu;
+struct VjpFork {
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+};
+const VjpFork* vjp_fork() {
+  static VjpFork f;
+  static bool ok = false;
+  if (!ok) {
+    if (cudaStreamCreateWithFlags(&f.side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&f.fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&f.join, cudaEventDisableTiming) != cudaSuccess)
+      return nullptr;
+    ok = true;
+  }
+  return &f;
+}
+}  // namespace
+
 int launch_step_vjp(const AjStepParams& p, const Layout& L, void* ws, void* aws, const float* u,
                     const float* v, const float* mask, const float* gu_o, const float* gv_o,
                     const float* gp_o, float* gu, float* gv, float* gsdf, double* gscal,
@@ -524,10 +592,24 @@ int launch_step_vjp(const AjStepParams& p, const Layout& L, void* ws, void* aws,
   auto F = [&](size_t off) { return at<float>(aws, off); };
   const dim3 blk(kAdjBX, kAdjBY), grd(cdiv(ny, kAdjBX), cdiv(nx, kAdjBY));
   int rc;
-  // ---- forward: dt and the predictor's stage states
+  std::lock_guard<std::mutex> lk(g_vjp_mu);
+  const VjpFork* fk = vjp_fork();
+  if (!fk) return AJ_ERR_CUDA;
+  // ---- forward: dt, then the predictor's stage states.  With one V-cycle
+  // nothing before the predictor's reverse pass reads them: the predictor
+  // runs on a side branch joined before k_adj_rk_out.  With more cycles the
+  // forward solve counts the cycles the reverse pass replays, in line.
   if ((rc = launch_set_dt(p, ws, st)) != AJ_OK) return rc;
-  if ((rc = launch_predictor(p, L, ws, u, v, mask, nullptr, 0, F(A.wnu), F(A.wnv), st)) != AJ_OK)
-    return rc;
+  const bool branch = p.v_cycles == 1;
+  if (branch) {
+    if (cudaEventRecord(fk->fork, st) != cudaSuccess ||
+        cudaStreamWaitEvent(fk->side, fk->fork, 0) != cudaSuccess)
+      return AJ_ERR_CUDA;
+  }
+  rc = launch_predictor(p, L, ws, u, v, mask, nullptr, 0, F(A.wnu), F(A.wnv),
+                        branch ? fk->side : st);
+  if (rc != AJ_OK) return rc;
+  if (branch && cudaEventRecord(fk->join, fk->side) != cudaSuccess) return AJ_ERR_CUDA;
   const int* ncyc = nullptr;
   if (p.v_cycles > 1) {
     // the V-cycles the forward ran (the reference skips cycles once converged)
@@ -569,12 +651,19 @@ int launch_step_vjp(const AjStepParams& p, const Layout& L, void* ws, void* aws,
     launch_pdl(true, k_adj_jac, lg(l), blk, 0, st, gin, gout, F(A.GB[l]), L.ln[l], L.lm[l], ax,
                ay, den, zero_last, assign, nc, cyc);
   };
+  auto pair = [&](int l, const float* gin, float* gout, const float* gbc, int assign,
+                  const int* nc, int cyc) {
+    launch_pdl(true, k_adj_pair, dim3(cdiv(L.lm[l], kPairBX), cdiv(L.ln[l], kPairBY)),
+               dim3(kPairBX, kPairBY), 0, st, gin, gout, F(A.GB[l]), gbc, L.ln[l], L.lm[l], ax, ay,
+               den, assign, nc, cyc);
+  };
   for (int cyc = p.v_cycles - 1; cyc >= 0; --cyc) {
     const int* nc = cyc == 0 ? nullptr : ncyc;                 // cycle 0 always ran
-    for (int l = 0; l < nl; ++l) {                             // up-sweep, reversed
-      jac(l, F(A.GX[l]), F(A.GT[l]), 1, l > 0, nc, cyc);
-      jac(l, F(A.GT[l]), F(A.GX[l]), 0, 0, nc, cyc);
-      launch_pdl(true, k_adj_prolong, lg(l + 1), blk, 0, st, F(A.GX[l]), F(A.GX[l + 1]),
+    // up-sweep, reversed: the two post-sweeps (GX -> GT), then the
+    // prolongation's transpose onto the coarser level's GX
+    for (int l = 0; l < nl; ++l) {
+      pair(l, F(A.GX[l]), F(A.GT[l]), nullptr, l > 0, nc, cyc);
+      launch_pdl(true, k_adj_prolong, lg(l + 1), blk, 0, st, F(A.GT[l]), F(A.GX[l + 1]),
                  L.ln[l + 1], L.lm[l + 1], nc, cyc);
     }
     if (parity_coarsest_fused(L)) {                            // coarsest: 10 sweeps from zero
@@ -590,13 +679,11 @@ int launch_step_vjp(const AjStepParams& p, const Layout& L, void* ws, void* aws,
         jac(nl, gin, gout, 0, s == 9, nc, cyc);
       }
     }
-    for (int l = nl - 1; l >= 0; --l) {                        // down-sweep, reversed
-      launch_pdl(true, k_adj_restrict, lg(l), blk, 0, st, F(A.GB[l + 1]), F(A.GB[l]), F(A.GX[l]),
-                 L.ln[l], L.lm[l], ax, ay, nc, cyc);
-      jac(l, F(A.GX[l]), F(A.GT[l]), 1, 0, nc, cyc);
-      // the first pre-sweep's input: zero below level 0 and in the first cycle
-      jac(l, F(A.GT[l]), (l == 0 && cyc > 0) ? F(A.GX[0]) : nullptr, 0, 0, nc, cyc);
-    }
+    // down-sweep, reversed: the restriction's transpose and the two
+    // pre-sweeps on GT; the first pre-sweep's input is zero below level 0
+    // and in the first cycle, else its cotangent goes to GX[0]
+    for (int l = nl - 1; l >= 0; --l)
+      pair(l, F(A.GT[l]), (l == 0 && cyc > 0) ? F(A.GX[0]) : nullptr, F(A.GB[l + 1]), 0, nc, cyc);
   }
   // ---- rhs and divergence, reversed
   launch_pdl(true, k_adj_div, grd, blk, 0, st, F(A.GB[0]), mask, F(A.gus), F(A.gvs), sc, nx, ny,
@@ -629,6 +716,7 @@ int launch_step_vjp(const AjStepParams& p, const Layout& L, void* ws, void* aws,
   r.inv_eta = (float)(1.0 / p.brinkman_eta);
   r.sdf_fac = (float)(-1.0 / (0.1 * p.dx));
   r.cn = rk2 ? 0.5f : (float)(2.0 / 3.0);
+  if (branch && cudaStreamWaitEvent(st, fk->join, 0) != cudaSuccess) return AJ_ERR_CUDA;
   launch_pdl(true, k_adj_rk_out, grd, blk, 0, st, r);
   // stage states: RK3 w3 = sB, w2 = sA; RK2 w2 = sA; stage 1 is the input
   const float* Wu[3] = {u, at<float>(ws, L.sA_u), at<float>(ws, L.sB_u)};
@@ -669,7 +757,7 @@ int step_vjp_kernel_count(const AjStepParams& p, const Layout& L) {
   if (p.v_cycles > 1)                               // rhs, forward solve
     n += 1 + 1 + p.v_cycles * (5 * L.nlev + (fused ? 1 : 10) + 2);
   n += 2;                                           // correction, gradient
-  n += p.v_cycles * (6 * L.nlev + (fused ? 1 : 10));  // reversed V-cycles
+  n += p.v_cycles * (3 * L.nlev + (fused ? 1 : 10));  // reversed V-cycles
   n += 1 + 1 + nst + 1;                             // divergence, output, stages, scalars
   return n;
 }

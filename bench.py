@@ -596,14 +596,14 @@ def side_workload(args):
 #     the stage state, u, v, chi, write 2                              20+28+28
 #   correction: reads gu, gv, mask, writes gu*, gv*, gdpx, gdpy            28
 #   gradient transpose: reads gdpx, gdpy, gp, writes pbar                  16
-#   level-0 multigrid: 4 reversed sweeps (read 1, update b 2, write 1),
-#     restriction transpose (update b and x: 4), prolongation read 1       88
-#   levels 1-4 of the V-cycle: a third of level 0 (1/4 + 1/16 + ...)      29
+#   level-0 multigrid: two sweep pairs (read 1, update b 2, write 1; the
+#     down pair also reads the coarse b: 1/4), prolongation read 1 + 1/4  38
+#   levels 1-4 of the V-cycle: a third of level 0 (1/4 + 1/16 + ...)      13
 #   divergence transpose: reads b, mask, updates gu*, gv*                  24
 #   output stage: reads gu*, gv*, mask, chi, u*, v*, writes 5 fields       44
 #   three reversed stages: read slope 2, state 2, chi, update w1 2 and
 #     den 1, write slope 2 (the last writes gu, gv, updates gsdf)   52+52+52
-VJP_BYTES_PER_CELL = 20 + 28 + 28 + 28 + 16 + 88 + 29 + 24 + 44 + 3 * 52
+VJP_BYTES_PER_CELL = 20 + 28 + 28 + 28 + 16 + 38 + 13 + 24 + 44 + 3 * 52
 
 
 def adjoint_workload(args, dev, st):
