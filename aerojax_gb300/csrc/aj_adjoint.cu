@@ -292,7 +292,7 @@ __global__ void __launch_bounds__(kPairBX * kPairBY) k_adj_pair(
 // zero guess, multigrid_solver.py:186-187) in one block: the cotangent
 // ping-pongs in shared memory, b's cotangent accumulates in a third array.
 // Used when 3 arrays of the level fit the block's shared memory.
-constexpr int kCoarsestThreads = 1024;
+constexpr int kCoarsestThreads = 1024;   // 32 x 32: column lanes x row strides
 __global__ void __launch_bounds__(kCoarsestThreads) k_adj_coarsest(const float* __restrict__ gin,
                                                                    float* __restrict__ gb, int n,
                                                                    int m, float ax, float ay,
@@ -305,18 +305,23 @@ __global__ void __launch_bounds__(kCoarsestThreads) k_adj_coarsest(const float* 
   float* A = csm;
   float* B = csm + nm;
   float* G = csm + 2 * nm;
-  for (int c = threadIdx.x; c < nm; c += blockDim.x) A[c] = gin[c];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  // A holds h = cotangent/d (one division per cell per sweep); B the next
+  for (int i = ty; i < n; i += 32)
+    for (int j = tx; j < m; j += 32) {
+      const float hc = gin[(long)i * m + j] / d;
+      A[i * m + j] = hc;
+      G[i * m + j] = -hc;
+    }
   __syncthreads();
-  for (int s = 9; s >= 0; --s) {
-    for (int c = threadIdx.x; c < nm; c += blockDim.x) {
-      const int i = c / m, j = c - i * m;
-      const float hc = A[c] / d;
-      G[c] = s == 9 ? -hc : G[c] - hc;
-      if (s > 0) {
-        const int ip = i + 1 < n ? i + 1 : n - 1, im = i > 0 ? i - 1 : 0;
+  for (int s = 9; s >= 1; --s) {
+    for (int i = ty; i < n; i += 32) {
+      const int rp = (i + 1 < n ? i + 1 : n - 1) * m, rm = (i > 0 ? i - 1 : 0) * m, rc = i * m;
+      for (int j = tx; j < m; j += 32) {
         const int jp = j + 1 < m ? j + 1 : m - 1, jm = j > 0 ? j - 1 : 0;
-        B[c] = ax * (A[ip * m + j] / d + A[im * m + j] / d) +
-               ay * (A[i * m + jp] / d + A[i * m + jm] / d);
+        const float hn = (ax * (A[rp + j] + A[rm + j]) + ay * (A[rc + jp] + A[rc + jm])) / d;
+        B[rc + j] = hn;
+        G[rc + j] = G[rc + j] - hn;
       }
     }
     __syncthreads();
@@ -324,7 +329,8 @@ __global__ void __launch_bounds__(kCoarsestThreads) k_adj_coarsest(const float* 
     A = B;
     B = t;
   }
-  for (int c = threadIdx.x; c < nm; c += blockDim.x) gb[c] = G[c];
+  for (int i = ty; i < n; i += 32)
+    for (int j = tx; j < m; j += 32) gb[(long)i * m + j] = G[i * m + j];
 }
 
 // transpose of the reference prolongation (multigrid_solver.py:134-156) onto
@@ -755,7 +761,7 @@ int step_vjp_kernel_count(const AjStepParams& p, const Layout& L) {
   int n = 1 + nst;                                  // dt + forward predictor stages
   const bool fused = parity_coarsest_fused(L);
   if (p.v_cycles > 1)                               // rhs, forward solve
-    n += 1 + 1 + p.v_cycles * (5 * L.nlev + (fused ? 1 : 10) + 2);
+    n += 1 + 1 + p.v_cycles * (2 * L.nlev + (fused ? 1 : 10) + 1);
   n += 2;                                           // correction, gradient
   n += p.v_cycles * (3 * L.nlev + (fused ? 1 : 10));  // reversed V-cycles
   n += 1 + 1 + nst + 1;                             // divergence, output, stages, scalars

@@ -63,25 +63,23 @@ __device__ __forceinline__ float prolong_ref(const float* __restrict__ c, int nc
 
 struct ParJac {
   const float* pin;    // null = zero guess
-  const float* ec;     // coarse correction to add on the fly (null = none)
   const float* b;
   const float* mask;   // MAC: p_new *= mask
   float* pout;
   const int* skip;
-  int n, m, nc, mc, zero_last;
+  int n, m, zero_last;
   float ax, ay, den;
 };
 
-// one undamped Jacobi sweep with edge ghosts (multigrid_solver.py:158-171)
+// one undamped Jacobi sweep with edge ghosts (multigrid_solver.py:158-171):
+// the coarsest level's sweeps when they do not fit one block
 __global__ void __launch_bounds__(256) k_par_jacobi(ParJac a) {
   if (a.skip && *a.skip) return;
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= a.n || j >= a.m) return;
   auto pv = [&](int ii, int jj) -> float {
-    float v = a.pin ? ldg(a.pin + (long)ii * a.m + jj) : 0.f;
-    if (a.ec) v = v + prolong_ref(a.ec, a.nc, a.mc, ii, jj);
-    return v;
+    return a.pin ? ldg(a.pin + (long)ii * a.m + jj) : 0.f;
   };
   int ip = i + 1 < a.n ? i + 1 : a.n - 1, im = i > 0 ? i - 1 : 0;
   int jp = j + 1 < a.m ? j + 1 : a.m - 1, jm = j > 0 ? j - 1 : 0;
@@ -90,64 +88,6 @@ __global__ void __launch_bounds__(256) k_par_jacobi(ParJac a) {
   if (a.mask) pn = pn * ldg(a.mask + k);
   if (a.zero_last && i == a.n - 1) pn = 0.f;
   a.pout[k] = pn;
-}
-
-// residual r = b - A p (edge ghosts; MAC zeroes the outlet row of A p) and its
-// unscaled 2x2 average onto the coarse grid (multigrid_solver.py:108-132, 173-201)
-__global__ void __launch_bounds__(256) k_par_resid_restrict(const float* __restrict__ p,
-                                                            const float* __restrict__ b,
-                                                            float* __restrict__ rc, int n, int m,
-                                                            float ax, float ay, int mac_outlet,
-                                                            const int* skip) {
-  if (skip && *skip) return;
-  int J = blockIdx.x * blockDim.x + threadIdx.x;
-  int I = blockIdx.y * blockDim.y + threadIdx.y;
-  int nc = n / 2, mc = m / 2;
-  if (I >= nc || J >= mc) return;
-  float r[4];
-#pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    int i = 2 * I + (q & 1), j = 2 * J + (q >> 1);   // order: (0,0),(1,0),(0,1),(1,1)
-    long k = (long)i * m + j;
-    float c = ldg(p + k);
-    float xp = ldg(p + (long)(i + 1 < n ? i + 1 : n - 1) * m + j);
-    float xm = ldg(p + (long)(i > 0 ? i - 1 : 0) * m + j);
-    float yp = ldg(p + (long)i * m + (j + 1 < m ? j + 1 : m - 1));
-    float ym = ldg(p + (long)i * m + (j > 0 ? j - 1 : 0));
-    float lap = ax * (xp + xm - 2.f * c) + ay * (yp + ym - 2.f * c);
-    if (mac_outlet && i == n - 1) lap = 0.f;
-    r[q] = ldg(b + k) - lap;
-  }
-  rc[(long)I * mc + J] = 0.25f * (r[0] + r[1] + r[2] + r[3]);
-}
-
-// sum over the fine grid of (b - A p)^2 in FP64 (multigrid_solver.py:229-231)
-__global__ void __launch_bounds__(256) k_par_norm(const float* __restrict__ p,
-                                                  const float* __restrict__ b, int n, int m,
-                                                  float ax, float ay, int mac_outlet,
-                                                  DevScalars* sc, int also_b) {
-  if (sc->mg_skip) return;
-  double acc = 0.0, accb = 0.0;
-  long N = (long)n * m;
-  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < N; k += (long)gridDim.x * blockDim.x) {
-    int i = (int)(k / m), j = (int)(k - (long)i * m);
-    float c = ldg(p + k);
-    float xp = ldg(p + (long)(i + 1 < n ? i + 1 : n - 1) * m + j);
-    float xm = ldg(p + (long)(i > 0 ? i - 1 : 0) * m + j);
-    float yp = ldg(p + (long)i * m + (j + 1 < m ? j + 1 : m - 1));
-    float ym = ldg(p + (long)i * m + (j > 0 ? j - 1 : 0));
-    float lap = ax * (xp + xm - 2.f * c) + ay * (yp + ym - 2.f * c);
-    if (mac_outlet && i == n - 1) lap = 0.f;
-    float bb = ldg(b + k);
-    double r = (double)bb - (double)lap;
-    acc += r * r;
-    accb += (double)bb * (double)bb;
-  }
-  block_sum_atomic(acc, &sc->acc[0]);
-  if (also_b) {
-    __syncthreads();
-    block_sum_atomic(accb, &sc->acc[1]);
-  }
 }
 
 __global__ void k_par_begin(DevScalars* sc) {
@@ -176,7 +116,7 @@ __global__ void k_par_check(DevScalars* sc, double dxdy, double tol2, int first)
 // (multigrid_solver.py:186-187) in one block: the iterate ping-pongs in
 // shared memory, b is staged once.  Same arithmetic as k_par_jacobi; used
 // when three arrays of the level fit the block's shared memory.
-constexpr int kParCoarsestThreads = 1024;
+constexpr int kParCoarsestThreads = 1024;   // 32 x 32: column lanes x row strides
 __global__ void __launch_bounds__(kParCoarsestThreads) k_par_coarsest(
     const float* __restrict__ b, const float* __restrict__ mask, float* __restrict__ x, int n,
     int m, float ax, float ay, float den, const int* skip) {
@@ -186,30 +126,205 @@ __global__ void __launch_bounds__(kParCoarsestThreads) k_par_coarsest(
   float* P = psm;
   float* Q = psm + nm;
   float* Bs = psm + 2 * nm;
-  for (int c = threadIdx.x; c < nm; c += blockDim.x) Bs[c] = b[c];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int i = ty; i < n; i += 32)
+    for (int j = tx; j < m; j += 32) Bs[i * m + j] = b[(long)i * m + j];
   __syncthreads();
   for (int s = 0; s < 10; ++s) {
-    for (int c = threadIdx.x; c < nm; c += blockDim.x) {
-      const int i = c / m, j = c - i * m;
-      const int ip = i + 1 < n ? i + 1 : n - 1, im = i > 0 ? i - 1 : 0;
-      const int jp = j + 1 < m ? j + 1 : m - 1, jm = j > 0 ? j - 1 : 0;
-      auto pv = [&](int ii, int jj) -> float { return s == 0 ? 0.f : P[ii * m + jj]; };
-      float pn = (ax * (pv(ip, j) + pv(im, j)) + ay * (pv(i, jp) + pv(i, jm)) - Bs[c]) / den;
-      if (mask) pn = pn * mask[c];
-      Q[c] = pn;
+    for (int i = ty; i < n; i += 32) {
+      const int rp = (i + 1 < n ? i + 1 : n - 1) * m, rm = (i > 0 ? i - 1 : 0) * m, rc = i * m;
+      for (int j = tx; j < m; j += 32) {
+        const int jp = j + 1 < m ? j + 1 : m - 1, jm = j > 0 ? j - 1 : 0;
+        const float xp = s ? P[rp + j] : 0.f, xm = s ? P[rm + j] : 0.f;
+        const float yp = s ? P[rc + jp] : 0.f, ym = s ? P[rc + jm] : 0.f;
+        float pn = (ax * (xp + xm) + ay * (yp + ym) - Bs[rc + j]) / den;
+        if (mask) pn = pn * mask[rc + j];
+        Q[rc + j] = pn;
+      }
     }
     __syncthreads();
     float* t = P;
     P = Q;
     Q = t;
   }
-  for (int c = threadIdx.x; c < nm; c += blockDim.x) x[c] = P[c];
+  for (int i = ty; i < n; i += 32)
+    for (int j = tx; j < m; j += 32) x[(long)i * m + j] = P[i * m + j];
 }
 
 // whether the coarsest level's sweeps run as one k_par_coarsest block
 bool parity_coarsest_fused(const Layout& L) {
   return (size_t)L.ln[L.nlev] * L.lm[L.nlev] * 12 <= kBlockSmemMax;
 }
+
+// ---- one level of the V-cycle per launch, on tiles
+// (multigrid_solver.py:173-211).  A tile stages what its output needs with
+// halos in shared memory; edge ghosts map to the cell itself; cells outside
+// the domain are never read by cells inside it.  Each block writes only its
+// own cells, and no output aliases an input another block reads.
+struct ParTile {
+  const float* xin;   // down: the cycle's input state (null: zero); up: the level's down result
+  const float* xc;    // up: the coarser level's result (prolonged on the fly)
+  const float* b;
+  const float* mask;  // MAC level mask (null: collocated)
+  float* xout;        // down: the state after the two pre-sweeps; up: after the post-sweeps
+  float* bc;          // down: the restricted residual (the coarser level's b)
+  DevScalars* sc;     // up on level 0: the residual norm (multigrid_solver.py:229-231)
+  const int* skip;
+  int n, m, nc, mc, zero_last, mac_outlet, also_b;
+  float ax, ay, den;
+};
+// Output tiles: 16 x 64 on the finest level (4 cells per thread: fewer halo
+// cells per output, more loads in flight), 8 x 32 on the coarser ones (their
+// grids have few blocks, and a block's dependent phases set the time).
+constexpr int kPtThreads = 256;
+
+// Jacobi value at tile cell (r, c) from the staged iterate S (same arithmetic
+// as k_par_jacobi); (gi, gj) its global index
+template <int RJ>
+__device__ __forceinline__ float tile_jacobi(float (*S)[RJ], int r, int c, int gi, int gj,
+                                             const ParTile& a) {
+  const int rp = gi + 1 < a.n ? r + 1 : r, rm = gi > 0 ? r - 1 : r;
+  const int cp = gj + 1 < a.m ? c + 1 : c, cm = gj > 0 ? c - 1 : c;
+  const long k = (long)gi * a.m + gj;
+  float pn = (a.ax * (S[rp][c] + S[rm][c]) + a.ay * (S[r][cp] + S[r][cm]) - ldg(a.b + k)) / a.den;
+  if (a.mask) pn = pn * ldg(a.mask + k);
+  return pn;
+}
+
+// b - A x at tile cell (r, c) of the staged x (the MAC variant zeroes A x on
+// the outlet row)
+template <int RJ>
+__device__ __forceinline__ float tile_resid(float (*S)[RJ], int r, int c, int gi, int gj,
+                                            const ParTile& a) {
+  const int rp = gi + 1 < a.n ? r + 1 : r, rm = gi > 0 ? r - 1 : r;
+  const int cp = gj + 1 < a.m ? c + 1 : c, cm = gj > 0 ? c - 1 : c;
+  const float x = S[r][c];
+  float lap = a.ax * (S[rp][c] + S[rm][c] - 2.f * x) + a.ay * (S[r][cp] + S[r][cm] - 2.f * x);
+  if (a.mac_outlet && gi == a.n - 1) lap = 0.f;
+  return ldg(a.b + (long)gi * a.m + gj) - lap;
+}
+
+// down: two pre-sweeps (the second resets the outlet row), the residual and
+// its 2x2 average onto the coarser level (multigrid_solver.py:182-201)
+template <int kPtBY, int kPtBX>
+__global__ void __launch_bounds__(kPtThreads) k_par_down(ParTile a) {
+  if (a.skip && *a.skip) return;
+  __shared__ float X0[kPtBY + 6][kPtBX + 6];   // input, halo 3
+  __shared__ float X1[kPtBY + 4][kPtBX + 4];   // first sweep, halo 2
+  __shared__ float X2[kPtBY + 2][kPtBX + 2];   // second sweep, halo 1
+  __shared__ float R[kPtBY][kPtBX];            // residual
+  const int ti0 = blockIdx.y * kPtBY, tj0 = blockIdx.x * kPtBX;
+  const int tid = threadIdx.x, nt = kPtThreads;
+  auto inside = [&](int gi, int gj) { return gi >= 0 && gi < a.n && gj >= 0 && gj < a.m; };
+  for (int q = tid; q < (kPtBY + 6) * (kPtBX + 6); q += nt) {
+    const int r = q / (kPtBX + 6), c = q - r * (kPtBX + 6);
+    const int gi = ti0 - 3 + r, gj = tj0 - 3 + c;
+    X0[r][c] = (a.xin && inside(gi, gj)) ? ldg(a.xin + (long)gi * a.m + gj) : 0.f;
+  }
+  __syncthreads();
+  for (int q = tid; q < (kPtBY + 4) * (kPtBX + 4); q += nt) {
+    const int r = q / (kPtBX + 4), c = q - r * (kPtBX + 4);
+    const int gi = ti0 - 2 + r, gj = tj0 - 2 + c;
+    X1[r][c] = inside(gi, gj) ? tile_jacobi<kPtBX + 6>(X0, r + 1, c + 1, gi, gj, a) : 0.f;
+  }
+  __syncthreads();
+  for (int q = tid; q < (kPtBY + 2) * (kPtBX + 2); q += nt) {
+    const int r = q / (kPtBX + 2), c = q - r * (kPtBX + 2);
+    const int gi = ti0 - 1 + r, gj = tj0 - 1 + c;
+    float x = 0.f;
+    if (inside(gi, gj))
+      x = (a.zero_last && gi == a.n - 1) ? 0.f : tile_jacobi<kPtBX + 4>(X1, r + 1, c + 1, gi, gj, a);
+    X2[r][c] = x;
+  }
+  __syncthreads();
+  for (int q = tid; q < kPtBY * kPtBX; q += nt) {
+    const int r = q / kPtBX, c = q - r * kPtBX;
+    const int gi = ti0 + r, gj = tj0 + c;
+    float res = 0.f;
+    if (inside(gi, gj)) {
+      a.xout[(long)gi * a.m + gj] = X2[r + 1][c + 1];
+      res = tile_resid<kPtBX + 2>(X2, r + 1, c + 1, gi, gj, a);
+    }
+    R[r][c] = res;
+  }
+  __syncthreads();
+  for (int q = tid; q < (kPtBY / 2) * (kPtBX / 2); q += nt) {
+    const int I = q / (kPtBX / 2), J = q - I * (kPtBX / 2);
+    const int gI = ti0 / 2 + I, gJ = tj0 / 2 + J;
+    if (gI < a.nc && gJ < a.mc)   // summed in the order (0,0), (1,0), (0,1), (1,1)
+      a.bc[(long)gI * a.mc + gJ] =
+          0.25f * (R[2 * I][2 * J] + R[2 * I + 1][2 * J] + R[2 * I][2 * J + 1] + R[2 * I + 1][2 * J + 1]);
+  }
+}
+
+// up: p + P(e) and two post-sweeps (the second resets the outlet row,
+// multigrid_solver.py:203-211); with NORM (level 0) also sum (b - A p)^2 and,
+// on the first cycle, b^2 (double-FP32 per block, FP64 across blocks)
+template <int kPtBY, int kPtBX, bool NORM>
+__global__ void __launch_bounds__(kPtThreads) k_par_up(ParTile a) {
+  if (a.skip && *a.skip) return;
+  constexpr int H = NORM ? 3 : 2;                       // halo of the corrected iterate
+  __shared__ float Y[kPtBY + 2 * H][kPtBX + 2 * H];
+  __shared__ float X1[kPtBY + 2 * H - 2][kPtBX + 2 * H - 2];
+  __shared__ float X2[NORM ? kPtBY + 2 : 1][NORM ? kPtBX + 2 : 1];
+  const int ti0 = blockIdx.y * kPtBY, tj0 = blockIdx.x * kPtBX;
+  const int tid = threadIdx.x, nt = kPtThreads;
+  auto inside = [&](int gi, int gj) { return gi >= 0 && gi < a.n && gj >= 0 && gj < a.m; };
+  for (int q = tid; q < (kPtBY + 2 * H) * (kPtBX + 2 * H); q += nt) {
+    const int r = q / (kPtBX + 2 * H), c = q - r * (kPtBX + 2 * H);
+    const int gi = ti0 - H + r, gj = tj0 - H + c;
+    float y = 0.f;
+    if (inside(gi, gj)) {
+      y = ldg(a.xin + (long)gi * a.m + gj);
+      y = y + prolong_ref(a.xc, a.nc, a.mc, gi, gj);
+    }
+    Y[r][c] = y;
+  }
+  __syncthreads();
+  for (int q = tid; q < (kPtBY + 2 * H - 2) * (kPtBX + 2 * H - 2); q += nt) {
+    const int r = q / (kPtBX + 2 * H - 2), c = q - r * (kPtBX + 2 * H - 2);
+    const int gi = ti0 - H + 1 + r, gj = tj0 - H + 1 + c;
+    X1[r][c] = inside(gi, gj) ? tile_jacobi<kPtBX + 2 * H>(Y, r + 1, c + 1, gi, gj, a) : 0.f;
+  }
+  __syncthreads();
+  auto second = [&](int r, int c, int gi, int gj) {   // (r, c) in X1 coordinates
+    return (a.zero_last && gi == a.n - 1) ? 0.f : tile_jacobi<kPtBX + 2 * H - 2>(X1, r, c, gi, gj, a);
+  };
+  if constexpr (!NORM) {
+    for (int q = tid; q < kPtBY * kPtBX; q += nt) {
+      const int r = q / kPtBX, c = q - r * kPtBX;
+      const int gi = ti0 + r, gj = tj0 + c;
+      if (inside(gi, gj)) a.xout[(long)gi * a.m + gj] = second(r + 1, c + 1, gi, gj);
+    }
+  } else {
+  for (int q = tid; q < (kPtBY + 2) * (kPtBX + 2); q += nt) {
+    const int r = q / (kPtBX + 2), c = q - r * (kPtBX + 2);
+    const int gi = ti0 - 1 + r, gj = tj0 - 1 + c;
+    X2[r][c] = inside(gi, gj) ? second(r + 1, c + 1, gi, gj) : 0.f;
+  }
+  __syncthreads();
+  df rr{0.f, 0.f}, bb{0.f, 0.f};
+  for (int q = tid; q < kPtBY * kPtBX; q += nt) {
+    const int r = q / kPtBX, c = q - r * kPtBX;
+    const int gi = ti0 + r, gj = tj0 + c;
+    if (inside(gi, gj)) {
+      a.xout[(long)gi * a.m + gj] = X2[r + 1][c + 1];
+      const float bv = ldg(a.b + (long)gi * a.m + gj);
+      const float res = tile_resid<kPtBX + 2>(X2, r + 1, c + 1, gi, gj, a);
+      // (b - A p) in FP32 as the reference evaluates it; its square exactly
+      rr = df_add(rr, two_prod(res, res));
+      bb = df_add(bb, two_prod(bv, bv));
+    }
+  }
+  const double s = block_sum_df(rr);
+  const double sb = a.also_b ? block_sum_df(bb) : 0.0;
+  if (tid == 0) {
+    atomicAdd(&a.sc->acc[0], s);
+    if (a.also_b) atomicAdd(&a.sc->acc[1], sb);
+  }
+  }
+}
+
 
 __global__ void k_copy(const float* __restrict__ s, float* __restrict__ d, long n) {
   long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
@@ -255,35 +370,33 @@ static int parity_solve(const AjStepParams& p, const Layout& L, void* ws, const 
     if (!mac) return nullptr;
     return l == 0 ? mask : at<float>(ws, L.M[l]);
   };
+  const int vk = p.flow_type == AJ_FLOW_VON_KARMAN;
+  auto tile_grid = [&](int l) {
+    return l == 0 ? dim3(cdiv(L.lm[l], 64), cdiv(L.ln[l], 16)) : dim3(cdiv(L.lm[l], 32), cdiv(L.ln[l], 8));
+  };
   for (int cyc = 0; cyc < p.v_cycles; ++cyc) {
     const int* sk = cyc == 0 ? nullptr : skip;   // the first cycle always runs
-    // down sweep of the V: levels 0..nl-1
+    // down the V: levels 0..nl-1; each level's pre-smoothed state goes to T,
+    // its restricted residual to the next level's b
     for (int l = 0; l < nl; ++l) {
-      int n = L.ln[l], m = L.lm[l];
-      dim3 g(cdiv(m, 32), cdiv(n, 8));
-      bool zero_in = (l > 0) || (cyc == 0 && !p0);
-      ParJac a{};
+      ParTile a{};
+      a.xin = (l == 0 && !(cyc == 0 && !p0)) ? X(0) : nullptr;
       a.b = B(l);
       a.mask = M(l);
+      a.xout = T(l);
+      a.bc = B(l + 1);
       a.skip = sk;
-      a.n = n;
-      a.m = m;
+      a.n = L.ln[l];
+      a.m = L.lm[l];
+      a.nc = L.ln[l + 1];
+      a.mc = L.lm[l + 1];
+      a.zero_last = vk;
+      a.mac_outlet = mac && vk;
       a.ax = ax;
       a.ay = ay;
       a.den = den;
-      // sweep 1: X -> T (or zero -> T)
-      a.pin = zero_in ? nullptr : X(l);
-      a.pout = T(l);
-      a.zero_last = 0;
-      k_par_jacobi<<<g, blk, 0, st>>>(a);
-      // sweep 2: T -> X, outlet row reset
-      a.pin = T(l);
-      a.pout = X(l);
-      a.zero_last = p.flow_type == AJ_FLOW_VON_KARMAN;
-      k_par_jacobi<<<g, blk, 0, st>>>(a);
-      dim3 gc(cdiv(m / 2, 32), cdiv(n / 2, 8));
-      k_par_resid_restrict<<<gc, blk, 0, st>>>(X(l), B(l), B(l + 1), n, m, ax, ay,
-                                               mac && p.flow_type == AJ_FLOW_VON_KARMAN, sk);
+      if (l == 0) k_par_down<16, 64><<<tile_grid(l), kPtThreads, 0, st>>>(a);
+      else k_par_down<8, 32><<<tile_grid(l), kPtThreads, 0, st>>>(a);
     }
     // coarsest: 10 sweeps from zero, ending in X
     if (parity_coarsest_fused(L)) {
@@ -311,35 +424,30 @@ static int parity_solve(const AjStepParams& p, const Layout& L, void* ws, const 
         k_par_jacobi<<<g, blk, 0, st>>>(a);
       }
     }
-    // up sweep: p + P(e) fused into post-sweep 1, then post-sweep 2
+    // up the V: T + P(coarser X), two post-sweeps, into X; level 0 also
+    // forms the residual norm of the early exit (multigrid_solver.py:222-232)
     for (int l = nl - 1; l >= 0; --l) {
-      int n = L.ln[l], m = L.lm[l];
-      dim3 g(cdiv(m, 32), cdiv(n, 8));
-      ParJac a{};
+      ParTile a{};
+      a.xin = T(l);
+      a.xc = X(l + 1);
       a.b = B(l);
       a.mask = M(l);
+      a.xout = X(l);
+      a.sc = sc;
       a.skip = sk;
-      a.n = n;
-      a.m = m;
+      a.n = L.ln[l];
+      a.m = L.lm[l];
       a.nc = L.ln[l + 1];
       a.mc = L.lm[l + 1];
+      a.zero_last = vk;
+      a.mac_outlet = mac && vk;
+      a.also_b = cyc == 0;
       a.ax = ax;
       a.ay = ay;
       a.den = den;
-      a.pin = X(l);
-      a.ec = X(l + 1);
-      a.pout = T(l);
-      a.zero_last = 0;
-      k_par_jacobi<<<g, blk, 0, st>>>(a);
-      a.pin = T(l);
-      a.ec = nullptr;
-      a.pout = X(l);
-      a.zero_last = p.flow_type == AJ_FLOW_VON_KARMAN;
-      k_par_jacobi<<<g, blk, 0, st>>>(a);
+      if (l == 0) k_par_up<16, 64, true><<<tile_grid(l), kPtThreads, 0, st>>>(a);
+      else k_par_up<8, 32, false><<<tile_grid(l), kPtThreads, 0, st>>>(a);
     }
-    k_par_norm<<<cdiv((long)p.nx * p.ny, 256 * 4) < 1216 ? cdiv((long)p.nx * p.ny, 256 * 4) : 1216,
-                 256, 0, st>>>(pout, b0, p.nx, p.ny, ax, ay, mac && p.flow_type == AJ_FLOW_VON_KARMAN,
-                               sc, cyc == 0);
     k_par_check<<<1, 1, 0, st>>>(sc, p.dx * p.dy, tol * tol, cyc == 0);
   }
   return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;

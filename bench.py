@@ -52,7 +52,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="naca",
-                    choices=["naca", "ensemble", "tri4096", "post", "adjoint"],
+                    choices=["naca", "ensemble", "tri4096", "post", "adjoint", "parity"],
                     help="naca: the metric's workload (default); ensemble: 64 cylinder "
                          "channels of uneven sizes in one graph launch; tri4096: the "
                          "4096x2048 three-cylinder dynamic-LES flow")
@@ -545,6 +545,9 @@ def side_workload(args):
     if args.workload == "adjoint":
         adjoint_workload(args, dev, st)
         return
+    if args.workload == "parity":
+        parity_workload(args, dev, st)
+        return
     from aerojax_gb300 import configs
     from aerojax_gb300 import nn as NNW
     case = configs.tri_cyl_4096x2048(device=dev)
@@ -588,6 +591,69 @@ def side_workload(args):
         "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": case["name"], "arms": out,
                    "l2": "working set (~1 GB) above the L2 size (no flush)"}}))
+
+
+def parity_workload(args, dev, st):
+    """The reference's own algorithm on the GPU: the GUI MAC step
+    (step_handlers.py:62-301) with the reference multigrid, 5 V-cycles (the
+    GUI default), on the 2048x512 NACA 0012 workload, configured like the
+    CPU port that is timed beside it (Smagorinsky 0.17, eta 1e-4, CFL 0.5)."""
+    import torch
+    from dataclasses import replace
+    import aerojax_gb300 as aj
+    from aerojax_gb300 import _lib, configs
+    nx, ny = args.nx, args.ny
+    case = configs.naca_mac_2048x512(device=dev, nx=nx, ny=ny, mg_mode="parity")
+    cfg = replace(case["cfg"], v_cycles=5, brinkman_eta=1e-4, nu_hyper_ratio=0.0,
+                  warm_start=False)
+    plan = aj.Plan(cfg, dev)
+    plan.prepare(case["mask"])
+    mask = case["mask"]
+    bufs = [(case["u"].clone(), case["v"].clone(), torch.zeros((nx, ny), device=dev))
+            for _ in range(2)]
+    flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    cur = [0]
+
+    def step():
+        src, dst = bufs[cur[0]], bufs[1 - cur[0]]
+        aj.run_step(plan, src[0], src[1], mask, out=dst)
+        cur[0] = 1 - cur[0]
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    ev, cyc = [], []
+    for _ in range(args.steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        step()
+        e1.record(st)
+        ev.append((e0, e1))
+        cyc.append(plan.stats_buf.clone())
+    torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in ev) / args.steps
+    cycles = [_lib.AjStats.from_buffer_copy(bytes(c.cpu().numpy().tobytes())).cycles for c in cyc]
+    L = _lib.lib()
+    kc = int(L.aj_kernel_count(ctypes.byref(plan.params), 0))
+    cpu = None
+    if not args.no_cpu_baseline and not args.quick:
+        n = args.cpu_sample_steps
+        cval, cel = run_cpu(nx, ny, n, 1)
+        cpu = {"value": cval, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"{n} full {nx}x{ny} MAC steps ({cel:.1f} s), NumPy float32 port of the "
+                         "reference GUI step with 5 reference V-cycles"}
+    print(json.dumps({
+        "metric": "Mcell-steps/s, reference GUI step with the reference multigrid (5 V-cycles), "
+                  f"{nx}x{ny} MAC",
+        "value": nx * ny / (ms * 1e-3) / 1e6, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "dtype": "f32",
+        "data": "synthetic (seeded NACA 0012 flow)",
+        "config": {"workload": f"naca0012_{nx}x{ny}_mac_gui_parity_mg5", "v_cycles": 5,
+                   "mg_cycles_mean": statistics.mean(cycles), "kernels_per_step": kc,
+                   "l2": "flushed before every step (256 MiB write outside the timed events)"},
+        "cpu_baseline": cpu,
+        "gpu_launches": kc * args.steps}))
 
 
 # algorithmic bytes per cell of one aj_step_vjp (RK3, one V-cycle, four
