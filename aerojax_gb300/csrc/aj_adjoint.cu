@@ -28,6 +28,7 @@
 // by the forward predictor kernels (stage buffers of the step workspace).
 #include "aj_internal.cuh"
 
+#include <cooperative_groups.h>
 #include <mutex>
 
 namespace aj {
@@ -289,48 +290,51 @@ __global__ void __launch_bounds__(kPairBX * kPairBY) k_adj_pair(
 }
 
 // the ten reversed coarsest-grid sweeps (the forward smooths 10 times from a
-// zero guess, multigrid_solver.py:186-187) in one block: the cotangent
-// ping-pongs in shared memory, b's cotangent accumulates in a third array.
-// Used when 3 arrays of the level fit the block's shared memory.
-constexpr int kCoarsestThreads = 1024;   // 32 x 32: column lanes x row strides
-__global__ void __launch_bounds__(kCoarsestThreads) k_adj_coarsest(const float* __restrict__ gin,
-                                                                   float* __restrict__ gb, int n,
-                                                                   int m, float ax, float ay,
-                                                                   float d, const int* ncyc,
-                                                                   int cyc) {
+// zero guess, multigrid_solver.py:186-187) on a cluster of kCoarseCtas
+// blocks, each holding a band of rows: h = cotangent/d ping-pongs in shared
+// memory (the rows next to the band read from the neighbours' shared memory),
+// b's cotangent accumulates in a third array.  One cluster barrier per sweep
+// (see k_par_coarsest); used when the three band arrays fit a block.
+__global__ void __cluster_dims__(kCoarseCtas, 1, 1) __launch_bounds__(kCoarseThreads)
+    k_adj_coarsest(const float* __restrict__ gin, float* __restrict__ gb, int n, int m, float ax,
+                   float ay, float d, const int* ncyc, int cyc) {
   pdl_wait();
   if (ncyc && cyc >= *ncyc) return;
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  const int rank = (int)cl.block_rank();
+  const int R = coarse_band_rows(n);
+  const int r0 = rank * R, nr = max(0, min(n, r0 + R) - r0);
   extern __shared__ float csm[];
-  const int nm = n * m;
-  float* A = csm;
-  float* B = csm + nm;
-  float* G = csm + 2 * nm;
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  // A holds h = cotangent/d (one division per cell per sweep); B the next
-  for (int i = ty; i < n; i += 32)
-    for (int j = tx; j < m; j += 32) {
-      const float hc = gin[(long)i * m + j] / d;
-      A[i * m + j] = hc;
-      G[i * m + j] = -hc;
-    }
-  __syncthreads();
+  float* A = csm;            // h = cotangent/d of the band (ping-pong with B)
+  float* B = csm + R * m;
+  float* G = csm + 2 * R * m;
+  for (int q = threadIdx.x; q < nr * m; q += blockDim.x) {
+    const float hc = gin[(long)r0 * m + q] / d;
+    A[q] = hc;
+    G[q] = -hc;
+  }
+  cl.sync();                 // the neighbours' first values are in place
   for (int s = 9; s >= 1; --s) {
-    for (int i = ty; i < n; i += 32) {
-      const int rp = (i + 1 < n ? i + 1 : n - 1) * m, rm = (i > 0 ? i - 1 : 0) * m, rc = i * m;
-      for (int j = tx; j < m; j += 32) {
-        const int jp = j + 1 < m ? j + 1 : m - 1, jm = j > 0 ? j - 1 : 0;
-        const float hn = (ax * (A[rp + j] + A[rm + j]) + ay * (A[rc + jp] + A[rc + jm])) / d;
-        B[rc + j] = hn;
-        G[rc + j] = G[rc + j] - hn;
-      }
+    for (int q = threadIdx.x; q < nr * m; q += blockDim.x) {
+      const int li = q / m, j = q - li * m, i = r0 + li;
+      const int ip = i + 1 < n ? i + 1 : n - 1, im = i > 0 ? i - 1 : 0;
+      const int jp = j + 1 < m ? j + 1 : m - 1, jm = j > 0 ? j - 1 : 0;
+      auto hv = [&](int ii, int jj) -> float {
+        const int owner = ii / R;
+        const float* base = owner == rank ? A : cl.map_shared_rank(A, owner);
+        return base[(ii - owner * R) * m + jj];
+      };
+      const float hn = (ax * (hv(ip, j) + hv(im, j)) + ay * (hv(i, jp) + hv(i, jm))) / d;
+      B[q] = hn;
+      G[q] = G[q] - hn;
     }
-    __syncthreads();
+    cl.sync();
     float* t = A;
     A = B;
     B = t;
   }
-  for (int i = ty; i < n; i += 32)
-    for (int j = tx; j < m; j += 32) gb[(long)i * m + j] = G[i * m + j];
+  for (int q = threadIdx.x; q < nr * m; q += blockDim.x) gb[(long)r0 * m + q] = G[q];
 }
 
 // transpose of the reference prolongation (multigrid_solver.py:134-156) onto
@@ -676,8 +680,9 @@ int launch_step_vjp(const AjStepParams& p, const Layout& L, void* ws, void* aws,
       const int n = L.ln[nl], m = L.lm[nl];
       cudaFuncSetAttribute(k_adj_coarsest, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)kBlockSmemMax);
-      launch_pdl(true, k_adj_coarsest, dim3(1), dim3(kCoarsestThreads), (size_t)n * m * 12, st,
-                 F(A.GX[nl]), F(A.GB[nl]), n, m, ax, ay, den, nc, cyc);
+      launch_pdl(true, k_adj_coarsest, dim3(kCoarseCtas), dim3(kCoarseThreads),
+                 (size_t)coarse_band_rows(n) * m * 12, st, F(A.GX[nl]), F(A.GB[nl]), n, m, ax, ay,
+                 den, nc, cyc);
     } else {
       for (int s = 9; s >= 0; --s) {
         const float* gin = (s % 2 == 1) ? F(A.GX[nl]) : F(A.GT[nl]);

@@ -282,6 +282,11 @@ bool nn_step_shape_ok(const AjStepParams& p);
 int nn_correct_state(const AjStepParams& p, const Layout& L, void* ws, const float* b,
                      const NnWarm& nn, float* state, cudaStream_t st);
 constexpr size_t kBlockSmemMax = 220 * 1024;   // coarse-level kernel shared memory budget
+// The parity V-cycle's coarsest level (10 Jacobi sweeps) runs on a cluster of
+// kCoarseCtas blocks, each holding a band of rows in shared memory.
+constexpr int kCoarseCtas = 8;
+constexpr int kCoarseThreads = 256;
+__host__ __device__ inline int coarse_band_rows(int n) { return (n + kCoarseCtas - 1) / kCoarseCtas; }
 
 inline unsigned cdiv(long a, long b) { return (unsigned)((a + b - 1) / b); }
 

@@ -11,6 +11,8 @@
 //
 // The converging mode lives in aj_converge.cu; this file dispatches to it.
 #include "aj_internal.cuh"
+
+#include <cooperative_groups.h>
 #include <math.h>
 
 namespace aj {
@@ -113,47 +115,56 @@ __global__ void k_par_check(DevScalars* sc, double dxdy, double tol2, int first)
 }
 
 // the coarsest level's 10 Jacobi sweeps from a zero guess
-// (multigrid_solver.py:186-187) in one block: the iterate ping-pongs in
-// shared memory, b is staged once.  Same arithmetic as k_par_jacobi; used
-// when three arrays of the level fit the block's shared memory.
-constexpr int kParCoarsestThreads = 1024;   // 32 x 32: column lanes x row strides
-__global__ void __launch_bounds__(kParCoarsestThreads) k_par_coarsest(
-    const float* __restrict__ b, const float* __restrict__ mask, float* __restrict__ x, int n,
-    int m, float ax, float ay, float den, const int* skip) {
+// (multigrid_solver.py:186-187) on a cluster of kCoarseCtas blocks: block k
+// holds rows [k R, k R + R) of the iterate (ping-pong) and of b in shared
+// memory and reads the rows next to its band from its neighbours' shared
+// memory.  One cluster barrier per sweep: a sweep reads one buffer and writes
+// the other, so after the barrier nobody still reads what the next sweep
+// overwrites.  The skip test comes before any barrier and is the same for
+// every block; after the last barrier a block reads only its own memory.
+// Same arithmetic as k_par_jacobi.
+__global__ void __cluster_dims__(kCoarseCtas, 1, 1) __launch_bounds__(kCoarseThreads)
+    k_par_coarsest(const float* __restrict__ b, const float* __restrict__ mask,
+                   float* __restrict__ x, int n, int m, float ax, float ay, float den,
+                   const int* skip) {
   if (skip && *skip) return;
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  const int rank = (int)cl.block_rank();
+  const int R = coarse_band_rows(n);
+  const int r0 = rank * R, nr = max(0, min(n, r0 + R) - r0);
   extern __shared__ float psm[];
-  const int nm = n * m;
   float* P = psm;
-  float* Q = psm + nm;
-  float* Bs = psm + 2 * nm;
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  for (int i = ty; i < n; i += 32)
-    for (int j = tx; j < m; j += 32) Bs[i * m + j] = b[(long)i * m + j];
+  float* Q = psm + R * m;
+  float* Bs = psm + 2 * R * m;
+  for (int q = threadIdx.x; q < nr * m; q += blockDim.x) Bs[q] = b[(long)r0 * m + q];
   __syncthreads();
   for (int s = 0; s < 10; ++s) {
-    for (int i = ty; i < n; i += 32) {
-      const int rp = (i + 1 < n ? i + 1 : n - 1) * m, rm = (i > 0 ? i - 1 : 0) * m, rc = i * m;
-      for (int j = tx; j < m; j += 32) {
-        const int jp = j + 1 < m ? j + 1 : m - 1, jm = j > 0 ? j - 1 : 0;
-        const float xp = s ? P[rp + j] : 0.f, xm = s ? P[rm + j] : 0.f;
-        const float yp = s ? P[rc + jp] : 0.f, ym = s ? P[rc + jm] : 0.f;
-        float pn = (ax * (xp + xm) + ay * (yp + ym) - Bs[rc + j]) / den;
-        if (mask) pn = pn * mask[rc + j];
-        Q[rc + j] = pn;
-      }
+    for (int q = threadIdx.x; q < nr * m; q += blockDim.x) {
+      const int li = q / m, j = q - li * m, i = r0 + li;
+      const int ip = i + 1 < n ? i + 1 : n - 1, im = i > 0 ? i - 1 : 0;
+      const int jp = j + 1 < m ? j + 1 : m - 1, jm = j > 0 ? j - 1 : 0;
+      auto pv = [&](int ii, int jj) -> float {
+        if (s == 0) return 0.f;
+        const int owner = ii / R;
+        const float* base = owner == rank ? P : cl.map_shared_rank(P, owner);
+        return base[(ii - owner * R) * m + jj];
+      };
+      float pn = (ax * (pv(ip, j) + pv(im, j)) + ay * (pv(i, jp) + pv(i, jm)) - Bs[q]) / den;
+      if (mask) pn = pn * mask[(long)i * m + j];
+      Q[q] = pn;
     }
-    __syncthreads();
+    cl.sync();
     float* t = P;
     P = Q;
     Q = t;
   }
-  for (int i = ty; i < n; i += 32)
-    for (int j = tx; j < m; j += 32) x[(long)i * m + j] = P[i * m + j];
+  for (int q = threadIdx.x; q < nr * m; q += blockDim.x) x[(long)r0 * m + q] = P[q];
 }
 
 // whether the coarsest level's sweeps run as one k_par_coarsest block
 bool parity_coarsest_fused(const Layout& L) {
-  return (size_t)L.ln[L.nlev] * L.lm[L.nlev] * 12 <= kBlockSmemMax;
+  return (size_t)coarse_band_rows(L.ln[L.nlev]) * L.lm[L.nlev] * 12 <= kBlockSmemMax;
 }
 
 // ---- one level of the V-cycle per launch, on tiles
@@ -401,11 +412,11 @@ static int parity_solve(const AjStepParams& p, const Layout& L, void* ws, const 
     // coarsest: 10 sweeps from zero, ending in X
     if (parity_coarsest_fused(L)) {
       const int n = L.ln[nl], m = L.lm[nl];
-      const size_t csm = (size_t)n * m * 12;
+      const size_t csm = (size_t)coarse_band_rows(n) * m * 12;
       cudaFuncSetAttribute(k_par_coarsest, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)kBlockSmemMax);
-      k_par_coarsest<<<1, kParCoarsestThreads, csm, st>>>(B(nl), M(nl), X(nl), n, m, ax, ay, den,
-                                                           sk);
+      k_par_coarsest<<<kCoarseCtas, kCoarseThreads, csm, st>>>(B(nl), M(nl), X(nl), n, m, ax, ay,
+                                                               den, sk);
     } else {
       int n = L.ln[nl], m = L.lm[nl];
       dim3 g(cdiv(m, 32), cdiv(n, 8));
