@@ -566,7 +566,7 @@ __global__ void __launch_bounds__(TC::NTH, 4) k_cv_up0(
     }
   }
   if (profile) return;
-  block_sum_atomic((double)acc, &sc->acc[0]);
+  block_sum_atomic_f(acc, &sc->acc[0]);
   if (tid == 0) {
     __threadfence();
     unsigned int ticket = atomicAdd(&sc->red_count, 1u);
@@ -1099,8 +1099,8 @@ __global__ void __launch_bounds__(256) k_cv_resid(const float* __restrict__ ps,
       acc = fmaf(rr, rr, acc);
     }
   }
-  block_sum_atomic((double)acc, &sc->acc[0]);
-  block_sum_atomic((double)accb, &sc->acc[1]);
+  block_sum_atomic_f(acc, &sc->acc[0]);
+  block_sum_atomic_f(accb, &sc->acc[1]);
   // the last block: commit the history rotation, reset the solve's counters
   // and run the test before the first cycle (the guess may already satisfy rtol)
   __shared__ int am_last;

@@ -168,6 +168,32 @@ __device__ __forceinline__ double block_sum_df(df v) {
   return t;
 }
 
+// Block-wide sum of one float per thread added atomically to *dst by one
+// thread: a double-FP32 TwoSum butterfly in each warp (the FP32 pipes; the
+// FP64 butterfly of block_sum_atomic costs ~10 FP64 operations per thread on
+// GB300's 1/64-rate FP64 pipe), one FP64 value per warp.  Every thread of the
+// block must call it (it synchronises).
+__device__ __forceinline__ void block_sum_atomic_f(float v, double* dst) {
+  __shared__ double wf_[32];
+  df s{v, 0.f};
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float h = __shfl_xor_sync(0xffffffffu, s.hi, o);
+    const float l = __shfl_xor_sync(0xffffffffu, s.lo, o);
+    s = df_add(s, df{h, l});
+  }
+  const int nthreads = blockDim.x * blockDim.y;
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  if ((tid & 31) == 0) wf_[tid >> 5] = (double)s.hi + (double)s.lo;
+  __syncthreads();
+  if (tid == 0) {
+    double t = 0.0;
+    for (int k = 0; k < (nthreads >> 5); ++k) t += wf_[k];
+    atomicAdd(dst, t);
+  }
+  __syncthreads();
+}
+
 // Block-wide sum of one double per thread in a fixed order (the result is
 // bit-reproducible); the total is returned to thread 0.  Every thread of the
 // block must call it (it synchronises).
