@@ -109,3 +109,28 @@ def test_no_cpu_fallback_without_library(monkeypatch, tmp_path):
     monkeypatch.setattr(_lib, "LIB_PATH", str(tmp_path / "missing.so"))
     with pytest.raises(RuntimeError, match="no CPU fallback"):
         _lib.lib()
+
+
+def test_step_vjp_covers_the_rollout_configuration_only(L):
+    """aj_step_vjp's host checks: the collocated von Karman step_pure with
+    upwind RK3/RK2, a fixed dt and the parity V-cycle; anything else gets no
+    workspace size and no kernel count (aj_step_vjp itself returns
+    AJ_ERR_PARAM)."""
+    from dataclasses import replace
+    from aerojax_gb300.adjoint import _config
+    from aerojax_gb300.solver import make_params
+    base = _config(128, 64, 0.05, 0.05, 0.02, 1.0, 4e-3, True)
+    for ok in (base, replace(base, fast_mode=True), replace(base, v_cycles=3)):
+        p = make_params(ok)
+        assert L.aj_step_vjp_workspace_size(ctypes.byref(p)) > 0
+        assert L.aj_step_vjp_kernel_count(ctypes.byref(p)) > 0
+    for bad in (replace(base, grid_type="mac", variant="gui"), replace(base, variant="gui"),
+                replace(base, mg_mode="converge"), replace(base, cfl_dt=True),
+                replace(base, advection_scheme="weno5"), replace(base, warm_start=True)):
+        p = make_params(bad)
+        assert L.aj_step_vjp_workspace_size(ctypes.byref(p)) == 0
+        assert L.aj_step_vjp_kernel_count(ctypes.byref(p)) == -1
+    # the reversed V-cycles and the recomputed stages are counted
+    k1 = L.aj_step_vjp_kernel_count(ctypes.byref(make_params(base)))
+    k3 = L.aj_step_vjp_kernel_count(ctypes.byref(make_params(replace(base, v_cycles=3))))
+    assert k3 > k1

@@ -138,17 +138,3 @@ def test_rollout_vjp_matches_oracle(dev):
     assert _rel(got["sdf"].cpu(), ref["sdf"]) <= 2e-4
     assert _scalar_ok(got["nu"], ref, "nu", 2e-4), (got["nu"], ref["nu"], ref["nu_abs"])
     assert _scalar_ok(got["U_inf"], ref, "U_inf", 2e-4), (got["U_inf"], ref["U_inf"])
-
-
-def test_step_vjp_rejects_uncovered_configurations(dev):
-    import ctypes
-    from dataclasses import replace
-    from aerojax_gb300 import _lib
-    from aerojax_gb300.adjoint import _config
-    from aerojax_gb300.solver import make_params
-    base = _config(128, 64, DX, DX, NU, U, DT, False)
-    for bad in (replace(base, grid_type="mac", variant="gui"), replace(base, mg_mode="converge"),
-                replace(base, cfl_dt=True), replace(base, advection_scheme="weno5")):
-        p = make_params(bad)
-        assert _lib.lib().aj_step_vjp_workspace_size(ctypes.byref(p)) == 0
-        assert _lib.lib().aj_step_vjp_kernel_count(ctypes.byref(p)) == -1
