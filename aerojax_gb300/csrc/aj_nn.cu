@@ -816,13 +816,19 @@ __global__ void __launch_bounds__(512) k_nn_scale(const float* __restrict__ x, l
     am_last = atomicAdd(&sc->red_count, 1u) == gridDim.x - 1;
   }
   __syncthreads();
-  if (am_last && threadIdx.x == 0) {
-    __threadfence();
-    double tr = 0.0, tp = 0.0;
-    for (unsigned b = 0; b < gridDim.x; ++b) {
-      tr += __ldcg(part + 2 * b);
-      tp += __ldcg(part + 2 * b + 1);
-    }
+  if (!am_last) return;
+  // the last block: every thread loads its partials at once (one thread
+  // walking them waited on one L2 round trip per partial), then a fixed-order
+  // block sum
+  __threadfence();
+  double lr = 0.0, lp = 0.0;
+  for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+    lr += __ldcg(part + 2 * b);
+    lp += __ldcg(part + 2 * b + 1);
+  }
+  const double tr = block_sum(lr);
+  const double tp = block_sum(lp);
+  if (threadIdx.x == 0) {
     const double rr = sqrt(tr / (double)cells), rp = sqrt(tp / (double)cells);
     const double rrc = rr > 1e-30 ? rr : 1e-30, rpc = rp > 1e-30 ? rp : 1e-30;
     sc->nn_rms_r = rrc;
