@@ -26,7 +26,8 @@ import numpy as np
 
 from . import ref_np as R
 
-__all__ = ["step_pure_vjp", "forward_stages", "mg_vjp", "rollout", "rollout_vjp"]
+__all__ = ["step_pure_vjp", "step_gui_vjp", "forward_stages", "mg_vjp", "rollout",
+           "rollout_vjp"]
 
 
 # ------------------------------------------------------------------ pieces
@@ -66,21 +67,34 @@ def _one_sided_T(alpha, vel, h, axis):
     return np.moveaxis(out, 0, axis)
 
 
-def _rhs(u, v, nu, dx, dy):
-    """compute_rhs_explicit (rk3_simple_new.py:284-313) without LES or
-    hyperviscosity, as step_pure calls it on the collocated grid."""
+def _rhs(u, v, nu, dx, dy, hyper=0.0):
+    """compute_rhs_explicit (rk3_simple_new.py:284-313) without LES: upwind
+    advection, nu * Laplacian and, with ``hyper`` (nu_hyper_ratio) > 0, the
+    bi-Laplacian term nu * hyper * dx * dy * lap(lap(w)) (:307-312, sponge
+    disabled)."""
     adv_u = u * _one_sided(u, u, dx, 0) + v * _one_sided(u, v, dy, 1)
     adv_v = u * _one_sided(v, u, dx, 0) + v * _one_sided(v, v, dy, 1)
-    return -adv_u + nu * _lap(u, dx, dy), -adv_v + nu * _lap(v, dx, dy)
+    lu, lv = _lap(u, dx, dy), _lap(v, dx, dy)
+    ru, rv = -adv_u + nu * lu, -adv_v + nu * lv
+    if hyper > 0:
+        nh = nu * hyper * (dx * dy)
+        ru = ru - nh * _lap(lu, dx, dy)
+        rv = rv - nh * _lap(lv, dx, dy)
+    return ru, rv
 
 
-def _rhs_T(ku_bar, kv_bar, u, v, nu, dx, dy):
-    """Cotangents of (u, v) from cotangents of _rhs(u, v), and d/d nu."""
+def _rhs_T(ku_bar, kv_bar, u, v, nu, dx, dy, hyper=0.0):
+    """Cotangents of (u, v) from cotangents of _rhs(u, v), and d/d nu (the
+    Laplacian and its square are symmetric, so each is its own transpose)."""
     a, b = -ku_bar, -kv_bar                          # cotangents of adv_u, adv_v
     fxu, fyu = _one_sided(u, u, dx, 0), _one_sided(u, v, dy, 1)
     fxv, fyv = _one_sided(v, u, dx, 0), _one_sided(v, v, dy, 1)
     ub = nu * _lap(ku_bar, dx, dy)
     vb = nu * _lap(kv_bar, dx, dy)
+    if hyper > 0:
+        nh = nu * hyper * (dx * dy)
+        ub = ub - nh * _lap(_lap(ku_bar, dx, dy), dx, dy)
+        vb = vb - nh * _lap(_lap(kv_bar, dx, dy), dx, dy)
     # velocity roles
     ub += a * fxu + b * fxv
     vb += a * fyu + b * fyv
@@ -88,12 +102,16 @@ def _rhs_T(ku_bar, kv_bar, u, v, nu, dx, dy):
     ub += _one_sided_T(a * u, u, dx, 0) + _one_sided_T(a * v, v, dy, 1)
     vb += _one_sided_T(b * u, u, dx, 0) + _one_sided_T(b * v, v, dy, 1)
     tu, tv = ku_bar * _lap(u, dx, dy), kv_bar * _lap(v, dx, dy)
+    if hyper > 0:
+        hh = hyper * (dx * dy)
+        tu = tu - hh * ku_bar * _lap(_lap(u, dx, dy), dx, dy)
+        tv = tv - hh * kv_bar * _lap(_lap(v, dx, dy), dx, dy)
     nu_bar = float(np.sum(tu) + np.sum(tv))
     nu_abs = float(np.sum(np.abs(tu)) + np.sum(np.abs(tv)))   # the sum's magnitude scale
     return ub, vb, nu_bar, nu_abs
 
 
-def _bc_T(gu, gv):
+def _bc_T(gu, gv, slip=True):
     """Transpose of the von Karman slip-wall boundary conditions
     (rk3_simple_new.py:262-275 and step.py:365-377, the same statements):
     u[0]=U, v[0]=0, u[-1]=u[-2], v[-1]=v[-2], u[:,0]=u[:,1], u[:,-1]=u[:,-2],
@@ -102,9 +120,10 @@ def _bc_T(gu, gv):
     gu, gv = gu.copy(), gv.copy()
     gv[:, -1] = 0.0
     gv[:, 0] = 0.0
-    gu[:, -2] += gu[:, -1]
-    gu[:, -1] = 0.0
-    gu[:, 1] += gu[:, 0]
+    if slip:
+        gu[:, -2] += gu[:, -1]
+        gu[:, 1] += gu[:, 0]
+    gu[:, -1] = 0.0                                   # (no-slip: u = 0 on the walls)
     gu[:, 0] = 0.0
     gv[-2, :] += gv[-1, :]
     gv[-1, :] = 0.0
@@ -114,6 +133,26 @@ def _bc_T(gu, gv):
     U_bar = float(np.sum(gu[0, :]))
     U_abs = float(np.sum(np.abs(gu[0, :])))
     gu[0, :] = 0.0
+    return gu, gv, U_bar, U_abs
+
+
+def _bc_gui_T(gu, gv):
+    """Transpose of the GUI step's boundary rows (step_handlers.py:143-161):
+    u[0, 1:-1] = U, v[0] = 0, u[-1] = u[-2], v[-1] = v[-2], u and v zero on
+    both walls, undone in reverse order."""
+    gu, gv = gu.copy(), gv.copy()
+    gv[:, -1] = 0.0
+    gv[:, 0] = 0.0
+    gu[:, -1] = 0.0
+    gu[:, 0] = 0.0
+    gv[-2, :] += gv[-1, :]
+    gv[-1, :] = 0.0
+    gu[-2, :] += gu[-1, :]
+    gu[-1, :] = 0.0
+    gv[0, :] = 0.0
+    U_bar = float(np.sum(gu[0, 1:-1]))
+    U_abs = float(np.sum(np.abs(gu[0, 1:-1])))
+    gu[0, 1:-1] = 0.0
     return gu, gv, U_bar, U_abs
 
 
@@ -245,25 +284,26 @@ def _chi(mask, sdf, dx):
     return R.sigmoid(-sdf / (0.1 * dx)) if sdf is not None else 1.0 - mask
 
 
-def forward_stages(u, v, dt, mask, sdf, dx, dy, nu, U_inf, fast_mode=False, brinkman_eta=0.005):
+def forward_stages(u, v, dt, mask, sdf, dx, dy, nu, U_inf, fast_mode=False, brinkman_eta=0.005,
+                   hyper=0.0):
     """The predictor of step_pure with its stage states kept: returns
     (stages, (us, vs)), stages = list of (u_k, v_k) fed to compute_rhs_explicit
     and the pre-mask final combination."""
     chi = _chi(mask, sdf, dx)
     den = 1 + dt * chi / brinkman_eta
-    k1u, k1v = _rhs(u, v, nu, dx, dy)
+    k1u, k1v = _rhs(u, v, nu, dx, dy, hyper)
     if not fast_mode:
         u2, v2 = (u + dt * k1u) / den, (v + dt * k1v) / den
-        k2u, k2v = _rhs(u2, v2, nu, dx, dy)
+        k2u, k2v = _rhs(u2, v2, nu, dx, dy, hyper)
         u3 = (0.75 * u + 0.25 * (u + dt * k2u)) / den
         v3 = (0.75 * v + 0.25 * (v + dt * k2v)) / den
-        k3u, k3v = _rhs(u3, v3, nu, dx, dy)
+        k3u, k3v = _rhs(u3, v3, nu, dx, dy, hyper)
         un = ((1 / 3) * u + (2 / 3) * (u + dt * k3u)) / den
         vn = ((1 / 3) * v + (2 / 3) * (v + dt * k3v)) / den
         stages = [(u, v), (u2, v2), (u3, v3)]
     else:
         u2, v2 = (u + dt * k1u) / den, (v + dt * k1v) / den
-        k2u, k2v = _rhs(u2, v2, nu, dx, dy)
+        k2u, k2v = _rhs(u2, v2, nu, dx, dy, hyper)
         un = (u + 0.5 * dt * (k1u + k2u)) / den
         vn = (v + 0.5 * dt * (k1v + k2v)) / den
         stages = [(u, v), (u2, v2)]
@@ -331,28 +371,48 @@ def step_pure_vjp(u, v, dt, mask, sdf, dx, dy, nu, U_inf, gu, gv, gp=None, *, v_
     U_bar += ub
     U_abs += ua
     # ---- predictor, reversed
-    us_bar, vs_bar, ub, ua = _bc_T(us_bar, vs_bar)
-    U_bar += ub
-    U_abs += ua
+    g = _predictor_T(us_bar, vs_bar, stages, (un_pre, vn_pre), den, chi, live, dt, nu, dx, dy,
+                     fast_mode, 0.0, True, sdf is not None, brinkman_eta)
+    U_bar += g["U_inf"]
+    U_abs += g["U_inf_abs"]
+    # forward outputs (for callers and tests)
+    un, vn, pp = R.step_pure(u, v, dt, mask, sdf, dx, dy, nu, U_inf, v_cycles=v_cycles,
+                             fast_mode=fast_mode, brinkman_eta=brinkman_eta,
+                             mg=R.MGConfig(mode="parity", v_cycles=v_cycles, levels=levels))
+    return {"u": g["u"], "v": g["v"], "sdf": g["sdf"], "nu": g["nu"], "U_inf": U_bar,
+            "nu_abs": g["nu_abs"], "U_inf_abs": U_abs, "cycles": info["cycles"],
+            "out": (un, vn, pp)}
+
+
+def _predictor_T(us_bar, vs_bar, stages, wn, den, chi, live, dt, nu, dx, dy, fast_mode, hyper,
+                 slip, has_sdf, brinkman_eta):
+    """Reverse of rk_step_unified (rk3_simple_new.py:315-358) from the
+    cotangent of its output (after its hard mask and boundary rows): the
+    cotangents of its inputs u, v, of the SDF through chi (has_sdf), of nu
+    and of U_inf (the inlet row it sets)."""
+    us_bar, vs_bar, U_bar, U_abs = _bc_T(us_bar, vs_bar, slip)
+    un_pre, vn_pre = wn
     xu = np.where(live, us_bar, 0.0) / den
     xv = np.where(live, vs_bar, 0.0) / den
     den_bar = -(xu * un_pre + xv * vn_pre)
     nu_bar = nu_abs = 0.0
+
+    def rT(ku, kv, uu, vv):
+        nonlocal nu_bar, nu_abs
+        a, b, nb, na = _rhs_T(ku, kv, uu, vv, nu, dx, dy, hyper)
+        nu_bar += nb
+        nu_abs += na
+        return a, b
+
     if not fast_mode:
         (u1, v1), (u2, v2), (u3, v3) = stages
         w1u, w1v = xu.copy(), xv.copy()                         # (1/3 + 2/3) of x_n
-        ku, kv = (2 / 3) * dt * xu, (2 / 3) * dt * xv
-        a, b, nb, na = _rhs_T(ku, kv, u3, v3, nu, dx, dy)
-        nu_bar += nb
-        nu_abs += na
+        a, b = rT((2 / 3) * dt * xu, (2 / 3) * dt * xv, u3, v3)
         xu, xv = a / den, b / den
         den_bar -= xu * u3 + xv * v3
         w1u += xu                                               # 0.75 + 0.25
         w1v += xv
-        ku, kv = 0.25 * dt * xu, 0.25 * dt * xv
-        a, b, nb, na = _rhs_T(ku, kv, u2, v2, nu, dx, dy)
-        nu_bar += nb
-        nu_abs += na
+        a, b = rT(0.25 * dt * xu, 0.25 * dt * xv, u2, v2)
         xu, xv = a / den, b / den
         den_bar -= xu * u2 + xv * v2
         w1u += xu
@@ -362,27 +422,70 @@ def step_pure_vjp(u, v, dt, mask, sdf, dx, dy, nu, U_inf, gu, gv, gp=None, *, v_
         (u1, v1), (u2, v2) = stages
         w1u, w1v = xu.copy(), xv.copy()
         k1u, k1v = 0.5 * dt * xu, 0.5 * dt * xv
-        a, b, nb, na = _rhs_T(0.5 * dt * xu, 0.5 * dt * xv, u2, v2, nu, dx, dy)
-        nu_bar += nb
-        nu_abs += na
+        a, b = rT(0.5 * dt * xu, 0.5 * dt * xv, u2, v2)
         xu, xv = a / den, b / den
         den_bar -= xu * u2 + xv * v2
         w1u += xu
         w1v += xv
         ku, kv = k1u + dt * xu, k1v + dt * xv
-    a, b, nb, na = _rhs_T(ku, kv, u1, v1, nu, dx, dy)
-    nu_bar += nb
-    nu_abs += na
+    a, b = rT(ku, kv, u1, v1)
     sdf_bar = None
-    if sdf is not None:
+    if has_sdf:
         chi_bar = den_bar * dt / brinkman_eta
         sdf_bar = chi_bar * chi * (1.0 - chi) * (-1.0 / (0.1 * dx))
-    # forward outputs (for callers and tests)
-    un, vn, pp = R.step_pure(u, v, dt, mask, sdf, dx, dy, nu, U_inf, v_cycles=v_cycles,
-                             fast_mode=fast_mode, brinkman_eta=brinkman_eta,
-                             mg=R.MGConfig(mode="parity", v_cycles=v_cycles, levels=levels))
-    return {"u": w1u + a, "v": w1v + b, "sdf": sdf_bar, "nu": nu_bar, "U_inf": U_bar,
-            "nu_abs": nu_abs, "U_inf_abs": U_abs, "cycles": info["cycles"], "out": (un, vn, pp)}
+    return {"u": w1u + a, "v": w1v + b, "sdf": sdf_bar, "nu": nu_bar, "nu_abs": nu_abs,
+            "U_inf": U_bar, "U_inf_abs": U_abs}
+
+
+def step_gui_vjp(u, v, dt, mask, sdf, dx, dy, nu, U_inf, gu, gv, gp=None, *, v_cycles=5,
+                 levels=4, fast_mode=False, brinkman_eta=1e-4, nu_hyper_ratio=0.0,
+                 slip_walls=True):
+    """Reverse mode of the collocated GUI step without LES
+    (step_handlers.py:62-185: BaselineSolver._step, which the WIP optimizer
+    scans under jax.grad, inverse_design_WIP/optimizer_autodiff.py:113-205).
+    Differences from step_pure: hyperviscosity and the wall condition are
+    options of the predictor, rhs = div/dt (no mask), the correction has no
+    interface projection, its boundary rows exclude the inlet corners and
+    hold u = v = 0 on the walls, one hard mask at the end.  The corner
+    smoothing of the gradient (corner_smoothing.py:39-61) scales a row that
+    was just zeroed, so it adds nothing.  Same return value as
+    step_pure_vjp."""
+    u, v, mask = (np.asarray(a, np.float64) for a in (u, v, mask))
+    sdf = None if sdf is None else np.asarray(sdf, np.float64)
+    gu, gv = np.asarray(gu, np.float64), np.asarray(gv, np.float64)
+    nx, ny = u.shape
+    gp = np.zeros((nx, ny)) if gp is None else np.asarray(gp, np.float64)
+    live = mask > 0.5
+    stages, (un_pre, vn_pre), den, chi = forward_stages(u, v, dt, mask, sdf, dx, dy, nu, U_inf,
+                                                        fast_mode, brinkman_eta, nu_hyper_ratio)
+    us = np.where(live, un_pre, 0.0)
+    vs = np.where(live, vn_pre, 0.0)
+    us, vs = R.bc_collocated(us, vs, U_inf, "von_karman", slip_walls)
+    rhs = R.divergence_nonperiodic(us, vs, dx, dy) / dt
+    p, info = R.poisson_multigrid(rhs, mask, dx, dy, levels, v_cycles, 1e-6, "von_karman",
+                                  return_info=True)
+    # ---- correction (step_handlers.py:128-183), reversed
+    g_u = np.where(live, gu, 0.0)
+    g_v = np.where(live, gv, 0.0)
+    g_u, g_v, U_bar, U_abs = _bc_gui_T(g_u, g_v)
+    us_bar, vs_bar = g_u.copy(), g_v.copy()
+    dpx_bar, dpy_bar = -dt * g_u, -dt * g_v
+    dpx_bar[0, :] = 0.0                                         # :134-135
+    p_bar = gp + _gx_T(dpx_bar, dx) + _gy_T(dpy_bar, dy)
+    # ---- pressure solve, rhs and divergence (:92-98), reversed
+    rhs_bar = mg_vjp(p_bar, dx, dy, levels, info["cycles"])
+    dub, dvb = _div_T(rhs_bar / dt, dx, dy)
+    us_bar += dub
+    vs_bar += dvb
+    g = _predictor_T(us_bar, vs_bar, stages, (un_pre, vn_pre), den, chi, live, dt, nu, dx, dy,
+                     fast_mode, nu_hyper_ratio, slip_walls, sdf is not None, brinkman_eta)
+    un, vn, pp = R.step_gui(u, v, mask, dt, sdf=sdf, dx=dx, dy=dy, nu=nu, U_inf=U_inf,
+                            nu_hyper_ratio=nu_hyper_ratio, slip_walls=slip_walls,
+                            fast_mode=fast_mode, brinkman_eta=brinkman_eta, v_cycles=v_cycles,
+                            mg=R.MGConfig(mode="parity", v_cycles=v_cycles, levels=levels))
+    return {"u": g["u"], "v": g["v"], "sdf": g["sdf"], "nu": g["nu"],
+            "U_inf": U_bar + g["U_inf"], "nu_abs": g["nu_abs"], "U_inf_abs": U_abs + g["U_inf_abs"],
+            "cycles": info["cycles"], "out": (un, vn, pp)}
 
 
 # ------------------------------------------------------------------ rollouts

@@ -101,3 +101,47 @@ def test_rollout_vjp_finite_differences():
     assert abs(num - np.sum(r["sdf"] * ds)) <= 1e-6 * abs(num)
     num = (loss(u, s, NU + eps) - loss(u, s, NU - eps)) / (2 * eps)
     assert abs(num - r["nu"]) <= 1e-6 * abs(num)
+
+
+def _loss_gui(u, v, mask, sdf, nu, Uinf, gu, gv, gp, **kw):
+    un, vn, p = R.step_gui(u, v, mask, DT, sdf=sdf, dx=DX, dy=DX, nu=nu, U_inf=Uinf,
+                           mg=R.MGConfig(mode="parity", v_cycles=kw["v_cycles"]), **{
+                               k: kw[k] for k in ("nu_hyper_ratio", "slip_walls", "fast_mode",
+                                                   "brinkman_eta")})
+    return float(np.sum(gu * un) + np.sum(gv * vn) + np.sum(gp * p))
+
+
+@pytest.mark.parametrize("fast,hyper,slip,sdf,cycles", [
+    (False, 0.0, True, True, 5), (False, 0.05, True, True, 2), (True, 0.05, False, True, 1),
+    (False, 0.0, True, False, 3)])
+def test_gui_step_vjp_finite_differences(fast, hyper, slip, sdf, cycles):
+    """The collocated GUI step (BaselineSolver._step without LES): every
+    cotangent against central differences of oracle.ref_np.step_gui."""
+    u, v, mask, s, rng = _case(3, sdf)
+    gu, gv, gp = (rng.standard_normal((NX, NY)) for _ in range(3))
+    kw = dict(v_cycles=cycles, fast_mode=fast, nu_hyper_ratio=hyper, slip_walls=slip,
+              brinkman_eta=1e-3)
+    r = A.step_gui_vjp(u, v, DT, mask, s, DX, DX, NU, U, gu, gv, gp, **kw)
+    eps = 1e-6
+
+    def fd(du=0.0, dv=0.0, ds=0.0, dnu=0.0, dU=0.0):
+        sp = None if s is None else s + eps * ds
+        sm = None if s is None else s - eps * ds
+        lp = _loss_gui(u + eps * du, v + eps * dv, mask, sp, NU + eps * dnu, U + eps * dU,
+                       gu, gv, gp, **kw)
+        lm = _loss_gui(u - eps * du, v - eps * dv, mask, sm, NU - eps * dnu, U - eps * dU,
+                       gu, gv, gp, **kw)
+        return (lp - lm) / (2 * eps)
+
+    du, dv = rng.standard_normal((NX, NY)), rng.standard_normal((NX, NY))
+    checks = [(fd(du=du), float(np.sum(r["u"] * du))),
+              (fd(dv=dv), float(np.sum(r["v"] * dv))),
+              (fd(dnu=1.0), r["nu"]),
+              (fd(dU=1.0), r["U_inf"])]
+    if s is not None:
+        ds = rng.standard_normal((NX, NY)) * DX
+        checks.append((fd(ds=ds), float(np.sum(r["sdf"] * ds))))
+    for num, ana in checks:
+        assert abs(num - ana) <= 1e-6 * max(abs(ana), 1e-3), (num, ana)
+    un, vn, _ = r["out"]
+    assert np.all(np.isfinite(un)) and np.all(np.isfinite(vn))
