@@ -10,7 +10,9 @@ aj_step_vjp, one graph launch per step each; the cotangent of the final
 state comes from the caller's loss.
 
 Covered: the collocated von Karman step_pure with upwind RK3/RK2, a fixed dt
-and the parity V-cycle (the configuration the reference's rollouts use).
+and the parity V-cycle (the configuration the reference's rollouts use), and
+the collocated GUI step without LES (hyperviscosity and either wall
+condition), the step the WIP optimizer differentiates.
 Cotangents returned: the initial u, v; the SDF (through the Brinkman chi,
 when one is given); nu and U_inf.
 """
@@ -27,7 +29,7 @@ from ._lib import check, lib
 from .params import SimState, StepConfig
 from .solver import Plan, _f32, _ptr, _stream
 
-__all__ = ["StepVjp", "step_pure_vjp", "differentiable_rollout", "rollout_vjp"]
+__all__ = ["StepVjp", "step_pure_vjp", "gui_step_vjp", "differentiable_rollout", "rollout_vjp"]
 
 
 def _config(nx, ny, dx, dy, nu, U_inf, dt, has_sdf, v_cycles=1, fast_mode=False,
@@ -108,6 +110,34 @@ def step_pure_vjp(state: SimState, mask, sdf, dx, dy, nu, U_inf, g_u, g_v, g_p=N
     op = StepVjp(cfg, u.device)
     op.prepare(mask, sdf, stream)
     gu, gv = op(u, state.v, mask, g_u, g_v, g_p, stream=stream)
+    sc = op.gscal.cpu()
+    return {"u": gu.clone(), "v": gv.clone(), "sdf": op.gsdf.clone() if sdf is not None else None,
+            "nu": float(sc[0]), "U_inf": float(sc[1])}
+
+
+def gui_step_vjp(u, v, mask, dt, g_u, g_v, g_p=None, *, sdf=None, dx, dy, nu, U_inf=1.0,
+                 nu_hyper_ratio=0.0, slip_walls=True, fast_mode=False, brinkman_eta=1e-4,
+                 multigrid_v_cycles=5, stream=None) -> dict:
+    """Reverse mode of the collocated GUI step without LES
+    (BaselineSolver._step, step_handlers.py:62-185; the step the WIP
+    optimizer scans under jax.grad, inverse_design_WIP/optimizer_autodiff.py
+    :113-205), with StepHandler's keywords: the cotangents of u, v, the SDF
+    (None without one), nu and U_inf from those of the new u, v and p."""
+    u = _f32(u, "u")
+    nx, ny = u.shape
+    _f32(v, "v", (nx, ny))
+    _f32(mask, "mask", (nx, ny))
+    if sdf is not None:
+        _f32(sdf, "sdf", (nx, ny))
+    cfg = StepConfig(nx=nx, ny=ny, dx=float(dx), dy=float(dy), nu=float(nu), U_inf=float(U_inf),
+                     grid_type="collocated", flow_type="von_karman", variant="gui",
+                     use_les=False, advection_scheme="upwind", fast_mode=bool(fast_mode),
+                     slip_walls=bool(slip_walls), brinkman_eta=float(brinkman_eta),
+                     nu_hyper_ratio=float(nu_hyper_ratio), v_cycles=int(multigrid_v_cycles),
+                     mg_mode="parity", warm_start=False, has_sdf=sdf is not None, dt=float(dt))
+    op = StepVjp(cfg, u.device)
+    op.prepare(mask, sdf, stream)
+    gu, gv = op(u, v, mask, g_u, g_v, g_p, stream=stream)
     sc = op.gscal.cpu()
     return {"u": gu.clone(), "v": gv.clone(), "sdf": op.gsdf.clone() if sdf is not None else None,
             "nu": float(sc[0]), "U_inf": float(sc[1])}

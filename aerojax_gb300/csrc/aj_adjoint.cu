@@ -129,21 +129,26 @@ __device__ __forceinline__ float grad_T(const float* __restrict__ g, long s, int
 // cj(ny-1) = ny-2) and v(i, j) copies v(ci(i), j) (0 < j < ny-1); the inlet
 // row and the wall columns of v are constants.  Each output may be weighted
 // by its hard mask (the correction's last mask, step.py:396-397).
+// With walls = false the wall columns of u are constants too (no-slip: the
+// GUI step's correction, step_handlers.py:143-161, and the predictor with
+// slip_walls off).
 template <bool MASKED>
 __device__ __forceinline__ void bc_gather_T(const float* __restrict__ gu_o,
                                             const float* __restrict__ gv_o,
                                             const float* __restrict__ mask, int a, int b, int nx,
-                                            int ny, float& gu, float& gv) {
+                                            int ny, bool walls, float& gu, float& gv) {
   gu = 0.f;
   gv = 0.f;
   if (!interior(a, b, nx, ny)) return;
   const int nrow = a == nx - 2 ? 2 : 1;
   for (int r = 0; r < nrow; ++r) {
     const long base = (long)(r == 0 ? a : nx - 1) * ny;
-    auto take = [&](const float* g, long q) { return MASKED ? (live_at(mask, q) ? ldg(g + q) : 0.f) : ldg(g + q); };
+    auto take = [&](const float* g, long q) {
+      return MASKED ? (live_at(mask, q) ? ldg(g + q) : 0.f) : ldg(g + q);
+    };
     gu += take(gu_o, base + b);
-    if (b == 1) gu += take(gu_o, base);
-    if (b == ny - 2) gu += take(gu_o, base + ny - 1);
+    if (walls && b == 1) gu += take(gu_o, base);
+    if (walls && b == ny - 2) gu += take(gu_o, base + ny - 1);
     gv += take(gv_o, base + b);
   }
 }
@@ -153,12 +158,15 @@ struct AdjCorr {
   const float *gu_o, *gv_o, *gp_o, *mask;
   float *gus, *gvs, *gdpx, *gdpy, *pbar;
   const DevScalars* sc;
-  int nx, ny;
+  int nx, ny, gui;
   float idx, idy, h2x, h2y, thresh;
 };
 
-// cotangents of u*, v* and of the projected gradient at source (a, b)
-// (step.py:341-397 reversed)
+// cotangents of u*, v* and of the (projected) gradient at source (a, b):
+// step_pure, step.py:341-397 reversed (slip-wall copies, a hard mask before
+// and after the boundary rows, the interface projection); the GUI step,
+// step_handlers.py:128-183 reversed (no-slip walls, the inlet corners
+// excluded, one hard mask at the end, no projection)
 __global__ void __launch_bounds__(256) k_adj_correct(AdjCorr c) {
   pdl_wait();
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -167,12 +175,17 @@ __global__ void __launch_bounds__(256) k_adj_correct(AdjCorr c) {
   if (i >= nx || j >= ny) return;
   const long k = (long)i * ny + j;
   float gu, gv;
-  bc_gather_T<true>(c.gu_o, c.gv_o, c.mask, i, j, nx, ny, gu, gv);
-  if (!live_at(c.mask, k)) gu = gv = 0.f;                      // step.py:348-349
+  bc_gather_T<true>(c.gu_o, c.gv_o, c.mask, i, j, nx, ny, !c.gui, gu, gv);
+  if (!c.gui && !live_at(c.mask, k)) gu = gv = 0.f;            // step.py:348-349
   c.gus[k] = gu;
   c.gvs[k] = gv;
   const float dt = c.sc->dt_corr;
   float ax = -dt * gu, ay = -dt * gv;                           // (row 0: gu = 0, :341)
+  if (c.gui) {
+    c.gdpx[k] = ax;
+    c.gdpy[k] = ay;
+    return;
+  }
   const float dmx = gx_nonper(c.mask, i, j, nx, ny, c.idx, c.h2x);
   const float dmy = gy_nonper(c.mask, i, j, ny, c.idy, c.h2y);
   const float gm = sqrtf(dmx * dmx + dmy * dmy);
@@ -365,14 +378,15 @@ __global__ void __launch_bounds__(256) k_adj_prolong(const float* __restrict__ g
 }
 
 // ------------------------------------------------------------------ rhs
-// rhs = (div * mask)/dt with b[-1] = 0 (step.py:199, multigrid_solver.py:75-77);
+// rhs = (div * mask)/dt (step.py:199; the GUI step: div/dt,
+// step_handlers.py:98) with b[-1] = 0 (multigrid_solver.py:75-77);
 // div = central differences on the interior (operators.py:81-96): adds the
 // transpose to the predictor-output cotangent
 __global__ void __launch_bounds__(256) k_adj_div(const float* __restrict__ gb0,
                                                  const float* __restrict__ mask,
                                                  float* __restrict__ gus, float* __restrict__ gvs,
                                                  const DevScalars* sc, int nx, int ny, float h2x,
-                                                 float h2y) {
+                                                 float h2y, int rhs_mask) {
   pdl_wait();
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = blockIdx.y * blockDim.y + threadIdx.y;
@@ -381,7 +395,7 @@ __global__ void __launch_bounds__(256) k_adj_div(const float* __restrict__ gb0,
   auto dv = [&](int a, int b) -> float {
     if (!interior(a, b, nx, ny)) return 0.f;                  // (a <= nx-2: never the zeroed row)
     const long q = (long)a * ny + b;
-    return (ldg(gb0 + q) * ldg(mask + q)) / dt;
+    return rhs_mask ? (ldg(gb0 + q) * ldg(mask + q)) / dt : ldg(gb0 + q) / dt;   // GUI: div/dt
   };
   const long k = (long)i * ny + j;
   gus[k] += h2x * (dv(i - 1, j) - dv(i + 1, j));
@@ -402,12 +416,16 @@ struct AdjRk {
   double* part;                    // per-block d/d nu
   const float* mask;
   const DevScalars* sc;
-  int nx, ny, last;
+  int nx, ny, last, slip;
   float idx, idy, idx2, idy2, nu, inv_eta, cn, sdf_fac;
+  float nuh;                       // nu * nu_hyper_ratio * dx * dy (hyperviscosity)
+  float nuh_fac;                   // nu_hyper_ratio * dx * dy
 };
 
 // cotangent of the final combination x_n / den, through the predictor's hard
-// mask and boundary rows (rk3_simple_new.py:332-337, 262-275; step.py:182-191)
+// mask and boundary rows (rk3_simple_new.py:332-337, 262-275, slip or
+// no-slip walls; step_pure's second pass, step.py:182-191, composes to the
+// first)
 __global__ void __launch_bounds__(256) k_adj_rk_out(AdjRk a) {
   pdl_wait();
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -416,7 +434,7 @@ __global__ void __launch_bounds__(256) k_adj_rk_out(AdjRk a) {
   if (i >= nx || j >= ny) return;
   const long k = (long)i * ny + j;
   float gu, gv;
-  bc_gather_T<false>(a.gus, a.gvs, nullptr, i, j, nx, ny, gu, gv);
+  bc_gather_T<false>(a.gus, a.gvs, nullptr, i, j, nx, ny, a.slip, gu, gv);
   if (!live_at(a.mask, k)) gu = gv = 0.f;
   const float dt = a.sc->dt;
   const float rden = 1.f / (1.f + dt * ldg(a.chi + k) * a.inv_eta);
@@ -439,6 +457,7 @@ __global__ void __launch_bounds__(256) k_adj_rk_out(AdjRk a) {
 // combination.  For target cell c the upwind difference of cell q reads
 // +f(q) - f(W(q)) when its velocity is positive, else -f(q) + f(E(q)): the
 // gather visits q = c and its four neighbours.
+template <bool HYPER>
 __global__ void __launch_bounds__(256) k_adj_rk_stage(AdjRk a) {
   pdl_wait();
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -496,6 +515,27 @@ __global__ void __launch_bounds__(256) k_adj_rk_stage(AdjRk a) {
     const float lv = (vxp + vxm - 2.f * V) * a.idx2 + (vyp + vym - 2.f * V) * a.idy2;
     // exact products, summed in double-FP32 (the sum cancels heavily)
     nub = df_add(two_prod(ku, lu), two_prod(kv, lv));
+    if (HYPER) {
+      // - nu nuh_fac lap(lap(w)) (rk3_simple_new.py:307-312, the edge
+      // Laplacian of the edge Laplacian, as the forward evaluates it): its
+      // own transpose; lap at the clamped neighbours of (i, j)
+      auto lap = [&](const float* __restrict__ f, int ii, int jj) {
+        const int p1 = ii < nx - 1 ? ii + 1 : nx - 1, m1 = ii > 0 ? ii - 1 : 0;
+        const int q1 = jj < ny - 1 ? jj + 1 : ny - 1, n1 = jj > 0 ? jj - 1 : 0;
+        const float c0 = ldg(f + (long)ii * ny + jj);
+        return (ldg(f + (long)p1 * ny + jj) + ldg(f + (long)m1 * ny + jj) - 2.f * c0) * a.idx2 +
+               (ldg(f + (long)ii * ny + q1) + ldg(f + (long)ii * ny + n1) - 2.f * c0) * a.idy2;
+      };
+      auto bih = [&](const float* __restrict__ f) {
+        const float l0 = lap(f, i, j);
+        return (lap(f, ip, j) + lap(f, im, j) - 2.f * l0) * a.idx2 +
+               (lap(f, i, jp) + lap(f, i, jm) - 2.f * l0) * a.idy2;
+      };
+      gu -= a.nuh * bih(a.kin_u);
+      gv -= a.nuh * bih(a.kin_v);
+      nub = df_add(nub, df_add(two_prod(ku, -a.nuh_fac * bih(a.wu)),
+                               two_prod(kv, -a.nuh_fac * bih(a.wv))));
+    }
     const float dt = a.sc->dt;
     if (!a.last) {
       const float rden = 1.f / (1.f + dt * ldg(a.chi + k) * a.inv_eta);
@@ -529,10 +569,14 @@ __global__ void __launch_bounds__(256) k_adj_rk_stage(AdjRk a) {
 // summed in a fixed order and added to gscal[0], gscal[1]
 // (four independent accumulators per thread keep four loads in flight: one
 // accumulator left the block waiting on one partial at a time, 28 us)
+// The inlet rows: the correction's final row 0 where live (the GUI step
+// leaves the two corners on the walls: corr_walls = 0) and the predictor
+// output's row 0 (with no-slip walls its two corners are 0: pred_walls = 0).
 __global__ void __launch_bounds__(1024) k_adj_scalars(const double* __restrict__ part, int nparts,
                                                       const float* __restrict__ gu_o,
                                                       const float* __restrict__ gus,
                                                       const float* __restrict__ mask, int ny,
+                                                      int corr_walls, int pred_walls,
                                                       double* gscal) {
   pdl_wait();
   const int bd = blockDim.x;
@@ -548,8 +592,9 @@ __global__ void __launch_bounds__(1024) k_adj_scalars(const double* __restrict__
   for (; q < nparts; q += bd) s0 += part[q];
   double s = (s0 + s1) + (s2 + s3);
   for (int q = threadIdx.x; q < ny; q += blockDim.x) {
-    u += (double)ldg(gus + q);
-    if (live_at(mask, q)) u += (double)ldg(gu_o + q);
+    const bool wall = q == 0 || q == ny - 1;
+    if (pred_walls || !wall) u += (double)ldg(gus + q);
+    if ((corr_walls || !wall) && live_at(mask, q)) u += (double)ldg(gu_o + q);
   }
   s = block_sum(s);
   u = block_sum(u);
@@ -647,6 +692,7 @@ int launch_step_vjp(const AjStepParams& p, const Layout& L, void* ws, void* aws,
   c.h2x = (float)(1.0 / (2.0 * p.dx));
   c.h2y = (float)(1.0 / (2.0 * p.dy));
   c.thresh = (float)(0.1 / p.dx);
+  c.gui = p.variant == AJ_VARIANT_GUI;
   launch_pdl(true, k_adj_correct, grd, blk, 0, st, c);
   launch_pdl(true, k_adj_grad, grd, blk, 0, st, c);
   // ---- multigrid, reversed (cycles from the last to the first)
@@ -698,7 +744,8 @@ int launch_step_vjp(const AjStepParams& p, const Layout& L, void* ws, void* aws,
   }
   // ---- rhs and divergence, reversed
   launch_pdl(true, k_adj_div, grd, blk, 0, st, F(A.GB[0]), mask, F(A.gus), F(A.gvs), sc, nx, ny,
-             (float)(1.0 / (2.0 * p.dx)), (float)(1.0 / (2.0 * p.dy)));
+             (float)(1.0 / (2.0 * p.dx)), (float)(1.0 / (2.0 * p.dy)),
+             (int)(p.variant == AJ_VARIANT_PURE));
   // ---- predictor, reversed
   const bool rk2 = p.fast_mode != 0;
   AdjRk r{};
@@ -727,6 +774,10 @@ int launch_step_vjp(const AjStepParams& p, const Layout& L, void* ws, void* aws,
   r.inv_eta = (float)(1.0 / p.brinkman_eta);
   r.sdf_fac = (float)(-1.0 / (0.1 * p.dx));
   r.cn = rk2 ? 0.5f : (float)(2.0 / 3.0);
+  r.slip = p.slip_walls;
+  r.nuh_fac = (float)(p.nu_hyper_ratio * p.dx * p.dy);
+  r.nuh = (float)p.nu * r.nuh_fac;
+  const bool hyper = p.nu_hyper_ratio > 0.0;
   if (branch && cudaStreamWaitEvent(st, fk->join, 0) != cudaSuccess) return AJ_ERR_CUDA;
   launch_pdl(true, k_adj_rk_out, grd, blk, 0, st, r);
   // stage states: RK3 w3 = sB, w2 = sA; RK2 w2 = sA; stage 1 is the input
@@ -752,12 +803,14 @@ int launch_step_vjp(const AjStepParams& p, const Layout& L, void* ws, void* aws,
     r.gv = gv;
     r.gsdf = (s == 1 && p.has_sdf) ? gsdf : nullptr;
     r.part = at<double>(aws, A.part) + (size_t)(nst - s) * A.nblk;
-    launch_pdl(true, k_adj_rk_stage, grd, blk, 0, st, r);
+    if (hyper) launch_pdl(true, k_adj_rk_stage<true>, grd, blk, 0, st, r);
+    else launch_pdl(true, k_adj_rk_stage<false>, grd, blk, 0, st, r);
     cur = 1 - cur;
   }
   if (gscal)
     launch_pdl(true, k_adj_scalars, dim3(1), dim3(1024), 0, st, at<double>(aws, A.part),
-               nst * A.nblk, gu_o, F(A.gus), mask, ny, gscal);
+               nst * A.nblk, gu_o, F(A.gus), mask, ny, (int)(p.variant == AJ_VARIANT_PURE),
+               (int)(p.slip_walls != 0), gscal);
   return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
 }
 

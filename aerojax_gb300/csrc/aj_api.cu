@@ -544,13 +544,15 @@ int32_t aj_step_host(const AjStepParams* prm, const float* h_u, const float* h_v
   });
 }
 
-// the configurations the reverse pass covers: the collocated step_pure with
-// the von Karman boundaries, upwind RK3/RK2, a fixed dt and the parity V-cycle
+// the configurations the reverse pass covers: the collocated step_pure and
+// GUI step (without LES) with the von Karman boundaries, upwind RK3/RK2, a
+// fixed dt and the parity V-cycle
 static int vjp_params_ok(const AjStepParams& p) {
-  if (p.variant != AJ_VARIANT_PURE || p.grid_type != AJ_GRID_COLLOCATED ||
-      p.flow_type != AJ_FLOW_VON_KARMAN || p.mg_mode != AJ_MG_PARITY ||
-      p.advection != AJ_ADV_UPWIND || p.cfl_dt || p.warm_start || p.nn_factor > 0)
+  if (p.grid_type != AJ_GRID_COLLOCATED || p.flow_type != AJ_FLOW_VON_KARMAN ||
+      p.mg_mode != AJ_MG_PARITY || p.advection != AJ_ADV_UPWIND || p.cfl_dt || p.warm_start ||
+      p.nn_factor > 0)
     return AJ_ERR_PARAM;
+  if (p.variant == AJ_VARIANT_GUI && p.les_model != AJ_LES_NONE) return AJ_ERR_PARAM;
   if (p.nx < 3 || p.ny < 3) return AJ_ERR_SHAPE;
   return AJ_OK;
 }

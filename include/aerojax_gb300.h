@@ -142,8 +142,11 @@ int32_t aj_step(const AjStepParams* prm, const float* u, const float* v, const f
    evaluates through the reference's differentiable rollouts
    (solver/solver.py:34-75 differentiable_rollout, :78-114 design_loss /
    grad_design_loss; inverse_design_WIP/optimizer_autodiff.py:113-205).
-   Covers the collocated von Karman step_pure with upwind RK3/RK2, a fixed dt
-   (cfl_dt = 0) and the parity V-cycle (AJ_ERR_PARAM otherwise).
+   Covers the collocated von Karman step with upwind RK3/RK2, a fixed dt
+   (cfl_dt = 0) and the parity V-cycle: variant PURE (step_pure) and variant
+   GUI without LES (BaselineSolver._step, step_handlers.py:62-185: the step
+   the WIP optimizer scans, hyperviscosity and either wall condition);
+   AJ_ERR_PARAM otherwise.
    Inputs: the step's inputs u, v (nx*ny) and the mask of aj_prepare on this
    workspace (prepared with the SDF when has_sdf), and the cotangents of the
    step's outputs gu_out, gv_out and gp_out (nullable: zero).  Writes the

@@ -112,10 +112,10 @@ def test_no_cpu_fallback_without_library(monkeypatch, tmp_path):
 
 
 def test_step_vjp_covers_the_rollout_configuration_only(L):
-    """aj_step_vjp's host checks: the collocated von Karman step_pure with
-    upwind RK3/RK2, a fixed dt and the parity V-cycle; anything else gets no
-    workspace size and no kernel count (aj_step_vjp itself returns
-    AJ_ERR_PARAM)."""
+    """aj_step_vjp's host checks: the collocated von Karman step_pure, or the
+    GUI step without LES, with upwind RK3/RK2, a fixed dt and the parity
+    V-cycle; anything else gets no workspace size and no kernel count
+    (aj_step_vjp itself returns AJ_ERR_PARAM)."""
     from dataclasses import replace
     from aerojax_gb300.adjoint import _config
     from aerojax_gb300.solver import make_params
@@ -124,7 +124,11 @@ def test_step_vjp_covers_the_rollout_configuration_only(L):
         p = make_params(ok)
         assert L.aj_step_vjp_workspace_size(ctypes.byref(p)) > 0
         assert L.aj_step_vjp_kernel_count(ctypes.byref(p)) > 0
-    for bad in (replace(base, grid_type="mac", variant="gui"), replace(base, variant="gui"),
+    gui = replace(base, variant="gui", nu_hyper_ratio=0.05, slip_walls=False)
+    for ok in (gui, replace(gui, fast_mode=True, nu_hyper_ratio=0.0)):
+        assert L.aj_step_vjp_workspace_size(ctypes.byref(make_params(ok))) > 0
+    for bad in (replace(base, grid_type="mac", variant="gui"),
+                replace(gui, use_les=True, les_model="smagorinsky"),
                 replace(base, mg_mode="converge"), replace(base, cfl_dt=True),
                 replace(base, advection_scheme="weno5"), replace(base, warm_start=True)):
         p = make_params(bad)

@@ -138,3 +138,29 @@ def test_rollout_vjp_matches_oracle(dev):
     assert _rel(got["sdf"].cpu(), ref["sdf"]) <= 2e-4
     assert _scalar_ok(got["nu"], ref, "nu", 2e-4), (got["nu"], ref["nu"], ref["nu_abs"])
     assert _scalar_ok(got["U_inf"], ref, "U_inf", 2e-4), (got["U_inf"], ref["U_inf"])
+
+
+@pytest.mark.parametrize("fast,hyper,slip,use_sdf,cycles", [
+    (False, 0.05, True, True, 2), (True, 0.0, False, True, 1), (False, 0.05, False, False, 5)])
+def test_gui_step_vjp_matches_oracle(dev, fast, hyper, slip, use_sdf, cycles):
+    """The collocated GUI step without LES (hyperviscosity, both wall
+    conditions): every cotangent within 1e-4 of the oracle's at 128x64."""
+    from oracle import adjoint_np as A
+    from aerojax_gb300 import adjoint as ADJ
+    nx, ny = 128, 64
+    u, v, mask, s, rng = _case(nx, ny, 14)
+    sdf = s if use_sdf else None
+    gu, gv, gp = (rng.standard_normal((nx, ny)).astype(np.float32) for _ in range(3))
+    kw = dict(v_cycles=cycles, fast_mode=fast, nu_hyper_ratio=hyper, slip_walls=slip,
+              brinkman_eta=1e-3)
+    ref = A.step_gui_vjp(u, v, DT, mask, sdf, DX, DX, NU, U, gu, gv, gp, **kw)
+    got = ADJ.gui_step_vjp(_t(u, dev), _t(v, dev), _t(mask, dev), DT, _t(gu, dev), _t(gv, dev),
+                           _t(gp, dev), sdf=None if sdf is None else _t(sdf, dev), dx=DX, dy=DX,
+                           nu=NU, U_inf=U, nu_hyper_ratio=hyper, slip_walls=slip,
+                           fast_mode=fast, brinkman_eta=1e-3, multigrid_v_cycles=cycles)
+    assert _rel(got["u"].cpu(), ref["u"]) <= 1e-4
+    assert _rel(got["v"].cpu(), ref["v"]) <= 1e-4
+    if use_sdf:
+        assert _rel(got["sdf"].cpu(), ref["sdf"]) <= 1e-4
+    assert _scalar_ok(got["nu"], ref, "nu", 1e-4), (got["nu"], ref["nu"], ref["nu_abs"])
+    assert _scalar_ok(got["U_inf"], ref, "U_inf", 1e-4), (got["U_inf"], ref["U_inf"])
