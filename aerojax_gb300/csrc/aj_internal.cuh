@@ -252,7 +252,7 @@ int launch_les(const AjStepParams& p, const Layout& L, void* ws, int model, cons
 int launch_cfl(const AjStepParams& p, void* ws, const float* u, const float* v,
                float* dt_out, cudaStream_t st);
 int launch_set_dt(const AjStepParams& p, void* ws, cudaStream_t st);
-bool parity_coarsest_fused(const Layout& L);   // coarsest sweeps in one block (aj_pressure.cu)
+bool parity_coarsest_fused(const Layout& L);   // coarsest sweeps on one cluster (aj_pressure.cu)
 // reverse mode of the collocated step_pure (aj_adjoint.cu)
 size_t step_vjp_workspace(const AjStepParams& p, const Layout& L);
 int launch_step_vjp(const AjStepParams& p, const Layout& L, void* ws, void* aws, const float* u,

@@ -74,7 +74,7 @@ struct ParJac {
 };
 
 // one undamped Jacobi sweep with edge ghosts (multigrid_solver.py:158-171):
-// the coarsest level's sweeps when they do not fit one block
+// the coarsest level's sweeps when its bands do not fit the cluster's blocks
 __global__ void __launch_bounds__(256) k_par_jacobi(ParJac a) {
   if (a.skip && *a.skip) return;
   int j = blockIdx.x * blockDim.x + threadIdx.x;
