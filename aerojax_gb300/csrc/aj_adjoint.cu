@@ -819,7 +819,7 @@ int step_vjp_kernel_count(const AjStepParams& p, const Layout& L) {
   int n = 1 + nst;                                  // dt + forward predictor stages
   const bool fused = parity_coarsest_fused(L);
   if (p.v_cycles > 1)                               // rhs, forward solve
-    n += 1 + 1 + p.v_cycles * (2 * L.nlev + (fused ? 1 : 10) + 1);
+    n += 1 + 1 + p.v_cycles * (2 * L.nlev + (fused ? 1 : 10));
   n += 2;                                           // correction, gradient
   n += p.v_cycles * (3 * L.nlev + (fused ? 1 : 10));  // reversed V-cycles
   n += 1 + 1 + nst + 1;                             // divergence, output, stages, scalars

@@ -702,7 +702,7 @@ int32_t aj_kernel_count(const AjStepParams* prm, int32_t cycles) {
   n += p.fast_mode ? 2 : 3;                                     // predictor stages
   n += 1;                                                       // rhs
   if (p.mg_mode == AJ_MG_PARITY) {
-    int per_cycle = 2 * L.nlev + (parity_coarsest_fused(L) ? 1 : 10) + 1;   // levels, coarsest, check
+    int per_cycle = 2 * L.nlev + (parity_coarsest_fused(L) ? 1 : 10);   // levels, coarsest
     n += 1 + p.v_cycles * per_cycle;                            // begin + cycles
   } else {
     int body = 2 * L.lc + 1 + (L.ld > 0 ? 2 : 0);               // downs, coarse solve, ups

@@ -93,6 +93,7 @@ __global__ void __launch_bounds__(256) k_par_jacobi(ParJac a) {
 }
 
 __global__ void k_par_begin(DevScalars* sc) {
+  sc->red_count = 0u;
   sc->mg_skip = 0;
   sc->mg_cycles = 0;
   sc->acc[0] = 0.0;
@@ -101,8 +102,9 @@ __global__ void k_par_begin(DevScalars* sc) {
 }
 
 // converged = sum r^2 dx dy < tol^2 (multigrid_solver.py:222-232)
-__global__ void k_par_check(DevScalars* sc, double dxdy, double tol2, int first) {
-  if (sc->mg_skip) return;
+// converged = sum r^2 dx dy < tol^2 (multigrid_solver.py:222-232), run by the
+// last block of the level-0 up kernel once every block's norm is in
+__device__ void par_check_body(DevScalars* sc, double dxdy, double tol2, int first) {
   if (first) sc->bnorm = sqrt(sc->acc[1]);
   double s = sc->acc[0];
   sc->mg_cycles += 1;
@@ -183,6 +185,7 @@ struct ParTile {
   const int* skip;
   int n, m, nc, mc, zero_last, mac_outlet, also_b;
   float ax, ay, den;
+  double dxdy, tol2;  // up on level 0: the early-exit test
 };
 // Output tiles: 16 x 64 on the finest level (4 cells per thread: fewer halo
 // cells per output, more loads in flight), 8 x 32 on the coarser ones (their
@@ -329,9 +332,18 @@ __global__ void __launch_bounds__(kPtThreads) k_par_up(ParTile a) {
   }
   const double s = block_sum_df(rr);
   const double sb = a.also_b ? block_sum_df(bb) : 0.0;
+  __shared__ int am_last;
   if (tid == 0) {
     atomicAdd(&a.sc->acc[0], s);
     if (a.also_b) atomicAdd(&a.sc->acc[1], sb);
+    __threadfence();
+    am_last = atomicAdd(&a.sc->red_count, 1u) == gridDim.x * gridDim.y - 1;
+  }
+  __syncthreads();
+  if (am_last && tid == 0) {   // every block's sums are in: the early-exit test
+    __threadfence();
+    a.sc->red_count = 0u;
+    par_check_body(a.sc, a.dxdy, a.tol2, a.also_b);
   }
   }
 }
@@ -436,7 +448,8 @@ static int parity_solve(const AjStepParams& p, const Layout& L, void* ws, const 
       }
     }
     // up the V: T + P(coarser X), two post-sweeps, into X; level 0 also
-    // forms the residual norm of the early exit (multigrid_solver.py:222-232)
+    // forms the residual norm and its last block runs the early-exit test
+    // (multigrid_solver.py:222-232)
     for (int l = nl - 1; l >= 0; --l) {
       ParTile a{};
       a.xin = T(l);
@@ -456,10 +469,11 @@ static int parity_solve(const AjStepParams& p, const Layout& L, void* ws, const 
       a.ax = ax;
       a.ay = ay;
       a.den = den;
+      a.dxdy = p.dx * p.dy;
+      a.tol2 = tol * tol;
       if (l == 0) k_par_up<16, 64, true><<<tile_grid(l), kPtThreads, 0, st>>>(a);
       else k_par_up<8, 32, false><<<tile_grid(l), kPtThreads, 0, st>>>(a);
     }
-    k_par_check<<<1, 1, 0, st>>>(sc, p.dx * p.dy, tol * tol, cyc == 0);
   }
   return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
 }
