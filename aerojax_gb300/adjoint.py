@@ -156,6 +156,35 @@ def _rollout_config(state, params):
     return cfg, sdf
 
 
+# Plans, staging buffers and reverse-pass operators of the rollouts, kept per
+# configuration: repeated rollouts replay the graphs captured by the first.
+_FWD: dict = {}
+_REV: dict = {}
+
+
+def _forward_plan(cfg: StepConfig, device):
+    key = (repr(replace(cfg, dt=0.0)), str(device))
+    ent = _FWD.get(key)
+    if ent is None:
+        plan = Plan(cfg, device)
+        shape = (cfg.nx, cfg.ny)
+        e = lambda: torch.empty(shape, dtype=torch.float32, device=device)
+        ent = (plan, [(e(), e()), (e(), e())], e())
+        _FWD[key] = ent
+    ent[0].params.dt = float(cfg.dt)
+    return ent
+
+
+def _reverse_op(cfg: StepConfig, device) -> "StepVjp":
+    key = (repr(replace(cfg, dt=0.0)), str(device))
+    op = _REV.get(key)
+    if op is None:
+        op = StepVjp(cfg, device)
+        _REV[key] = op
+    op.plan.params.dt = float(cfg.dt)
+    return op
+
+
 def differentiable_rollout(initial_state: SimState, mask, params: dict, num_steps: int = 200,
                            stream=None):
     """solver/solver.py:34-75 on the GPU: ``num_steps`` step_pure calls with
@@ -164,15 +193,14 @@ def differentiable_rollout(initial_state: SimState, mask, params: dict, num_step
     stacked like lax.scan's output, [num_steps, nx, ny] each."""
     cfg, sdf = _rollout_config(initial_state, params)
     dev = initial_state.u.device
-    plan = Plan(cfg, dev)
+    plan, bufs, p = _forward_plan(cfg, dev)
     plan.prepare(mask, sdf, stream)
     nx, ny = cfg.nx, cfg.ny
     hu = torch.empty((num_steps, nx, ny), dtype=torch.float32, device=dev)
     hv = torch.empty_like(hu)
     # fixed ping-pong buffers: one cached graph serves every step
-    bufs = [(initial_state.u.clone(), initial_state.v.clone()),
-            (torch.empty_like(initial_state.u), torch.empty_like(initial_state.v))]
-    p = torch.empty((nx, ny), dtype=torch.float32, device=dev)
+    bufs[0][0].copy_(initial_state.u)
+    bufs[0][1].copy_(initial_state.v)
     cur = 0
     for k in range(num_steps):
         (u, v), (uo, vo) = bufs[cur], bufs[1 - cur]
@@ -185,7 +213,8 @@ def differentiable_rollout(initial_state: SimState, mask, params: dict, num_step
         cur = 1 - cur
     prev_u = hu[-2] if num_steps > 1 else initial_state.u
     prev_v = hv[-2] if num_steps > 1 else initial_state.v
-    final = SimState(u=hu[-1], v=hv[-1], p=p, u_prev=prev_u, v_prev=prev_v, c=initial_state.c,
+    final = SimState(u=hu[-1], v=hv[-1], p=p.clone(), u_prev=prev_u, v_prev=prev_v,
+                     c=initial_state.c,
                      dt=initial_state.dt, iteration=initial_state.iteration + num_steps,
                      grid_type="collocated", integral=initial_state.integral,
                      prev_error=initial_state.prev_error)
@@ -203,7 +232,7 @@ def rollout_vjp(initial_state: SimState, mask, params: dict, num_steps: int, g_u
     if history is None:
         _, history = differentiable_rollout(initial_state, mask, params, num_steps, stream)
     hu, hv = history
-    op = StepVjp(cfg, initial_state.u.device)
+    op = _reverse_op(cfg, initial_state.u.device)
     op.prepare(mask, sdf, stream)
     op.zero_grad()
     gA = (op.g_in[0], op.g_in[1])

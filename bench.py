@@ -728,6 +728,25 @@ def adjoint_workload(args, dev, st):
     fwd_ms = timed(fwd, args.steps)
     vjp_ms = timed(vjp, args.steps)
     kc = int(L.aj_step_vjp_kernel_count(ctypes.byref(P.params)))
+    # a gradient through a rollout, as grad_design_loss runs it
+    # (solver/solver.py:34-114): the forward scan keeping the history, then the
+    # reverse scan, through the public Python API (one graph launch per step
+    # each, plus the staging copies); no L2 flush inside the rollout
+    from aerojax_gb300 import adjoint as ADJ
+    from aerojax_gb300.params import SimState
+    n_roll = 50
+    state = SimState(u=u, v=v, p=None, u_prev=None, v_prev=None, c=None, dt=dt, iteration=0)
+    params = {"dx": dx, "dy": dx, "nu": 1e-3, "U_inf": 1.0, "sdf": sdf}
+    ADJ.rollout_vjp(state, mask, params, 3, op.g_in[0], op.g_in[1])   # warm-up (graphs)
+    torch.cuda.synchronize()
+    r0, r1, r2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    r0.record(st)
+    _, hist = ADJ.differentiable_rollout(state, mask, params, n_roll)
+    r1.record(st)
+    ADJ.rollout_vjp(state, mask, params, n_roll, op.g_in[0], op.g_in[1], history=hist)
+    r2.record(st)
+    torch.cuda.synchronize()
+    roll_fwd_ms, roll_rev_ms = r0.elapsed_time(r1) / n_roll, r1.elapsed_time(r2) / n_roll
     hbm = 6800.0
     if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")):
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -754,6 +773,11 @@ def adjoint_workload(args, dev, st):
                    "gradients": ["u", "v", "sdf", "nu", "U_inf"],
                    "forward_ms_per_step": fwd_ms, "vjp_over_forward": vjp_ms / fwd_ms,
                    "kernels_per_vjp": kc, "algorithmic_bytes_per_cell": VJP_BYTES_PER_CELL,
+                   "rollout": {"steps": n_roll, "forward_ms_per_step": roll_fwd_ms,
+                               "reverse_ms_per_step": roll_rev_ms,
+                               "gradient_mcell_steps_per_s":
+                                   cells / ((roll_fwd_ms + roll_rev_ms) * 1e-3) / 1e6,
+                               "api": "adjoint.differentiable_rollout + adjoint.rollout_vjp"},
                    "achieved_gbs": gbs, "frac_of_measured_hbm": gbs / hbm,
                    "l2": "flushed before every call (256 MiB write outside the timed events)"},
         "cpu_baseline": cpu,
