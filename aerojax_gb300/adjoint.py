@@ -158,29 +158,35 @@ def _rollout_config(state, params):
 
 # Plans, staging buffers and reverse-pass operators of the rollouts, kept per
 # configuration: repeated rollouts replay the graphs captured by the first.
+# Nothing in them carries over from one rollout to the next, so the oldest
+# configuration is dropped beyond _MAX_CACHED.
 _FWD: dict = {}
 _REV: dict = {}
+_MAX_CACHED = 8
+
+
+def _cached(cache: dict, key, make):
+    ent = cache.get(key)
+    if ent is None:
+        while len(cache) >= _MAX_CACHED:
+            cache.pop(next(iter(cache)))
+        ent = make()
+        cache[key] = ent
+    return ent
 
 
 def _forward_plan(cfg: StepConfig, device):
-    key = (repr(replace(cfg, dt=0.0)), str(device))
-    ent = _FWD.get(key)
-    if ent is None:
-        plan = Plan(cfg, device)
+    def make():
         shape = (cfg.nx, cfg.ny)
         e = lambda: torch.empty(shape, dtype=torch.float32, device=device)
-        ent = (plan, [(e(), e()), (e(), e())], e())
-        _FWD[key] = ent
+        return (Plan(cfg, device), [(e(), e()), (e(), e())], e())
+    ent = _cached(_FWD, (repr(replace(cfg, dt=0.0)), str(device)), make)
     ent[0].params.dt = float(cfg.dt)
     return ent
 
 
 def _reverse_op(cfg: StepConfig, device) -> "StepVjp":
-    key = (repr(replace(cfg, dt=0.0)), str(device))
-    op = _REV.get(key)
-    if op is None:
-        op = StepVjp(cfg, device)
-        _REV[key] = op
+    op = _cached(_REV, (repr(replace(cfg, dt=0.0)), str(device)), lambda: StepVjp(cfg, device))
     op.plan.params.dt = float(cfg.dt)
     return op
 
