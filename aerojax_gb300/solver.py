@@ -173,12 +173,18 @@ def run_step_host(plan: Plan, h_u, h_v, mask, h_p=None, h_out=None, net=None, st
         stage = (torch.empty(n, dtype=torch.float32, device=dev),
                  torch.empty(n, dtype=torch.float32, device=dev))
         plan._host_stage = stage
-    for t, name in ((h_u, "h_u"), (h_v, "h_v")):
-        if t.is_cuda or not t.is_pinned():
-            raise ValueError(f"{name} must be a pinned host tensor")
     if h_out is None:
         h_out = (torch.empty_like(h_u).pin_memory(), torch.empty_like(h_v).pin_memory(),
                  torch.empty((cfg.nx, cfg.ny), dtype=torch.float32).pin_memory())
+    # the copies are recorded into the step's graph: every host buffer must be
+    # page-locked
+    named = [(h_u, "h_u"), (h_v, "h_v"), (h_out[0], "h_out[0]"), (h_out[1], "h_out[1]"),
+             (h_out[2], "h_out[2]")]
+    if h_p is not None:
+        named.append((h_p, "h_p"))
+    for t, name in named:
+        if t.is_cuda or not t.is_pinned():
+            raise ValueError(f"{name} must be a pinned host tensor")
     packed = master = None
     if net is not None:   # an aerojax_gb300.nn.WarmStartNet (its packed BF16 weights current)
         packed, master = net.packed.data_ptr(), net.master.data_ptr()
