@@ -143,3 +143,27 @@ def test_shape_error_like_reference(cuda_lib):
     rhs = torch.zeros((100, 64), device="cuda")
     with pytest.raises(ValueError):
         aj.poisson_multigrid(rhs, torch.ones_like(rhs), 0.01, 0.01)
+
+
+def test_step_gui_no_slip_walls_against_oracle(cuda_lib):
+    """The collocated GUI step with no-slip walls (slip_walls=False) and
+    hyperviscosity, which the golden fixtures (slip walls) do not cover,
+    against the oracle's step_gui on a 96x80 cylinder case."""
+    import aerojax_gb300 as aj
+    from oracle import ref_np as R
+    nx, ny, dx, dt = 96, 80, 0.05, 0.004
+    rng = np.random.default_rng(21)
+    X, Y = np.meshgrid((np.arange(nx) + 0.5) * dx, (np.arange(ny) + 0.5) * dx, indexing="ij")
+    sdf = R.sdf_cylinder(X, Y, 1.4, 2.0, 0.4)
+    mask = R.mask_from_sdf(sdf, 0.5 * dx)
+    u = 1.0 + 0.1 * rng.standard_normal((nx, ny))
+    v = 0.1 * rng.standard_normal((nx, ny))
+    kw = dict(nu_hyper_ratio=0.05, slip_walls=False, brinkman_eta=1e-3)
+    ur, vr, pr = R.step_gui(u, v, mask, dt, sdf=sdf, dx=dx, dy=dx, nu=0.02, U_inf=1.0,
+                            v_cycles=3, **kw)
+    h = aj.StepHandler(nx, ny, dx, dx, 0.02, 1.0, grid_type="collocated", use_les=False,
+                       multigrid_v_cycles=3, sdf=T(sdf), dt=dt, **kw)
+    ug, vg, pg = h._step(T(u), T(v), T(mask))
+    assert rel(ug, ur) < TOL
+    assert rel(vg, vr) < TOL
+    assert rel(pg, pr) < TOL
