@@ -22,7 +22,7 @@ FLOW = {"von_karman": 0, "lid_driven_cavity": 1, "taylor_green": 2}
 VARIANT = {"pure": 0, "gui": 1}
 LES = {None: 0, "none": 0, "smagorinsky": 1, "dynamic_smagorinsky": 2}
 ADV = {"upwind": 0, "rk3": 0, "weno5": 1}
-MG = {"parity": 0, "converge": 1}
+MG = {"parity": 0, "converge": 1, "none": 2}
 GEOM = {"cylinder": 1, "naca4": 2, "cyl3_row": 3, "cyl3_tri": 4}
 
 STATUS_NAMES = {0: "AJ_OK", 1: "AJ_ERR_SHAPE", 2: "AJ_ERR_PARAM", 3: "AJ_ERR_NONFINITE",

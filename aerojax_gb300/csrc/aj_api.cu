@@ -80,8 +80,11 @@ int check_params(const AjStepParams& p) {
   if (p.grid_type != AJ_GRID_COLLOCATED && p.grid_type != AJ_GRID_MAC) return AJ_ERR_PARAM;
   if (p.flow_type < AJ_FLOW_VON_KARMAN || p.flow_type > AJ_FLOW_TAYLOR_GREEN) return AJ_ERR_PARAM;
   if (p.les_model < AJ_LES_NONE || p.les_model > AJ_LES_DYNAMIC) return AJ_ERR_PARAM;
-  if (p.mg_mode != AJ_MG_PARITY && p.mg_mode != AJ_MG_CONVERGE) return AJ_ERR_PARAM;
-  if (p.mg_mode == AJ_MG_PARITY) {
+  if (p.mg_mode != AJ_MG_PARITY && p.mg_mode != AJ_MG_CONVERGE && p.mg_mode != AJ_MG_NONE)
+    return AJ_ERR_PARAM;
+  if (p.mg_mode == AJ_MG_NONE) {
+    // predictor / LES workspace: no multigrid shape rules
+  } else if (p.mg_mode == AJ_MG_PARITY) {
     int ml;
     int rc = parity_levels(p.nx, p.ny, p.levels > 0 ? p.levels : 4, &ml);
     if (rc != AJ_OK) return rc;
@@ -140,7 +143,7 @@ bool make_layout(const AjStepParams& p, Layout& L) {
       L.B[l] = take(n * 4);
       if (mac) L.M[l] = take(n * 4);
     }
-  } else {
+  } else if (p.mg_mode == AJ_MG_CONVERGE) {
     int D = converge_depth(p.nx, p.ny);
     L.nlev = D;
     for (int l = 0; l <= D; ++l) {
@@ -179,7 +182,7 @@ bool make_layout(const AjStepParams& p, Layout& L) {
 // effective parameters: step_pure hard-wires slip walls and no hyperviscosity
 // (step.py:177-180) and cannot run on the MAC grid (step.py:348 broadcasts
 // (nx+1, ny) against (nx, ny))
-static AjStepParams normalise(const AjStepParams& in) {
+AjStepParams normalise(const AjStepParams& in) {
   AjStepParams p = in;
   if (p.levels <= 0) p.levels = 4;
   if (p.variant == AJ_VARIANT_PURE) {
@@ -417,11 +420,19 @@ int32_t aj_check_params(const AjStepParams* prm) {
   AjStepParams p = normalise(*prm);
   int rc = check_params(p);
   if (rc != AJ_OK) return rc;
+  if (p.mg_mode == AJ_MG_NONE) return AJ_OK;     // predictor / LES only: any flow type
   if (p.variant == AJ_VARIANT_PURE && p.grid_type == AJ_GRID_MAC) return AJ_ERR_PARAM;
   if (p.flow_type != AJ_FLOW_VON_KARMAN) return AJ_ERR_PARAM;   // step + solver: von Karman
   if (p.mg_mode == AJ_MG_CONVERGE && p.grid_type == AJ_GRID_MAC && p.flow_type != AJ_FLOW_VON_KARMAN)
     return AJ_ERR_PARAM;
   return AJ_OK;
+}
+
+// the parameters of a call that runs a pressure solve
+static int32_t solve_check(const AjStepParams* prm) {
+  int32_t rc = aj_check_params(prm);
+  if (rc != AJ_OK) return rc;
+  return prm->mg_mode == AJ_MG_NONE ? AJ_ERR_PARAM : AJ_OK;
 }
 
 size_t aj_workspace_size(const AjStepParams* prm) {
@@ -452,7 +463,7 @@ int32_t aj_step(const AjStepParams* prm, const float* u, const float* v, const f
                 const float* p_guess, float* u_out, float* v_out, float* p_out, void* ws,
                 size_t bytes, AjStats* stats, void* stream) {
   if (!prm || !u || !v || !mask || !u_out || !v_out || !p_out) return AJ_ERR_PARAM;
-  int rc = aj_check_params(prm);
+  int rc = solve_check(prm);
   if (rc != AJ_OK) return rc;
   AjStepParams p = normalise(*prm);
   if (p.warm_start == AJ_WARM_GUESS && !p_guess) return AJ_ERR_PARAM;
@@ -473,7 +484,7 @@ int32_t aj_step_nn(const AjStepParams* prm, const float* u, const float* v, cons
   if (!prm || !u || !v || !mask || !p_prev || !nn_packed || !nn_master || !u_out || !v_out ||
       !p_out)
     return AJ_ERR_PARAM;
-  int rc = aj_check_params(prm);
+  int rc = solve_check(prm);
   if (rc != AJ_OK) return rc;
   AjStepParams p = normalise(*prm);
   if (p.mg_mode != AJ_MG_CONVERGE || p.nn_factor <= 0) return AJ_ERR_PARAM;
@@ -500,7 +511,7 @@ int32_t aj_step_host(const AjStepParams* prm, const float* h_u, const float* h_v
   if (!prm || !h_u || !h_v || !mask || !h_u_out || !h_v_out || !h_p_out || !d_in || !d_out)
     return AJ_ERR_PARAM;
   if ((nn_packed == nullptr) != (nn_master == nullptr)) return AJ_ERR_PARAM;
-  int rc = aj_check_params(prm);
+  int rc = solve_check(prm);
   if (rc != AJ_OK) return rc;
   AjStepParams p = normalise(*prm);
   if (nn_packed) {
@@ -570,7 +581,7 @@ int32_t aj_step_vjp(const AjStepParams* prm, const float* u, const float* v, con
                     float* gv, float* gsdf, double* gscal, void* ws, size_t bytes, void* aws,
                     size_t adj_bytes, void* stream) {
   if (!prm || !u || !v || !mask || !gu_out || !gv_out || !gu || !gv || !aws) return AJ_ERR_PARAM;
-  int rc = aj_check_params(prm);
+  int rc = solve_check(prm);
   if (rc != AJ_OK) return rc;
   AjStepParams p = normalise(*prm);
   if ((rc = vjp_params_ok(p)) != AJ_OK) return rc;
@@ -608,7 +619,7 @@ int32_t aj_poisson_mg(const AjStepParams* prm, const float* rhs, const float* ma
   AjStepParams p = normalise(*prm);
   int rc = check_params(p);
   if (rc != AJ_OK) return rc;
-  if (p.flow_type != AJ_FLOW_VON_KARMAN) return AJ_ERR_PARAM;
+  if (p.flow_type != AJ_FLOW_VON_KARMAN || p.mg_mode == AJ_MG_NONE) return AJ_ERR_PARAM;
   Layout L;
   make_layout(p, L);
   if ((rc = ws_ok(L, ws, bytes)) != AJ_OK) return rc;
@@ -633,9 +644,8 @@ int32_t aj_les(const AjStepParams* prm, int32_t model, const float* u, const flo
   Layout L;
   AjStepParams q = p;
   q.grid_type = AJ_GRID_COLLOCATED;
-  q.mg_mode = AJ_MG_CONVERGE;   // layout only needs the field buffers
-  q.mg_rtol = 1e-6;
-  q.max_cycles = 1;
+  q.mg_mode = AJ_MG_NONE;       // layout only needs the field buffers
+  q.warm_start = AJ_WARM_ZERO;
   q.cfl_dt = 0;
   q.dt = 1.0;
   if (model == AJ_LES_DYNAMIC) {
@@ -743,7 +753,7 @@ int32_t aj_ensemble_step(int32_t n, const AjStepParams* prms, const float* const
   std::vector<Layout> Ls(n);
   std::string key;
   for (int i = 0; i < n; ++i) {
-    int rc = aj_check_params(&prms[i]);
+    int rc = solve_check(&prms[i]);
     if (rc != AJ_OK) return rc;
     P[i] = normalise(prms[i]);
     if (P[i].warm_start == AJ_WARM_GUESS && !(p_guess && p_guess[i])) return AJ_ERR_PARAM;

@@ -71,6 +71,8 @@ constexpr int kPartials = 4096;
 
 bool make_layout(const AjStepParams& p, Layout& L);
 int check_params(const AjStepParams& p);
+// effective parameters of a call (defaults filled in, step_pure's fixed options)
+AjStepParams normalise(const AjStepParams& in);
 int parity_levels(int nx, int ny, int levels, int* max_levels);
 int converge_depth(int nx, int ny);
 

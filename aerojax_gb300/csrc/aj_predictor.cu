@@ -738,6 +738,106 @@ __device__ __forceinline__ float stage_mac(const RkMac& a, int i, int j, float d
   return finish_mac<COMP>(a, k, r, chi, dt, k1o);
 }
 
+// ------------------------------------------------------------ MAC WENO5
+// WENO5-JS on the staggered grid (no reference counterpart; the reference's
+// MAC advection is the blended upwind above, rk3_mac.py:373-417).  Both
+// derivatives of both components use the upwind WENO5 reconstruction of
+// weno5() on the boundary-conditioned working copies, upwinded on the sign of
+// the advecting velocity at the face, with ghost values three cells deep by
+// edge padding (non-periodic flows) or wrap (Taylor-Green):
+//   adv_u = u d_x(u) + v_at_u d_y(u),   adv_v = u_at_v d_x(v) + v d_y(v).
+// FAST: the face and every value its stencils read lie in the interior of the
+// slip-wall von Karman channel, where the working copy is the input itself.
+template <bool FAST>
+__device__ __forceinline__ float uw_f(const RkMac& a, int i, int j) {
+  return FAST ? ldg(a.uin + (long)i * a.ny + j) : uw_at(a, a.uin, i, j);
+}
+template <bool FAST>
+__device__ __forceinline__ float vw_f(const RkMac& a, int i, int j) {
+  return FAST ? ldg(a.vin + (long)i * (a.ny + 1) + j) : vw_at(a, a.vin, i, j);
+}
+
+// ghost index of a WENO5 stencil: edge (clamp) or periodic wrap
+__device__ __forceinline__ int widx(int i, int n, bool per) {
+  return per ? wrapi(i, n) : clampi(i, n);
+}
+
+// upwind WENO5 derivative from seven samples g[0..6] = f[i-3 .. i+3]
+__device__ __forceinline__ float weno_d7(const float (&g)[7], float ih, float vel) {
+  float d0 = (g[1] - g[0]) * ih, d1 = (g[2] - g[1]) * ih, d2 = (g[3] - g[2]) * ih;
+  float d3 = (g[4] - g[3]) * ih, d4 = (g[5] - g[4]) * ih, d5 = (g[6] - g[5]) * ih;
+  return vel > 0.f ? weno5(d0, d1, d2, d3, d4) : weno5(d5, d4, d3, d2, d1);
+}
+
+template <bool HYPER, bool FAST>
+__device__ float rhs_mac_u_weno(const RkMac& a, int i, int j) {
+  const int nx = a.nx, ny = a.ny;
+  const bool per = a.flow == AJ_FLOW_TAYLOR_GREEN;
+  const float uw = uw_f<FAST>(a, i, j);
+  auto vcen = [&](int ci) {
+    ci = clampi(ci, nx);
+    return 0.5f * (vw_f<FAST>(a, ci, j + 1) + vw_f<FAST>(a, ci, j));
+  };
+  const float v_at_u = 0.5f * (vcen(i) + vcen(i - 1));
+  float g[7];
+#pragma unroll
+  for (int o = -3; o <= 3; ++o) g[o + 3] = uw_f<FAST>(a, FAST ? i + o : widx(i + o, nx + 1, per), j);
+  const float dudx = weno_d7(g, a.idx, uw);
+#pragma unroll
+  for (int o = -3; o <= 3; ++o) g[o + 3] = uw_f<FAST>(a, i, FAST ? j + o : widx(j + o, ny, per));
+  const float dudy = weno_d7(g, a.idy, v_at_u);
+  const float adv = (uw * dudx + v_at_u * dudy) * xface(a.mask, i, j, nx, ny);
+  const float lap = lap_face<0>(a, a.uin, i, j);
+  const float nut = a.nsg ? a.nu + xface(a.nsg, i, j, nx, ny) : a.nu;
+  float r = -adv + nut * lap;
+  if (HYPER) r -= a.nuh * bih_face<0>(a, a.uin, i, j, lap);
+  return r;
+}
+
+template <bool HYPER, bool FAST>
+__device__ float rhs_mac_v_weno(const RkMac& a, int i, int j) {
+  const int nx = a.nx, ny = a.ny;
+  const bool per = a.flow == AJ_FLOW_TAYLOR_GREEN;
+  const float vw = vw_f<FAST>(a, i, j);
+  auto ucen = [&](int cj) {
+    cj = clampi(cj, ny);
+    return 0.5f * (uw_f<FAST>(a, i + 1, cj) + uw_f<FAST>(a, i, cj));
+  };
+  const float u_at_v = 0.5f * (ucen(j) + ucen(j - 1));
+  float g[7];
+#pragma unroll
+  for (int o = -3; o <= 3; ++o) g[o + 3] = vw_f<FAST>(a, FAST ? i + o : widx(i + o, nx, per), j);
+  const float dvdx = weno_d7(g, a.idx, u_at_v);
+#pragma unroll
+  for (int o = -3; o <= 3; ++o) g[o + 3] = vw_f<FAST>(a, i, FAST ? j + o : widx(j + o, ny + 1, per));
+  const float dvdy = weno_d7(g, a.idy, vw);
+  const float adv = (u_at_v * dvdx + vw * dvdy) * yface(a.mask, i, j, nx, ny);
+  const float lap = lap_face<1>(a, a.vin, i, j);
+  const float nut = a.nsg ? a.nu + yface(a.nsg, i, j, nx, ny) : a.nu;
+  float r = -adv + nut * lap;
+  if (HYPER) r -= a.nuh * bih_face<1>(a, a.vin, i, j, lap);
+  return r;
+}
+
+// one stage of one face, upwind (the reference) or WENO5
+template <int COMP, bool HYPER, int ADV, bool FAST = false>
+__device__ __forceinline__ float stage_mac_any(const RkMac& a, int i, int j, float dt, float* k1o) {
+  if (ADV != AJ_ADV_WENO5) return stage_mac<COMP, HYPER>(a, i, j, dt, k1o);
+  const int m = COMP == 0 ? a.ny : a.ny + 1;
+  const long k = (long)i * m + j;
+  const float r = COMP == 0 ? rhs_mac_u_weno<HYPER, FAST>(a, i, j)
+                            : rhs_mac_v_weno<HYPER, FAST>(a, i, j);
+  float chi;
+  if (COMP == 0) {
+    chi = 0.5f * ((1.f - ldg(a.mask + (long)clampi(i, a.nx) * a.ny + j)) +
+                  (1.f - ldg(a.mask + (long)clampi(i - 1, a.nx) * a.ny + j)));
+  } else {
+    chi = 0.5f * ((1.f - ldg(a.mask + (long)i * a.ny + clampi(j, a.ny))) +
+                  (1.f - ldg(a.mask + (long)i * a.ny + clampi(j - 1, a.ny))));
+  }
+  return finish_mac<COMP>(a, k, r, chi, dt, k1o);
+}
+
 // Interior faces of the von Karman channel with slip walls (u faces
 // 2 <= i <= nx-2, 2 <= j <= ny-3; v faces 2 <= i <= nx-3, 2 <= j <= ny-2):
 // every neighbour the stencils touch, including the bi-Laplacian's, is an
@@ -812,7 +912,7 @@ __device__ __forceinline__ float stage_mac_v_int(const RkMac& a, int i, int j, f
   return finish_mac<1>(a, k, r, chi, dt, k1o);
 }
 
-template <bool HYPER>
+template <bool HYPER, int ADV>
 __global__ void __launch_bounds__(256) k_rk_mac(RkMac a) {
   pdl_wait();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -821,6 +921,54 @@ __global__ void __launch_bounds__(256) k_rk_mac(RkMac a) {
   const float dt = a.sc->dt;
   bool last = a.rk2 ? a.stage == 2 : a.stage == 3;
   const bool fast = a.flow == AJ_FLOW_VON_KARMAN && a.slip;
+  if (ADV == AJ_ADV_WENO5) {
+    // interior faces: u 4 <= i <= nx-4, 4 <= j <= ny-5; v 4 <= i <= nx-5,
+    // 4 <= j <= ny-4 (the 7-point stencils and the face velocities stay off
+    // the rows the boundary conditions rewrite)
+    if (i <= nx && j < ny) {
+      const long k = (long)i * ny + j;
+      float o;
+      if (fast && i >= 4 && i <= nx - 4 && j >= 4 && j <= ny - 5) {
+        o = stage_mac_any<0, HYPER, ADV, true>(a, i, j, dt, last ? nullptr : a.k1u_out);
+      } else if (!last) {
+        o = stage_mac_any<0, HYPER, ADV>(a, i, j, dt, a.k1u_out);
+      } else if (a.flow == AJ_FLOW_VON_KARMAN) {
+        if (!a.slip && (j == 0 || j == ny - 1)) o = 0.f;
+        else if (i == 0) o = a.U;
+        else {
+          int ii = i == nx ? nx - 1 : i;
+          int jj = a.slip ? (j == 0 ? 1 : (j == ny - 1 ? ny - 2 : j)) : j;
+          o = stage_mac_any<0, HYPER, ADV>(a, ii, jj, dt, nullptr);
+        }
+      } else if (a.flow == AJ_FLOW_LID_DRIVEN_CAVITY) {
+        if (i == 0 || i == nx || j == 0) o = 0.f;
+        else if (j == ny - 1) o = a.U;
+        else o = stage_mac_any<0, HYPER, ADV>(a, i, j, dt, nullptr);
+      } else {
+        o = stage_mac_any<0, HYPER, ADV>(a, i, j, dt, nullptr);
+      }
+      a.uout[k] = o;
+    }
+    if (i < nx && j <= ny) {
+      const long k = (long)i * (ny + 1) + j;
+      float o;
+      if (fast && i >= 4 && i <= nx - 5 && j >= 4 && j <= ny - 4) {
+        o = stage_mac_any<1, HYPER, ADV, true>(a, i, j, dt, last ? nullptr : a.k1v_out);
+      } else if (!last) {
+        o = stage_mac_any<1, HYPER, ADV>(a, i, j, dt, a.k1v_out);
+      } else if (a.flow == AJ_FLOW_VON_KARMAN) {
+        if (i == 0 || j == 0 || j == ny) o = 0.f;
+        else o = stage_mac_any<1, HYPER, ADV>(a, i == nx - 1 ? nx - 2 : i, j, dt, nullptr);
+      } else if (a.flow == AJ_FLOW_LID_DRIVEN_CAVITY) {
+        if (i == 0 || i == nx - 1 || j == 0 || j == ny) o = 0.f;
+        else o = stage_mac_any<1, HYPER, ADV>(a, i, j, dt, nullptr);
+      } else {
+        o = stage_mac_any<1, HYPER, ADV>(a, i, j, dt, nullptr);
+      }
+      a.vout[k] = o;
+    }
+    return;
+  }
   if (fast && i >= 2 && i <= nx - 3 && j >= 2 && j <= ny - 3) {
     // both faces of the cell interior: one scope, so the loads they share
     // (u at (i,j), (i+1,j), (i,j-1); v at (i,j), (i,j+1), (i-1,j); mask and
@@ -935,7 +1083,7 @@ int launch_predictor(const AjStepParams& p, const Layout& L, void* ws, const flo
       in_v = a.vout;
     }
   } else {
-    if (p.advection != AJ_ADV_UPWIND) return AJ_ERR_PARAM;   // MAC: tanh-blended upwind only
+    if (p.advection != AJ_ADV_UPWIND && p.advection != AJ_ADV_WENO5) return AJ_ERR_PARAM;
     RkMac a{};
     a.u0 = u;
     a.v0 = v;
@@ -972,8 +1120,11 @@ int launch_predictor(const AjStepParams& p, const Layout& L, void* ws, const flo
       a.vout = last ? vs : dst[1];
       a.k1u_out = (rk2 && s == 1) ? K[0] : nullptr;
       a.k1v_out = (rk2 && s == 1) ? K[1] : nullptr;
-      if (hyper) launch_pdl(true, k_rk_mac<true>, dim3(grd), dim3(blk), 0, st, a);
-      else launch_pdl(true, k_rk_mac<false>, dim3(grd), dim3(blk), 0, st, a);
+      const bool weno = p.advection == AJ_ADV_WENO5;
+      if (hyper && weno) launch_pdl(true, k_rk_mac<true, AJ_ADV_WENO5>, dim3(grd), dim3(blk), 0, st, a);
+      else if (hyper) launch_pdl(true, k_rk_mac<true, AJ_ADV_UPWIND>, dim3(grd), dim3(blk), 0, st, a);
+      else if (weno) launch_pdl(true, k_rk_mac<false, AJ_ADV_WENO5>, dim3(grd), dim3(blk), 0, st, a);
+      else launch_pdl(true, k_rk_mac<false, AJ_ADV_UPWIND>, dim3(grd), dim3(blk), 0, st, a);
       in_u = a.uout;
       in_v = a.vout;
     }

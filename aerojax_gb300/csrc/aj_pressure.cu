@@ -490,7 +490,7 @@ int prepare_pressure(const AjStepParams& p, const Layout& L, void* ws, const flo
         k_mask_restrict<<<g, blk, 0, st>>>(mf, at<float>(ws, L.M[l + 1]), n, m);
       }
     }
-  } else {
+  } else if (p.mg_mode == AJ_MG_CONVERGE) {
     int rc = converge_prepare(p, L, ws, st);
     if (rc != AJ_OK) return rc;
   }

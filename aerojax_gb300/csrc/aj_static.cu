@@ -9,10 +9,11 @@
 // synchronisation is not acceptable.  Such a caller passes only the
 // right-hand side, the mask and the output pressure.
 //
-// The scratch array below is part of the library image: every GPU on which
-// this entry point is first used holds kStaticScratchBytes of device memory
-// until the process exits.  Grids above AJ_STATIC_MAX_CELLS cells are
-// rejected.  All calls share the one array, which keeps the last call's
+// The scratch array below is part of the library image: it is reserved on
+// every device where the library's module is loaded - at first use under the
+// default lazy module loading, at context creation with
+// CUDA_MODULE_LOADING=EAGER - and held until the process exits.  Grids above
+// AJ_STATIC_MAX_CELLS cells are rejected.  All calls share the one array, which keeps the last call's
 // contents; each call clears the part that must start at zero.  Calls whose
 // work overlaps on the GPU (other streams, other host threads) race on the
 // array: order them on one stream or serialise them.
@@ -22,6 +23,13 @@
 namespace aj {
 
 constexpr size_t kStaticScratchBytes = (size_t)14 << 20;   // 14 MiB
+
+// Worst case of static_layout at AJ_STATIC_MAX_CELLS: the level-0 rhs and
+// scratch (8 B per cell), three arrays per coarse level (12 B per cell times
+// sum 4^-l < 1/3, i.e. < 4 B per cell), and at most 255 B of alignment per
+// array for the scalars and up to 16 levels.
+static_assert((size_t)AJ_STATIC_MAX_CELLS * 12 + 256 * (3 + 3 * 16) <= kStaticScratchBytes,
+              "the static scratch array cannot hold the largest allowed grid");
 
 static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
 
@@ -87,21 +95,37 @@ extern "C" int32_t aj_poisson_mg_static(const AjStepParams* prm, const float* rh
                                         const float* mask, float* p_out, AjStats* stats,
                                         void* stream) {
   if (!prm || !rhs || !mask || !p_out) return AJ_ERR_PARAM;
-  AjStepParams p = *prm;
-  if (p.levels <= 0) p.levels = 4;
-  if (p.mg_tolerance <= 0) p.mg_tolerance = AJ_PARITY_TOL_DEFAULT;
+  // the same parameter rules as aj_poisson_mg, in the one mode this entry
+  // point runs (the parity solve from a zero guess on the collocated grid)
+  AjStepParams p = normalise(*prm);
   p.mg_mode = AJ_MG_PARITY;
-  p.warm_start = 0;
+  p.warm_start = AJ_WARM_ZERO;
+  int rc = check_params(p);
+  if (rc != AJ_OK) return rc;                                           // multigrid_solver.py:104-106
   if (p.grid_type != AJ_GRID_COLLOCATED || p.flow_type != AJ_FLOW_VON_KARMAN) return AJ_ERR_PARAM;
-  if (p.dx <= 0 || p.dy <= 0 || p.v_cycles < 1) return AJ_ERR_PARAM;
   if ((long)p.nx * p.ny > AJ_STATIC_MAX_CELLS) return AJ_ERR_WORKSPACE;   // above the stated limit
   Layout L;
-  if (!static_layout(p, L)) return AJ_ERR_SHAPE;                        // multigrid_solver.py:104-106
+  if (!static_layout(p, L)) return AJ_ERR_SHAPE;
   if (L.total > kStaticScratchBytes) return AJ_ERR_WORKSPACE;
-  void* ws = nullptr;
-  int rc = static_scratch_address(&ws);
-  if (rc != AJ_OK) return rc;
+  // the array used is the current device's: the stream and the buffers must
+  // belong to that device
+  int dev = -1, sdev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess) return AJ_ERR_CUDA;
   cudaStream_t st = (cudaStream_t)stream;
+  if (st && cudaStreamGetDevice(st, &sdev) == cudaSuccess && sdev != dev) return AJ_ERR_PARAM;
+  cudaGetLastError();
+  for (const void* ptr : {(const void*)rhs, (const void*)mask, (const void*)p_out}) {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, ptr) != cudaSuccess) {
+      cudaGetLastError();
+      return AJ_ERR_PARAM;
+    }
+    if (at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged) return AJ_ERR_PARAM;
+    if (at.device != dev) return AJ_ERR_PARAM;
+  }
+  void* ws = nullptr;
+  rc = static_scratch_address(&ws);
+  if (rc != AJ_OK) return rc;
   // the device scalars must start at zero on every call (the array keeps the
   // previous call's contents); every other region is written before it is read
   if (cudaMemsetAsync(ws, 0, 256, st) != cudaSuccess) return AJ_ERR_CUDA;

@@ -338,12 +338,6 @@ def poisson_multigrid_converge(rhs, mask, dx, dy, rtol=1e-6, p0=None, max_cycles
 
 
 # ----------------------------------------------------------------- pieces
-def _small_plan(nx, ny, dx, dy, **kw):
-    cfg = StepConfig(nx=nx, ny=ny, dx=float(dx), dy=float(dy), nu=kw.pop("nu", 1.0),
-                     mg_mode="converge", max_cycles=1, **kw)
-    return cfg
-
-
 def constant_smagorinsky(u, v, dx, dy, delta, C_s=0.1, stream=None):
     """solver/les_models.py:179-200 (collocated inputs)."""
     _f32(u, "u")
@@ -352,7 +346,7 @@ def constant_smagorinsky(u, v, dx, dy, delta, C_s=0.1, stream=None):
     out = torch.empty_like(u)
     p = make_params(StepConfig(nx=nx, ny=ny, dx=float(dx), dy=float(dy), nu=1.0,
                                smagorinsky_constant=float(C_s), les_delta=float(delta),
-                               mg_mode="converge"))
+                               mg_mode="none"))
     check("aj_les", lib().aj_les(ctypes.byref(p), 1, u.data_ptr(), v.data_ptr(), out.data_ptr(),
                                  None, None, 0, _stream(stream)))
     return out
@@ -366,7 +360,7 @@ def dynamic_smagorinsky(u, v, dx, dy, delta, alpha=2.0, stream=None):
     nx, ny = u.shape
     _f32(v, "v", (nx, ny))
     cfg = StepConfig(nx=nx, ny=ny, dx=float(dx), dy=float(dy), nu=1.0, les_delta=float(delta),
-                     mg_mode="converge")
+                     mg_mode="none")
     plan = get_plan(cfg, u.device)
     out, cd = torch.empty_like(u), torch.empty_like(u)
     check("aj_les", lib().aj_les(ctypes.byref(plan.params), 2, u.data_ptr(), v.data_ptr(),
@@ -382,7 +376,7 @@ def _predictor(grid_type, u, v, dt, nu, dx, dy, mask, sdf, U_inf, nu_sgs, nu_hyp
                      grid_type=grid_type, flow_type=flow_type, variant="gui",
                      advection_scheme=advection, fast_mode=bool(fast_mode),
                      slip_walls=bool(slip_walls), brinkman_eta=float(brinkman_eta),
-                     nu_hyper_ratio=float(nu_hyper_ratio), mg_mode="converge",
+                     nu_hyper_ratio=float(nu_hyper_ratio), mg_mode="none",
                      has_sdf=sdf is not None, dt=float(dt))
     plan = get_plan(cfg, u.device)
     plan.prepare(mask, sdf, stream)
@@ -411,13 +405,15 @@ def rk_step_unified(u, v, dt, nu, dx, dy, mask, sdf=None, U_inf=1.0, nu_sgs=None
 
 def rk_step_unified_mac(u, v, dt, nu, dx, dy, mask, U_inf=1.0, nu_sgs=None, nu_hyper_ratio=0.0,
                         slip_walls=True, fast_mode=False, brinkman_eta=0.01,
-                        flow_type="von_karman", *, stream=None):
-    """advection_schemes/rk3_mac.py:220-504."""
+                        flow_type="von_karman", *, advection="upwind", stream=None):
+    """advection_schemes/rk3_mac.py:220-504.  ``advection='weno5'`` replaces
+    the reference's blended upwind and central advection terms by WENO5-JS
+    derivatives on the faces."""
     nx, ny = mask.shape
     _f32(u, "u", (nx + 1, ny))
     _f32(v, "v", (nx, ny + 1))
     return _predictor("mac", u, v, dt, nu, dx, dy, mask, None, U_inf, nu_sgs, nu_hyper_ratio,
-                      slip_walls, fast_mode, brinkman_eta, flow_type, False, "upwind", stream)
+                      slip_walls, fast_mode, brinkman_eta, flow_type, False, advection, stream)
 
 
 def compute_cfl_timestep(u, v, dx, dy, nu, mask=None, cfl_target=0.3, dt_min=1e-4, dt_max=0.01,

@@ -53,8 +53,12 @@ enum { AJ_ADV_UPWIND = 0, AJ_ADV_WENO5 = 1 };
 /* PARITY   = the reference V-cycle, fixed v_cycles, absolute early exit;
    CONVERGE = FP32 red-black Gauss-Seidel V-cycles inside double-FP32
               iterative refinement, an exact separable coarse solve (or an FP64
-              dense one), FP64 norms, relative stop. */
-enum { AJ_MG_PARITY = 0, AJ_MG_CONVERGE = 1 };
+              dense one), FP64 norms, relative stop;
+   NONE     = no pressure solve: a workspace for aj_prepare, aj_predictor and
+              aj_les only, on any grid of at least 4x4 cells and any flow type
+              (the reference's rk_step_unified and LES models take any shape);
+              the solving entry points reject it with AJ_ERR_PARAM. */
+enum { AJ_MG_PARITY = 0, AJ_MG_CONVERGE = 1, AJ_MG_NONE = 2 };
 /* Initial guess of the converging solve (no reference counterpart: the
    reference always starts from p = 0, multigrid_solver.py:219).
    ZERO        p = 0
@@ -306,11 +310,17 @@ int32_t aj_post_step(const AjStepParams* prm, const float* u, const float* v, co
    synchronisation.  Same result as aj_poisson_mg in parity mode on the
    collocated grid (von Karman), but its scratch is a 14 MiB device array
    inside the library, so the caller passes only rhs, mask (nx*ny) and p
-   (nx*ny); stats may be NULL.  Grids above AJ_STATIC_MAX_CELLS cells return
-   AJ_ERR_WORKSPACE.  The first call on each device looks up the array's
-   device address (cudaGetSymbolAddress); make that first call before any
-   stream capture.  Every call shares the array: calls that overlap on the GPU
-   race, so order them on one stream.  No counterpart in the reference. */
+   (nx*ny); stats may be NULL.  The array is reserved on every device where
+   the library's module is loaded (at first use under lazy module loading,
+   the default; at context creation with CUDA_MODULE_LOADING=EAGER) until the
+   process exits.  The call uses the current device's array: the stream and
+   the three buffers must belong to the current device (AJ_ERR_PARAM
+   otherwise).  Parameters follow aj_poisson_mg's rules; grids above
+   AJ_STATIC_MAX_CELLS cells return AJ_ERR_WORKSPACE.  The first call on each
+   device looks up the array's device address (cudaGetSymbolAddress); make
+   that first call before any stream capture.  Every call shares the array:
+   calls that overlap on the GPU race, so order them on one stream.  No
+   counterpart in the reference. */
 #define AJ_STATIC_MAX_CELLS (1 << 20)
 int32_t aj_poisson_mg_static(const AjStepParams* prm, const float* rhs, const float* mask,
                              float* p, AjStats* stats, void* stream);

@@ -472,22 +472,83 @@ def weno5_advection(fld, vu, vv, dx, dy, pad_mode):
 # ---------------------------------------------------------------------------
 # MAC predictor — advection_schemes/rk3_mac.py:220-504
 # ---------------------------------------------------------------------------
+def v_to_u_face(vf):
+    """v (nx, ny+1) at the u faces (nx+1, ny): rk3_mac.py:239-245."""
+    vc = 0.5 * (vf[:, 1:] + vf[:, :-1])
+    vp = np.pad(vc, ((1, 1), (0, 0)), mode="edge")
+    return 0.5 * (vp[1:, :] + vp[:-1, :])
+
+
+def u_to_v_face(uf):
+    """u (nx+1, ny) at the v faces (nx, ny+1): rk3_mac.py:247-253."""
+    uc = 0.5 * (uf[1:, :] + uf[:-1, :])
+    up = np.pad(uc, ((0, 0), (1, 1)), mode="edge")
+    return 0.5 * (up[:, 1:] + up[:, :-1])
+
+
+def mac_advection_terms(uw, vw, dx, dy, nonper=True, scheme="upwind"):
+    """(u.grad) u on the u faces and (u.grad) v on the v faces from the
+    boundary-conditioned working copies uw (nx+1, ny), vw (nx, ny+1), before
+    the face-mask factor.
+
+    scheme='upwind' is the reference (rk3_mac.py:373-417): along the face
+    normal a tanh blend alpha = (1 + tanh(u/0.05))/2 of the backward and
+    forward differences (edge or wrap padding), across it a central
+    difference (one-sided at the walls, or periodic) times the interpolated
+    velocity.
+
+    scheme='weno5' (new; the reference has no WENO5) uses the upwind WENO5-JS
+    derivative of :func:`weno5_derivative` for both directions of both
+    components, upwinded on the sign of the advecting velocity at the face,
+    with ghost values three cells deep by edge (non-periodic) or wrap
+    padding: adv_u = uw d_x^W(uw) + v_at_u d_y^W(uw), adv_v = u_at_v
+    d_x^W(vw) + vw d_y^W(vw)."""
+    v_at_u, u_at_v = v_to_u_face(vw), u_to_v_face(uw)
+    pm = "edge" if nonper else "wrap"
+    if scheme == "weno5":
+        adv_u = (uw * weno5_derivative(uw, uw, dx, 0, pm)
+                 + v_at_u * weno5_derivative(uw, v_at_u, dy, 1, pm))
+        adv_v = (u_at_v * weno5_derivative(vw, u_at_v, dx, 0, pm)
+                 + vw * weno5_derivative(vw, vw, dy, 1, pm))
+        return adv_u, adv_v
+    upx = np.pad(uw, ((1, 1), (0, 0)), mode=pm)
+    back = (uw - upx[:-2, :]) / dx
+    fwd = (upx[2:, :] - uw) / dx
+    al = 0.5 * (1 + np.tanh(uw / 0.05))
+    adv_ux = uw * (al * back + (1 - al) * fwd)
+    if nonper:
+        du_dy = np.zeros_like(uw)
+        du_dy[:, 1:-1] = (uw[:, 2:] - uw[:, :-2]) / (2.0 * dy)
+        du_dy[:, 0] = (uw[:, 1] - uw[:, 0]) / dy
+        du_dy[:, -1] = (uw[:, -1] - uw[:, -2]) / dy
+    else:
+        du_dy = (np.roll(uw, -1, axis=1) - np.roll(uw, 1, axis=1)) / (2.0 * dy)
+    adv_u = adv_ux + v_at_u * du_dy
+    vpy = np.pad(vw, ((0, 0), (1, 1)), mode=pm)
+    back = (vw - vpy[:, :-2]) / dy
+    fwd = (vpy[:, 2:] - vw) / dy
+    al = 0.5 * (1 + np.tanh(vw / 0.05))
+    adv_vy = vw * (al * back + (1 - al) * fwd)
+    if nonper:
+        dv_dx = np.zeros_like(vw)
+        dv_dx[1:-1, :] = (vw[2:, :] - vw[:-2, :]) / (2.0 * dx)
+        dv_dx[0, :] = (vw[1, :] - vw[0, :]) / dx
+        dv_dx[-1, :] = (vw[-1, :] - vw[-2, :]) / dx
+    else:
+        dv_dx = (np.roll(vw, -1, axis=0) - np.roll(vw, 1, axis=0)) / (2.0 * dx)
+    adv_v = u_at_v * dv_dx + adv_vy
+    return adv_u, adv_v
+
+
 def rk_step_unified_mac(u, v, dt, nu, dx, dy, mask, U_inf=1.0, nu_sgs=None,
                         nu_hyper_ratio=0.0, slip_walls=True, fast_mode=False,
-                        brinkman_eta=0.01, flow_type="von_karman"):
+                        brinkman_eta=0.01, flow_type="von_karman", advection="upwind"):
+    """Staggered predictor.  ``advection='weno5'`` replaces the blended
+    upwind and central terms by WENO5-JS derivatives (a new option; see
+    :func:`mac_advection_terms`)."""
     chi = 1.0 - mask                                           # :231
     eta_safe = max(brinkman_eta, 1e-10)                        # :234
     nonper = flow_type in ("von_karman", "lid_driven_cavity")
-
-    def v_to_u_face(vf):                                       # :239-245
-        vc = 0.5 * (vf[:, 1:] + vf[:, :-1])
-        vp = np.pad(vc, ((1, 1), (0, 0)), mode="edge")
-        return 0.5 * (vp[1:, :] + vp[:-1, :])
-
-    def u_to_v_face(uf):                                       # :247-253
-        uc = 0.5 * (uf[1:, :] + uf[:-1, :])
-        up = np.pad(uc, ((0, 0), (1, 1)), mode="edge")
-        return 0.5 * (up[:, 1:] + up[:, :-1])
 
     def lap_face(f, axis):                                     # :268-290
         if slip_walls:
@@ -508,40 +569,13 @@ def rk_step_unified_mac(u, v, dt, nu, dx, dy, mask, U_inf=1.0, nu_sgs=None,
     mask_u = interpolate_to_x_face(mask)
     mask_v = interpolate_to_y_face(mask)
 
-    def advection(ui, vi):                                     # :332-417
-        uw, vw = bc_mac(ui, vi, U_inf, flow_type, slip_walls)
-        v_at_u, u_at_v = v_to_u_face(vw), u_to_v_face(uw)
-        pm = "edge" if nonper else "wrap"
-        upx = np.pad(uw, ((1, 1), (0, 0)), mode=pm)
-        back = (uw - upx[:-2, :]) / dx
-        fwd = (upx[2:, :] - uw) / dx
-        al = 0.5 * (1 + np.tanh(uw / 0.05))
-        adv_ux = uw * (al * back + (1 - al) * fwd)
-        if nonper:
-            du_dy = np.zeros_like(uw)
-            du_dy[:, 1:-1] = (uw[:, 2:] - uw[:, :-2]) / (2.0 * dy)
-            du_dy[:, 0] = (uw[:, 1] - uw[:, 0]) / dy
-            du_dy[:, -1] = (uw[:, -1] - uw[:, -2]) / dy
-        else:
-            du_dy = (np.roll(uw, -1, axis=1) - np.roll(uw, 1, axis=1)) / (2.0 * dy)
-        adv_u = adv_ux + v_at_u * du_dy
-        vpy = np.pad(vw, ((0, 0), (1, 1)), mode=pm)
-        back = (vw - vpy[:, :-2]) / dy
-        fwd = (vpy[:, 2:] - vw) / dy
-        al = 0.5 * (1 + np.tanh(vw / 0.05))
-        adv_vy = vw * (al * back + (1 - al) * fwd)
-        if nonper:
-            dv_dx = np.zeros_like(vw)
-            dv_dx[1:-1, :] = (vw[2:, :] - vw[:-2, :]) / (2.0 * dx)
-            dv_dx[0, :] = (vw[1, :] - vw[0, :]) / dx
-            dv_dx[-1, :] = (vw[-1, :] - vw[-2, :]) / dx
-        else:
-            dv_dx = (np.roll(vw, -1, axis=0) - np.roll(vw, 1, axis=0)) / (2.0 * dx)
-        adv_v = u_at_v * dv_dx + adv_vy
+    def adv_terms(ui, vi):                                     # :332-417
+        uw, vw = bc_mac(ui, vi, U_inf, flow_type, slip_walls)  # working copies, :381
+        adv_u, adv_v = mac_advection_terms(uw, vw, dx, dy, nonper, advection)
         return adv_u * mask_u, adv_v * mask_v
 
     def rhs_explicit(ui, vi):                                  # :425-458
-        au, av = advection(ui, vi)
+        au, av = adv_terms(ui, vi)
         lu, lv = lap_face(ui, 0), lap_face(vi, 1)
         if nu_sgs is None:
             ntu = ntv = nu
@@ -743,7 +777,8 @@ class MGConfig:
 
     mode='parity'   : the reference's V-cycle, ``v_cycles`` cycles, zero guess.
     mode='converge' : converging multigrid to ``rtol`` relative residual with
-                      an optional warm start ``p0`` (see :func:`mg_converge`).
+                      an optional warm start ``p0``, or ``guess(b)`` computed
+                      from the solve's right-hand side (see :func:`mg_converge`).
     """
     mode: str = "parity"
     v_cycles: int = 3
@@ -751,6 +786,7 @@ class MGConfig:
     rtol: float = 1e-6
     max_cycles: int = 40
     p0: object = None
+    guess: object = None        # callable b -> p0 (converging mode), overrides p0
     info: dict = field(default_factory=dict)
 
 
@@ -759,7 +795,8 @@ def _solve_pressure(rhs, mask, dx, dy, mg: MGConfig, flow_type, mac):
         return poisson_multigrid(rhs, mask, dx, dy, mg.levels, mg.v_cycles, 1e-6,
                                  flow_type, mac=mac)
     b = rhs * mask if mac else rhs
-    p, info = mg_converge(b, dx, dy, rtol=mg.rtol, max_cycles=mg.max_cycles, p0=mg.p0)
+    p0 = mg.guess(b) if mg.guess is not None else mg.p0
+    p, info = mg_converge(b, dx, dy, rtol=mg.rtol, max_cycles=mg.max_cycles, p0=p0)
     mg.info.update(info)
     return p.astype(rhs.dtype)
 
@@ -863,7 +900,7 @@ def step_gui(u, v, mask, dt, *, sdf, dx, dy, nu, U_inf, grid_type="collocated", 
         us, vs = rk_step_unified_mac(u, v, dt, nu, dx, dy, mask, U_inf=U_inf, nu_sgs=nu_sgs,
                                      nu_hyper_ratio=nu_hyper_ratio, slip_walls=slip_walls,
                                      fast_mode=fast_mode, brinkman_eta=brinkman_eta,
-                                     flow_type=flow_type)
+                                     flow_type=flow_type, advection=advection)
         div = divergence_staggered(us, vs, dx, dy)            # :219-222
         rhs = div / dt
         p = _solve_pressure(rhs, mask, dx, dy, mg, flow_type, mac=True)

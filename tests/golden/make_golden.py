@@ -6,8 +6,8 @@ stand-in for the jax API, float64).  Nothing here is imported by the product
 or by the GPU tests; the fixtures it writes (``tests/golden/*.npz``) are what
 travels.
 
-Usage:  python tests/golden/make_golden.py [REFERENCE_ROOT]
-(REFERENCE_ROOT defaults to $AEROJAX_REF or /root/reference.)
+Usage:  python tests/golden/make_golden.py REFERENCE_ROOT
+(or set $AEROJAX_REF to the AeroJAX checkout and omit the argument).
 """
 from __future__ import annotations
 
@@ -279,5 +279,7 @@ def main(root):
 
 
 if __name__ == "__main__":
-    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("AEROJAX_REF", "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("AEROJAX_REF")
+    if not root:
+        sys.exit("usage: make_golden.py REFERENCE_ROOT (or set AEROJAX_REF)")
     main(root)

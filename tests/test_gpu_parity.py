@@ -2,7 +2,9 @@
 reproduced by the CUDA path through the C ABI, in FP32.
 
 Tolerance: max|gpu - ref| / max|ref| <= 1e-5 for velocity and pressure
-(the FP32 bar), unless a test states otherwise."""
+(the FP32 bar).  The one exception is the dynamic Smagorinsky model, whose
+bound is the distance of the reference's own algorithm evaluated in FP32 from
+its FP64 run (test_les)."""
 import numpy as np
 import pytest
 
@@ -71,9 +73,23 @@ def test_les(cuda_lib):
     d, cd = aj.dynamic_smagorinsky(T(g["u"]), T(g["v"]), float(g["dx"]), float(g["dy"]),
                                    float(g["delta"]))
     assert rel(c, g["nu_const"]) < TOL
-    # C_d = <LM>/(<MM>+1e-8) divides two small contractions: FP32 keeps ~1e-4
-    assert rel(cd, g["cd"]) < 2e-4
-    assert rel(d, g["nu_dyn"]) < 2e-4
+    # C_d = <LM>/(<MM>+1e-8): L_ij = filter(u_i)filter(u_j) - filter(u_i u_j)
+    # cancels to ~1e-4 of its terms, so the reference's own algorithm
+    # evaluated in FP32 departs from its FP64 run by ~1.2e-4 on this field.
+    # The GPU must be no further from FP64 than that FP32 evaluation.
+    d32, cd32 = _dynamic_fp32(g)
+    assert rel(cd, g["cd"]) <= max(TOL, 2.0 * rel(cd32, g["cd"]))
+    assert rel(d, g["nu_dyn"]) <= max(TOL, 2.0 * rel(d32, g["nu_dyn"]))
+    assert rel(d32, g["nu_dyn"]) > 10 * TOL     # the bound is the FP32 evaluation's, not 1e-5
+
+
+def _dynamic_fp32(g):
+    """The oracle's dynamic Smagorinsky in FP32 arithmetic (the reference's
+    default precision, solver/config.py:28) on the fixture's inputs."""
+    from oracle import ref_np as R
+    f = np.float32
+    return R.dynamic_smagorinsky(g["u"].astype(f), g["v"].astype(f), f(g["dx"]), f(g["dy"]),
+                                 f(g["delta"]))
 
 
 def test_step_pure(cuda_lib):
@@ -103,10 +119,23 @@ def test_step_gui(cuda_lib, name):
                        brinkman_eta=float(g["eta"]), multigrid_v_cycles=int(g["v_cycles"]),
                        sdf=None if mac else T(g["sdf"]), dt=float(g["dt"]))
     u, v, p = h._step(T(g["u"]), T(g["v"]), T(g["mask"]))
-    tol = 2e-4 if int(g["dynamic"]) else TOL    # dynamic C_d: see test_les
-    assert rel(u, g["u_new"]) < tol
-    assert rel(v, g["v_new"]) < tol
-    assert rel(p, g["p"]) < tol
+    if int(g["dynamic"]):
+        # dynamic C_d (see test_les): bounded by the reference's own step
+        # evaluated in FP32 from the same inputs
+        from oracle import ref_np as R
+        f = np.float32
+        r32 = R.step_gui(g["u"].astype(f), g["v"].astype(f), g["mask"].astype(f), f(g["dt"]),
+                         sdf=None if mac else g["sdf"].astype(f), dx=f(g["dx"]), dy=f(g["dy"]),
+                         nu=f(g["nu"]), U_inf=f(g["U"]), grid_type="mac" if mac else "collocated",
+                         use_les=True, les_model="dynamic_smagorinsky",
+                         smagorinsky_constant=f(g["cs"]), nu_hyper_ratio=f(g["hyper"]),
+                         brinkman_eta=f(g["eta"]), v_cycles=int(g["v_cycles"]))
+        for got, key, ref32 in ((u, "u_new", r32[0]), (v, "v_new", r32[1]), (p, "p", r32[2])):
+            assert rel(got, g[key]) <= max(TOL, 2.0 * rel(ref32, g[key])), key
+        return
+    assert rel(u, g["u_new"]) < TOL
+    assert rel(v, g["v_new"]) < TOL
+    assert rel(p, g["p"]) < TOL
 
 
 def test_cfl(cuda_lib):
@@ -135,6 +164,14 @@ def test_geometry(cuda_lib):
         assert np.nanmax(np.abs(sdf.cpu().numpy() - ref)) < 1e-6
         mref = R.mask_from_sdf(ref, eps)
         assert np.max(np.abs(mask.cpu().numpy() - mref)) < 1e-5
+    # the triangle of three cylinders has no reference counterpart: the oracle's
+    # SDF (sdf_three_cylinders_triangle) on the fixture's grid
+    X, Y = g["X"], g["Y"]
+    geo = (2.0, 1.5, 0.5, 0.8)
+    mask, sdf = aj.make_geometry("cyl3_tri", nx, ny, lx, ly, geo, eps)
+    ref = R.sdf_three_cylinders_triangle(X, Y, *geo)
+    assert np.max(np.abs(sdf.cpu().numpy() - ref)) < 1e-6
+    assert np.max(np.abs(mask.cpu().numpy() - R.mask_from_sdf(ref, eps))) < 1e-5
 
 
 def test_shape_error_like_reference(cuda_lib):

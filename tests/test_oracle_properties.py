@@ -1,5 +1,6 @@
-"""Known-answer checks of the oracle's new parts (converging multigrid, WENO5)
-and of the reference behaviours it must reproduce (shape errors).  CPU only."""
+"""Known-answer checks of the oracle's new parts (converging multigrid, WENO5 on
+the collocated and the staggered grid) and of the reference behaviours it
+must reproduce (shape errors).  CPU only."""
 import numpy as np
 import pytest
 
@@ -80,6 +81,53 @@ def test_weno5_upwind_direction():
     dneg = R.weno5_derivative(f, -np.ones_like(f), h, 0, "wrap")
     assert np.max(np.abs(dpos - dneg)) < 1e-5       # both O(h^5)-consistent on smooth data
     assert not np.array_equal(dpos, dneg)           # but different stencils
+
+
+@pytest.mark.parametrize("sign", [1.0, -1.0])
+def test_mac_weno5_order(sign):
+    """Fifth-order convergence of the staggered WENO5 advection terms
+    (mac_advection_terms, scheme='weno5') on smooth fields, both upwind
+    directions.  The advecting velocity interpolated to the face
+    (rk3_mac.py:239-253) is second order by itself, so the check isolates
+    the derivatives: adv_u - (u du/dx + v_at_u du/dy) with exact
+    derivatives, on faces at least four cells from every edge."""
+    errs = []
+    for n in (32, 64, 128):
+        h = 2 * np.pi / n
+        xf, xc = np.arange(n + 1) * h, (np.arange(n) + 0.5) * h
+        U = lambda x, y: sign * (2.0 + np.sin(x) * np.cos(y))
+        V = lambda x, y: sign * (1.5 + np.cos(x) * np.sin(y))
+        uw = U(xf[:, None], xc[None, :])
+        vw = V(xc[:, None], xf[None, :])
+        au, av = R.mac_advection_terms(uw, vw, h, h, True, "weno5")
+        vu, uv = R.v_to_u_face(vw), R.u_to_v_face(uw)
+        xu, yu = xf[:, None], xc[None, :]
+        xv, yv = xc[:, None], xf[None, :]
+        ex_u = uw * sign * np.cos(xu) * np.cos(yu) - vu * sign * np.sin(xu) * np.sin(yu)
+        ex_v = -uv * sign * np.sin(xv) * np.sin(yv) + vw * sign * np.cos(xv) * np.cos(yv)
+        k = 4
+        errs.append(max(np.max(np.abs(au - ex_u)[k:-k, k:-k]),
+                        np.max(np.abs(av - ex_v)[k:-k, k:-k])))
+    orders = [np.log2(errs[i] / errs[i + 1]) for i in range(2)]
+    assert min(orders) > 4.5, orders
+
+
+def test_mac_upwind_scheme_unchanged():
+    """scheme='upwind' of mac_advection_terms is the reference's blended
+    upwind: a first-order scheme on the same smooth fields."""
+    errs = []
+    for n in (32, 64, 128):
+        h = 2 * np.pi / n
+        xf, xc = np.arange(n + 1) * h, (np.arange(n) + 0.5) * h
+        uw = 2.0 + np.sin(xf[:, None]) * np.cos(xc[None, :])
+        vw = 1.5 + np.cos(xc[:, None]) * np.sin(xf[None, :])
+        au, _ = R.mac_advection_terms(uw, vw, h, h, True, "upwind")
+        vu = R.v_to_u_face(vw)
+        xu, yu = xf[:, None], xc[None, :]
+        ex_u = uw * np.cos(xu) * np.cos(yu) - vu * np.sin(xu) * np.sin(yu)
+        errs.append(np.max(np.abs(au - ex_u)[4:-4, 4:-4]))
+    orders = [np.log2(errs[i] / errs[i + 1]) for i in range(2)]
+    assert 0.8 < min(orders) < 1.5, orders
 
 
 @pytest.mark.parametrize("shape,ok", [((512, 96), True), ((64, 32), True), ((100, 64), False),

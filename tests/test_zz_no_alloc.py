@@ -34,11 +34,15 @@ def _static_solve(L, prm, rhs, mask):
     return p
 
 
-def test_static_matches_workspace_solver_twice(cuda_lib):
+@pytest.mark.parametrize("nx,ny", [(512, 96), (2048, 512)])
+def test_static_matches_workspace_solver_twice(cuda_lib, nx, ny):
+    """512x96, and 2048x512: exactly AJ_STATIC_MAX_CELLS cells, the largest
+    layout the library's array must hold."""
     import torch
     import aerojax_gb300 as aj
     L = cuda_lib
-    nx, ny, dx, vc = 512, 96, 1 / 64, 3
+    dx, vc = 1 / 64, 3
+    assert nx * ny <= 1 << 20
     prm = _params(nx, ny, dx, vc)
     rng = np.random.default_rng(11)
     mask = torch.as_tensor((rng.random((nx, ny)) > 0.05).astype(np.float32), device="cuda")
