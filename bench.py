@@ -19,9 +19,14 @@ Arms on the GPU (whole step captured in one CUDA graph each):
 value = cell-steps/s of `nn` (the metric's arm); the others are reported in
 config.arms.
 
-`python bench.py --impl reference` times the reference algorithm's CPU path
-(the NumPy port of the reference GUI step, float32, 5 reference V-cycles) on
-the host cores.  The reference itself is JAX and cannot be installed here.
+`python bench.py --impl reference` times the same workload and method on the
+host cores: the oracle's NumPy restatement (the reference's GUI step, the
+converging multigrid to the same tolerance, the same extrapolation and
+network), one replica per core, run concurrently (oracle/method_np.py); the
+reference's own V-cycle (5 cycles) is reported beside it.  The reference
+itself is JAX and cannot be installed here.  The GPU line's cpu_baseline is
+the same restatement started from the GPU's developed state, and its
+parity_sample checks one step of the method's arm against the FP64 oracle.
 """
 from __future__ import annotations
 
@@ -58,7 +63,7 @@ def parse():
                          "4096x2048 three-cylinder dynamic-LES flow")
     ap.add_argument("--nx", type=int, default=2048)
     ap.add_argument("--ny", type=int, default=512)
-    ap.add_argument("--cpu-sample-steps", type=int, default=20)
+    ap.add_argument("--cpu-sample-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quick", action="store_true",
                     help="timed GPU arms only (no clock soak, e2e or CPU leg)")
@@ -124,41 +129,28 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------ CPU arm
-def cpu_step_fn(nx, ny):
-    """The reference algorithm on the host: NumPy float32 port of the GUI MAC
-    step with the reference multigrid (5 V-cycles, the GUI default)."""
-    import numpy as np
-    from oracle import ref_np as R
-    lx, ly = 32.0 * nx / 2048, 8.0 * ny / 512
-    dx, dy = lx / nx, ly / ny
-    X, Y = R.grid_coords(nx, ny, lx, ly)
-    chord = 256 * dx * nx / 2048
-    xle, yle = (400 * nx // 2048) * dx, (ny // 2) * dy
-    sdf = R.sdf_naca4(X, Y, chord, 10.0, xle, yle, 0.0, 0.0, 0.12)
-    f = np.float32
-    mask = R.mask_from_sdf(sdf, 0.05 * dx).astype(f)
-    rng = np.random.default_rng(0)
-    u = (1.0 + 1e-3 * rng.standard_normal((nx + 1, ny))).astype(f)
-    v = np.zeros((nx, ny + 1), f)
-    nu = chord / 1000.0
-
-    def step(u, v):
-        dt = f(R.compute_cfl_timestep(u, v, dx, dy, nu, 0.5, 1e-6, 1.0))
-        return R.step_gui(u, v, mask, dt, sdf=None, dx=f(dx), dy=f(dy), nu=f(nu), U_inf=f(1.0),
-                          grid_type="mac", use_les=True, les_model="smagorinsky",
-                          smagorinsky_constant=f(0.17), brinkman_eta=f(1e-4), v_cycles=5)
-    return step, u, v
+WEIGHTS_NACA = os.path.join(ROOT, "aerojax_gb300", "weights", "warmstart_naca0012_2048x512_f8.npz")
+METHOD = ("learned warm start (4-level BF16 conv encoder-decoder on the 256x64 grid correcting "
+          "the extrapolation p1 + (dt/dt1)(p1 - p2) of the last two pressures), then converging "
+          "multigrid to a 1e-6 relative residual (FP64 norms)")
 
 
-def run_cpu(nx, ny, steps, warmup):
-    step, u, v = cpu_step_fn(nx, ny)
-    for _ in range(warmup):
-        u, v, _ = step(u, v)
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        u, v, _ = step(u, v)
-    el = time.perf_counter() - t0
-    return nx * ny * steps / el / 1e6, el
+def bench_config(nx, ny):
+    """The workload and method both arms run; identical in the two lines."""
+    return {"workload": f"naca0012_{nx}x{ny}_mac_re1000_les", "nx": nx, "ny": ny, "grid": "mac",
+            "les": "smagorinsky C_s=0.17", "dt": "CFL 0.5", "method": METHOD,
+            "rel_residual_target": 1e-6,
+            "l2": "GPU arm: flushed before every step (256 MiB write outside the timed events); "
+                  "CPU arm: one replica per core, working set far above the caches"}
+
+
+def cpu_replicas(nx, ny, steps, warmup, mode="nn", init=None):
+    """The same step on the host cores: one replica of the oracle's
+    restatement of the method (oracle/method_np.py) per core, run
+    concurrently; returns (aggregate Mcell-steps/s, info)."""
+    from oracle import method_np as M
+    return M.run_replicas(nx, ny, mode, WEIGHTS_NACA if mode == "nn" else None, steps, warmup,
+                          init=init)
 
 
 def reference_arm(args):
@@ -166,18 +158,28 @@ def reference_arm(args):
     if rank != 0:
         return
     steps, warm = max(1, args.steps), max(0, args.warmup)
-    val, el = run_cpu(args.nx, args.ny, steps, warm)
-    sample = (f"{steps} full {args.nx}x{args.ny} MAC steps after {warm} warm-up steps, "
-              "NumPy float32 port of the reference GUI step (5 reference V-cycles)")
+    val, info = cpu_replicas(args.nx, args.ny, steps, warm, "nn")
+    # the reference's own algorithm (its V-cycle, 5 cycles, no convergence
+    # target) on the same cores, for context
+    rsteps = min(steps, 10)
+    rval, rinfo = cpu_replicas(args.nx, args.ny, rsteps, min(warm, 2), "reference")
+    sample = (f"{info['procs']} concurrent replicas x {steps} full {args.nx}x{args.ny} MAC steps "
+              f"after {warm} warm-up steps from the seeded start ({info['seconds']:.1f} s), "
+              f"NumPy restatement of the method (float32 predictor, float64 multigrid and network)")
     print(json.dumps({
         "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
-        "warmup": warm, "ms_per_step": el / steps * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "impl": "reference",
-        "data": "synthetic (seeded NACA 0012 flow)",
-        "config": {"workload": f"naca0012_{args.nx}x{args.ny}_mac_re1000_les",
-                   "solver": "reference multigrid, 5 V-cycles (the GUI default)"},
-        "cpu_baseline": {"value": val, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
+        "warmup": warm, "ms_per_step": info["seconds"] / steps * 1e3 / info["procs"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "impl": "reference", "data": "synthetic (seeded NACA 0012 flow)",
+        "config": bench_config(args.nx, args.ny),
+        "cpu_baseline": {"value": val, "unit": UNIT, "cores": info["procs"], "kind": "port",
+                         "sample": sample},
         "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "mg_cycles_mean": info["mg_cycles_mean"],
+        "reference_algorithm": {
+            "value": rval, "unit": UNIT, "cores": rinfo["procs"],
+            "what": f"the reference's GUI step with its own V-cycle (5 cycles, no convergence "
+                    f"target), {rsteps} steps per replica"},
     }))
 
 
@@ -320,6 +322,23 @@ def gpu_arm(args):
                      "frac_of_measured_hbm": bpc * cells / (ms_step * 1e-3) / 1e9 / hbm}
     launches = sum(int(L.aj_kernel_count(ctypes.byref(plan.params), c)) for c in cyc_m)
 
+    # ---- a developed state of the method's arm for the CPU legs: two more
+    # steps record the solve history, a third is the sampled step whose fields
+    # are checked against the FP64 oracle (untimed)
+    sample_in = None
+    if rank == 0 and not args.no_cpu_baseline and not args.quick:
+        sb = meth["bufs"]
+        hist = []
+        for k in range(3):
+            src, dst = sb[k % 2], sb[1 - k % 2]
+            if k == 2:
+                sample_in = tuple(t.detach().cpu().numpy() for t in src[:2])
+            step(plan, head, src, dst)
+            st_k = plan.stats()
+            hist.append((dst[2].detach().cpu().numpy(), st_k["dt"], st_k))
+        sample_out = tuple(t.detach().cpu().numpy() for t in sb[1])
+        sample_dt, sample_stats = hist[2][1], hist[2][2]
+
     # ---- e2e: host buffers through aj_step_host (one graph launch: the H2D of
     # the step's inputs, the step, the D2H of its result)
     nxu, nyv = (args.nx + 1) * args.ny, args.nx * (args.ny + 1)
@@ -359,42 +378,95 @@ def gpu_arm(args):
     if rank != 0:
         replicas.finalize()
         return
-    cpu = None
-    if not args.no_cpu_baseline and not args.quick:
-        n = args.cpu_sample_steps
-        cval, cel = run_cpu(args.nx, args.ny, n, 1)
-        cpu = {"value": cval, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": f"{n} full {args.nx}x{args.ny} MAC steps ({cel:.1f} s), NumPy float32 "
-                         "port of the reference GUI step with 5 reference V-cycles"}
+    cpu = parity = None
+    if sample_in is not None:
+        cpu, parity = cpu_leg(args, mask.detach().cpu().numpy(), hist, sample_in, sample_out,
+                              sample_dt, sample_stats)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded NACA 0012 flow; the solver generates every step)",
-        "config": {
-            "workload": case["name"], "nx": args.nx, "ny": args.ny, "grid": "mac",
-            "method": ("learned warm start (4-level BF16 conv encoder-decoder on the 256x64 grid, "
-                       "correction to the double-FP32 extrapolation of the last two pressures), "
-                       "then converging MG (FP32 red-black V-cycles, exact separable coarse solve, "
-                       "double-FP32 refinement, FP64 norms)") if head == "nn" else
-                      "converging MG warm-started from the double-FP32 extrapolation",
-            "rel_residual_target": 1e-6, "arms": arms,
-            "autotuned_level0_tiles": tuned[0] if tuned else None,
-            "step_roofline": step_roofline,
-            "plain_mg_value": plain_value, "speedup_vs_plain": value / plain_value,
-            "l2": "flushed before every step (256 MiB write outside the timed events)",
-            "e2e_api": "aj_step_host: pinned host u, v, p in; u, v, p out; copies inside the "
-                       "step's graph",
-            "parallelism": "replicas only" if world > 1 else "single GPU",
-        },
+        "config": bench_config(args.nx, args.ny),
+        "arms": arms,
+        "speedup_vs_plain": value / plain_value,
+        "autotuned_level0_tiles": tuned[0] if tuned else None,
+        "step_roofline": step_roofline,
+        "e2e_api": "aj_step_host: pinned host u, v, p in; u, v, p out; copies inside the "
+                   "step's graph",
+        "parallelism": "replicas only" if world > 1 else "single GPU",
         "roofline": roof,
         "cpu_baseline": cpu,
+        "parity_sample": parity,
         "e2e": e2e,
         "gpu_launches": launches,
         "clocks": clk,
     }
     print(json.dumps(line))
     replicas.finalize()
+
+
+def cpu_leg(args, mask, hist, sample_in, sample_out, sample_dt, sample_stats):
+    """The CPU baseline and the parity sample (host only, after every GPU
+    measurement).
+
+    cpu_baseline: the oracle's restatement of the same method, one replica
+    per host core, started from the GPU's developed state (velocities and the
+    last two pressures), so that its solves see the same flow stage.
+
+    parity_sample: one step of the method's arm against the FP64 oracle from
+    the same input state - the maximum relative error of u, v, p against the
+    exact step (pressure solved to 1e-12), beside the distance of the
+    reference's own step evaluated in FP32, and the post-projection
+    divergence of the GPU step, of the reference's own step (its V-cycle, 5
+    cycles) and of the exact step."""
+    import tempfile
+    import numpy as np
+    from oracle import ref_np as R
+    from oracle import method_np as M
+    nx, ny = args.nx, args.ny
+    with tempfile.TemporaryDirectory() as tmp:
+        init = os.path.join(tmp, "state.npz")
+        np.savez(init, u=sample_in[0], v=sample_in[1], p1=hist[1][0], dt1=hist[1][1],
+                 p2=hist[0][0], dt2=hist[0][1])
+        steps = 3
+        val, info = cpu_replicas(nx, ny, steps, 1, "nn", init=init)
+    cpu = {"value": val, "unit": UNIT, "cores": info["procs"], "kind": "port",
+           "sample": f"{info['procs']} concurrent replicas x {steps} full {nx}x{ny} MAC steps "
+                     f"after 1 warm-up step from the GPU's developed state ({info['seconds']:.1f} "
+                     f"s; {info['mg_cycles_mean']} V-cycles per solve), NumPy restatement of the "
+                     "method", "mg_cycles_mean": info["mg_cycles_mean"]}
+    case = M.naca_case(nx, ny)
+    u0, v0 = (a.astype(np.float64) for a in sample_in)
+    m = mask.astype(np.float64)
+    kw = dict(sdf=None, dx=case["dx"], dy=case["dy"], nu=case["nu"], U_inf=1.0, grid_type="mac",
+              use_les=True, les_model="smagorinsky", smagorinsky_constant=0.17,
+              brinkman_eta=1e-4)
+    ex = R.step_gui(u0, v0, m, sample_dt, mg=R.MGConfig(mode="converge", rtol=1e-12,
+                                                         max_cycles=80), **kw)
+    f = np.float32
+    kw32 = {k: (f(x) if isinstance(x, float) else x) for k, x in kw.items()}
+    r32 = R.step_gui(u0.astype(f), v0.astype(f), m.astype(f), f(sample_dt),
+                     mg=R.MGConfig(mode="converge", rtol=1e-12, max_cycles=80), **kw32)
+    ref = R.step_gui(u0, v0, m, sample_dt, v_cycles=5, **kw)
+
+    def rel(a, b):
+        return float(np.max(np.abs(np.asarray(a, np.float64) - b)) / max(np.max(np.abs(b)), 1e-300))
+
+    def div(u, v):
+        d = R.divergence_staggered(np.asarray(u, np.float64), np.asarray(v, np.float64),
+                                   case["dx"], case["dy"])
+        return float(np.sqrt(np.sum(d * d) * case["dx"] * case["dy"]))
+    parity = {
+        "what": "one step of the method's arm from a developed state against the FP64 oracle "
+                "(max |x - x_exact| / max |x_exact|)",
+        "max_rel_err": {k: rel(g, e) for k, g, e in zip("uvp", sample_out, ex)},
+        "fp32_reference_max_rel_err": {k: rel(g, e) for k, g, e in zip("uvp", r32, ex)},
+        "post_projection_divergence_l2": {"gpu": div(*sample_out[:2]), "exact": div(*ex[:2]),
+                                          "reference_step_5_vcycles": div(*ref[:2])},
+        "rel_residual": sample_stats["rel_residual"], "mg_cycles": sample_stats["cycles"],
+    }
+    return cpu, parity
 
 
 def step_bytes_per_cell(n_cycles, les=True):
@@ -639,10 +711,11 @@ def parity_workload(args, dev, st):
     cpu = None
     if not args.no_cpu_baseline and not args.quick:
         n = args.cpu_sample_steps
-        cval, cel = run_cpu(nx, ny, n, 1)
-        cpu = {"value": cval, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": f"{n} full {nx}x{ny} MAC steps ({cel:.1f} s), NumPy float32 port of the "
-                         "reference GUI step with 5 reference V-cycles"}
+        cval, info = cpu_replicas(nx, ny, n, 1, "reference")
+        cpu = {"value": cval, "unit": UNIT, "cores": info["procs"], "kind": "port",
+               "sample": f"{info['procs']} concurrent replicas x {n} full {nx}x{ny} MAC steps "
+                         f"({info['seconds']:.1f} s), NumPy float32 port of the reference GUI "
+                         "step with 5 reference V-cycles"}
     print(json.dumps({
         "metric": "Mcell-steps/s, reference GUI step with the reference multigrid (5 V-cycles), "
                   f"{nx}x{ny} MAC",
