@@ -380,10 +380,16 @@ static int enqueue_step(const AjStepParams& p, const Layout& L, void* ws, const 
   if (les && cudaStreamWaitEvent(st, fk->les_done, 0) != cudaSuccess) return AJ_ERR_CUDA;
   float* us = at<float>(ws, L.sS_u);
   float* vs = at<float>(ws, L.sS_v);
-  rc = launch_predictor(p, L, ws, u, v, mask, nsg, dc, us, vs, st);
-  if (rc != AJ_OK) return rc;
-  rc = launch_rhs(p, L, ws, us, vs, mask, at<float>(ws, L.b0), st);
-  if (rc != AJ_OK) return rc;
+  if (tile_predictor_ok(p, u, mask, nsg)) {
+    // the three stages, boundary rows and the pressure rhs in one tile kernel
+    rc = launch_predictor_tile(p, ws, u, v, mask, nsg, us, vs, at<float>(ws, L.b0), st);
+    if (rc != AJ_OK) return rc;
+  } else {
+    rc = launch_predictor(p, L, ws, u, v, mask, nsg, dc, us, vs, st);
+    if (rc != AJ_OK) return rc;
+    rc = launch_rhs(p, L, ws, us, vs, mask, at<float>(ws, L.b0), st);
+    if (rc != AJ_OK) return rc;
+  }
   if (conv && cudaStreamWaitEvent(st, fk->init_done, 0) != cudaSuccess) return AJ_ERR_CUDA;
   if (io && io->h_p && cudaStreamWaitEvent(st, fk->io_p_in, 0) != cudaSuccess)
     return AJ_ERR_CUDA;
@@ -709,8 +715,8 @@ int32_t aj_kernel_count(const AjStepParams* prm, int32_t cycles) {
   int n = 1;                                                    // cfl or set-dt
   if (p.les_model != AJ_LES_NONE && (p.variant == AJ_VARIANT_GUI || mac))
     n += p.les_model == AJ_LES_DYNAMIC ? (mac ? 1 : 0) + 4 : 1;
-  n += p.fast_mode ? 2 : 3;                                     // predictor stages
-  n += 1;                                                       // rhs
+  if (tile_predictor_params_ok(p)) n += 1;                      // stages + rhs in one tile kernel
+  else n += (p.fast_mode ? 2 : 3) + 1;                          // predictor stages, rhs
   if (p.mg_mode == AJ_MG_PARITY) {
     int per_cycle = 2 * L.nlev + (parity_coarsest_fused(L) ? 1 : 10);   // levels, coarsest
     n += 1 + p.v_cycles * per_cycle;                            // begin + cycles

@@ -249,6 +249,14 @@ inline cudaError_t launch_pdl(bool pdl, void (*kernel)(KArgs...), dim3 grid, dim
 int launch_predictor(const AjStepParams& p, const Layout& L, void* ws, const float* u,
                      const float* v, const float* mask, const float* nsg, int double_count,
                      float* us, float* vs, cudaStream_t st);
+// the MAC predictor's three stages, boundary rows and pressure rhs (b,
+// nullable) in one shared-memory tile kernel (aj_predictor_tile.cu)
+bool tile_predictor_params_ok(const AjStepParams& p);
+bool tile_predictor_ok(const AjStepParams& p, const float* u, const float* mask,
+                       const float* nsg);
+int launch_predictor_tile(const AjStepParams& p, void* ws, const float* u, const float* v,
+                          const float* mask, const float* nsg, float* us, float* vs, float* b,
+                          cudaStream_t st);
 int launch_les(const AjStepParams& p, const Layout& L, void* ws, int model, const float* u,
                const float* v, int mac_input, float* nu_sgs, float* cd, cudaStream_t st);
 int launch_cfl(const AjStepParams& p, void* ws, const float* u, const float* v,

@@ -1084,6 +1084,8 @@ int launch_predictor(const AjStepParams& p, const Layout& L, void* ws, const flo
     }
   } else {
     if (p.advection != AJ_ADV_UPWIND && p.advection != AJ_ADV_WENO5) return AJ_ERR_PARAM;
+    if (tile_predictor_ok(p, u, mask, nsg))
+      return launch_predictor_tile(p, ws, u, v, mask, nsg, us, vs, nullptr, st);
     RkMac a{};
     a.u0 = u;
     a.v0 = v;

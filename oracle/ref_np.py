@@ -1125,12 +1125,39 @@ def direct_level(nx, ny, depth, max_cells=65536, max_m=128, max_n=1024):
     return 0
 
 
-def coarse_solve_separable(r, level, dx, dy):
+def _pcr(a, b, c, d):
+    """Parallel cyclic reduction of the tridiagonal system (a: sub-, b: main,
+    c: super-diagonal) in the arrays' own precision - the GPU's k_cv_dpcr
+    schedule (log2 n steps, each eliminating the neighbours at distance st)."""
+    a, b, c, d = (x.copy() for x in (a, b, c, d))
+    n, st = len(b), 1
+    i = np.arange(n)
+    while st < n:
+        lo, hi = i - st >= 0, i + st < n
+        an, cn = np.zeros_like(a), np.zeros_like(c)
+        bn, dn = b.copy(), d.copy()
+        k1 = a[lo] / b[i[lo] - st]
+        an[lo] = -a[i[lo] - st] * k1
+        bn[lo] -= c[i[lo] - st] * k1
+        dn[lo] -= d[i[lo] - st] * k1
+        k2 = c[hi] / b[i[hi] + st]
+        cn[hi] = -c[i[hi] + st] * k2
+        bn[hi] -= a[i[hi] + st] * k2
+        dn[hi] -= d[i[hi] + st] * k2
+        a, b, c, d = an, bn, cn, dn
+        st *= 2
+    return d / b
+
+
+def coarse_solve_separable(r, level, dx, dy, dtype=np.float64):
     """Exact solve of the level-l operator (level >= 1).  It is separable:
     A = ax Tx (x) I + ay I (x) Ty with Ty the Neumann-Neumann 1-D Laplacian,
     diagonalised by the orthonormal DCT-II (eigenvalues -4 sin^2(pi k/2m)),
     and Tx tridiagonal with an edge ghost at the inlet and the outlet ghost
-    g * e_last; one tridiagonal solve in x per cosine mode."""
+    g * e_last; one tridiagonal solve in x per cosine mode.
+    dtype=np.float32 evaluates the transforms and the parallel cyclic
+    reduction in FP32, the precision of the GPU's k_cv_dfwd / k_cv_dpcr /
+    k_cv_dbwd."""
     from scipy.linalg import solve_banded
     n, m = r.shape
     hx, hy = dx * 2 ** level, dy * 2 ** level
@@ -1140,10 +1167,22 @@ def coarse_solve_separable(r, level, dx, dy):
     C = np.sqrt(2.0 / m) * np.cos(np.pi * kk * (2 * jj + 1) / (2.0 * m))
     C[0, :] = np.sqrt(1.0 / m)
     ly = -4.0 * ay * np.sin(np.pi * np.arange(m) / (2.0 * m)) ** 2
-    rh = r @ C.T
     dxv = np.full(n, -2.0)
     dxv[0] += 1.0
     dxv[-1] += outlet_ghost_factor(level)
+    if dtype == np.float32:
+        f = np.float32
+        C32 = C.astype(f)
+        rh = r.astype(f) @ C32.T
+        eh = np.empty_like(rh)
+        sub = np.full(n, ax, f)
+        sub[0] = 0
+        sup = np.full(n, ax, f)
+        sup[-1] = 0
+        for k in range(m):
+            eh[:, k] = _pcr(sub, (ax * dxv + ly[k]).astype(f), sup, rh[:, k])
+        return (eh @ C32).astype(np.float64)
+    rh = r @ C.T
     eh = np.empty_like(rh)
     for k in range(m):
         ab = np.zeros((3, n))
@@ -1154,13 +1193,13 @@ def coarse_solve_separable(r, level, dx, dy):
     return eh @ C
 
 
-def v_cycle_converge(r, dx, dy, depth, nu1=2, nu2=2, direct=0):
+def v_cycle_converge(r, dx, dy, depth, nu1=2, nu2=2, direct=0, coarse_dtype=np.float64):
     """One V(nu1,nu2) cycle for A e = r from e = 0; returns e (level 0).
     With direct > 0 the cycle stops at that level with the separable exact
-    solve; else it descends to the dense coarsest grid."""
+    solve (in coarse_dtype); else it descends to the dense coarsest grid."""
     def cyc(rl, level):
         if direct and level == direct:
-            return coarse_solve_separable(rl, level, dx, dy)
+            return coarse_solve_separable(rl, level, dx, dy, coarse_dtype)
         if level == depth:
             A = coarse_matrix(rl.shape, level, dx, dy)
             return np.linalg.solve(A, rl.ravel()).reshape(rl.shape)
@@ -1177,12 +1216,13 @@ def v_cycle_converge(r, dx, dy, depth, nu1=2, nu2=2, direct=0):
 
 
 def mg_converge(b, dx, dy, rtol=1e-6, max_cycles=40, p0=None, nu1=2, nu2=2, max_coarse=64,
-                direct=True):
+                direct=True, coarse_dtype=np.float64):
     """Converging mode: iterative refinement around V-cycles.  Each outer
     iteration computes r = b - A p in float64, runs one V-cycle on A e = r and
     adds e.  Stops when ||r||/||b|| <= rtol.  Returns (p, info).  The V-cycle
     ends in the separable direct solve at direct_level() when direct is True
-    (as on the GPU), else at the dense coarsest grid."""
+    (as on the GPU), else at the dense coarsest grid; coarse_dtype selects the
+    precision of that direct solve."""
     b = np.asarray(b, np.float64).copy()
     b[-1, :] = 0.0
     nx, ny = b.shape
@@ -1200,7 +1240,7 @@ def mg_converge(b, dx, dy, rtol=1e-6, max_cycles=40, p0=None, nu1=2, nu2=2, max_
         hist.append(float(rel))
         if rel <= rtol or cycles >= max_cycles:
             break
-        p = p + v_cycle_converge(r, dx, dy, depth, nu1, nu2, dlev)
+        p = p + v_cycle_converge(r, dx, dy, depth, nu1, nu2, dlev, coarse_dtype)
         p[-1, :] = 0.0
         cycles += 1
     return p, {"cycles": cycles, "rel_residual": hist[-1], "history": hist, "depth": depth,

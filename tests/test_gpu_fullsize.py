@@ -341,6 +341,50 @@ np.savez(sys.argv[2], **out)
 """
 
 
+_TILE_SCRIPT = r"""
+import sys, numpy as np, torch
+sys.path.insert(0, sys.argv[1])
+from dataclasses import replace
+from aerojax_gb300 import configs
+import aerojax_gb300 as aj
+out = {}
+for nx, ny in ((512, 128), (2048, 512)):
+    c = configs.naca_mac_2048x512(nx=nx, ny=ny, mg_mode="converge")
+    plan = aj.get_plan(replace(c["cfg"], warm_start="extrapolate"), "cuda")
+    plan.prepare(c["mask"])
+    u, v, p = c["u"].clone(), c["v"].clone(), torch.zeros((nx, ny), device="cuda")
+    for _ in range(4):
+        u, v, p = aj.run_step(plan, u, v, c["mask"], p_guess=p)
+        assert plan.stats()["err"] == 0
+    out[f"u{nx}"], out[f"v{nx}"], out[f"p{nx}"] = (t.cpu().numpy() for t in (u, v, p))
+np.savez(sys.argv[2], **out)
+"""
+
+
+def test_tile_predictor_matches_stage_kernels(cuda_lib, tmp_path):
+    """The one-kernel tile predictor (three RK3 stages, boundary rows and the
+    pressure rhs from shared memory) and the per-stage kernels give the same
+    four steps of the NACA workload at 512x128 and 2048x512
+    (AEROJAX_TILE_PREDICTOR=0 selects the per-stage kernels)."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    res = {}
+    for mode in ("1", "0"):
+        f = tmp_path / f"tile{mode}.npz"
+        env = dict(os.environ, AEROJAX_TILE_PREDICTOR=mode)
+        r = subprocess.run([sys.executable, "-c", _TILE_SCRIPT, root, str(f)], env=env,
+                           capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stderr[-2000:]
+        res[mode] = np.load(f)
+    for k in res["1"].files:
+        a, b = res["1"][k], res["0"][k]
+        err = float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-30))
+        print(k, "max relative difference tile vs stage kernels:", err)
+        assert err <= 1e-6, (k, err)
+
+
 def test_dependent_launches_change_nothing(cuda_lib, tmp_path):
     """Programmatic dependent launch only moves when a kernel is scheduled:
     four steps of the extrapolation and learned-warm-start arms are bit for
