@@ -108,6 +108,8 @@ _SIGS = {
     "aj_step_vjp_kernel_count": (c_int32, [POINTER(AjStepParams)]),
     "aj_autotune": (c_int32, [POINTER(AjStepParams), c_void_p, c_size_t, c_int32,
                               POINTER(ctypes.c_float), POINTER(c_int32), c_void_p]),
+    "aj_ffi_prepare": (c_void_p, [c_void_p]),
+    "aj_ffi_step": (c_void_p, [c_void_p]),
     "aj_ensemble_step": (c_int32, [c_int32, POINTER(AjStepParams), POINTER(c_void_p),
                                    POINTER(c_void_p), POINTER(c_void_p), POINTER(c_void_p),
                                    POINTER(c_void_p), POINTER(c_void_p), POINTER(c_void_p),
@@ -154,4 +156,4 @@ def header_symbols():
     with open(HEADER) as f:
         text = f.read()
     return sorted(set(re.findall(
-        r"^\s*(?:const\s+)?(?:int32_t|size_t|float)\s*\*?\s*(aj_\w+)\s*\(", text, re.M)))
+        r"^\s*(?:const\s+)?(?:int32_t|size_t|float|void)\s*\*?\s*(aj_\w+)\s*\(", text, re.M)))

@@ -382,7 +382,9 @@ static int enqueue_step(const AjStepParams& p, const Layout& L, void* ws, const 
   float* vs = at<float>(ws, L.sS_v);
   if (tile_predictor_ok(p, u, mask, nsg)) {
     // the three stages, boundary rows and the pressure rhs in one tile kernel
-    rc = launch_predictor_tile(p, ws, u, v, mask, nsg, us, vs, at<float>(ws, L.b0), st);
+    const float* sb[4] = {at<float>(ws, L.sA_u), at<float>(ws, L.sA_v), at<float>(ws, L.sB_u),
+                          at<float>(ws, L.sB_v)};
+    rc = launch_predictor_tile(p, ws, u, v, mask, nsg, us, vs, at<float>(ws, L.b0), sb, st);
     if (rc != AJ_OK) return rc;
   } else {
     rc = launch_predictor(p, L, ws, u, v, mask, nsg, dc, us, vs, st);
@@ -715,7 +717,7 @@ int32_t aj_kernel_count(const AjStepParams* prm, int32_t cycles) {
   int n = 1;                                                    // cfl or set-dt
   if (p.les_model != AJ_LES_NONE && (p.variant == AJ_VARIANT_GUI || mac))
     n += p.les_model == AJ_LES_DYNAMIC ? (mac ? 1 : 0) + 4 : 1;
-  if (tile_predictor_params_ok(p)) n += 1;                      // stages + rhs in one tile kernel
+  if (tile_predictor_params_ok(p)) n += tile_predictor_kernels();   // stages + rhs in tile kernels
   else n += (p.fast_mode ? 2 : 3) + 1;                          // predictor stages, rhs
   if (p.mg_mode == AJ_MG_PARITY) {
     int per_cycle = 2 * L.nlev + (parity_coarsest_fused(L) ? 1 : 10);   // levels, coarsest

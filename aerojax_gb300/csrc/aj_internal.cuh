@@ -254,9 +254,13 @@ int launch_predictor(const AjStepParams& p, const Layout& L, void* ws, const flo
 bool tile_predictor_params_ok(const AjStepParams& p);
 bool tile_predictor_ok(const AjStepParams& p, const float* u, const float* mask,
                        const float* nsg);
+// stage_bufs: the workspace's stage buffers (A_u, A_v, B_u, B_v) the
+// per-stage tile kernels pass the intermediate stages through
 int launch_predictor_tile(const AjStepParams& p, void* ws, const float* u, const float* v,
                           const float* mask, const float* nsg, float* us, float* vs, float* b,
-                          cudaStream_t st);
+                          const float* const* stage_bufs, cudaStream_t st);
+// kernels one tile predictor launches (1 fused, 3 per stage)
+int tile_predictor_kernels();
 int launch_les(const AjStepParams& p, const Layout& L, void* ws, int model, const float* u,
                const float* v, int mac_input, float* nu_sgs, float* cd, cudaStream_t st);
 int launch_cfl(const AjStepParams& p, void* ws, const float* u, const float* v,

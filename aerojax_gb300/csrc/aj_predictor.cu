@@ -1084,8 +1084,10 @@ int launch_predictor(const AjStepParams& p, const Layout& L, void* ws, const flo
     }
   } else {
     if (p.advection != AJ_ADV_UPWIND && p.advection != AJ_ADV_WENO5) return AJ_ERR_PARAM;
-    if (tile_predictor_ok(p, u, mask, nsg))
-      return launch_predictor_tile(p, ws, u, v, mask, nsg, us, vs, nullptr, st);
+    if (tile_predictor_ok(p, u, mask, nsg)) {
+      const float* sb[4] = {A[0], A[1], B[0], B[1]};
+      return launch_predictor_tile(p, ws, u, v, mask, nsg, us, vs, nullptr, sb, st);
+    }
     RkMac a{};
     a.u0 = u;
     a.v0 = v;

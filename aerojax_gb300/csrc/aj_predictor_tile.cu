@@ -18,9 +18,14 @@
 // written once; the price is ~1.2x stage evaluations on the halo.
 //
 // The stencil formulas and their operation order are those of k_rk_mac
-// (aj_predictor.cu), so both paths give the same values.  Used for the MAC
-// grid, RK3, upwind advection, no hyperviscosity, the von Karman flow; other
-// options take the per-stage kernels.  AEROJAX_TILE_PREDICTOR=0 turns it off.
+// (aj_predictor.cu), so every path gives the same values (bit for bit on the
+// GPU).  They cover the MAC grid, RK3, upwind advection, no hyperviscosity,
+// the von Karman flow, and are opt-in: AEROJAX_TILE_PREDICTOR=1 selects the
+// fused kernel, =2 the per-stage tile kernels below.  Both measured slower
+// than the k_rk_mac stage kernels on the 2048x512 step (+23 and +37 us): the
+// stencils are issue-bound, the global-memory kernels get their neighbour
+// re-reads from L1, and the tiles add a staging phase, a barrier per stage
+// and (fused) 1.2x halo evaluations and 1.7 waves of large blocks.
 #include "aj_internal.cuh"
 #include <cuda.h>
 #include <cudaTypedefs.h>
@@ -43,10 +48,15 @@ constexpr size_t F_SMEM = (size_t)F_ARRAYS * FNP * sizeof(float);
 static_assert(FSI * FSJ <= FNP && (FNP * 4) % 128 == 0, "shared-memory arrays must stay 128-byte aligned");
 static_assert(FJ0 >= FH && FSJ >= FJ0 + FTJ + FH + 1, "the box must cover the halo");
 constexpr unsigned F_TMA_BOX_BYTES = FSI * FSJ * 4;
+// measured on the 2048x512 NACA step (GB300, graph-launched): the k_rk_mac
+// stage kernels 0.323 ms per extrapolated step, the fused tile kernel 0.346,
+// the per-stage tile kernels 0.360 - both tiled paths are opt-in
+constexpr int kTileDefault = 0;
 
 struct FArgs {
   const float* u;      // u (nx+1, ny): the RK combinations' x0 (read from L1/L2)
   const float* v;      // v (nx, ny+1), loaded with plain loads; also x0
+  const float* vin;    // per-stage kernels: the stage input's v
   float *uo, *vo, *b;  // u*, v*, pressure rhs (nullable)
   DevScalars* sc;
   int nx, ny, slip, has_nsg, outlet;
@@ -422,6 +432,136 @@ __global__ void __launch_bounds__(F_THREADS, 5) k_pred_mac_tile(
   }
 }
 
+// ------------------------------------------------------------ per-stage tiles
+// One RK3 stage per launch on the same 32 x 32 tiles with a one-face halo:
+// the stage input's u, the mask and the viscosity arrive by TMA (a 40 x 35
+// box), v by coalesced loads; every stencil then reads shared memory.  The
+// tile computes faces [i0, i0+32] x [j0, j0+32] (the +1 row and column only
+// serve the last stage's divergence) and stores the faces it owns; the last
+// stage also applies the boundary rows and forms the pressure rhs.
+constexpr int SSI = FTI + 3;                // 35 rows: faces i0-1 .. i0+33
+constexpr int SNP = 1408;                   // floats per array (35*40 = 1400, padded to 128 B)
+constexpr size_t S_SMEM = (size_t)6 * SNP * sizeof(float);
+constexpr unsigned S_TMA_BOX_BYTES = SSI * FSJ * 4;
+static_assert(SSI * FSJ <= SNP && (SNP * 4) % 128 == 0, "per-stage arrays must stay aligned");
+
+template <int STAGE>
+__global__ void __launch_bounds__(F_THREADS, 5) k_pred_mac_stage(
+    FArgs a, const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ CUtensorMap tm_m,
+    const __grid_constant__ CUtensorMap tm_s) {
+  pdl_wait();
+  extern __shared__ __align__(128) float sm[];
+  __shared__ uint64_t bar;
+  const int tid = threadIdx.x;
+  const int nx = a.nx, ny = a.ny;
+  const int i0 = blockIdx.y * FTI, j0 = blockIdx.x * FTJ;
+  float *Us = sm, *Vs = sm + SNP, *M = sm + 2 * SNP, *S = sm + 3 * SNP;
+  float *Au = sm + 4 * SNP, *Av = sm + 5 * SNP;
+  if (tid == 0) {
+    mbar_init(&bar, 1);
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+  }
+  __syncthreads();
+  if (tid == 0) {
+    mbar_expect_tx(&bar, S_TMA_BOX_BYTES * (a.has_nsg ? 3u : 2u));
+    tma_load_2d(Us, &tm_u, j0 - FJ0, i0 - 1, &bar);
+    tma_load_2d(M, &tm_m, j0 - FJ0, i0 - 1, &bar);
+    if (a.has_nsg) tma_load_2d(S, &tm_s, j0 - FJ0, i0 - 1, &bar);
+  }
+  for (int t = tid; t < SSI * FSJ; t += F_THREADS) {
+    const int r = t / FSJ, q = t - r * FSJ;
+    const int gi = i0 - 1 + r, gj = j0 - FJ0 + q;
+    Vs[t] = ((unsigned)gi < (unsigned)nx && (unsigned)gj <= (unsigned)ny)
+                ? ldg(a.vin + (long)gi * (ny + 1) + gj)
+                : 0.f;
+  }
+  const bool landed = mbar_wait_bounded(&bar);
+  if (__syncthreads_or(!landed)) {
+    if (tid == 0) a.sc->err = AJ_ERR_TIMEOUT;
+    mbar_wait_bounded(&bar);
+    __syncthreads();
+    return;
+  }
+  FCtx c;
+  c.nx = nx;
+  c.ny = ny;
+  c.bi = i0 - 1;
+  c.bj = j0 - FJ0;
+  c.slip = a.slip;
+  c.idx = a.idx;
+  c.idy = a.idy;
+  c.idx2 = a.idx2;
+  c.idy2 = a.idy2;
+  c.nu = a.nu;
+  c.inv_eta = a.inv_eta;
+  c.U = a.U;
+  c.M = M;
+  c.S = a.has_nsg ? S : nullptr;
+  c.gu = a.u;
+  c.gv = a.v;
+  const float dt = a.sc->dt;
+  const bool fast_flow = a.slip != 0;
+  const bool interior = fast_flow && i0 >= 2 && i0 + FTI <= nx - 3 && j0 >= 2 && j0 + FTJ <= ny - 3;
+  if (interior)
+    f_stage<STAGE, FTI + 1, FTJ + 1, true>(c, fast_flow, Us, Vs, Au, Av, i0, j0, dt);
+  else
+    f_stage<STAGE, FTI + 1, FTJ + 1, false>(c, fast_flow, Us, Vs, Au, Av, i0, j0, dt);
+  __syncthreads();
+  if (STAGE < 3) {
+    // the faces this tile owns, to the stage buffer
+    for (int t = tid; t < (FTI + 1) * (FTJ + 1); t += F_THREADS) {
+      const int r = t / (FTJ + 1);
+      const int i = i0 + r, j = j0 + (t - r * (FTJ + 1));
+      const int k = c.at(i, j);
+      if (i <= nx && j < ny && (i < i0 + FTI || i == nx) && j < j0 + FTJ)
+        a.uo[(long)i * ny + j] = Au[k];
+      if (i < nx && j <= ny && i < i0 + FTI && (j < j0 + FTJ || j == ny))
+        a.vo[(long)i * (ny + 1) + j] = Av[k];
+    }
+    return;
+  }
+  // last stage: boundary rows into Us/Vs (the stage input is consumed) and
+  // the owned faces to u*, v*
+  float *Bu = Us, *Bv = Vs;
+  for (int t = tid; t < (FTI + 1) * (FTJ + 1); t += F_THREADS) {
+    const int r = t / (FTJ + 1);
+    const int i = i0 + r, j = j0 + (t - r * (FTJ + 1));
+    const int k = c.at(i, j);
+    if (i <= nx && j < ny) {
+      float o;
+      if (!a.slip && (j == 0 || j == ny - 1)) o = 0.f;
+      else if (i == 0) o = a.U;
+      else {
+        const int ii = i == nx ? nx - 1 : i;
+        const int jj = a.slip ? (j == 0 ? 1 : (j == ny - 1 ? ny - 2 : j)) : j;
+        o = Au[c.at(ii, jj)];
+      }
+      Bu[k] = o;
+      if ((i < i0 + FTI || i == nx) && j < j0 + FTJ) a.uo[(long)i * ny + j] = o;
+    }
+    if (i < nx && j <= ny) {
+      float o;
+      if (i == 0 || j == 0 || j == ny) o = 0.f;
+      else o = Av[c.at(i == nx - 1 ? nx - 2 : i, j)];
+      Bv[k] = o;
+      if (i < i0 + FTI && (j < j0 + FTJ || j == ny)) a.vo[(long)i * (ny + 1) + j] = o;
+    }
+  }
+  if (!a.b) return;
+  __syncthreads();
+  for (int t = tid; t < FTI * FTJ; t += F_THREADS) {
+    const int r = t / FTJ;
+    const int i = i0 + r, j = j0 + (t - r * FTJ);
+    if (i >= nx || j >= ny) continue;
+    const int k = c.at(i, j);
+    const float du = (Bu[k + FSJ] - Bu[k]) * a.idx;
+    const float dv = (Bv[k + 1] - Bv[k]) * a.idy;
+    float out = ((du + dv) / dt) * M[k];
+    if (a.outlet && i == nx - 1) out = 0.f;
+    a.b[(long)i * ny + j] = out;
+  }
+}
+
 // ------------------------------------------------------------ host side
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -439,27 +579,30 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 }
 
 // a rows x cols float32 array (row stride cols) as a 2-D tensor with a
-// FSI x FSJ box; out-of-range box elements read as zero
-bool encode_box(CUtensorMap* map, const float* base, int rows, int cols) {
+// box_rows x FSJ box; out-of-range box elements read as zero
+bool encode_box(CUtensorMap* map, const float* base, int rows, int cols, int box_rows = FSI) {
   PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn();
   if (!fn) return false;
   cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
   cuuint64_t strides[1] = {(cuuint64_t)cols * sizeof(float)};
-  cuuint32_t box[2] = {FSJ, FSI};
+  cuuint32_t box[2] = {FSJ, (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1, 1};
   return fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides,
             box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-bool tile_predictor_enabled() {
+// AEROJAX_TILE_PREDICTOR: 0 = the k_rk_mac stage kernels, 1 = the fused
+// three-stage tile kernel, 2 = the per-stage tile kernels
+int tile_predictor_mode() {
   static int v = -1;
   if (v < 0) {
     const char* e = getenv("AEROJAX_TILE_PREDICTOR");
-    v = (e && e[0] == '0') ? 0 : 1;
+    v = (e && e[0] >= '0' && e[0] <= '2') ? e[0] - '0' : kTileDefault;
   }
-  return v == 1;
+  return v;
 }
+bool tile_predictor_enabled() { return tile_predictor_mode() != 0; }
 
 bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
 
@@ -483,22 +626,13 @@ bool tile_predictor_ok(const AjStepParams& p, const float* u, const float* mask,
 
 int launch_predictor_tile(const AjStepParams& p, void* ws, const float* u, const float* v,
                           const float* mask, const float* nsg, float* us, float* vs, float* b,
-                          cudaStream_t st) {
-  CUtensorMap tu, tm, ts;
-  if (!encode_box(&tu, u, p.nx + 1, p.ny) || !encode_box(&tm, mask, p.nx, p.ny) ||
-      !encode_box(&ts, nsg ? nsg : mask, p.nx, p.ny))
-    return AJ_ERR_CUDA;
-  static std::once_flag once;
-  static cudaError_t attr_rc = cudaSuccess;
-  std::call_once(once, [] {
-    attr_rc = cudaFuncSetAttribute(k_pred_mac_tile, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)F_SMEM);
-  });
-  if (attr_rc != cudaSuccess) return AJ_ERR_CUDA;
+                          const float* const* stage_bufs, cudaStream_t st) {
+  const int mode = tile_predictor_mode();
   const double eta = p.brinkman_eta > 1e-10 ? p.brinkman_eta : 1e-10;   // rk3_mac.py:234
   FArgs a{};
   a.u = u;
   a.v = v;
+  a.vin = v;
   a.uo = us;
   a.vo = vs;
   a.b = b;
@@ -516,8 +650,58 @@ int launch_predictor_tile(const AjStepParams& p, void* ws, const float* u, const
   a.inv_eta = (float)(1.0 / eta);
   a.U = (float)p.U_inf;
   dim3 grd(cdiv(p.ny, FTJ), cdiv(p.nx, FTI));
-  launch_pdl(true, k_pred_mac_tile, grd, dim3(F_THREADS), F_SMEM, st, a, tu, tm, ts);
+  if (mode == 1) {
+    CUtensorMap tu, tm, ts;
+    if (!encode_box(&tu, u, p.nx + 1, p.ny) || !encode_box(&tm, mask, p.nx, p.ny) ||
+        !encode_box(&ts, nsg ? nsg : mask, p.nx, p.ny))
+      return AJ_ERR_CUDA;
+    static std::once_flag once;
+    static cudaError_t attr_rc = cudaSuccess;
+    std::call_once(once, [] {
+      attr_rc = cudaFuncSetAttribute(k_pred_mac_tile, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)F_SMEM);
+    });
+    if (attr_rc != cudaSuccess) return AJ_ERR_CUDA;
+    launch_pdl(true, k_pred_mac_tile, grd, dim3(F_THREADS), F_SMEM, st, a, tu, tm, ts);
+    return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+  }
+  // per-stage tiles: stage 1 u, v -> buffers A; stage 2 A -> B; stage 3 B -> u*, v*, b
+  float* A_u = const_cast<float*>(stage_bufs[0]);
+  float* A_v = const_cast<float*>(stage_bufs[1]);
+  float* B_u = const_cast<float*>(stage_bufs[2]);
+  float* B_v = const_cast<float*>(stage_bufs[3]);
+  CUtensorMap tm, ts, t1, t2, t3;
+  if (!encode_box(&tm, mask, p.nx, p.ny, SSI) || !encode_box(&ts, nsg ? nsg : mask, p.nx, p.ny, SSI) ||
+      !encode_box(&t1, u, p.nx + 1, p.ny, SSI) || !encode_box(&t2, A_u, p.nx + 1, p.ny, SSI) ||
+      !encode_box(&t3, B_u, p.nx + 1, p.ny, SSI))
+    return AJ_ERR_CUDA;
+  static std::once_flag once2;
+  static cudaError_t attr2 = cudaSuccess;
+  std::call_once(once2, [] {
+    cudaError_t e1 = cudaFuncSetAttribute(k_pred_mac_stage<1>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S_SMEM);
+    cudaError_t e2 = cudaFuncSetAttribute(k_pred_mac_stage<2>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S_SMEM);
+    cudaError_t e3 = cudaFuncSetAttribute(k_pred_mac_stage<3>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S_SMEM);
+    attr2 = e1 != cudaSuccess ? e1 : (e2 != cudaSuccess ? e2 : e3);
+  });
+  if (attr2 != cudaSuccess) return AJ_ERR_CUDA;
+  FArgs a1 = a, a2 = a, a3 = a;
+  a1.uo = A_u;
+  a1.vo = A_v;
+  a1.b = nullptr;
+  a2.vin = A_v;
+  a2.uo = B_u;
+  a2.vo = B_v;
+  a2.b = nullptr;
+  a3.vin = B_v;
+  launch_pdl(true, k_pred_mac_stage<1>, grd, dim3(F_THREADS), S_SMEM, st, a1, t1, tm, ts);
+  launch_pdl(true, k_pred_mac_stage<2>, grd, dim3(F_THREADS), S_SMEM, st, a2, t2, tm, ts);
+  launch_pdl(true, k_pred_mac_stage<3>, grd, dim3(F_THREADS), S_SMEM, st, a3, t3, tm, ts);
   return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
 }
+
+int tile_predictor_kernels() { return tile_predictor_mode() == 1 ? 1 : 3; }
 
 }  // namespace aj

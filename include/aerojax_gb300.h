@@ -369,6 +369,25 @@ int32_t aj_ensemble_step(int32_t n, const AjStepParams* prms, const float* const
                          float* const* p_out, void* const* workspaces,
                          const size_t* workspace_bytes, AjStats* stats, void* stream);
 
+/* ---------------------------------------------------------------------------
+   XLA FFI handlers: aj_prepare and aj_step as JAX custom calls, the binding
+   of the reference's jit boundary (solver/simulation/step_handlers.py:304-315
+   jax.jit(self._step); solver/pure_functions/step.py:49 step_pure's jit).
+   Each takes XLA's XLA_FFI_CallFrame* (typed FFI, API version 0) and returns
+   NULL or an XLA_FFI_Error* made with the call frame's API; register with
+   jax.ffi.register_ffi_target(name, jax.ffi.pycapsule(fn), platform="CUDA").
+   Both read one attribute "params": a uint8 array holding an AjStepParams.
+   aj_ffi_prepare: (mask f32[nx*ny], sdf f32[nx*ny] or f32[0]) -> workspace
+                   u8[>= aj_workspace_size]; synchronous, like aj_prepare.
+   aj_ffi_step:    (u, v, mask, p_guess f32 (p_guess may be f32[0]),
+                   workspace u8) -> (u_out, v_out, p_out f32[, workspace u8
+                   aliased with the argument]).
+   Argument errors come back as INVALID_ARGUMENT (RESOURCE_EXHAUSTED for a
+   short workspace) with the AjStatus name in the message.  Stages other
+   than execute return NULL. */
+void* aj_ffi_prepare(void* call_frame);
+void* aj_ffi_step(void* call_frame);
+
 #ifdef __cplusplus
 }
 #endif
