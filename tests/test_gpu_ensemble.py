@@ -61,6 +61,49 @@ def test_ensemble_matches_single_steps(dev):
         assert torch.equal(pe, p), (k, float((pe - p).abs().max()))
 
 
+def test_ensemble_instances_against_oracle(dev):
+    """One instance of each grid size, WENO5 and the converging multigrid:
+    after three batched steps, the fourth step of every instance against the
+    FP64 oracle step (step_pure with the pressure solved exactly) from the
+    same input state.  Bound: the GPU is within max(1e-5, 2 e32) + 2 e6 of
+    the exact step, e32 being the distance of the oracle's own step in FP32
+    and e6 that of the FP64 step stopped at the same 1e-6 tolerance."""
+    from aerojax_gb300 import ensemble as E
+    from oracle import ref_np as R
+    specs = [E.Instance(nx, ny, d, 0.15, 0.5, re) for (nx, ny), d, re in
+             zip(E.SIZES, (10.0, 16.0, 24.0, 30.0), (120.0, 300.0, 600.0, 950.0))]
+    ens = E.Ensemble(specs, device=dev, seed=30)
+    for _ in range(3):
+        ens.step()
+    before = [tuple(t.clone() for t in ens.state(k)[:2]) for k in range(len(specs))]
+    ens.step()
+    st = ens.stats()
+    H = lambda t: t.detach().double().cpu().numpy()
+    rel = lambda a, b: float(np.max(np.abs(np.asarray(a, np.float64) - b)) /
+                             max(np.max(np.abs(b)), 1e-300))
+    for k, spec in enumerate(specs):
+        assert st[k]["err"] == 0 and st[k]["rel_residual"] <= 1e-6, (k, st[k])
+        cfg = ens.plans[k].cfg
+        mask, sdf = (H(t) for t in ens.masks[k])
+        u0, v0 = (H(t) for t in before[k])
+        dt = st[k]["dt"]
+        kw = dict(brinkman_eta=cfg.brinkman_eta, advection="weno5")
+        ex = R.step_pure(u0, v0, dt, mask, sdf, cfg.dx, cfg.dy, cfg.nu, cfg.U_inf,
+                         mg=R.MGConfig(mode="converge", rtol=1e-12, max_cycles=80), **kw)
+        r6 = R.step_pure(u0, v0, dt, mask, sdf, cfg.dx, cfg.dy, cfg.nu, cfg.U_inf,
+                         mg=R.MGConfig(mode="converge", rtol=1e-6), **kw)
+        f = np.float32
+        r32 = R.step_pure(u0.astype(f), v0.astype(f), f(dt), mask.astype(f), sdf.astype(f),
+                          f(cfg.dx), f(cfg.dy), f(cfg.nu), f(cfg.U_inf),
+                          brinkman_eta=f(cfg.brinkman_eta), advection="weno5",
+                          mg=R.MGConfig(mode="converge", rtol=1e-12, max_cycles=80))
+        for name, g, a, b32, b6 in zip("uvp", ens.state(k), ex, r32, r6):
+            e, e32, e6 = rel(H(g), a), rel(b32, a), rel(b6, a)
+            print(f"instance {k} {spec.nx}x{spec.ny} {name}: gpu {e:.2e} fp32 {e32:.2e} "
+                  f"fp64@1e-6 {e6:.2e}")
+            assert e <= max(1e-5, 2.0 * e32) + 2.0 * e6, (k, name, e, e32, e6)
+
+
 def test_full_ensemble_steps(dev):
     """The 64-instance workload: three graph launches, every solve converged."""
     from aerojax_gb300 import ensemble as E
