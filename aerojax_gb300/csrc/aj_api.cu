@@ -317,6 +317,50 @@ static const StepForks* step_forks(int lane) {
   return &v[lane];
 }
 
+// Concurrent copies on forked branches (aj_step_host): each piece goes on its
+// own stream after an event on s, and s waits for all of them.  Inside a
+// capture the pieces become parallel memcpy nodes.
+constexpr int kCopyLanes = 4;
+struct CopyPiece {
+  void* dst;
+  const void* src;
+  size_t bytes;
+};
+struct CopyForks {
+  cudaStream_t lane[kCopyLanes];
+  cudaEvent_t start, done[kCopyLanes];
+};
+static const CopyForks* copy_forks() {
+  static CopyForks f;
+  static int ok = -1;
+  static std::mutex mu;
+  std::lock_guard<std::mutex> lk(mu);
+  if (ok < 0) {
+    ok = cudaEventCreateWithFlags(&f.start, cudaEventDisableTiming) == cudaSuccess;
+    for (int k = 0; k < kCopyLanes && ok; ++k)
+      ok = cudaStreamCreateWithFlags(&f.lane[k], cudaStreamNonBlocking) == cudaSuccess &&
+           cudaEventCreateWithFlags(&f.done[k], cudaEventDisableTiming) == cudaSuccess;
+  }
+  return ok ? &f : nullptr;
+}
+static int parallel_copies(const CopyPiece (&pc)[kCopyLanes], cudaMemcpyKind kind,
+                           cudaStream_t s) {
+  const CopyForks* f = copy_forks();
+  if (!f) return AJ_ERR_CUDA;
+  std::lock_guard<std::mutex> forks_lock(g_forks_mu);   // the forks' events are shared
+  if (cudaEventRecord(f->start, s) != cudaSuccess) return AJ_ERR_CUDA;
+  for (int k = 0; k < kCopyLanes; ++k) {
+    if (cudaStreamWaitEvent(f->lane[k], f->start, 0) != cudaSuccess ||
+        (pc[k].bytes && cudaMemcpyAsync(pc[k].dst, pc[k].src, pc[k].bytes, kind, f->lane[k]) !=
+                            cudaSuccess) ||
+        cudaEventRecord(f->done[k], f->lane[k]) != cudaSuccess)
+      return AJ_ERR_CUDA;
+  }
+  for (int k = 0; k < kCopyLanes; ++k)
+    if (cudaStreamWaitEvent(s, f->done[k], 0) != cudaSuccess) return AJ_ERR_CUDA;
+  return AJ_OK;
+}
+
 // Host buffers of a step (aj_step_host): the pressure guess is uploaded on a
 // side branch that only the pressure solve waits for, and the new pressure
 // is downloaded on that branch while the correction runs.
@@ -430,9 +474,9 @@ int32_t aj_check_params(const AjStepParams* prm) {
   if (rc != AJ_OK) return rc;
   if (p.mg_mode == AJ_MG_NONE) return AJ_OK;     // predictor / LES only: any flow type
   if (p.variant == AJ_VARIANT_PURE && p.grid_type == AJ_GRID_MAC) return AJ_ERR_PARAM;
-  if (p.flow_type != AJ_FLOW_VON_KARMAN) return AJ_ERR_PARAM;   // step + solver: von Karman
-  if (p.mg_mode == AJ_MG_CONVERGE && p.grid_type == AJ_GRID_MAC && p.flow_type != AJ_FLOW_VON_KARMAN)
-    return AJ_ERR_PARAM;
+  // the lid-driven cavity and Taylor-Green flows run with the reference's own
+  // V-cycle; the converging solver's operator pins the von Karman outlet
+  if (p.flow_type != AJ_FLOW_VON_KARMAN && p.mg_mode != AJ_MG_PARITY) return AJ_ERR_PARAM;
   return AJ_OK;
 }
 
@@ -548,17 +592,24 @@ int32_t aj_step_host(const AjStepParams* prm, const float* h_u, const float* h_v
   std::string key = make_key(5, p, {ws, h_u, h_v, mask, hp, h_u_out, h_v_out, h_p_out, d_in,
                                     d_out, nn_packed, nn_master, stats});
   return run_captured(key, (cudaStream_t)stream, [&](cudaStream_t s) {
-    if (cudaMemcpyAsync(du, h_u, nu * 4, cudaMemcpyHostToDevice, s) != cudaSuccess ||
-        cudaMemcpyAsync(dv, h_v, nv * 4, cudaMemcpyHostToDevice, s) != cudaSuccess)
-      return (int)AJ_ERR_CUDA;
+    // u and v travel as kCopyLanes concurrent copies each way (halves of u
+    // and of v on their own branches), so that several copy engines share
+    // the host link instead of one copy at a time
+    const CopyPiece up[kCopyLanes] = {{du, h_u, nu / 2 * 4},
+                                      {du + nu / 2, h_u + nu / 2, (nu - nu / 2) * 4},
+                                      {dv, h_v, nv / 2 * 4},
+                                      {dv + nv / 2, h_v + nv / 2, (nv - nv / 2) * 4}};
+    if (parallel_copies(up, cudaMemcpyHostToDevice, s) != AJ_OK) return (int)AJ_ERR_CUDA;
     // the pressure guess goes up, and the new pressure comes down, on the
     // step's io stream (enqueue_step), beside the predictor and the correction
     int r = enqueue_step(p, L, ws, du, dv, mask, hp ? dp : nullptr, duo, dvo, dpo, stats, s, nn,
                          0, &io);
     if (r != AJ_OK) return r;
-    if (cudaMemcpyAsync(h_u_out, duo, nu * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaMemcpyAsync(h_v_out, dvo, nv * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess)
-      return (int)AJ_ERR_CUDA;
+    const CopyPiece down[kCopyLanes] = {{h_u_out, duo, nu / 2 * 4},
+                                        {h_u_out + nu / 2, duo + nu / 2, (nu - nu / 2) * 4},
+                                        {h_v_out, dvo, nv / 2 * 4},
+                                        {h_v_out + nv / 2, dvo + nv / 2, (nv - nv / 2) * 4}};
+    if (parallel_copies(down, cudaMemcpyDeviceToHost, s) != AJ_OK) return (int)AJ_ERR_CUDA;
     return (int)AJ_OK;
   });
 }
@@ -627,7 +678,8 @@ int32_t aj_poisson_mg(const AjStepParams* prm, const float* rhs, const float* ma
   AjStepParams p = normalise(*prm);
   int rc = check_params(p);
   if (rc != AJ_OK) return rc;
-  if (p.flow_type != AJ_FLOW_VON_KARMAN || p.mg_mode == AJ_MG_NONE) return AJ_ERR_PARAM;
+  if (p.mg_mode == AJ_MG_NONE) return AJ_ERR_PARAM;
+  if (p.flow_type != AJ_FLOW_VON_KARMAN && p.mg_mode != AJ_MG_PARITY) return AJ_ERR_PARAM;
   Layout L;
   make_layout(p, L);
   if ((rc = ws_ok(L, ws, bytes)) != AJ_OK) return rc;
@@ -720,8 +772,11 @@ int32_t aj_kernel_count(const AjStepParams* prm, int32_t cycles) {
   if (tile_predictor_params_ok(p)) n += tile_predictor_kernels();   // stages + rhs in tile kernels
   else n += (p.fast_mode ? 2 : 3) + 1;                          // predictor stages, rhs
   if (p.mg_mode == AJ_MG_PARITY) {
-    int per_cycle = 2 * L.nlev + (parity_coarsest_fused(L) ? 1 : 10);   // levels, coarsest
+    const int coarse = parity_coarsest_fused(L) ? 1 : 10;
+    int per_cycle = 2 * L.nlev + coarse;                        // levels, coarsest
+    if (p.flow_type == AJ_FLOW_TAYLOR_GREEN) per_cycle = 6 * L.nlev + coarse + 1;   // unfused
     n += 1 + p.v_cycles * per_cycle;                            // begin + cycles
+    if (p.flow_type == AJ_FLOW_LID_DRIVEN_CAVITY) n += 4;       // mean and centre pin
   } else {
     int body = 2 * L.lc + 1 + (L.ld > 0 ? 2 : 0);               // downs, coarse solve, ups
     n += 2 + (cycles > 1 ? cycles : 1) * body + 1;              // init, resid, loop, out+stats

@@ -17,23 +17,62 @@
 
 namespace aj {
 
-// b = rhs (* mask for MAC), b[-1, :] = 0 (multigrid_solver.py:75-77,
-// multigrid_solver_mac.py:78-83)
+// b = rhs (* mask for MAC), b[-1, :] = 0 for the von Karman outlet
+// (multigrid_solver.py:75-77, multigrid_solver_mac.py:78-83)
 __global__ void k_mg_rhs(const float* __restrict__ rhs, const float* __restrict__ mask,
-                         float* __restrict__ b, int nx, int ny, int mac) {
+                         float* __restrict__ b, int nx, int ny, int mac, int outlet) {
   long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (k >= (long)nx * ny) return;
   int i = (int)(k / ny);
   float v = mac ? rhs[k] * mask[k] : rhs[k];
-  b[k] = (i == nx - 1) ? 0.f : v;
+  b[k] = (outlet && i == nx - 1) ? 0.f : v;
 }
 
 int launch_mg_rhs(const AjStepParams& p, const Layout& L, void* ws, const float* rhs,
                   const float* mask, cudaStream_t st) {
   long n = (long)p.nx * p.ny;
   k_mg_rhs<<<cdiv(n, 256), 256, 0, st>>>(rhs, mask, at<float>(ws, L.b0), p.nx, p.ny,
-                                         p.grid_type == AJ_GRID_MAC);
+                                         p.grid_type == AJ_GRID_MAC,
+                                         p.flow_type == AJ_FLOW_VON_KARMAN);
   return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+}
+
+// ---------------------------------------------------------- other flow types
+// Lid-driven cavity: b -= mean(b) before the cycles (multigrid_solver.py:78-80)
+// and p -= p[nx/2, ny/2] after them.  The mean: FP64 block partials, summed
+// in block order by the last block (reproducible), kept in sc->acc[2].
+constexpr int kMeanBlocks = 256;
+__global__ void __launch_bounds__(256) k_mean_partials(const float* __restrict__ b, long n,
+                                                       DevScalars* sc, double* part) {
+  double s = 0.0;
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n;
+       k += (long)gridDim.x * blockDim.x)
+    s += (double)b[k];
+  const double bs = block_sum(s);
+  __shared__ int am_last;
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = bs;
+    __threadfence();
+    am_last = atomicAdd(&sc->red_count, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!am_last || threadIdx.x != 0) return;
+  __threadfence();
+  double t = 0.0;
+  for (unsigned q = 0; q < gridDim.x; ++q) t += __ldcg(part + q);
+  sc->acc[2] = t / (double)n;
+  sc->red_count = 0u;
+}
+__global__ void k_sub_mean(float* __restrict__ b, long n, const DevScalars* sc) {
+  const long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (k < n) b[k] = b[k] - (float)sc->acc[2];
+}
+__global__ void k_store_center(const float* __restrict__ p, long c, DevScalars* sc) {
+  sc->acc[3] = (double)p[c];
+}
+__global__ void k_sub_center(float* __restrict__ p, long n, const DevScalars* sc) {
+  const long k = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (k < n) p[k] = p[k] - (float)sc->acc[3];
 }
 
 // ====================================================================== parity
@@ -371,6 +410,86 @@ __global__ void k_stats(const DevScalars* sc, AjStats* st, int converge_mode) {
   st->abs_residual_sq = abs_sq;
 }
 
+// Taylor-Green: the reference's residual wraps periodically while its
+// smoother keeps edge ghosts (multigrid_solver.py:158-183), so the residual
+// at a boundary cell needs the smoothed iterate on the far side of the
+// domain.  Its V-cycle therefore runs unfused: Jacobi sweeps (k_par_jacobi),
+// then these kernels.
+// r = b - A x with wrapped neighbours, 2x2 average onto the coarser b
+__global__ void __launch_bounds__(256) k_tg_resid_restrict(const float* __restrict__ x,
+                                                           const float* __restrict__ b,
+                                                           float* __restrict__ bc, int n, int m,
+                                                           float ax, float ay, const int* skip) {
+  if (skip && *skip) return;
+  const int J = blockIdx.x * blockDim.x + threadIdx.x;
+  const int I = blockIdx.y * blockDim.y + threadIdx.y;
+  const int nc = n / 2, mc = m / 2;
+  if (I >= nc || J >= mc) return;
+  float r[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int i = 2 * I + (q & 1), j = 2 * J + (q >> 1);
+    const int ip = i + 1 < n ? i + 1 : 0, im = i > 0 ? i - 1 : n - 1;
+    const int jp = j + 1 < m ? j + 1 : 0, jm = j > 0 ? j - 1 : m - 1;
+    const float c = ldg(x + (long)i * m + j);
+    const float lap = ax * (ldg(x + (long)ip * m + j) + ldg(x + (long)im * m + j) - 2.f * c) +
+                      ay * (ldg(x + (long)i * m + jp) + ldg(x + (long)i * m + jm) - 2.f * c);
+    r[q] = ldg(b + (long)i * m + j) - lap;
+  }
+  // summed in the order (0,0), (1,0), (0,1), (1,1) like the tiled kernels
+  bc[(long)I * mc + J] = 0.25f * (r[0] + r[1] + r[2] + r[3]);
+}
+// x += P(xc) in place (the reference prolongation, last row and column 0)
+__global__ void __launch_bounds__(256) k_tg_prolong_add(float* __restrict__ x,
+                                                        const float* __restrict__ xc, int n,
+                                                        int m, const int* skip) {
+  if (skip && *skip) return;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= n || j >= m) return;
+  const long k = (long)i * m + j;
+  x[k] = x[k] + prolong_ref(xc, n / 2, m / 2, i, j);
+}
+// level 0 after the cycle: sum (b - A x)^2 with wrapped neighbours (and, on
+// the first cycle, b^2) in double-FP32 per block, FP64 across blocks; the
+// last block runs the early-exit test
+__global__ void __launch_bounds__(256) k_tg_norm(const float* __restrict__ x,
+                                                 const float* __restrict__ b, int n, int m,
+                                                 float ax, float ay, DevScalars* sc, double dxdy,
+                                                 double tol2, int also_b, const int* skip) {
+  if (skip && *skip) return;
+  df rr{0.f, 0.f}, bb{0.f, 0.f};
+  const long N = (long)n * m;
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < N;
+       k += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(k / m), j = (int)(k - (long)i * m);
+    const int ip = i + 1 < n ? i + 1 : 0, im = i > 0 ? i - 1 : n - 1;
+    const int jp = j + 1 < m ? j + 1 : 0, jm = j > 0 ? j - 1 : m - 1;
+    const float c = ldg(x + k);
+    const float lap = ax * (ldg(x + (long)ip * m + j) + ldg(x + (long)im * m + j) - 2.f * c) +
+                      ay * (ldg(x + (long)i * m + jp) + ldg(x + (long)i * m + jm) - 2.f * c);
+    const float bv = ldg(b + k);
+    const float res = bv - lap;
+    rr = df_add(rr, two_prod(res, res));
+    bb = df_add(bb, two_prod(bv, bv));
+  }
+  const double s = block_sum_df(rr);
+  const double sb = also_b ? block_sum_df(bb) : 0.0;
+  __shared__ int am_last;
+  if (threadIdx.x == 0) {
+    atomicAdd(&sc->acc[0], s);
+    if (also_b) atomicAdd(&sc->acc[1], sb);
+    __threadfence();
+    am_last = atomicAdd(&sc->red_count, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (am_last && threadIdx.x == 0) {
+    __threadfence();
+    sc->red_count = 0u;
+    par_check_body(sc, dxdy, tol2, also_b);
+  }
+}
+
 static int parity_solve(const AjStepParams& p, const Layout& L, void* ws, const float* mask,
                         const float* p0, float* pout, cudaStream_t st) {
   DevScalars* sc = at<DevScalars>(ws, 0);
@@ -383,8 +502,13 @@ static int parity_solve(const AjStepParams& p, const Layout& L, void* ws, const 
   float* T0 = at<float>(ws, L.T0);
   const int* skip = &sc->mg_skip;
   dim3 blk(32, 8);
+  const long N0 = (long)p.nx * p.ny;
   k_par_begin<<<1, 1, 0, st>>>(sc);
-  if (p0) k_copy<<<cdiv((long)p.nx * p.ny, 256), 256, 0, st>>>(p0, pout, (long)p.nx * p.ny);
+  if (p0) k_copy<<<cdiv(N0, 256), 256, 0, st>>>(p0, pout, N0);
+  if (p.flow_type == AJ_FLOW_LID_DRIVEN_CAVITY) {   // b -= mean(b) (multigrid_solver.py:78-80)
+    k_mean_partials<<<kMeanBlocks, 256, 0, st>>>(b0, N0, sc, at<double>(ws, L.part));
+    k_sub_mean<<<cdiv(N0, 256), 256, 0, st>>>(b0, N0, sc);
+  }
 
   auto X = [&](int l) { return l == 0 ? pout : at<float>(ws, L.X[l]); };
   auto T = [&](int l) { return l == 0 ? T0 : at<float>(ws, L.T[l]); };
@@ -394,6 +518,73 @@ static int parity_solve(const AjStepParams& p, const Layout& L, void* ws, const 
     return l == 0 ? mask : at<float>(ws, L.M[l]);
   };
   const int vk = p.flow_type == AJ_FLOW_VON_KARMAN;
+  // the coarsest level's 10 sweeps from zero, ending in X(nl)
+  auto coarsest = [&](const int* sk) {
+    if (parity_coarsest_fused(L)) {
+      const int n = L.ln[nl], m = L.lm[nl];
+      const size_t csm = (size_t)coarse_band_rows(n) * m * 12;
+      cudaFuncSetAttribute(k_par_coarsest, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)kBlockSmemMax);
+      k_par_coarsest<<<kCoarseCtas, kCoarseThreads, csm, st>>>(B(nl), M(nl), X(nl), n, m, ax, ay,
+                                                               den, sk);
+    } else {
+      int n = L.ln[nl], m = L.lm[nl];
+      dim3 g(cdiv(m, 32), cdiv(n, 8));
+      ParJac a{};
+      a.b = B(nl);
+      a.mask = M(nl);
+      a.skip = sk;
+      a.n = n;
+      a.m = m;
+      a.ax = ax;
+      a.ay = ay;
+      a.den = den;
+      for (int s = 0; s < 10; ++s) {
+        a.pin = s == 0 ? nullptr : (s % 2 == 1 ? T(nl) : X(nl));
+        a.pout = s % 2 == 0 ? T(nl) : X(nl);
+        k_par_jacobi<<<g, blk, 0, st>>>(a);
+      }
+    }
+  };
+  if (p.flow_type == AJ_FLOW_TAYLOR_GREEN) {
+    // unfused V-cycle (the wrapped residual needs the other side of the domain):
+    // every level's iterate lives in X(l), T(l) is the sweeps' other buffer
+    for (int cyc = 0; cyc < p.v_cycles; ++cyc) {
+      const int* sk = cyc == 0 ? nullptr : skip;
+      auto sweeps = [&](int l, const float* first_in) {
+        ParJac a{};
+        a.b = B(l);
+        a.mask = M(l);
+        a.skip = sk;
+        a.n = L.ln[l];
+        a.m = L.lm[l];
+        a.ax = ax;
+        a.ay = ay;
+        a.den = den;
+        dim3 g(cdiv(a.m, 32), cdiv(a.n, 8));
+        a.pin = first_in;
+        a.pout = T(l);
+        k_par_jacobi<<<g, blk, 0, st>>>(a);
+        a.pin = T(l);
+        a.pout = X(l);
+        k_par_jacobi<<<g, blk, 0, st>>>(a);
+      };
+      for (int l = 0; l < nl; ++l) {
+        sweeps(l, (l == 0 && !(cyc == 0 && !p0)) ? X(0) : nullptr);
+        dim3 g(cdiv(L.lm[l + 1], 32), cdiv(L.ln[l + 1], 8));
+        k_tg_resid_restrict<<<g, blk, 0, st>>>(X(l), B(l), B(l + 1), L.ln[l], L.lm[l], ax, ay, sk);
+      }
+      coarsest(sk);
+      for (int l = nl - 1; l >= 0; --l) {
+        dim3 g(cdiv(L.lm[l], 32), cdiv(L.ln[l], 8));
+        k_tg_prolong_add<<<g, blk, 0, st>>>(X(l), X(l + 1), L.ln[l], L.lm[l], sk);
+        sweeps(l, X(l));
+      }
+      k_tg_norm<<<kMeanBlocks, 256, 0, st>>>(X(0), B(0), p.nx, p.ny, ax, ay, sc, p.dx * p.dy,
+                                             tol * tol, cyc == 0, sk);
+    }
+    return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
+  }
   auto tile_grid = [&](int l) {
     return l == 0 ? dim3(cdiv(L.lm[l], 64), cdiv(L.ln[l], 16)) : dim3(cdiv(L.lm[l], 32), cdiv(L.ln[l], 8));
   };
@@ -422,31 +613,7 @@ static int parity_solve(const AjStepParams& p, const Layout& L, void* ws, const 
       else k_par_down<8, 32><<<tile_grid(l), kPtThreads, 0, st>>>(a);
     }
     // coarsest: 10 sweeps from zero, ending in X
-    if (parity_coarsest_fused(L)) {
-      const int n = L.ln[nl], m = L.lm[nl];
-      const size_t csm = (size_t)coarse_band_rows(n) * m * 12;
-      cudaFuncSetAttribute(k_par_coarsest, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)kBlockSmemMax);
-      k_par_coarsest<<<kCoarseCtas, kCoarseThreads, csm, st>>>(B(nl), M(nl), X(nl), n, m, ax, ay,
-                                                               den, sk);
-    } else {
-      int n = L.ln[nl], m = L.lm[nl];
-      dim3 g(cdiv(m, 32), cdiv(n, 8));
-      ParJac a{};
-      a.b = B(nl);
-      a.mask = M(nl);
-      a.skip = sk;
-      a.n = n;
-      a.m = m;
-      a.ax = ax;
-      a.ay = ay;
-      a.den = den;
-      for (int s = 0; s < 10; ++s) {
-        a.pin = s == 0 ? nullptr : (s % 2 == 1 ? T(nl) : X(nl));
-        a.pout = s % 2 == 0 ? T(nl) : X(nl);
-        k_par_jacobi<<<g, blk, 0, st>>>(a);
-      }
-    }
+    coarsest(sk);
     // up the V: T + P(coarser X), two post-sweeps, into X; level 0 also
     // forms the residual norm and its last block runs the early-exit test
     // (multigrid_solver.py:222-232)
@@ -474,6 +641,10 @@ static int parity_solve(const AjStepParams& p, const Layout& L, void* ws, const 
       if (l == 0) k_par_up<16, 64, true><<<tile_grid(l), kPtThreads, 0, st>>>(a);
       else k_par_up<8, 32, false><<<tile_grid(l), kPtThreads, 0, st>>>(a);
     }
+  }
+  if (p.flow_type == AJ_FLOW_LID_DRIVEN_CAVITY) {   // p -= p[nx/2, ny/2]
+    k_store_center<<<1, 1, 0, st>>>(pout, (long)(p.nx / 2) * p.ny + p.ny / 2, sc);
+    k_sub_center<<<cdiv(N0, 256), 256, 0, st>>>(pout, N0, sc);
   }
   return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
 }

@@ -19,12 +19,14 @@ namespace aj {
 //   MAC:        div = face differences (solver/operators_mac.py:73-80),
 //               rhs = div/dt, b = rhs*mask (multigrid_solver_mac.py:78)
 //   von Karman: b[-1, :] = 0 (multigrid_solver.py:75-77)
+//   Taylor-Green (collocated): the periodic central divergence
+//               (solver/operators.py:75-78, step.py:192-197)
 __global__ void __launch_bounds__(256) k_rhs(const float* __restrict__ us,
                                              const float* __restrict__ vs,
                                              const float* __restrict__ mask,
                                              float* __restrict__ b, int nx, int ny, float h2x,
                                              float h2y, float idx, float idy, int mac, int pure,
-                                             int outlet, const DevScalars* sc) {
+                                             int outlet, int periodic, const DevScalars* sc) {
   pdl_wait();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   int i = blockIdx.y * blockDim.y + threadIdx.y;
@@ -38,9 +40,15 @@ __global__ void __launch_bounds__(256) k_rhs(const float* __restrict__ us,
     out = ((du + dv) / dt) * ldg(mask + k);
   } else {
     float div = 0.f;
-    if (i > 0 && i < nx - 1 && j > 0 && j < ny - 1)
+    if (periodic) {
+      const int ip = wrapi(i + 1, nx), im = wrapi(i - 1, nx);
+      const int jp = wrapi(j + 1, ny), jm = wrapi(j - 1, ny);
+      div = (ldg(us + (long)ip * ny + j) - ldg(us + (long)im * ny + j)) * h2x +
+            (ldg(vs + (long)i * ny + jp) - ldg(vs + (long)i * ny + jm)) * h2y;
+    } else if (i > 0 && i < nx - 1 && j > 0 && j < ny - 1) {
       div = (ldg(us + (long)(i + 1) * ny + j) - ldg(us + (long)(i - 1) * ny + j)) * h2x +
             (ldg(vs + (long)i * ny + j + 1) - ldg(vs + (long)i * ny + j - 1)) * h2y;
+    }
     out = pure ? (div * ldg(mask + k)) / dt : div / dt;
   }
   if (outlet && i == nx - 1) out = 0.f;
@@ -53,7 +61,8 @@ int launch_rhs(const AjStepParams& p, const Layout& L, void* ws, const float* us
   launch_pdl(true, k_rhs, dim3(grd), dim3(blk), 0, st, us, vs, mask, b, p.nx, p.ny,
              (float)(1.0 / (2.0 * p.dx)), (float)(1.0 / (2.0 * p.dy)), (float)(1.0 / p.dx),
              (float)(1.0 / p.dy), p.grid_type == AJ_GRID_MAC, p.variant == AJ_VARIANT_PURE,
-             p.flow_type == AJ_FLOW_VON_KARMAN, at<DevScalars>(ws, 0));
+             p.flow_type == AJ_FLOW_VON_KARMAN, p.flow_type == AJ_FLOW_TAYLOR_GREEN,
+             at<DevScalars>(ws, 0));
   return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
 }
 
@@ -111,6 +120,62 @@ __device__ __forceinline__ float w_gui(const Corr& c, int a, int b, float dt) {
   return ldg(c.vs + k) - dt * gny(c.p, a, b, c.nx, c.ny, c.idy, c.h2y);
 }
 
+// periodic central gradient (solver/operators.py:11-38), the form both steps
+// use for every flow but the von Karman channel
+__device__ __forceinline__ float gpx(const float* __restrict__ f, int a, int b, int nx, int ny,
+                                     float h2x) {
+  return (ldg(f + (long)wrapi(a + 1, nx) * ny + b) - ldg(f + (long)wrapi(a - 1, nx) * ny + b)) *
+         h2x;
+}
+__device__ __forceinline__ float gpy(const float* __restrict__ f, int a, int b, int ny,
+                                     float h2y) {
+  const float* r = f + (long)a * ny;
+  return (ldg(r + wrapi(b + 1, ny)) - ldg(r + wrapi(b - 1, ny))) * h2y;
+}
+
+// corrected velocity with periodic gradients: step_pure (interface
+// projection on the periodic mask gradient, step.py:259-335) or the GUI step
+// (step_handlers.py:129-140), before the boundary rows
+template <int COMP>
+__device__ __forceinline__ float w_periodic(const Corr& c, int a, int b, float dt) {
+  const long k = (long)a * c.ny + b;
+  float dpx = gpx(c.p, a, b, c.nx, c.ny, c.h2x);
+  float dpy = gpy(c.p, a, b, c.ny, c.h2y);
+  if (c.variant == AJ_VARIANT_PURE) {
+    const float dmx = gpx(c.mask, a, b, c.nx, c.ny, c.h2x);
+    const float dmy = gpy(c.mask, a, b, c.ny, c.h2y);
+    const float gm = sqrtf(dmx * dmx + dmy * dmy);
+    if (gm > c.thresh) {
+      const float nxv = dmx / (gm + 1e-8f), nyv = dmy / (gm + 1e-8f);
+      const float dn = dpx * nxv + dpy * nyv;
+      dpx = dpx - dn * nxv;
+      dpy = dpy - dn * nyv;
+    }
+  }
+  return COMP == 0 ? ldg(c.us + k) - dt * dpx : ldg(c.vs + k) - dt * dpy;
+}
+
+// collocated correction of the lid-driven cavity and Taylor-Green flows:
+// the lid rows of step.py:378-390 (lid velocity 1) / step_handlers.py:162-171
+// (lid velocity U_inf), none for Taylor-Green, then the hard mask
+__device__ __forceinline__ void correct_col_other(const Corr& c, int i, int j, float dt,
+                                                  float* uo, float* vo) {
+  const int nx = c.nx, ny = c.ny;
+  float u, v;
+  if (c.flow == AJ_FLOW_LID_DRIVEN_CAVITY) {
+    const bool edge = i == 0 || i == nx - 1 || j == 0;
+    const float lid = c.variant == AJ_VARIANT_PURE ? 1.f : c.U;
+    u = edge ? 0.f : (j == ny - 1 ? lid : w_periodic<0>(c, i, j, dt));
+    v = (edge || j == ny - 1) ? 0.f : w_periodic<1>(c, i, j, dt);
+  } else {
+    u = w_periodic<0>(c, i, j, dt);
+    v = w_periodic<1>(c, i, j, dt);
+  }
+  const bool m = ldg(c.mask + (long)i * ny + j) > 0.5f;
+  *uo = m ? u : 0.f;
+  *vo = m ? v : 0.f;
+}
+
 __global__ void __launch_bounds__(256) k_correct_col(Corr c) {
   pdl_wait();
   int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -119,6 +184,10 @@ __global__ void __launch_bounds__(256) k_correct_col(Corr c) {
   if (i >= nx || j >= ny) return;
   long k = (long)i * ny + j;
   const float dt = c.sc->dt_corr;
+  if (c.flow != AJ_FLOW_VON_KARMAN) {
+    correct_col_other(c, i, j, dt, c.uo + k, c.vo + k);
+    return;
+  }
   float uo, vo;
   int ai = (i == nx - 1) ? nx - 2 : i;
   if (c.variant == AJ_VARIANT_PURE) {
@@ -145,6 +214,33 @@ __global__ void __launch_bounds__(256) k_correct_mac(Corr c) {
   int i = blockIdx.y * blockDim.y + threadIdx.y;
   const int nx = c.nx, ny = c.ny;
   const float dt = c.sc->dt_corr;
+  if (c.flow != AJ_FLOW_VON_KARMAN) {
+    // the same staggered gradients; the lid-driven cavity's rows
+    // (step_handlers.py:265-274), none for Taylor-Green
+    const bool ldc = c.flow == AJ_FLOW_LID_DRIVEN_CAVITY;
+    if (i <= nx && j < ny) {
+      float o;
+      if (ldc && (i == 0 || i == nx || j == 0)) o = 0.f;
+      else if (ldc && j == ny - 1) o = c.U;
+      else {
+        const float dpx = (ldg(c.p + (long)clampi(i, nx) * ny + j) -
+                           ldg(c.p + (long)clampi(i - 1, nx) * ny + j)) * c.idx;
+        o = ldg(c.us + (long)i * ny + j) - dt * dpx;
+      }
+      c.uo[(long)i * ny + j] = o;
+    }
+    if (i < nx && j <= ny) {
+      float o;
+      if (ldc && (i == 0 || i == nx - 1 || j == 0 || j == ny)) o = 0.f;
+      else {
+        const float dpy = (ldg(c.p + (long)i * ny + clampi(j, ny)) -
+                           ldg(c.p + (long)i * ny + clampi(j - 1, ny))) * c.idy;
+        o = ldg(c.vs + (long)i * (ny + 1) + j) - dt * dpy;
+      }
+      c.vo[(long)i * (ny + 1) + j] = o;
+    }
+    return;
+  }
   if (i <= nx && j < ny) {
     float o;
     if (j == 0 || j == ny - 1) o = 0.f;

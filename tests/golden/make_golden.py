@@ -7,7 +7,8 @@ or by the GPU tests; the fixtures it writes (``tests/golden/*.npz``) are what
 travels.
 
 Usage:  python tests/golden/make_golden.py REFERENCE_ROOT
-(or set $AEROJAX_REF to the AeroJAX checkout and omit the argument).
+(or set $AEROJAX_REF to the AeroJAX checkout and omit the argument;
+$AEROJAX_GOLDEN_ONLY=prefix writes only the fixtures whose names start with it).
 """
 from __future__ import annotations
 
@@ -272,10 +273,51 @@ def main(root):
     out["geometry"] = dict(X=X, Y=Y, sdf_naca0012=A(sdf_n), sdf_naca2412=A(sdf_n2),
                            sdf_three=A(sdf_3))
 
+    # --- the other flow types: lid-driven cavity and Taylor-Green -----------------
+    # (multigrid_solver.py:75-80 and :173-183, step.py:259-264 and :378-390,
+    # step_handlers.py:129-183 / :240-274 with sim_params.flow_type)
+    for flow, tag in (("lid_driven_cavity", "ldc"), ("taylor_green", "tg")):
+        cm = flow_case(64, 32, 4.0, 2.0, 1)
+        rhs = np.random.default_rng(11).standard_normal((64, 32)) * 10.0
+        p = R.mg.poisson_multigrid(rhs, cm["mask"], cm["dx"], cm["dy"], v_cycles=3, flow_type=flow)
+        pm = R.mgm.poisson_multigrid_mac(rhs, cm["mask"], cm["dx"], cm["dy"], v_cycles=3,
+                                         flow_type=flow)
+        out[f"flow_mg_{tag}"] = dict(rhs=rhs, mask=cm["mask"], dx=cm["dx"], dy=cm["dy"],
+                                     v_cycles=3, flow=flow, p=A(p), p_mac=A(pm))
+        st = R.params.SimState(u=c["u"], v=c["v"], p=np.zeros((64, 32)), u_prev=c["u"],
+                               v_prev=c["v"], c=np.zeros((64, 32)), dt=dt, iteration=0)
+        res = R.step.step_pure(st, c["mask"], c["sdf"], c["dx"], c["dy"], nu, U, v_cycles=3,
+                               brinkman_eta=1e-3, flow_type=flow)
+        out[f"flow_step_pure_{tag}"] = dict(u=c["u"], v=c["v"], mask=c["mask"], sdf=c["sdf"],
+                                            dx=c["dx"], dy=c["dy"], dt=dt, nu=nu, U=U, eta=1e-3,
+                                            v_cycles=3, flow=flow, u_new=A(res.u),
+                                            v_new=A(res.v), p=A(res.p))
+        s = fake_solver(c, nu=nu, U=U, eta=1e-3, v_cycles=3, dt=dt, grid_type="collocated",
+                        use_les=True, les_model="smagorinsky", cs=0.17, hyper=0.01)
+        s.sim_params.flow_type = flow
+        un, vn, p = R.sh._step_collocated(s, J(c["u"]), J(c["v"]), J(c["mask"]), dt)
+        out[f"flow_gui_col_{tag}"] = dict(u=c["u"], v=c["v"], mask=c["mask"], sdf=c["sdf"],
+                                          dx=c["dx"], dy=c["dy"], dt=dt, nu=nu, U=U, eta=1e-3,
+                                          v_cycles=3, use_les=1, dynamic=0, cs=0.17, hyper=0.01,
+                                          flow=flow, u_new=A(un), v_new=A(vn), p=A(p))
+        s = fake_solver(c, nu=nu, U=U, eta=1e-3, v_cycles=3, dt=dt, grid_type="mac",
+                        use_les=True, les_model="smagorinsky", cs=0.17, hyper=0.0)
+        s.sim_params.flow_type = flow
+        un, vn, p = R.sh._step_mac(s, J(um), J(vm), J(c["mask"]), dt)
+        out[f"flow_gui_mac_{tag}"] = dict(u=um, v=vm, mask=c["mask"], dx=c["dx"], dy=c["dy"],
+                                          dt=dt, nu=nu, U=U, eta=1e-3, v_cycles=3, use_les=1,
+                                          dynamic=0, cs=0.17, hyper=0.0, flow=flow, u_new=A(un),
+                                          v_new=A(vn), p=A(p))
+
+    only = os.environ.get("AEROJAX_GOLDEN_ONLY", "")
+    n = 0
     for name, d in out.items():
+        if only and not name.startswith(only):
+            continue
         path = os.path.join(HERE, f"{name}.npz")
         np.savez_compressed(path, **{k: np.asarray(v) for k, v in d.items()})
-    print(f"wrote {len(out)} fixtures to {HERE}")
+        n += 1
+    print(f"wrote {n} fixtures to {HERE}")
 
 
 if __name__ == "__main__":

@@ -125,3 +125,35 @@ def test_diagnostics_match_reference():
             tag = ("mac_" if mac else "") + ("per" if per else "np")
             assert np.array_equal(vort, z["vort_" + tag]), tag
             assert np.allclose(div, z["div_" + tag], rtol=0, atol=1e-12), tag
+
+
+@pytest.mark.parametrize("tag", ["ldc", "tg"])
+def test_other_flow_types(tag):
+    """Lid-driven cavity and Taylor-Green: the reference's multigrid (mean
+    subtraction, wrapped residual), step_pure and both GUI steps with that
+    flow type, run from its own source (fixtures flow_*)."""
+    g = golden(f"flow_mg_{tag}")
+    flow = str(g["flow"])
+    p = R.poisson_multigrid(g["rhs"], g["mask"], float(g["dx"]), float(g["dy"]),
+                            v_cycles=int(g["v_cycles"]), flow_type=flow)
+    pm = R.poisson_multigrid_mac(g["rhs"], g["mask"], float(g["dx"]), float(g["dy"]),
+                                 v_cycles=int(g["v_cycles"]), flow_type=flow)
+    assert rel(p, g["p"]) < TOL and rel(pm, g["p_mac"]) < TOL
+    g = golden(f"flow_step_pure_{tag}")
+    un, vn, pn = R.step_pure(g["u"], g["v"], float(g["dt"]), g["mask"], g["sdf"], float(g["dx"]),
+                             float(g["dy"]), float(g["nu"]), float(g["U"]),
+                             v_cycles=int(g["v_cycles"]), brinkman_eta=float(g["eta"]),
+                             flow_type=flow)
+    assert rel(un, g["u_new"]) < TOL and rel(vn, g["v_new"]) < TOL and rel(pn, g["p"]) < TOL
+    for grid in ("col", "mac"):
+        g = golden(f"flow_gui_{grid}_{tag}")
+        mac = grid == "mac"
+        un, vn, pn = R.step_gui(g["u"], g["v"], g["mask"], float(g["dt"]),
+                                sdf=None if mac else g["sdf"], dx=float(g["dx"]),
+                                dy=float(g["dy"]), nu=float(g["nu"]), U_inf=float(g["U"]),
+                                grid_type="mac" if mac else "collocated", use_les=True,
+                                les_model="smagorinsky", smagorinsky_constant=float(g["cs"]),
+                                nu_hyper_ratio=float(g["hyper"]), brinkman_eta=float(g["eta"]),
+                                v_cycles=int(g["v_cycles"]), flow_type=flow)
+        for a, key in ((un, "u_new"), (vn, "v_new"), (pn, "p")):
+            assert rel(a, g[key]) < TOL, (grid, key, rel(a, g[key]))
