@@ -317,50 +317,6 @@ static const StepForks* step_forks(int lane) {
   return &v[lane];
 }
 
-// Concurrent copies on forked branches (aj_step_host): each piece goes on its
-// own stream after an event on s, and s waits for all of them.  Inside a
-// capture the pieces become parallel memcpy nodes.
-constexpr int kCopyLanes = 4;
-struct CopyPiece {
-  void* dst;
-  const void* src;
-  size_t bytes;
-};
-struct CopyForks {
-  cudaStream_t lane[kCopyLanes];
-  cudaEvent_t start, done[kCopyLanes];
-};
-static const CopyForks* copy_forks() {
-  static CopyForks f;
-  static int ok = -1;
-  static std::mutex mu;
-  std::lock_guard<std::mutex> lk(mu);
-  if (ok < 0) {
-    ok = cudaEventCreateWithFlags(&f.start, cudaEventDisableTiming) == cudaSuccess;
-    for (int k = 0; k < kCopyLanes && ok; ++k)
-      ok = cudaStreamCreateWithFlags(&f.lane[k], cudaStreamNonBlocking) == cudaSuccess &&
-           cudaEventCreateWithFlags(&f.done[k], cudaEventDisableTiming) == cudaSuccess;
-  }
-  return ok ? &f : nullptr;
-}
-static int parallel_copies(const CopyPiece (&pc)[kCopyLanes], cudaMemcpyKind kind,
-                           cudaStream_t s) {
-  const CopyForks* f = copy_forks();
-  if (!f) return AJ_ERR_CUDA;
-  std::lock_guard<std::mutex> forks_lock(g_forks_mu);   // the forks' events are shared
-  if (cudaEventRecord(f->start, s) != cudaSuccess) return AJ_ERR_CUDA;
-  for (int k = 0; k < kCopyLanes; ++k) {
-    if (cudaStreamWaitEvent(f->lane[k], f->start, 0) != cudaSuccess ||
-        (pc[k].bytes && cudaMemcpyAsync(pc[k].dst, pc[k].src, pc[k].bytes, kind, f->lane[k]) !=
-                            cudaSuccess) ||
-        cudaEventRecord(f->done[k], f->lane[k]) != cudaSuccess)
-      return AJ_ERR_CUDA;
-  }
-  for (int k = 0; k < kCopyLanes; ++k)
-    if (cudaStreamWaitEvent(s, f->done[k], 0) != cudaSuccess) return AJ_ERR_CUDA;
-  return AJ_OK;
-}
-
 // Host buffers of a step (aj_step_host): the pressure guess is uploaded on a
 // side branch that only the pressure solve waits for, and the new pressure
 // is downloaded on that branch while the correction runs.
@@ -592,24 +548,20 @@ int32_t aj_step_host(const AjStepParams* prm, const float* h_u, const float* h_v
   std::string key = make_key(5, p, {ws, h_u, h_v, mask, hp, h_u_out, h_v_out, h_p_out, d_in,
                                     d_out, nn_packed, nn_master, stats});
   return run_captured(key, (cudaStream_t)stream, [&](cudaStream_t s) {
-    // u and v travel as kCopyLanes concurrent copies each way (halves of u
-    // and of v on their own branches), so that several copy engines share
-    // the host link instead of one copy at a time
-    const CopyPiece up[kCopyLanes] = {{du, h_u, nu / 2 * 4},
-                                      {du + nu / 2, h_u + nu / 2, (nu - nu / 2) * 4},
-                                      {dv, h_v, nv / 2 * 4},
-                                      {dv + nv / 2, h_v + nv / 2, (nv - nv / 2) * 4}};
-    if (parallel_copies(up, cudaMemcpyHostToDevice, s) != AJ_OK) return (int)AJ_ERR_CUDA;
+    // u and v as one copy each way on the step's stream: splitting them over
+    // four concurrent branches measured no faster (the host link, not the
+    // number of copy engines, sets the rate)
+    if (cudaMemcpyAsync(du, h_u, nu * 4, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemcpyAsync(dv, h_v, nv * 4, cudaMemcpyHostToDevice, s) != cudaSuccess)
+      return (int)AJ_ERR_CUDA;
     // the pressure guess goes up, and the new pressure comes down, on the
     // step's io stream (enqueue_step), beside the predictor and the correction
     int r = enqueue_step(p, L, ws, du, dv, mask, hp ? dp : nullptr, duo, dvo, dpo, stats, s, nn,
                          0, &io);
     if (r != AJ_OK) return r;
-    const CopyPiece down[kCopyLanes] = {{h_u_out, duo, nu / 2 * 4},
-                                        {h_u_out + nu / 2, duo + nu / 2, (nu - nu / 2) * 4},
-                                        {h_v_out, dvo, nv / 2 * 4},
-                                        {h_v_out + nv / 2, dvo + nv / 2, (nv - nv / 2) * 4}};
-    if (parallel_copies(down, cudaMemcpyDeviceToHost, s) != AJ_OK) return (int)AJ_ERR_CUDA;
+    if (cudaMemcpyAsync(h_u_out, duo, nu * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaMemcpyAsync(h_v_out, dvo, nv * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+      return (int)AJ_ERR_CUDA;
     return (int)AJ_OK;
   });
 }

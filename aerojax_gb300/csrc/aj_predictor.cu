@@ -656,14 +656,20 @@ __device__ float rhs_mac_u(const RkMac& a, int i, int j) {
     return 0.5f * (vw_at(a, a.vin, ci, j + 1) + vw_at(a, a.vin, ci, j));
   };
   float v_at_u = 0.5f * (vcen(i) + vcen(i - 1));
-  float uxm = uw_at(a, a.uin, i > 0 ? i - 1 : 0, j);
-  float uxp = uw_at(a, a.uin, i < nx ? i + 1 : nx, j);
+  // the periodic (Taylor-Green) flow wraps both differences (rk3_mac.py's
+  // wrap padding and np.roll), every other flow pads by the edge
+  const bool per = a.flow == AJ_FLOW_TAYLOR_GREEN;
+  float uxm = uw_at(a, a.uin, per ? wrapi(i - 1, nx + 1) : (i > 0 ? i - 1 : 0), j);
+  float uxp = uw_at(a, a.uin, per ? wrapi(i + 1, nx + 1) : (i < nx ? i + 1 : nx), j);
   float back = (uw - uxm) * a.idx, fwd = (uxp - uw) * a.idx;
   // upwind blend 0.5 (1 + tanh(u / 0.05)) of rk3_mac.py, the argument formed as 20 u
   float al = 0.5f * (1.f + tanhf(uw * 20.f));
   float adv_x = uw * (al * back + (1.f - al) * fwd);
   float du_dy;
-  if (j == 0) du_dy = (uw_at(a, a.uin, i, 1) - uw) * a.idy;
+  if (per)
+    du_dy = (uw_at(a, a.uin, i, wrapi(j + 1, ny)) - uw_at(a, a.uin, i, wrapi(j - 1, ny))) *
+            (0.5f * a.idy);
+  else if (j == 0) du_dy = (uw_at(a, a.uin, i, 1) - uw) * a.idy;
   else if (j == ny - 1) du_dy = (uw - uw_at(a, a.uin, i, ny - 2)) * a.idy;
   else du_dy = (uw_at(a, a.uin, i, j + 1) - uw_at(a, a.uin, i, j - 1)) * (0.5f * a.idy);
   float adv = (adv_x + v_at_u * du_dy) * xface(a.mask, i, j, nx, ny);
@@ -683,13 +689,17 @@ __device__ float rhs_mac_v(const RkMac& a, int i, int j) {
     return 0.5f * (uw_at(a, a.uin, i + 1, cj) + uw_at(a, a.uin, i, cj));
   };
   float u_at_v = 0.5f * (ucen(j) + ucen(j - 1));
-  float vym = vw_at(a, a.vin, i, j > 0 ? j - 1 : 0);
-  float vyp = vw_at(a, a.vin, i, j < ny ? j + 1 : ny);
+  const bool per = a.flow == AJ_FLOW_TAYLOR_GREEN;
+  float vym = vw_at(a, a.vin, i, per ? wrapi(j - 1, ny + 1) : (j > 0 ? j - 1 : 0));
+  float vyp = vw_at(a, a.vin, i, per ? wrapi(j + 1, ny + 1) : (j < ny ? j + 1 : ny));
   float back = (vw - vym) * a.idy, fwd = (vyp - vw) * a.idy;
   float al = 0.5f * (1.f + tanhf(vw * 20.f));
   float adv_y = vw * (al * back + (1.f - al) * fwd);
   float dv_dx;
-  if (i == 0) dv_dx = (vw_at(a, a.vin, 1, j) - vw) * a.idx;
+  if (per)
+    dv_dx = (vw_at(a, a.vin, wrapi(i + 1, nx), j) - vw_at(a, a.vin, wrapi(i - 1, nx), j)) *
+            (0.5f * a.idx);
+  else if (i == 0) dv_dx = (vw_at(a, a.vin, 1, j) - vw) * a.idx;
   else if (i == nx - 1) dv_dx = (vw - vw_at(a, a.vin, nx - 2, j)) * a.idx;
   else dv_dx = (vw_at(a, a.vin, i + 1, j) - vw_at(a, a.vin, i - 1, j)) * (0.5f * a.idx);
   float adv = (u_at_v * dv_dx + adv_y) * yface(a.mask, i, j, nx, ny);
