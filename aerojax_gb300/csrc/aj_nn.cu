@@ -170,29 +170,46 @@ __device__ __forceinline__ void conv_tile(const ConvArgs& cv, int t, int co0,
     __syncthreads();
   }
   if (Xc) {   // input = nearest 2x up-sampling of Xc (H/2 x W/2) + X
-    constexpr int C4 = CIN / 4;
+    // four loads in flight per thread, then their four additions
+    constexpr int C4 = CIN / 4, XB = 4;
     const int Hc = H >> 1, Wc = W >> 1;
-    for (int e = tid; e < CT_HALO * C4; e += CONV_THREADS) {
-      const int px = e / C4, q = e - px * C4;
-      const int hy = px / (CT + 2), hx = px - hy * (CT + 2);
-      const int gh = h0 - 1 + hy, gw = w0 - 1 + hx;
-      if (gh >= 0 && gh < H && gw >= 0 && gw < W) {
-        const float4 u = __ldcg(reinterpret_cast<const float4*>(
-            Xc + (((long)n * Hc + (gh >> 1)) * Wc + (gw >> 1)) * CIN + q * 4));
-        float4* a = reinterpret_cast<float4*>(As + px * AS + q * 4);
+    for (int e0 = tid; e0 < CT_HALO * C4; e0 += XB * CONV_THREADS) {
+      float4 u[XB];
+      int dst[XB];
+#pragma unroll
+      for (int k = 0; k < XB; ++k) {
+        const int e = e0 + k * CONV_THREADS;
+        const int px = e / C4, q = e - px * C4;
+        const int hy = px / (CT + 2), hx = px - hy * (CT + 2);
+        const int gh = h0 - 1 + hy, gw = w0 - 1 + hx;
+        dst[k] = -1;
+        if (e < CT_HALO * C4 && gh >= 0 && gh < H && gw >= 0 && gw < W) {
+          u[k] = __ldcg(reinterpret_cast<const float4*>(
+              Xc + (((long)n * Hc + (gh >> 1)) * Wc + (gw >> 1)) * CIN + q * 4));
+          dst[k] = px * AS + q * 4;
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < XB; ++k) {
+        if (dst[k] < 0) continue;
+        float4* a = reinterpret_cast<float4*>(As + dst[k]);
         float4 v = *a;
-        v.x = u.x + v.x;
-        v.y = u.y + v.y;
-        v.z = u.z + v.z;
-        v.w = u.w + v.w;
+        v.x = u[k].x + v.x;
+        v.y = u[k].y + v.y;
+        v.z = u[k].z + v.z;
+        v.w = u[k].w + v.w;
         *a = v;
       }
     }
     __syncthreads();
   }
-  float acc[NT][4];
+  // two accumulator sets, even and odd 16-channel steps, halve each chain of
+  // dependent MMAs again; they are added before the hand-over
+  float acc[NT][4], acc2[NT][4];
 #pragma unroll
-  for (int q = 0; q < NT; ++q) acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = 0.f;
+  for (int q = 0; q < NT; ++q)
+#pragma unroll
+    for (int e = 0; e < 4; ++e) acc[q][e] = acc2[q][e] = 0.f;
   // warp w: tile rows 2 (w & 3) and 2 (w & 3) + 1 (fragment rows g, g + 8);
   // warps 0-3 run taps 0-4 and warps 4-7 taps 5-8, which halves each chain
   // of dependent MMAs (9 Cin / 16 of them in one warp before)
@@ -221,10 +238,14 @@ __device__ __forceinline__ void conv_tile(const ConvArgs& cv, int t, int co0,
         uint32_t b[2];
         b[0] = *reinterpret_cast<const uint32_t*>(bp);
         b[1] = *reinterpret_cast<const uint32_t*>(bp + 8);
-        mma_bf16(acc[q], a, b);
+        mma_bf16((ks & 1) ? acc2[q] : acc[q], a, b);
       }
     }
   }
+#pragma unroll
+  for (int q = 0; q < NT; ++q)
+#pragma unroll
+    for (int e = 0; e < 4; ++e) acc[q][e] += acc2[q][e];
   // warps 4-7 hand their partial sums to warps 0-3 through the (now free)
   // halo buffer; the sum is (taps 0-4) + (taps 5-8)
   static_assert(4 * NT * 4 * 32 <= CT_HALO * AS, "the hand-over must fit the halo buffer");
