@@ -60,15 +60,22 @@ __device__ __forceinline__ void mma_bf16(float* d, const uint32_t* a, const uint
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
+// four 8x8 BF16 matrices from shared memory, one row address per lane
+__device__ __forceinline__ void ldsm_x4(uint32_t* r, unsigned addr) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(addr));
+}
+
 // ---------------------------------------------------------------- convolution
 // Implicit GEMM on 8 x 8 pixel tiles: M = 64 pixels (16 per warp: two tile
 // rows), N = BN output channels of the block, K = 9 taps x Cin.  The block
-// stages the 10 x 10 x Cin FP32 halo of its tile (zero-filled outside the
-// image) and the BF16 weights of all 9 taps for its BN channels
-// (WT[tap][co][ci]) with cp.async: one wait, one barrier, then the whole K
-// loop runs from shared memory, every tap an offset into the halo; operands
-// are rounded to BF16 as the fragments are built.  Row strides of Cin + 8
-// keep the fragment loads free of bank conflicts.
+// stages the BF16 weights of all 9 taps for its BN channels (WT[tap][co][ci])
+// with cp.async and the 10 x 10 x Cin halo of its tile (zero-filled outside
+// the image), rounded once to BF16 as it is stored; one barrier, then the
+// whole K loop runs from shared memory, every tap an offset into the halo,
+// the fragments loaded by ldmatrix.  Row strides of Cin + 8 BF16 keep the
+// ldmatrix rows 16-byte aligned and free of bank conflicts.
 constexpr int CT = 8;                       // pixel tile edge
 constexpr int CT_HALO = (CT + 2) * (CT + 2);
 constexpr int CONV_THREADS = 256;   // 8 warps: 4 pixel-row pairs x 2 halves of K
@@ -76,11 +83,6 @@ constexpr int CONV_THREADS = 256;   // 8 warps: 4 pixel-row pairs x 2 halves of 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
-}
-// 16 bytes, or zeros when src_bytes == 0 (the source is then not read)
-__device__ __forceinline__ void cp_async16z(void* smem, const void* gmem, int src_bytes) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(src_bytes));
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
 template <int NPEND>
@@ -90,8 +92,11 @@ __device__ __forceinline__ void cp_async_wait() {
 
 template <int CIN, int NT>
 struct ConvSmem {
-  static constexpr int AS = CIN + 8, BN = NT * 8;   // AS: FP32 halo stride, BF16 weight stride
-  static constexpr size_t bytes = (size_t)CT_HALO * AS * 4 + (size_t)9 * BN * AS * 2;
+  static constexpr int AS = CIN + 8, BN = NT * 8;   // BF16 row stride of the halo and the weights
+  static constexpr size_t a_bytes = (size_t)CT_HALO * AS * 2;
+  static constexpr size_t bytes = a_bytes + (size_t)9 * BN * AS * 2;
+  static_assert(a_bytes % 16 == 0 && (AS * 2) % 16 == 0, "ldmatrix rows must be 16-byte aligned");
+  static_assert((size_t)4 * NT * 4 * 32 * 4 <= bytes, "the K halves' hand-over must fit");
 };
 
 // One convolution's operands (NHWC activations, WT[tap][Cout][Cin] BF16).
@@ -125,8 +130,8 @@ __device__ __forceinline__ void conv_tile(const ConvArgs& cv, int t, int co0,
   const float* __restrict__ Xc = cv.Xc;
   using S = ConvSmem<CIN, NT>;
   constexpr int AS = S::AS, BN = S::BN;
-  float* As = reinterpret_cast<float*>(conv_sm);                              // [px][AS] FP32
-  __nv_bfloat16* Bs = reinterpret_cast<__nv_bfloat16*>(As + CT_HALO * AS);   // [tap][BN][AS]
+  __nv_bfloat16* As = reinterpret_cast<__nv_bfloat16*>(conv_sm);          // [px][AS] BF16
+  __nv_bfloat16* Bs = reinterpret_cast<__nv_bfloat16*>(conv_sm + S::a_bytes);   // [tap][BN][AS]
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int g = lane >> 2, tg = lane & 3;
   const int tilesW = (W + CT - 1) / CT, tilesH = (H + CT - 1) / CT;
@@ -147,62 +152,67 @@ __device__ __forceinline__ void conv_tile(const ConvArgs& cv, int t, int co0,
   // the weights do not depend on the previous layer: staged before the wait
   // for the previous layer's output
   if (PDL) pdl_wait();
-  {  // the halo tile, FP32, zeros outside the image
-    constexpr int C4 = CIN / 4;
-    for (int e = tid; e < CT_HALO * C4; e += CONV_THREADS) {
-      const int px = e / C4, q = e - px * C4;
-      const int hy = px / (CT + 2), hx = px - hy * (CT + 2);
-      const int gh = h0 - 1 + hy, gw = w0 - 1 + hx;
-      const bool in = gh >= 0 && gh < H && gw >= 0 && gw < W;
-      const float* src = in ? X + (((long)n * H + gh) * W + gw) * CIN + q * 4 : X;
-      cp_async16z(As + px * AS + q * 4, src, in ? 16 : 0);
-    }
-    cp_async_commit();
-  }
-  cp_async_wait<0>();
-  __syncthreads();
-  if (cv.norm) {   // k_nn_norm's scaling of the staged features (same arithmetic)
-    const float ir = (float)(1.0 / cv.norm->nn_rms_r), ip = (float)(1.0 / cv.norm->nn_rms_p);
-    for (int px = tid; px < CT_HALO; px += CONV_THREADS) {
-      As[px * AS] *= ir;
-      As[px * AS + 2] *= ip;
-    }
-    __syncthreads();
-  }
-  if (Xc) {   // input = nearest 2x up-sampling of Xc (H/2 x W/2) + X
-    // four loads in flight per thread, then their four additions
-    constexpr int C4 = CIN / 4, XB = 4;
+  {  // the halo tile, rounded once to BF16 (the MMA operands), zeros outside
+     // the image.  The FP32 input is formed first exactly as the layer
+     // defines it - the features scaled by 1 / their RMS (k_nn_norm's
+     // arithmetic), or the decoder's up2(Xc) + X - and rounded as the
+     // fragments were before.  Four 8-channel pieces per thread in flight.
+    constexpr int C8 = CIN / 8, XB = 4;
     const int Hc = H >> 1, Wc = W >> 1;
-    for (int e0 = tid; e0 < CT_HALO * C4; e0 += XB * CONV_THREADS) {
-      float4 u[XB];
-      int dst[XB];
+    float ir = 1.f, ip = 1.f;
+    if (cv.norm) {
+      ir = (float)(1.0 / cv.norm->nn_rms_r);
+      ip = (float)(1.0 / cv.norm->nn_rms_p);
+    }
+    for (int e0 = tid; e0 < CT_HALO * C8; e0 += XB * CONV_THREADS) {
+      float4 xa[XB], xb[XB], ca[XB], cb[XB];
+      bool in[XB];
 #pragma unroll
       for (int k = 0; k < XB; ++k) {
         const int e = e0 + k * CONV_THREADS;
-        const int px = e / C4, q = e - px * C4;
+        const int px = e / C8, q = e - px * C8;
         const int hy = px / (CT + 2), hx = px - hy * (CT + 2);
         const int gh = h0 - 1 + hy, gw = w0 - 1 + hx;
-        dst[k] = -1;
-        if (e < CT_HALO * C4 && gh >= 0 && gh < H && gw >= 0 && gw < W) {
-          u[k] = __ldcg(reinterpret_cast<const float4*>(
-              Xc + (((long)n * Hc + (gh >> 1)) * Wc + (gw >> 1)) * CIN + q * 4));
-          dst[k] = px * AS + q * 4;
+        in[k] = e < CT_HALO * C8 && gh >= 0 && gh < H && gw >= 0 && gw < W;
+        xa[k] = xb[k] = ca[k] = cb[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (in[k]) {
+          const float4* src =
+              reinterpret_cast<const float4*>(X + (((long)n * H + gh) * W + gw) * CIN + q * 8);
+          xa[k] = __ldcg(src);
+          xb[k] = __ldcg(src + 1);
+          if (Xc) {
+            const float4* cs = reinterpret_cast<const float4*>(
+                Xc + (((long)n * Hc + (gh >> 1)) * Wc + (gw >> 1)) * CIN + q * 8);
+            ca[k] = __ldcg(cs);
+            cb[k] = __ldcg(cs + 1);
+          }
         }
       }
 #pragma unroll
       for (int k = 0; k < XB; ++k) {
-        if (dst[k] < 0) continue;
-        float4* a = reinterpret_cast<float4*>(As + dst[k]);
-        float4 v = *a;
-        v.x = u[k].x + v.x;
-        v.y = u[k].y + v.y;
-        v.z = u[k].z + v.z;
-        v.w = u[k].w + v.w;
-        *a = v;
+        const int e = e0 + k * CONV_THREADS;
+        if (e >= CT_HALO * C8) break;
+        const int px = e / C8, q = e - px * C8;
+        float4 a = xa[k], b = xb[k];
+        if (cv.norm && q == 0) {
+          a.x *= ir;
+          a.z *= ip;
+        }
+        if (Xc && in[k]) {
+          a = make_float4(ca[k].x + a.x, ca[k].y + a.y, ca[k].z + a.z, ca[k].w + a.w);
+          b = make_float4(cb[k].x + b.x, cb[k].y + b.y, cb[k].z + b.z, cb[k].w + b.w);
+        }
+        uint4 v;
+        v.x = pack_bf16x2(a.x, a.y);
+        v.y = pack_bf16x2(a.z, a.w);
+        v.z = pack_bf16x2(b.x, b.y);
+        v.w = pack_bf16x2(b.z, b.w);
+        *reinterpret_cast<uint4*>(As + px * AS + q * 8) = v;
       }
     }
-    __syncthreads();
   }
+  cp_async_wait<0>();
+  __syncthreads();
   // two accumulator sets, even and odd 16-channel steps, halve each chain of
   // dependent MMAs again; they are added before the hand-over
   float acc[NT][4], acc2[NT][4];
@@ -212,33 +222,33 @@ __device__ __forceinline__ void conv_tile(const ConvArgs& cv, int t, int co0,
     for (int e = 0; e < 4; ++e) acc[q][e] = acc2[q][e] = 0.f;
   // warp w: tile rows 2 (w & 3) and 2 (w & 3) + 1 (fragment rows g, g + 8);
   // warps 0-3 run taps 0-4 and warps 4-7 taps 5-8, which halves each chain
-  // of dependent MMAs (9 Cin / 16 of them in one warp before)
+  // of dependent MMAs (9 Cin / 16 of them in one warp before).  Fragments
+  // come by ldmatrix: lane l addresses row l & 7 of 8x8 matrix l >> 3 - for
+  // A the pixel (tile row + (m & 1), column r + dx) at channel offset
+  // (m >> 1) * 8, for B output channel 8 (m >> 1) + r of the pair of
+  // 8-channel groups at channel offset (m & 1) * 8.
   const int prow = warp & 3, kh = warp >> 2;
   const int ty0 = 2 * prow;
+  const int lm = lane >> 3, lr = lane & 7;
+  const unsigned as0 = (unsigned)__cvta_generic_to_shared(As);
+  const unsigned bs0 = (unsigned)__cvta_generic_to_shared(Bs);
+  static_assert(NT % 2 == 0, "B fragments load in pairs of 8-channel groups");
 #pragma unroll 1
   for (int tap = kh ? 5 : 0; tap < (kh ? 9 : 5); ++tap) {
     const int dy = tap / 3, dx = tap % 3;   // halo offsets (tap - centre + 1)
-    const float* a0p = As + ((ty0 + dy) * (CT + 2) + g + dx) * AS + tg * 2;
-    const float* a1p = a0p + (CT + 2) * AS;
-    const __nv_bfloat16* Bt = Bs + tap * BN * AS;
+    const unsigned a_row =
+        as0 + (unsigned)((((ty0 + dy + (lm & 1)) * (CT + 2) + lr + dx) * AS + (lm >> 1) * 8) * 2);
+    const unsigned b_row = bs0 + (unsigned)(((tap * BN + (lm >> 1) * 8 + lr) * AS + (lm & 1) * 8) * 2);
 #pragma unroll
     for (int ks = 0; ks < CIN / 16; ++ks) {
       uint32_t a[4];
-      const float2 f0 = *reinterpret_cast<const float2*>(a0p + ks * 16);
-      const float2 f1 = *reinterpret_cast<const float2*>(a1p + ks * 16);
-      const float2 f2 = *reinterpret_cast<const float2*>(a0p + ks * 16 + 8);
-      const float2 f3 = *reinterpret_cast<const float2*>(a1p + ks * 16 + 8);
-      a[0] = pack_bf16x2(f0.x, f0.y);
-      a[1] = pack_bf16x2(f1.x, f1.y);
-      a[2] = pack_bf16x2(f2.x, f2.y);
-      a[3] = pack_bf16x2(f3.x, f3.y);
+      ldsm_x4(a, a_row + ks * 32);
 #pragma unroll
-      for (int q = 0; q < NT; ++q) {
-        const __nv_bfloat16* bp = Bt + (q * 8 + g) * AS + ks * 16 + tg * 2;
-        uint32_t b[2];
-        b[0] = *reinterpret_cast<const uint32_t*>(bp);
-        b[1] = *reinterpret_cast<const uint32_t*>(bp + 8);
-        mma_bf16((ks & 1) ? acc2[q] : acc[q], a, b);
+      for (int qp = 0; qp < NT / 2; ++qp) {
+        uint32_t b[4];
+        ldsm_x4(b, b_row + (unsigned)(qp * 16 * AS * 2) + ks * 32);
+        mma_bf16((ks & 1) ? acc2[2 * qp] : acc[2 * qp], a, b);
+        mma_bf16((ks & 1) ? acc2[2 * qp + 1] : acc[2 * qp + 1], a, b + 2);
       }
     }
   }
@@ -248,9 +258,8 @@ __device__ __forceinline__ void conv_tile(const ConvArgs& cv, int t, int co0,
     for (int e = 0; e < 4; ++e) acc[q][e] += acc2[q][e];
   // warps 4-7 hand their partial sums to warps 0-3 through the (now free)
   // halo buffer; the sum is (taps 0-4) + (taps 5-8)
-  static_assert(4 * NT * 4 * 32 <= CT_HALO * AS, "the hand-over must fit the halo buffer");
   __syncthreads();
-  float* red = As;   // 4 x NT x 4 x 32 floats <= the halo buffer for every CIN
+  float* red = reinterpret_cast<float*>(conv_sm);   // 4 x NT x 4 x 32 floats (ConvSmem checks)
   if (kh) {
 #pragma unroll
     for (int q = 0; q < NT; ++q)

@@ -249,12 +249,12 @@ def gpu_arm(args):
             if timed:
                 cycles.append(plan.stats_buf.clone())
         torch.cuda.synchronize()
-        ms = sum(a.elapsed_time(b) for a, b in times)
+        per = [a.elapsed_time(b) for a, b in times]
         cyc = []
         for s in cycles:
             raw = _lib.AjStats.from_buffer_copy(bytes(s.cpu().numpy().tobytes()))
             cyc.append((raw.cycles, raw.rel_residual, raw.err))
-        return ms, cyc
+        return sum(per), cyc, per
 
     barrier = replicas.barrier
     max_over_ranks = replicas.max_over_ranks
@@ -268,7 +268,7 @@ def gpu_arm(args):
     if args.profile:
         plan, bufs = make_arm(head)
         run(plan, bufs, max(3, args.warmup), False, head)
-        ms, cyc = run(plan, bufs, args.steps, True, head)
+        ms, cyc, _ = run(plan, bufs, args.steps, True, head)
         if rank == 0:
             print(json.dumps({"profile_steps": args.steps, "arm": head,
                               "ms_per_step": ms / args.steps,
@@ -290,20 +290,25 @@ def gpu_arm(args):
         if sample_clocks:
             clocks.start()                      # sample clocks over >= 1.5 s of load
         soak(plan, bufs, kind, 0.0 if args.quick else 1.0)   # the same flow stage for every arm
-        ms, cyc = run(plan, bufs, args.steps, True, kind)
+        ms, cyc, per = run(plan, bufs, args.steps, True, kind)
         if sample_clocks:
             soak(plan, bufs, kind, 0.5)
             clk = clocks.stop()
         barrier()
         ms = max_over_ranks(ms)
-        results[kind] = dict(ms=ms, cycles=cyc, plan=plan, bufs=bufs)
+        results[kind] = dict(ms=ms, cycles=cyc, plan=plan, bufs=bufs, per=per)
 
     def arm_summary(r):
         ms = r["ms"] / args.steps
         return {"value": replicas.throughput(cells, args.steps, r["ms"], world), "ms_per_step": ms,
                 "mg_cycles_mean": statistics.mean(c[0] for c in r["cycles"]),
                 "rel_residual_max": max(c[1] for c in r["cycles"]),
-                "device_errors": sorted({c[2] for c in r["cycles"]})}
+                "device_errors": sorted({c[2] for c in r["cycles"]}),
+                # spread of this rank's per-step device times (CUDA events,
+                # L2 flushed before each step)
+                "step_ms": {"median": statistics.median(r["per"]), "min": min(r["per"]),
+                            "max": max(r["per"]),
+                            "stdev": statistics.stdev(r["per"]) if len(r["per"]) > 1 else 0.0}}
 
     arms = {k: arm_summary(r) for k, r in results.items()}
     meth = results[head]

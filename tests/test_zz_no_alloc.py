@@ -6,7 +6,8 @@ cudaMalloc's synchronisation.  For them the library keeps the multigrid's
 scratch in a device array of its own.  This test calls that entry point
 through the C ABI, twice in a row with different inputs, and checks each
 result against the ordinary workspace-based entry point (aj_poisson_mg, via
-poisson_multigrid) within the suite's FP32 tolerance.  It sits in a file that
+poisson_multigrid) within the suite's FP32 tolerance, and against the
+reference's own float64 multigrid (golden fixtures).  It sits in a file that
 pytest collects last, and needs nothing from the other tests."""
 import ctypes
 
@@ -17,11 +18,11 @@ pytestmark = pytest.mark.gpu
 TOL = 1e-5
 
 
-def _params(nx, ny, dx, v_cycles):
+def _params(nx, ny, dx, v_cycles, dy=None):
     from aerojax_gb300.params import StepConfig
     from aerojax_gb300.solver import make_params
-    return make_params(StepConfig(nx=nx, ny=ny, dx=dx, dy=dx, nu=1.0, variant="gui",
-                                  v_cycles=v_cycles, mg_mode="parity"))
+    return make_params(StepConfig(nx=nx, ny=ny, dx=dx, dy=dx if dy is None else dy, nu=1.0,
+                                  variant="gui", v_cycles=v_cycles, mg_mode="parity"))
 
 
 def _static_solve(L, prm, rhs, mask):
@@ -58,6 +59,26 @@ def test_static_matches_workspace_solver_twice(cuda_lib, nx, ny):
         assert err < TOL, (call, err)
         results.append(p_static.clone())
     assert not torch.equal(results[0], results[1])
+
+
+@pytest.mark.parametrize("name", ["mg_64x32", "mg_128x48"])
+def test_static_matches_reference_fixture(cuda_lib, name):
+    """The same entry point against the reference's own multigrid run in
+    float64 (the golden fixtures of tests/golden, collocated operator), two
+    calls in a row, within the suite's FP32 tolerance."""
+    import torch
+    from conftest import golden
+    g = golden(name)
+    nx, ny = g["rhs"].shape
+    prm = _params(nx, ny, float(g["dx"]), int(g["v_cycles"]), float(g["dy"]))
+    rhs = torch.as_tensor(g["rhs"].astype(np.float32), device="cuda")
+    mask = torch.as_tensor(g["mask"].astype(np.float32), device="cuda")
+    ref = np.asarray(g["p"], np.float64)
+    for call in range(2):
+        p = _static_solve(cuda_lib, prm, rhs, mask)
+        torch.cuda.synchronize()
+        err = float(np.max(np.abs(p.double().cpu().numpy() - ref)) / np.max(np.abs(ref)))
+        assert err < TOL, (call, err)
 
 
 def test_static_rejects_oversized_grid(cuda_lib):
