@@ -87,6 +87,8 @@ _SIGS = {
     "aj_nn_features": (c_int32, [POINTER(AjStepParams), c_void_p, c_void_p, c_void_p, c_void_p,
                                  c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
     "aj_workspace_rhs": (c_void_p, [POINTER(AjStepParams), c_void_p]),
+    "aj_nn_warmstart": (c_int32, [POINTER(AjStepParams), c_void_p, c_void_p, c_void_p, c_void_p,
+                                  c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
     "aj_step_nn": (c_int32, [POINTER(AjStepParams), c_void_p, c_void_p, c_void_p, c_void_p,
                              c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                              c_size_t, c_void_p, c_void_p]),

@@ -901,17 +901,10 @@ __global__ void k_nn_target(const float* __restrict__ pt, const float* __restric
   target[(long)I * w + J] = (float)((double)(a / (float)(F * F)) / sc->nn_out_scale);
 }
 
-// state += bilinear prolongation of (prediction * out_scale), added to the
-// double-FP32 state (hi: N floats, lo: N floats) with Knuth's TwoSum; the
-// outlet row stays pinned at 0
-__global__ void k_nn_apply(const float* __restrict__ y, int nx, int ny, int F,
-                           float* __restrict__ state, const DevScalars* sc) {
-  pdl_wait();
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= nx - 1 || j >= ny) return;
-  const long N = (long)nx * ny;
-  const long k = (long)i * ny + j;
+// the correction at fine cell (i, j): bilinear prolongation of the network
+// output (channel 0 of 16 on the grid F times coarser) times out_scale
+__device__ __forceinline__ float nn_corr_at(const float* __restrict__ y, int nx, int ny, int F,
+                                            double out_scale, int i, int j) {
   const int h = nx / F, w = ny / F;
   const float xi = (i + 0.5f) / F - 0.5f, xj = (j + 0.5f) / F - 0.5f;
   int i0 = (int)floorf(xi), j0 = (int)floorf(xj);
@@ -922,13 +915,39 @@ __global__ void k_nn_apply(const float* __restrict__ y, int nx, int ny, int F,
   const float v00 = y[((long)i0 * w + j0) * 16], v01 = y[((long)i0 * w + j1) * 16];
   const float v10 = y[((long)i1 * w + j0) * 16], v11 = y[((long)i1 * w + j1) * 16];
   const float v = (1.f - ti) * ((1.f - tj) * v00 + tj * v01) + ti * ((1.f - tj) * v10 + tj * v11);
-  const float c = (float)(v * sc->nn_out_scale);
+  return (float)(v * out_scale);
+}
+
+// state += the correction, added to the double-FP32 state (hi: N floats, lo:
+// N floats) with Knuth's TwoSum; the outlet row stays pinned at 0
+__global__ void k_nn_apply(const float* __restrict__ y, int nx, int ny, int F,
+                           float* __restrict__ state, const DevScalars* sc) {
+  pdl_wait();
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= nx - 1 || j >= ny) return;
+  const long N = (long)nx * ny;
+  const long k = (long)i * ny + j;
+  const float c = nn_corr_at(y, nx, ny, F, sc->nn_out_scale, i, j);
   const float hi = state[k], lo = state[N + k];
   const float s = hi + c, bb = s - hi;
   const float e = (hi - (s - bb)) + (c - bb) + lo;
   const float s2 = s + e;
   state[k] = s2;
   state[N + k] = e - (s2 - s);
+}
+
+// p0 = p_prev + the correction in FP32 (aj_nn_warmstart); the outlet row is
+// 0, the value every solve pins there
+__global__ void k_nn_apply_guess(const float* __restrict__ y, int nx, int ny, int F,
+                                 const float* __restrict__ pp, float* __restrict__ p0,
+                                 const DevScalars* sc) {
+  pdl_wait();
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= nx || j >= ny) return;
+  const long k = (long)i * ny + j;
+  p0[k] = i == nx - 1 ? 0.f : pp[k] + nn_corr_at(y, nx, ny, F, sc->nn_out_scale, i, j);
 }
 
 // [n][h][w][3] -> [n][h][w][16] (zeros beyond the features)
@@ -1081,6 +1100,36 @@ int32_t aj_nn_features(const AjStepParams* prm, const float* b, const float* mas
   NnActs A = act_layout(1, prm->nx / F, prm->ny / F, at<char>(ws, L.nn_act));
   return nn_features(*prm, ws, at<double>(ws, L.part), b, mask, p_prev, p_true, A.x, x3_out,
                      target_out, (cudaStream_t)stream, false, true);
+}
+
+int32_t aj_nn_warmstart(const AjStepParams* prm, const float* rhs, const float* mask,
+                        const float* p_prev, const uint16_t* nn_packed, const float* nn_master,
+                        float* p0, void* ws, size_t ws_bytes, void* stream) {
+  if (!prm || !rhs || !mask || !p_prev || !nn_packed || !nn_master || !p0) return AJ_ERR_PARAM;
+  const AjStepParams p = normalise(*prm);
+  if (p.nn_factor <= 0 || p.mg_mode != AJ_MG_CONVERGE) return AJ_ERR_PARAM;
+  Layout L;
+  if (!make_layout(p, L) || !nn_step_shape_ok(p)) return AJ_ERR_SHAPE;
+  if (!ws || ws_bytes < L.total || !L.nn_act) return AJ_ERR_WORKSPACE;
+  conv_attrs();
+  const cudaStream_t st = (cudaStream_t)stream;
+  DevScalars* sc = at<DevScalars>(ws, 0);
+  // the scale reduction's last-block counter starts at zero (a workspace
+  // that no step has used yet holds anything)
+  if (cudaMemsetAsync(&sc->red_count, 0, sizeof(sc->red_count), st) != cudaSuccess)
+    return AJ_ERR_CUDA;
+  const int F = p.nn_factor, h = p.nx / F, w = p.ny / F;
+  NnActs A = act_layout(1, h, w, at<char>(ws, L.nn_act));
+  int rc = nn_features(p, ws, at<double>(ws, L.part), rhs, mask, p_prev, nullptr, A.x, nullptr,
+                       nullptr, st, false, false);
+  if (rc != AJ_OK) return rc;
+  const NnW W{reinterpret_cast<const __nv_bfloat16*>(nn_packed), nn_master};
+  rc = nn_forward(1, h, w, W, A, st, false, sc);
+  if (rc != AJ_OK) return rc;
+  const dim3 blk(32, 8), grd(cdiv(p.ny, 32), cdiv(p.nx, 8));
+  launch_pdl(true, k_nn_apply_guess, grd, blk, 0, st, (const float*)A.y, p.nx, p.ny, F, p_prev, p0,
+             (const DevScalars*)sc);
+  return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
 }
 
 int32_t aj_nn_adam(float* master, const float* grad, float* m, float* v, int32_t step, float lr,

@@ -358,6 +358,21 @@ def train(net: WarmStartNet, data: Snapshots, epochs=3, batch=16, lr=1e-3, holdo
     return hist
 
 
+def warm_start_guess(plan: Plan, net: WarmStartNet, rhs, mask, p_prev, out=None, stream=None):
+    """The learned warm start on its own (aj_nn_warmstart): p0 = p_prev + the
+    network's correction from (rhs, mask, p_prev) - the guess to hand to
+    poisson_multigrid_converge(..., p0=p0).  plan: a converging-mode plan
+    with nn_factor set (its workspace holds the network's activations)."""
+    cfg = plan.cfg
+    p0 = out if out is not None else torch.empty((cfg.nx, cfg.ny), dtype=torch.float32,
+                                                 device=rhs.device)
+    check("aj_nn_warmstart", lib().aj_nn_warmstart(
+        ctypes.byref(plan.params), rhs.data_ptr(), mask.data_ptr(), p_prev.data_ptr(),
+        net.packed.data_ptr(), net.master.data_ptr(), p0.data_ptr(), plan.ws.data_ptr(),
+        plan.nbytes, _stream(stream)))
+    return p0
+
+
 def run_step_nn(plan: Plan, net: WarmStartNet, u, v, mask, p_prev, out=None, stream=None):
     """One step whose pressure solve starts from the plan's initial guess
     (p_prev, or the extrapolation of the workspace's history) plus the

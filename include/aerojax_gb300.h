@@ -253,6 +253,17 @@ int32_t aj_nn_expand(int32_t n, int32_t h, int32_t w, const float* x3, float* x1
 int32_t aj_nn_features(const AjStepParams* prm, const float* b, const float* mask,
                        const float* p_prev, const float* p_true, float* x3_out, float* target_out,
                        void* workspace, size_t workspace_bytes, void* stream);
+/* The learned warm start on its own, the reference's learned pressure
+   operator call model(rhs, mask) (step_handlers.py:104-107,
+   neural_operators/nn_pressure_operator_*.py) recast as a multigrid guess:
+   p0 = p_prev + the network's correction from (rhs, mask, p_prev), for
+   aj_poisson_mg's p0 in converging mode.  prm as for aj_step_nn (converging
+   mode, nn_factor > 0); the workspace is the step's (aj_workspace_size(prm)).
+   The outlet row of p0 is 0 (pinned in every solve).  Returns AJ_ERR_PARAM, AJ_ERR_SHAPE (the
+   network grid's shape rule) or AJ_ERR_WORKSPACE before enqueueing anything. */
+int32_t aj_nn_warmstart(const AjStepParams* prm, const float* rhs, const float* mask,
+                        const float* p_prev, const uint16_t* nn_packed, const float* nn_master,
+                        float* p0, void* workspace, size_t workspace_bytes, void* stream);
 /* The pressure right-hand side of the last aj_step / aj_step_nn on this
    workspace (device pointer, nx*ny). */
 const float* aj_workspace_rhs(const AjStepParams* prm, void* workspace);

@@ -220,6 +220,40 @@ def test_features_match_oracle(dev):
     assert _rel(tg.cpu().numpy(), rt) < 1e-4
 
 
+def test_warm_start_guess_matches_oracle(dev):
+    """aj_nn_warmstart on its own (features, network, correction): the
+    correction p0 - p_prev against the oracle's (nn_np.features, forward with
+    the same BF16 operand rounding, apply_correction) at the forward pass's
+    tolerance, the outlet row pinned at 0; the guess then starts a converging
+    solve that meets its tolerance."""
+    from aerojax_gb300.nn import WarmStartNet, warm_start_guess
+    import aerojax_gb300 as aj
+    case, plan = _nn_plan(dev, 512, 128, 8)
+    c = plan.cfg
+    F = c.nn_factor
+    flat = _live_params(4)
+    net = WarmStartNet(device=dev, params=flat)
+    rng = np.random.default_rng(12)
+    b = rng.standard_normal((c.nx, c.ny)).astype(np.float32)
+    pp = rng.standard_normal((c.nx, c.ny)).astype(np.float32)
+    pp[-1, :] = 0.0
+    bd, ppd = torch.as_tensor(b, device=dev), torch.as_tensor(pp, device=dev)
+    m = case["mask"]
+    p0 = warm_start_guess(plan, net, bd, m, ppd).cpu().numpy().astype(np.float64)
+    x3, _, scale = N.features(b, m.cpu().numpy(), pp, c.dx, c.dy, F)
+    h, w = c.nx // F, c.ny // F
+    x = np.zeros((h, w, 16))
+    x[..., :3] = x3
+    y = N.forward(flat.astype(np.float64), x, emulate_bf16=True)
+    ref = N.apply_correction(y[..., 0], pp, F, scale)
+    assert np.all(p0[-1, :] == 0.0)
+    assert _rel(p0 - pp, ref - pp) < 2e-2, _rel(p0 - pp, ref - pp)
+    assert _rel(p0 - pp, np.zeros_like(pp)) > 0          # the network did something
+    p, st = aj.poisson_multigrid_converge(bd, m, c.dx, c.dy, rtol=1e-6, mac=True,
+                                          p0=torch.as_tensor(p0.astype(np.float32), device=dev))
+    assert st["err"] == 0 and st["converged"] and st["rel_residual"] <= 1e-6
+
+
 def test_step_nn_converges_to_the_same_solution(dev):
     """The learned warm start changes only where the multigrid starts: the
     step's result matches the plain step to the solver tolerance."""
