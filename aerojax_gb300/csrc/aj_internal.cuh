@@ -81,6 +81,14 @@ inline T* at(void* ws, size_t off) { return reinterpret_cast<T*>(static_cast<cha
 
 // ------------------------------------------------------------------ helpers
 __device__ __forceinline__ int clampi(int i, int n) { return i < 0 ? 0 : (i >= n ? n - 1 : i); }
+// The MAC predictor's upwind weight alpha = (1 + tanh(w / 0.05)) / 2 of
+// rk3_mac.py:386-391, evaluated as the equal logistic 1 / (1 + e^(-40 w))
+// with the hardware exponential and a fast reciprocal: a few instructions
+// instead of tanhf's sequence, relative error ~1e-7, exactly 0 and 1 in the
+// tails (e^(-40 w) overflowing to infinity gives 0).
+__device__ __forceinline__ float upwind_weight(float w) {
+  return __fdividef(1.f, 1.f + __expf(-40.f * w));
+}
 __device__ __forceinline__ int wrapi(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 template <bool PER>
 __device__ __forceinline__ int pidx(int i, int n) { return PER ? wrapi(i, n) : clampi(i, n); }

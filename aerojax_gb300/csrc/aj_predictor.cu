@@ -662,8 +662,8 @@ __device__ float rhs_mac_u(const RkMac& a, int i, int j) {
   float uxm = uw_at(a, a.uin, per ? wrapi(i - 1, nx + 1) : (i > 0 ? i - 1 : 0), j);
   float uxp = uw_at(a, a.uin, per ? wrapi(i + 1, nx + 1) : (i < nx ? i + 1 : nx), j);
   float back = (uw - uxm) * a.idx, fwd = (uxp - uw) * a.idx;
-  // upwind blend 0.5 (1 + tanh(u / 0.05)) of rk3_mac.py, the argument formed as 20 u
-  float al = 0.5f * (1.f + tanhf(uw * 20.f));
+  // upwind blend 0.5 (1 + tanh(u / 0.05)) of rk3_mac.py (upwind_weight)
+  float al = upwind_weight(uw);
   float adv_x = uw * (al * back + (1.f - al) * fwd);
   float du_dy;
   if (per)
@@ -693,7 +693,7 @@ __device__ float rhs_mac_v(const RkMac& a, int i, int j) {
   float vym = vw_at(a, a.vin, i, per ? wrapi(j - 1, ny + 1) : (j > 0 ? j - 1 : 0));
   float vyp = vw_at(a, a.vin, i, per ? wrapi(j + 1, ny + 1) : (j < ny ? j + 1 : ny));
   float back = (vw - vym) * a.idy, fwd = (vyp - vw) * a.idy;
-  float al = 0.5f * (1.f + tanhf(vw * 20.f));
+  float al = upwind_weight(vw);
   float adv_y = vw * (al * back + (1.f - al) * fwd);
   float dv_dx;
   if (per)
@@ -866,7 +866,7 @@ __device__ __forceinline__ float stage_mac_u_int(const RkMac& a, int i, int j, f
   const float vc_m = 0.5f * (ldg(v - nyv + 1) + ldg(v - nyv));
   const float v_at_u = 0.5f * (vc_i + vc_m);
   const float back = (uw - uxm) * a.idx, fwd = (uxp - uw) * a.idx;
-  const float al = 0.5f * (1.f + tanhf(uw * 20.f));
+  const float al = upwind_weight(uw);
   const float adv_x = uw * (al * back + (1.f - al) * fwd);
   const float du_dy = (uyp - uym) * (0.5f * a.idy);
   const float m_i = ldg(a.mask + k), m_im = ldg(a.mask + k - ny);
@@ -900,7 +900,7 @@ __device__ __forceinline__ float stage_mac_v_int(const RkMac& a, int i, int j, f
   const float uc_m = 0.5f * (ldg(u + ny - 1) + ldg(u - 1));
   const float u_at_v = 0.5f * (uc_j + uc_m);
   const float back = (vw - vym) * a.idy, fwd = (vyp - vw) * a.idy;
-  const float al = 0.5f * (1.f + tanhf(vw * 20.f));
+  const float al = upwind_weight(vw);
   const float adv_y = vw * (al * back + (1.f - al) * fwd);
   const float dv_dx = (vxp - vxm) * (0.5f * a.idx);
   const long c = (long)i * ny + j;

@@ -189,7 +189,7 @@ __device__ float f_stage_u(const FCtx& c, const float* Us, const float* Vs, int 
   const float uxm = f_uw(c, Us, i > 0 ? i - 1 : 0, j);
   const float uxp = f_uw(c, Us, i < nx ? i + 1 : nx, j);
   const float back = (uw - uxm) * c.idx, fwd = (uxp - uw) * c.idx;
-  const float al = 0.5f * (1.f + tanhf(uw * 20.f));
+  const float al = upwind_weight(uw);
   const float adv_x = uw * (al * back + (1.f - al) * fwd);
   float du_dy;
   if (j == 0) du_dy = (f_uw(c, Us, i, 1) - uw) * c.idy;
@@ -218,7 +218,7 @@ __device__ float f_stage_v(const FCtx& c, const float* Us, const float* Vs, int 
   const float vym = f_vw(c, Vs, i, j > 0 ? j - 1 : 0);
   const float vyp = f_vw(c, Vs, i, j < ny ? j + 1 : ny);
   const float back = (vw - vym) * c.idy, fwd = (vyp - vw) * c.idy;
-  const float al = 0.5f * (1.f + tanhf(vw * 20.f));
+  const float al = upwind_weight(vw);
   const float adv_y = vw * (al * back + (1.f - al) * fwd);
   float dv_dx;
   if (i == 0) dv_dx = (f_vw(c, Vs, 1, j) - vw) * c.idx;
@@ -244,7 +244,7 @@ __device__ __forceinline__ float f_stage_u_int(const FCtx& c, const float* Us, c
   const float vc_m = 0.5f * (v[1 - FSJ] + v[-FSJ]);
   const float v_at_u = 0.5f * (vc_i + vc_m);
   const float back = (uw - uxm) * c.idx, fwd = (uxp - uw) * c.idx;
-  const float al = 0.5f * (1.f + tanhf(uw * 20.f));
+  const float al = upwind_weight(uw);
   const float adv_x = uw * (al * back + (1.f - al) * fwd);
   const float du_dy = (uyp - uym) * (0.5f * c.idy);
   const float m_i = c.M[k], m_im = c.M[k - FSJ];
@@ -266,7 +266,7 @@ __device__ __forceinline__ float f_stage_v_int(const FCtx& c, const float* Us, c
   const float uc_m = 0.5f * (u[FSJ - 1] + u[-1]);
   const float u_at_v = 0.5f * (uc_j + uc_m);
   const float back = (vw - vym) * c.idy, fwd = (vyp - vw) * c.idy;
-  const float al = 0.5f * (1.f + tanhf(vw * 20.f));
+  const float al = upwind_weight(vw);
   const float adv_y = vw * (al * back + (1.f - al) * fwd);
   const float dv_dx = (vxp - vxm) * (0.5f * c.idx);
   const float m_j = c.M[k], m_jm = c.M[k - 1];
