@@ -719,15 +719,15 @@ __device__ __forceinline__ float finish_mac(const RkMac& a, long k, float r, flo
   if (a.rk2) {
     if (a.stage == 1) {
       if (k1o) k1o[k] = r;
-      return (x0 + dt * r) / den;
+      return brinkman_div(x0 + dt * r, den);
     }
-    float out = (x0 + 0.5f * dt * (ldg((COMP == 0 ? a.k1u : a.k1v) + k) + r)) / den;
+    float out = brinkman_div(x0 + 0.5f * dt * (ldg((COMP == 0 ? a.k1u : a.k1v) + k) + r), den);
     return chi < 0.5f ? out : 0.f;                   // hard mask (rk3_mac.py:498-499)
   }
-  if (a.stage == 1) return (x0 + dt * r) / den;
+  if (a.stage == 1) return brinkman_div(x0 + dt * r, den);
   float xs = x0 + dt * r;
-  if (a.stage == 2) return (0.75f * x0 + 0.25f * xs) / den;
-  float out = ((1.f / 3.f) * x0 + (2.f / 3.f) * xs) / den;
+  if (a.stage == 2) return brinkman_div(0.75f * x0 + 0.25f * xs, den);
+  float out = brinkman_div((1.f / 3.f) * x0 + (2.f / 3.f) * xs, den);
   return chi < 0.5f ? out : 0.f;                     // hard mask (rk3_mac.py:483-484)
 }
 

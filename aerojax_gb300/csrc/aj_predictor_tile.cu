@@ -168,10 +168,10 @@ __device__ __forceinline__ float f_yface(const FCtx& c, const float* C, int i, i
 template <int STAGE>
 __device__ __forceinline__ float f_finish(const FCtx& c, float x0, float r, float chi, float dt) {
   const float den = 1.f + dt * chi * c.inv_eta;
-  if (STAGE == 1) return (x0 + dt * r) / den;
+  if (STAGE == 1) return brinkman_div(x0 + dt * r, den);
   const float xs = x0 + dt * r;
-  if (STAGE == 2) return (0.75f * x0 + 0.25f * xs) / den;
-  const float out = ((1.f / 3.f) * x0 + (2.f / 3.f) * xs) / den;
+  if (STAGE == 2) return brinkman_div(0.75f * x0 + 0.25f * xs, den);
+  const float out = brinkman_div((1.f / 3.f) * x0 + (2.f / 3.f) * xs, den);
   return chi < 0.5f ? out : 0.f;
 }
 
