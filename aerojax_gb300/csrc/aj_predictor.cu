@@ -390,13 +390,16 @@ __device__ __forceinline__ float weno5(float v1, float v2, float v3, float v4, f
              0.25f * (v2 - v4) * (v2 - v4);
   float b3 = (13.f / 12.f) * (v3 - 2.f * v4 + v5) * (v3 - 2.f * v4 + v5) +
              0.25f * (3.f * v3 - 4.f * v4 + v5) * (3.f * v3 - 4.f * v4 + v5);
-  float a1 = 0.1f / ((eps + b1) * (eps + b1));
-  float a2 = 0.6f / ((eps + b2) * (eps + b2));
-  float a3 = 0.3f / ((eps + b3) * (eps + b3));
+  // the weights' divisions with the fast reciprocal (2 ulp; the denominators,
+  // (1e-6 + beta)^2 and the weights' sum, stay far below 2^126 for any
+  // velocity field a step can hold)
+  float a1 = __fdividef(0.1f, (eps + b1) * (eps + b1));
+  float a2 = __fdividef(0.6f, (eps + b2) * (eps + b2));
+  float a3 = __fdividef(0.3f, (eps + b3) * (eps + b3));
   float q1 = v1 * (1.f / 3.f) - (7.f / 6.f) * v2 + (11.f / 6.f) * v3;
   float q2 = -v2 * (1.f / 6.f) + (5.f / 6.f) * v3 + v4 * (1.f / 3.f);
   float q3 = v3 * (1.f / 3.f) + (5.f / 6.f) * v4 - v5 * (1.f / 6.f);
-  return (a1 * q1 + a2 * q2 + a3 * q3) / (a1 + a2 + a3);
+  return __fdividef(a1 * q1 + a2 * q2 + a3 * q3, a1 + a2 + a3);
 }
 
 // upwind-biased WENO5 derivative of f along one axis at (i, j)
@@ -467,14 +470,14 @@ __device__ __forceinline__ float stage_val(const RkArgs& a, const float* f, cons
   if (a.rk2) {
     if (a.stage == 1) {
       if (k1_out) k1_out[k] = r;
-      return (x0 + dt * r) / den;
+      return brinkman_div(x0 + dt * r, den);
     }
-    return (x0 + 0.5f * dt * (ldg(k1 + k) + r)) / den;
+    return brinkman_div(x0 + 0.5f * dt * (ldg(k1 + k) + r), den);
   }
-  if (a.stage == 1) return (x0 + dt * r) / den;
+  if (a.stage == 1) return brinkman_div(x0 + dt * r, den);
   float xs = x0 + dt * r;
-  if (a.stage == 2) return (0.75f * x0 + 0.25f * xs) / den;
-  return ((1.f / 3.f) * x0 + (2.f / 3.f) * xs) / den;
+  if (a.stage == 2) return brinkman_div(0.75f * x0 + 0.25f * xs, den);
+  return brinkman_div((1.f / 3.f) * x0 + (2.f / 3.f) * xs, den);
 }
 
 template <bool PER, bool HYPER, int ADV>
