@@ -1,6 +1,6 @@
 """CPU oracle for the AeroJAX projection step — TEST INFRASTRUCTURE ONLY.
 
-This module is the checker, never the product.  Only ``tests/``,
+This module checks the product and is never part of it.  Only ``tests/``,
 ``__graft_entry__.smoke()`` and ``bench.py`` (its CPU-baseline leg and its
 ``--impl reference`` arm) may import it.  The shipped package
 ``aerojax_gb300`` never imports it and has no CPU fallback.
