@@ -448,15 +448,27 @@ template <bool PER, int AXIS>
 __device__ __forceinline__ float weno_d(const float* __restrict__ f, int i, int j, int nx,
                                         int ny, float ih, float vel) {
   float g[7];
+  const int c = AXIS == 0 ? i : j, n = AXIS == 0 ? nx : ny;
+  if (c >= 3 && c <= n - 4) {   // the seven points lie inside the grid: plain offsets
+    const float* q = f + (long)i * ny + j;
+    const long st = AXIS == 0 ? ny : 1;
 #pragma unroll
-  for (int o = -3; o <= 3; ++o) {
-    long k = AXIS == 0 ? (long)pidx<PER>(i + o, nx) * ny + j : (long)i * ny + pidx<PER>(j + o, ny);
-    g[o + 3] = ldg(f + k);
+    for (int o = -3; o <= 3; ++o) g[o + 3] = ldg(q + o * st);
+  } else {
+#pragma unroll
+    for (int o = -3; o <= 3; ++o) {
+      long k = AXIS == 0 ? (long)pidx<PER>(i + o, nx) * ny + j : (long)i * ny + pidx<PER>(j + o, ny);
+      g[o + 3] = ldg(f + k);
+    }
   }
   // D_m = (f[m+1]-f[m])/h for m = i-3 .. i+2  ->  d[0..5]
   float d0 = (g[1] - g[0]) * ih, d1 = (g[2] - g[1]) * ih, d2 = (g[3] - g[2]) * ih;
   float d3 = (g[4] - g[3]) * ih, d4 = (g[5] - g[4]) * ih, d5 = (g[6] - g[5]) * ih;
-  return vel > 0.f ? weno5(d0, d1, d2, d3, d4) : weno5(d5, d4, d3, d2, d1);
+  // weno5(d0..d4) upwind of a positive velocity, weno5(d5..d1) otherwise: the
+  // operands are chosen first and one reconstruction runs (no divergence
+  // where the velocity changes sign inside a warp)
+  const bool up = vel > 0.f;
+  return weno5(up ? d0 : d5, up ? d1 : d4, up ? d2 : d3, up ? d3 : d2, up ? d4 : d1);
 }
 
 // explicit right-hand side for one velocity component f at (i, j)
@@ -847,7 +859,8 @@ __device__ __forceinline__ int widx(int i, int n, bool per) {
 __device__ __forceinline__ float weno_d7(const float (&g)[7], float ih, float vel) {
   float d0 = (g[1] - g[0]) * ih, d1 = (g[2] - g[1]) * ih, d2 = (g[3] - g[2]) * ih;
   float d3 = (g[4] - g[3]) * ih, d4 = (g[5] - g[4]) * ih, d5 = (g[6] - g[5]) * ih;
-  return vel > 0.f ? weno5(d0, d1, d2, d3, d4) : weno5(d5, d4, d3, d2, d1);
+  const bool up = vel > 0.f;   // operands first, one reconstruction (as in weno_d)
+  return weno5(up ? d0 : d5, up ? d1 : d4, up ? d2 : d3, up ? d3 : d2, up ? d4 : d1);
 }
 
 template <bool HYPER, bool FAST>
