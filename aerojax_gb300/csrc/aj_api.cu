@@ -389,8 +389,12 @@ static int enqueue_step(const AjStepParams& p, const Layout& L, void* ws, const 
   } else {
     rc = launch_predictor(p, L, ws, u, v, mask, nsg, dc, us, vs, st);
     if (rc != AJ_OK) return rc;
-    rc = launch_rhs(p, L, ws, us, vs, mask, at<float>(ws, L.b0), st);
-    if (rc != AJ_OK) return rc;
+    // with the learned warm start on the MAC grid, the network's features
+    // kernel forms the right-hand side (one launch fewer before the network)
+    if (!nn_forms_rhs(p, nn.packed != nullptr)) {
+      rc = launch_rhs(p, L, ws, us, vs, mask, at<float>(ws, L.b0), st);
+      if (rc != AJ_OK) return rc;
+    }
   }
   if (conv && cudaStreamWaitEvent(st, fk->init_done, 0) != cudaSuccess) return AJ_ERR_CUDA;
   if (io && io->h_p && cudaStreamWaitEvent(st, fk->io_p_in, 0) != cudaSuccess)
@@ -399,6 +403,10 @@ static int enqueue_step(const AjStepParams& p, const Layout& L, void* ws, const 
   nw.packed = nn.packed;
   nw.master = nn.master;
   nw.mask = mask;
+  if (nn_forms_rhs(p, nn.packed != nullptr) && !tile_predictor_ok(p, u, mask, nsg)) {
+    nw.us = us;
+    nw.vs = vs;
+  }
   rc = launch_pressure(p, L, ws, mask, p_guess, po, stats, st, nn.packed ? &nw : nullptr, conv);
   if (rc != AJ_OK) return rc;
   if (io) {   // the pressure's download, beside the correction
@@ -722,7 +730,7 @@ int32_t aj_kernel_count(const AjStepParams* prm, int32_t cycles) {
   if (p.les_model != AJ_LES_NONE && (p.variant == AJ_VARIANT_GUI || mac))
     n += p.les_model == AJ_LES_DYNAMIC ? (mac ? 1 : 0) + 4 : 1;
   if (tile_predictor_params_ok(p)) n += tile_predictor_kernels();   // stages + rhs in tile kernels
-  else n += (p.fast_mode ? 2 : 3) + 1;                          // predictor stages, rhs
+  else n += (p.fast_mode ? 2 : 3) + (nn_forms_rhs(p, p.nn_factor > 0) ? 0 : 1);   // stages, rhs
   if (p.mg_mode == AJ_MG_PARITY) {
     const int coarse = parity_coarsest_fused(L) ? 1 : 10;
     int per_cycle = 2 * L.nlev + coarse;                        // levels, coarsest

@@ -1171,7 +1171,7 @@ __global__ void k_cv_out(PState ps, DevScalars* sc, float* __restrict__ p, long 
     }
     if (stats) {
       stats->cycles = cycles;
-      stats->converged = done;
+      stats->converged = done && err == AJ_OK;   // the tolerance met, not just the loop ended
       stats->err = err;
       stats->pad = 0;
       stats->rel_residual = rel;

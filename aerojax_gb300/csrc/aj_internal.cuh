@@ -94,6 +94,19 @@ __device__ __forceinline__ float upwind_weight(float w) {
 __device__ __forceinline__ float brinkman_div(float num, float den) {
   return __fdividef(num, den);
 }
+// The pressure right-hand side of a MAC cell, mask * div(u*) / dt
+// (operators_mac.py:73-80, multigrid_solver_mac.py:78), 0 on the outlet row
+// when the flow pins it (multigrid_solver.py:75-77); k_rhs and the learned
+// warm start's features kernel both use it.
+__device__ __forceinline__ float rhs_mac_cell(const float* __restrict__ us,
+                                              const float* __restrict__ vs,
+                                              const float* __restrict__ mask, int i, int j, int nx,
+                                              int ny, float idx, float idy, float dt, int outlet) {
+  const float du = (__ldg(us + (long)(i + 1) * ny + j) - __ldg(us + (long)i * ny + j)) * idx;
+  const float dv = (__ldg(vs + (long)i * (ny + 1) + j + 1) - __ldg(vs + (long)i * (ny + 1) + j)) * idy;
+  const float out = ((du + dv) / dt) * __ldg(mask + (long)i * ny + j);
+  return (outlet && i == nx - 1) ? 0.f : out;
+}
 __device__ __forceinline__ int wrapi(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 template <bool PER>
 __device__ __forceinline__ int pidx(int i, int n) { return PER ? wrapi(i, n) : clampi(i, n); }
@@ -301,10 +314,19 @@ int prepare_pressure(const AjStepParams& p, const Layout& L, void* ws, const flo
 int launch_mg_rhs(const AjStepParams& p, const Layout& L, void* ws, const float* rhs,
                   const float* mask, cudaStream_t st);
 // the learned warm start inside a converging solve (null pointers: off)
+// the MAC converging step with the learned warm start forms its pressure
+// right-hand side in the network's features kernel (no k_rhs launch)
+inline bool nn_forms_rhs(const AjStepParams& p, bool learned) {
+  return learned && p.grid_type == AJ_GRID_MAC && p.mg_mode == AJ_MG_CONVERGE;
+}
 struct NnWarm {
   const uint16_t* packed = nullptr;
   const float* master = nullptr;
   const float* mask = nullptr;
+  // MAC predictor outputs: when set, the features kernel forms the pressure
+  // right-hand side itself (and stores it) instead of reading k_rhs's
+  const float* us = nullptr;
+  const float* vs = nullptr;
 };
 // init_done: converge_init already ran (the step launches it beside the
 // predictor)

@@ -765,11 +765,22 @@ static bool nn_shape_ok(int n, int h, int w) { return n >= 1 && h >= 8 && w >= 8
 // channels 3..15 are zero.  Also the FP64 sums of channel 0^2 and 2^2.
 // one thread per fine cell: the F x F window sums reduce across F lanes with
 // shuffles and across F rows through shared memory (F in {2, 4, 8}; a
-// 32 x 8 block holds whole windows)
+// 32 x 8 block holds whole windows).  With rs.us set (a MAC step), the
+// kernel forms the right-hand side b of its cell itself from the predictor's
+// u*, v* (k_rhs's arithmetic) and stores it for the solve.
+struct RhsSrc {
+  const float* us = nullptr;   // null: read b
+  const float* vs = nullptr;
+  float idx = 0.f, idy = 0.f;
+  int outlet = 0;
+  const DevScalars* sc = nullptr;
+  float* b_out = nullptr;
+};
 __global__ void __launch_bounds__(256) k_nn_feat(const float* __restrict__ b,
                                                  const float* __restrict__ mask,
                                                  const float* __restrict__ pp, int nx, int ny,
-                                                 int F, float ax, float ay, float* __restrict__ x) {
+                                                 int F, float ax, float ay, float* __restrict__ x,
+                                                 RhsSrc rs) {
   pdl_wait();
   __shared__ float red[3][8][32];
   const int lane = threadIdx.x, row = threadIdx.y;
@@ -778,12 +789,19 @@ __global__ void __launch_bounds__(256) k_nn_feat(const float* __restrict__ b,
   if (i < nx && j < ny) {
     const long k = (long)i * ny + j;
     const float c = pp[k];
+    float bk;
+    if (rs.us) {
+      bk = rhs_mac_cell(rs.us, rs.vs, mask, i, j, nx, ny, rs.idx, rs.idy, rs.sc->dt, rs.outlet);
+      rs.b_out[k] = bk;
+    } else {
+      bk = b[k];
+    }
     if (i != nx - 1) {
       const float xp = pp[k + ny];
       const float xm = i > 0 ? pp[k - ny] : c;
       const float yp = j + 1 < ny ? pp[k + 1] : c;
       const float ym = j > 0 ? pp[k - 1] : c;
-      vr = b[k] - (ax * ((xp - c) + (xm - c)) + ay * ((yp - c) + (ym - c)));
+      vr = bk - (ax * ((xp - c) + (xm - c)) + ay * ((yp - c) + (ym - c)));
     }
     vm = mask[k];
     vp = c;
@@ -962,12 +980,23 @@ __global__ void k_nn_expand(const float* __restrict__ x3, float* __restrict__ x1
 // features (+ optional dataset copy and target) for one step's pressure solve
 int nn_features(const AjStepParams& p, void* ws, double* part, const float* b, const float* mask,
                 const float* pp, const float* pt, float* x16, float* x3, float* target,
-                cudaStream_t st, bool pdl, bool normalise) {
+                cudaStream_t st, bool pdl, bool normalise, const float* us = nullptr,
+                const float* vs = nullptr) {
   const int F = p.nn_factor, h = p.nx / F, w = p.ny / F;
   DevScalars* sc = at<DevScalars>(ws, 0);
   dim3 blk(32, 8), grd(cdiv(w, 32), cdiv(h, 8));
+  RhsSrc rs;
+  if (us) {   // b formed here (k_rhs's launch arguments for a MAC grid)
+    rs.us = us;
+    rs.vs = vs;
+    rs.idx = (float)(1.0 / p.dx);
+    rs.idy = (float)(1.0 / p.dy);
+    rs.outlet = p.flow_type == AJ_FLOW_VON_KARMAN;
+    rs.sc = sc;
+    rs.b_out = const_cast<float*>(b);
+  }
   launch_pdl(pdl, k_nn_feat, dim3(cdiv(p.ny, 32), cdiv(p.nx, 8)), blk, 0, st, b, mask, pp, p.nx,
-             p.ny, F, (float)(1.0 / (p.dx * p.dx)), (float)(1.0 / (p.dy * p.dy)), x16);
+             p.ny, F, (float)(1.0 / (p.dx * p.dx)), (float)(1.0 / (p.dy * p.dy)), x16, rs);
   const double lx = p.nx * p.dx, ly = p.ny * p.dy, lmin = lx < ly ? lx : ly;
   launch_pdl(pdl, k_nn_scale, dim3(NN_SCALE_BLOCKS), dim3(512), 0, st, x16, (long)h * w, sc,
              lmin * lmin, part);
@@ -990,7 +1019,7 @@ int nn_correct_state(const AjStepParams& p, const Layout& L, void* ws, const flo
   // packed weights were written before the step began)
   // (the first convolution normalises the features as it stages them)
   int rc = nn_features(p, ws, at<double>(ws, L.part), b, nn.mask, state, nullptr, A.x, nullptr,
-                       nullptr, st, true, false);
+                       nullptr, st, true, false, nn.us, nn.vs);
   if (rc != AJ_OK) return rc;
   NnW W{reinterpret_cast<const __nv_bfloat16*>(nn.packed), nn.master};
   rc = nn_forward(1, h, w, W, A, st, false, at<DevScalars>(ws, 0));

@@ -35,9 +35,7 @@ __global__ void __launch_bounds__(256) k_rhs(const float* __restrict__ us,
   long k = (long)i * ny + j;
   float out;
   if (mac) {
-    float du = (ldg(us + (long)(i + 1) * ny + j) - ldg(us + (long)i * ny + j)) * idx;
-    float dv = (ldg(vs + (long)i * (ny + 1) + j + 1) - ldg(vs + (long)i * (ny + 1) + j)) * idy;
-    out = ((du + dv) / dt) * ldg(mask + k);
+    out = rhs_mac_cell(us, vs, mask, i, j, nx, ny, idx, idy, dt, 0);
   } else {
     float div = 0.f;
     if (periodic) {

@@ -164,6 +164,27 @@ def test_converging_solve_met_by_initial_state(cuda_lib):
     assert torch.equal(p2, p)
 
 
+def test_converging_solve_stops_at_max_cycles(cuda_lib):
+    """The converging solve's loop is bounded on the device: a tolerance it
+    cannot reach (1e-13) in max_cycles = 3 ends the graph's while loop after
+    exactly three bodies with AJ_ERR_NOT_CONVERGED (4) in the device-side
+    statistics; the context stays usable - the next solve on the same stream
+    meets 1e-6 as usual."""
+    import torch
+    import aerojax_gb300 as aj
+    nx, ny, dx = 512, 128, 1 / 64
+    rng = np.random.default_rng(21)
+    b = torch.as_tensor(rng.standard_normal((nx, ny)).astype(np.float32), device="cuda")
+    m = torch.ones_like(b)
+    p, st = aj.poisson_multigrid_converge(b, m, dx, dx, rtol=1e-13, max_cycles=3)
+    torch.cuda.synchronize()
+    assert st["err"] == 4 and not st["converged"] and st["cycles"] == 3, st
+    assert st["rel_residual"] > 1e-13 and torch.isfinite(p).all()
+    p2, st2 = aj.poisson_multigrid_converge(b, m, dx, dx, rtol=1e-6)
+    torch.cuda.synchronize()
+    assert st2["err"] == 0 and st2["converged"] and st2["rel_residual"] <= 1e-6, st2
+
+
 def test_naca_converge_step(cuda_lib):
     import aerojax_gb300 as aj
     from aerojax_gb300 import configs
