@@ -743,8 +743,9 @@ int32_t aj_kernel_count(const AjStepParams* prm, int32_t cycles) {
   }
   if (p.mg_mode == AJ_MG_PARITY) n += 1;                        // stats
   n += 1;                                                       // correction
-  // features and scales, 12 convolutions (the first normalises), correction
-  if (p.nn_factor > 0) n += 2 + 12 + 1;
+  // features, scales, the convolutions (12, or 10 with the two
+  // full-resolution layer pairs fused), correction
+  if (p.nn_factor > 0) n += 2 + nn_inference_conv_launches() + 1;
   return n;
 }
 

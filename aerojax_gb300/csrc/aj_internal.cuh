@@ -319,6 +319,8 @@ int launch_mg_rhs(const AjStepParams& p, const Layout& L, void* ws, const float*
 inline bool nn_forms_rhs(const AjStepParams& p, bool learned) {
   return learned && p.grid_type == AJ_GRID_MAC && p.mg_mode == AJ_MG_CONVERGE;
 }
+// convolution launches of one inference pass (the layer pairs fused or not)
+int nn_inference_conv_launches();
 struct NnWarm {
   const uint16_t* packed = nullptr;
   const float* master = nullptr;

@@ -19,6 +19,7 @@
 // gradient.
 #include "aj_internal.cuh"
 #include <cuda_bf16.h>
+#include <stdlib.h>
 #include <string.h>
 
 namespace aj {
@@ -113,6 +114,128 @@ struct ConvArgs {
                             // sample's RMS (the features' normalisation)
 };
 
+// The output side of one conv tile: outputs of one 8 x 8 pixel tile and
+// BN = NT * 8 channels from co0.
+struct ConvOut {
+  float* Y;
+  float* Yp;          // nullable: 2x2 average pool of Y
+  const float* bias;  // nullable
+  int relu, H, W, Cout, n, h0, w0, co0;
+};
+
+// The K loop and epilogue of one conv tile from shared memory: As holds the
+// tile's 10 x 10 halo in BF16 ([px][CIN + 8]), Bs the 9 taps' weights
+// ([tap][BN][CIN + 8]); sm is the start of the block's dynamic shared memory
+// (the K halves' hand-over buffer once the loop is done).
+template <int CIN, int NT>
+__device__ __forceinline__ void conv_core(const __nv_bfloat16* As, const __nv_bfloat16* Bs,
+                                          unsigned char* sm, const ConvOut& o) {
+  constexpr int AS = CIN + 8, BN = NT * 8;
+  // two accumulator sets, even and odd 16-channel steps, halve each chain of
+  // dependent MMAs again; they are added before the hand-over
+  float acc[NT][4], acc2[NT][4];
+#pragma unroll
+  for (int q = 0; q < NT; ++q)
+#pragma unroll
+    for (int e = 0; e < 4; ++e) acc[q][e] = acc2[q][e] = 0.f;
+  // warp w: tile rows 2 (w & 3) and 2 (w & 3) + 1 (fragment rows g, g + 8);
+  // warps 0-3 run taps 0-4 and warps 4-7 taps 5-8, which halves each chain
+  // of dependent MMAs (9 Cin / 16 of them in one warp before).  Fragments
+  // come by ldmatrix: lane l addresses row l & 7 of 8x8 matrix l >> 3 - for
+  // A the pixel (tile row + (m & 1), column r + dx) at channel offset
+  // (m >> 1) * 8, for B output channel 8 (m >> 1) + r of the pair of
+  // 8-channel groups at channel offset (m & 1) * 8.
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int g = lane >> 2, tg = lane & 3;
+  float* __restrict__ Y = o.Y;
+  float* __restrict__ Yp = o.Yp;
+  const float* __restrict__ bias = o.bias;
+  const int relu = o.relu, H = o.H, W = o.W, Cout = o.Cout, n = o.n, h0 = o.h0, w0 = o.w0,
+            co0 = o.co0;
+  const int prow = warp & 3, kh = warp >> 2;
+  const int ty0 = 2 * prow;
+  const int lm = lane >> 3, lr = lane & 7;
+  const unsigned as0 = (unsigned)__cvta_generic_to_shared(As);
+  const unsigned bs0 = (unsigned)__cvta_generic_to_shared(Bs);
+  static_assert(NT % 2 == 0, "B fragments load in pairs of 8-channel groups");
+#pragma unroll 1
+  for (int tap = kh ? 5 : 0; tap < (kh ? 9 : 5); ++tap) {
+    const int dy = tap / 3, dx = tap % 3;   // halo offsets (tap - centre + 1)
+    const unsigned a_row =
+        as0 + (unsigned)((((ty0 + dy + (lm & 1)) * (CT + 2) + lr + dx) * AS + (lm >> 1) * 8) * 2);
+    const unsigned b_row = bs0 + (unsigned)(((tap * BN + (lm >> 1) * 8 + lr) * AS + (lm & 1) * 8) * 2);
+#pragma unroll
+    for (int ks = 0; ks < CIN / 16; ++ks) {
+      uint32_t a[4];
+      ldsm_x4(a, a_row + ks * 32);
+#pragma unroll
+      for (int qp = 0; qp < NT / 2; ++qp) {
+        uint32_t b[4];
+        ldsm_x4(b, b_row + (unsigned)(qp * 16 * AS * 2) + ks * 32);
+        mma_bf16((ks & 1) ? acc2[2 * qp] : acc[2 * qp], a, b);
+        mma_bf16((ks & 1) ? acc2[2 * qp + 1] : acc[2 * qp + 1], a, b + 2);
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < NT; ++q)
+#pragma unroll
+    for (int e = 0; e < 4; ++e) acc[q][e] += acc2[q][e];
+  // warps 4-7 hand their partial sums to warps 0-3 through the (now free)
+  // halo buffer; the sum is (taps 0-4) + (taps 5-8)
+  __syncthreads();
+  float* red = reinterpret_cast<float*>(sm);   // 4 x NT x 4 x 32 floats (ConvSmem checks)
+  if (kh) {
+#pragma unroll
+    for (int q = 0; q < NT; ++q)
+#pragma unroll
+      for (int e = 0; e < 4; ++e) red[((prow * NT + q) * 4 + e) * 32 + lane] = acc[q][e];
+  }
+  __syncthreads();
+  if (kh) return;
+#pragma unroll
+  for (int q = 0; q < NT; ++q)
+#pragma unroll
+    for (int e = 0; e < 4; ++e) acc[q][e] += red[((prow * NT + q) * 4 + e) * 32 + lane];
+  // epilogue: bias, ReLU, store; with Yp also the 2x2 average pool of the
+  // output (the warp holds both rows of a pooling window; the column
+  // neighbour is 4 lanes up), summed in the order s00 + s10 + s01 + s11 of the
+  // oracle's pool2
+  const int gw = w0 + g;
+#pragma unroll
+  for (int q = 0; q < NT; ++q) {
+    const int col = co0 + q * 8 + tg * 2;
+    const float b0 = bias ? bias[col] : 0.f, b1 = bias ? bias[col + 1] : 0.f;
+    float y[2][2];
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      y[half][0] = acc[q][half * 2] + b0;
+      y[half][1] = acc[q][half * 2 + 1] + b1;
+      if (relu) {
+        y[half][0] = fmaxf(y[half][0], 0.f);
+        y[half][1] = fmaxf(y[half][1], 0.f);
+      }
+      const int gh = h0 + ty0 + half;
+      if (gh < H && gw < W)
+        *reinterpret_cast<float2*>(&Y[(((long)n * H + gh) * W + gw) * Cout + col]) =
+            make_float2(y[half][0], y[half][1]);
+    }
+    if (Yp) {
+      float pv[2];
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        const float s01 = __shfl_down_sync(0xffffffffu, y[0][c], 4);
+        const float s11 = __shfl_down_sync(0xffffffffu, y[1][c], 4);
+        pv[c] = 0.25f * (((y[0][c] + y[1][c]) + s01) + s11);
+      }
+      const int ph = (h0 + ty0) >> 1, pw = gw >> 1;
+      if (!(g & 1) && h0 + ty0 + 1 < H && gw + 1 < W)
+        *reinterpret_cast<float2*>(&Yp[(((long)n * (H / 2) + ph) * (W / 2) + pw) * Cout + col]) =
+            make_float2(pv[0], pv[1]);
+    }
+  }
+}
+
 // One 8 x 8 pixel tile t (tiles ordered w fastest, then h, then sample) and
 // the BN = NT * 8 output channels from co0.  PDL: dependent launch (wait for
 // the previous layer after staging the weights).  Warps 4-7 return before the
@@ -132,8 +255,7 @@ __device__ __forceinline__ void conv_tile(const ConvArgs& cv, int t, int co0,
   constexpr int AS = S::AS, BN = S::BN;
   __nv_bfloat16* As = reinterpret_cast<__nv_bfloat16*>(conv_sm);          // [px][AS] BF16
   __nv_bfloat16* Bs = reinterpret_cast<__nv_bfloat16*>(conv_sm + S::a_bytes);   // [tap][BN][AS]
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int g = lane >> 2, tg = lane & 3;
+  const int tid = threadIdx.x;
   const int tilesW = (W + CT - 1) / CT, tilesH = (H + CT - 1) / CT;
   const int tw = t % tilesW;
   t /= tilesW;
@@ -213,102 +335,7 @@ __device__ __forceinline__ void conv_tile(const ConvArgs& cv, int t, int co0,
   }
   cp_async_wait<0>();
   __syncthreads();
-  // two accumulator sets, even and odd 16-channel steps, halve each chain of
-  // dependent MMAs again; they are added before the hand-over
-  float acc[NT][4], acc2[NT][4];
-#pragma unroll
-  for (int q = 0; q < NT; ++q)
-#pragma unroll
-    for (int e = 0; e < 4; ++e) acc[q][e] = acc2[q][e] = 0.f;
-  // warp w: tile rows 2 (w & 3) and 2 (w & 3) + 1 (fragment rows g, g + 8);
-  // warps 0-3 run taps 0-4 and warps 4-7 taps 5-8, which halves each chain
-  // of dependent MMAs (9 Cin / 16 of them in one warp before).  Fragments
-  // come by ldmatrix: lane l addresses row l & 7 of 8x8 matrix l >> 3 - for
-  // A the pixel (tile row + (m & 1), column r + dx) at channel offset
-  // (m >> 1) * 8, for B output channel 8 (m >> 1) + r of the pair of
-  // 8-channel groups at channel offset (m & 1) * 8.
-  const int prow = warp & 3, kh = warp >> 2;
-  const int ty0 = 2 * prow;
-  const int lm = lane >> 3, lr = lane & 7;
-  const unsigned as0 = (unsigned)__cvta_generic_to_shared(As);
-  const unsigned bs0 = (unsigned)__cvta_generic_to_shared(Bs);
-  static_assert(NT % 2 == 0, "B fragments load in pairs of 8-channel groups");
-#pragma unroll 1
-  for (int tap = kh ? 5 : 0; tap < (kh ? 9 : 5); ++tap) {
-    const int dy = tap / 3, dx = tap % 3;   // halo offsets (tap - centre + 1)
-    const unsigned a_row =
-        as0 + (unsigned)((((ty0 + dy + (lm & 1)) * (CT + 2) + lr + dx) * AS + (lm >> 1) * 8) * 2);
-    const unsigned b_row = bs0 + (unsigned)(((tap * BN + (lm >> 1) * 8 + lr) * AS + (lm & 1) * 8) * 2);
-#pragma unroll
-    for (int ks = 0; ks < CIN / 16; ++ks) {
-      uint32_t a[4];
-      ldsm_x4(a, a_row + ks * 32);
-#pragma unroll
-      for (int qp = 0; qp < NT / 2; ++qp) {
-        uint32_t b[4];
-        ldsm_x4(b, b_row + (unsigned)(qp * 16 * AS * 2) + ks * 32);
-        mma_bf16((ks & 1) ? acc2[2 * qp] : acc[2 * qp], a, b);
-        mma_bf16((ks & 1) ? acc2[2 * qp + 1] : acc[2 * qp + 1], a, b + 2);
-      }
-    }
-  }
-#pragma unroll
-  for (int q = 0; q < NT; ++q)
-#pragma unroll
-    for (int e = 0; e < 4; ++e) acc[q][e] += acc2[q][e];
-  // warps 4-7 hand their partial sums to warps 0-3 through the (now free)
-  // halo buffer; the sum is (taps 0-4) + (taps 5-8)
-  __syncthreads();
-  float* red = reinterpret_cast<float*>(conv_sm);   // 4 x NT x 4 x 32 floats (ConvSmem checks)
-  if (kh) {
-#pragma unroll
-    for (int q = 0; q < NT; ++q)
-#pragma unroll
-      for (int e = 0; e < 4; ++e) red[((prow * NT + q) * 4 + e) * 32 + lane] = acc[q][e];
-  }
-  __syncthreads();
-  if (kh) return;
-#pragma unroll
-  for (int q = 0; q < NT; ++q)
-#pragma unroll
-    for (int e = 0; e < 4; ++e) acc[q][e] += red[((prow * NT + q) * 4 + e) * 32 + lane];
-  // epilogue: bias, ReLU, store; with Yp also the 2x2 average pool of the
-  // output (the warp holds both rows of a pooling window; the column
-  // neighbour is 4 lanes up), summed in the order s00 + s10 + s01 + s11 of the
-  // oracle's pool2
-  const int gw = w0 + g;
-#pragma unroll
-  for (int q = 0; q < NT; ++q) {
-    const int col = co0 + q * 8 + tg * 2;
-    const float b0 = bias ? bias[col] : 0.f, b1 = bias ? bias[col + 1] : 0.f;
-    float y[2][2];
-#pragma unroll
-    for (int half = 0; half < 2; ++half) {
-      y[half][0] = acc[q][half * 2] + b0;
-      y[half][1] = acc[q][half * 2 + 1] + b1;
-      if (relu) {
-        y[half][0] = fmaxf(y[half][0], 0.f);
-        y[half][1] = fmaxf(y[half][1], 0.f);
-      }
-      const int gh = h0 + ty0 + half;
-      if (gh < H && gw < W)
-        *reinterpret_cast<float2*>(&Y[(((long)n * H + gh) * W + gw) * Cout + col]) =
-            make_float2(y[half][0], y[half][1]);
-    }
-    if (Yp) {
-      float pv[2];
-#pragma unroll
-      for (int c = 0; c < 2; ++c) {
-        const float s01 = __shfl_down_sync(0xffffffffu, y[0][c], 4);
-        const float s11 = __shfl_down_sync(0xffffffffu, y[1][c], 4);
-        pv[c] = 0.25f * (((y[0][c] + y[1][c]) + s01) + s11);
-      }
-      const int ph = (h0 + ty0) >> 1, pw = gw >> 1;
-      if (!(g & 1) && h0 + ty0 + 1 < H && gw + 1 < W)
-        *reinterpret_cast<float2*>(&Yp[(((long)n * (H / 2) + ph) * (W / 2) + pw) * Cout + col]) =
-            make_float2(pv[0], pv[1]);
-    }
-  }
+  conv_core<CIN, NT>(As, Bs, conv_sm, ConvOut{Y, Yp, bias, relu, H, W, Cout, n, h0, w0, co0});
 }
 
 template <int CIN, int NT>
@@ -316,6 +343,218 @@ __global__ void __launch_bounds__(CONV_THREADS) k_conv3x3(ConvArgs a) {
   extern __shared__ __align__(16) unsigned char conv_sm[];
   conv_tile<CIN, NT, true>(a, blockIdx.x, blockIdx.y * NT * 8, conv_sm);
 }
+
+// ---------------------------------------------------------------- layer pairs
+// Two 3x3 convolutions at the same resolution in one launch (inference):
+// phase A computes the first layer on the 10 x 10 region around the output
+// tile - the second layer's halo - from a 12 x 12 input halo, as seven
+// 16-row fragments whose rows ldmatrix addresses pixel by pixel (100 of the
+// 112 rows are used), and stores it, bias and ReLU applied, rounded to BF16
+// (the rounding the second layer's staging applies) and zero outside the
+// image (the second layer's 'SAME' padding), in shared memory; phase B is
+// conv_core on that intermediate.  The first layer's output never leaves
+// the SM, and the pair costs one launch and one staging round.  Used for the
+// full-resolution pairs (e0a/e0b, d0a/d0b), whose 256 tiles fill the GPU;
+// at 128 x 32 (e1a/e1b: 64 tiles of 64 channels) the fused pair measured
+// slower than two launches of 256 lighter blocks, and the deeper pairs keep
+// one launch per layer, where splitting the output channels over blocks is
+// the parallelism.
+template <int CIN, int CMID, int COUT>
+struct PairSmem {
+  static constexpr int ASI = CIN + 8, ASM = CMID + 8;
+  static constexpr int HE = CT + 4, HIN = HE * HE;   // 12 x 12 input halo
+  static constexpr size_t in_bytes = (size_t)HIN * ASI * 2;
+  static constexpr size_t wa_bytes = (size_t)9 * CMID * ASI * 2;
+  static constexpr size_t mid_bytes = (size_t)CT_HALO * ASM * 2;
+  static constexpr size_t wb_bytes = (size_t)9 * COUT * ASM * 2;
+  static constexpr size_t off_wa = in_bytes, off_mid = off_wa + wa_bytes,
+                          off_wb = off_mid + mid_bytes, bytes = off_wb + wb_bytes;
+  static_assert(in_bytes % 16 == 0 && wa_bytes % 16 == 0 && mid_bytes % 16 == 0 &&
+                    (ASI * 2) % 16 == 0 && (ASM * 2) % 16 == 0,
+                "ldmatrix rows and sections 16-byte aligned");
+  static_assert((size_t)4 * (COUT / 8) * 4 * 32 * 4 <= off_mid,
+                "the K halves' hand-over fits the dead input sections");
+};
+
+struct PairArgs {
+  const float* X;        // first layer's input, NHWC [H][W][CIN]
+  const float* Xc;       // nullable: the input is up2(Xc) + X
+  const DevScalars* norm;   // nullable: scale input channels 0 and 2 (the features)
+  int H, W;
+  const __nv_bfloat16* WA;  // [tap][CMID][CIN]
+  const float* biasA;
+  int reluA;
+  const __nv_bfloat16* WB;  // [tap][COUT][CMID]
+  const float* biasB;
+  int reluB;
+  float* Y;              // second layer's output [H][W][COUT]
+  float* Yp;             // nullable: its 2x2 average pool
+};
+
+template <int CIN, int CMID, int COUT>
+__global__ void __launch_bounds__(CONV_THREADS) k_conv_pair(PairArgs a) {
+  extern __shared__ __align__(16) unsigned char pair_sm[];
+  using S = PairSmem<CIN, CMID, COUT>;
+  constexpr int ASI = S::ASI, ASM = S::ASM, HE = S::HE;
+  __nv_bfloat16* In = reinterpret_cast<__nv_bfloat16*>(pair_sm);
+  __nv_bfloat16* Wa = reinterpret_cast<__nv_bfloat16*>(pair_sm + S::off_wa);
+  __nv_bfloat16* Mid = reinterpret_cast<__nv_bfloat16*>(pair_sm + S::off_mid);
+  __nv_bfloat16* Wb = reinterpret_cast<__nv_bfloat16*>(pair_sm + S::off_wb);
+  const int H = a.H, W = a.W;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int g = lane >> 2, tg = lane & 3;
+  const int tilesW = (W + CT - 1) / CT;
+  const int h0 = (blockIdx.x / tilesW) * CT, w0 = (blockIdx.x % tilesW) * CT;
+  {  // both layers' weights (all channels), before the wait for the input
+    constexpr int PRA = CIN / 8, PRB = CMID / 8;
+    for (int e = tid; e < 9 * CMID * PRA; e += CONV_THREADS) {
+      const int row = e / PRA, q = e - row * PRA;
+      cp_async16(Wa + row * ASI + q * 8, a.WA + (long)row * CIN + q * 8);
+    }
+    for (int e = tid; e < 9 * COUT * PRB; e += CONV_THREADS) {
+      const int row = e / PRB, q = e - row * PRB;
+      cp_async16(Wb + row * ASM + q * 8, a.WB + (long)row * CMID + q * 8);
+    }
+    cp_async_commit();
+  }
+  pdl_wait();
+  {  // the 12 x 12 input halo in BF16 (conv_tile's staging, two cells deep)
+    constexpr int C8 = CIN / 8, XB = 4;
+    const int Hc = H >> 1, Wc = W >> 1;
+    float ir = 1.f, ip = 1.f;
+    if (a.norm) {
+      ir = (float)(1.0 / a.norm->nn_rms_r);
+      ip = (float)(1.0 / a.norm->nn_rms_p);
+    }
+    for (int e0 = tid; e0 < S::HIN * C8; e0 += XB * CONV_THREADS) {
+      float4 xa[XB], xb[XB], ca[XB], cb[XB];
+      bool in[XB];
+#pragma unroll
+      for (int k = 0; k < XB; ++k) {
+        const int e = e0 + k * CONV_THREADS;
+        const int px = e / C8, q = e - px * C8;
+        const int hy = px / HE, hx = px - hy * HE;
+        const int gh = h0 - 2 + hy, gw = w0 - 2 + hx;
+        in[k] = e < S::HIN * C8 && gh >= 0 && gh < H && gw >= 0 && gw < W;
+        xa[k] = xb[k] = ca[k] = cb[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (in[k]) {
+          const float4* src = reinterpret_cast<const float4*>(a.X + ((long)gh * W + gw) * CIN + q * 8);
+          xa[k] = __ldcg(src);
+          xb[k] = __ldcg(src + 1);
+          if (a.Xc) {
+            const float4* cs = reinterpret_cast<const float4*>(
+                a.Xc + ((long)(gh >> 1) * Wc + (gw >> 1)) * CIN + q * 8);
+            ca[k] = __ldcg(cs);
+            cb[k] = __ldcg(cs + 1);
+          }
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < XB; ++k) {
+        const int e = e0 + k * CONV_THREADS;
+        if (e >= S::HIN * C8) break;
+        const int px = e / C8, q = e - px * C8;
+        float4 u = xa[k], w = xb[k];
+        if (a.norm && q == 0) {
+          u.x *= ir;
+          u.z *= ip;
+        }
+        if (a.Xc && in[k]) {
+          u = make_float4(ca[k].x + u.x, ca[k].y + u.y, ca[k].z + u.z, ca[k].w + u.w);
+          w = make_float4(cb[k].x + w.x, cb[k].y + w.y, cb[k].z + w.z, cb[k].w + w.w);
+        }
+        uint4 v;
+        v.x = pack_bf16x2(u.x, u.y);
+        v.y = pack_bf16x2(u.z, u.w);
+        v.z = pack_bf16x2(w.x, w.y);
+        v.w = pack_bf16x2(w.z, w.w);
+        *reinterpret_cast<uint4*>(In + px * ASI + q * 8) = v;
+      }
+    }
+    (void)Hc;
+  }
+  cp_async_wait<0>();
+  __syncthreads();
+  // phase A: warp w < 7 computes rows 16 w .. 16 w + 15 of the 10 x 10
+  // intermediate (pixel p = 10 py + px at (h0 - 1 + py, w0 - 1 + px)), all
+  // CMID channels, the nine taps in order with even and odd 16-channel steps
+  // in separate accumulators
+  if (warp < 7) {
+    constexpr int NQ = CMID / 8;
+    float acc[NQ][4], acc2[NQ][4];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q)
+#pragma unroll
+      for (int e = 0; e < 4; ++e) acc[q][e] = acc2[q][e] = 0.f;
+    const int lm = lane >> 3, lr = lane & 7;
+    int pr = warp * 16 + (lm & 1) * 8 + lr;   // this lane's ldmatrix row (a pixel)
+    pr = pr < CT_HALO ? pr : CT_HALO - 1;     // rows 100..111: any valid pixel, discarded
+    const int py = pr / (CT + 2), pxx = pr - py * (CT + 2);
+    const unsigned in0 = (unsigned)__cvta_generic_to_shared(In);
+    const unsigned wa0 = (unsigned)__cvta_generic_to_shared(Wa);
+#pragma unroll 1
+    for (int tap = 0; tap < 9; ++tap) {
+      const int dy = tap / 3, dx = tap % 3;
+      const unsigned a_row =
+          in0 + (unsigned)((((py + dy) * HE + pxx + dx) * ASI + (lm >> 1) * 8) * 2);
+      const unsigned b_row =
+          wa0 + (unsigned)(((tap * CMID + (lm >> 1) * 8 + lr) * ASI + (lm & 1) * 8) * 2);
+#pragma unroll
+      for (int ks = 0; ks < CIN / 16; ++ks) {
+        uint32_t af[4];
+        ldsm_x4(af, a_row + ks * 32);
+#pragma unroll
+        for (int qp = 0; qp < NQ / 2; ++qp) {
+          uint32_t b[4];
+          ldsm_x4(b, b_row + (unsigned)(qp * 16 * ASI * 2) + ks * 32);
+          mma_bf16((ks & 1) ? acc2[2 * qp] : acc[2 * qp], af, b);
+          mma_bf16((ks & 1) ? acc2[2 * qp + 1] : acc[2 * qp + 1], af, b + 2);
+        }
+      }
+    }
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      const int pix = warp * 16 + g + 8 * half;
+      if (pix >= CT_HALO) continue;
+      const int qy = pix / (CT + 2), qx = pix - qy * (CT + 2);
+      const int gh = h0 - 1 + qy, gw = w0 - 1 + qx;
+      const bool inside = gh >= 0 && gh < H && gw >= 0 && gw < W;
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) {
+        const int col = q * 8 + tg * 2;
+        float v0 = acc[q][half * 2] + acc2[q][half * 2] + a.biasA[col];
+        float v1 = acc[q][half * 2 + 1] + acc2[q][half * 2 + 1] + a.biasA[col + 1];
+        if (a.reluA) {
+          v0 = fmaxf(v0, 0.f);
+          v1 = fmaxf(v1, 0.f);
+        }
+        if (!inside) v0 = v1 = 0.f;
+        *reinterpret_cast<uint32_t*>(Mid + pix * ASM + col) = pack_bf16x2(v0, v1);
+      }
+    }
+  }
+  __syncthreads();
+  // phase B: the second layer on the intermediate, all COUT channels
+  conv_core<CMID, COUT / 8>(Mid, Wb, pair_sm,
+                            ConvOut{a.Y, a.Yp, a.biasB, a.reluB, H, W, COUT, 0, h0, w0, 0});
+}
+
+template <int CIN, int CMID, int COUT>
+static void pair_launch(const PairArgs& a, cudaStream_t st) {
+  const int tiles = ((a.W + CT - 1) / CT) * ((a.H + CT - 1) / CT);
+  launch_pdl(true, k_conv_pair<CIN, CMID, COUT>, dim3(tiles), dim3(CONV_THREADS),
+             PairSmem<CIN, CMID, COUT>::bytes, st, a);
+}
+
+// AEROJAX_NN_PAIRS=0: every layer its own launch (read once)
+static bool nn_pairs_enabled() {
+  static const bool on = [] {
+    const char* e = getenv("AEROJAX_NN_PAIRS");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+int nn_inference_conv_launches() { return nn_pairs_enabled() ? 10 : 12; }
 
 template <int CIN, int NT>
 static void conv_launch(const float* X, int N, int H, int W, int Cout, const __nv_bfloat16* WT,
@@ -342,6 +581,11 @@ static void conv_attrs() {
   conv_attr<32, 2>(); conv_attr<32, 4>();
   conv_attr<64, 2>(); conv_attr<64, 4>();
   conv_attr<128, 2>(); conv_attr<128, 4>();
+  cudaFuncSetAttribute(k_conv_pair<16, 32, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)PairSmem<16, 32, 32>::bytes);
+  cudaFuncSetAttribute(k_conv_pair<32, 32, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)PairSmem<32, 32, 16>::bytes);
+
   done = true;
 }
 
@@ -678,8 +922,16 @@ int nn_forward(int n, int h, int w, const NnW& W, const NnActs& A, cudaStream_t 
                    kLayers[l].relu, st, pooled, coarse, !keep, l == E0A ? norm : nullptr);
   };
   int rc = AJ_OK;
-  rc |= conv(E0A, A.x, A.a0, H0, W0);
-  rc |= conv(E0B, A.a0, A.s0, H0, W0, A.p0);     // s0 and its pool p0
+  // inference on one sample: the full-resolution layer pairs in one launch each
+  const bool pairs = !keep && n == 1 && nn_pairs_enabled();
+  if (pairs) {
+    pair_launch<16, 32, 32>(PairArgs{A.x, nullptr, norm, H0, W0, W.wf(E0A), W.bias(E0A),
+                                     kLayers[E0A].relu, W.wf(E0B), W.bias(E0B),
+                                     kLayers[E0B].relu, A.s0, A.p0}, st);
+  } else {
+    rc |= conv(E0A, A.x, A.a0, H0, W0);
+    rc |= conv(E0B, A.a0, A.s0, H0, W0, A.p0);   // s0 and its pool p0
+  }
   rc |= conv(E1A, A.p0, A.a1, H1, W1);
   rc |= conv(E1B, A.a1, A.s1, H1, W1, A.p1);
   rc |= conv(E2A, A.p1, A.a2, H2, W2);
@@ -696,9 +948,14 @@ int nn_forward(int n, int h, int w, const NnW& W, const NnActs& A, cudaStream_t 
   } else {
     rc |= conv(D2, A.s2, A.o2, H2, W2, nullptr, A.bt);
     rc |= conv(D1, A.s1, A.o1, H1, W1, nullptr, A.o2);
-    rc |= conv(D0A, A.s0, A.o0, H0, W0, nullptr, A.o1);
+    if (pairs)
+      pair_launch<32, 32, 16>(PairArgs{A.s0, A.o1, nullptr, H0, W0, W.wf(D0A), W.bias(D0A),
+                                       kLayers[D0A].relu, W.wf(D0B), W.bias(D0B),
+                                       kLayers[D0B].relu, A.y, nullptr}, st);
+    else
+      rc |= conv(D0A, A.s0, A.o0, H0, W0, nullptr, A.o1);
   }
-  rc |= conv(D0B, A.o0, A.y, H0, W0);
+  if (!pairs) rc |= conv(D0B, A.o0, A.y, H0, W0);
   if (rc != AJ_OK) return AJ_ERR_PARAM;
   return cudaGetLastError() == cudaSuccess ? AJ_OK : AJ_ERR_CUDA;
 }
