@@ -10,10 +10,13 @@
 //                      restriction, the FP64 dense solve of the coarsest grid,
 //                      prolongation, sweeps
 //   levels lc-1 .. 1   k_cv_up: e += P(e_coarse), 2 red-black sweeps
-//   level 0            k_cv_up0: the same, then p += e, the residual
-//                      r = b - A p for the next iteration, its FP64 norm, and
-//                      (last block) the convergence test that sets the while
-//                      node's condition with cudaGraphSetConditional
+//   level 0            k_cv_up0: e += P(e_coarse), 1 red-black sweep (a
+//                      V(2,1) cycle on the fine grid: from the warm starts of
+//                      a developed flow it ends in as many cycles as V(2,2)
+//                      with a halo of 3 instead of 5), then p += e, the
+//                      residual r = b - A p for the next iteration, its FP64
+//                      norm, and (last block) the convergence test that sets
+//                      the while node's condition with cudaGraphSetConditional
 //
 // Precision.  The V-cycle runs in FP32.  The refinement state p and the
 // refinement residual are kept in double-FP32 ("double-single") arithmetic:
@@ -97,6 +100,63 @@ __device__ __forceinline__ df df_residual(float b, df c, df xp, df xm, df yp, df
   return df_add_f(df_neg(ap), b);
 }
 
+// ---------------------------------------------------------------- paired double-FP32
+// Two double-FP32 values side by side (a thread's two columns of a tile row)
+// through the same error-free transformations on Blackwell's paired FP32
+// instructions: each lane of __fadd2_rn / __fmul2_rn / __ffma2_rn rounds as
+// the scalar operation does, and the explicit intrinsics are never contracted.
+struct df2 {
+  float2 hi, lo;
+};
+__device__ __forceinline__ float2 f2(float x) { return make_float2(x, x); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+// a - b as fma(b, -1, a): the exact difference, rounded once
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, f2(-1.f), a); }
+__device__ __forceinline__ df2 two_sum2(float2 a, float2 b) {
+  const float2 s = add2(a, b);
+  const float2 bb = sub2(s, a);
+  return {s, add2(sub2(a, sub2(s, bb)), sub2(b, bb))};
+}
+__device__ __forceinline__ df2 quick_two_sum2(float2 a, float2 b) {
+  const float2 s = add2(a, b);
+  return {s, sub2(b, sub2(s, a))};
+}
+__device__ __forceinline__ df2 df2_add_s(df2 a, df2 b) {   // as df_add_s
+  df2 s = two_sum2(a.hi, b.hi);
+  s.lo = add2(s.lo, add2(a.lo, b.lo));
+  return quick_two_sum2(s.hi, s.lo);
+}
+__device__ __forceinline__ df2 df2_add_f(df2 a, float2 b) {   // as df_add_f
+  df2 s = two_sum2(a.hi, b);
+  s.lo = add2(s.lo, a.lo);
+  return quick_two_sum2(s.hi, s.lo);
+}
+// a * b for one double-FP32 a: TwoProd by fma, whose error term is formed
+// negated (fma(-a, b, p) = -(a b - p) exactly) and subtracted
+__device__ __forceinline__ df2 df2_mul_u(df a, df2 b) {
+  const float2 ah = f2(a.hi);
+  const float2 p = __fmul2_rn(ah, b.hi);
+  const float2 en = __ffma2_rn(f2(-a.hi), b.hi, p);
+  const float2 cross = __ffma2_rn(ah, b.lo, __fmul2_rn(f2(a.lo), b.hi));
+  return quick_two_sum2(p, sub2(cross, en));
+}
+// b - a: df_add_f(df_neg(a), b) with the signs carried through (negation
+// is exact, so every rounding is the scalar form's)
+__device__ __forceinline__ df2 df2_rsub_f(float2 b, df2 a) {
+  const float2 s = sub2(b, a.hi);
+  const float2 bb = add2(s, a.hi);
+  const float2 e = sub2(sub2(b, bb), add2(a.hi, sub2(s, bb)));
+  return quick_two_sum2(s, sub2(e, a.lo));
+}
+// df_residual for two cells
+__device__ __forceinline__ df2 df2_residual(float2 b, df2 c, df2 xp, df2 xm, df2 yp, df2 ym,
+                                            df ax, df ay) {
+  const df2 c2{__fmul2_rn(c.hi, f2(-2.f)), __fmul2_rn(c.lo, f2(-2.f))};
+  const df2 sx = df2_add_s(df2_add_s(xp, xm), c2);
+  const df2 sy = df2_add_s(df2_add_s(yp, ym), c2);
+  return df2_rsub_f(b, df2_add_s(df2_mul_u(ax, sx), df2_mul_u(ay, sy)));
+}
+
 struct DfCoef {
   float axh, axl, ayh, ayl;   // 1/dx^2 and 1/dy^2 split into hi + lo
 };
@@ -111,14 +171,15 @@ static DfCoef df_coef(double ax, double ay) {
 
 // ---------------------------------------------------------------- tiles
 // A tile is SI x SJ cells of shared memory: the TI x TJ interior plus a halo
-// of CV_H cells.  Threads form a (SJ/2) x RG grid: thread (tx, ty) owns the
-// column pair {2tx, 2tx+1} and walks the rows ty, ty+RG, ...; in a red-black
-// half-sweep exactly one cell of its pair per row has the colour being
-// updated, so no index needs a division.
-template <int SI_, int SJ_, int NTH_>
+// of H = 2 NS + 1 cells (NS red-black sweeps, one cell for the residual).
+// Threads form a (SJ/2) x RG grid: thread (tx, ty) owns the column pair
+// {2tx, 2tx+1} and walks the rows ty, ty+RG, ...; in a red-black half-sweep
+// exactly one cell of its pair per row has the colour being updated, so no
+// index needs a division.
+template <int SI_, int SJ_, int NTH_, int NS_ = CV_NS>
 struct TileCfg {
-  static constexpr int SI = SI_, SJ = SJ_, NTH = NTH_;
-  static constexpr int TI = SI - 2 * CV_H, TJ = SJ - 2 * CV_H;
+  static constexpr int SI = SI_, SJ = SJ_, NTH = NTH_, NS = NS_, H = 2 * NS_ + 1;
+  static constexpr int TI = SI - 2 * H, TJ = SJ - 2 * H;
   static constexpr int PAIRS = SJ / 2, RG = NTH / PAIRS, NT = SI * SJ;
   static_assert(TI % 2 == 0 && TJ % 2 == 0, "tile interiors must align with the coarse grid");
   static_assert(NTH % PAIRS == 0, "threads must fill whole rows of column pairs");
@@ -127,6 +188,12 @@ using T0 = TileCfg<48, 64, 256>;   // level 0: 38 x 54 interior (default)
 using T0b = TileCfg<32, 64, 256>;  // level 0: 22 x 54 interior (more, shorter tiles)
 using T0c = TileCfg<64, 32, 256>;  // level 0: 54 x 22 interior (narrow tiles)
 using T1 = TileCfg<32, 32, 256>;   // coarser levels: 22 x 22 interior
+// Level 0 post-smooths with one sweep (a V(2,1) cycle on the fine grid,
+// V(2,2) below it): the same tiles with a halo of 3
+constexpr int CV_NS_UP0 = 1;
+using T0u = TileCfg<48, 64, 256, CV_NS_UP0>;    // 42 x 58 interior
+using T0bu = TileCfg<32, 64, 256, CV_NS_UP0>;   // 26 x 58 interior
+using T0cu = TileCfg<64, 32, 256, CV_NS_UP0>;   // 58 x 26 interior
 constexpr int CV_TILE_VARIANTS = 3;
 
 __device__ __forceinline__ float cv_diag(const CvLvl& L, int gi, int gj) {
@@ -150,7 +217,7 @@ __device__ __forceinline__ void cv_sweeps_t(float* E, const float* R, const CvLv
   constexpr int ROWS = (SI - 2 + TC::RG - 1) / TC::RG;   // rows of a thread per half-sweep
   const int tx = threadIdx.x, ty = threadIdx.y;
   const float inv_int = 1.f / (-2.f * (L.ax + L.ay));
-  for (int h = 0; h < 2 * CV_NS; ++h) {
+  for (int h = 0; h < 2 * TC::NS; ++h) {
     const int color = h & 1;
     // every new value of this thread's rows first, then the stores: a
     // half-sweep reads only the other colour, so no store can feed a load of
@@ -281,7 +348,7 @@ __global__ void __launch_bounds__(TC::NTH) k_cv_down(CvLvl L, const float* r0, c
   __shared__ float E[TC::NT];
   __shared__ float R[TC::NT];
   const int i0 = blockIdx.y * TI, j0 = blockIdx.x * TJ;
-  const int gi0 = i0 - CV_H, gj0 = j0 - CV_H;
+  const int gi0 = i0 - TC::H, gj0 = j0 - TC::H;
   const int tx = threadIdx.x, ty = threadIdx.y;
   const float* r = (r1 && *cur) ? r1 : r0;
   cv_load<TC, true>(E, R, L, gi0, gj0, r, nullptr, nullptr);
@@ -294,15 +361,15 @@ __global__ void __launch_bounds__(TC::NTH) k_cv_down(CvLvl L, const float* r0, c
   int rc_[DR][2];
 #pragma unroll
   for (int it = 0; it < DR; ++it) {
-    const int ti = CV_H + ty + it * TC::RG;
+    const int ti = TC::H + ty + it * TC::RG;
     const int gi = gi0 + ti;
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
-      const int tj = CV_H + tx + q * TC::PAIRS;
+      const int tj = TC::H + tx + q * TC::PAIRS;
       const int gj = gj0 + tj;
       rc_[it][q] = -1;
       res[it][q] = 0.f;
-      if (ti >= CV_H + TI || gi >= L.n || tj >= CV_H + TJ || gj >= L.m) continue;
+      if (ti >= TC::H + TI || gi >= L.n || tj >= TC::H + TJ || gj >= L.m) continue;
       const int c = ti * SJ + tj;
       e_out[(long)gi * L.m + gj] = E[c];
       if (!(L.level == 0 && gi == L.n - 1)) {
@@ -325,7 +392,7 @@ __global__ void __launch_bounds__(TC::NTH) k_cv_down(CvLvl L, const float* r0, c
     for (int cj = tx; cj < TJ / 2; cj += TC::PAIRS) {
       const int J = (j0 >> 1) + cj;
       if (J >= mc) break;
-      const int c = (CV_H + 2 * ci) * SJ + CV_H + 2 * cj;
+      const int c = (TC::H + 2 * ci) * SJ + TC::H + 2 * cj;
       rc[(long)I * mc + J] = 0.25f * (R[c] + R[c + SJ] + R[c + 1] + R[c + SJ + 1]);
     }
   }
@@ -344,21 +411,21 @@ __global__ void __launch_bounds__(TC::NTH) k_cv_up(CvLvl L, const float* __restr
   __shared__ float E[TC::NT];
   __shared__ float R[TC::NT];
   const int i0 = blockIdx.y * TI, j0 = blockIdx.x * TJ;
-  const int gi0 = i0 - CV_H, gj0 = j0 - CV_H;
+  const int gi0 = i0 - TC::H, gj0 = j0 - TC::H;
   const int tx = threadIdx.x, ty = threadIdx.y;
   __shared__ float W[CoarseWin<TC>::R * CoarseWin<TC>::C];
   cv_load_coarse<TC>(W, gi0, gj0, ec, nc, mc, gc);
   __syncthreads();
   cv_load<TC, false>(E, R, L, gi0, gj0, r, e_in, W);
   cv_sweeps<TC>(E, R, L, gi0, gj0);
-  for (int ti = CV_H + ty; ti < CV_H + TI; ti += TC::RG) {
+  for (int ti = TC::H + ty; ti < TC::H + TI; ti += TC::RG) {
     const int gi = gi0 + ti;
     if (gi >= L.n) break;
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
-      const int tj = CV_H + tx + q * TC::PAIRS;
+      const int tj = TC::H + tx + q * TC::PAIRS;
       const int gj = gj0 + tj;
-      if (tj >= CV_H + TJ || gj >= L.m) continue;
+      if (tj >= TC::H + TJ || gj >= L.m) continue;
       e_out[(long)gi * L.m + gj] = E[ti * SJ + tj];
     }
   }
@@ -457,7 +524,7 @@ __global__ void __launch_bounds__(TC::NTH, 4) k_cv_up0(
   __shared__ float PL[PI * PJ];
   __shared__ int am_last;
   const int i0 = blockIdx.y * TI, j0 = blockIdx.x * TJ;
-  const int gi0 = i0 - CV_H, gj0 = j0 - CV_H;
+  const int gi0 = i0 - TC::H, gj0 = j0 - TC::H;
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int tid = ty * TC::PAIRS + tx;
   const long N = (long)L.n * L.m;
@@ -503,37 +570,46 @@ __global__ void __launch_bounds__(TC::NTH, 4) k_cv_up0(
   cv_sweeps<TC>(E, R, L, gi0, gj0);
   asm volatile("cp.async.wait_group 0;\n" ::: "memory");
   __syncthreads();
-  // new pressure on the interior and one cell around it (all of this
-  // thread's sums first, then the stores)
+  // new pressure on the interior and one cell around it, the thread's two
+  // columns of a row as one pair (all of this thread's sums first, then the
+  // stores)
   constexpr int PR = (PI + TC::RG - 1) / TC::RG;
-  df pv[PR][2];
+  df2 pv[PR];
   int pt[PR][2];
 #pragma unroll
   for (int it = 0; it < PR; ++it) {
     const int pi = ty + it * TC::RG;
     const int gi = i0 - 1 + pi;
     const bool row_in = pi < PI && (unsigned)gi < (unsigned)L.n && gi != L.n - 1;
+    float h[2], l[2], e[2];
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
       const int pj = tx + q * TC::PAIRS;
       const int gj = j0 - 1 + pj;
       pt[it][q] = -1;
-      pv[it][q] = df{0.f, 0.f};
+      h[q] = l[q] = e[q] = 0.f;
       if (row_in && pj < PJ && (unsigned)gj < (unsigned)L.m) {
         const int t = pi * PJ + pj;
-        pv[it][q] = df_add_f(df{PH[t], PL[t]}, E[(CV_H - 1 + pi) * SJ + (CV_H - 1 + pj)]);
+        h[q] = PH[t];
+        l[q] = PL[t];
+        e[q] = E[(TC::H - 1 + pi) * SJ + (TC::H - 1 + pj)];
         pt[it][q] = t;
       }
     }
+    pv[it] = df2_add_f(df2{make_float2(h[0], h[1]), make_float2(l[0], l[1])},
+                       make_float2(e[0], e[1]));
   }
 #pragma unroll
-  for (int it = 0; it < PR; ++it)
-#pragma unroll
-    for (int q = 0; q < 2; ++q)
-      if (pt[it][q] >= 0) {
-        PH[pt[it][q]] = pv[it][q].hi;
-        PL[pt[it][q]] = pv[it][q].lo;
-      }
+  for (int it = 0; it < PR; ++it) {
+    if (pt[it][0] >= 0) {
+      PH[pt[it][0]] = pv[it].hi.x;
+      PL[pt[it][0]] = pv[it].lo.x;
+    }
+    if (pt[it][1] >= 0) {
+      PH[pt[it][1]] = pv[it].hi.y;
+      PL[pt[it][1]] = pv[it].lo.y;
+    }
+  }
   __syncthreads();
   const df ax{co.axh, co.axl}, ay{co.ayh, co.ayl};
   float acc = 0.f;
@@ -542,27 +618,44 @@ __global__ void __launch_bounds__(TC::NTH, 4) k_cv_up0(
     const int ti = ty + it * TC::RG;
     const int gi = i0 + ti;
     if (ti >= TI || gi >= L.n) break;
+    // the row's two columns tx and tx + PAIRS; a column outside the tile or
+    // the grid reads the row's first window cell (in bounds) and stores nothing
+    bool ok[2];
+    long k[2];
+    df pc[2], xp[2], xm[2], yp[2], ym[2];
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
       const int tj = tx + q * TC::PAIRS;
       const int gj = j0 + tj;
-      if (tj >= TJ || gj >= L.m) continue;
-      const long k = (long)gi * L.m + gj;
-      const int c = (ti + 1) * PJ + (tj + 1);
-      const df pc{PH[c], PL[c]};
-      pout[k] = pc.hi;
-      pout[N + k] = pc.lo;
-      float rr = 0.f;
-      if (gi != L.n - 1) {
-        const df xp{PH[c + PJ], PL[c + PJ]};                      // row n-1 holds the pinned 0
-        const df xm = gi > 0 ? df{PH[c - PJ], PL[c - PJ]} : pc;   // Neumann ghosts
-        const df yp = gj < L.m - 1 ? df{PH[c + 1], PL[c + 1]} : pc;
-        const df ym = gj > 0 ? df{PH[c - 1], PL[c - 1]} : pc;
-        const df res = df_residual(bpre[it][q], pc, xp, xm, yp, ym, ax, ay);
-        rr = res.hi + res.lo;
+      ok[q] = tj < TJ && gj < L.m;
+      k[q] = (long)gi * L.m + gj;
+      const int c = (ti + 1) * PJ + (ok[q] ? tj + 1 : 1);
+      pc[q] = df{PH[c], PL[c]};
+      xp[q] = df{PH[c + PJ], PL[c + PJ]};                        // row n-1 holds the pinned 0
+      xm[q] = gi > 0 ? df{PH[c - PJ], PL[c - PJ]} : pc[q];       // Neumann ghosts
+      yp[q] = gj < L.m - 1 ? df{PH[c + 1], PL[c + 1]} : pc[q];
+      ym[q] = gj > 0 ? df{PH[c - 1], PL[c - 1]} : pc[q];
+      if (ok[q]) {
+        pout[k[q]] = pc[q].hi;
+        pout[N + k[q]] = pc[q].lo;
       }
-      if (!profile) r_next[k] = rr;
-      acc = fmaf(rr, rr, acc);
+    }
+    float rr[2] = {0.f, 0.f};
+    if (gi != L.n - 1) {
+      auto pair = [](const df* v) {
+        return df2{make_float2(v[0].hi, v[1].hi), make_float2(v[0].lo, v[1].lo)};
+      };
+      const df2 res = df2_residual(make_float2(bpre[it][0], bpre[it][1]), pair(pc), pair(xp),
+                                   pair(xm), pair(yp), pair(ym), ax, ay);
+      const float2 s = add2(res.hi, res.lo);
+      rr[0] = s.x;
+      rr[1] = s.y;
+    }
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      if (!ok[q]) continue;
+      if (!profile) r_next[k[q]] = rr[q];
+      acc = fmaf(rr[q], rr[q], acc);
     }
   }
   if (profile) return;
@@ -1268,9 +1361,9 @@ static void level0_down_v(int v, const CvLvl& c, const Layout& L, void* ws, cons
 }
 static void level0_up_v(int v, const AjStepParams& p, const CvLvl& c, const Layout& L, void* ws,
                         DevScalars* sc, const CvCheck& ck, int profile, cudaStream_t st) {
-  if (v == 1) level0_up<T0b>(p, c, L, ws, sc, ck, profile, st);
-  else if (v == 2) level0_up<T0c>(p, c, L, ws, sc, ck, profile, st);
-  else level0_up<T0>(p, c, L, ws, sc, ck, profile, st);
+  if (v == 1) level0_up<T0bu>(p, c, L, ws, sc, ck, profile, st);
+  else if (v == 2) level0_up<T0cu>(p, c, L, ws, sc, ck, profile, st);
+  else level0_up<T0u>(p, c, L, ws, sc, ck, profile, st);
 }
 
 // one refinement iteration

@@ -1193,10 +1193,13 @@ def coarse_solve_separable(r, level, dx, dy, dtype=np.float64):
     return eh @ C
 
 
-def v_cycle_converge(r, dx, dy, depth, nu1=2, nu2=2, direct=0, coarse_dtype=np.float64):
+def v_cycle_converge(r, dx, dy, depth, nu1=2, nu2=2, direct=0, coarse_dtype=np.float64,
+                     nu2_fine=1):
     """One V(nu1,nu2) cycle for A e = r from e = 0; returns e (level 0).
-    With direct > 0 the cycle stops at that level with the separable exact
-    solve (in coarse_dtype); else it descends to the dense coarsest grid."""
+    The finest level post-smooths with nu2_fine sweeps (the GPU's k_cv_up0:
+    one red-black sweep, a V(2,1) cycle on the fine grid).  With direct > 0
+    the cycle stops at that level with the separable exact solve (in
+    coarse_dtype); else it descends to the dense coarsest grid."""
     def cyc(rl, level):
         if direct and level == direct:
             return coarse_solve_separable(rl, level, dx, dy, coarse_dtype)
@@ -1211,12 +1214,12 @@ def v_cycle_converge(r, dx, dy, depth, nu1=2, nu2=2, direct=0, coarse_dtype=np.f
         e = e + prolong_bilinear(ec, level + 1)
         if level == 0:
             e[-1, :] = 0.0
-        return rbgs(e, rl, level, dx, dy, nu2)
+        return rbgs(e, rl, level, dx, dy, nu2_fine if level == 0 else nu2)
     return cyc(r, 0)
 
 
 def mg_converge(b, dx, dy, rtol=1e-6, max_cycles=40, p0=None, nu1=2, nu2=2, max_coarse=64,
-                direct=True, coarse_dtype=np.float64):
+                direct=True, coarse_dtype=np.float64, nu2_fine=1):
     """Converging mode: iterative refinement around V-cycles.  Each outer
     iteration computes r = b - A p in float64, runs one V-cycle on A e = r and
     adds e.  Stops when ||r||/||b|| <= rtol.  Returns (p, info).  The V-cycle
@@ -1240,7 +1243,7 @@ def mg_converge(b, dx, dy, rtol=1e-6, max_cycles=40, p0=None, nu1=2, nu2=2, max_
         hist.append(float(rel))
         if rel <= rtol or cycles >= max_cycles:
             break
-        p = p + v_cycle_converge(r, dx, dy, depth, nu1, nu2, dlev, coarse_dtype)
+        p = p + v_cycle_converge(r, dx, dy, depth, nu1, nu2, dlev, coarse_dtype, nu2_fine)
         p[-1, :] = 0.0
         cycles += 1
     return p, {"cycles": cycles, "rel_residual": hist[-1], "history": hist, "depth": depth,
