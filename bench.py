@@ -47,7 +47,7 @@ UNIT = "Mcell-steps/s"
 FLUSH_BYTES = 256 << 20          # larger than the 126 MB L2
 NN_FACTOR = 8                    # network grid 256x64 at 2048x512
 # DRAM bytes of one k_cv_up0 launch at 2048x512 from an ncu capture
-TRAFFIC_UP0 = 22085888
+TRAFFIC_UP0 = 22079232
 
 
 def parse():
@@ -487,11 +487,13 @@ def step_bytes_per_cell(n_cycles, les=True):
 
 def roofline(args, plan, state, mask, flush, L):
     """Times the converging multigrid's level-0 post-smoothing kernel alone
-    (k_cv_up0: prolongation, 2 red-black sweeps, FP64 pressure update, FP64
-    residual for the next cycle).  Per cell it reads r (4 B), e (4 B), the
-    coarse correction (4 B / 4 cells), the FP64 pressure (8 B) and b (4 B), and
-    writes the new FP64 pressure (8 B) and the next residual (4 B): 33
-    algorithmic bytes per cell.  The L2 is flushed before every launch."""
+    (k_cv_up0: prolongation, 1 red-black sweep, double-FP32 pressure update
+    and residual for the next cycle).  Per cell it reads r (4 B), e (4 B),
+    the coarse correction (4 B / 4 cells), the double-FP32 pressure (8 B) and
+    b (4 B), and writes the new pressure (8 B) and the next residual (4 B): 33
+    algorithmic bytes per cell.  The L2 is flushed before every launch; the
+    duration is the mean of 40 launches (the event timer ticks in steps of
+    about 2 us on this part, so single launches are not resolved)."""
     import torch
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     peak, src = 6800.0, "fallback"
@@ -501,7 +503,7 @@ def roofline(args, plan, state, mask, flush, L):
     st = torch.cuda.current_stream()
     which, bpc = 1, 33
     times = []
-    for k in range(13):
+    for k in range(43):
         flush.zero_()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(st)
@@ -517,8 +519,8 @@ def roofline(args, plan, state, mask, flush, L):
     dur = statistics.mean(a.elapsed_time(b) for a, b in times) * 1e-3
     algo = bpc * args.nx * args.ny
     achieved = algo / dur / 1e9
-    return {"kernel": "k_cv_up0 (level 0: prolongation + 2 red-black sweeps + FP64 update "
-                      "and residual)",
+    return {"kernel": "k_cv_up0 (level 0: prolongation + 1 red-black sweep + double-FP32 "
+                      "update and residual)",
             "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_source": src, "traffic": TRAFFIC_UP0,
             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch "
