@@ -43,8 +43,6 @@
 namespace aj {
 
 constexpr int CV_NS = 2;                         // red-black sweeps per smoothing phase
-constexpr int CV_H = 2 * CV_NS + 1;              // tile halo: sweeps + one cell for the residual
-constexpr int CV_THREADS = 256;
 constexpr int CV_BLOCK_THREADS = 1024;
 constexpr int CV_BLOCK_MAX_CELLS = 16384;        // levels handled by the one-block kernel
 
@@ -294,13 +292,70 @@ __device__ __forceinline__ void cv_load_coarse(float* W, int gi0, int gj0,
   }
 }
 
-// tile + halo load: E = e_in + P(ec) (or 0), R = r; each row is read as two
-// coalesced runs of SJ/2 floats.  W (nullable when ZERO_E) holds the coarse
-// window after a cv_load_coarse and a barrier.
-template <class TC, bool ZERO_E>
-__device__ __forceinline__ void cv_load(float* E, float* R, const CvLvl& L, int gi0, int gj0,
-                                        const float* __restrict__ r, const float* __restrict__ e_in,
-                                        const float* W) {
+// tile + halo load for a pre-smoothing: E = 0, R = r; each row is read as
+// two coalesced runs of SJ/2 floats
+template <class TC>
+__device__ __forceinline__ void cv_load_r(float* E, float* R, const CvLvl& L, int gi0, int gj0,
+                                          const float* __restrict__ r) {
+  constexpr int SJ = TC::SJ;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+#pragma unroll
+  for (int ti = ty; ti < TC::SI; ti += TC::RG) {
+    const int gi = gi0 + ti;
+    const bool row_in = (unsigned)gi < (unsigned)L.n;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int tj = tx + q * TC::PAIRS;
+      const int gj = gj0 + tj;
+      const bool in = row_in && (unsigned)gj < (unsigned)L.m;
+      E[ti * SJ + tj] = 0.f;
+      R[ti * SJ + tj] = in ? ldg(r + (long)gi * L.m + gj) : 0.f;
+    }
+  }
+  __syncthreads();
+}
+
+// 4-byte asynchronous global-to-shared copy; zero-fill when !in (the source
+// is then not read)
+__device__ __forceinline__ void cv_cp4(float* dst, const float* src, bool in) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(src),
+               "r"(in ? 4 : 0));
+}
+
+// tile + halo of a post-smoothing, requested without waiting: R = r and
+// E = e_in by cp.async (zero outside the level, e also on level 0's pinned
+// outlet row), so that their round trip overlaps the coarse window's; the
+// caller commits, waits, synchronises and then adds the prolongation
+template <class TC>
+__device__ __forceinline__ void cv_stage_async(float* E, float* R, const CvLvl& L, int gi0,
+                                               int gj0, const float* __restrict__ r,
+                                               const float* __restrict__ e_in) {
+  constexpr int SJ = TC::SJ;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+#pragma unroll
+  for (int ti = ty; ti < TC::SI; ti += TC::RG) {
+    const int gi = gi0 + ti;
+    const bool row_in = (unsigned)gi < (unsigned)L.n;
+    const bool row_e = row_in && !(L.level == 0 && gi == L.n - 1);
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int tj = tx + q * TC::PAIRS;
+      const int gj = gj0 + tj;
+      const bool in = row_in && (unsigned)gj < (unsigned)L.m;
+      const long k = in ? (long)gi * L.m + gj : 0;
+      cv_cp4(R + ti * SJ + tj, r + k, in);
+      cv_cp4(E + ti * SJ + tj, e_in + k, in && row_e);
+    }
+  }
+}
+
+// e += P(e_coarse) on the cells this thread staged: the cell-centred
+// bilinear prolongation (weights 9/16, 3/16, 3/16, 1/16) from the coarse
+// window W (after cv_load_coarse, the copies' wait and a barrier)
+template <class TC>
+__device__ __forceinline__ void cv_add_prolong(float* E, const CvLvl& L, int gi0, int gj0,
+                                               const float* W) {
   constexpr int SJ = TC::SJ;
   using CW = CoarseWin<TC>;
   const int tx = threadIdx.x, ty = threadIdx.y;
@@ -308,31 +363,20 @@ __device__ __forceinline__ void cv_load(float* E, float* R, const CvLvl& L, int 
 #pragma unroll
   for (int ti = ty; ti < TC::SI; ti += TC::RG) {
     const int gi = gi0 + ti;
-    const bool row_in = (unsigned)gi < (unsigned)L.n;
-    const bool row_e = row_in && !ZERO_E && !(L.level == 0 && gi == L.n - 1);
+    if ((unsigned)gi >= (unsigned)L.n || (L.level == 0 && gi == L.n - 1)) continue;
     const int a = (gi >> 1) - I0, ai = (gi & 1) ? a + 1 : a - 1;
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
       const int tj = tx + q * TC::PAIRS;
       const int gj = gj0 + tj;
-      const bool in = row_in && (unsigned)gj < (unsigned)L.m;
-      float rr = 0.f, e = 0.f;
-      if (in) {
-        const long k = (long)gi * L.m + gj;
-        rr = ldg(r + k);
-        if (row_e) {
-          // cell-centred bilinear prolongation (weights 9/16, 3/16, 3/16, 1/16)
-          const int b = (gj >> 1) - J0, bj = (gj & 1) ? b + 1 : b - 1;
-          const float c0 = W[a * CW::C + b], cx = W[ai * CW::C + b];
-          const float cy = W[a * CW::C + bj], cxy = W[ai * CW::C + bj];
-          e = ldg(e_in + k) + (9.f * c0 + 3.f * cx + 3.f * cy + cxy) * (1.f / 16.f);
-        }
-      }
-      E[ti * SJ + tj] = e;
-      R[ti * SJ + tj] = rr;
+      if ((unsigned)gj >= (unsigned)L.m) continue;
+      const int b = (gj >> 1) - J0, bj = (gj & 1) ? b + 1 : b - 1;
+      const float c0 = W[a * CW::C + b], cx = W[ai * CW::C + b];
+      const float cy = W[a * CW::C + bj], cxy = W[ai * CW::C + bj];
+      float* e = E + ti * SJ + tj;
+      *e = *e + (9.f * c0 + 3.f * cx + 3.f * cy + cxy) * (1.f / 16.f);
     }
   }
-  __syncthreads();
 }
 
 // pre-smoothing from e = 0, residual, 2x2 average onto the coarse rhs.  On
@@ -351,7 +395,7 @@ __global__ void __launch_bounds__(TC::NTH) k_cv_down(CvLvl L, const float* r0, c
   const int gi0 = i0 - TC::H, gj0 = j0 - TC::H;
   const int tx = threadIdx.x, ty = threadIdx.y;
   const float* r = (r1 && *cur) ? r1 : r0;
-  cv_load<TC, true>(E, R, L, gi0, gj0, r, nullptr, nullptr);
+  cv_load_r<TC>(E, R, L, gi0, gj0, r);
   cv_sweeps<TC>(E, R, L, gi0, gj0);
   // store e and compute the residual on the tile interior (in place in R:
   // every residual of this thread first, then the stores, so that no store
@@ -413,10 +457,14 @@ __global__ void __launch_bounds__(TC::NTH) k_cv_up(CvLvl L, const float* __restr
   const int i0 = blockIdx.y * TI, j0 = blockIdx.x * TJ;
   const int gi0 = i0 - TC::H, gj0 = j0 - TC::H;
   const int tx = threadIdx.x, ty = threadIdx.y;
+  cv_stage_async<TC>(E, R, L, gi0, gj0, r, e_in);
+  asm volatile("cp.async.commit_group;\n" ::);
   __shared__ float W[CoarseWin<TC>::R * CoarseWin<TC>::C];
   cv_load_coarse<TC>(W, gi0, gj0, ec, nc, mc, gc);
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
   __syncthreads();
-  cv_load<TC, false>(E, R, L, gi0, gj0, r, e_in, W);
+  cv_add_prolong<TC>(E, L, gi0, gj0, W);
+  __syncthreads();
   cv_sweeps<TC>(E, R, L, gi0, gj0);
   for (int ti = TC::H + ty; ti < TC::H + TI; ti += TC::RG) {
     const int gi = gi0 + ti;
@@ -485,14 +533,6 @@ struct PState {
   float* b;   // buffer 1
 };
 
-// 4-byte asynchronous global-to-shared copy; zero-fill when !in (the source
-// is then not read)
-__device__ __forceinline__ void cv_cp4(float* dst, const float* src, bool in) {
-  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(src),
-               "r"(in ? 4 : 0));
-}
-
 // level 0: e + P(e_coarse), post-smoothing, p += e (double-FP32, ping-pong), the
 // residual of the reference operator for the next iteration (double-FP32), its
 // FP64 norm, and the convergence test in the last block to finish.  The
@@ -533,10 +573,13 @@ __global__ void __launch_bounds__(TC::NTH, 4) k_cv_up0(
   float* __restrict__ pout = cur ? ps.a : ps.b;
   const float* __restrict__ r = cur ? rs.b : rs.a;
   float* __restrict__ r_next = cur ? rs.a : rs.b;
-  // the pressure window (interior + 1) and b are requested first, so that
-  // their latency overlaps the prolongation and the sweeps: the window by
-  // cp.async straight into PH/PL, b into registers (this thread's residual
-  // cells: rows ty + RG q, columns tx and tx + PAIRS)
+  // Every global read is requested before the first wait, so that the block
+  // pays one round trip: the tile of r and e (tile and halo) and the pressure
+  // window (interior + 1) by cp.async straight into R, E, PH and PL, b into
+  // registers (this thread's residual cells: rows ty + RG q, columns tx and
+  // tx + PAIRS), the coarse window by plain loads; the prolongation is then
+  // added to E in shared memory.
+  cv_stage_async<TC>(E, R, L, gi0, gj0, r, e_in);
   for (int pi = ty; pi < PI; pi += TC::RG) {
     const int gi = i0 - 1 + pi;
     const bool row_in = (unsigned)gi < (unsigned)L.n && gi != L.n - 1;
@@ -565,11 +608,11 @@ __global__ void __launch_bounds__(TC::NTH, 4) k_cv_up0(
   }
   __shared__ float W[CoarseWin<TC>::R * CoarseWin<TC>::C];
   cv_load_coarse<TC>(W, gi0, gj0, ec, nc, mc, gc);
-  __syncthreads();
-  cv_load<TC, false>(E, R, L, gi0, gj0, r, e_in, W);
-  cv_sweeps<TC>(E, R, L, gi0, gj0);
   asm volatile("cp.async.wait_group 0;\n" ::: "memory");
   __syncthreads();
+  cv_add_prolong<TC>(E, L, gi0, gj0, W);
+  __syncthreads();
+  cv_sweeps<TC>(E, R, L, gi0, gj0);
   // new pressure on the interior and one cell around it, the thread's two
   // columns of a row as one pair (all of this thread's sums first, then the
   // stores)
