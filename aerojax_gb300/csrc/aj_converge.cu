@@ -100,16 +100,11 @@ __device__ __forceinline__ df df_residual(float b, df c, df xp, df xm, df yp, df
 
 // ---------------------------------------------------------------- paired double-FP32
 // Two double-FP32 values side by side (a thread's two columns of a tile row)
-// through the same error-free transformations on Blackwell's paired FP32
-// instructions: each lane of __fadd2_rn / __fmul2_rn / __ffma2_rn rounds as
-// the scalar operation does, and the explicit intrinsics are never contracted.
+// through the same error-free transformations on the paired FP32
+// instructions (f2, add2, sub2: aj_internal.cuh).
 struct df2 {
   float2 hi, lo;
 };
-__device__ __forceinline__ float2 f2(float x) { return make_float2(x, x); }
-__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
-// a - b as fma(b, -1, a): the exact difference, rounded once
-__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, f2(-1.f), a); }
 __device__ __forceinline__ df2 two_sum2(float2 a, float2 b) {
   const float2 s = add2(a, b);
   const float2 bb = sub2(s, a);

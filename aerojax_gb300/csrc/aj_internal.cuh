@@ -141,6 +141,18 @@ __device__ __forceinline__ void block_sum_atomic(double v, double* dst) {
   __syncthreads();
 }
 
+// ------------------------------------------------------------------ paired FP32
+// Blackwell's paired FP32 instructions: each lane of __fadd2_rn / __fmul2_rn /
+// __ffma2_rn rounds as the scalar operation does, and the explicit
+// intrinsics are never contracted, so two independent values computed side
+// by side cost one instruction per operation
+__device__ __forceinline__ float2 f2(float x) { return make_float2(x, x); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+// a - b as fma(b, -1, a): the exact difference, rounded once
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, f2(-1.f), a); }
+
 // ------------------------------------------------------------------ double-FP32
 // an unevaluated sum hi + lo of two floats (~48-bit significand on the FP32
 // pipes; GB300 runs FP64 at 1/64 of the FP32 rate)

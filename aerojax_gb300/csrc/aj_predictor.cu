@@ -1006,6 +1006,57 @@ __device__ __forceinline__ float stage_mac_v_int(const RkMac& a, int i, int j, f
   return finish_mac<1>(a, k, r, chi, dt, k1o);
 }
 
+// stage_mac_u_int and stage_mac_v_int (without hyperviscosity) for the two
+// faces of one interior cell as the lanes of paired FP32 instructions: lane
+// x the u-face (i, j), lane y the v-face (i, j).  "Along" is a face's own
+// direction (x for u, y for v, the upwinded difference), "across" the other
+// (the central difference); the cross velocity is v at the u-face and u at
+// the v-face.  Every lane evaluates its face's expressions in the same order
+// as the scalar functions (products added by fma where those contract).
+__device__ __forceinline__ float2 stage_mac_uv_int(const RkMac& a, int i, int j, float dt,
+                                                   float* k1u, float* k1v) {
+  const int ny = a.ny, nyv = ny + 1;
+  const long ku = (long)i * ny + j, kv = (long)i * nyv + j;
+  const float* u = a.uin + ku;
+  const float* v = a.vin + kv;
+  const float uw = ldg(u), uxm = ldg(u - ny), uxp = ldg(u + ny), uym = ldg(u - 1),
+              uyp = ldg(u + 1);
+  const float vw = ldg(v), vym = ldg(v - 1), vyp = ldg(v + 1), vxm = ldg(v - nyv),
+              vxp = ldg(v + nyv);
+  const float2 c = make_float2(uw, vw);
+  const float2 am = make_float2(uxm, vym), ap = make_float2(uxp, vyp);
+  const float2 cm = make_float2(uym, vxm), cp = make_float2(uyp, vxp);
+  const float2 half = f2(0.5f);
+  // 0.5 (0.5 (v[j+1] + v[j]) + 0.5 (v[i-1, j+1] + v[i-1, j])) and
+  // 0.5 (0.5 (u[i+1] + u[i]) + 0.5 (u[i+1, j-1] + u[i, j-1]))
+  const float2 q0 = make_float2(ldg(v + 1), uxp), q1 = make_float2(vw, uw);
+  const float2 q2 = make_float2(ldg(v - nyv + 1), ldg(u + ny - 1)), q3 = make_float2(vxm, uym);
+  const float2 cross = mul2(half, add2(mul2(half, add2(q0, q1)), mul2(half, add2(q2, q3))));
+  const float2 h_al = make_float2(a.idx, a.idy);
+  const float2 back = mul2(sub2(c, am), h_al), fwd = mul2(sub2(ap, c), h_al);
+  const float2 al = make_float2(upwind_weight(uw), upwind_weight(vw));
+  const float2 adv_al = mul2(c, fma2(al, back, mul2(sub2(f2(1.f), al), fwd)));
+  const float2 d_ac = mul2(sub2(cp, cm), make_float2(0.5f * a.idy, 0.5f * a.idx));
+  // the cell's mask and its neighbour across the face (i-1 for u, j-1 for v)
+  const float2 mc = f2(ldg(a.mask + ku));
+  const float2 mo = make_float2(ldg(a.mask + ku - ny), ldg(a.mask + ku - 1));
+  const float2 adv = mul2(fma2(cross, d_ac, adv_al), mul2(half, add2(mc, mo)));
+  // Laplacian: x terms are u's along and v's across sums, y terms the others
+  const float2 s_al = add2(ap, am), s_ac = add2(cp, cm);
+  const float2 two_c = mul2(f2(2.f), c);
+  const float2 lap = fma2(sub2(make_float2(s_al.x, s_ac.y), two_c), f2(a.idx2),
+                          mul2(sub2(make_float2(s_ac.x, s_al.y), two_c), f2(a.idy2)));
+  float2 nut = f2(a.nu);
+  if (a.nsg) {
+    const float2 no = make_float2(ldg(a.nsg + ku - ny), ldg(a.nsg + ku - 1));
+    nut = add2(nut, mul2(half, add2(f2(ldg(a.nsg + ku)), no)));
+  }
+  const float2 r = fma2(nut, lap, make_float2(-adv.x, -adv.y));
+  const float2 chi = mul2(half, add2(sub2(f2(1.f), mc), sub2(f2(1.f), mo)));
+  return make_float2(finish_mac<0>(a, ku, r.x, chi.x, dt, k1u),
+                     finish_mac<1>(a, kv, r.y, chi.y, dt, k1v));
+}
+
 template <bool HYPER, int ADV>
 __global__ void __launch_bounds__(256) k_rk_mac(RkMac a) {
   pdl_wait();
@@ -1066,9 +1117,18 @@ __global__ void __launch_bounds__(256) k_rk_mac(RkMac a) {
   if (fast && i >= 2 && i <= nx - 3 && j >= 2 && j <= ny - 3) {
     // both faces of the cell interior: one scope, so the loads they share
     // (u at (i,j), (i+1,j), (i,j-1); v at (i,j), (i,j+1), (i-1,j); mask and
-    // nu_sgs at (i,j)) are issued once
-    const float uo = stage_mac_u_int<HYPER>(a, i, j, dt, last ? nullptr : a.k1u_out);
-    const float vo = stage_mac_v_int<HYPER>(a, i, j, dt, last ? nullptr : a.k1v_out);
+    // nu_sgs at (i,j)) are issued once; without hyperviscosity the two faces
+    // share the paired FP32 instructions
+    float uo, vo;
+    if (HYPER) {
+      uo = stage_mac_u_int<HYPER>(a, i, j, dt, last ? nullptr : a.k1u_out);
+      vo = stage_mac_v_int<HYPER>(a, i, j, dt, last ? nullptr : a.k1v_out);
+    } else {
+      const float2 o = stage_mac_uv_int(a, i, j, dt, last ? nullptr : a.k1u_out,
+                                        last ? nullptr : a.k1v_out);
+      uo = o.x;
+      vo = o.y;
+    }
     a.uout[(long)i * ny + j] = uo;
     a.vout[(long)i * (ny + 1) + j] = vo;
     return;

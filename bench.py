@@ -47,7 +47,7 @@ UNIT = "Mcell-steps/s"
 FLUSH_BYTES = 256 << 20          # larger than the 126 MB L2
 NN_FACTOR = 8                    # network grid 256x64 at 2048x512
 # DRAM bytes of one k_cv_up0 launch at 2048x512 from an ncu capture
-TRAFFIC_UP0 = 22079232
+TRAFFIC_UP0 = 22080256
 
 
 def parse():
