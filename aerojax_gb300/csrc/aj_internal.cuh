@@ -262,7 +262,9 @@ __device__ __forceinline__ double block_sum(double v) {
 // still implies its predecessors'.  A no-op in a kernel launched normally.
 // (Early triggers, griddepcontrol.launch_dependents at the start of the
 // network's convolutions so that the next layer stages its weights sooner,
-// measured slower and are not used.)
+// or after the wait in the multigrid kernels, measured slower - the latter
+// by a quarter of the solve: the dependent's blocks sit resident beside the
+// running grid - and are not used.)
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
 // AEROJAX_PDL=0 turns dependent launches off (read once)
 bool pdl_enabled();
