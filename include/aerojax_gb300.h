@@ -51,9 +51,11 @@ enum { AJ_VARIANT_PURE = 0, AJ_VARIANT_GUI = 1 };
 enum { AJ_LES_NONE = 0, AJ_LES_SMAGORINSKY = 1, AJ_LES_DYNAMIC = 2 };
 enum { AJ_ADV_UPWIND = 0, AJ_ADV_WENO5 = 1 };
 /* PARITY   = the reference V-cycle, fixed v_cycles, absolute early exit;
-   CONVERGE = FP32 red-black Gauss-Seidel V-cycles inside double-FP32
-              iterative refinement, an exact separable coarse solve (or an FP64
-              dense one), FP64 norms, relative stop;
+   CONVERGE = FP32 red-black Gauss-Seidel V-cycles (2 pre- and 2
+              post-smoothing sweeps per level, 1 post-smoothing sweep on the
+              finest) inside double-FP32 iterative refinement, an exact
+              separable coarse solve (or an FP64 dense one), FP64 norms,
+              relative stop;
    NONE     = no pressure solve: a workspace for aj_prepare, aj_predictor and
               aj_les only, on any grid of at least 4x4 cells and any flow type
               (the reference's rk_step_unified and LES models take any shape);
