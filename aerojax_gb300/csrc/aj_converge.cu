@@ -169,11 +169,20 @@ static DfCoef df_coef(double ax, double ay) {
 // {2tx, 2tx+1} and walks the rows ty, ty+RG, ...; in a red-black half-sweep
 // exactly one cell of its pair per row has the colour being updated, so no
 // index needs a division.
-template <int SI_, int SJ_, int NTH_, int NS_ = CV_NS>
+// VEC tiles (k_cv_up0 on a level whose rows are a multiple of 4 floats) are
+// staged in 16-byte chunks: their shared rows start at the 16-byte column at
+// or left of the tile's first one and are SJS = SJ + 4 floats long (the
+// pressure window's PJS likewise), and the kernel indexes them through base
+// pointers shifted by the tile's offset from that column.
+template <int SI_, int SJ_, int NTH_, int NS_ = CV_NS, bool VEC_ = false>
 struct TileCfg {
   static constexpr int SI = SI_, SJ = SJ_, NTH = NTH_, NS = NS_, H = 2 * NS_ + 1;
+  static constexpr bool VEC = VEC_;
   static constexpr int TI = SI - 2 * H, TJ = SJ - 2 * H;
-  static constexpr int PAIRS = SJ / 2, RG = NTH / PAIRS, NT = SI * SJ;
+  static constexpr int SJS = VEC ? SJ + 4 : SJ;
+  static constexpr int PJS = VEC ? (TJ + 2 + 3 + 3) / 4 * 4 : TJ + 2;
+  static constexpr int PAIRS = SJ / 2, RG = NTH / PAIRS, NT = SI * SJS;
+  static_assert(!VEC || SJ % 4 == 0, "a 16-byte staged row is whole chunks");
   static_assert(TI % 2 == 0 && TJ % 2 == 0, "tile interiors must align with the coarse grid");
   static_assert(NTH % PAIRS == 0, "threads must fill whole rows of column pairs");
 };
@@ -187,6 +196,9 @@ constexpr int CV_NS_UP0 = 1;
 using T0u = TileCfg<48, 64, 256, CV_NS_UP0>;    // 42 x 58 interior
 using T0bu = TileCfg<32, 64, 256, CV_NS_UP0>;   // 26 x 58 interior
 using T0cu = TileCfg<64, 32, 256, CV_NS_UP0>;   // 58 x 26 interior
+using T0uv = TileCfg<48, 64, 256, CV_NS_UP0, true>;
+using T0buv = TileCfg<32, 64, 256, CV_NS_UP0, true>;
+using T0cuv = TileCfg<64, 32, 256, CV_NS_UP0, true>;
 constexpr int CV_TILE_VARIANTS = 3;
 
 __device__ __forceinline__ float cv_diag(const CvLvl& L, int gi, int gj) {
@@ -230,8 +242,8 @@ __device__ __forceinline__ void cv_sweeps_t(float* E, const float* R, const CvLv
       cc[q] = -1;
       val[q] = 0.f;
       if (upd) {
-        const int c = ti * SJ + tj;
-        const float nb = L.ax * (E[c + SJ] + E[c - SJ]) + L.ay * (E[c + 1] + E[c - 1]);
+        const int c = ti * TC::SJS + tj;
+        const float nb = L.ax * (E[c + TC::SJS] + E[c - TC::SJS]) + L.ay * (E[c + 1] + E[c - 1]);
         float inv = inv_int;
         if (!INTERIOR && (gi == 0 || gj == 0 || gi == L.n - 1 || gj == L.m - 1))
           inv = 1.f / cv_diag(L, gi, gj);
@@ -339,9 +351,36 @@ __device__ __forceinline__ void cv_stage_async(float* E, float* R, const CvLvl& 
       const int gj = gj0 + tj;
       const bool in = row_in && (unsigned)gj < (unsigned)L.m;
       const long k = in ? (long)gi * L.m + gj : 0;
-      cv_cp4(R + ti * SJ + tj, r + k, in);
-      cv_cp4(E + ti * SJ + tj, e_in + k, in && row_e);
+      cv_cp4(R + ti * TC::SJS + tj, r + k, in);
+      cv_cp4(E + ti * TC::SJS + tj, e_in + k, in && row_e);
     }
+  }
+}
+
+// 16-byte asynchronous copy, zero-filled when !in; both addresses 16-byte
+// aligned (the caller's VEC tiles guarantee it)
+__device__ __forceinline__ void cv_cp16(float* dst, const float* src, bool in) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src),
+               "r"(in ? 16 : 0));
+}
+
+// cv_stage_async of a VEC tile: rows of SJS floats from global column x0 (a
+// multiple of 4; the level's row length m is one too, so a chunk is wholly
+// inside or outside the level)
+template <class TC>
+__device__ __forceinline__ void cv_stage_async_v(float* E, float* R, const CvLvl& L, int gi0,
+                                                 int x0, const float* __restrict__ r,
+                                                 const float* __restrict__ e_in, int tid) {
+  constexpr int CH = TC::SJS / 4;
+  for (int t = tid; t < TC::SI * CH; t += TC::NTH) {
+    const int ti = t / CH, ch = t - ti * CH;
+    const int gi = gi0 + ti, gx = x0 + 4 * ch;
+    const bool in = (unsigned)gi < (unsigned)L.n && gx >= 0 && gx < L.m;
+    const bool ine = in && !(L.level == 0 && gi == L.n - 1);
+    const long k = in ? (long)gi * L.m + gx : 0;
+    cv_cp16(R + ti * TC::SJS + 4 * ch, r + k, in);
+    cv_cp16(E + ti * TC::SJS + 4 * ch, e_in + k, ine);
   }
 }
 
@@ -368,7 +407,7 @@ __device__ __forceinline__ void cv_add_prolong(float* E, const CvLvl& L, int gi0
       const int b = (gj >> 1) - J0, bj = (gj & 1) ? b + 1 : b - 1;
       const float c0 = W[a * CW::C + b], cx = W[ai * CW::C + b];
       const float cy = W[a * CW::C + bj], cxy = W[ai * CW::C + bj];
-      float* e = E + ti * SJ + tj;
+      float* e = E + ti * TC::SJS + tj;
       *e = *e + (9.f * c0 + 3.f * cx + 3.f * cy + cxy) * (1.f / 16.f);
     }
   }
@@ -383,6 +422,7 @@ __global__ void __launch_bounds__(TC::NTH) k_cv_down(CvLvl L, const float* r0, c
                                                      float* __restrict__ rc, const int* done) {
   pdl_wait();
   constexpr int SJ = TC::SJ, TI = TC::TI, TJ = TC::TJ;
+  static_assert(!TC::VEC, "the pre-smoothing indexes its tile with stride SJ");
   if (*done) return;
   __shared__ float E[TC::NT];
   __shared__ float R[TC::NT];
@@ -446,6 +486,7 @@ __global__ void __launch_bounds__(TC::NTH) k_cv_up(CvLvl L, const float* __restr
                                                    const int* done) {
   pdl_wait();
   constexpr int SJ = TC::SJ, TI = TC::TI, TJ = TC::TJ;
+  static_assert(!TC::VEC, "the level >= 1 post-smoothing indexes its tile with stride SJ");
   if (*done) return;
   __shared__ float E[TC::NT];
   __shared__ float R[TC::NT];
@@ -540,8 +581,8 @@ __global__ void __launch_bounds__(TC::NTH, 4) k_cv_up0(
     const float* __restrict__ ec, int nc, int mc, float gc, PState ps, const float* __restrict__ b,
     DevScalars* sc, DfCoef co, CvCheck ck, int profile) {
   pdl_wait();
-  constexpr int TI = TC::TI, TJ = TC::TJ, SJ = TC::SJ;
-  constexpr int PI = TI + 2, PJ = TJ + 2;
+  constexpr int TI = TC::TI, TJ = TC::TJ, SJS = TC::SJS;
+  constexpr int PI = TI + 2, PJ = TJ + 2, PJS = TC::PJS;
   static_assert(PJ <= 2 * TC::PAIRS, "the pressure window must fit two column runs");
   if (!profile && sc->mg_done) {
     // met before this body ran (the initial guess already satisfied the
@@ -553,13 +594,21 @@ __global__ void __launch_bounds__(TC::NTH, 4) k_cv_up0(
       cudaGraphSetConditional(ck.h, 0u);
     return;
   }
-  __shared__ float E[TC::NT];
-  __shared__ float R[TC::NT];
-  __shared__ float PH[PI * PJ];
-  __shared__ float PL[PI * PJ];
+  __shared__ __align__(16) float E[TC::NT];
+  __shared__ __align__(16) float R[TC::NT];
+  __shared__ __align__(16) float PH[PI * PJS];
+  __shared__ __align__(16) float PL[PI * PJS];
   __shared__ int am_last;
   const int i0 = blockIdx.y * TI, j0 = blockIdx.x * TJ;
   const int gi0 = i0 - TC::H, gj0 = j0 - TC::H;
+  // the tile's and the window's first logical cells (VEC: the shared rows
+  // start at the 16-byte column at or left of them)
+  const int xe = TC::VEC ? (gj0 & ~3) : gj0;
+  const int xw = TC::VEC ? ((j0 - 1) & ~3) : j0 - 1;
+  float* const Es = E + (gj0 - xe);
+  float* const Rs = R + (gj0 - xe);
+  float* const PHs = PH + (j0 - 1 - xw);
+  float* const PLs = PL + (j0 - 1 - xw);
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int tid = ty * TC::PAIRS + tx;
   const long N = (long)L.n * L.m;
@@ -574,19 +623,32 @@ __global__ void __launch_bounds__(TC::NTH, 4) k_cv_up0(
   // registers (this thread's residual cells: rows ty + RG q, columns tx and
   // tx + PAIRS), the coarse window by plain loads; the prolongation is then
   // added to E in shared memory.
-  cv_stage_async<TC>(E, R, L, gi0, gj0, r, e_in);
-  for (int pi = ty; pi < PI; pi += TC::RG) {
-    const int gi = i0 - 1 + pi;
-    const bool row_in = (unsigned)gi < (unsigned)L.n && gi != L.n - 1;
+  if constexpr (TC::VEC) {
+    cv_stage_async_v<TC>(E, R, L, gi0, xe, r, e_in, tid);
+    constexpr int PCH = PJS / 4;
+    for (int t = tid; t < PI * PCH; t += TC::NTH) {
+      const int pi = t / PCH, ch = t - pi * PCH;
+      const int gi = i0 - 1 + pi, gx = xw + 4 * ch;
+      const bool in = (unsigned)gi < (unsigned)L.n && gi != L.n - 1 && gx >= 0 && gx < L.m;
+      const long k = in ? (long)gi * L.m + gx : 0;
+      cv_cp16(PH + pi * PJS + 4 * ch, pin + k, in);
+      cv_cp16(PL + pi * PJS + 4 * ch, pin + N + k, in);
+    }
+  } else {
+    cv_stage_async<TC>(E, R, L, gi0, gj0, r, e_in);
+    for (int pi = ty; pi < PI; pi += TC::RG) {
+      const int gi = i0 - 1 + pi;
+      const bool row_in = (unsigned)gi < (unsigned)L.n && gi != L.n - 1;
 #pragma unroll
-    for (int q = 0; q < 2; ++q) {
-      const int pj = tx + q * TC::PAIRS;
-      if (pj >= PJ) continue;
-      const int gj = j0 - 1 + pj;
-      const bool in = row_in && (unsigned)gj < (unsigned)L.m;
-      const long k = in ? (long)gi * L.m + gj : 0;
-      cv_cp4(PH + pi * PJ + pj, pin + k, in);
-      cv_cp4(PL + pi * PJ + pj, pin + N + k, in);
+      for (int q = 0; q < 2; ++q) {
+        const int pj = tx + q * TC::PAIRS;
+        if (pj >= PJ) continue;
+        const int gj = j0 - 1 + pj;
+        const bool in = row_in && (unsigned)gj < (unsigned)L.m;
+        const long k = in ? (long)gi * L.m + gj : 0;
+        cv_cp4(PH + pi * PJS + pj, pin + k, in);
+        cv_cp4(PL + pi * PJS + pj, pin + N + k, in);
+      }
     }
   }
   asm volatile("cp.async.commit_group;\n" ::);
@@ -605,9 +667,9 @@ __global__ void __launch_bounds__(TC::NTH, 4) k_cv_up0(
   cv_load_coarse<TC>(W, gi0, gj0, ec, nc, mc, gc);
   asm volatile("cp.async.wait_group 0;\n" ::: "memory");
   __syncthreads();
-  cv_add_prolong<TC>(E, L, gi0, gj0, W);
+  cv_add_prolong<TC>(Es, L, gi0, gj0, W);
   __syncthreads();
-  cv_sweeps<TC>(E, R, L, gi0, gj0);
+  cv_sweeps<TC>(Es, Rs, L, gi0, gj0);
   // new pressure on the interior and one cell around it, the thread's two
   // columns of a row as one pair (all of this thread's sums first, then the
   // stores)
@@ -627,10 +689,10 @@ __global__ void __launch_bounds__(TC::NTH, 4) k_cv_up0(
       pt[it][q] = -1;
       h[q] = l[q] = e[q] = 0.f;
       if (row_in && pj < PJ && (unsigned)gj < (unsigned)L.m) {
-        const int t = pi * PJ + pj;
-        h[q] = PH[t];
-        l[q] = PL[t];
-        e[q] = E[(TC::H - 1 + pi) * SJ + (TC::H - 1 + pj)];
+        const int t = pi * PJS + pj;
+        h[q] = PHs[t];
+        l[q] = PLs[t];
+        e[q] = Es[(TC::H - 1 + pi) * SJS + (TC::H - 1 + pj)];
         pt[it][q] = t;
       }
     }
@@ -640,12 +702,12 @@ __global__ void __launch_bounds__(TC::NTH, 4) k_cv_up0(
 #pragma unroll
   for (int it = 0; it < PR; ++it) {
     if (pt[it][0] >= 0) {
-      PH[pt[it][0]] = pv[it].hi.x;
-      PL[pt[it][0]] = pv[it].lo.x;
+      PHs[pt[it][0]] = pv[it].hi.x;
+      PLs[pt[it][0]] = pv[it].lo.x;
     }
     if (pt[it][1] >= 0) {
-      PH[pt[it][1]] = pv[it].hi.y;
-      PL[pt[it][1]] = pv[it].lo.y;
+      PHs[pt[it][1]] = pv[it].hi.y;
+      PLs[pt[it][1]] = pv[it].lo.y;
     }
   }
   __syncthreads();
@@ -667,12 +729,12 @@ __global__ void __launch_bounds__(TC::NTH, 4) k_cv_up0(
       const int gj = j0 + tj;
       ok[q] = tj < TJ && gj < L.m;
       k[q] = (long)gi * L.m + gj;
-      const int c = (ti + 1) * PJ + (ok[q] ? tj + 1 : 1);
-      pc[q] = df{PH[c], PL[c]};
-      xp[q] = df{PH[c + PJ], PL[c + PJ]};                        // row n-1 holds the pinned 0
-      xm[q] = gi > 0 ? df{PH[c - PJ], PL[c - PJ]} : pc[q];       // Neumann ghosts
-      yp[q] = gj < L.m - 1 ? df{PH[c + 1], PL[c + 1]} : pc[q];
-      ym[q] = gj > 0 ? df{PH[c - 1], PL[c - 1]} : pc[q];
+      const int c = (ti + 1) * PJS + (ok[q] ? tj + 1 : 1);
+      pc[q] = df{PHs[c], PLs[c]};
+      xp[q] = df{PHs[c + PJS], PLs[c + PJS]};                    // row n-1 holds the pinned 0
+      xm[q] = gi > 0 ? df{PHs[c - PJS], PLs[c - PJS]} : pc[q];   // Neumann ghosts
+      yp[q] = gj < L.m - 1 ? df{PHs[c + 1], PLs[c + 1]} : pc[q];
+      ym[q] = gj > 0 ? df{PHs[c - 1], PLs[c - 1]} : pc[q];
       if (ok[q]) {
         pout[k[q]] = pc[q].hi;
         pout[N + k[q]] = pc[q].lo;
@@ -1397,11 +1459,20 @@ static void level0_down_v(int v, const CvLvl& c, const Layout& L, void* ws, cons
   else if (v == 2) level0_down<T0c>(c, L, ws, done, st);
   else level0_down<T0>(c, L, ws, done, st);
 }
+// the 16-byte staged tiles need rows of a multiple of 4 floats and every
+// staged buffer 16-byte aligned (workspace offsets are multiples of 256)
+static bool level0_vec_ok(const CvLvl& c, const void* ws) {
+  return c.m % 4 == 0 && (reinterpret_cast<uintptr_t>(ws) & 15) == 0;
+}
 static void level0_up_v(int v, const AjStepParams& p, const CvLvl& c, const Layout& L, void* ws,
                         DevScalars* sc, const CvCheck& ck, int profile, cudaStream_t st) {
-  if (v == 1) level0_up<T0bu>(p, c, L, ws, sc, ck, profile, st);
-  else if (v == 2) level0_up<T0cu>(p, c, L, ws, sc, ck, profile, st);
-  else level0_up<T0u>(p, c, L, ws, sc, ck, profile, st);
+  const bool vec = level0_vec_ok(c, ws);
+  if (v == 1) vec ? level0_up<T0buv>(p, c, L, ws, sc, ck, profile, st)
+                  : level0_up<T0bu>(p, c, L, ws, sc, ck, profile, st);
+  else if (v == 2) vec ? level0_up<T0cuv>(p, c, L, ws, sc, ck, profile, st)
+                       : level0_up<T0cu>(p, c, L, ws, sc, ck, profile, st);
+  else vec ? level0_up<T0uv>(p, c, L, ws, sc, ck, profile, st)
+           : level0_up<T0u>(p, c, L, ws, sc, ck, profile, st);
 }
 
 // one refinement iteration
