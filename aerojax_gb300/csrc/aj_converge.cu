@@ -172,8 +172,9 @@ static DfCoef df_coef(double ax, double ay) {
 // VEC tiles (k_cv_up0 on a level whose rows are a multiple of 4 floats) are
 // staged in 16-byte chunks: their shared rows start at the 16-byte column at
 // or left of the tile's first one and are SJS = SJ + 4 floats long (the
-// pressure window's PJS likewise), and the kernel indexes them through base
-// pointers shifted by the tile's offset from that column.
+// pressure window's rows, PJS, cover its TJ + 2 columns from the 16-byte
+// column at or left of its first, in whole chunks), and the kernel indexes
+// them through base pointers shifted by the offsets from those columns.
 template <int SI_, int SJ_, int NTH_, int NS_ = CV_NS, bool VEC_ = false>
 struct TileCfg {
   static constexpr int SI = SI_, SJ = SJ_, NTH = NTH_, NS = NS_, H = 2 * NS_ + 1;
