@@ -339,7 +339,6 @@ template <class TC>
 __device__ __forceinline__ void cv_stage_async(float* E, float* R, const CvLvl& L, int gi0,
                                                int gj0, const float* __restrict__ r,
                                                const float* __restrict__ e_in) {
-  constexpr int SJ = TC::SJ;
   const int tx = threadIdx.x, ty = threadIdx.y;
 #pragma unroll
   for (int ti = ty; ti < TC::SI; ti += TC::RG) {
@@ -391,7 +390,6 @@ __device__ __forceinline__ void cv_stage_async_v(float* E, float* R, const CvLvl
 template <class TC>
 __device__ __forceinline__ void cv_add_prolong(float* E, const CvLvl& L, int gi0, int gj0,
                                                const float* W) {
-  constexpr int SJ = TC::SJ;
   using CW = CoarseWin<TC>;
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int I0 = (gi0 >> 1) - 1, J0 = (gj0 >> 1) - 1;
